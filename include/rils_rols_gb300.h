@@ -1,0 +1,184 @@
+/*
+ * rils_rols_gb300 - C ABI of the GB300 fitness path of RILS-ROLS.
+ *
+ * The reference evaluates one candidate at a time through two private member
+ * functions of its search class:
+ *     tune_constants(tree, X, y) -> tree      rils_rols_cpp/rils_rols_cpp.cpp:445-518
+ *     fitness(tree, X, y) -> (1-R2, RMSE, size) rils_rols_cpp/rils_rols_cpp.cpp:520-541
+ * both driving the recursive evaluator node::evaluate_all (rils_rols_cpp/node.cpp:5-95)
+ * and Eigen's column-pivoted QR (rils_rols_cpp/rils_rols_cpp.cpp:484).
+ * This ABI replaces that pair with a batched call: the host flattens every
+ * candidate of one local-search round into postfix programs (one program per
+ * top-level factor, see rrg_op below) and submits them together; the device
+ * evaluates the factors, refits the linear coefficients and returns the
+ * fitness tuple of the rebuilt tree for every candidate.
+ *
+ * Plain pointers and sizes only; every call returns an rrg_status.  No call
+ * exits the process (the reference calls exit(1) on bad input,
+ * rils_rols_cpp.cpp:722-725).
+ */
+#ifndef RILS_ROLS_GB300_H
+#define RILS_ROLS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RRG_ABI_VERSION 1
+#define RRG_MAX_TERMS 64   /* factors + free term of one tuned candidate */
+#define RRG_MAX_STACK 16   /* spill-stack depth of one factor program */
+
+typedef enum {
+  RRG_OK = 0,
+  RRG_E_INVALID = 1,      /* bad argument or malformed batch */
+  RRG_E_CUDA = 2,         /* CUDA runtime error (message via rrg_last_error) */
+  RRG_E_NO_DEVICE = 3,    /* no usable GB300 device / extension not loaded */
+  RRG_E_TIMEOUT = 4,      /* bounded wait ran out; the context stays usable */
+  RRG_E_TOO_LARGE = 5,    /* a candidate exceeds RRG_MAX_TERMS or RRG_MAX_STACK */
+  RRG_E_OOM = 6,          /* device memory budget exceeded */
+  RRG_E_DEVICE_FAULT = 7  /* a kernel reported an error status (bounded wait, bad code) */
+} rrg_status;
+
+/* Arithmetic of one round. */
+typedef enum {
+  RRG_PLAIN_FP64 = 0,  /* FP64 evaluation, column-pivoted Householder OLS, FP64 residual */
+  RRG_MIXED = 1        /* FP32 evaluation, compensated Gram, FP64 Cholesky + refinement, FP64 SSE */
+} rrg_precision;
+
+/* How one candidate is scored. */
+typedef enum {
+  RRG_UNTUNED = 0,  /* fitness(tree): yp = factor 0 (the whole tree), rils_rols_cpp.cpp:520-541 */
+  RRG_TUNED = 1     /* fitness(tune_constants(tree)): OLS over [factors..., 1] then the rebuilt sum */
+} rrg_mode;
+
+/* Result flag bits. */
+#define RRG_F_NONFINITE      0x1u   /* R2 or RMSE was NaN: the (1000,1000,1000) sentinel was returned */
+#define RRG_F_RANK_DEFICIENT 0x2u   /* numerical rank < number of columns */
+#define RRG_F_QR_FALLBACK    0x4u   /* mixed round: ill-conditioned Gram, re-solved by the FP64 QR path */
+#define RRG_F_VERIFIED_FP64  0x8u   /* mixed round: re-scored by the FP64 path (argbest verification) */
+#define RRG_F_TOO_LARGE      0x10u  /* candidate rejected: RRG_MAX_TERMS / RRG_MAX_STACK exceeded */
+
+/*
+ * Postfix code.  One 32-bit word per instruction: low 8 bits opcode, high 24
+ * bits argument (feature index, constant-pool index or factor slot).
+ * The evaluator keeps the top of stack (TOS) in registers and spills older
+ * values to a per-thread stack.  Binary operators take their second operand
+ * from the spill stack (S), a feature column (V) or the constant pool (C);
+ * the direction bit says whether TOS is the right (N) or the left (R) operand:
+ *     N: TOS = op(other, TOS)      R: TOS = op(TOS, other)
+ * Element-wise semantics are those of node::evaluate_inner (node.cpp:23-95).
+ */
+enum rrg_op {
+  RRG_OP_LDV = 1,   /* TOS = X[arg] */
+  RRG_OP_LDC = 2,   /* TOS = K[arg] */
+  RRG_OP_PSV = 3,   /* spill TOS; TOS = X[arg] */
+  RRG_OP_PSC = 4,   /* spill TOS; TOS = K[arg] */
+  RRG_OP_SIN = 5, RRG_OP_COS = 6, RRG_OP_LN = 7, RRG_OP_EXP = 8, RRG_OP_SQRT = 9, RRG_OP_SQR = 10,
+  RRG_OP_EMIT = 11, /* factor slot arg = TOS; the stack is empty afterwards */
+  RRG_OP_BIN = 16   /* binary: RRG_OP_BIN + 8*base + 2*src + dir */
+};
+enum rrg_bin_base { RRG_ADD = 0, RRG_SUB, RRG_MUL, RRG_DIV, RRG_POW, RRG_LT, RRG_EQ, RRG_NE, RRG_MIN, RRG_MAX, RRG_N_BASE };
+enum rrg_bin_src { RRG_SRC_S = 0, RRG_SRC_V = 1, RRG_SRC_C = 2 };
+enum rrg_bin_dir { RRG_DIR_N = 0, RRG_DIR_R = 1 };
+#define RRG_BIN_OP(base, src, dir) (RRG_OP_BIN + 8 * (base) + 2 * (src) + (dir))
+#define RRG_INSN(op, arg) ((uint32_t)(op) | ((uint32_t)(arg) << 8))
+
+typedef struct {
+  int32_t code_offset;  /* first instruction of the candidate (all its factors, in order) */
+  int32_t code_len;     /* instructions of all its factors; each factor ends with EMIT */
+  int32_t first_factor; /* index of its first rrg_factor */
+  int32_t n_factors;    /* non-constant factors (tuned) or 1 (untuned) */
+  int32_t mode;         /* rrg_mode */
+  int32_t coef_offset;  /* tuned: n_factors + 1 coefficients written at coefs[coef_offset] */
+  int32_t stack_need;   /* deepest spill of its programs (<= RRG_MAX_STACK) */
+  int32_t reserved;
+} rrg_cand;
+
+typedef struct {
+  int32_t n_nodes;      /* node count of the factor subtree (node.h:311-322) */
+  int32_t reserved;
+} rrg_factor;
+
+typedef struct {
+  int32_t n_cand;
+  int32_t n_factors;
+  int32_t n_code;
+  int32_t n_consts;
+  const rrg_cand* cands;
+  const rrg_factor* factors;
+  const uint32_t* code;
+  const double* consts;
+} rrg_batch;
+
+typedef struct {
+  double loss;      /* 1 - R2 (also the classifier loss, rils_rols_cpp.cpp:526-531); 1000 on NaN */
+  double rmse;      /* sqrt(mean((y - yp)^2)); 1000 on NaN */
+  int32_t size;     /* node count of the rebuilt tree (tuned) or of the tree (untuned); 1000 on NaN */
+  int32_t rank;     /* tuned: nonzero pivots of the OLS design; untuned: 0 */
+  uint32_t flags;   /* RRG_F_* */
+  int32_t n_coef;   /* tuned: n_factors + 1 (free term last); untuned: 0 */
+} rrg_result;
+
+typedef struct rrg_context rrg_context;
+typedef struct rrg_dataset rrg_dataset;
+
+/* Version of this ABI (RRG_ABI_VERSION). */
+int32_t rrg_abi_version(void);
+
+/* Text of the last error on this thread (never NULL). */
+const char* rrg_last_error(void);
+
+/* One context per device: owns a stream, pinned staging and scratch arenas. */
+rrg_status rrg_context_create(int32_t device, rrg_context** out);
+rrg_status rrg_context_destroy(rrg_context* ctx);
+
+/*
+ * Make a dataset resident on the device.  X_col is d columns of n FP64 values
+ * (column-major, the layout get_x builds, rils_rols_cpp.cpp:675-698); y has n
+ * values.  Both are copied; the caller keeps ownership.  The device keeps FP64
+ * and FP32 copies.  Replaces the `const vector<ArrayXd>& X, const ArrayXd& y`
+ * arguments of tune_constants / fitness (rils_rols_cpp.cpp:445, 520).
+ */
+rrg_status rrg_dataset_create(rrg_context* ctx, const double* X_col, const double* y, int64_t n, int32_t d,
+                              rrg_dataset** out);
+rrg_status rrg_dataset_destroy(rrg_dataset* ds);
+
+/*
+ * Score a batch of candidates (one local-search round).  Asynchronous: the
+ * batch is copied into pinned staging before the call returns, so the caller
+ * may reuse its buffers at once; `results` (n_cand entries) and `coefs` (the
+ * sum of n_coef over tuned candidates, may be NULL) are written when
+ * rrg_round_wait returns RRG_OK.  One round in flight per context.
+ * Replaces, per candidate j: tune_constants (rils_rols_cpp.cpp:615) followed
+ * by fitness (:616), or fitness alone (:828, :842) for RRG_UNTUNED.
+ */
+rrg_status rrg_round_submit(rrg_dataset* ds, const rrg_batch* batch, int32_t precision, rrg_result* results,
+                            double* coefs);
+/* Bounded wait for the round in flight; RRG_E_TIMEOUT leaves it in flight. */
+rrg_status rrg_round_wait(rrg_context* ctx, int32_t timeout_ms);
+
+/* submit + wait (no timeout). */
+rrg_status rrg_eval(rrg_dataset* ds, const rrg_batch* batch, int32_t precision, rrg_result* results,
+                    double* coefs);
+
+/*
+ * Values of candidate 0 of `batch` (RRG_UNTUNED, one factor) on every row of
+ * the dataset, FP64, written to values[n].  Replaces
+ * final_solution->evaluate_all(X) in predict (rils_rols_cpp.cpp:738).
+ */
+rrg_status rrg_predict(rrg_dataset* ds, const rrg_batch* batch, double* values);
+
+/* Rows and columns of a dataset. */
+int64_t rrg_dataset_rows(const rrg_dataset* ds);
+int32_t rrg_dataset_cols(const rrg_dataset* ds);
+
+/* Kernels launched by the last completed round on this context (for audits). */
+int64_t rrg_last_round_launches(const rrg_context* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
