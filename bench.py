@@ -1,0 +1,376 @@
+"""Benchmark of the RILS-ROLS fitness path on GB300.
+
+Metric: candidate fitness evaluations per second (tune_constants + fitness of
+rils_rols_cpp.cpp:445-541 per candidate) at n = 1M rows.
+
+Workload (one step): one batched round of the mixed-precision path over
+B = 8192 candidate trees drawn like the standalone batched-fitness
+configuration (sizes uniform 3..50 nodes over + - * / sin cos ln exp sqrt,
+leaves x_j or U(-5, 5) constants), scored on the 1M-row, 5-feature regression
+dataset (X ~ U(-3, 3), y = 2.5 x1 x2 - sin(x3)/(1+x4^2) + 0.7 exp(0.3 x5) +
+0.5% noise).  Synthetic, seeded data; nothing is downloaded.
+
+  value  device-resident: dataset in HBM, each step = one rrg_eval round
+         (batch upload, kernels, result download), timed with CUDA events on
+         the library's stream, L2 flushed (256 MB write) before every step;
+  e2e    through the C ABI from host buffers: per step the trees are
+         flattened, X and y are uploaded from pinned host memory
+         (rrg_dataset_create), the round runs and the results come back.
+
+Reported beside it: the plain FP64 path's unbatched launch (one candidate per
+round), the mixed-vs-FP64 fitness error of every candidate, the roofline of
+the dominant kernel, the CPU oracle timed on the host cores, clocks.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT / "rils-rols_gb300"))
+sys.path.insert(0, str(ROOT))
+
+METRIC = "candidate fitness evals/s at n=1M (mixed precision, batched round)"
+UNIT = "evals/s"
+N_ROWS = 1_000_000
+N_FEAT = 5
+BATCH = 8192
+SEED = 12345
+
+
+def workload(n=N_ROWS, batch=BATCH, seed=SEED):
+    from rils_rols_gb300 import synth
+    X, y = synth.regression_1m(n=n, seed=seed)
+    rng = np.random.default_rng(seed + 1)
+    trees = [synth.random_tree(rng, int(rng.integers(3, 51)), N_FEAT) for _ in range(batch)]
+    return X, y, trees
+
+
+def config(n, batch):
+    return {"workload": f"batched tuned fitness: {batch} random trees (3-50 nodes) x n={n} rows, d={N_FEAT}",
+            "n_rows": n, "n_features": N_FEAT, "batch": batch, "tree_sizes": "U{3..50}",
+            "operators": "+ - * / sin cos ln exp sqrt", "precision": "FP32 eval, FP64 solve / SSE",
+            "l2": "flushed (256 MB write on the round's stream) before every timed step"}
+
+
+# ------------------------------------------------------------------ clocks --
+class ClockSampler:
+    """nvidia-smi samples (200 ms) while the timed region runs."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.path or not os.path.exists(self.path):
+            return None
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------ CPU baseline --
+def cpu_baseline(X, y, trees, sample, threads=None):
+    """The oracle (CPU restatement of the reference's path, FP64) on `sample`
+    candidates with all host threads."""
+    from oracle import pyoracle
+    from rils_rols_gb300.fitness import encode
+    threads = threads or os.cpu_count() or 1
+    ods = pyoracle.OracleDataset(X, y)
+    b = encode(trees[:sample], tuned=True)
+    t = time.perf_counter()
+    ods.evaluate(b, threads=threads)
+    dt = time.perf_counter() - t
+    return {"value": sample / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{sample} of the {len(trees)} candidates at n={len(y)} (oracle/rrg_oracle.c, FP64, "
+                      f"{threads} threads, {dt:.1f} s)"}
+
+
+# ----------------------------------------------------------- multi-rank --
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        backend = os.environ.get("BENCH_DIST_BACKEND", "nccl")
+        if backend == "nccl":
+            import torch
+            torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        dist.init_process_group(backend=backend)
+    return rank, world
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x: float, world: int) -> float:
+    """Largest value of x over all ranks (the job's time is its slowest rank)."""
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def aggregate(units_per_rank: float, seconds: float, world: int) -> tuple[float, float]:
+    """Whole-job throughput: all ranks' units over the slowest rank's time."""
+    t = max_over_ranks(seconds, world)
+    return units_per_rank * world / t, t
+
+
+# ------------------------------------------------------------------- ours --
+def run_ours(args):
+    import torch
+
+    from rils_rols_gb300.fitness import MIXED, PLAIN, Context, encode
+
+    rank, world = dist_setup()
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    X, y, trees = workload(args.n, args.batch)
+    ctx = Context(local)
+    ds = ctx.dataset(X, y)
+    batch = encode(trees, tuned=True)
+    stream = torch.cuda.ExternalStream(ctx.stream(), device=torch.device("cuda", local))
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=torch.device("cuda", local))
+
+    # warm-up (also checks the path end to end)
+    for _ in range(args.warmup):
+        ds.evaluate(batch, MIXED)
+    ctx.set_timing(True)
+    phase_ms, phase_n = {}, {}
+    times = []
+    launches = 0
+    barrier(world)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+            out = ds.evaluate(batch, MIXED)
+            with torch.cuda.stream(stream):
+                e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1) / 1e3)
+            launches += ctx.last_round_launches()
+            for k, (ms, cnt) in ctx.last_round_timing().items():
+                phase_ms[k] = phase_ms.get(k, 0.0) + ms
+                phase_n[k] = phase_n.get(k, 0) + cnt
+    torch.cuda.synchronize()
+    barrier(world)
+    stats = ctx.last_round_stats()
+    ctx.set_timing(False)
+    value, t_max = aggregate(args.batch * args.steps, sum(times), world)
+
+    # e2e: trees in, fitness out, through the C ABI from host buffers
+    Xp = torch.from_numpy(np.ascontiguousarray(X)).pin_memory().numpy()
+    yp = torch.from_numpy(np.ascontiguousarray(y)).pin_memory().numpy()
+    e2e_times = []
+    for step in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        b = encode(trees, tuned=True)
+        d2 = ctx.dataset(Xp, yp)
+        r = d2.evaluate(b, MIXED)
+        d2.close()
+        torch.cuda.synchronize()
+        if step >= args.warmup:
+            e2e_times.append(time.perf_counter() - t)
+    e2e_value, _ = aggregate(args.batch * args.steps, sum(e2e_times), world)
+    h2d = X.nbytes + y.nbytes + batch.cands.nbytes + batch.factors.nbytes + batch.code.nbytes + batch.consts.nbytes
+    d2h = args.batch * 32 + batch.n_coefs * 8
+
+    if rank != 0:
+        return
+    res = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32/f64", "data": "synthetic (seeded)",
+           "config": config(args.n, args.batch),
+           "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+           "gpu_launches": int(launches), "round_stats": stats}
+    # dominant kernel: the mixed gram pass
+    gram_ms, gram_n = phase_ms.get("mixed_gram", 0.0), max(1, phase_n.get("mixed_gram", 1))
+    avg_launch_s = gram_ms / 1e3 / gram_n
+    algo_bytes = args.n * (N_FEAT + 1) * 4  # X (FP32) and y read once per launch
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    peak = peaks.get("hbm_gbs", 6800.0)
+    achieved = algo_bytes / avg_launch_s / 1e9 if avg_launch_s > 0 else 0.0
+    res["roofline"] = {"kernel": "mixed_pass_kernel (gram pass)", "bound": "hbm", "achieved": achieved,
+                       "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                       "traffic": read_profile_traffic(), "peak_source": "measured" if peaks else "fallback",
+                       "note": "issue-bound interpreter: the HBM roofline is far away; see DESIGN.md"}
+    res["phase_ms_per_step"] = {k: v / args.steps for k, v in phase_ms.items() if v > 0}
+    res["clocks"] = clk.summary()
+    if not args.quick:
+        res.update(compare_paths(ctx, ds, X, y, trees, batch, out, args))
+        res["mixed_over_plain_unbatched"] = value / world / res["plain_fp64_unbatched_evals_per_s"]
+        res["cpu_baseline"] = cpu_baseline(X, y, trees, args.cpu_sample)
+        res["mixed_over_cpu_baseline"] = value / world / res["cpu_baseline"]["value"]
+    print(json.dumps(res))
+
+
+def compare_paths(ctx, ds, X, y, trees, batch, mixed_out, args):
+    """Plain FP64 path: unbatched launches (one candidate per round) and the
+    whole batch (accuracy reference for the mixed round)."""
+    import torch
+
+    from rils_rols_gb300.fitness import PLAIN, encode
+    singles = [encode([t], tuned=True) for t in trees[:args.unbatched_sample]]
+    ds.evaluate(singles[0], PLAIN)
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    for s in singles:
+        ds.evaluate(s, PLAIN)
+    torch.cuda.synchronize()
+    unbatched = len(singles) / (time.perf_counter() - t)
+    t = time.perf_counter()
+    plain = ds.evaluate(batch, PLAIN)
+    plain_batched = len(trees) / (time.perf_counter() - t)
+    fv = lambda r: (1 + r["loss"]) * (1 + r["rmse"]) * (1 + r["size"] * 1e-3)  # noqa: E731
+    ok = (plain["loss"] != 1000) & np.isfinite(fv(plain))
+    err = np.abs(fv(mixed_out)[ok] - fv(plain)[ok]) / fv(plain)[ok]
+    best_m = int(np.argmin(np.where(ok, fv(mixed_out), np.inf)))
+    best_p = int(np.argmin(np.where(ok, fv(plain), np.inf)))
+    order_m = np.argsort(np.where(ok, fv(mixed_out), np.inf))[:100]
+    order_p = np.argsort(np.where(ok, fv(plain), np.inf))[:100]
+    return {
+        "plain_fp64_unbatched_evals_per_s": unbatched,
+        "plain_fp64_batched_evals_per_s": plain_batched,
+        "mixed_over_plain_unbatched": None,  # filled by the caller from `value`
+        "accuracy_vs_fp64": {
+            "candidates_compared": int(ok.sum()),
+            "sentinel_agreement": float(np.mean((mixed_out["loss"] == 1000) == (plain["loss"] == 1000))),
+            "fitness_rel_err_median": float(np.median(err)), "fitness_rel_err_p99": float(np.quantile(err, 0.99)),
+            "fitness_rel_err_max": float(err.max()), "frac_within_1e-6": float(np.mean(err <= 1e-6)),
+            "argbest_same": best_m == best_p, "top100_overlap": len(set(order_m) & set(order_p)) / 100.0,
+            "fitness": "(1 + (1 - R2)) (1 + RMSE) (1 + 0.001 size)"},
+    }
+
+
+def read_profile_traffic():
+    """DRAM bytes per launch of the gram pass from the committed ncu summary."""
+    p = ROOT / "profiles" / "mixed_gram_pass.txt"
+    if not p.exists():
+        return None
+    for line in p.read_text().splitlines():
+        if line.startswith("traffic_bytes_per_launch_full_size"):
+            try:
+                return float(line.split("=")[1].split()[0])
+            except (IndexError, ValueError):
+                return None
+    return None
+
+
+# -------------------------------------------------------------- reference --
+def run_reference(args):
+    """The reference's CPU path for this workload: the oracle restatement
+    (oracle/rrg_oracle.c; the reference harness only builds where the
+    reference checkout exists), all host threads, a bounded sample per step."""
+    rank, world = dist_setup()
+    if rank != 0:
+        return
+    from oracle import pyoracle
+    from rils_rols_gb300.fitness import encode
+    X, y, trees = workload(args.n, args.batch)
+    threads = os.cpu_count() or 1
+    ods = pyoracle.OracleDataset(X, y)
+    sample = args.ref_sample
+    rng = np.random.default_rng(7)
+    times = []
+    for step in range(args.warmup + args.steps):
+        idx = rng.choice(len(trees), sample, replace=False)
+        b = encode([trees[i] for i in idx], tuned=True)
+        t = time.perf_counter()
+        ods.evaluate(b, threads=threads)
+        dt = time.perf_counter() - t
+        if step >= args.warmup:
+            times.append(dt)
+    value = sample * len(times) / sum(times)
+    desc = f"{sample} random candidates of the batch per step at n={args.n}, FP64, {threads} threads"
+    print(json.dumps({"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+                      "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
+                      "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                      "data": "synthetic (seeded)", "config": config(args.n, args.batch),
+                      "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                                       "sample": desc},
+                      "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=N_ROWS)
+    ap.add_argument("--batch", type=int, default=BATCH)
+    ap.add_argument("--cpu-sample", type=int, default=96)
+    ap.add_argument("--ref-sample", type=int, default=32)
+    ap.add_argument("--unbatched-sample", type=int, default=64)
+    ap.add_argument("--quick", action="store_true", help="skip the FP64 comparison and the CPU baseline")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

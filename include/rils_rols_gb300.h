@@ -171,12 +171,36 @@ rrg_status rrg_eval(rrg_dataset* ds, const rrg_batch* batch, int32_t precision, 
  */
 rrg_status rrg_predict(rrg_dataset* ds, const rrg_batch* batch, double* values);
 
+/* Host-side check of a batch against a dataset of d features: opcodes,
+ * feature / constant / slot indices and spill depths.  rrg_round_submit runs
+ * the same check; no device is needed. */
+rrg_status rrg_batch_validate(const rrg_batch* batch, int32_t d);
+
 /* Rows and columns of a dataset. */
 int64_t rrg_dataset_rows(const rrg_dataset* ds);
 int32_t rrg_dataset_cols(const rrg_dataset* ds);
 
 /* Kernels launched by the last completed round on this context (for audits). */
 int64_t rrg_last_round_launches(const rrg_context* ctx);
+
+/* Statistics of the last completed round, written to out[0..n):
+ *   [0] kernels launched   [1] candidates routed to the FP64 path (beyond the
+ *   mixed kernels' limits)  [2] ill-conditioned systems re-solved in FP64
+ *   [3] candidates that needed the residual pass.  Returns the count written. */
+int32_t rrg_last_round_stats(const rrg_context* ctx, int64_t* out, int32_t n);
+
+/* The CUDA stream (cudaStream_t) every kernel of this context runs on, so that
+ * a caller can order or time its own work against the rounds. */
+void* rrg_context_stream(const rrg_context* ctx);
+
+/* Per-phase device timing of later rounds (CUDA events around every launch on
+ * the context stream); off by default. */
+rrg_status rrg_context_set_timing(rrg_context* ctx, int32_t on);
+/* Device milliseconds and launch counts of the last completed round, per
+ * phase: [0] mixed gram pass, [1] mixed solve, [2] mixed residual pass,
+ * [3] finalize, [4] FP64 evaluation, [5] FP64 QR, [6] FP64 residual.
+ * Returns the number of phases written. */
+int32_t rrg_last_round_timing(const rrg_context* ctx, double* ms, int64_t* launches, int32_t n);
 
 #ifdef __cplusplus
 }

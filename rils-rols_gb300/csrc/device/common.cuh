@@ -1,0 +1,53 @@
+// Shared device-side definitions of the GB300 fitness path.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../../include/rils_rols_gb300.h"
+
+namespace rrd {
+
+// Error bits a kernel may raise in the round's status word.
+enum : uint32_t {
+  ST_BAD_CODE = 0x1,       // unknown opcode or argument out of range
+  ST_STACK = 0x2,          // spill stack over/underflow
+  ST_WAIT_TIMEOUT = 0x4,   // a bounded mbarrier / flag wait ran out
+  ST_TOO_LARGE = 0x8       // candidate beyond the kernel's term limit
+};
+
+// Batch of one round, resident on the device.
+struct DevBatch {
+  const rrg_cand* cands;
+  const rrg_factor* factors;
+  const uint32_t* code;
+  const double* consts;
+  const float* consts32;
+  int32_t n_cand, n_factors, n_code, n_consts;
+};
+
+// Resident dataset: d columns of n_pad values each (rows >= n are zero).
+struct DevData {
+  const double* X64;
+  const float* X32;
+  const double* y64;
+  const float* y32;    // y rounded to FP32 (high part)
+  const float* y32lo;  // y - y32, rounded to FP32 (low part)
+  int64_t n, n_pad;
+  int32_t d;
+  double ymean, sst, ysum, yy;  // mean(y), sum((y - mean)^2), sum(y), sum(y^2): FP64 sums
+};
+
+// Per-candidate scratch placement of a plain round.
+struct PlainCand {
+  int64_t a_col;   // first column of its factor values in the A arena (n_pad doubles per column)
+  int64_t m_col;   // first column of its QR working copy (k+1 columns)
+  int64_t s_off;   // offset of its stacked R blocks (TSQR only)
+  int32_t k;       // OLS columns (factors + free term); 1 when untuned
+  int32_t pad;
+};
+
+constexpr double kEps12 = 1e-12;  // value_zero / value_one threshold (node.h:13-14)
+
+__host__ __device__ inline int64_t round_up(int64_t a, int64_t b) { return (a + b - 1) / b * b; }
+
+}  // namespace rrd

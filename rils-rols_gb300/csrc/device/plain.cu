@@ -1,0 +1,468 @@
+// Plain FP64 fitness path: the drop-in form of tune_constants + fitness
+// (rils_rols_cpp/rils_rols_cpp.cpp:445-541).
+//
+//   plain_eval   evaluates every factor program of a candidate on every row
+//                (node::evaluate_all, node.cpp:5-95) into the A arena and,
+//                for tall tiled (TSQR) rounds, reduces each row slice of
+//                [A | 1 | y] to a k x (k+1) triangle by Householder QR;
+//   plain_qr     column-pivoted Householder least squares with the pivot,
+//                rank and norm-down-dating rules of Eigen's
+//                ColPivHouseholderQR (eigen/Eigen/src/QR/ColPivHouseholderQR.h:482-608),
+//                on [A | 1 | y] directly (one slice) or on the stacked
+//                triangles (TSQR; the column norms, pivots and least-squares
+//                solution are those of A up to rounding);
+//   plain_resid  the rebuilt sum  sum_i c_i * f_i  with the drop / snap rules
+//                of rils_rols_cpp.cpp:488-517 and its squared residual;
+//   finalize     R2, RMSE and the NaN sentinel (rils_rols_cpp.cpp:40-49, 520-541).
+#include <cfloat>
+#include <cstdint>
+
+#include "common.cuh"
+#include "plain.cuh"
+#include "reduce.cuh"
+
+namespace rrd {
+
+namespace {
+
+constexpr int kMaxK = RRG_MAX_TERMS;
+
+__device__ __forceinline__ double bin64(int base, double a, double b) {
+  switch (base) {
+    case RRG_ADD: return __dadd_rn(a, b);
+    case RRG_SUB: return __dsub_rn(a, b);
+    case RRG_MUL: return __dmul_rn(a, b);
+    case RRG_DIV: return __ddiv_rn(a, b);
+    case RRG_POW: return pow(a, b);
+    case RRG_LT: return a < b ? 1.0 : 0.0;
+    case RRG_EQ: return a == b ? 1.0 : 0.0;
+    case RRG_NE: return a != b ? 1.0 : 0.0;
+    case RRG_MIN: return a < b ? a : b;
+    case RRG_MAX: return a > b ? a : b;
+    default: return __longlong_as_double(0x7ff8000000000000ll);
+  }
+}
+
+// Runs the code of one candidate on `row`; factor slot s is written to
+// out[s * n_pad + row].  Spill stack in shared memory, stride blockDim.x.
+__device__ __forceinline__ void run_row64(const uint32_t* code, int len, const double* consts, const DevData& ds,
+                                          int64_t row, double* st, double* out, uint32_t* status) {
+  double tos = 0.0;
+  int sp = 0;
+  const int stride = blockDim.x;
+  for (int pc = 0; pc < len; ++pc) {
+    const uint32_t w = code[pc];
+    const int op = (int)(w & 0xffu);
+    const uint32_t arg = w >> 8;
+    switch (op) {
+      case RRG_OP_LDV: tos = ds.X64[(int64_t)arg * ds.n_pad + row]; break;
+      case RRG_OP_LDC: tos = consts[arg]; break;
+      case RRG_OP_PSV:
+        if (sp >= RRG_MAX_STACK) { atomicOr(status, ST_STACK); return; }
+        st[sp++ * stride] = tos;
+        tos = ds.X64[(int64_t)arg * ds.n_pad + row];
+        break;
+      case RRG_OP_PSC:
+        if (sp >= RRG_MAX_STACK) { atomicOr(status, ST_STACK); return; }
+        st[sp++ * stride] = tos;
+        tos = consts[arg];
+        break;
+      case RRG_OP_SIN: tos = sin(tos); break;
+      case RRG_OP_COS: tos = cos(tos); break;
+      case RRG_OP_LN: tos = log(tos); break;
+      case RRG_OP_EXP: tos = exp(tos); break;
+      case RRG_OP_SQRT: tos = __dsqrt_rn(tos); break;
+      case RRG_OP_SQR: tos = __dmul_rn(tos, tos); break;
+      case RRG_OP_EMIT:
+        out[(int64_t)arg * ds.n_pad + row] = tos;
+        sp = 0;
+        break;
+      default: {
+        const int kk = op - RRG_OP_BIN;
+        if (kk < 0 || kk >= 8 * RRG_N_BASE) { atomicOr(status, ST_BAD_CODE); return; }
+        const int base = kk >> 3, src = (kk & 7) >> 1, dir = kk & 1;
+        double other;
+        if (src == RRG_SRC_S) {
+          if (sp <= 0) { atomicOr(status, ST_STACK); return; }
+          other = st[--sp * stride];
+        } else if (src == RRG_SRC_V) {
+          other = ds.X64[(int64_t)arg * ds.n_pad + row];
+        } else {
+          other = consts[arg];
+        }
+        tos = dir == RRG_DIR_N ? bin64(base, other, tos) : bin64(base, tos, other);
+      }
+    }
+  }
+}
+
+// Householder reflector of Q[kk.., kk] (Householder.h:67-96 semantics).
+// Returns tau; writes beta to Q[kk,kk] and the essential part below it.
+__device__ double make_householder(double* Q, int64_t ld, int64_t rows, int kk, double* red) {
+  double* col = Q + (int64_t)kk * ld;
+  double part = 0.0;
+  for (int64_t i = kk + 1 + threadIdx.x; i < rows; i += blockDim.x) part = __dadd_rn(part, __dmul_rn(col[i], col[i]));
+  const double tail_sq = (rows - kk == 1) ? 0.0 : block_sum(part, red);
+  const double c0 = col[kk];
+  double tau, beta;
+  __syncthreads();
+  if (tail_sq <= DBL_MIN) {
+    tau = 0.0;
+    beta = c0;
+    for (int64_t i = kk + 1 + threadIdx.x; i < rows; i += blockDim.x) col[i] = 0.0;
+  } else {
+    beta = __dsqrt_rn(__dadd_rn(__dmul_rn(c0, c0), tail_sq));
+    if (c0 >= 0.0) beta = -beta;
+    const double den = __dsub_rn(c0, beta);
+    for (int64_t i = kk + 1 + threadIdx.x; i < rows; i += blockDim.x) col[i] = __ddiv_rn(col[i], den);
+    tau = __ddiv_rn(__dsub_rn(beta, c0), beta);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) col[kk] = beta;
+  __syncthreads();
+  return tau;
+}
+
+// Applies H_kk = I - tau v v^T (v = [1, Q[kk+1.., kk]]) to columns
+// [c_lo, c_hi) of Q (rows kk..rows-1).  Householder.h:116-133 semantics.
+__device__ void apply_householder(double* Q, int64_t ld, int64_t rows, int kk, double tau, int c_lo, int c_hi,
+                                  double* red, double* sh_tmp) {
+  const int cnt = c_hi - c_lo;
+  if (cnt <= 0) return;
+  if (rows - kk == 1) {
+    for (int j = threadIdx.x; j < cnt; j += blockDim.x) {
+      double* q = Q + (int64_t)(c_lo + j) * ld + kk;
+      *q = __dmul_rn(*q, __dsub_rn(1.0, tau));
+    }
+    __syncthreads();
+    return;
+  }
+  if (tau == 0.0) return;
+  const double* v = Q + (int64_t)kk * ld;
+  double part[kMaxK + 1];
+  for (int j = 0; j < cnt; ++j) part[j] = 0.0;
+  for (int64_t i = kk + 1 + threadIdx.x; i < rows; i += blockDim.x) {
+    const double vi = v[i];
+    for (int j = 0; j < cnt; ++j) part[j] = __dadd_rn(part[j], __dmul_rn(vi, Q[(int64_t)(c_lo + j) * ld + i]));
+  }
+  block_sum_vec(part, cnt, red, sh_tmp);
+  // tmp_j += Q[kk, j]; Q[kk, j] -= tau * tmp_j
+  if (threadIdx.x == 0) {
+    for (int j = 0; j < cnt; ++j) {
+      double* q = Q + (int64_t)(c_lo + j) * ld + kk;
+      sh_tmp[j] = __dadd_rn(sh_tmp[j], *q);
+      *q = __dsub_rn(*q, __dmul_rn(tau, sh_tmp[j]));
+    }
+  }
+  __syncthreads();
+  for (int64_t i = kk + 1 + threadIdx.x; i < rows; i += blockDim.x) {
+    const double tv = __dmul_rn(tau, v[i]);
+    for (int j = 0; j < cnt; ++j) {
+      double* q = Q + (int64_t)(c_lo + j) * ld + i;
+      *q = __dsub_rn(*q, __dmul_rn(tv, sh_tmp[j]));
+    }
+  }
+  __syncthreads();
+}
+
+}  // namespace
+
+// ------------------------------------------------------------- kernels ----
+// grid (blocks per candidate, candidates); rows of block b: [b*n/nb, (b+1)*n/nb)
+__global__ void __launch_bounds__(256) plain_eval_kernel(DevBatch b, DevData ds, const PlainCand* pc,
+                                                          const int32_t* list, int cand0, double* A, double* M,
+                                                          double* S, int tsqr, uint32_t* status) {
+  extern __shared__ double smem[];
+  const int c = list ? list[cand0 + blockIdx.y] : cand0 + blockIdx.y;
+  const rrg_cand cd = b.cands[c];
+  const int nb = gridDim.x;
+  const int64_t r0 = ds.n * (int64_t)blockIdx.x / nb, r1 = ds.n * (int64_t)(blockIdx.x + 1) / nb;
+  double* st = smem + threadIdx.x;  // spill stack, RRG_MAX_STACK * blockDim.x doubles
+  uint32_t* code_s = reinterpret_cast<uint32_t*>(smem + RRG_MAX_STACK * blockDim.x);
+  const bool staged = cd.code_len <= kMaxCodeSmem;
+  if (staged)
+    for (int i = threadIdx.x; i < cd.code_len; i += blockDim.x) code_s[i] = b.code[cd.code_offset + i];
+  __syncthreads();
+  const uint32_t* code = staged ? code_s : b.code + cd.code_offset;
+  double* Ac = A + pc[c].a_col * ds.n_pad;
+  for (int64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x)
+    run_row64(code, cd.code_len, b.consts, ds, r, st, Ac, status);
+  if (!tsqr || cd.mode != RRG_TUNED) return;
+
+  // TSQR: [A | 1 | y] of this slice -> R (k x (k+1)) into S block blockIdx.x
+  const int k = pc[c].k;
+  double* Mc = M + pc[c].m_col * ds.n_pad;
+  for (int j = 0; j <= k; ++j)
+    for (int64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x)
+      Mc[(int64_t)j * ds.n_pad + r] = j < k - 1 ? Ac[(int64_t)j * ds.n_pad + r] : (j == k - 1 ? 1.0 : ds.y64[r]);
+  __syncthreads();
+  double* red = smem;  // reuse: (256/32) * (kMaxK+1) doubles
+  double* sh_tmp = smem + 8 * (kMaxK + 1);
+  double* Qs = Mc + r0;  // slice view, leading dimension n_pad
+  const int64_t rows = r1 - r0;
+  for (int kk = 0; kk < k; ++kk) {
+    const double tau = make_householder(Qs, ds.n_pad, rows, kk, red);
+    apply_householder(Qs, ds.n_pad, rows, kk, tau, kk + 1, k + 1, red, sh_tmp);
+  }
+  double* Sc = S + pc[c].s_off;
+  const int64_t ldS = (int64_t)nb * k;
+  for (int idx = threadIdx.x; idx < k * (k + 1); idx += blockDim.x) {
+    const int i = idx % k, j = idx / k;
+    Sc[(int64_t)j * ldS + (int64_t)blockIdx.x * k + i] = i <= j ? Qs[(int64_t)j * ds.n_pad + i] : 0.0;
+  }
+}
+
+// One block per tuned candidate: column-pivoted QR least squares.
+__global__ void __launch_bounds__(256) plain_qr_kernel(DevBatch b, DevData ds, const PlainCand* pc,
+                                                        const int32_t* list, int cand0, const double* A, double* M,
+                                                        double* S, int tsqr, int nb, double* coefs, rrg_result* res,
+                                                        uint32_t* status) {
+  extern __shared__ double smem[];
+  const int c = list ? list[cand0 + blockIdx.x] : cand0 + blockIdx.x;
+  const rrg_cand cd = b.cands[c];
+  if (cd.mode != RRG_TUNED) return;
+  const int k = pc[c].k;
+  if (k > kMaxK) {
+    if (threadIdx.x == 0) atomicOr(status, ST_TOO_LARGE);
+    return;
+  }
+  double* red = smem;                       // 8 * (kMaxK + 1)
+  double* sh_tmp = red + 8 * (kMaxK + 1);   // kMaxK + 1
+  double* nupd = sh_tmp + (kMaxK + 1);      // kMaxK
+  double* ndir = nupd + kMaxK;              // kMaxK
+  double* hc = ndir + kMaxK;                // kMaxK
+  int* perm = reinterpret_cast<int*>(hc + kMaxK);
+  int* misc = perm + kMaxK;                 // [0] pivot, [1] nonzero, [2..] recompute flags
+
+  double* Q;
+  int64_t ld, rows;
+  if (tsqr) {
+    Q = S + pc[c].s_off;
+    ld = (int64_t)nb * k;
+    rows = ld;
+  } else {
+    Q = M + pc[c].m_col * ds.n_pad;
+    ld = ds.n_pad;
+    rows = ds.n;
+    const double* Ac = A + pc[c].a_col * ds.n_pad;
+    for (int j = 0; j <= k; ++j)
+      for (int64_t r = threadIdx.x; r < rows; r += blockDim.x)
+        Q[(int64_t)j * ld + r] = j < k - 1 ? Ac[(int64_t)j * ds.n_pad + r] : (j == k - 1 ? 1.0 : ds.y64[r]);
+    __syncthreads();
+  }
+  const double rows_thr = (double)ds.n;
+  const int size = (int)(rows < k ? rows : k);
+
+  // initial column norms
+  {
+    double part[kMaxK];
+    for (int j = 0; j < k; ++j) part[j] = 0.0;
+    for (int64_t i = threadIdx.x; i < rows; i += blockDim.x)
+      for (int j = 0; j < k; ++j) {
+        const double q = Q[(int64_t)j * ld + i];
+        part[j] = __dadd_rn(part[j], __dmul_rn(q, q));
+      }
+    block_sum_vec(part, k, red, sh_tmp);
+  }
+  if (threadIdx.x == 0) {
+    for (int j = 0; j < k; ++j) {
+      ndir[j] = __dsqrt_rn(sh_tmp[j]);
+      nupd[j] = ndir[j];
+      perm[j] = j;
+    }
+    misc[1] = size;
+  }
+  __syncthreads();
+  double maxn = nupd[0];
+  for (int j = 1; j < k; ++j)
+    if (nupd[j] > maxn) maxn = nupd[j];
+  const double thr_helper = __ddiv_rn(__dmul_rn(__dmul_rn(maxn, DBL_EPSILON), __dmul_rn(maxn, DBL_EPSILON)), rows_thr);
+  const double downdate_thr = 1.4901161193847656e-08;  // sqrt(DBL_EPSILON)
+
+  for (int kk = 0; kk < size; ++kk) {
+    if (threadIdx.x == 0) {
+      int big = kk;
+      double bign = nupd[kk];
+      for (int j = kk + 1; j < k; ++j)
+        if (nupd[j] > bign) {
+          bign = nupd[j];
+          big = j;
+        }
+      if (misc[1] == size && __dmul_rn(bign, bign) < __dmul_rn(thr_helper, rows_thr - kk)) misc[1] = kk;
+      misc[0] = big;
+      if (big != kk) {
+        double t = nupd[kk]; nupd[kk] = nupd[big]; nupd[big] = t;
+        t = ndir[kk]; ndir[kk] = ndir[big]; ndir[big] = t;
+        int p = perm[kk]; perm[kk] = perm[big]; perm[big] = p;
+      }
+    }
+    __syncthreads();
+    const int big = misc[0];
+    if (big != kk) {
+      double* ca = Q + (int64_t)kk * ld;
+      double* cb = Q + (int64_t)big * ld;
+      for (int64_t i = threadIdx.x; i < rows; i += blockDim.x) {
+        const double t = ca[i];
+        ca[i] = cb[i];
+        cb[i] = t;
+      }
+    }
+    __syncthreads();
+    const double tau = make_householder(Q, ld, rows, kk, red);
+    if (threadIdx.x == 0) hc[kk] = tau;
+    // reflector kk reaches the right-hand side only while kk < rank
+    const int c_hi = misc[1] == size ? k + 1 : k;
+    apply_householder(Q, ld, rows, kk, tau, kk + 1, c_hi, red, sh_tmp);
+    // LAWN 176 norm down-dating (ColPivHouseholderQR.h:549-572)
+    int* rec = misc + 2;
+    if (threadIdx.x == 0) {
+      for (int j = kk + 1; j < k; ++j) {
+        rec[j] = 0;
+        if (nupd[j] != 0.0) {
+          double temp = __ddiv_rn(fabs(Q[(int64_t)j * ld + kk]), nupd[j]);
+          temp = __dmul_rn(__dadd_rn(1.0, temp), __dsub_rn(1.0, temp));
+          temp = temp < 0.0 ? 0.0 : temp;
+          const double ratio = __ddiv_rn(nupd[j], ndir[j]);
+          const double temp2 = __dmul_rn(temp, __dmul_rn(ratio, ratio));
+          if (temp2 <= downdate_thr) rec[j] = 1;
+          else nupd[j] = __dmul_rn(nupd[j], __dsqrt_rn(temp));
+        }
+      }
+    }
+    __syncthreads();
+    for (int j = kk + 1; j < k; ++j) {
+      if (!rec[j]) continue;  // uniform
+      double part = 0.0;
+      for (int64_t i = kk + 1 + threadIdx.x; i < rows; i += blockDim.x) {
+        const double q = Q[(int64_t)j * ld + i];
+        part = __dadd_rn(part, __dmul_rn(q, q));
+      }
+      const double s = block_sum(part, red);
+      if (threadIdx.x == 0) {
+        ndir[j] = __dsqrt_rn(s);
+        nupd[j] = ndir[j];
+      }
+      __syncthreads();
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const int r = misc[1];
+    double cvec[kMaxK];
+    for (int i = 0; i < r; ++i) cvec[i] = Q[(int64_t)k * ld + i];
+    for (int kk = r - 1; kk >= 0; --kk) {
+      cvec[kk] = __ddiv_rn(cvec[kk], Q[(int64_t)kk * ld + kk]);
+      for (int i = 0; i < kk; ++i) cvec[i] = __dsub_rn(cvec[i], __dmul_rn(cvec[kk], Q[(int64_t)kk * ld + i]));
+    }
+    double* out = coefs + cd.coef_offset;
+    for (int j = 0; j < k; ++j) out[j] = 0.0;
+    for (int i = 0; i < r; ++i) out[perm[i]] = cvec[i];
+    res[c].rank = r;
+  }
+}
+
+// grid (blocks per candidate, candidates): partial SSE of the rebuilt sum
+__global__ void __launch_bounds__(256) plain_resid_kernel(DevBatch b, DevData ds, const PlainCand* pc,
+                                                           const int32_t* list, int cand0, const double* A,
+                                                           const double* coefs, double* partial) {
+  __shared__ double red[32];
+  __shared__ double cs[kMaxK];
+  __shared__ int kind[kMaxK];  // 0 skip, 1 free term, 2 bare factor, 3 scaled factor
+  const int c = list ? list[cand0 + blockIdx.y] : cand0 + blockIdx.y;
+  const rrg_cand cd = b.cands[c];
+  const int nb = gridDim.x;
+  const bool tuned = cd.mode == RRG_TUNED;
+  const int k = pc[c].k;
+  const int m = tuned ? k - 1 : 1;
+  if (tuned) {
+    for (int i = threadIdx.x; i < k; i += blockDim.x) {
+      const double ci = coefs[cd.coef_offset + i];
+      cs[i] = ci;
+      kind[i] = fabs(ci) < kEps12 ? 0 : (i == m ? 1 : (fabs(ci - 1) < kEps12 ? 2 : 3));
+    }
+  }
+  __syncthreads();
+  const int64_t r0 = ds.n * (int64_t)blockIdx.x / nb, r1 = ds.n * (int64_t)(blockIdx.x + 1) / nb;
+  const double* Ac = A + pc[c].a_col * ds.n_pad;
+  double acc = 0.0;
+  for (int64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
+    double yp;
+    if (tuned) {
+      yp = 0.0;
+      bool have = false;
+      for (int i = 0; i < k; ++i) {
+        const int kd = kind[i];
+        if (kd == 0) continue;
+        const double term = kd == 1 ? __dmul_rn(cs[i], 1.0)
+                                    : (kd == 2 ? Ac[(int64_t)i * ds.n_pad + r] : __dmul_rn(cs[i], Ac[(int64_t)i * ds.n_pad + r]));
+        yp = have ? __dadd_rn(yp, term) : term;
+        have = true;
+      }
+    } else {
+      yp = Ac[r];
+    }
+    const double e = __dsub_rn(ds.y64[r], yp);
+    acc = __dadd_rn(acc, __dmul_rn(e, e));
+  }
+  const double s = block_sum(acc, red);
+  if (threadIdx.x == 0) partial[(int64_t)c * nb + blockIdx.x] = s;
+}
+
+// one thread per candidate: R2, RMSE, sentinel, rebuilt size
+__global__ void finalize_kernel(DevBatch b, DevData ds, const int32_t* list, int cand0, int cand1,
+                                const double* partial, int nb, const double* coefs, rrg_result* res,
+                                uint32_t flags_or, const double* sse_direct) {
+  const int i = cand0 + blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= cand1) return;
+  const int c = list ? list[i] : i;
+  const rrg_cand cd = b.cands[c];
+  double ssr = 0.0;
+  if (sse_direct && !(sse_direct[c] < 0.0)) {
+    ssr = sse_direct[c];
+  } else {
+    for (int j = 0; j < nb; ++j) ssr = __dadd_rn(ssr, partial[(int64_t)c * nb + j]);
+  }
+  const double r2 = __dsub_rn(1.0, __ddiv_rn(ssr, ds.sst));
+  const double rmse = __dsqrt_rn(__ddiv_rn(ssr, (double)ds.n));
+  rrg_result out = res[c];
+  out.flags |= flags_or;
+  int size = 0;
+  if (cd.mode == RRG_TUNED) {
+    const int m = cd.n_factors;
+    int kept = 0;
+    for (int i = 0; i <= m; ++i) {
+      const double ci = coefs[cd.coef_offset + i];
+      if (fabs(ci) < kEps12) continue;
+      ++kept;
+      if (i == m) size += 1;
+      else if (fabs(ci - 1) < kEps12) size += b.factors[cd.first_factor + i].n_nodes;
+      else size += 2 + b.factors[cd.first_factor + i].n_nodes;
+    }
+    size = kept == 0 ? 1 : size + kept - 1;
+    out.n_coef = m + 1;
+    if (out.rank < m + 1) out.flags |= RRG_F_RANK_DEFICIENT;
+  } else {
+    size = b.factors[cd.first_factor].n_nodes;
+    out.n_coef = 0;
+    out.rank = 0;
+  }
+  if (r2 != r2 || rmse != rmse) {
+    out.loss = 1000;
+    out.rmse = 1000;
+    out.size = 1000;
+    out.flags |= RRG_F_NONFINITE;
+  } else {
+    out.loss = __dsub_rn(1.0, r2);
+    out.rmse = rmse;
+    out.size = size;
+  }
+  res[c] = out;
+}
+
+// ----------------------------------------------------------- launchers ----
+size_t plain_eval_smem() { return RRG_MAX_STACK * 256 * sizeof(double) + kMaxCodeSmem * sizeof(uint32_t); }
+size_t plain_qr_smem() {
+  return (8 * (kMaxK + 1) + (kMaxK + 1) + 3 * kMaxK) * sizeof(double) + (kMaxK + 2 + kMaxK) * sizeof(int);
+}
+
+}  // namespace rrd

@@ -1,0 +1,841 @@
+// Device runtime and C ABI of the GB300 fitness path (include/rils_rols_gb300.h).
+//
+// A context owns one CUDA stream, pinned staging buffers and device arenas
+// that only grow.  A round is: validate the batch on the host, pack it into
+// pinned staging, one host-to-device copy, the kernels of the chosen
+// precision (plain.cu or mixed.cu), one device-to-host copy of the results,
+// and an event that rrg_round_wait polls with a bounded wait.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../common/error.h"
+#include "common.cuh"
+#include "mixed.cuh"
+#include "plain.cuh"
+#include "runtime.cuh"
+
+using namespace rrd;
+
+namespace {
+
+bool cuda_ok(cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return true;
+  rrc::set_error(std::string(what) + ": " + cudaGetErrorString(e));
+  return false;
+}
+
+#define RRG_CUDA(call)                                   \
+  do {                                                   \
+    if (!cuda_ok((call), #call)) return RRG_E_CUDA;      \
+  } while (0)
+
+}  // namespace
+
+// ------------------------------------------------------------- buffers ----
+bool DevBuf::reserve(size_t bytes) {
+  if (bytes <= cap) return true;
+  if (ptr) {
+    cudaDeviceSynchronize();  // queued kernels may still use the old buffer
+    cudaFree(ptr);
+  }
+  ptr = nullptr;
+  cap = 0;
+  size_t want = round_up((int64_t)bytes, 1 << 20);
+  if (cudaMalloc(&ptr, want) != cudaSuccess) {
+    cudaGetLastError();
+    if (cudaMalloc(&ptr, bytes) != cudaSuccess) {
+      cudaGetLastError();
+      ptr = nullptr;
+      return false;
+    }
+    want = bytes;
+  }
+  cap = want;
+  return true;
+}
+void DevBuf::release() {
+  if (ptr) cudaFree(ptr);
+  ptr = nullptr;
+  cap = 0;
+}
+bool HostBuf::reserve(size_t bytes) {
+  if (bytes <= cap) return true;
+  if (ptr) cudaFreeHost(ptr);
+  ptr = nullptr;
+  cap = 0;
+  size_t want = round_up((int64_t)std::max(bytes, (size_t)(1 << 16)), 1 << 16);
+  if (cudaMallocHost(&ptr, want) != cudaSuccess) {
+    cudaGetLastError();
+    ptr = nullptr;
+    return false;
+  }
+  cap = want;
+  return true;
+}
+void HostBuf::release() {
+  if (ptr) cudaFreeHost(ptr);
+  ptr = nullptr;
+  cap = 0;
+}
+
+// --------------------------------------------------------------- timing ----
+cudaEvent_t rrg_context::mark_begin() {
+  if (!timing) return nullptr;
+  if (event_next >= event_pool.size()) {
+    cudaEvent_t e;
+    if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+    event_pool.push_back(e);
+  }
+  cudaEvent_t e = event_pool[event_next++];
+  cudaEventRecord(e, stream);
+  return e;
+}
+void rrg_context::mark_end(int phase, cudaEvent_t begin) {
+  if (!timing || !begin) return;
+  cudaEvent_t e = mark_begin();
+  if (e) marks.push_back({phase, {begin, e}});
+}
+
+// ----------------------------------------------------------- validation ----
+// Every instruction is checked on the host so that kernels never index out of
+// bounds: opcodes, feature and constant indices, factor slots, and the spill
+// depth of every program.
+static rrg_status validate(const rrg_batch* b, int32_t d, int64_t* n_coefs_out) {
+  if (!b || b->n_cand < 0 || b->n_factors < 0 || b->n_code < 0 || b->n_consts < 0) return RRG_E_INVALID;
+  if (b->n_cand > 0 && (!b->cands || !b->factors || !b->code)) return RRG_E_INVALID;
+  int64_t n_coefs = 0;
+  for (int32_t c = 0; c < b->n_cand; ++c) {
+    const rrg_cand& cd = b->cands[c];
+    if (cd.code_offset < 0 || cd.code_len < 0 || (int64_t)cd.code_offset + cd.code_len > b->n_code) return RRG_E_INVALID;
+    if (cd.code_len == 0 && !(cd.mode == RRG_TUNED && cd.n_factors == 0)) return RRG_E_INVALID;
+    if (cd.first_factor < 0 || cd.n_factors < 0 || (int64_t)cd.first_factor + cd.n_factors > b->n_factors)
+      return RRG_E_INVALID;
+    if (cd.mode == RRG_TUNED) {
+      if (cd.n_factors + 1 > RRG_MAX_TERMS) return RRG_E_TOO_LARGE;
+      if (cd.coef_offset < 0) return RRG_E_INVALID;
+      n_coefs = std::max(n_coefs, (int64_t)cd.coef_offset + cd.n_factors + 1);
+    } else if (cd.mode == RRG_UNTUNED) {
+      if (cd.n_factors != 1) return RRG_E_INVALID;
+    } else {
+      return RRG_E_INVALID;
+    }
+    if (cd.stack_need < 0 || cd.stack_need > RRG_MAX_STACK) return RRG_E_TOO_LARGE;
+    int sp = 0, depth = 0, emitted = 0;
+    bool live = false;
+    for (int32_t pc = 0; pc < cd.code_len; ++pc) {
+      const uint32_t w = b->code[cd.code_offset + pc];
+      const int op = (int)(w & 0xffu);
+      const uint32_t arg = w >> 8;
+      switch (op) {
+        case RRG_OP_LDV: case RRG_OP_PSV:
+          if ((int64_t)arg >= d) return RRG_E_INVALID;
+          break;
+        case RRG_OP_LDC: case RRG_OP_PSC:
+          if ((int64_t)arg >= b->n_consts) return RRG_E_INVALID;
+          break;
+        default: break;
+      }
+      if (op == RRG_OP_LDV || op == RRG_OP_LDC) {
+        if (live) return RRG_E_INVALID;
+        live = true;
+      } else if (op == RRG_OP_PSV || op == RRG_OP_PSC) {
+        if (!live) return RRG_E_INVALID;
+        if (++sp > RRG_MAX_STACK) return RRG_E_TOO_LARGE;
+        depth = std::max(depth, sp);
+      } else if (op >= RRG_OP_SIN && op <= RRG_OP_SQR) {
+        if (!live) return RRG_E_INVALID;
+      } else if (op == RRG_OP_EMIT) {
+        if (!live || (int)arg != emitted || sp != 0) return RRG_E_INVALID;
+        ++emitted;
+        live = false;
+      } else if (op >= RRG_OP_BIN) {
+        const int k = op - RRG_OP_BIN;
+        if (k >= 8 * RRG_N_BASE || (k & 7) >= 6 || !live) return RRG_E_INVALID;
+        const int src = (k & 7) >> 1;
+        if (src == RRG_SRC_S) {
+          if (--sp < 0) return RRG_E_INVALID;
+        } else if (src == RRG_SRC_V) {
+          if ((int64_t)arg >= d) return RRG_E_INVALID;
+        } else if ((int64_t)arg >= b->n_consts) {
+          return RRG_E_INVALID;
+        }
+      } else {
+        return RRG_E_INVALID;
+      }
+    }
+    if (live || emitted != cd.n_factors || depth > cd.stack_need) return RRG_E_INVALID;
+  }
+  *n_coefs_out = n_coefs;
+  return RRG_OK;
+}
+
+// -------------------------------------------------------------- context ----
+rrg_status rrg_context::stage_batch(const rrg_batch* b) {
+  const size_t sz_c = sizeof(rrg_cand) * b->n_cand, sz_f = sizeof(rrg_factor) * b->n_factors;
+  const size_t sz_k = sizeof(uint32_t) * b->n_code, sz_d = sizeof(double) * b->n_consts;
+  const size_t sz_s = sizeof(float) * b->n_consts;
+  off_c = 0;
+  off_f = round_up(off_c + sz_c, 256);
+  off_k = round_up(off_f + sz_f, 256);
+  off_d = round_up(off_k + sz_k, 256);
+  off_s = round_up(off_d + sz_d, 256);
+  batch_bytes = round_up(off_s + sz_s + 8, 256);
+  if (!h_batch.reserve(batch_bytes) || !d_batch.reserve(batch_bytes)) {
+    rrc::set_error("cannot reserve batch staging");
+    return RRG_E_OOM;
+  }
+  char* h = static_cast<char*>(h_batch.ptr);
+  if (sz_c) std::memcpy(h + off_c, b->cands, sz_c);
+  if (sz_f) std::memcpy(h + off_f, b->factors, sz_f);
+  if (sz_k) std::memcpy(h + off_k, b->code, sz_k);
+  if (sz_d) std::memcpy(h + off_d, b->consts, sz_d);
+  float* c32 = reinterpret_cast<float*>(h + off_s);
+  for (int32_t i = 0; i < b->n_consts; ++i) c32[i] = (float)b->consts[i];
+  char* d = static_cast<char*>(d_batch.ptr);
+  dev.cands = reinterpret_cast<const rrg_cand*>(d + off_c);
+  dev.factors = reinterpret_cast<const rrg_factor*>(d + off_f);
+  dev.code = reinterpret_cast<const uint32_t*>(d + off_k);
+  dev.consts = reinterpret_cast<const double*>(d + off_d);
+  dev.consts32 = reinterpret_cast<const float*>(d + off_s);
+  dev.n_cand = b->n_cand;
+  dev.n_factors = b->n_factors;
+  dev.n_code = b->n_code;
+  dev.n_consts = b->n_consts;
+  host_cands.assign(b->cands, b->cands + b->n_cand);
+  if (!cuda_ok(cudaMemcpyAsync(d_batch.ptr, h_batch.ptr, batch_bytes, cudaMemcpyHostToDevice, stream),
+               "batch upload"))
+    return RRG_E_CUDA;
+  return RRG_OK;
+}
+
+// Plain FP64 round over `list` (or [lo, hi)), in sub-batches that fit the
+// scratch budget.
+rrg_status rrg_context::run_plain(const rrg_dataset* ds, int32_t lo, int32_t hi, bool predict_only,
+                                  const std::vector<int32_t>* list, uint32_t flags_or) {
+  const DevData dd = ds->view();
+  const int64_t n_pad = ds->n_pad;
+  std::vector<int32_t> all;
+  if (!list) {
+    for (int32_t c = lo; c < hi; ++c) all.push_back(c);
+    list = &all;
+  }
+  const int32_t cnt = (int32_t)list->size();
+  if (cnt == 0) return RRG_OK;
+  struct Sub {
+    int32_t p, e, nb;
+    bool tsqr;
+  };
+  std::vector<Sub> subs;
+  std::vector<PlainCand> pcs(host_cands.size());
+  int64_t max_cols = 1, max_s = 1, max_nb = 1;
+  for (int32_t p = 0; p < cnt;) {
+    int64_t cols = 0;
+    int32_t e = p;
+    while (e < cnt) {
+      const int32_t c = (*list)[e];
+      const rrg_cand& cd = host_cands[c];
+      const int64_t k = cd.mode == RRG_TUNED ? cd.n_factors + 1 : 1;
+      const int64_t need = (cols + 2 * k + 1) * n_pad * (int64_t)sizeof(double);
+      if (e > p && (size_t)need > scratch_budget_bytes) break;
+      pcs[c].a_col = cols;
+      pcs[c].m_col = cols + k;
+      pcs[c].k = (int32_t)k;
+      cols += 2 * k + 1;
+      ++e;
+    }
+    const int32_t ns = e - p;
+    int nb = (int)std::min<int64_t>(std::max<int64_t>(1, (4LL * sm_count + ns - 1) / ns), (ds->n + 1023) / 1024);
+    nb = std::max(nb, 1);
+    bool tsqr = !predict_only && ds->n >= 65536 && ns < 2 * sm_count;
+    if (tsqr) nb = (int)std::max<int64_t>(1, std::min<int64_t>(nb, ds->n / 2048));
+    tsqr = tsqr && nb > 1;
+    int64_t s_total = 0;
+    for (int32_t i = p; i < e; ++i) {
+      const int32_t c = (*list)[i];
+      pcs[c].s_off = s_total;
+      if (tsqr) s_total += (int64_t)nb * pcs[c].k * (pcs[c].k + 1);
+    }
+    max_cols = std::max(max_cols, cols);
+    max_s = std::max(max_s, s_total);
+    max_nb = std::max<int64_t>(max_nb, nb);
+    subs.push_back(Sub{p, e, nb, tsqr});
+    p = e;
+  }
+  const size_t pc_bytes = sizeof(PlainCand) * host_cands.size();
+  const size_t list_bytes = sizeof(int32_t) * cnt;
+  if (!d_A.reserve((size_t)max_cols * n_pad * sizeof(double)) || !d_S.reserve((size_t)max_s * sizeof(double)) ||
+      !d_pc.reserve(pc_bytes) || !d_partial.reserve(sizeof(double) * (size_t)host_cands.size() * max_nb) ||
+      !h_pc.reserve(pc_bytes + list_bytes) || !d_list.reserve(list_bytes)) {
+    rrc::set_error("device scratch allocation failed");
+    return RRG_E_OOM;
+  }
+  // h_pc may still feed a copy queued by an earlier call of this round
+  RRG_CUDA(cudaStreamSynchronize(stream));
+  std::memcpy(h_pc.ptr, pcs.data(), pc_bytes);
+  std::memcpy(static_cast<char*>(h_pc.ptr) + pc_bytes, list->data(), list_bytes);
+  RRG_CUDA(cudaMemcpyAsync(d_pc.ptr, h_pc.ptr, pc_bytes, cudaMemcpyHostToDevice, stream));
+  RRG_CUDA(cudaMemcpyAsync(d_list.ptr, static_cast<char*>(h_pc.ptr) + pc_bytes, list_bytes, cudaMemcpyHostToDevice,
+                           stream));
+  const PlainCand* pc = static_cast<const PlainCand*>(d_pc.ptr);
+  const int32_t* dl = static_cast<const int32_t*>(d_list.ptr);
+  double* A = static_cast<double*>(d_A.ptr);
+  double* S = static_cast<double*>(d_S.ptr);
+  double* coefs = static_cast<double*>(d_coefs.ptr);
+  rrg_result* res = static_cast<rrg_result*>(d_res.ptr);
+  uint32_t* status = static_cast<uint32_t*>(d_status.ptr);
+  double* partial = static_cast<double*>(d_partial.ptr);
+  for (const Sub& sb : subs) {
+    const int32_t ns = sb.e - sb.p;
+    cudaEvent_t t0 = mark_begin();
+    plain_eval_kernel<<<dim3(sb.nb, ns), 256, plain_eval_smem(), stream>>>(dev, dd, pc, dl, sb.p, A, A, S,
+                                                                            sb.tsqr ? 1 : 0, status);
+    mark_end(P_PLAIN_EVAL, t0);
+    ++launches;
+    if (predict_only) continue;
+    t0 = mark_begin();
+    plain_qr_kernel<<<ns, 256, plain_qr_smem(), stream>>>(dev, dd, pc, dl, sb.p, A, A, S, sb.tsqr ? 1 : 0, sb.nb,
+                                                          coefs, res, status);
+    mark_end(P_PLAIN_QR, t0);
+    t0 = mark_begin();
+    plain_resid_kernel<<<dim3(sb.nb, ns), 256, 0, stream>>>(dev, dd, pc, dl, sb.p, A, coefs, partial);
+    mark_end(P_PLAIN_RESID, t0);
+    t0 = mark_begin();
+    finalize_kernel<<<(ns + 127) / 128, 128, 0, stream>>>(dev, dd, dl, sb.p, sb.e, partial, sb.nb, coefs, res,
+                                                          flags_or, nullptr);
+    mark_end(P_FINAL, t0);
+    launches += 3;
+  }
+  RRG_CUDA(cudaGetLastError());
+  return RRG_OK;
+}
+
+// Mixed round.  Candidates are bucketed by factor count (untuned programs use
+// the 1-factor bucket) and sorted by program length within a bucket; programs
+// beyond the mixed kernels' limits go to the FP64 path.  Gram pass + solve for
+// every bucket; the residual pass only for candidates whose one-pass SSE is
+// not accurate enough; ill-conditioned systems are re-solved in FP64.
+rrg_status rrg_context::run_mixed(const rrg_dataset* ds, int32_t n_cand) {
+  const DevData dd = ds->view();
+  static const int kBuckets[4] = {1, 2, 4, 8};
+  std::vector<int32_t> bucket[4], plain;
+  for (int32_t c = 0; c < n_cand; ++c) {
+    const rrg_cand& cd = host_cands[c];
+    const bool fits = cd.stack_need <= kMixedStackCap && (cd.mode != RRG_TUNED || cd.n_factors <= kMixedMaxM);
+    if (!fits) {
+      plain.push_back(c);
+      continue;
+    }
+    const int m = cd.mode == RRG_TUNED ? std::max(cd.n_factors, 1) : 1;
+    int b = 0;
+    while (kBuckets[b] < m) ++b;
+    bucket[b].push_back(c);
+  }
+  for (auto& v : bucket)  // longest programs first: the short ones fill the tail of each work unit
+    std::stable_sort(v.begin(), v.end(),
+                     [&](int32_t x, int32_t y) { return host_cands[x].code_len > host_cands[y].code_len; });
+  last_plain_routed = (int64_t)plain.size();
+  // one tile height for the round: the largest multiple of 128 (<= 4096) whose
+  // staging fits next to the stacks and code buffers of every bucket in use
+  int tile = 4096;
+  for (int b = 0; b < 4; ++b)
+    if (!bucket[b].empty())
+      while (tile > 128 && mixed_smem(kBuckets[b], ds->d, tile, true) > 227 * 1024) tile -= 128;
+  if (mixed_tile_override > 0) tile = mixed_tile_override;
+  tile = (int)std::min<int64_t>(tile, ds->n_pad);
+  const int n_tiles = (int)((ds->n_pad + tile - 1) / tile);
+  std::vector<int32_t> lists;
+  int32_t off[5];
+  for (int b = 0; b < 4; ++b) {
+    off[b] = (int32_t)lists.size();
+    lists.insert(lists.end(), bucket[b].begin(), bucket[b].end());
+  }
+  off[4] = (int32_t)lists.size();
+  const int32_t n_mixed = off[4];
+  size_t gram_elems = 0, goff[4];
+  for (int b = 0; b < 4; ++b) {
+    goff[b] = gram_elems;
+    gram_elems += bucket[b].size() * (size_t)n_tiles * mixed_gram_entries(kBuckets[b]);
+  }
+  const int fb_cap = std::max(1, n_cand);
+  const size_t list_bytes = sizeof(int32_t) * (lists.size() * 2 + 8);
+  const size_t back_bytes = sizeof(int32_t) * (fb_cap + 1) + (size_t)fb_cap;  // fallback list + pass2 flags
+  if (!d_mlist.reserve(list_bytes) || !h_mlist.reserve(list_bytes) ||
+      !d_gram.reserve(sizeof(float2) * std::max<size_t>(1, gram_elems)) ||
+      !d_terms.reserve(sizeof(MixedTerm) * fb_cap) || !d_sse1.reserve(sizeof(double) * fb_cap) ||
+      !d_partial.reserve(sizeof(double) * (size_t)fb_cap * n_tiles) || !d_fallback.reserve(back_bytes) ||
+      !h_fallback.reserve(back_bytes)) {
+    rrc::set_error("mixed round: scratch allocation failed");
+    return RRG_E_OOM;
+  }
+  int32_t* hl = static_cast<int32_t*>(h_mlist.ptr);
+  std::memcpy(hl, lists.data(), sizeof(int32_t) * lists.size());
+  RRG_CUDA(cudaMemcpyAsync(d_mlist.ptr, hl, sizeof(int32_t) * std::max<size_t>(1, lists.size()), cudaMemcpyHostToDevice,
+                           stream));
+  RRG_CUDA(cudaMemsetAsync(d_fallback.ptr, 0, back_bytes, stream));
+  const int32_t* dl = static_cast<const int32_t*>(d_mlist.ptr);
+  float2* gram = static_cast<float2*>(d_gram.ptr);
+  MixedTerm* terms = static_cast<MixedTerm*>(d_terms.ptr);
+  double* sse = static_cast<double*>(d_partial.ptr);
+  double* sse1 = static_cast<double*>(d_sse1.ptr);
+  int32_t* fallback = static_cast<int32_t*>(d_fallback.ptr);
+  uint8_t* pass2 = reinterpret_cast<uint8_t*>(fallback + fb_cap + 1);
+  uint32_t* status = static_cast<uint32_t*>(d_status.ptr);
+  rrg_result* res = static_cast<rrg_result*>(d_res.ptr);
+  double* coefs = static_cast<double*>(d_coefs.ptr);
+
+  auto make_args = [&](int mmax, const int32_t* list, int32_t cnt, float2* g) {
+    MixedArgs a;
+    a.b = dev;
+    a.ds = dd;
+    a.list = list;
+    a.n_list = cnt;
+    const int nw = mixed_threads(mmax) / 32;
+    const int want_groups = std::max(1, (int)((4LL * sm_count + n_tiles - 1) / n_tiles));
+    a.group = std::max(4 * nw, (cnt + want_groups - 1) / want_groups);
+    a.n_tiles = n_tiles;
+    a.tile = tile;
+    a.n_units = n_tiles * ((cnt + a.group - 1) / a.group);
+    a.gram = g;
+    a.sse = sse;
+    a.terms = terms;
+    a.status = status;
+    return a;
+  };
+  for (int b = 0; b < 4; ++b) {
+    const int32_t cnt = (int32_t)bucket[b].size();
+    if (!cnt) continue;
+    MixedArgs a = make_args(kBuckets[b], dl + off[b], cnt, gram + goff[b]);
+    const int grid = std::min(a.n_units, sm_count);
+    cudaEvent_t t0 = mark_begin();
+    if (!launch_gram(kBuckets[b], a, grid, mixed_smem(kBuckets[b], ds->d, tile, false), stream)) {
+      cuda_ok(cudaGetLastError(), "mixed gram launch");
+      return RRG_E_CUDA;
+    }
+    mark_end(P_GRAM, t0);
+    SolveArgs sa;
+    sa.b = dev;
+    sa.ds = dd;
+    sa.list = dl + off[b];
+    sa.n_list = cnt;
+    sa.n_tiles = n_tiles;
+    sa.mmax = kBuckets[b];
+    sa.gram = gram + goff[b];
+    sa.coefs = coefs;
+    sa.terms = terms;
+    sa.res = res;
+    sa.fallback = fallback;
+    sa.fallback_cap = fb_cap;
+    sa.sse1 = sse1;
+    sa.pass2 = pass2;
+    sa.rank_tol = 1e-11;
+    sa.fallback_tol = 1e-7;
+    sa.pass2_tol = 1e-8;
+    t0 = mark_begin();
+    if (!launch_solve(sa, stream)) {
+      cuda_ok(cudaGetLastError(), "mixed solve launch");
+      return RRG_E_CUDA;
+    }
+    mark_end(P_SOLVE, t0);
+    launches += 2;
+  }
+  // fallback list and residual-pass flags back to the host
+  RRG_CUDA(cudaMemcpyAsync(h_fallback.ptr, d_fallback.ptr, back_bytes, cudaMemcpyDeviceToHost, stream));
+  RRG_CUDA(cudaStreamSynchronize(stream));
+  const int32_t* hf = static_cast<const int32_t*>(h_fallback.ptr);
+  const uint8_t* hp2 = reinterpret_cast<const uint8_t*>(hf + fb_cap + 1);
+  const int32_t nf = std::min(hf[0], fb_cap);
+  std::vector<int32_t> fb(hf + 1, hf + 1 + nf);
+  std::sort(fb.begin(), fb.end());
+  last_fallback = nf;
+  // residual pass on the flagged candidates, bucket by bucket
+  int32_t* hl2 = hl + lists.size();
+  int32_t n2 = 0, off2[5];
+  for (int b = 0; b < 4; ++b) {
+    off2[b] = n2;
+    for (int32_t c : bucket[b])
+      if (hp2[c]) hl2[n2++] = c;
+  }
+  off2[4] = n2;
+  last_pass2 = n2;
+  if (n2 > 0) {
+    RRG_CUDA(cudaMemcpyAsync(const_cast<int32_t*>(dl) + lists.size(), hl2, sizeof(int32_t) * n2,
+                             cudaMemcpyHostToDevice, stream));
+    for (int b = 0; b < 4; ++b) {
+      const int32_t cnt = off2[b + 1] - off2[b];
+      if (!cnt) continue;
+      MixedArgs a = make_args(kBuckets[b], dl + lists.size() + off2[b], cnt, nullptr);
+      const int grid = std::min(a.n_units, sm_count);
+      cudaEvent_t t0 = mark_begin();
+      if (!launch_resid(kBuckets[b], a, grid, mixed_smem(kBuckets[b], ds->d, tile, true), stream)) {
+        cuda_ok(cudaGetLastError(), "mixed residual launch");
+        return RRG_E_CUDA;
+      }
+      mark_end(P_RESID, t0);
+      ++launches;
+    }
+  }
+  if (n_mixed > 0) {
+    cudaEvent_t t0 = mark_begin();
+    finalize_kernel<<<(n_mixed + 127) / 128, 128, 0, stream>>>(dev, dd, dl, 0, n_mixed, sse, n_tiles, coefs, res, 0u,
+                                                               sse1);
+    mark_end(P_FINAL, t0);
+    ++launches;
+  }
+  RRG_CUDA(cudaGetLastError());
+  rrg_status st = RRG_OK;
+  if (!plain.empty()) st = run_plain(ds, 0, 0, false, &plain, 0u);
+  if (st == RRG_OK && !fb.empty()) st = run_plain(ds, 0, 0, false, &fb, RRG_F_QR_FALLBACK);
+  return st;
+}
+
+rrg_status rrg_context::submit(rrg_dataset* ds, const rrg_batch* b, int32_t precision, rrg_result* results,
+                               double* coefs) {
+  if (in_flight) {
+    rrc::set_error("a round is already in flight on this context");
+    return RRG_E_INVALID;
+  }
+  int64_t n_coefs = 0;
+  rrg_status st = validate(b, ds->d, &n_coefs);
+  if (st != RRG_OK) {
+    rrc::set_error("rrg_round_submit: malformed or oversized batch");
+    return st;
+  }
+  if (precision != RRG_PLAIN_FP64 && precision != RRG_MIXED) return RRG_E_INVALID;
+  if (n_coefs > 0 && !coefs) return RRG_E_INVALID;
+  RRG_CUDA(cudaSetDevice(device));
+  launches = 0;
+  last_plain_routed = last_fallback = last_pass2 = 0;
+  marks.clear();
+  event_next = 0;
+  st = stage_batch(b);
+  if (st != RRG_OK) return st;
+  const size_t res_bytes = sizeof(rrg_result) * std::max(1, b->n_cand);
+  const size_t coef_bytes = sizeof(double) * std::max<int64_t>(1, n_coefs);
+  if (!d_res.reserve(res_bytes) || !d_coefs.reserve(coef_bytes) || !d_status.reserve(64) ||
+      !h_res.reserve(res_bytes) || !h_coefs.reserve(coef_bytes) || !h_status.reserve(64)) {
+    rrc::set_error("cannot reserve result buffers");
+    return RRG_E_OOM;
+  }
+  RRG_CUDA(cudaMemsetAsync(d_res.ptr, 0, res_bytes, stream));
+  RRG_CUDA(cudaMemsetAsync(d_coefs.ptr, 0, coef_bytes, stream));
+  RRG_CUDA(cudaMemsetAsync(d_status.ptr, 0, 64, stream));
+  if (precision == RRG_PLAIN_FP64) st = run_plain(ds, 0, b->n_cand, false);
+  else st = run_mixed(ds, b->n_cand);
+  if (st != RRG_OK) return st;
+  RRG_CUDA(cudaMemcpyAsync(h_res.ptr, d_res.ptr, res_bytes, cudaMemcpyDeviceToHost, stream));
+  RRG_CUDA(cudaMemcpyAsync(h_coefs.ptr, d_coefs.ptr, coef_bytes, cudaMemcpyDeviceToHost, stream));
+  RRG_CUDA(cudaMemcpyAsync(h_status.ptr, d_status.ptr, 64, cudaMemcpyDeviceToHost, stream));
+  RRG_CUDA(cudaEventRecord(done, stream));
+  in_flight = true;
+  out_results = results;
+  out_coefs = coefs;
+  out_n = b->n_cand;
+  out_ncoef = n_coefs;
+  return RRG_OK;
+}
+
+rrg_status rrg_context::wait(int32_t timeout_ms) {
+  if (!in_flight) return RRG_OK;
+  const auto t0 = std::chrono::steady_clock::now();
+  for (;;) {
+    cudaError_t e = cudaEventQuery(done);
+    if (e == cudaSuccess) break;
+    if (e != cudaErrorNotReady) {
+      in_flight = false;
+      cuda_ok(e, "round execution");
+      return RRG_E_CUDA;
+    }
+    if (timeout_ms >= 0 &&
+        std::chrono::steady_clock::now() - t0 > std::chrono::milliseconds(timeout_ms)) {
+      rrc::set_error("rrg_round_wait: timed out");
+      return RRG_E_TIMEOUT;
+    }
+    std::this_thread::yield();
+  }
+  in_flight = false;
+  const uint32_t dev_status = *static_cast<uint32_t*>(h_status.ptr);
+  if (dev_status != 0) {
+    char msg[128];
+    std::snprintf(msg, sizeof msg, "device reported error status 0x%x", dev_status);
+    rrc::set_error(msg);
+    return RRG_E_DEVICE_FAULT;
+  }
+  for (int i = 0; i < P_COUNT; ++i) {
+    phase_ms[i] = 0;
+    phase_launches[i] = 0;
+  }
+  for (auto& mk : marks) {
+    float ms = 0;
+    if (cudaEventElapsedTime(&ms, mk.second.first, mk.second.second) == cudaSuccess) {
+      phase_ms[mk.first] += ms;
+      phase_launches[mk.first] += 1;
+    }
+  }
+  if (out_results) std::memcpy(out_results, h_res.ptr, sizeof(rrg_result) * out_n);
+  if (out_coefs && out_ncoef > 0) std::memcpy(out_coefs, h_coefs.ptr, sizeof(double) * out_ncoef);
+  last_launches = launches;
+  return RRG_OK;
+}
+
+rrg_context::~rrg_context() {
+  if (in_flight) cudaEventSynchronize(done);
+  d_batch.release();
+  d_A.release();
+  d_S.release();
+  d_pc.release();
+  d_partial.release();
+  d_res.release();
+  d_coefs.release();
+  d_status.release();
+  d_list.release();
+  d_gram.release();
+  d_terms.release();
+  d_mlist.release();
+  d_fallback.release();
+  d_sse1.release();
+  h_mlist.release();
+  h_fallback.release();
+  mixed_scratch.release();
+  h_batch.release();
+  h_res.release();
+  h_coefs.release();
+  h_status.release();
+  h_pc.release();
+  for (cudaEvent_t e : event_pool) cudaEventDestroy(e);
+  if (done) cudaEventDestroy(done);
+  if (stream) cudaStreamDestroy(stream);
+}
+
+DevData rrg_dataset::view() const {
+  DevData v;
+  v.X64 = X64;
+  v.X32 = X32;
+  v.y64 = y64;
+  v.y32 = y32;
+  v.y32lo = y32lo;
+  v.ysum = ysum;
+  v.yy = yy;
+  v.n = n;
+  v.n_pad = n_pad;
+  v.d = d;
+  v.ymean = ymean;
+  v.sst = sst;
+  return v;
+}
+
+// ------------------------------------------------------------------ ABI ----
+extern "C" {
+
+rrg_status rrg_context_create(int32_t device, rrg_context** out) {
+  if (!out) return RRG_E_INVALID;
+  *out = nullptr;
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count <= device || device < 0) {
+    cudaGetLastError();
+    rrc::set_error("no CUDA device available for the GB300 fitness path");
+    return RRG_E_NO_DEVICE;
+  }
+  RRG_CUDA(cudaSetDevice(device));
+  cudaDeviceProp prop;
+  RRG_CUDA(cudaGetDeviceProperties(&prop, device));
+  if (prop.major < 10) {
+    rrc::set_error("the GB300 fitness path needs a Blackwell (sm_10x) device");
+    return RRG_E_NO_DEVICE;
+  }
+  rrg_context* ctx = new rrg_context();
+  ctx->device = device;
+  ctx->sm_count = prop.multiProcessorCount;
+  size_t free_b = 0, total_b = 0;
+  cudaMemGetInfo(&free_b, &total_b);
+  ctx->scratch_budget_bytes = std::min<size_t>((size_t)8 << 30, free_b / 4);
+  if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&ctx->done, cudaEventDisableTiming) != cudaSuccess) {
+    cuda_ok(cudaGetLastError(), "stream creation");
+    delete ctx;
+    return RRG_E_CUDA;
+  }
+  if (cudaFuncSetAttribute(plain_eval_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)plain_eval_smem()) !=
+          cudaSuccess ||
+      !rrd::mixed_allow_smem()) {
+    cuda_ok(cudaGetLastError(), "kernel attributes");
+    delete ctx;
+    return RRG_E_CUDA;
+  }
+  *out = ctx;
+  return RRG_OK;
+}
+
+rrg_status rrg_context_destroy(rrg_context* ctx) {
+  if (!ctx) return RRG_E_INVALID;
+  cudaSetDevice(ctx->device);
+  delete ctx;
+  return RRG_OK;
+}
+
+rrg_status rrg_dataset_create(rrg_context* ctx, const double* X_col, const double* y, int64_t n, int32_t d,
+                              rrg_dataset** out) {
+  if (!ctx || !out || !y || n <= 0 || d < 0 || (d > 0 && !X_col) || n > (int64_t)1 << 40) {
+    rrc::set_error("rrg_dataset_create: invalid arguments");
+    return RRG_E_INVALID;
+  }
+  *out = nullptr;
+  RRG_CUDA(cudaSetDevice(ctx->device));
+  rrg_dataset* ds = new rrg_dataset();
+  ds->ctx = ctx;
+  ds->n = n;
+  ds->d = d;
+  ds->n_pad = round_up(n, 256);
+  const int64_t cols = std::max(d, 1);
+  // sequential FP64 mean and total sum of squares (rils_rols_cpp.cpp:41-43)
+  double s = 0.0;
+  for (int64_t i = 0; i < n; ++i) s += y[i];
+  ds->ysum = s;
+  ds->ymean = s / (double)n;
+  double sst = 0.0;
+  for (int64_t i = 0; i < n; ++i) sst += (y[i] - ds->ymean) * (y[i] - ds->ymean);
+  ds->sst = sst;
+  double yy = 0.0;
+  for (int64_t i = 0; i < n; ++i) yy += y[i] * y[i];
+  ds->yy = yy;
+  const size_t b64 = sizeof(double) * ds->n_pad * cols, b32 = sizeof(float) * ds->n_pad * cols;
+  const size_t y64b = sizeof(double) * ds->n_pad, y32b = sizeof(float) * ds->n_pad;
+  if (cudaMalloc(&ds->X64, b64) != cudaSuccess || cudaMalloc(&ds->X32, b32) != cudaSuccess ||
+      cudaMalloc(&ds->y64, y64b) != cudaSuccess || cudaMalloc(&ds->y32, y32b) != cudaSuccess ||
+      cudaMalloc(&ds->y32lo, y32b) != cudaSuccess) {
+    cudaGetLastError();
+    rrg_dataset_destroy(ds);
+    rrc::set_error("rrg_dataset_create: out of device memory");
+    return RRG_E_OOM;
+  }
+  // pinned staging of the padded columns; FP32 copies are converted on the device
+  HostBuf stage;
+  if (!stage.reserve(b64 + y64b)) {
+    rrg_dataset_destroy(ds);
+    rrc::set_error("rrg_dataset_create: cannot pin staging memory");
+    return RRG_E_OOM;
+  }
+  double* hx = static_cast<double*>(stage.ptr);
+  std::memset(hx, 0, b64 + y64b);
+  for (int64_t j = 0; j < d; ++j) std::memcpy(hx + j * ds->n_pad, X_col + j * n, sizeof(double) * n);
+  std::memcpy(hx + cols * ds->n_pad, y, sizeof(double) * n);
+  cudaStream_t st = ctx->stream;
+  bool ok = cudaMemcpyAsync(ds->X64, hx, b64, cudaMemcpyHostToDevice, st) == cudaSuccess &&
+            cudaMemcpyAsync(ds->y64, hx + cols * ds->n_pad, y64b, cudaMemcpyHostToDevice, st) == cudaSuccess;
+  if (ok)
+    ok = launch_to_f32(ds->X64, ds->X32, ds->n_pad * cols, st) &&
+         launch_split_f32(ds->y64, ds->y32, ds->y32lo, ds->n_pad, st);
+  ok = ok && cudaStreamSynchronize(st) == cudaSuccess;
+  stage.release();
+  if (!ok) {
+    cuda_ok(cudaGetLastError(), "dataset upload");
+    rrg_dataset_destroy(ds);
+    return RRG_E_CUDA;
+  }
+  *out = ds;
+  return RRG_OK;
+}
+
+rrg_status rrg_dataset_destroy(rrg_dataset* ds) {
+  if (!ds) return RRG_E_INVALID;
+  if (ds->ctx) cudaSetDevice(ds->ctx->device);
+  if (ds->ctx && ds->ctx->in_flight) cudaEventSynchronize(ds->ctx->done);
+  if (ds->X64) cudaFree(ds->X64);
+  if (ds->X32) cudaFree(ds->X32);
+  if (ds->y64) cudaFree(ds->y64);
+  if (ds->y32) cudaFree(ds->y32);
+  if (ds->y32lo) cudaFree(ds->y32lo);
+  delete ds;
+  return RRG_OK;
+}
+
+rrg_status rrg_round_submit(rrg_dataset* ds, const rrg_batch* batch, int32_t precision, rrg_result* results,
+                            double* coefs) {
+  if (!ds || !batch || (!results && batch->n_cand > 0)) return RRG_E_INVALID;
+  return ds->ctx->submit(ds, batch, precision, results, coefs);
+}
+
+rrg_status rrg_round_wait(rrg_context* ctx, int32_t timeout_ms) {
+  if (!ctx) return RRG_E_INVALID;
+  return ctx->wait(timeout_ms);
+}
+
+rrg_status rrg_eval(rrg_dataset* ds, const rrg_batch* batch, int32_t precision, rrg_result* results, double* coefs) {
+  rrg_status st = rrg_round_submit(ds, batch, precision, results, coefs);
+  if (st != RRG_OK) return st;
+  return ds->ctx->wait(-1);
+}
+
+rrg_status rrg_predict(rrg_dataset* ds, const rrg_batch* batch, double* values) {
+  if (!ds || !batch || !values || batch->n_cand < 1) return RRG_E_INVALID;
+  rrg_context* ctx = ds->ctx;
+  if (ctx->in_flight) return RRG_E_INVALID;
+  int64_t n_coefs = 0;
+  rrg_batch one = *batch;
+  one.n_cand = 1;
+  rrg_status st = validate(&one, ds->d, &n_coefs);
+  if (st != RRG_OK || one.cands[0].mode != RRG_UNTUNED) {
+    rrc::set_error("rrg_predict: candidate 0 must be a valid untuned program");
+    return RRG_E_INVALID;
+  }
+  RRG_CUDA(cudaSetDevice(ctx->device));
+  st = ctx->stage_batch(&one);
+  if (st != RRG_OK) return st;
+  if (!ctx->d_status.reserve(64) || !ctx->h_status.reserve(64)) return RRG_E_OOM;
+  RRG_CUDA(cudaMemsetAsync(ctx->d_status.ptr, 0, 64, ctx->stream));
+  st = ctx->run_plain(ds, 0, 1, true, nullptr, 0u);
+  if (st != RRG_OK) return st;
+  RRG_CUDA(cudaMemcpyAsync(ctx->h_status.ptr, ctx->d_status.ptr, 64, cudaMemcpyDeviceToHost, ctx->stream));
+  RRG_CUDA(cudaMemcpyAsync(values, ctx->d_A.ptr, sizeof(double) * ds->n, cudaMemcpyDeviceToHost, ctx->stream));
+  RRG_CUDA(cudaStreamSynchronize(ctx->stream));
+  if (*static_cast<uint32_t*>(ctx->h_status.ptr) != 0) {
+    rrc::set_error("rrg_predict: device reported an error status");
+    return RRG_E_DEVICE_FAULT;
+  }
+  return RRG_OK;
+}
+
+rrg_status rrg_batch_validate(const rrg_batch* batch, int32_t d) {
+  int64_t n_coefs = 0;
+  rrg_status st = validate(batch, d, &n_coefs);
+  if (st != RRG_OK) rrc::set_error("rrg_batch_validate: malformed or oversized batch");
+  return st;
+}
+
+int64_t rrg_dataset_rows(const rrg_dataset* ds) { return ds ? ds->n : -1; }
+int32_t rrg_dataset_cols(const rrg_dataset* ds) { return ds ? ds->d : -1; }
+int64_t rrg_last_round_launches(const rrg_context* ctx) { return ctx ? ctx->last_launches : -1; }
+
+int32_t rrg_last_round_stats(const rrg_context* ctx, int64_t* out, int32_t n) {
+  if (!ctx || !out || n <= 0) return 0;
+  const int64_t v[4] = {ctx->last_launches, ctx->last_plain_routed, ctx->last_fallback, ctx->last_pass2};
+  const int32_t k = n < 4 ? n : 4;
+  for (int32_t i = 0; i < k; ++i) out[i] = v[i];
+  return k;
+}
+
+void* rrg_context_stream(const rrg_context* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+
+rrg_status rrg_context_set_timing(rrg_context* ctx, int32_t on) {
+  if (!ctx) return RRG_E_INVALID;
+  ctx->timing = on != 0;
+  return RRG_OK;
+}
+
+int32_t rrg_last_round_timing(const rrg_context* ctx, double* ms, int64_t* launches, int32_t n) {
+  if (!ctx || !ms || n <= 0) return 0;
+  const int32_t k = n < (int32_t)rrg_context::P_COUNT ? n : (int32_t)rrg_context::P_COUNT;
+  for (int32_t i = 0; i < k; ++i) {
+    ms[i] = ctx->phase_ms[i];
+    if (launches) launches[i] = ctx->phase_launches[i];
+  }
+  return k;
+}
+
+}  // extern "C"

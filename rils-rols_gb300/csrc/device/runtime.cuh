@@ -1,0 +1,87 @@
+// Context and dataset objects behind the C ABI (runtime.cu).
+#pragma once
+#include <cstdint>
+#include <vector>
+
+#include "common.cuh"
+
+// Device allocation that only grows.
+struct DevBuf {
+  void* ptr = nullptr;
+  size_t cap = 0;
+  bool reserve(size_t bytes);
+  void release();
+};
+// Pinned host allocation that only grows.
+struct HostBuf {
+  void* ptr = nullptr;
+  size_t cap = 0;
+  bool reserve(size_t bytes);
+  void release();
+};
+
+struct rrg_dataset {
+  rrg_context* ctx = nullptr;
+  int64_t n = 0, n_pad = 0;
+  int32_t d = 0;
+  double* X64 = nullptr;
+  float* X32 = nullptr;
+  double* y64 = nullptr;
+  float* y32 = nullptr;
+  float* y32lo = nullptr;
+  double ymean = 0, sst = 0, ysum = 0, yy = 0;
+  rrd::DevData view() const;
+};
+
+struct rrg_context {
+  int device = 0;
+  int sm_count = 0;
+  size_t scratch_budget_bytes = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t done = nullptr;
+  // batch staging
+  HostBuf h_batch;
+  DevBuf d_batch;
+  size_t off_c = 0, off_f = 0, off_k = 0, off_d = 0, off_s = 0, batch_bytes = 0;
+  rrd::DevBatch dev{};
+  std::vector<rrg_cand> host_cands;
+  // plain scratch
+  DevBuf d_A, d_S, d_pc, d_partial, d_list;
+  HostBuf h_pc, h_list;
+  // mixed scratch
+  DevBuf d_gram, d_terms, d_mlist, d_fallback, d_sse1;
+  HostBuf h_mlist, h_fallback;
+  DevBuf mixed_scratch;
+  // results
+  DevBuf d_res, d_coefs, d_status;
+  HostBuf h_res, h_coefs, h_status;
+  // round in flight
+  bool in_flight = false;
+  rrg_result* out_results = nullptr;
+  double* out_coefs = nullptr;
+  int32_t out_n = 0;
+  int64_t out_ncoef = 0;
+  int64_t launches = 0, last_launches = 0;
+  // mixed-round statistics of the last round
+  int64_t last_fallback = 0, last_plain_routed = 0, last_pass2 = 0;
+  int32_t mixed_tile_override = 0;
+  // optional per-phase device timing (CUDA events on the context stream)
+  bool timing = false;
+  enum Phase { P_GRAM = 0, P_SOLVE, P_RESID, P_FINAL, P_PLAIN_EVAL, P_PLAIN_QR, P_PLAIN_RESID, P_COUNT };
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> marks;
+  std::vector<cudaEvent_t> event_pool;
+  size_t event_next = 0;
+  double phase_ms[P_COUNT] = {0};
+  int64_t phase_launches[P_COUNT] = {0};
+  cudaEvent_t mark_begin();
+  void mark_end(int phase, cudaEvent_t begin);
+
+  rrg_status stage_batch(const rrg_batch* b);
+  // plain FP64 over `list` (absolute candidate indices) or over [lo, hi) when list is empty
+  rrg_status run_plain(const rrg_dataset* ds, int32_t lo, int32_t hi, bool predict_only,
+                       const std::vector<int32_t>* list = nullptr, uint32_t flags_or = 0);
+  rrg_status run_mixed(const rrg_dataset* ds, int32_t n_cand);
+  rrg_status submit(rrg_dataset* ds, const rrg_batch* b, int32_t precision, rrg_result* results, double* coefs);
+  rrg_status wait(int32_t timeout_ms);
+  ~rrg_context();
+};

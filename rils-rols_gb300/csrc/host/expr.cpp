@@ -2,6 +2,7 @@
 #include "expr.h"
 
 #include <climits>
+#include <limits>
 #include <cmath>
 #include <cstdio>
 #include <sstream>
@@ -91,7 +92,7 @@ void append_const(double v, std::string& o) {
   if (std::fabs(std::round(v) - v) < kEpsRt) {
     o += std::to_string(x86_int(std::round(v)));
   } else if (std::isnan(v)) {
-    o += "-nan";  // the x86 default NaN carries the sign bit
+    o += std::signbit(v) ? "-nan" : "nan";  // glibc's %f spelling of a NaN
   } else {
     char buf[512];
     std::snprintf(buf, sizeof buf, "%f", v);
@@ -311,7 +312,7 @@ void expand(Node* t, Arena& a) {
 }
 
 namespace {
-double fold(uint8_t type, double a, double b) {
+double fold_raw(uint8_t type, double a, double b) {
   switch (type) {
     case PLUS: return a + b;
     case MINUS: return a - b;
@@ -326,6 +327,13 @@ double fold(uint8_t type, double a, double b) {
     case MAX: return a > b ? a : b;
     default: throw std::runtime_error("Simplification is not supported for this binary operator!");
   }
+}
+// A NaN made by an invalid operation on non-NaN operands gets the sign of the
+// x86-64 default NaN, so that folded constants print alike on every host.
+double fold(uint8_t type, double a, double b) {
+  const double r = fold_raw(type, a, b);
+  if (std::isnan(r) && !std::isnan(a) && !std::isnan(b)) return -std::numeric_limits<double>::quiet_NaN();
+  return r;
 }
 }  // namespace
 

@@ -1,0 +1,195 @@
+"""Python view of the batched fitness C ABI (include/rils_rols_gb300.h).
+
+    ctx = Context()                       # one CUDA stream + scratch on device 0
+    ds = ctx.dataset(X, y)                # X: n x d (row-major) float64, resident in HBM
+    batch = encode(trees, tuned=True)     # trees in prefix form, e.g. "add x0 mul c:2 sin x1"
+    out = ds.evaluate(batch, precision=MIXED)
+
+`out` holds per-candidate loss (1 - R2), rmse, size, rank, flags and the
+fitted coefficients (free term last), exactly what the reference's
+tune_constants + fitness return per candidate (rils_rols_cpp.cpp:445-541).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib
+from ._lib import RRG_MIXED, RRG_PLAIN_FP64, RRG_TUNED, RRG_UNTUNED, Batch, Cand, Factor, Result, check
+
+PLAIN = RRG_PLAIN_FP64
+MIXED = RRG_MIXED
+
+
+@dataclass
+class EncodedBatch:
+    """An rrg_batch whose arrays are owned by numpy."""
+    cands: np.ndarray
+    factors: np.ndarray
+    code: np.ndarray
+    consts: np.ndarray
+    n_coefs: int
+
+    def __len__(self) -> int:
+        return len(self.cands)
+
+    def struct(self) -> Batch:
+        b = Batch()
+        b.n_cand = len(self.cands)
+        b.n_factors = len(self.factors)
+        b.n_code = len(self.code)
+        b.n_consts = len(self.consts)
+        b.cands = self.cands.ctypes.data_as(C.POINTER(Cand))
+        b.factors = self.factors.ctypes.data_as(C.POINTER(Factor))
+        b.code = self.code.ctypes.data_as(C.POINTER(C.c_uint32))
+        b.consts = self.consts.ctypes.data_as(C.POINTER(C.c_double))
+        return b
+
+
+_CAND_DT = np.dtype([(n, np.int32) for n, _ in Cand._fields_])
+_FACT_DT = np.dtype([(n, np.int32) for n, _ in Factor._fields_])
+_RES_DT = np.dtype([("loss", np.float64), ("rmse", np.float64), ("size", np.int32), ("rank", np.int32),
+                    ("flags", np.uint32), ("n_coef", np.int32)])
+
+
+def encode(trees: list[str], tuned: bool = True) -> EncodedBatch:
+    """Flatten prefix-form trees into postfix programs (host library, rrh_encode).
+
+    tuned=True splits each tree into its top-level factors as tune_constants
+    does (rils_rols_cpp.cpp:448-475); tuned=False scores the tree as given.
+    """
+    lib = _lib.load()
+    b = Batch()
+    text = "\n".join(trees).encode()
+    check(lib.rrh_encode(text, RRG_TUNED if tuned else RRG_UNTUNED, C.byref(b)), "rrh_encode")
+    def arr(ptr, n, dt):
+        if n == 0:
+            return np.zeros(0, dtype=dt)
+        raw = np.ctypeslib.as_array(C.cast(ptr, C.POINTER(C.c_byte)), shape=(n * np.dtype(dt).itemsize,))
+        return raw.view(dt).copy()
+    cands = arr(b.cands, b.n_cand, _CAND_DT)
+    factors = arr(b.factors, b.n_factors, _FACT_DT)
+    code = arr(b.code, b.n_code, np.uint32)
+    consts = arr(b.consts, b.n_consts, np.float64)
+    n_coefs = int(np.max(cands["coef_offset"] + cands["n_factors"] + 1)) if tuned and len(cands) else 0
+    return EncodedBatch(cands, factors, code, consts, n_coefs)
+
+
+def decode_results(res: np.ndarray, coefs: np.ndarray, batch: EncodedBatch) -> dict:
+    out = {k: res[k].copy() for k in ("loss", "rmse", "size", "rank", "flags")}
+    cl = []
+    for c in batch.cands:
+        if c["mode"] == RRG_TUNED:
+            cl.append(coefs[c["coef_offset"]:c["coef_offset"] + c["n_factors"] + 1].copy())
+        else:
+            cl.append(np.zeros(0))
+    out["coefs"] = cl
+    return out
+
+
+class Context:
+    """rrg_context on one device (default 0)."""
+
+    def __init__(self, device: int = 0):
+        self.lib = _lib.load()
+        h = C.c_void_p()
+        check(self.lib.rrg_context_create(device, C.byref(h)), "rrg_context_create")
+        self.h = h
+
+    def dataset(self, X: np.ndarray, y: np.ndarray) -> "Dataset":
+        return Dataset(self, X, y)
+
+    def last_round_launches(self) -> int:
+        return int(self.lib.rrg_last_round_launches(self.h))
+
+    def last_round_stats(self) -> dict:
+        out = (C.c_int64 * 4)()
+        self.lib.rrg_last_round_stats(self.h, out, 4)
+        return {"launches": out[0], "plain_routed": out[1], "fp64_fallback": out[2], "residual_pass": out[3]}
+
+    PHASES = ("mixed_gram", "mixed_solve", "mixed_residual", "finalize", "fp64_eval", "fp64_qr", "fp64_residual")
+
+    def set_timing(self, on: bool = True) -> None:
+        check(self.lib.rrg_context_set_timing(self.h, int(on)), "rrg_context_set_timing")
+
+    def last_round_timing(self) -> dict:
+        ms = (C.c_double * 7)()
+        cnt = (C.c_int64 * 7)()
+        self.lib.rrg_last_round_timing(self.h, ms, cnt, 7)
+        return {p: (ms[i], cnt[i]) for i, p in enumerate(self.PHASES)}
+
+    def stream(self) -> int:
+        """cudaStream_t of this context, as an integer handle."""
+        return int(self.lib.rrg_context_stream(self.h) or 0)
+
+    def close(self):
+        if self.h:
+            self.lib.rrg_context_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Dataset:
+    """rrg_dataset: X (n x d, any layout) and y made resident on the device."""
+
+    def __init__(self, ctx: Context, X: np.ndarray, y: np.ndarray):
+        self.ctx = ctx
+        X = np.asarray(X, dtype=np.float64)
+        if X.ndim == 1:
+            X = X[:, None]
+        self.n, self.d = X.shape
+        Xcol = np.ascontiguousarray(X.T)
+        yv = np.ascontiguousarray(np.asarray(y, dtype=np.float64).reshape(-1))
+        if len(yv) != self.n:
+            raise ValueError("X and y disagree on the number of rows")
+        h = C.c_void_p()
+        dp = C.POINTER(C.c_double)
+        check(ctx.lib.rrg_dataset_create(ctx.h, Xcol.ctypes.data_as(dp), yv.ctypes.data_as(dp), self.n, self.d,
+                                         C.byref(h)), "rrg_dataset_create")
+        self.h = h
+
+    def evaluate(self, batch: EncodedBatch, precision: int = PLAIN) -> dict:
+        res = np.zeros(len(batch), dtype=_RES_DT)
+        coefs = np.zeros(max(1, batch.n_coefs), dtype=np.float64)
+        b = batch.struct()
+        check(self.ctx.lib.rrg_eval(self.h, C.byref(b), precision, res.ctypes.data_as(C.POINTER(Result)),
+                                    coefs.ctypes.data_as(C.POINTER(C.c_double))), "rrg_eval")
+        return decode_results(res, coefs, batch)
+
+    def submit(self, batch: EncodedBatch, precision: int, res: np.ndarray, coefs: np.ndarray):
+        """Asynchronous round; complete it with wait().  Buffers must stay alive."""
+        b = batch.struct()
+        check(self.ctx.lib.rrg_round_submit(self.h, C.byref(b), precision, res.ctypes.data_as(C.POINTER(Result)),
+                                            coefs.ctypes.data_as(C.POINTER(C.c_double))), "rrg_round_submit")
+
+    def wait(self, timeout_ms: int = -1):
+        check(self.ctx.lib.rrg_round_wait(self.ctx.h, timeout_ms), "rrg_round_wait")
+
+    def predict(self, tree: str) -> np.ndarray:
+        batch = encode([tree], tuned=False)
+        out = np.zeros(self.n, dtype=np.float64)
+        b = batch.struct()
+        check(self.ctx.lib.rrg_predict(self.h, C.byref(b), out.ctypes.data_as(C.POINTER(C.c_double))), "rrg_predict")
+        return out
+
+    def close(self):
+        if self.h:
+            self.ctx.lib.rrg_dataset_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def result_dtype() -> np.dtype:
+    return _RES_DT

@@ -1,0 +1,122 @@
+"""Device fitness path against the oracle and the reference's golden vectors.
+
+Plain FP64: every fitness within 1e-10 relative of the oracle (which is
+bit-exact with the reference), same size, same NaN sentinel.
+Mixed: penalised fitness within the tolerances below of the FP64 oracle.
+"""
+import numpy as np
+import pytest
+
+from oracle import pyoracle
+from rils_rols_gb300 import synth
+from rils_rols_gb300.fitness import MIXED, PLAIN, Context, encode
+
+pytestmark = pytest.mark.gpu
+
+REL_PLAIN = 1e-10
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    c = Context(0)
+    yield c
+    c.close()
+
+
+def rel_err(a, b):
+    a, b = np.asarray(a, dtype=float), np.asarray(b, dtype=float)
+    both_inf = np.isinf(a) & np.isinf(b) & (np.sign(a) == np.sign(b))
+    err = np.abs(a - b) / np.maximum(np.abs(b), 1e-300)
+    err[both_inf] = 0.0
+    err[(a == b)] = 0.0
+    return err
+
+
+def fitness_value(loss, rmse, size, cp=0.001):
+    return (1 + np.asarray(loss)) * (1 + np.asarray(rmse)) * (1 + np.asarray(size) * cp)
+
+
+def check_plain(dev, ora, tag):
+    assert np.array_equal(dev["size"], ora["size"]), tag
+    sent_d, sent_o = dev["loss"] == 1000, ora["loss"] == 1000
+    assert np.array_equal(sent_d, sent_o), tag
+    ok = ~sent_o
+    # 1 - R2 is compared through R2 itself (1 - R2 == 0 for exact fits)
+    assert np.all(rel_err(1 - dev["loss"][ok], 1 - ora["loss"][ok]) <= REL_PLAIN), tag
+    assert np.all(rel_err(dev["rmse"][ok], ora["rmse"][ok]) <= REL_PLAIN + 1e-300), tag
+
+
+@pytest.mark.parametrize("name", ["toy", "rand257x3", "cls120x4", "tiny3x2"])
+def test_plain_matches_golden(ctx, golden, name):
+    spec = golden("fitness")[name]
+    X, y = np.array(spec["X"]), np.array(spec["y"])
+    ds = ctx.dataset(X, y)
+    ods = pyoracle.OracleDataset(X, y)
+    trees = [c["tree"] for c in spec["cases"]]
+    for tuned in (True, False):
+        b = encode(trees, tuned=tuned)
+        dev, ora = ds.evaluate(b, PLAIN), ods.evaluate(b)
+        check_plain(dev, ora, (name, tuned))
+        key = "tuned" if tuned else "untuned"
+        gold = np.array([c[key]["fit"][2] for c in spec["cases"]])
+        assert np.array_equal(dev["size"], gold)
+
+
+def test_plain_tall_tsqr_matches_oracle(ctx):
+    # n >= 65536 with few candidates takes the tiled (TSQR) path
+    X, y, trees, _ = synth.batched_fitness(n=100_000, d=5, n_trees=24, seed=3, max_size=25)
+    ds = ctx.dataset(X, y)
+    ods = pyoracle.OracleDataset(X, y)
+    b = encode(trees, tuned=True)
+    check_plain(ds.evaluate(b, PLAIN), ods.evaluate(b, threads=8), "tsqr")
+
+
+def test_plain_batched_medium_matches_oracle(ctx):
+    X, y, trees, _ = synth.batched_fitness(n=3000, d=4, n_trees=400, seed=5, max_size=40)
+    ds = ctx.dataset(X, y)
+    ods = pyoracle.OracleDataset(X, y)
+    for tuned in (True, False):
+        b = encode(trees, tuned=tuned)
+        check_plain(ds.evaluate(b, PLAIN), ods.evaluate(b, threads=8), ("medium", tuned))
+
+
+def test_predict_matches_oracle(ctx):
+    X, y, trees, _ = synth.batched_fitness(n=5000, d=3, n_trees=20, seed=9)
+    ds = ctx.dataset(X, y)
+    ods = pyoracle.OracleDataset(X, y)
+    for t in trees:
+        got = ds.predict(t)
+        want = ods.predict(encode([t], tuned=False))
+        fin = np.isfinite(want)
+        assert np.array_equal(np.isfinite(got), fin)
+        assert np.all(rel_err(got[fin], want[fin]) <= 1e-12)
+
+
+def test_mixed_close_to_fp64_oracle(ctx):
+    X, y, trees, _ = synth.batched_fitness(n=20_000, d=6, n_trees=600, seed=13)
+    ds = ctx.dataset(X, y)
+    ods = pyoracle.OracleDataset(X, y)
+    b = encode(trees, tuned=True)
+    mix, ora = ds.evaluate(b, MIXED), ods.evaluate(b, threads=8)
+    assert np.array_equal(mix["loss"] == 1000, ora["loss"] == 1000)
+    ok = (ora["loss"] != 1000) & np.isfinite(ora["loss"]) & np.isfinite(ora["rmse"])
+    fv_m = fitness_value(mix["loss"], mix["rmse"], mix["size"])[ok]
+    fv_o = fitness_value(ora["loss"], ora["rmse"], ora["size"])[ok]
+    err = rel_err(fv_m, fv_o)
+    assert np.median(err) <= 1e-6
+    assert np.mean(err <= 1e-6) >= 0.95
+    # the best candidate is the same
+    assert np.argmin(np.where(ok, fitness_value(mix["loss"], mix["rmse"], mix["size"]), np.inf)) == \
+        np.argmin(np.where(ok, fitness_value(ora["loss"], ora["rmse"], ora["size"]), np.inf))
+
+
+def test_round_is_deterministic_and_mix_independent(ctx):
+    # the same candidate scores bit-identically alone and inside a larger batch
+    X, y, trees, _ = synth.batched_fitness(n=8192, d=4, n_trees=300, seed=21)
+    ds = ctx.dataset(X, y)
+    for prec in (PLAIN, MIXED):
+        full = ds.evaluate(encode(trees, tuned=True), prec)
+        for i in (0, 17, 299):
+            one = ds.evaluate(encode([trees[i]], tuned=True), prec)
+            assert one["loss"][0] == full["loss"][i] or (np.isnan(one["loss"][0]) and np.isnan(full["loss"][i]))
+            assert one["rmse"][0] == full["rmse"][i] or (np.isnan(one["rmse"][0]) and np.isnan(full["rmse"][i]))
