@@ -3,12 +3,15 @@
 Metric: candidate fitness evaluations per second (tune_constants + fitness of
 rils_rols_cpp.cpp:445-541 per candidate) at n = 1M rows.
 
-Workload (one step): one batched round of the mixed-precision path over
-B = 8192 candidate trees drawn like the standalone batched-fitness
-configuration (sizes uniform 3..50 nodes over + - * / sin cos ln exp sqrt,
-leaves x_j or U(-5, 5) constants), scored on the 1M-row, 5-feature regression
-dataset (X ~ U(-3, 3), y = 2.5 x1 x2 - sin(x3)/(1+x4^2) + 0.7 exp(0.3 x5) +
-0.5% noise).  Synthetic, seeded data; nothing is downloaded.
+Workload (one step): the local-search rounds of a search on the 1M-row,
+5-feature regression problem (X ~ U(-3, 3), y = 2.5 x1 x2 - sin(x3)/(1+x4^2) +
+0.7 exp(0.3 x5) + 0.5% noise): every local-search candidate (all_candidates,
+rils_rols_cpp.cpp:348-443) of the eight intermediate models in
+synth.REGRESSION_1M_TRAJECTORY, 7083 tuned candidates, scored in one batched
+round of the mixed-precision path.  Synthetic, seeded data; nothing is
+downloaded.  The same numbers are reported for 8192 random trees drawn like
+the standalone batched-fitness configuration (sizes 3..50 over
++ - * / sin cos ln exp sqrt, leaves x_j or U(-5, 5)).
 
   value  device-resident: dataset in HBM, each step = one rrg_eval round
          (batch upload, kernels, result download), timed with CUDA events on
@@ -41,7 +44,7 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT / "rils-rols_gb300"))
 sys.path.insert(0, str(ROOT))
 
-METRIC = "candidate fitness evals/s at n=1M (mixed precision, batched round)"
+METRIC = "candidate fitness evals/s at n=1M (mixed precision, batched local-search round)"
 UNIT = "evals/s"
 N_ROWS = 1_000_000
 N_FEAT = 5
@@ -50,17 +53,21 @@ SEED = 12345
 
 
 def workload(n=N_ROWS, batch=BATCH, seed=SEED):
+    """(X, y, local-search candidates, random trees)"""
     from rils_rols_gb300 import synth
     X, y = synth.regression_1m(n=n, seed=seed)
+    ls = synth.ls_round_batch(d=N_FEAT)
     rng = np.random.default_rng(seed + 1)
-    trees = [synth.random_tree(rng, int(rng.integers(3, 51)), N_FEAT) for _ in range(batch)]
-    return X, y, trees
+    rand = [synth.random_tree(rng, int(rng.integers(3, 51)), N_FEAT) for _ in range(batch)]
+    return X, y, ls, rand
 
 
 def config(n, batch):
-    return {"workload": f"batched tuned fitness: {batch} random trees (3-50 nodes) x n={n} rows, d={N_FEAT}",
-            "n_rows": n, "n_features": N_FEAT, "batch": batch, "tree_sizes": "U{3..50}",
-            "operators": "+ - * / sin cos ln exp sqrt", "precision": "FP32 eval, FP64 solve / SSE",
+    return {"workload": f"local-search rounds of the 1M-row regression search: {batch} tuned candidates "
+                        f"x n={n} rows, d={N_FEAT}",
+            "n_rows": n, "n_features": N_FEAT, "batch": batch,
+            "candidates": "all_candidates(model, local_search) of 8 models on the way to the generating formula",
+            "precision": "RRG_MIXED: FP32 eval, exact-product Gram sums, FP64 Cholesky / SSE",
             "l2": "flushed (256 MB write on the round's stream) before every timed step"}
 
 
@@ -174,21 +181,55 @@ def aggregate(units_per_rank: float, seconds: float, world: int) -> tuple[float,
 
 
 # ------------------------------------------------------------------- ours --
+def timed_round(ctx, ds, batch, prec, stream, flush):
+    import torch
+    with torch.cuda.stream(stream):
+        flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+    out = ds.evaluate(batch, prec)
+    with torch.cuda.stream(stream):
+        e1.record(stream)
+    e1.synchronize()
+    return e0.elapsed_time(e1) / 1e3, out
+
+
+def fv(r):
+    return (1 + r["loss"]) * (1 + r["rmse"]) * (1 + r["size"] * 1e-3)
+
+
+def accuracy(test, ref):
+    ok = (ref["loss"] != 1000) & np.isfinite(fv(ref))
+    with np.errstate(all="ignore"):
+        err = np.abs(fv(test)[ok] - fv(ref)[ok]) / fv(ref)[ok]
+    err = np.where(np.isfinite(err), err, np.inf)
+    best = lambda r: int(np.argmin(np.where(ok, fv(r), np.inf)))  # noqa: E731
+    top = lambda r: set(np.argsort(np.where(ok, fv(r), np.inf))[:100].tolist())  # noqa: E731
+    return {"candidates_compared": int(ok.sum()),
+            "sentinel_agreement": float(np.mean((test["loss"] == 1000) == (ref["loss"] == 1000))),
+            "size_agreement": float(np.mean(test["size"] == ref["size"])),
+            "fitness_rel_err_median": float(np.median(err)), "fitness_rel_err_p99": float(np.quantile(err, 0.99)),
+            "fitness_rel_err_max": float(err.max()), "frac_within_1e-6": float(np.mean(err <= 1e-6)),
+            "argbest_same": best(test) == best(ref), "top100_overlap": len(top(test) & top(ref)) / 100.0}
+
+
 def run_ours(args):
     import torch
 
-    from rils_rols_gb300.fitness import MIXED, PLAIN, Context, encode
+    from rils_rols_gb300.fitness import CERTIFIED, MIXED, PLAIN, Context, encode
 
     rank, world = dist_setup()
     local = int(os.environ.get("LOCAL_RANK", "0"))
-    X, y, trees = workload(args.n, args.batch)
+    X, y, ls_trees, rand_trees = workload(args.n, args.batch)
+    trees = ls_trees
+    B = len(trees)
     ctx = Context(local)
     ds = ctx.dataset(X, y)
     batch = encode(trees, tuned=True)
     stream = torch.cuda.ExternalStream(ctx.stream(), device=torch.device("cuda", local))
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=torch.device("cuda", local))
 
-    # warm-up (also checks the path end to end)
     for _ in range(args.warmup):
         ds.evaluate(batch, MIXED)
     ctx.set_timing(True)
@@ -199,16 +240,8 @@ def run_ours(args):
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
         for _ in range(args.steps):
-            with torch.cuda.stream(stream):
-                flush.zero_()
-                e0 = torch.cuda.Event(enable_timing=True)
-                e1 = torch.cuda.Event(enable_timing=True)
-                e0.record(stream)
-            out = ds.evaluate(batch, MIXED)
-            with torch.cuda.stream(stream):
-                e1.record(stream)
-            e1.synchronize()
-            times.append(e0.elapsed_time(e1) / 1e3)
+            dt, out = timed_round(ctx, ds, batch, MIXED, stream, flush)
+            times.append(dt)
             launches += ctx.last_round_launches()
             for k, (ms, cnt) in ctx.last_round_timing().items():
                 phase_ms[k] = phase_ms.get(k, 0.0) + ms
@@ -217,7 +250,7 @@ def run_ours(args):
     barrier(world)
     stats = ctx.last_round_stats()
     ctx.set_timing(False)
-    value, t_max = aggregate(args.batch * args.steps, sum(times), world)
+    value, t_max = aggregate(B * args.steps, sum(times), world)
 
     # e2e: trees in, fitness out, through the C ABI from host buffers
     Xp = torch.from_numpy(np.ascontiguousarray(X)).pin_memory().numpy()
@@ -228,24 +261,23 @@ def run_ours(args):
         t = time.perf_counter()
         b = encode(trees, tuned=True)
         d2 = ctx.dataset(Xp, yp)
-        r = d2.evaluate(b, MIXED)
+        d2.evaluate(b, MIXED)
         d2.close()
         torch.cuda.synchronize()
         if step >= args.warmup:
             e2e_times.append(time.perf_counter() - t)
-    e2e_value, _ = aggregate(args.batch * args.steps, sum(e2e_times), world)
+    e2e_value, _ = aggregate(B * args.steps, sum(e2e_times), world)
     h2d = X.nbytes + y.nbytes + batch.cands.nbytes + batch.factors.nbytes + batch.code.nbytes + batch.consts.nbytes
-    d2h = args.batch * 32 + batch.n_coefs * 8
+    d2h = B * 32 + batch.n_coefs * 8
 
     if rank != 0:
         return
     res = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f32/f64", "data": "synthetic (seeded)",
-           "config": config(args.n, args.batch),
+           "config": config(args.n, B),
            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
            "gpu_launches": int(launches), "round_stats": stats}
-    # dominant kernel: the mixed gram pass
     gram_ms, gram_n = phase_ms.get("mixed_gram", 0.0), max(1, phase_n.get("mixed_gram", 1))
     avg_launch_s = gram_ms / 1e3 / gram_n
     algo_bytes = args.n * (N_FEAT + 1) * 4  # X (FP32) and y read once per launch
@@ -255,53 +287,44 @@ def run_ours(args):
     res["roofline"] = {"kernel": "mixed_pass_kernel (gram pass)", "bound": "hbm", "achieved": achieved,
                        "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                        "traffic": read_profile_traffic(), "peak_source": "measured" if peaks else "fallback",
-                       "note": "issue-bound interpreter: the HBM roofline is far away; see DESIGN.md"}
+                       "note": "issue-bound interpreter (FP32/SFU): the HBM roofline is far away; see DESIGN.md"}
     res["phase_ms_per_step"] = {k: v / args.steps for k, v in phase_ms.items() if v > 0}
     res["clocks"] = clk.summary()
-    if not args.quick:
-        res.update(compare_paths(ctx, ds, X, y, trees, batch, out, args))
-        res["mixed_over_plain_unbatched"] = value / world / res["plain_fp64_unbatched_evals_per_s"]
-        res["cpu_baseline"] = cpu_baseline(X, y, trees, args.cpu_sample)
-        res["mixed_over_cpu_baseline"] = value / world / res["cpu_baseline"]["value"]
-    print(json.dumps(res))
-
-
-def compare_paths(ctx, ds, X, y, trees, batch, mixed_out, args):
-    """Plain FP64 path: unbatched launches (one candidate per round) and the
-    whole batch (accuracy reference for the mixed round)."""
-    import torch
-
-    from rils_rols_gb300.fitness import PLAIN, encode
+    if args.quick:
+        print(json.dumps(res))
+        return
+    # certified mixed form: every fitness within 1e-6 of the FP64 path or re-scored in FP64
+    dt_c, cert = timed_round(ctx, ds, batch, CERTIFIED, stream, flush)
+    res["certified"] = {"evals_per_s": B / dt_c, "round_stats": ctx.last_round_stats()}
+    # random-tree batch (standalone batched-fitness generator) at the same n
+    rb = encode(rand_trees, tuned=True)
+    ds.evaluate(rb, MIXED)
+    dt_r, _ = timed_round(ctx, ds, rb, MIXED, stream, flush)
+    rs = ctx.last_round_stats()
+    dt_rc, _ = timed_round(ctx, ds, rb, CERTIFIED, stream, flush)
+    res["random_trees_8192"] = {"mixed_evals_per_s": len(rand_trees) / dt_r, "mixed_round_stats": rs,
+                                "certified_evals_per_s": len(rand_trees) / dt_rc,
+                                "certified_round_stats": ctx.last_round_stats()}
+    # plain FP64: unbatched launches and the whole batch (accuracy reference)
     singles = [encode([t], tuned=True) for t in trees[:args.unbatched_sample]]
     ds.evaluate(singles[0], PLAIN)
     torch.cuda.synchronize()
     t = time.perf_counter()
-    for s in singles:
-        ds.evaluate(s, PLAIN)
+    for s1 in singles:
+        ds.evaluate(s1, PLAIN)
     torch.cuda.synchronize()
     unbatched = len(singles) / (time.perf_counter() - t)
     t = time.perf_counter()
     plain = ds.evaluate(batch, PLAIN)
-    plain_batched = len(trees) / (time.perf_counter() - t)
-    fv = lambda r: (1 + r["loss"]) * (1 + r["rmse"]) * (1 + r["size"] * 1e-3)  # noqa: E731
-    ok = (plain["loss"] != 1000) & np.isfinite(fv(plain))
-    err = np.abs(fv(mixed_out)[ok] - fv(plain)[ok]) / fv(plain)[ok]
-    best_m = int(np.argmin(np.where(ok, fv(mixed_out), np.inf)))
-    best_p = int(np.argmin(np.where(ok, fv(plain), np.inf)))
-    order_m = np.argsort(np.where(ok, fv(mixed_out), np.inf))[:100]
-    order_p = np.argsort(np.where(ok, fv(plain), np.inf))[:100]
-    return {
-        "plain_fp64_unbatched_evals_per_s": unbatched,
-        "plain_fp64_batched_evals_per_s": plain_batched,
-        "mixed_over_plain_unbatched": None,  # filled by the caller from `value`
-        "accuracy_vs_fp64": {
-            "candidates_compared": int(ok.sum()),
-            "sentinel_agreement": float(np.mean((mixed_out["loss"] == 1000) == (plain["loss"] == 1000))),
-            "fitness_rel_err_median": float(np.median(err)), "fitness_rel_err_p99": float(np.quantile(err, 0.99)),
-            "fitness_rel_err_max": float(err.max()), "frac_within_1e-6": float(np.mean(err <= 1e-6)),
-            "argbest_same": best_m == best_p, "top100_overlap": len(set(order_m) & set(order_p)) / 100.0,
-            "fitness": "(1 + (1 - R2)) (1 + RMSE) (1 + 0.001 size)"},
-    }
+    res["plain_fp64_unbatched_evals_per_s"] = unbatched
+    res["plain_fp64_batched_evals_per_s"] = B / (time.perf_counter() - t)
+    res["mixed_over_plain_unbatched"] = value / world / unbatched
+    res["certified_over_plain_unbatched"] = res["certified"]["evals_per_s"] / unbatched
+    res["accuracy_vs_fp64"] = {"mixed": accuracy(out, plain), "certified": accuracy(cert, plain),
+                               "fitness": "(1 + (1 - R2)) (1 + RMSE) (1 + 0.001 size)"}
+    res["cpu_baseline"] = cpu_baseline(X, y, trees, args.cpu_sample)
+    res["mixed_over_cpu_baseline"] = value / world / res["cpu_baseline"]["value"]
+    print(json.dumps(res))
 
 
 def read_profile_traffic():
@@ -328,7 +351,7 @@ def run_reference(args):
         return
     from oracle import pyoracle
     from rils_rols_gb300.fitness import encode
-    X, y, trees = workload(args.n, args.batch)
+    X, y, trees, _ = workload(args.n, args.batch)
     threads = os.cpu_count() or 1
     ods = pyoracle.OracleDataset(X, y)
     sample = args.ref_sample
@@ -347,7 +370,7 @@ def run_reference(args):
     print(json.dumps({"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
                       "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
                       "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-                      "data": "synthetic (seeded)", "config": config(args.n, args.batch),
+                      "data": "synthetic (seeded)", "config": config(args.n, len(trees)),
                       "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                                        "sample": desc},
                       "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))

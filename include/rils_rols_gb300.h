@@ -44,8 +44,12 @@ typedef enum {
 
 /* Arithmetic of one round. */
 typedef enum {
-  RRG_PLAIN_FP64 = 0,  /* FP64 evaluation, column-pivoted Householder OLS, FP64 residual */
-  RRG_MIXED = 1        /* FP32 evaluation, compensated Gram, FP64 Cholesky + refinement, FP64 SSE */
+  RRG_PLAIN_FP64 = 0,        /* FP64 evaluation, column-pivoted Householder OLS, FP64 residual */
+  RRG_MIXED = 1,             /* FP32 evaluation, exact-product Gram sums, FP64 pivoted Cholesky + refinement;
+                                non-finite and ill-conditioned systems re-solved in FP64 */
+  RRG_MIXED_CERTIFIED = 2    /* RRG_MIXED, and every result whose fitness error cannot be bounded below
+                                5e-7 relative (or whose rank / drop / snap decision is ambiguous) is
+                                re-scored by the FP64 path: results equal the FP64 path's within 1e-6 */
 } rrg_precision;
 
 /* How one candidate is scored. */
@@ -185,8 +189,13 @@ int64_t rrg_last_round_launches(const rrg_context* ctx);
 
 /* Statistics of the last completed round, written to out[0..n):
  *   [0] kernels launched   [1] candidates routed to the FP64 path (beyond the
- *   mixed kernels' limits)  [2] ill-conditioned systems re-solved in FP64
- *   [3] candidates that needed the residual pass.  Returns the count written. */
+ *   mixed kernels' limits)  [2] mixed candidates re-scored by the FP64 path
+ *   [3] candidates that needed the residual pass  [4..14] re-scoring reasons:
+ *   FP32/FP64 non-finite mismatch on a probe row, FP64 overflow, FP32
+ *   overflow, NaN factor beside a rank-deficient rest, rank cut,
+ *   ill-conditioning, coefficient near 1, coefficient near 0, one-pass SSE
+ *   inaccurate, certified error bound too large, other NaN.
+ * Returns the count written. */
 int32_t rrg_last_round_stats(const rrg_context* ctx, int64_t* out, int32_t n);
 
 /* The CUDA stream (cudaStream_t) every kernel of this context runs on, so that

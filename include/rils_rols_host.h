@@ -42,7 +42,8 @@ void rrh_destroy(rrh_model* m);
 
 /* Install a backend (copied).  NULL restores the device backend. */
 int32_t rrh_set_backend(rrh_model* m, const rrh_backend* be);
-/* RRG_PLAIN_FP64 (default, the drop-in) or RRG_MIXED. */
+/* RRG_PLAIN_FP64 (default, the drop-in), RRG_MIXED_CERTIFIED (search
+ * decisions equal to the FP64 path's) or RRG_MIXED. */
 int32_t rrh_set_precision(rrh_model* m, int32_t precision);
 
 /* fit(X, y, data_cnt, feat_cnt), X row-major n x d (rils_rols_cpp.cpp:717-728).

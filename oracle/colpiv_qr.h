@@ -18,7 +18,8 @@
  *   (makeHouseholder) and :116-133 (applyHouseholderOnTheLeft).
  *
  * Reduction order (the one thing the vendored, incomplete Eigen cannot pin):
- * every sum, dot product and norm here is a sequential left-to-right loop.
+ * every sum, dot product and norm here follows the fixed RR256 order of
+ * rils-rols_gb300/csrc/common/rr_sum.h (the order of a 256-thread block).
  * The Eigen-subset shim that compiles the reference sources uses this same
  * header, so the oracle and the compiled reference agree bit for bit.
  *
@@ -30,16 +31,12 @@
 #include <math.h>
 #include <float.h>
 
+#include "../rils-rols_gb300/csrc/common/rr_sum.h"
+
 #ifdef __cplusplus
 extern "C" {
 #endif
 
-/* sequential sum of squares of x[0..len) with stride 1 */
-static inline double rrq_sqnorm(const double* x, long len) {
-    double s = 0.0;
-    for (long i = 0; i < len; ++i) s += x[i] * x[i];
-    return s;
-}
 
 /* Work space (doubles) needed by rrq_lstsq for a rows x cols problem. */
 static inline long rrq_work_size(long rows, long cols) {
@@ -62,7 +59,7 @@ static inline long rrq_lstsq(double* A, long lda, long rows, long cols,
     long k, j, i;
 
     for (k = 0; k < cols; ++k) {
-        norm_dir[k] = sqrt(rrq_sqnorm(A + k * lda, rows));
+        norm_dir[k] = sqrt(rr_sumsq256(A + k * lda, 0, rows));
         norm_upd[k] = norm_dir[k];
         permf[k] = (double)k;
     }
@@ -92,7 +89,7 @@ static inline long rrq_lstsq(double* A, long lda, long rows, long cols,
         /* Householder reflector of A[k:rows, k] */
         double* col = A + k * lda;
         const long m = rows - k;
-        const double tail_sq = (m == 1) ? 0.0 : rrq_sqnorm(col + k + 1, m - 1);
+        const double tail_sq = (m == 1) ? 0.0 : rr_sumsq256(col, k + 1, rows);
         const double c0 = col[k];
         double tau, beta;
         if (tail_sq <= DBL_MIN) {
@@ -116,8 +113,7 @@ static inline long rrq_lstsq(double* A, long lda, long rows, long cols,
             } else if (tau != 0.0) {
                 for (j = k + 1; j < cols; ++j) {
                     double* cj = A + j * lda;
-                    double tmp = 0.0;
-                    for (i = k + 1; i < rows; ++i) tmp += col[i] * cj[i];
+                    double tmp = rr_dot256(col, cj, k + 1, rows);
                     tmp += cj[k];
                     cj[k] -= tau * tmp;
                     for (i = k + 1; i < rows; ++i) cj[i] -= (tau * col[i]) * tmp;
@@ -134,7 +130,7 @@ static inline long rrq_lstsq(double* A, long lda, long rows, long cols,
                 const double ratio = norm_upd[j] / norm_dir[j];
                 const double temp2 = temp * (ratio * ratio);
                 if (temp2 <= downdate_thr) {
-                    norm_dir[j] = sqrt(rrq_sqnorm(A + j * lda + k + 1, rows - k - 1));
+                    norm_dir[j] = sqrt(rr_sumsq256(A + j * lda, k + 1, rows));
                     norm_upd[j] = norm_dir[j];
                 } else {
                     norm_upd[j] *= sqrt(temp);
@@ -155,8 +151,7 @@ static inline long rrq_lstsq(double* A, long lda, long rows, long cols,
         if (m == 1) {
             c[k] *= (1.0 - tau);
         } else if (tau != 0.0) {
-            double tmp = 0.0;
-            for (i = k + 1; i < rows; ++i) tmp += v[i] * c[i];
+            double tmp = rr_dot256(v, c, k + 1, rows);
             tmp += c[k];
             c[k] -= tau * tmp;
             for (i = k + 1; i < rows; ++i) c[i] -= (tau * v[i]) * tmp;

@@ -7,13 +7,14 @@
  * candidate, consuming the same batch format as the device C ABI
  * (include/rils_rols_gb300.h):
  *   - factor evaluation: node::evaluate_all / evaluate_inner
- *       (rils_rols_cpp/node.cpp:5-95), element-wise FP64 with libm;
+ *       (rils_rols_cpp/node.cpp:5-95), element-wise FP64 (exp, log, sin, cos,
+ *       pow from rils-rols_gb300/csrc/common/rr_math.h);
  *   - the OLS refit of tune_constants: A = [factor_1 .. factor_m, 1],
  *       coefs = A.colPivHouseholderQr().solve(y)  (rils_rols_cpp.cpp:474-484),
  *       by oracle/colpiv_qr.h;
  *   - the rebuilt sum with the drop / snap rules (rils_rols_cpp.cpp:488-517);
  *   - fitness: R2, RMSE and the NaN sentinel (rils_rols_cpp.cpp:40-49, 520-541),
- *       every reduction a sequential left-to-right loop.
+ *       every sum in the fixed CSUM order of csrc/common/rr_sum.h.
  * The decoded programs are checked against the compiled reference through
  * the golden vectors in tests/golden/ (tree in -> fitness out).
  *
@@ -28,6 +29,8 @@
 #include <string.h>
 
 #include "../include/rils_rols_gb300.h"
+#include "../rils-rols_gb300/csrc/common/rr_math.h"
+#include "../rils-rols_gb300/csrc/common/rr_sum.h"
 #include "colpiv_qr.h"
 
 typedef struct {
@@ -74,7 +77,7 @@ static double bin_op(int base, double a, double b) {
     case RRG_SUB: return a - b;
     case RRG_MUL: return a * b;
     case RRG_DIV: return a / b;
-    case RRG_POW: return pow(a, b);
+    case RRG_POW: return rr_pow(a, b);
     case RRG_LT: return a < b ? 1 : 0;
     case RRG_EQ: return a == b ? 1 : 0;
     case RRG_NE: return a != b ? 1 : 0;
@@ -108,10 +111,10 @@ static int run_row(const oracle_dataset* ds, const rrg_batch* b, const rrg_cand*
         st[sp++] = tos;
         tos = b->consts[arg];
         break;
-      case RRG_OP_SIN: tos = sin(tos); break;
-      case RRG_OP_COS: tos = cos(tos); break;
-      case RRG_OP_LN: tos = log(tos); break;
-      case RRG_OP_EXP: tos = exp(tos); break;
+      case RRG_OP_SIN: tos = rr_sin(tos); break;
+      case RRG_OP_COS: tos = rr_cos(tos); break;
+      case RRG_OP_LN: tos = rr_log(tos); break;
+      case RRG_OP_EXP: tos = rr_exp(tos); break;
       case RRG_OP_SQRT: tos = sqrt(tos); break;
       case RRG_OP_SQR: tos = tos * tos; break;
       case RRG_OP_EMIT:
@@ -198,18 +201,20 @@ static int score_one(const oracle_dataset* ds, const rrg_batch* b, int ci, rrg_r
     size = b->factors[c->first_factor].n_nodes;
   }
   /* R2 and RMSE, rils_rols_cpp.cpp:40-49 */
-  double ysum = 0.0;
-  for (int64_t r = 0; r < n; ++r) ysum += ds->y[r];
-  const double ymean = ysum / (double)n;
-  double ssr = 0.0, sst = 0.0;
+  const double ymean = rr_csum(ds->y, (long)n) / (double)n;
+  rr_csum_acc acc;
+  rr_csum_init(&acc);
   for (int64_t r = 0; r < n; ++r) {
     const double e = ds->y[r] - yp[r];
-    ssr += e * e;
+    rr_csum_add(&acc, e * e);
   }
+  const double ssr = rr_csum_total(&acc);
+  rr_csum_init(&acc);
   for (int64_t r = 0; r < n; ++r) {
     const double e = ds->y[r] - ymean;
-    sst += e * e;
+    rr_csum_add(&acc, e * e);
   }
+  const double sst = rr_csum_total(&acc);
   const double r2 = 1 - ssr / sst;
   const double rmse = sqrt(ssr / (double)n);
   if (r2 != r2 || rmse != rmse) {

@@ -1,0 +1,84 @@
+/*
+ * The fixed summation order of the FP64 fitness path.
+ *
+ * RR256: a range [start, end) is summed by 256 lanes, lane t taking elements
+ * start + t, start + t + 256, ... in increasing order; each group of 32 lanes
+ * is folded by halving strides (16, 8, 4, 2, 1: lane t += lane t + stride),
+ * and the eight group totals are added in order starting from 0.  This is the
+ * order of a 256-thread CUDA block that sums with warp shuffles and then
+ * across warps, so device and host results agree bit for bit.
+ * CSUM: a whole column of n rows is summed as consecutive chunks of
+ * RR_CHUNK rows, each by RR256, the chunk totals added in order from 0.
+ * Every sum, mean, dot product and norm of the plain FP64 path uses one of
+ * these (host code must be built with -ffp-contract=off).
+ */
+#ifndef RR_SUM_H
+#define RR_SUM_H
+
+#define RR_LANES 256
+#define RR_CHUNK 16384
+
+static inline double rrs_fold(double* p) {
+  for (int w = 0; w < RR_LANES / 32; ++w) {
+    double* q = p + 32 * w;
+    for (int off = 16; off > 0; off >>= 1)
+      for (int t = 0; t < off; ++t) q[t] = q[t] + q[t + off];
+  }
+  double s = 0.0;
+  for (int w = 0; w < RR_LANES / 32; ++w) s = s + p[32 * w];
+  return s;
+}
+
+static inline double rr_sum256(const double* x, long start, long end) {
+  double p[RR_LANES] = {0};
+  for (long i = start; i < end; ++i) p[(i - start) & (RR_LANES - 1)] += x[i];
+  return rrs_fold(p);
+}
+
+static inline double rr_sumsq256(const double* x, long start, long end) {
+  double p[RR_LANES] = {0};
+  for (long i = start; i < end; ++i) p[(i - start) & (RR_LANES - 1)] += x[i] * x[i];
+  return rrs_fold(p);
+}
+
+static inline double rr_dot256(const double* a, const double* b, long start, long end) {
+  double p[RR_LANES] = {0};
+  for (long i = start; i < end; ++i) p[(i - start) & (RR_LANES - 1)] += a[i] * b[i];
+  return rrs_fold(p);
+}
+
+/* streaming CSUM: add values in row order, then rr_csum_total */
+typedef struct {
+  double p[RR_LANES];
+  long i;
+  double total;
+} rr_csum_acc;
+
+static inline void rr_csum_init(rr_csum_acc* a) {
+  for (int t = 0; t < RR_LANES; ++t) a->p[t] = 0.0;
+  a->i = 0;
+  a->total = 0.0;
+}
+static inline void rr_csum_add(rr_csum_acc* a, double v) {
+  a->p[a->i % RR_CHUNK & (RR_LANES - 1)] += v;
+  if (++a->i % RR_CHUNK == 0) {
+    a->total = a->total + rrs_fold(a->p);
+    for (int t = 0; t < RR_LANES; ++t) a->p[t] = 0.0;
+  }
+}
+static inline double rr_csum_total(rr_csum_acc* a) {
+  if (a->i % RR_CHUNK != 0) {
+    a->total = a->total + rrs_fold(a->p);
+    for (int t = 0; t < RR_LANES; ++t) a->p[t] = 0.0;
+    a->i = (a->i / RR_CHUNK + 1) * RR_CHUNK;
+  }
+  return a->total;
+}
+
+static inline double rr_csum(const double* x, long n) {
+  double s = 0.0;
+  for (long c = 0; c < n; c += RR_CHUNK) s = s + rr_sum256(x, c, c + RR_CHUNK < n ? c + RR_CHUNK : n);
+  return s;
+}
+
+#endif

@@ -23,6 +23,7 @@
 #include <cfloat>
 #include <cstdint>
 
+#include "../common/rr_math.h"
 #include "common.cuh"
 #include "mixed.cuh"
 #include "plain.cuh"
@@ -371,6 +372,23 @@ __global__ void __launch_bounds__(NWARPS * 32, 1) mixed_pass_kernel(MixedArgs a)
             f[s].z = m2 ? f[s].z : 0.f;
             f[s].w = m3 ? f[s].w : 0.f;
           }
+          {
+            // remember the first row with a NaN factor value (the solve
+            // re-evaluates that row in FP64 to tell a domain error from an
+            // FP32 breakdown)
+            bool nan_any = false;
+            int first = 4;
+#pragma unroll
+            for (int s = 0; s < MMAX; ++s) {
+              if (f[s].w != f[s].w) first = 3;
+              if (f[s].z != f[s].z) first = 2;
+              if (f[s].y != f[s].y) first = 1;
+              if (f[s].x != f[s].x) first = 0;
+            }
+            nan_any = first < 4;
+            if (nan_any && a.nanrow) atomicMin(reinterpret_cast<unsigned long long*>(a.nanrow + c),
+                                               (unsigned long long)(gr + first));
+          }
           yv.x = m0 ? yv.x : 0.f;
           yv.y = m1 ? yv.y : 0.f;
           yv.z = m2 ? yv.z : 0.f;
@@ -473,6 +491,10 @@ __global__ void __launch_bounds__(NWARPS * 32, 1) mixed_pass_kernel(MixedArgs a)
   }
 }
 
+template <int MM>
+__device__ bool probe_eval64(const uint32_t* code, int len, const double* K, const DevData& ds, int64_t row,
+                             double (&f)[MM]);
+
 // One warp per candidate: FP64 reduction of the Gram partials; tuned
 // candidates get a symmetric-pivoted Cholesky solve with one refinement step.
 // Every candidate then gets its SSE from the Gram identity
@@ -502,26 +524,60 @@ __global__ void __launch_bounds__(128) mixed_solve_kernel(SolveArgs a) {
   const double* ent = red[warp];
   const double yy = a.ds.yy;
   const double kU = 1e-11;  // relative accuracy of the double-float Gram sums
-  auto queue_fallback = [&]() {
+  auto queue_fallback = [&](int why) {
     const int slot = atomicAdd(a.fallback, 1);
     if (slot < a.fallback_cap) a.fallback[1 + slot] = c;
+    if (a.reasons) atomicAdd(a.reasons + why, 1u);
   };
+  const ProbeOut pr = a.probe[c];
+  const double n_d = (double)a.ds.n;
+  // certification: bound on the relative error of the penalised fitness
+  // (1 + loss)(1 + rmse)(1 + size * cp) caused by FP32 evaluation, from the
+  // per-row bound E on the error of the rebuilt sum (independent of cp)
+  auto cert_bound = [&](double sse, double E) {
+    if (!(sse >= 0.0) || !(E >= 0.0)) return 1e300;
+    const double dsse = 2.0 * sqrt(sse * n_d) * E + n_d * E * E;
+    const double loss = sse / a.ds.sst, rmse = sqrt(sse / n_d);
+    const double rl = (dsse / a.ds.sst) / (1.0 + loss);
+    const double rr = (sqrt((sse + dsse) / n_d) - rmse) / (1.0 + rmse);
+    return rl + rr;
+  };
+  // per-row error bound of factor i: the largest probed deviation with a
+  // safety factor (exact maximum when every row was probed)
+  const double safety = pr.all_rows ? 1.5 : 8.0;
+  auto ferr = [&](int i) { return safety * (double)pr.dev[i] + 1e-7 * (double)pr.rms[i]; };
   if (cd.mode != RRG_TUNED) {
     // yp = f: SSE = y'y - 2 f'y + f'f
-    const double ff = ent[0], fy = ent[Gn + mmax];
-    const bool nan = ff != ff || fy != fy, inf = fabs(ff) > DBL_MAX || fabs(fy) > DBL_MAX;
+    const double ff = ent[0], fs = ent[Gn], fy = ent[Gn + mmax];
+    const bool nan = ff != ff || fs != fs || fy != fy;
+    const bool inf = !nan && (fabs(ff) > DBL_MAX || fabs(fs) > DBL_MAX || fabs(fy) > DBL_MAX);
+    uint32_t confirmed = pr.nan64;
+    if (nan && !(confirmed & 1u) && a.nanrow && a.nanrow[c] >= 0 && a.nanrow[c] < a.ds.n) {
+      double f64[kMixedMaxM];
+      for (int i = 0; i < kMixedMaxM; ++i) f64[i] = 0.0;
+      if (probe_eval64<kMixedMaxM>(a.b.code + cd.code_offset, cd.code_len, a.b.consts, a.ds, a.nanrow[c], f64) &&
+          f64[0] != f64[0])
+        confirmed |= 1u;
+    }
     uint8_t p2 = 0;
     double sse;
-    if (nan) {
-      sse = __longlong_as_double(0x7ff8000000000000ll);
-    } else if (inf) {
-      queue_fallback();
+    if (pr.bad32 || pr.inf64 || inf || (nan && !(confirmed & 1u))) {
+      // FP32 broke down, FP64 overflows, or an FP32 NaN that the FP64 probe
+      // does not confirm: the FP64 path scores it
+      queue_fallback(pr.bad32 ? FB_PROBE_NONFINITE
+                              : (pr.inf64 ? FB_FP64_INF : (inf ? FB_FP32_OVERFLOW : FB_OTHER_NAN)));
       sse = -1.0;
+    } else if (nan || (pr.nan64 & 1u)) {
+      sse = __longlong_as_double(0x7ff8000000000000ll);
     } else {
       sse = __dadd_rn(__dsub_rn(yy, __dmul_rn(2.0, fy)), ff);
       const double bound = kU * (yy + 2.0 * fabs(fy) + ff);
       if (!(sse > 0.0 && bound <= a.pass2_tol * sse)) {
-        p2 = 1;
+        if (a.certify) queue_fallback(FB_ONE_PASS);
+        else p2 = 1;
+        sse = -1.0;
+      } else if (a.certify && cert_bound(sse, ferr(0)) > a.cert_tol) {
+        queue_fallback(FB_CERT);
         sse = -1.0;
       }
     }
@@ -553,6 +609,84 @@ __global__ void __launch_bounds__(128) mixed_solve_kernel(SolveArgs a) {
     }
     has_nan |= bvec[i] != bvec[i];
     has_inf |= fabs(bvec[i]) > DBL_MAX;
+  }
+  // factors whose own sums are NaN (a domain error on some row); the cross
+  // sums of a NaN factor are NaN for every partner, so only the diagonal,
+  // the factor sum and the factor-y sum identify it
+  uint32_t nanmask = 0, infmask = 0;
+  for (int i = 0; i < m; ++i) {
+    const double d = G[i][i], sf = G[i][m], sy = bvec[i];
+    if (d != d || sf != sf || sy != sy) nanmask |= 1u << i;
+    else if (fabs(d) > DBL_MAX || fabs(sf) > DBL_MAX || fabs(sy) > DBL_MAX) infmask |= 1u << i;
+  }
+  const uint32_t fullmask = (m >= 32) ? 0xffffffffu : ((1u << m) - 1u);
+  uint32_t confirmed = pr.nan64;
+  if ((nanmask & ~confirmed) && a.nanrow && a.nanrow[c] >= 0 && a.nanrow[c] < a.ds.n) {
+    // FP32 NaN outside the probe rows: evaluate the first such row in FP64
+    double f64[kMixedMaxM];
+    for (int i = 0; i < kMixedMaxM; ++i) f64[i] = 0.0;
+    if (probe_eval64<kMixedMaxM>(a.b.code + cd.code_offset, cd.code_len, a.b.consts, a.ds, a.nanrow[c], f64))
+      for (int i = 0; i < m; ++i)
+        if (f64[i] != f64[i]) confirmed |= 1u << i;
+  }
+  nanmask |= pr.nan64 & fullmask;
+  if (pr.bad32 || pr.inf64 || infmask || (nanmask & ~confirmed) ||
+      (!nanmask && (has_nan || has_inf))) {
+    // FP32 broke down where FP64 did not, FP64 overflow, FP32 overflow, an
+    // FP32 NaN the FP64 probe does not confirm, or a non-finite sum outside
+    // the factor columns: the FP64 path scores it
+    queue_fallback(pr.bad32 ? FB_PROBE_NONFINITE
+                            : (pr.inf64 ? FB_FP64_INF : (infmask ? FB_FP32_OVERFLOW : FB_OTHER_NAN)));
+    a.sse1[c] = -1.0;
+    a.pass2[c] = 0;
+    a.res[c].rank = 0;
+    return;
+  }
+  if (nanmask) {
+    // A NaN factor column makes the reference's QR return NaN coefficients
+    // (the sentinel) unless a rank cut among the other columns happens before
+    // the QR reaches it.  Full, well-conditioned rank of the other columns
+    // rules that out; otherwise the FP64 path decides.
+    int idx[kMixedMaxM + 1], kk2 = 0;
+    for (int i = 0; i < k; ++i)
+      if (i == m || !((nanmask >> i) & 1u)) idx[kk2++] = i;
+    double H[kMixedMaxM + 1][kMixedMaxM + 1];
+    for (int i = 0; i < kk2; ++i)
+      for (int j = 0; j < kk2; ++j) H[i][j] = G[idx[i]][idx[j]];
+    bool full = true;
+    double hmax = 0.0;
+    for (int i = 0; i < kk2; ++i) hmax = fmax(hmax, H[i][i]);
+    for (int s2 = 0; s2 < kk2 && full; ++s2) {
+      int p = s2;
+      for (int j = s2 + 1; j < kk2; ++j)
+        if (H[j][j] > H[p][p]) p = j;
+      if (!(H[p][p] > 1e-6 * hmax)) {
+        full = false;
+        break;
+      }
+      if (p != s2) {
+        for (int j = 0; j < kk2; ++j) { const double t2 = H[s2][j]; H[s2][j] = H[p][j]; H[p][j] = t2; }
+        for (int j = 0; j < kk2; ++j) { const double t2 = H[j][s2]; H[j][s2] = H[j][p]; H[j][p] = t2; }
+      }
+      const double l = sqrt(H[s2][s2]);
+      for (int i = s2 + 1; i < kk2; ++i) H[i][s2] /= l;
+      for (int i = s2 + 1; i < kk2; ++i)
+        for (int j = s2 + 1; j <= i; ++j) {
+          H[i][j] -= H[i][s2] * H[j][s2];
+          H[j][i] = H[i][j];
+        }
+    }
+    double* out = a.coefs + cd.coef_offset;
+    for (int i = 0; i < k; ++i) out[i] = __longlong_as_double(0x7ff8000000000000ll);
+    if (full) {
+      a.sse1[c] = __longlong_as_double(0x7ff8000000000000ll);
+    } else {
+      queue_fallback(FB_NAN_RANK);
+      a.sse1[c] = -1.0;
+    }
+    a.pass2[c] = 0;
+    a.res[c].rank = 0;
+    return;
   }
   // symmetric pivoted Cholesky (pivot = largest remaining diagonal, i.e. the
   // largest remaining column norm of the design, as column-pivoted QR picks)
@@ -626,8 +760,21 @@ __global__ void __launch_bounds__(128) mixed_solve_kernel(SolveArgs a) {
     }
   }
   if (rank < k) flags |= RRG_F_RANK_DEFICIENT;
-  const bool fallback = (has_inf && !has_nan) || (finite && rank == k && min_ratio < a.fallback_tol);
-  if (fallback) queue_fallback();
+  // Decisions the FP64 path must take itself: a rank cut (the reference's
+  // rule works at eps^2 of the column norms), ill-conditioning, and
+  // coefficients inside the ambiguity band of the drop (|c| < 1e-12) and
+  // snap (|c - 1| < 1e-12) rules of the rebuilt tree.
+  const double yrms = sqrt(yy / n_d);
+  int why = -1;
+  if (!finite) why = FB_OTHER_NAN;
+  else if (rank < k && a.certify) why = FB_RANK;
+  else if (rank == k && min_ratio < a.fallback_tol) why = FB_ILL_COND;
+  for (int i = 0; i < k && why < 0 && a.certify; ++i) {
+    const double ci = coef[i];
+    const double scale = i == m ? 1.0 : fmax((double)pr.rms[i], 1e-300);
+    if (fabs(ci - 1.0) < 1e-4 && i < m) why = FB_SNAP;
+    else if (fabs(ci) * scale < 1e-6 * yrms) why = FB_DROP;
+  }
   double* out = a.coefs + cd.coef_offset;
   MixedTerm& tm = a.terms[c];
   double ceff[kMixedMaxM + 1];
@@ -655,16 +802,230 @@ __global__ void __launch_bounds__(128) mixed_solve_kernel(SolveArgs a) {
       }
     }
     sse = yy - 2.0 * lin + quad;
-    if (!(sse > 0.0 && kU * mag <= a.pass2_tol * sse)) {
-      p2 = 1;
-      sse = -1.0;
+    double E = 0.0;
+    for (int i = 0; i < m; ++i) E += fabs(ceff[i]) * ferr(i);
+    if (why < 0 && !(sse > 0.0 && kU * mag <= a.pass2_tol * sse)) {
+      if (a.certify) why = FB_ONE_PASS;
+      else p2 = 1;
     }
+    if (why < 0 && a.certify && cert_bound(sse, E) > a.cert_tol) why = FB_CERT;
   }
-  if (fallback) p2 = 0;
+  const bool fallback = why >= 0;
+  if (fallback) {
+    queue_fallback(why);
+    p2 = 0;
+    sse = -1.0;
+  } else if (p2) {
+    sse = -1.0;
+  }
   a.sse1[c] = sse;
   a.pass2[c] = p2;
   a.res[c].rank = rank;
   a.res[c].flags |= flags;
+}
+
+// ------------------------------------------------------------- probe ----
+// Scalar interpreters for the probe: the FP64 one has the semantics of the
+// plain path (rr_math functions), the FP32 one those of eval4.
+template <int MM>
+__device__ bool probe_eval64(const uint32_t* code, int len, const double* K, const DevData& ds, int64_t row,
+                             double (&f)[MM]) {
+  double st[RRG_MAX_STACK];
+  double tos = 0.0;
+  int sp = 0;
+  for (int pc = 0; pc < len; ++pc) {
+    const uint32_t w = code[pc];
+    const int op = (int)(w & 0xffu);
+    const uint32_t arg = w >> 8;
+    switch (op) {
+      case RRG_OP_LDV: tos = ds.X64[(int64_t)arg * ds.n_pad + row]; break;
+      case RRG_OP_LDC: tos = K[arg]; break;
+      case RRG_OP_PSV:
+        if (sp >= RRG_MAX_STACK) return false;
+        st[sp++] = tos;
+        tos = ds.X64[(int64_t)arg * ds.n_pad + row];
+        break;
+      case RRG_OP_PSC:
+        if (sp >= RRG_MAX_STACK) return false;
+        st[sp++] = tos;
+        tos = K[arg];
+        break;
+      case RRG_OP_SIN: tos = rr_sin(tos); break;
+      case RRG_OP_COS: tos = rr_cos(tos); break;
+      case RRG_OP_LN: tos = rr_log(tos); break;
+      case RRG_OP_EXP: tos = rr_exp(tos); break;
+      case RRG_OP_SQRT: tos = __dsqrt_rn(tos); break;
+      case RRG_OP_SQR: tos = __dmul_rn(tos, tos); break;
+      case RRG_OP_EMIT:
+#pragma unroll
+        for (int s = 0; s < MM; ++s)
+          if ((int)arg == s) f[s] = tos;
+        sp = 0;
+        break;
+      default: {
+        const int kk = op - RRG_OP_BIN;
+        const int base = kk >> 3, src = (kk & 7) >> 1, dir = kk & 1;
+        double o;
+        if (src == RRG_SRC_S) {
+          if (sp <= 0) return false;
+          o = st[--sp];
+        } else if (src == RRG_SRC_V) {
+          o = ds.X64[(int64_t)arg * ds.n_pad + row];
+        } else {
+          o = K[arg];
+        }
+        const double a = dir == RRG_DIR_N ? o : tos, b = dir == RRG_DIR_N ? tos : o;
+        switch (base) {
+          case RRG_ADD: tos = __dadd_rn(a, b); break;
+          case RRG_SUB: tos = __dsub_rn(a, b); break;
+          case RRG_MUL: tos = __dmul_rn(a, b); break;
+          case RRG_DIV: tos = __ddiv_rn(a, b); break;
+          case RRG_POW: tos = rr_pow(a, b); break;
+          case RRG_LT: tos = a < b ? 1.0 : 0.0; break;
+          case RRG_EQ: tos = a == b ? 1.0 : 0.0; break;
+          case RRG_NE: tos = a != b ? 1.0 : 0.0; break;
+          case RRG_MIN: tos = a < b ? a : b; break;
+          default: tos = a > b ? a : b; break;
+        }
+      }
+    }
+  }
+  return true;
+}
+
+template <int MM>
+__device__ bool probe_eval32(const uint32_t* code, int len, const float* K, const DevData& ds, int64_t row,
+                             float (&f)[MM]) {
+  float st[RRG_MAX_STACK];
+  float tos = 0.f;
+  int sp = 0;
+  for (int pc = 0; pc < len; ++pc) {
+    const uint32_t w = code[pc];
+    const int op = (int)(w & 0xffu);
+    const uint32_t arg = w >> 8;
+    switch (op) {
+      case RRG_OP_LDV: tos = ds.X32[(int64_t)arg * ds.n_pad + row]; break;
+      case RRG_OP_LDC: tos = K[arg]; break;
+      case RRG_OP_PSV:
+        if (sp >= RRG_MAX_STACK) return false;
+        st[sp++] = tos;
+        tos = ds.X32[(int64_t)arg * ds.n_pad + row];
+        break;
+      case RRG_OP_PSC:
+        if (sp >= RRG_MAX_STACK) return false;
+        st[sp++] = tos;
+        tos = K[arg];
+        break;
+      case RRG_OP_SIN: tos = sin32(tos); break;
+      case RRG_OP_COS: tos = cos32(tos); break;
+      case RRG_OP_LN: tos = logf(tos); break;
+      case RRG_OP_EXP: tos = expf(tos); break;
+      case RRG_OP_SQRT: tos = sqrt32(tos); break;
+      case RRG_OP_SQR: tos = sqr32(tos); break;
+      case RRG_OP_EMIT:
+#pragma unroll
+        for (int s = 0; s < MM; ++s)
+          if ((int)arg == s) f[s] = tos;
+        sp = 0;
+        break;
+      default: {
+        const int kk = op - RRG_OP_BIN;
+        const int base = kk >> 3, src = (kk & 7) >> 1, dir = kk & 1;
+        float o;
+        if (src == RRG_SRC_S) {
+          if (sp <= 0) return false;
+          o = st[--sp];
+        } else if (src == RRG_SRC_V) {
+          o = ds.X32[(int64_t)arg * ds.n_pad + row];
+        } else {
+          o = K[arg];
+        }
+        tos = dir == RRG_DIR_N ? bin32(base, o, tos) : bin32(base, tos, o);
+      }
+    }
+  }
+  return true;
+}
+
+// One warp per candidate: both interpreters on kProbeRows rows spread evenly
+// over the dataset; per factor the largest FP32 deviation, the FP64 RMS and
+// the non-finite patterns.
+__global__ void __launch_bounds__(128) mixed_probe_kernel(DevBatch b, DevData ds, const int32_t* list,
+                                                          int32_t n_list, ProbeOut* out) {
+  const int lane = threadIdx.x & 31;
+  const int li = blockIdx.x * 4 + (threadIdx.x >> 5);
+  if (li >= n_list) return;
+  const int c = list[li];
+  const rrg_cand cd = b.cands[c];
+  const int nf = cd.n_factors;
+  const uint32_t* code = b.code + cd.code_offset;
+  const int P = ds.n < kProbeRows ? (int)ds.n : kProbeRows;
+  float dev[kMixedMaxM];
+  double ss[kMixedMaxM];
+  int cnt[kMixedMaxM];
+  uint32_t nan64 = 0, inf64 = 0, bad32 = 0;
+#pragma unroll
+  for (int i = 0; i < kMixedMaxM; ++i) {
+    dev[i] = 0.f;
+    ss[i] = 0.0;
+    cnt[i] = 0;
+  }
+  for (int p = lane; p < P; p += 32) {
+    const int64_t row = ds.n < kProbeRows ? p : ((2 * (int64_t)p + 1) * ds.n) / (2 * kProbeRows);
+    double f64[kMixedMaxM];
+    float f32[kMixedMaxM];
+#pragma unroll
+    for (int i = 0; i < kMixedMaxM; ++i) {
+      f64[i] = 0.0;
+      f32[i] = 0.f;
+    }
+    if (!probe_eval64<kMixedMaxM>(code, cd.code_len, b.consts, ds, row, f64) ||
+        !probe_eval32<kMixedMaxM>(code, cd.code_len, b.consts32, ds, row, f32)) {
+      bad32 = 0xffffffffu;
+      continue;
+    }
+#pragma unroll
+    for (int i = 0; i < kMixedMaxM; ++i) {
+      if (i >= nf) break;
+      const double v = f64[i];
+      const float u = f32[i];
+      const bool n64 = v != v, i64 = !n64 && fabs(v) > DBL_MAX;
+      const bool n32 = u != u, i32 = !n32 && fabsf(u) > FLT_MAX;
+      if (n64) nan64 |= 1u << i;
+      if (i64) inf64 |= 1u << i;
+      if (n64 != n32 || (i32 && !i64) || (i64 && !i32)) bad32 |= 1u << i;
+      if (!n64 && !i64 && !n32 && !i32) {
+        const float dv = (float)fabs((double)u - v);
+        dev[i] = fmaxf(dev[i], dv);
+        ss[i] = __fma_rn(v, v, ss[i]);
+        cnt[i] += 1;
+      }
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    nan64 |= __shfl_xor_sync(0xffffffffu, nan64, o);
+    inf64 |= __shfl_xor_sync(0xffffffffu, inf64, o);
+    bad32 |= __shfl_xor_sync(0xffffffffu, bad32, o);
+#pragma unroll
+    for (int i = 0; i < kMixedMaxM; ++i) {
+      dev[i] = fmaxf(dev[i], __shfl_xor_sync(0xffffffffu, dev[i], o));
+      ss[i] += __shfl_xor_sync(0xffffffffu, ss[i], o);
+      cnt[i] += __shfl_xor_sync(0xffffffffu, cnt[i], o);
+    }
+  }
+  if (lane == 0) {
+    ProbeOut r;
+    for (int i = 0; i < kMixedMaxM; ++i) {
+      r.dev[i] = dev[i];
+      r.rms[i] = cnt[i] > 0 ? (float)sqrt(ss[i] / (double)cnt[i]) : 0.f;
+    }
+    r.nan64 = nan64;
+    r.inf64 = inf64;
+    r.bad32 = bad32;
+    r.all_rows = P == ds.n ? 1u : 0u;
+    out[c] = r;
+  }
 }
 
 __global__ void to_f32_kernel(const double* src, float* dst, int64_t n) {
@@ -718,6 +1079,12 @@ bool launch_resid(int mmax, const MixedArgs& a, int grid, size_t smem, cudaStrea
     case 8: return launch_one<8, true>(a, grid, smem, st);
     default: return false;
   }
+}
+bool launch_probe(const DevBatch& b, const DevData& ds, const int32_t* list, int32_t n_list, ProbeOut* out,
+                  cudaStream_t st) {
+  if (n_list <= 0) return true;
+  mixed_probe_kernel<<<(n_list + 3) / 4, 128, 0, st>>>(b, ds, list, n_list, out);
+  return cudaGetLastError() == cudaSuccess;
 }
 bool launch_solve(const SolveArgs& a, cudaStream_t st) {
   mixed_solve_kernel<<<(a.n_list + 3) / 4, 128, 0, st>>>(a);

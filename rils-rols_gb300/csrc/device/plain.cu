@@ -17,6 +17,8 @@
 #include <cfloat>
 #include <cstdint>
 
+#include "../common/rr_math.h"
+#include "../common/rr_sum.h"
 #include "common.cuh"
 #include "plain.cuh"
 #include "reduce.cuh"
@@ -33,7 +35,7 @@ __device__ __forceinline__ double bin64(int base, double a, double b) {
     case RRG_SUB: return __dsub_rn(a, b);
     case RRG_MUL: return __dmul_rn(a, b);
     case RRG_DIV: return __ddiv_rn(a, b);
-    case RRG_POW: return pow(a, b);
+    case RRG_POW: return rr_pow(a, b);
     case RRG_LT: return a < b ? 1.0 : 0.0;
     case RRG_EQ: return a == b ? 1.0 : 0.0;
     case RRG_NE: return a != b ? 1.0 : 0.0;
@@ -67,10 +69,10 @@ __device__ __forceinline__ void run_row64(const uint32_t* code, int len, const d
         st[sp++ * stride] = tos;
         tos = consts[arg];
         break;
-      case RRG_OP_SIN: tos = sin(tos); break;
-      case RRG_OP_COS: tos = cos(tos); break;
-      case RRG_OP_LN: tos = log(tos); break;
-      case RRG_OP_EXP: tos = exp(tos); break;
+      case RRG_OP_SIN: tos = rr_sin(tos); break;
+      case RRG_OP_COS: tos = rr_cos(tos); break;
+      case RRG_OP_LN: tos = rr_log(tos); break;
+      case RRG_OP_EXP: tos = rr_exp(tos); break;
       case RRG_OP_SQRT: tos = __dsqrt_rn(tos); break;
       case RRG_OP_SQR: tos = __dmul_rn(tos, tos); break;
       case RRG_OP_EMIT:
@@ -216,11 +218,13 @@ __global__ void __launch_bounds__(256) plain_eval_kernel(DevBatch b, DevData ds,
 __global__ void __launch_bounds__(256) plain_qr_kernel(DevBatch b, DevData ds, const PlainCand* pc,
                                                         const int32_t* list, int cand0, const double* A, double* M,
                                                         double* S, int tsqr, int nb, double* coefs, rrg_result* res,
-                                                        uint32_t* status) {
+                                                        uint32_t* status, uint8_t* redo) {
   extern __shared__ double smem[];
   const int c = list ? list[cand0 + blockIdx.x] : cand0 + blockIdx.x;
   const rrg_cand cd = b.cands[c];
   if (cd.mode != RRG_TUNED) return;
+  // second pass of a tiled round: only the candidates the first pass flagged
+  if (!tsqr && redo && !redo[c]) return;
   const int k = pc[c].k;
   if (k > kMaxK) {
     if (threadIdx.x == 0) atomicOr(status, ST_TOO_LARGE);
@@ -358,10 +362,24 @@ __global__ void __launch_bounds__(256) plain_qr_kernel(DevBatch b, DevData ds, c
     for (int j = 0; j < k; ++j) out[j] = 0.0;
     for (int i = 0; i < r; ++i) out[perm[i]] = cvec[i];
     res[c].rank = r;
+    if (tsqr && redo) {
+      // The tiled factorisation reproduces the direct one to rounding only.
+      // Where the rank rule or the pivot order is sensitive to rounding
+      // (a rank cut, or a trailing pivot far below the leading one), the
+      // candidate is re-solved by the direct column-pivoted QR on [A | 1 | y].
+      double rmax = 0.0, rmin = 1e308;
+      for (int i = 0; i < size; ++i) {
+        const double d = fabs(Q[(int64_t)i * ld + i]);
+        rmax = d > rmax ? d : rmax;
+        rmin = d < rmin ? d : rmin;
+      }
+      redo[c] = (r < k || !(rmin > 1e-7 * rmax)) ? 1 : 0;
+    }
   }
 }
 
-// grid (blocks per candidate, candidates): partial SSE of the rebuilt sum
+// grid (ceil(n / RR_CHUNK), candidates): SSE of the rebuilt sum per chunk of
+// RR_CHUNK rows in the fixed order of csrc/common/rr_sum.h
 __global__ void __launch_bounds__(256) plain_resid_kernel(DevBatch b, DevData ds, const PlainCand* pc,
                                                            const int32_t* list, int cand0, const double* A,
                                                            const double* coefs, double* partial) {
@@ -382,7 +400,7 @@ __global__ void __launch_bounds__(256) plain_resid_kernel(DevBatch b, DevData ds
     }
   }
   __syncthreads();
-  const int64_t r0 = ds.n * (int64_t)blockIdx.x / nb, r1 = ds.n * (int64_t)(blockIdx.x + 1) / nb;
+  const int64_t r0 = (int64_t)blockIdx.x * RR_CHUNK, r1 = min(ds.n, r0 + (int64_t)RR_CHUNK);
   const double* Ac = A + pc[c].a_col * ds.n_pad;
   double acc = 0.0;
   for (int64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {

@@ -16,6 +16,7 @@
 #include <vector>
 
 #include "../common/error.h"
+#include "../common/rr_sum.h"
 #include "common.cuh"
 #include "mixed.cuh"
 #include "plain.cuh"
@@ -218,7 +219,8 @@ rrg_status rrg_context::stage_batch(const rrg_batch* b) {
 // Plain FP64 round over `list` (or [lo, hi)), in sub-batches that fit the
 // scratch budget.
 rrg_status rrg_context::run_plain(const rrg_dataset* ds, int32_t lo, int32_t hi, bool predict_only,
-                                  const std::vector<int32_t>* list, uint32_t flags_or) {
+                                  const std::vector<int32_t>* list, uint32_t flags_or, bool tiled_any,
+                                  bool redo_sensitive) {
   const DevData dd = ds->view();
   const int64_t n_pad = ds->n_pad;
   std::vector<int32_t> all;
@@ -253,8 +255,8 @@ rrg_status rrg_context::run_plain(const rrg_dataset* ds, int32_t lo, int32_t hi,
     const int32_t ns = e - p;
     int nb = (int)std::min<int64_t>(std::max<int64_t>(1, (4LL * sm_count + ns - 1) / ns), (ds->n + 1023) / 1024);
     nb = std::max(nb, 1);
-    bool tsqr = !predict_only && ds->n >= 65536 && ns < 2 * sm_count;
-    if (tsqr) nb = (int)std::max<int64_t>(1, std::min<int64_t>(nb, ds->n / 2048));
+    bool tsqr = !predict_only && ds->n >= 65536 && (ns < 2 * sm_count || tiled_any);
+    if (tsqr) nb = (int)std::max<int64_t>(1, std::min<int64_t>(std::max<int64_t>(nb, ds->n / 16384), ds->n / 2048));
     tsqr = tsqr && nb > 1;
     int64_t s_total = 0;
     for (int32_t i = p; i < e; ++i) {
@@ -268,11 +270,14 @@ rrg_status rrg_context::run_plain(const rrg_dataset* ds, int32_t lo, int32_t hi,
     subs.push_back(Sub{p, e, nb, tsqr});
     p = e;
   }
+  const int nb_res = (int)((ds->n + RR_CHUNK - 1) / RR_CHUNK);
+  max_nb = std::max<int64_t>(max_nb, nb_res);
   const size_t pc_bytes = sizeof(PlainCand) * host_cands.size();
   const size_t list_bytes = sizeof(int32_t) * cnt;
   if (!d_A.reserve((size_t)max_cols * n_pad * sizeof(double)) || !d_S.reserve((size_t)max_s * sizeof(double)) ||
       !d_pc.reserve(pc_bytes) || !d_partial.reserve(sizeof(double) * (size_t)host_cands.size() * max_nb) ||
-      !h_pc.reserve(pc_bytes + list_bytes) || !d_list.reserve(list_bytes)) {
+      !h_pc.reserve(pc_bytes + list_bytes) || !d_list.reserve(list_bytes) ||
+      !d_redo.reserve(std::max<size_t>(1, host_cands.size()))) {
     rrc::set_error("device scratch allocation failed");
     return RRG_E_OOM;
   }
@@ -300,14 +305,19 @@ rrg_status rrg_context::run_plain(const rrg_dataset* ds, int32_t lo, int32_t hi,
     ++launches;
     if (predict_only) continue;
     t0 = mark_begin();
+    uint8_t* redo = static_cast<uint8_t*>(d_redo.ptr);
     plain_qr_kernel<<<ns, 256, plain_qr_smem(), stream>>>(dev, dd, pc, dl, sb.p, A, A, S, sb.tsqr ? 1 : 0, sb.nb,
-                                                          coefs, res, status);
+                                                          coefs, res, status,
+                                                          (sb.tsqr && redo_sensitive) ? redo : nullptr);
+    if (sb.tsqr && redo_sensitive)
+      plain_qr_kernel<<<ns, 256, plain_qr_smem(), stream>>>(dev, dd, pc, dl, sb.p, A, A, S, 0, sb.nb, coefs, res,
+                                                            status, redo);
     mark_end(P_PLAIN_QR, t0);
     t0 = mark_begin();
-    plain_resid_kernel<<<dim3(sb.nb, ns), 256, 0, stream>>>(dev, dd, pc, dl, sb.p, A, coefs, partial);
+    plain_resid_kernel<<<dim3(nb_res, ns), 256, 0, stream>>>(dev, dd, pc, dl, sb.p, A, coefs, partial);
     mark_end(P_PLAIN_RESID, t0);
     t0 = mark_begin();
-    finalize_kernel<<<(ns + 127) / 128, 128, 0, stream>>>(dev, dd, dl, sb.p, sb.e, partial, sb.nb, coefs, res,
+    finalize_kernel<<<(ns + 127) / 128, 128, 0, stream>>>(dev, dd, dl, sb.p, sb.e, partial, nb_res, coefs, res,
                                                           flags_or, nullptr);
     mark_end(P_FINAL, t0);
     launches += 3;
@@ -321,7 +331,7 @@ rrg_status rrg_context::run_plain(const rrg_dataset* ds, int32_t lo, int32_t hi,
 // beyond the mixed kernels' limits go to the FP64 path.  Gram pass + solve for
 // every bucket; the residual pass only for candidates whose one-pass SSE is
 // not accurate enough; ill-conditioned systems are re-solved in FP64.
-rrg_status rrg_context::run_mixed(const rrg_dataset* ds, int32_t n_cand) {
+rrg_status rrg_context::run_mixed(const rrg_dataset* ds, int32_t n_cand, bool certify) {
   const DevData dd = ds->view();
   static const int kBuckets[4] = {1, 2, 4, 8};
   std::vector<int32_t> bucket[4], plain;
@@ -365,10 +375,12 @@ rrg_status rrg_context::run_mixed(const rrg_dataset* ds, int32_t n_cand) {
   }
   const int fb_cap = std::max(1, n_cand);
   const size_t list_bytes = sizeof(int32_t) * (lists.size() * 2 + 8);
-  const size_t back_bytes = sizeof(int32_t) * (fb_cap + 1) + (size_t)fb_cap;  // fallback list + pass2 flags
+  // fallback list, reason counters, pass2 flags
+  const size_t back_bytes = sizeof(int32_t) * (fb_cap + 1 + kFbReasons) + (size_t)fb_cap;
   if (!d_mlist.reserve(list_bytes) || !h_mlist.reserve(list_bytes) ||
       !d_gram.reserve(sizeof(float2) * std::max<size_t>(1, gram_elems)) ||
       !d_terms.reserve(sizeof(MixedTerm) * fb_cap) || !d_sse1.reserve(sizeof(double) * fb_cap) ||
+      !d_probe.reserve(sizeof(ProbeOut) * fb_cap) || !d_nanrow.reserve(sizeof(int64_t) * fb_cap) ||
       !d_partial.reserve(sizeof(double) * (size_t)fb_cap * n_tiles) || !d_fallback.reserve(back_bytes) ||
       !h_fallback.reserve(back_bytes)) {
     rrc::set_error("mixed round: scratch allocation failed");
@@ -379,17 +391,31 @@ rrg_status rrg_context::run_mixed(const rrg_dataset* ds, int32_t n_cand) {
   RRG_CUDA(cudaMemcpyAsync(d_mlist.ptr, hl, sizeof(int32_t) * std::max<size_t>(1, lists.size()), cudaMemcpyHostToDevice,
                            stream));
   RRG_CUDA(cudaMemsetAsync(d_fallback.ptr, 0, back_bytes, stream));
+  RRG_CUDA(cudaMemsetAsync(d_nanrow.ptr, 0x7f, sizeof(int64_t) * fb_cap, stream));  // "no NaN row"
+  int64_t* nanrow = static_cast<int64_t*>(d_nanrow.ptr);
   const int32_t* dl = static_cast<const int32_t*>(d_mlist.ptr);
   float2* gram = static_cast<float2*>(d_gram.ptr);
   MixedTerm* terms = static_cast<MixedTerm*>(d_terms.ptr);
   double* sse = static_cast<double*>(d_partial.ptr);
   double* sse1 = static_cast<double*>(d_sse1.ptr);
   int32_t* fallback = static_cast<int32_t*>(d_fallback.ptr);
-  uint8_t* pass2 = reinterpret_cast<uint8_t*>(fallback + fb_cap + 1);
+  uint32_t* reasons = reinterpret_cast<uint32_t*>(fallback + fb_cap + 1);
+  uint8_t* pass2 = reinterpret_cast<uint8_t*>(fallback + fb_cap + 1 + kFbReasons);
   uint32_t* status = static_cast<uint32_t*>(d_status.ptr);
   rrg_result* res = static_cast<rrg_result*>(d_res.ptr);
   double* coefs = static_cast<double*>(d_coefs.ptr);
 
+  ProbeOut* probe = static_cast<ProbeOut*>(d_probe.ptr);
+  {
+    // FP32-versus-FP64 probe of every mixed candidate (certification input)
+    cudaEvent_t t0 = mark_begin();
+    if (!launch_probe(dev, dd, dl, n_mixed, probe, stream)) {
+      cuda_ok(cudaGetLastError(), "mixed probe launch");
+      return RRG_E_CUDA;
+    }
+    mark_end(P_SOLVE, t0);
+    ++launches;
+  }
   auto make_args = [&](int mmax, const int32_t* list, int32_t cnt, float2* g) {
     MixedArgs a;
     a.b = dev;
@@ -406,6 +432,7 @@ rrg_status rrg_context::run_mixed(const rrg_dataset* ds, int32_t n_cand) {
     a.sse = sse;
     a.terms = terms;
     a.status = status;
+    a.nanrow = nanrow;
     return a;
   };
   for (int b = 0; b < 4; ++b) {
@@ -434,9 +461,14 @@ rrg_status rrg_context::run_mixed(const rrg_dataset* ds, int32_t n_cand) {
     sa.fallback_cap = fb_cap;
     sa.sse1 = sse1;
     sa.pass2 = pass2;
+    sa.probe = probe;
+    sa.reasons = reasons;
+    sa.nanrow = nanrow;
     sa.rank_tol = 1e-11;
     sa.fallback_tol = 1e-7;
     sa.pass2_tol = 1e-8;
+    sa.cert_tol = cert_tol;
+    sa.certify = certify ? 1 : 0;
     t0 = mark_begin();
     if (!launch_solve(sa, stream)) {
       cuda_ok(cudaGetLastError(), "mixed solve launch");
@@ -449,7 +481,9 @@ rrg_status rrg_context::run_mixed(const rrg_dataset* ds, int32_t n_cand) {
   RRG_CUDA(cudaMemcpyAsync(h_fallback.ptr, d_fallback.ptr, back_bytes, cudaMemcpyDeviceToHost, stream));
   RRG_CUDA(cudaStreamSynchronize(stream));
   const int32_t* hf = static_cast<const int32_t*>(h_fallback.ptr);
-  const uint8_t* hp2 = reinterpret_cast<const uint8_t*>(hf + fb_cap + 1);
+  const uint32_t* hr = reinterpret_cast<const uint32_t*>(hf + fb_cap + 1);
+  for (int i = 0; i < kFbReasons; ++i) last_reasons[i] = hr[i];
+  const uint8_t* hp2 = reinterpret_cast<const uint8_t*>(hf + fb_cap + 1 + kFbReasons);
   const int32_t nf = std::min(hf[0], fb_cap);
   std::vector<int32_t> fb(hf + 1, hf + 1 + nf);
   std::sort(fb.begin(), fb.end());
@@ -490,8 +524,10 @@ rrg_status rrg_context::run_mixed(const rrg_dataset* ds, int32_t n_cand) {
   }
   RRG_CUDA(cudaGetLastError());
   rrg_status st = RRG_OK;
-  if (!plain.empty()) st = run_plain(ds, 0, 0, false, &plain, 0u);
-  if (st == RRG_OK && !fb.empty()) st = run_plain(ds, 0, 0, false, &fb, RRG_F_QR_FALLBACK);
+  // FP64 re-scoring goes through the tiled QR on tall data; certified rounds
+  // re-solve its rounding-sensitive candidates by the direct QR
+  if (!plain.empty()) st = run_plain(ds, 0, 0, false, &plain, 0u, true, certify);
+  if (st == RRG_OK && !fb.empty()) st = run_plain(ds, 0, 0, false, &fb, RRG_F_QR_FALLBACK, true, certify);
   return st;
 }
 
@@ -507,11 +543,13 @@ rrg_status rrg_context::submit(rrg_dataset* ds, const rrg_batch* b, int32_t prec
     rrc::set_error("rrg_round_submit: malformed or oversized batch");
     return st;
   }
-  if (precision != RRG_PLAIN_FP64 && precision != RRG_MIXED) return RRG_E_INVALID;
+  if (precision != RRG_PLAIN_FP64 && precision != RRG_MIXED && precision != RRG_MIXED_CERTIFIED)
+    return RRG_E_INVALID;
   if (n_coefs > 0 && !coefs) return RRG_E_INVALID;
   RRG_CUDA(cudaSetDevice(device));
   launches = 0;
   last_plain_routed = last_fallback = last_pass2 = 0;
+  for (auto& r : last_reasons) r = 0;
   marks.clear();
   event_next = 0;
   st = stage_batch(b);
@@ -527,7 +565,7 @@ rrg_status rrg_context::submit(rrg_dataset* ds, const rrg_batch* b, int32_t prec
   RRG_CUDA(cudaMemsetAsync(d_coefs.ptr, 0, coef_bytes, stream));
   RRG_CUDA(cudaMemsetAsync(d_status.ptr, 0, 64, stream));
   if (precision == RRG_PLAIN_FP64) st = run_plain(ds, 0, b->n_cand, false);
-  else st = run_mixed(ds, b->n_cand);
+  else st = run_mixed(ds, b->n_cand, precision == RRG_MIXED_CERTIFIED);
   if (st != RRG_OK) return st;
   RRG_CUDA(cudaMemcpyAsync(h_res.ptr, d_res.ptr, res_bytes, cudaMemcpyDeviceToHost, stream));
   RRG_CUDA(cudaMemcpyAsync(h_coefs.ptr, d_coefs.ptr, coef_bytes, cudaMemcpyDeviceToHost, stream));
@@ -595,11 +633,14 @@ rrg_context::~rrg_context() {
   d_coefs.release();
   d_status.release();
   d_list.release();
+  d_redo.release();
   d_gram.release();
   d_terms.release();
   d_mlist.release();
   d_fallback.release();
   d_sse1.release();
+  d_probe.release();
+  d_nanrow.release();
   h_mlist.release();
   h_fallback.release();
   mixed_scratch.release();
@@ -693,17 +734,16 @@ rrg_status rrg_dataset_create(rrg_context* ctx, const double* X_col, const doubl
   ds->d = d;
   ds->n_pad = round_up(n, 256);
   const int64_t cols = std::max(d, 1);
-  // sequential FP64 mean and total sum of squares (rils_rols_cpp.cpp:41-43)
-  double s = 0.0;
-  for (int64_t i = 0; i < n; ++i) s += y[i];
-  ds->ysum = s;
-  ds->ymean = s / (double)n;
-  double sst = 0.0;
-  for (int64_t i = 0; i < n; ++i) sst += (y[i] - ds->ymean) * (y[i] - ds->ymean);
-  ds->sst = sst;
-  double yy = 0.0;
-  for (int64_t i = 0; i < n; ++i) yy += y[i] * y[i];
-  ds->yy = yy;
+  // mean and total sum of squares of y (rils_rols_cpp.cpp:41-43) in the fixed CSUM order
+  ds->ysum = rr_csum(y, (long)n);
+  ds->ymean = ds->ysum / (double)n;
+  rr_csum_acc acc;
+  rr_csum_init(&acc);
+  for (int64_t i = 0; i < n; ++i) rr_csum_add(&acc, (y[i] - ds->ymean) * (y[i] - ds->ymean));
+  ds->sst = rr_csum_total(&acc);
+  rr_csum_init(&acc);
+  for (int64_t i = 0; i < n; ++i) rr_csum_add(&acc, y[i] * y[i]);
+  ds->yy = rr_csum_total(&acc);
   const size_t b64 = sizeof(double) * ds->n_pad * cols, b32 = sizeof(float) * ds->n_pad * cols;
   const size_t y64b = sizeof(double) * ds->n_pad, y32b = sizeof(float) * ds->n_pad;
   if (cudaMalloc(&ds->X64, b64) != cudaSuccess || cudaMalloc(&ds->X32, b32) != cudaSuccess ||
@@ -814,8 +854,9 @@ int64_t rrg_last_round_launches(const rrg_context* ctx) { return ctx ? ctx->last
 
 int32_t rrg_last_round_stats(const rrg_context* ctx, int64_t* out, int32_t n) {
   if (!ctx || !out || n <= 0) return 0;
-  const int64_t v[4] = {ctx->last_launches, ctx->last_plain_routed, ctx->last_fallback, ctx->last_pass2};
-  const int32_t k = n < 4 ? n : 4;
+  int64_t v[4 + kFbReasons] = {ctx->last_launches, ctx->last_plain_routed, ctx->last_fallback, ctx->last_pass2};
+  for (int i = 0; i < kFbReasons; ++i) v[4 + i] = ctx->last_reasons[i];
+  const int32_t k = n < 4 + kFbReasons ? n : 4 + kFbReasons;
   for (int32_t i = 0; i < k; ++i) out[i] = v[i];
   return k;
 }

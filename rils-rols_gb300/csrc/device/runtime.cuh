@@ -46,10 +46,10 @@ struct rrg_context {
   rrd::DevBatch dev{};
   std::vector<rrg_cand> host_cands;
   // plain scratch
-  DevBuf d_A, d_S, d_pc, d_partial, d_list;
+  DevBuf d_A, d_S, d_pc, d_partial, d_list, d_redo;
   HostBuf h_pc, h_list;
   // mixed scratch
-  DevBuf d_gram, d_terms, d_mlist, d_fallback, d_sse1;
+  DevBuf d_gram, d_terms, d_mlist, d_fallback, d_sse1, d_probe, d_nanrow;
   HostBuf h_mlist, h_fallback;
   DevBuf mixed_scratch;
   // results
@@ -64,7 +64,11 @@ struct rrg_context {
   int64_t launches = 0, last_launches = 0;
   // mixed-round statistics of the last round
   int64_t last_fallback = 0, last_plain_routed = 0, last_pass2 = 0;
+  int64_t last_reasons[16] = {0};
   int32_t mixed_tile_override = 0;
+  // certified bound on the relative fitness error of a mixed result; larger
+  // bounds are re-scored by the FP64 path
+  double cert_tol = 5e-7;
   // optional per-phase device timing (CUDA events on the context stream)
   bool timing = false;
   enum Phase { P_GRAM = 0, P_SOLVE, P_RESID, P_FINAL, P_PLAIN_EVAL, P_PLAIN_QR, P_PLAIN_RESID, P_COUNT };
@@ -78,9 +82,12 @@ struct rrg_context {
 
   rrg_status stage_batch(const rrg_batch* b);
   // plain FP64 over `list` (absolute candidate indices) or over [lo, hi) when list is empty
+  // tiled_any: use the tiled QR on tall data whatever the candidate count;
+  // redo_sensitive: re-solve rounding-sensitive tiled candidates directly
   rrg_status run_plain(const rrg_dataset* ds, int32_t lo, int32_t hi, bool predict_only,
-                       const std::vector<int32_t>* list = nullptr, uint32_t flags_or = 0);
-  rrg_status run_mixed(const rrg_dataset* ds, int32_t n_cand);
+                       const std::vector<int32_t>* list = nullptr, uint32_t flags_or = 0, bool tiled_any = false,
+                       bool redo_sensitive = true);
+  rrg_status run_mixed(const rrg_dataset* ds, int32_t n_cand, bool certify);
   rrg_status submit(rrg_dataset* ds, const rrg_batch* b, int32_t precision, rrg_result* results, double* coefs);
   rrg_status wait(int32_t timeout_ms);
   ~rrg_context();

@@ -89,7 +89,7 @@ int32_t rrh_set_backend(rrh_model* m, const rrh_backend* be) {
 }
 
 int32_t rrh_set_precision(rrh_model* m, int32_t p) {
-  if (!m || (p != RRG_PLAIN_FP64 && p != RRG_MIXED)) return RRG_E_INVALID;
+  if (!m || (p != RRG_PLAIN_FP64 && p != RRG_MIXED && p != RRG_MIXED_CERTIFIED)) return RRG_E_INVALID;
   m->search.set_precision(p);
   return RRG_OK;
 }

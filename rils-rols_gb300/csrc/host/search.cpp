@@ -1,6 +1,8 @@
 // Host search driver; see search.h.
 #include "search.h"
 
+#include "../common/rr_sum.h"
+
 #include <algorithm>
 #include <cmath>
 #include <iostream>
@@ -398,16 +400,18 @@ std::vector<int> Search::relevant_features(const std::vector<std::vector<double>
     std::iota(rel.begin(), rel.end(), 0);
     return rel;
   }
-  // R2(X[i], y) with sequential sums (rils_rols_cpp.cpp:40-45, 753-770)
+  // R2(X[i], y) (rils_rols_cpp.cpp:40-45, 753-770), sums in the fixed CSUM order
   std::vector<std::tuple<double, int>> by_r2;
   for (int i = 0; i < feat_cnt; ++i) {
     const auto& a = X[i];
-    double s = 0;
-    for (double v : a) s += v;
-    const double avg = s / (double)a.size();
-    double ssr = 0, sst = 0;
-    for (size_t r = 0; r < a.size(); ++r) ssr += (a[r] - y[r]) * (a[r] - y[r]);
-    for (size_t r = 0; r < a.size(); ++r) sst += (a[r] - avg) * (a[r] - avg);
+    const double avg = rr_csum(a.data(), (long)a.size()) / (double)a.size();
+    rr_csum_acc acc;
+    rr_csum_init(&acc);
+    for (size_t r = 0; r < a.size(); ++r) rr_csum_add(&acc, (a[r] - y[r]) * (a[r] - y[r]));
+    const double ssr = rr_csum_total(&acc);
+    rr_csum_init(&acc);
+    for (size_t r = 0; r < a.size(); ++r) rr_csum_add(&acc, (a[r] - avg) * (a[r] - avg));
+    const double sst = rr_csum_total(&acc);
     by_r2.emplace_back(1 - ssr / sst, i);
   }
   std::sort(by_r2.begin(), by_r2.end(), std::greater<>());

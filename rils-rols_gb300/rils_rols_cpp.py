@@ -13,7 +13,7 @@ import ctypes as C
 import numpy as np
 
 from rils_rols_gb300 import _lib
-from rils_rols_gb300._lib import RRG_MIXED, RRG_PLAIN_FP64
+from rils_rols_gb300._lib import RRG_MIXED, RRG_MIXED_CERTIFIED, RRG_PLAIN_FP64
 
 
 class rils_rols:  # noqa: N801 - name of the reference class
@@ -35,7 +35,8 @@ class rils_rols:  # noqa: N801 - name of the reference class
                    "rrh_set_backend")
 
     def set_precision(self, precision: str | int) -> None:
-        p = {"plain": RRG_PLAIN_FP64, "fp64": RRG_PLAIN_FP64, "mixed": RRG_MIXED}.get(precision, precision)
+        p = {"plain": RRG_PLAIN_FP64, "fp64": RRG_PLAIN_FP64, "mixed": RRG_MIXED_CERTIFIED,
+             "mixed_uncertified": RRG_MIXED}.get(precision, precision)
         _lib.check(self._lib.rrh_set_precision(self._h, int(p)), "rrh_set_precision")
 
     def counters(self) -> dict:

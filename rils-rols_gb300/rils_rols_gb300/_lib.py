@@ -13,7 +13,7 @@ from pathlib import Path
 LIB_PATH = Path(__file__).resolve().parent / "librils_rols_gb300.so"
 
 RRG_OK, RRG_E_INVALID, RRG_E_CUDA, RRG_E_NO_DEVICE, RRG_E_TIMEOUT, RRG_E_TOO_LARGE, RRG_E_OOM, RRG_E_DEVICE_FAULT = range(8)
-RRG_PLAIN_FP64, RRG_MIXED = 0, 1
+RRG_PLAIN_FP64, RRG_MIXED, RRG_MIXED_CERTIFIED = 0, 1, 2
 RRG_UNTUNED, RRG_TUNED = 0, 1
 RRG_F_NONFINITE, RRG_F_RANK_DEFICIENT, RRG_F_QR_FALLBACK, RRG_F_VERIFIED_FP64, RRG_F_TOO_LARGE = 1, 2, 4, 8, 16
 RRG_MAX_TERMS = 64

@@ -17,10 +17,11 @@ from dataclasses import dataclass
 import numpy as np
 
 from . import _lib
-from ._lib import RRG_MIXED, RRG_PLAIN_FP64, RRG_TUNED, RRG_UNTUNED, Batch, Cand, Factor, Result, check
+from ._lib import RRG_MIXED, RRG_MIXED_CERTIFIED, RRG_PLAIN_FP64, RRG_TUNED, RRG_UNTUNED, Batch, Cand, Factor, Result, check
 
 PLAIN = RRG_PLAIN_FP64
 MIXED = RRG_MIXED
+CERTIFIED = RRG_MIXED_CERTIFIED
 
 
 @dataclass
@@ -77,6 +78,22 @@ def encode(trees: list[str], tuned: bool = True) -> EncodedBatch:
     return EncodedBatch(cands, factors, code, consts, n_coefs)
 
 
+def candidates(tree: str, d: int, local_search: bool = True, classification: bool = False) -> list[str]:
+    """The candidates one search step generates from `tree` (all_candidates of
+    rils_rols_cpp.cpp:348-443), in prefix form, in the reference's order."""
+    lib = _lib.load()
+    cap = 1 << 22
+    while True:
+        buf = C.create_string_buffer(cap)
+        r = lib.rrh_candidates(tree.encode(), int(local_search), int(d), int(classification), buf, cap)
+        if r >= 0:
+            break
+        if r == -1 or -r <= cap:
+            raise _lib.RRGError(_lib.RRG_E_INVALID, "rrh_candidates")
+        cap = -r + 16
+    return [line.split("\t")[1] for line in buf.value.decode().split("\n") if line]
+
+
 def decode_results(res: np.ndarray, coefs: np.ndarray, batch: EncodedBatch) -> dict:
     out = {k: res[k].copy() for k in ("loss", "rmse", "size", "rank", "flags")}
     cl = []
@@ -104,10 +121,15 @@ class Context:
     def last_round_launches(self) -> int:
         return int(self.lib.rrg_last_round_launches(self.h))
 
+    REASONS = ("probe_nonfinite", "fp64_inf", "fp32_overflow", "nan_rank", "rank", "ill_cond", "snap", "drop",
+               "one_pass", "cert", "other_nan")
+
     def last_round_stats(self) -> dict:
-        out = (C.c_int64 * 4)()
-        self.lib.rrg_last_round_stats(self.h, out, 4)
-        return {"launches": out[0], "plain_routed": out[1], "fp64_fallback": out[2], "residual_pass": out[3]}
+        out = (C.c_int64 * 15)()
+        self.lib.rrg_last_round_stats(self.h, out, 15)
+        d = {"launches": out[0], "plain_routed": out[1], "fp64_rescored": out[2], "residual_pass": out[3]}
+        d["rescore_reasons"] = {r: out[4 + i] for i, r in enumerate(self.REASONS) if out[4 + i]}
+        return d
 
     PHASES = ("mixed_gram", "mixed_solve", "mixed_residual", "finalize", "fp64_eval", "fp64_qr", "fp64_residual")
 

@@ -159,3 +159,28 @@ def serving_job_data(job: dict):
     _, y = finite_target(rng, X, job["size"])
     y = y + rng.normal(0.0, 0.01 * np.std(y), job["n"])
     return X, y
+
+
+# Intermediate models of a search on the 1M-row regression problem (prefix
+# form), from a single product term to the full generating formula; the
+# local-search rounds around them are the benchmark's candidate batches.
+REGRESSION_1M_TRAJECTORY = [
+    "mul c:2.5 mul x0 x1",
+    "add mul c:2.5 mul x0 x1 c:1.1",
+    "add mul c:2.5 mul x0 x1 mul c:0.7 exp mul c:0.3 x4",
+    "add mul c:2.48 mul x0 x1 mul c:0.93 exp x4",
+    "add add mul c:2.49 mul x0 x1 mul c:0.71 exp mul c:0.29 x4 mul c:-0.98 sin x2",
+    "add add mul c:2.5 mul x0 x1 mul c:0.7 exp mul c:0.3 x4 mul c:-1 div sin x2 add c:1 sqr x3",
+    "add add mul c:2.5 mul x0 x1 mul c:0.7 exp mul c:0.3 x4 div sin x2 sqr x3",
+    "sub add mul c:2.5 mul x0 x1 mul c:0.7 exp mul c:0.3 x4 div sin x2 add c:1 mul x3 x3",
+]
+
+
+def ls_round_batch(d: int = 5, trajectory=None) -> list[str]:
+    """Local-search candidates (tuned fitness inputs) of every model in the
+    trajectory, concatenated in round order."""
+    from .fitness import candidates
+    out = []
+    for t in trajectory or REGRESSION_1M_TRAJECTORY:
+        out.extend(candidates(t, d, local_search=True))
+    return out

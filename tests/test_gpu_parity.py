@@ -1,15 +1,18 @@
 """Device fitness path against the oracle and the reference's golden vectors.
 
-Plain FP64: every fitness within 1e-10 relative of the oracle (which is
-bit-exact with the reference), same size, same NaN sentinel.
-Mixed: penalised fitness within the tolerances below of the FP64 oracle.
+Plain FP64, one block per candidate (every round whose rows fit one block's
+pass, which is every round of the search on small data): bit-identical to the
+oracle, which is bit-identical to the reference.  Plain FP64 through the tiled
+QR (tall data, few candidates): every fitness within 1e-10 relative, same
+size, same NaN sentinel.  Mixed: penalised fitness within the tolerances
+below of the FP64 oracle.
 """
 import numpy as np
 import pytest
 
 from oracle import pyoracle
 from rils_rols_gb300 import synth
-from rils_rols_gb300.fitness import MIXED, PLAIN, Context, encode
+from rils_rols_gb300.fitness import CERTIFIED, MIXED, PLAIN, Context, encode
 
 pytestmark = pytest.mark.gpu
 
@@ -46,8 +49,13 @@ def check_plain(dev, ora, tag):
     assert np.all(rel_err(dev["rmse"][ok], ora["rmse"][ok]) <= REL_PLAIN + 1e-300), tag
 
 
+def same_bits(a, b):
+    a, b = np.asarray(a, dtype=np.float64), np.asarray(b, dtype=np.float64)
+    return np.all((a == b) | (np.isnan(a) & np.isnan(b)))
+
+
 @pytest.mark.parametrize("name", ["toy", "rand257x3", "cls120x4", "tiny3x2"])
-def test_plain_matches_golden(ctx, golden, name):
+def test_plain_bit_exact_with_golden(ctx, golden, name):
     spec = golden("fitness")[name]
     X, y = np.array(spec["X"]), np.array(spec["y"])
     ds = ctx.dataset(X, y)
@@ -56,10 +64,15 @@ def test_plain_matches_golden(ctx, golden, name):
     for tuned in (True, False):
         b = encode(trees, tuned=tuned)
         dev, ora = ds.evaluate(b, PLAIN), ods.evaluate(b)
-        check_plain(dev, ora, (name, tuned))
         key = "tuned" if tuned else "untuned"
-        gold = np.array([c[key]["fit"][2] for c in spec["cases"]])
-        assert np.array_equal(dev["size"], gold)
+        gold = np.array([c[key]["fit"] for c in spec["cases"]], dtype=np.float64)
+        assert same_bits(dev["loss"], gold[:, 0]), (name, tuned)
+        assert same_bits(dev["rmse"], gold[:, 1]), (name, tuned)
+        assert np.array_equal(dev["size"], gold[:, 2].astype(int)), (name, tuned)
+        assert same_bits(dev["loss"], ora["loss"]) and same_bits(dev["rmse"], ora["rmse"])
+        if tuned:
+            for i in range(len(trees)):
+                assert same_bits(dev["coefs"][i], ora["coefs"][i]), trees[i]
 
 
 def test_plain_tall_tsqr_matches_oracle(ctx):
@@ -71,13 +84,15 @@ def test_plain_tall_tsqr_matches_oracle(ctx):
     check_plain(ds.evaluate(b, PLAIN), ods.evaluate(b, threads=8), "tsqr")
 
 
-def test_plain_batched_medium_matches_oracle(ctx):
-    X, y, trees, _ = synth.batched_fitness(n=3000, d=4, n_trees=400, seed=5, max_size=40)
+def test_plain_batched_medium_bit_exact(ctx):
+    X, y, trees, _ = synth.batched_fitness(n=40_000, d=4, n_trees=400, seed=5, max_size=40)
     ds = ctx.dataset(X, y)
     ods = pyoracle.OracleDataset(X, y)
     for tuned in (True, False):
         b = encode(trees, tuned=tuned)
-        check_plain(ds.evaluate(b, PLAIN), ods.evaluate(b, threads=8), ("medium", tuned))
+        dev, ora = ds.evaluate(b, PLAIN), ods.evaluate(b, threads=8)
+        assert same_bits(dev["loss"], ora["loss"]) and same_bits(dev["rmse"], ora["rmse"]), tuned
+        assert np.array_equal(dev["size"], ora["size"])
 
 
 def test_predict_matches_oracle(ctx):
@@ -87,34 +102,51 @@ def test_predict_matches_oracle(ctx):
     for t in trees:
         got = ds.predict(t)
         want = ods.predict(encode([t], tuned=False))
-        fin = np.isfinite(want)
-        assert np.array_equal(np.isfinite(got), fin)
-        assert np.all(rel_err(got[fin], want[fin]) <= 1e-12)
+        assert same_bits(got, want), t
 
 
-def test_mixed_close_to_fp64_oracle(ctx):
-    X, y, trees, _ = synth.batched_fitness(n=20_000, d=6, n_trees=600, seed=13)
+@pytest.mark.parametrize("n,d,seed", [(20_000, 6, 13), (3000, 3, 4), (300, 2, 5)])
+def test_mixed_certified_against_fp64_oracle(ctx, n, d, seed):
+    # every mixed fitness within 1e-6 relative of the FP64 oracle (the
+    # certification re-scores in FP64 whatever it cannot bound), the same NaN
+    # sentinels, the same best candidate
+    X, y, trees, _ = synth.batched_fitness(n=n, d=d, n_trees=600, seed=seed)
     ds = ctx.dataset(X, y)
     ods = pyoracle.OracleDataset(X, y)
+    for tuned in (True, False):
+        b = encode(trees, tuned=tuned)
+        mix, ora = ds.evaluate(b, CERTIFIED), ods.evaluate(b, threads=8)
+        assert np.array_equal(mix["loss"] == 1000, ora["loss"] == 1000), tuned
+        assert np.array_equal(mix["size"], ora["size"]), tuned
+        ok = ora["loss"] != 1000
+        fv_m = fitness_value(mix["loss"], mix["rmse"], mix["size"])[ok]
+        fv_o = fitness_value(ora["loss"], ora["rmse"], ora["size"])[ok]
+        err = rel_err(fv_m, fv_o)
+        assert np.all(err <= 1e-6), (tuned, float(err.max()))
+        best = lambda r: int(np.argmin(np.where(ok, fitness_value(r["loss"], r["rmse"], r["size"]), np.inf)))  # noqa
+        assert best(mix) == best(ora), tuned
+
+
+def test_mixed_uncertified_close_to_fp64(ctx):
+    # the fast mixed form: same NaN sentinels, most fitnesses within 1e-6
+    X, y, trees, _ = synth.batched_fitness(n=20_000, d=6, n_trees=600, seed=13)
+    ds = ctx.dataset(X, y)
     b = encode(trees, tuned=True)
-    mix, ora = ds.evaluate(b, MIXED), ods.evaluate(b, threads=8)
+    mix, ora = ds.evaluate(b, MIXED), pyoracle.OracleDataset(X, y).evaluate(b, threads=8)
     assert np.array_equal(mix["loss"] == 1000, ora["loss"] == 1000)
-    ok = (ora["loss"] != 1000) & np.isfinite(ora["loss"]) & np.isfinite(ora["rmse"])
-    fv_m = fitness_value(mix["loss"], mix["rmse"], mix["size"])[ok]
-    fv_o = fitness_value(ora["loss"], ora["rmse"], ora["size"])[ok]
-    err = rel_err(fv_m, fv_o)
-    assert np.median(err) <= 1e-6
-    assert np.mean(err <= 1e-6) >= 0.95
-    # the best candidate is the same
-    assert np.argmin(np.where(ok, fitness_value(mix["loss"], mix["rmse"], mix["size"]), np.inf)) == \
-        np.argmin(np.where(ok, fitness_value(ora["loss"], ora["rmse"], ora["size"]), np.inf))
+    ok = ora["loss"] != 1000
+    err = rel_err(fitness_value(mix["loss"], mix["rmse"], mix["size"])[ok],
+                  fitness_value(ora["loss"], ora["rmse"], ora["size"])[ok])
+    # rank cuts (pivoted Cholesky) and the drop / snap rules may decide
+    # differently from the FP64 QR for exactly collinear factor sets
+    assert np.median(err) <= 1e-8 and np.mean(err <= 1e-6) >= 0.75
 
 
 def test_round_is_deterministic_and_mix_independent(ctx):
     # the same candidate scores bit-identically alone and inside a larger batch
     X, y, trees, _ = synth.batched_fitness(n=8192, d=4, n_trees=300, seed=21)
     ds = ctx.dataset(X, y)
-    for prec in (PLAIN, MIXED):
+    for prec in (PLAIN, MIXED, CERTIFIED):
         full = ds.evaluate(encode(trees, tuned=True), prec)
         for i in (0, 17, 299):
             one = ds.evaluate(encode([trees[i]], tuned=True), prec)

@@ -30,8 +30,11 @@ def test_oracle_matches_reference(golden, lib, name):
                                     BUF, len(BUF))
                 assert r >= 0
                 model, prefix = BUF.value.decode().split("\t")
-                assert model == case[key]["model"], (case["tree"], model)
-                assert prefix == case[key]["prefix"], (case["tree"], prefix)
+                # the sign of a NaN coefficient depends on operand order inside
+                # the compiled arithmetic, not on the algorithm
+                unsign = lambda t: t.replace("-nan", "nan")  # noqa: E731
+                assert unsign(model) == unsign(case[key]["model"]), (case["tree"], model)
+                assert unsign(prefix) == unsign(case[key]["prefix"]), (case["tree"], prefix)
 
 
 def test_oracle_threads_do_not_change_results(golden):
