@@ -287,7 +287,7 @@ def run_ours(args):
     res["roofline"] = {"kernel": "mixed_pass_kernel (gram pass)", "bound": "hbm", "achieved": achieved,
                        "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                        "traffic": read_profile_traffic(), "peak_source": "measured" if peaks else "fallback",
-                       "note": "issue-bound interpreter (FP32/SFU): the HBM roofline is far away; see DESIGN.md"}
+                       "note": "instruction-issue-bound interpreter (FP32 / ALU): far below the HBM roofline"}
     res["phase_ms_per_step"] = {k: v / args.steps for k, v in phase_ms.items() if v > 0}
     res["clocks"] = clk.summary()
     if args.quick:

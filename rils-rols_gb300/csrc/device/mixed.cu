@@ -7,9 +7,10 @@
 //                 (cp.async.bulk + mbarrier) and shared by every candidate of
 //                 a work unit; one warp interprets one candidate's factor
 //                 programs on 4 rows per lane in FP32 and accumulates the
-//                 factor Gram matrix, the factor sums and X^T y with
-//                 compensated (Kahan) FP32 sums; warps reduce with
-//                 double-float shuffles and write one partial per tile;
+//                 factor Gram matrix, the factor sums and X^T y as exact
+//                 products (FMA TwoProduct) added into double-float (hi, lo)
+//                 pairs; warps reduce with double-float shuffles and write
+//                 one partial per tile;
 //   solve         one warp per candidate: FP64 reduction of the tile partials,
 //                 symmetric-pivoted Cholesky in FP64 (pivot = largest
 //                 remaining column norm, as in column-pivoted QR), one step of
