@@ -175,6 +175,31 @@ rrg_status rrg_eval(rrg_dataset* ds, const rrg_batch* batch, int32_t precision, 
  */
 rrg_status rrg_predict(rrg_dataset* ds, const rrg_batch* batch, double* values);
 
+/*
+ * Allocation-free scoring of one candidate (batch->n_cand == 1) by the plain
+ * FP64 path, for callers that may not allocate device memory or have a
+ * library allocate it for them (a framework that owns every device byte
+ * through its own pool; a loop that cannot take cudaMalloc / cudaFree
+ * stalls).  No counterpart in the reference: it is the per-candidate
+ * tune_constants + fitness pair (rils_rols_cpp.cpp:445-541) without a
+ * context or dataset object.
+ *   X_col: device, d columns of ld >= n FP64 values (column j at X_col + j*ld);
+ *   y: device, n values; result: device, one rrg_result; coefs: device,
+ *   n_factors + 1 doubles for a tuned candidate (may be NULL when untuned);
+ *   batch: host; stream: a cudaStream_t (NULL = legacy default stream).
+ * Runs on the current device and returns after the stream has finished it.
+ * Scratch is a fixed 32 MiB device array inside the library (about
+ * (2k + 1) * ld * 8 bytes are needed for k = n_factors + 1); a larger call
+ * returns RRG_E_TOO_LARGE and allocates nothing.  The first call on each
+ * device looks up the scratch address: make it before any stream capture
+ * begins on that device.  Calls share the scratch, so calls that overlap on
+ * a device race: serialise them.  Results equal rrg_eval(RRG_PLAIN_FP64) on
+ * the same data when that call solves directly (n < 65536); above that
+ * rrg_eval may solve by tiled QR, which agrees within 1e-10 relative.
+ */
+rrg_status rrg_eval_plain_noalloc(const double* X_col, int64_t ld, const double* y, int64_t n, int32_t d,
+                                  const rrg_batch* batch, rrg_result* result, double* coefs, void* stream);
+
 /* Host-side check of a batch against a dataset of d features: opcodes,
  * feature / constant / slot indices and spill depths.  rrg_round_submit runs
  * the same check; no device is needed. */
