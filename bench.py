@@ -278,7 +278,7 @@ def run_ours(args):
            "config": config(args.n, B),
            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
            "gpu_launches": int(launches), "round_stats": stats}
-    gram_ms, gram_n = phase_ms.get("mixed_gram", 0.0), max(1, phase_n.get("mixed_gram", 1))
+    gram_ms, gram_n = phase_ms.get("factor_eval", 0.0), max(1, phase_n.get("factor_eval", 1))
     avg_launch_s = gram_ms / 1e3 / gram_n
     algo_bytes = args.n * (N_FEAT + 1) * 4  # X (FP32) and y read once per launch
     peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}

@@ -45,8 +45,9 @@ typedef enum {
 /* Arithmetic of one round. */
 typedef enum {
   RRG_PLAIN_FP64 = 0,        /* FP64 evaluation, column-pivoted Householder OLS, FP64 residual */
-  RRG_MIXED = 1,             /* FP32 evaluation, exact-product Gram sums, FP64 pivoted Cholesky + refinement;
-                                non-finite and ill-conditioned systems re-solved in FP64 */
+  RRG_MIXED = 1,             /* double-float (FP32-pair) evaluation of the round's distinct factors, Gram sums
+                                per distinct factor pair, FP64 pivoted Cholesky + refinement; non-finite and
+                                ill-conditioned systems re-solved by the FP64 path */
   RRG_MIXED_CERTIFIED = 2    /* RRG_MIXED, and every result whose fitness error cannot be bounded below
                                 5e-7 relative (or whose rank / drop / snap decision is ambiguous) is
                                 re-scored by the FP64 path: results equal the FP64 path's within 1e-6 */
@@ -231,9 +232,10 @@ void* rrg_context_stream(const rrg_context* ctx);
  * the context stream); off by default. */
 rrg_status rrg_context_set_timing(rrg_context* ctx, int32_t on);
 /* Device milliseconds and launch counts of the last completed round, per
- * phase: [0] mixed gram pass, [1] mixed solve, [2] mixed residual pass,
- * [3] finalize, [4] FP64 evaluation, [5] FP64 QR, [6] FP64 residual.
- * Returns the number of phases written. */
+ * phase: [0] mixed factor-table evaluation (with the self sums), [1] mixed
+ * solve (pair totals, probes, Cholesky), [2] mixed residual pass,
+ * [3] finalize, [4] FP64 evaluation, [5] FP64 QR, [6] FP64 residual,
+ * [7] mixed pair sums.  Returns the number of phases written. */
 int32_t rrg_last_round_timing(const rrg_context* ctx, double* ms, int64_t* launches, int32_t n);
 
 #ifdef __cplusplus

@@ -21,14 +21,16 @@ struct DevBatch {
   const rrg_factor* factors;
   const uint32_t* code;
   const double* consts;
-  const float* consts32;
+  const float* consts32;    // constants as double-floats: high parts
+  const float* consts32lo;  // low parts
   int32_t n_cand, n_factors, n_code, n_consts;
 };
 
 // Resident dataset: d columns of n_pad values each (rows >= n are zero).
 struct DevData {
   const double* X64;
-  const float* X32;
+  const float* X32;    // X as double-floats: high parts (the FP32 rounding of X)
+  const float* X32lo;  // low parts
   const double* y64;
   const float* y32;    // y rounded to FP32 (high part)
   const float* y32lo;  // y - y32, rounded to FP32 (low part)

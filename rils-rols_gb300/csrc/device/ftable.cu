@@ -1,0 +1,391 @@
+// Factor table of a mixed round: double-float evaluation of the distinct
+// factor programs, Gram sums per distinct pair, and the residual pass.
+//
+//   fac_eval      block = (group of factors, row chunk).  The chunk of X and
+//                 y (high and low parts) is staged in shared memory by TMA
+//                 bulk copies (cp.async.bulk + mbarrier, bounded wait) when
+//                 it fits, and every factor of the group is interpreted on
+//                 it in double-float arithmetic, 2 rows per thread, with the
+//                 semantics of node::evaluate_inner (node.cpp:23-95).
+//                 Values go to the table F in HBM (rows >= n set to 0); the
+//                 self sums  sum f*f, sum f, sum f*y  of the chunk are formed
+//                 on the way;
+//   pair_sum      block = (factor a with its partners b, row block): a's
+//                 values stay in registers, each partner column is streamed
+//                 once, sum a*b in double-float arithmetic;
+//   pair_reduce   FP64 totals of the partials, in chunk order;
+//   ftab_resid    the rebuilt sum  sum_i c_i f_i  (drop / snap rules of
+//                 rils_rols_cpp.cpp:488-517) from the table, its residual
+//                 against y and the squared residuals, all double-float.
+#include <cfloat>
+#include <cstdint>
+
+#include "common.cuh"
+#include "dfeval.cuh"
+#include "ftable.cuh"
+#include "tma.cuh"
+
+namespace rrd {
+
+namespace {
+
+constexpr int kPairPerThread = kPairRows / (2 * kPairThreads);  // row pairs per thread (8)
+
+__device__ __forceinline__ dfl shfl_dfl(dfl v, int o) {
+  return dfl_make(__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o));
+}
+__device__ __forceinline__ dfl warp_dfl_sum(dfl v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = dfl_add(v, shfl_dfl(v, o));
+  return v;
+}
+
+// One table program on 2 consecutive rows (r, r + 1 of the chunk); X column
+// j has its high parts at xh + j * ldx and its low parts at xl + j * ldx;
+// table column t (an earlier level) at tb + t * ldtab.
+__device__ __forceinline__ bool eval_fac2(const uint32_t* code, int len, const float* __restrict__ K,
+                                          const float* __restrict__ Klo, const float* xh, const float* xl,
+                                          int64_t ldx, const float2* tb, int64_t ldtab, int r, float4* st,
+                                          dfl& o0, dfl& o1) {
+  dfl t0 = dfl_make(0.f, 0.f), t1 = t0;
+  int sp = 0;
+  auto ldv = [&](uint32_t j, dfl& u0, dfl& u1) {
+    const float2 h = *reinterpret_cast<const float2*>(xh + (int64_t)j * ldx + r);
+    const float2 l = *reinterpret_cast<const float2*>(xl + (int64_t)j * ldx + r);
+    u0 = dfl_make(h.x, l.x);
+    u1 = dfl_make(h.y, l.y);
+  };
+  auto ldt = [&](uint32_t t, dfl& u0, dfl& u1) {
+    const float4 v = *reinterpret_cast<const float4*>(tb + (int64_t)t * ldtab + r);
+    u0 = dfl_make(v.x, v.y);
+    u1 = dfl_make(v.z, v.w);
+  };
+  for (int pc = 0; pc < len; ++pc) {
+    const uint32_t w = code[pc];
+    const int op = (int)(w & 0xffu);
+    const uint32_t arg = w >> 8;
+    switch (op) {
+      case RRG_OP_LDV: ldv(arg, t0, t1); break;
+      case RRG_OP_LDC: t0 = t1 = dfl_make(__ldg(K + arg), __ldg(Klo + arg)); break;
+      case RRG_OP_PSV:
+        if (sp >= kMixedStackCap) return false;
+        st[32 * sp++] = make_float4(t0.hi, t0.lo, t1.hi, t1.lo);
+        ldv(arg, t0, t1);
+        break;
+      case RRG_OP_PSC:
+        if (sp >= kMixedStackCap) return false;
+        st[32 * sp++] = make_float4(t0.hi, t0.lo, t1.hi, t1.lo);
+        t0 = t1 = dfl_make(__ldg(K + arg), __ldg(Klo + arg));
+        break;
+      case kOpLDT: ldt(arg, t0, t1); break;
+      case kOpPST:
+        if (sp >= kMixedStackCap) return false;
+        st[32 * sp++] = make_float4(t0.hi, t0.lo, t1.hi, t1.lo);
+        ldt(arg, t0, t1);
+        break;
+      case RRG_OP_EMIT:
+        o0 = t0;
+        o1 = t1;
+        sp = 0;
+        break;
+      default:
+        if (op >= RRG_OP_SIN && op <= RRG_OP_SQR) {
+          t0 = df_unary(op, t0);
+          t1 = df_unary(op, t1);
+        } else {
+          const int kk = op - RRG_OP_BIN;
+          const int base = kk >> 3, src = (kk & 7) >> 1, dir = kk & 1;
+          dfl u0, u1;
+          if (src == RRG_SRC_S) {
+            if (sp <= 0) return false;
+            const float4 v = st[32 * --sp];
+            u0 = dfl_make(v.x, v.y);
+            u1 = dfl_make(v.z, v.w);
+          } else if (src == RRG_SRC_V) {
+            ldv(arg, u0, u1);
+          } else if (src == kSrcT) {
+            ldt(arg, u0, u1);
+          } else {
+            u0 = u1 = dfl_make(__ldg(K + arg), __ldg(Klo + arg));
+          }
+          if (dir == RRG_DIR_N) {
+            t0 = df_bin(base, u0, t0);
+            t1 = df_bin(base, u1, t1);
+          } else {
+            t0 = df_bin(base, t0, u0);
+            t1 = df_bin(base, t1, u1);
+          }
+        }
+    }
+  }
+  return true;
+}
+
+// shared-memory layout of fac_eval
+constexpr size_t kFacRedOff = 128;                                   // [warp][6] floats
+constexpr size_t kFacCodeOff = kFacRedOff + 256;
+constexpr size_t kFacStackOff = kFacCodeOff + sizeof(uint32_t) * kFacCodeSmem;
+constexpr size_t kFacXOff = kFacStackOff + sizeof(float4) * (kFacThreads / 32) * kMixedStackCap * 32;
+
+}  // namespace
+
+__global__ void __launch_bounds__(kFacThreads) fac_eval_kernel(FacEvalArgs a, int staged) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int2 grp = a.groups[blockIdx.x];
+  const int q = blockIdx.y;
+  const int d = a.ds.d;
+  const int64_t n = a.ds.n, n_pad = a.ds.n_pad;
+  const int64_t row0 = (int64_t)q * a.chunk;
+  const int rows = (int)min((int64_t)a.chunk, n_pad - row0);  // a multiple of 256
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem);
+  int* abort_flag = reinterpret_cast<int*>(smem + 16);
+  float* red = reinterpret_cast<float*>(smem + kFacRedOff);
+  uint32_t* code_s = reinterpret_cast<uint32_t*>(smem + kFacCodeOff);
+  float4* stk = reinterpret_cast<float4*>(smem + kFacStackOff);
+  // staged: column j high parts at xs + 2j * chunk, low parts chunk later; y after the d columns
+  float* xs = reinterpret_cast<float*>(smem + kFacXOff);
+  if (staged) {
+    if (tid == 0) {
+      mbar_init(bar, 1);
+      *abort_flag = 0;
+    }
+    fence_proxy_async();
+    __syncthreads();
+    if (tid == 0) {
+      const uint32_t bytes = (uint32_t)rows * (uint32_t)sizeof(float);
+      fence_proxy_async();
+      mbar_expect_tx(bar, bytes * 2u * (uint32_t)(d + 1));
+      for (int j = 0; j < d; ++j) {
+        tma_bulk_g2s(xs + (size_t)(2 * j) * a.chunk, a.ds.X32 + (int64_t)j * n_pad + row0, bytes, bar);
+        tma_bulk_g2s(xs + (size_t)(2 * j + 1) * a.chunk, a.ds.X32lo + (int64_t)j * n_pad + row0, bytes, bar);
+      }
+      tma_bulk_g2s(xs + (size_t)(2 * d) * a.chunk, a.ds.y32 + row0, bytes, bar);
+      tma_bulk_g2s(xs + (size_t)(2 * d + 1) * a.chunk, a.ds.y32lo + row0, bytes, bar);
+    }
+  }
+  // the group's programs are contiguous: stage them
+  const int base = a.meta[grp.x].x;
+  const int2 last = a.meta[grp.x + grp.y - 1];
+  const int total = last.x + last.y - base;
+  for (int i = tid; i < total; i += kFacThreads) code_s[i] = a.code[base + i];
+  if (staged && !mbar_wait_bounded(bar, 0)) atomicExch(abort_flag, 1);
+  __syncthreads();
+  if (staged && *abort_flag) {
+    if (tid == 0) atomicOr(a.status, ST_WAIT_TIMEOUT);
+    return;
+  }
+  const float* xh = staged ? xs : a.ds.X32 + row0;
+  const float* xl = staged ? xs + a.chunk : a.ds.X32lo + row0;
+  const int64_t ldx = staged ? 2 * (int64_t)a.chunk : n_pad;
+  const float* yh = staged ? xs + (size_t)(2 * d) * a.chunk : a.ds.y32 + row0;
+  const float* yl = staged ? xs + (size_t)(2 * d + 1) * a.chunk : a.ds.y32lo + row0;
+  const float2* tb = a.F + row0;
+  float4* st = stk + (size_t)warp * kMixedStackCap * 32 + lane;
+  for (int i = 0; i < grp.y; ++i) {
+    const int f = grp.x + i;
+    const int2 mt = a.meta[f];
+    const uint32_t* code = code_s + (mt.x - base);
+    dfl ff = dfl_make(0.f, 0.f), fs = ff, fy = ff;
+    unsigned long long first = ~0ull;
+    bool ok = true;
+    for (int r = 2 * tid; r < rows; r += kFacStep) {
+      dfl v0 = dfl_make(0.f, 0.f), v1 = v0;
+      ok = eval_fac2(code, mt.y, a.K, a.Klo, xh, xl, ldx, tb, n_pad, r, st, v0, v1) && ok;
+      const int64_t gr = row0 + r;
+      if (gr >= n) v0 = dfl_make(0.f, 0.f);
+      if (gr + 1 >= n) v1 = dfl_make(0.f, 0.f);
+      if (v0.hi != v0.hi) first = min(first, (unsigned long long)gr);
+      else if (v1.hi != v1.hi) first = min(first, (unsigned long long)(gr + 1));
+      *reinterpret_cast<float4*>(a.F + (int64_t)f * n_pad + gr) = make_float4(v0.hi, v0.lo, v1.hi, v1.lo);
+      const float2 yhv = *reinterpret_cast<const float2*>(yh + r);
+      const float2 ylv = *reinterpret_cast<const float2*>(yl + r);
+      ff = dfl_add(ff, dfl_mul(v0, v0));
+      ff = dfl_add(ff, dfl_mul(v1, v1));
+      fs = dfl_add(fs, v0);
+      fs = dfl_add(fs, v1);
+      fy = dfl_add(fy, dfl_mul(v0, dfl_make(yhv.x, ylv.x)));
+      fy = dfl_add(fy, dfl_mul(v1, dfl_make(yhv.y, ylv.y)));
+    }
+    if (!ok) atomicOr(a.status, ST_STACK);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long other = __shfl_xor_sync(0xffffffffu, first, o);
+      first = other < first ? other : first;
+    }
+    if (lane == 0 && first != ~0ull) atomicMin(a.fnan + f, first);
+    const dfl s0 = warp_dfl_sum(ff), s1 = warp_dfl_sum(fs), s2 = warp_dfl_sum(fy);
+    if (lane == 0) {
+      float* rw = red + warp * 6;
+      rw[0] = s0.hi; rw[1] = s0.lo;
+      rw[2] = s1.hi; rw[3] = s1.lo;
+      rw[4] = s2.hi; rw[5] = s2.lo;
+    }
+    __syncthreads();
+    if (tid < 3) {
+      dfl s = dfl_make(0.f, 0.f);
+      for (int w = 0; w < kFacThreads / 32; ++w) s = dfl_add(s, dfl_make(red[w * 6 + 2 * tid], red[w * 6 + 2 * tid + 1]));
+      a.P[(size_t)q * a.n_pairs + 3 * (size_t)f + tid] = make_float2(s.hi, s.lo);
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(kPairThreads) pair_sum_kernel(PairArgs a) {
+  __shared__ float red[kPairBatch][kPairThreads / 32][2];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int u = blockIdx.x % a.n_units;
+  const int qs = blockIdx.x / a.n_units;
+  const int4 U = a.units[u];
+  const int64_t row0 = (int64_t)qs * kPairRows;
+  const int rows = (int)min((int64_t)kPairRows, a.n_pad - row0);
+  const float2* fa = a.F + (int64_t)U.x * a.n_pad + row0;
+  float4 av[kPairPerThread];
+#pragma unroll
+  for (int s = 0; s < kPairPerThread; ++s) {
+    const int r = 2 * tid + 2 * kPairThreads * s;
+    av[s] = r < rows ? *reinterpret_cast<const float4*>(fa + r) : make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+  for (int p0 = U.y; p0 < U.z; p0 += kPairBatch) {
+    const int nb = min(kPairBatch, U.z - p0);
+    for (int j = 0; j < nb; ++j) {
+      const float2* fb = a.F + (int64_t)a.partner[p0 + j] * a.n_pad + row0;
+      dfl acc = dfl_make(0.f, 0.f);
+#pragma unroll
+      for (int s = 0; s < kPairPerThread; ++s) {
+        const int r = 2 * tid + 2 * kPairThreads * s;
+        if (r < rows) {
+          const float4 bv = *reinterpret_cast<const float4*>(fb + r);
+          acc = dfl_add(acc, dfl_mul(dfl_make(av[s].x, av[s].y), dfl_make(bv.x, bv.y)));
+          acc = dfl_add(acc, dfl_mul(dfl_make(av[s].z, av[s].w), dfl_make(bv.z, bv.w)));
+        }
+      }
+      const dfl v = warp_dfl_sum(acc);
+      if (lane == 0) {
+        red[j][warp][0] = v.hi;
+        red[j][warp][1] = v.lo;
+      }
+    }
+    __syncthreads();
+    if (tid < nb) {
+      dfl s = dfl_make(0.f, 0.f);
+      for (int w = 0; w < kPairThreads / 32; ++w) s = dfl_add(s, dfl_make(red[tid][w][0], red[tid][w][1]));
+      a.P[(size_t)qs * a.n_pairs + a.cross0 + p0 + tid] = make_float2(s.hi, s.lo);
+    }
+    __syncthreads();
+  }
+}
+
+// psum[p] = sum over chunks q (in order) of P[q][p], in FP64.
+__global__ void pair_reduce_kernel(const float2* P, int32_t n_pairs, int32_t n_chunks, int32_t p0, int32_t p1,
+                                   double* psum) {
+  const int p = p0 + blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= p1) return;
+  double s = 0.0;
+  for (int q = 0; q < n_chunks; ++q) {
+    const float2 v = P[(size_t)q * n_pairs + p];
+    s = __dadd_rn(s, __dadd_rn((double)v.x, (double)v.y));
+  }
+  psum[p] = s;
+}
+
+__global__ void __launch_bounds__(kResidThreads) ftab_resid_kernel(ResidArgs a) {
+  __shared__ float red[kResidThreads / 32][2];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int i = blockIdx.x % a.n2;
+  const int qs = blockIdx.x / a.n2;
+  const int li = a.list2[i];
+  const int c = a.mlist[li];
+  const rrg_cand cd = a.b.cands[c];
+  const bool tuned = cd.mode == RRG_TUNED;
+  const int m = tuned ? cd.n_factors : 1;
+  const MixedTerm& tm = a.terms[c];
+  const int64_t n = a.ds.n, n_pad = a.ds.n_pad;
+  const int64_t row0 = (int64_t)qs * kPairRows;
+  const int rows = (int)min((int64_t)kPairRows, n_pad - row0);
+  const float2* col[kMixedMaxM];
+#pragma unroll
+  for (int s = 0; s < kMixedMaxM; ++s)
+    col[s] = s < m ? a.F + (int64_t)a.cand_col[(size_t)li * kMixedMaxM + s] * n_pad + row0 : nullptr;
+  dfl acc = dfl_make(0.f, 0.f);
+  for (int r = 2 * tid; r < rows; r += 2 * kResidThreads) {
+    const int64_t gr = row0 + r;
+    float4 fv[kMixedMaxM];
+#pragma unroll
+    for (int s = 0; s < kMixedMaxM; ++s)
+      fv[s] = s < m ? *reinterpret_cast<const float4*>(col[s] + r) : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float2 yh = *reinterpret_cast<const float2*>(a.ds.y32 + gr);
+    const float2 yl = *reinterpret_cast<const float2*>(a.ds.y32lo + gr);
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      dfl yp = dfl_make(0.f, 0.f);
+      if (tuned) {
+        bool have = false;
+#pragma unroll
+        for (int t = 0; t <= kMixedMaxM; ++t) {
+          if (t > m) break;
+          const int kd = tm.kind[t];
+          if (kd == 0) continue;
+          dfl f = dfl_make(0.f, 0.f);
+#pragma unroll
+          for (int s = 0; s < kMixedMaxM; ++s)
+            if (s == t) f = u == 0 ? dfl_make(fv[s].x, fv[s].y) : dfl_make(fv[s].z, fv[s].w);
+          const dfl cf = dfl_make(tm.hi[t], tm.lo[t]);
+          const dfl term = kd == 1 ? cf : (kd == 2 ? f : dfl_mul(cf, f));
+          yp = have ? dfl_add(yp, term) : term;
+          have = true;
+        }
+      } else {
+        yp = u == 0 ? dfl_make(fv[0].x, fv[0].y) : dfl_make(fv[0].z, fv[0].w);
+      }
+      const dfl y = u == 0 ? dfl_make(yh.x, yl.x) : dfl_make(yh.y, yl.y);
+      const dfl e = dfl_sub(y, yp);
+      if (gr + u < n) acc = dfl_add(acc, dfl_mul(e, e));
+    }
+  }
+  const dfl v = warp_dfl_sum(acc);
+  if (lane == 0) {
+    red[warp][0] = v.hi;
+    red[warp][1] = v.lo;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    dfl s = dfl_make(0.f, 0.f);
+    for (int w = 0; w < kResidThreads / 32; ++w) s = dfl_add(s, dfl_make(red[w][0], red[w][1]));
+    a.sse[(size_t)c * a.n_chunks + qs] = (double)s.hi + (double)s.lo;
+  }
+}
+
+// ----------------------------------------------------------- launchers ----
+size_t fac_eval_smem(int d, int chunk, bool staged) {
+  return kFacXOff + (staged ? sizeof(float) * 2 * (size_t)(d + 1) * chunk : 0);
+}
+bool fac_allow_smem() {
+  return cudaFuncSetAttribute(fac_eval_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) ==
+         cudaSuccess;
+}
+bool launch_fac_eval(const FacEvalArgs& a, int n_groups, int n_chunks, bool staged, cudaStream_t st) {
+  if (n_groups <= 0 || n_chunks <= 0) return true;
+  fac_eval_kernel<<<dim3(n_groups, n_chunks), kFacThreads, fac_eval_smem(a.ds.d, a.chunk, staged), st>>>(
+      a, staged ? 1 : 0);
+  return cudaGetLastError() == cudaSuccess;
+}
+int pair_row_blocks(int64_t n_pad) { return (int)((n_pad + kPairRows - 1) / kPairRows); }
+bool launch_pair_sum(const PairArgs& a, int n_super, cudaStream_t st) {
+  if (a.n_units <= 0 || n_super <= 0) return true;
+  pair_sum_kernel<<<a.n_units * n_super, kPairThreads, 0, st>>>(a);
+  return cudaGetLastError() == cudaSuccess;
+}
+bool launch_pair_reduce(const float2* P, int32_t n_pairs, int32_t n_chunks, int32_t p0, int32_t p1, double* psum,
+                        cudaStream_t st) {
+  if (p1 <= p0) return true;
+  pair_reduce_kernel<<<(p1 - p0 + 255) / 256, 256, 0, st>>>(P, n_pairs, n_chunks, p0, p1, psum);
+  return cudaGetLastError() == cudaSuccess;
+}
+bool launch_ftab_resid(const ResidArgs& a, cudaStream_t st) {
+  if (a.n2 <= 0 || a.n_chunks <= 0) return true;
+  ftab_resid_kernel<<<a.n2 * a.n_chunks, kResidThreads, 0, st>>>(a);
+  return cudaGetLastError() == cudaSuccess;
+}
+
+}  // namespace rrd

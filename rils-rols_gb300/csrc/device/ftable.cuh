@@ -1,0 +1,83 @@
+// Factor table of a mixed round (ftable.cu).
+//
+// The candidates of one local-search round are perturbations of the same
+// model, so most of their top-level factors are shared: a round of the
+// 1M-row regression search holds about six times fewer distinct factor
+// programs than factor instances.  Each distinct factor is evaluated once
+// in double-float arithmetic (csrc/common/df32.h) into HBM, and each
+// distinct pair of factors is summed once.
+#pragma once
+#include "common.cuh"
+#include "mixed.cuh"
+
+namespace rrd {
+
+constexpr int kFacThreads = 256;      // evaluator block: 2 rows per thread
+constexpr int kFacStep = 2 * kFacThreads;
+constexpr int kFacCodeSmem = 2048;    // program words of one evaluator group in shared memory
+constexpr int kFacGroupMax = 64;      // factors per evaluator group
+constexpr int kFacStageBytes = 64 * 1024;  // X and y chunk (hi and lo) staged by TMA when it fits
+constexpr int kPairThreads = 256;
+constexpr int kPairBatch = 16;        // partners reduced together
+constexpr int kPairRows = 4096;       // rows per pair-sum / residual block
+constexpr int kResidThreads = 256;
+
+// Internal instructions of table programs (never in a submitted batch: the
+// batch validation rejects them): read table column `arg` of the same rows.
+constexpr int kOpLDT = 12;   // TOS = T[arg]
+constexpr int kOpPST = 13;   // spill TOS; TOS = T[arg]
+constexpr int kSrcT = 3;     // binary operand from table column `arg`
+
+// Self pairs of factor f sit at pair index 3f (f*f), 3f+1 (f*1), 3f+2 (f*y);
+// cross pairs follow from 3 * n_factors.
+struct FacEvalArgs {
+  DevData ds;
+  const uint32_t* code;      // distinct factor programs, each ending in EMIT 0
+  const int2* meta;          // [f] (code offset, length)
+  const int2* groups;        // [g] (first factor, count); a group's programs are contiguous
+  const float* K;            // constant pool, double-float high parts
+  const float* Klo;          // low parts
+  int32_t chunk;             // rows per chunk, a multiple of kFacStep
+  float2* F;                 // [column][n_pad] values (hi, lo); 0 on rows >= n.  Programs
+                             // read columns of earlier levels from it
+  float2* P;                 // [chunk][n_pairs] double-float partial sums
+  int32_t n_pairs;
+  unsigned long long* fnan;  // [f] first row with a NaN value
+  uint32_t* status;
+};
+
+struct PairArgs {
+  const float2* F;
+  int64_t n_pad;
+  const int4* units;         // [u] (a, first cross pair, end cross pair, 0)
+  int32_t n_units;
+  const int32_t* partner;    // [cross pair] factor b (pairs of a unit share a)
+  float2* P;                 // [row block][n_pairs]
+  int32_t n_pairs, cross0;   // pair index of cross pair 0
+};
+
+struct ResidArgs {
+  DevBatch b;
+  DevData ds;
+  const float2* F;
+  const int32_t* mlist;      // mixed list: list index -> candidate
+  const int32_t* list2;      // [i] list index of a candidate that needs the residual pass
+  int32_t n2;
+  const int32_t* cand_col;   // [list index][kMixedMaxM] table column of each factor
+  const MixedTerm* terms;    // [candidate]
+  int32_t n_chunks;          // row blocks of pair_row_blocks(n_pad)
+  double* sse;               // [candidate][row block]
+};
+
+bool launch_fac_eval(const FacEvalArgs& a, int n_groups, int n_chunks, bool staged, cudaStream_t st);
+size_t fac_eval_smem(int d, int chunk, bool staged);
+bool fac_allow_smem();
+// Row blocks of the pair sums and the residual pass.
+int pair_row_blocks(int64_t n_pad);
+bool launch_pair_sum(const PairArgs& a, int n_row_blocks, cudaStream_t st);
+// psum[p] for p in [p0, p1): FP64 sum over the first n_chunks rows of P.
+bool launch_pair_reduce(const float2* P, int32_t n_pairs, int32_t n_chunks, int32_t p0, int32_t p1, double* psum,
+                        cudaStream_t st);
+bool launch_ftab_resid(const ResidArgs& a, cudaStream_t st);
+
+}  // namespace rrd

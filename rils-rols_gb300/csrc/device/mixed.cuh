@@ -1,12 +1,19 @@
-// Batched mixed-precision fitness path (mixed.cu).
+// Mixed-precision fitness path: solve and probes (mixed.cu); the factor
+// table kernels are in ftable.cu.
 #pragma once
 #include "common.cuh"
 
 namespace rrd {
 
-constexpr int kMixedStackCap = 4;    // spill levels kept in shared memory per warp
-constexpr int kMixedCodeCap = 128;   // program words staged per warp
-constexpr int kMixedMaxM = 8;        // factors per candidate handled by the mixed kernels
+constexpr int kMixedStackCap = 4;    // spill levels of the double-float factor evaluator
+constexpr int kMixedMaxM = 8;        // factors per candidate handled by the mixed solve
+
+template <int MMAX>
+struct GramSize {
+  static constexpr int G = MMAX * (MMAX + 1) / 2;
+  static constexpr int E = G + 2 * MMAX;
+};
+constexpr int kMixedE = GramSize<kMixedMaxM>::E;  // Gram entries per candidate in the pair map
 
 // Per-candidate solve output consumed by the residual pass.
 struct MixedTerm {
@@ -17,9 +24,9 @@ struct MixedTerm {
 
 // Why a mixed candidate was re-scored by the FP64 path (counters per round).
 enum FallbackReason : int {
-  FB_PROBE_NONFINITE = 0,  // FP32 non-finite where FP64 is finite (or the reverse) on a probe row
+  FB_PROBE_NONFINITE = 0,  // double-float non-finite where FP64 is finite (or the reverse) on a probe row
   FB_FP64_INF,             // FP64 overflow on a probe row
-  FB_FP32_OVERFLOW,        // +-inf in the FP32 sums without NaN
+  FB_FP32_OVERFLOW,        // +-inf in the double-float sums without NaN (FP32 exponent range)
   FB_NAN_RANK,             // NaN factor next to a rank-deficient rest
   FB_RANK,                 // rank cut
   FB_ILL_COND,             // pivot ratio below the conditioning bound
@@ -31,38 +38,31 @@ enum FallbackReason : int {
   kFbReasons
 };
 
-// FP32-versus-FP64 comparison of every factor on the probe rows of a mixed
-// round (mixed_probe_kernel), read by the certification in the solve.
+// Double-float-versus-FP64 comparison on the probe rows, per distinct factor
+// (fac_probe_kernel) and gathered per candidate (cand_probe_kernel).
 constexpr int kProbeRows = 1024;  // every row when n <= kProbeRows
+enum : uint32_t { FP_NAN64 = 1, FP_INF64 = 2, FP_BAD32 = 4, FP_FAIL = 8, FP_ALL_ROWS = 16 };
+struct FacProbe {
+  float dev;       // max |df - f64| over probe rows where both are finite
+  float rms;       // root mean square of f64 over those rows
+  uint32_t flags;  // FP_* bits
+  uint32_t pad;
+};
 struct ProbeOut {
-  float dev[kMixedMaxM];   // max |f32 - f64| over probe rows where both are finite
+  float dev[kMixedMaxM];   // max |df - f64| over probe rows where both are finite
   float rms[kMixedMaxM];   // root mean square of f64 over those rows
   uint32_t nan64, inf64;   // factor masks: FP64 NaN / +-inf on some probe row
-  uint32_t bad32;          // factor mask: FP32 non-finite where FP64 is finite, or the reverse
+  uint32_t bad32;          // factor mask: double-float non-finite where FP64 is finite, or the reverse
   uint32_t all_rows;       // 1 when every row of the dataset was probed
-};
-
-struct MixedArgs {
-  DevBatch b;
-  DevData ds;
-  const int32_t* list;   // candidates of this launch (absolute indices)
-  int32_t n_list;
-  int32_t group;         // candidates per work unit
-  int32_t n_tiles, tile; // row tiles
-  int32_t n_units;
-  float2* gram;          // [list index][tile][E] (gram pass)
-  double* sse;           // [absolute candidate][tile] (residual pass)
-  const MixedTerm* terms;  // [absolute candidate] (residual pass)
-  uint32_t* status;
-  int64_t* nanrow;         // [absolute candidate] first row with a NaN factor value (gram pass)
 };
 
 struct SolveArgs {
   DevBatch b;
   DevData ds;
-  const int32_t* list;
-  int32_t n_list, n_tiles, mmax;
-  const float2* gram;
+  const int32_t* list;     // mixed candidates (absolute indices)
+  int32_t n_list;
+  const int32_t* pair_of;  // [list index][kMixedE] pair index of each Gram entry, -1 for none
+  const double* psum;      // [pair] FP64 sum over all rows
   double* coefs;
   MixedTerm* terms;
   rrg_result* res;
@@ -72,25 +72,25 @@ struct SolveArgs {
   uint8_t* pass2;          // [candidate] 1: run the residual pass
   const ProbeOut* probe;   // [candidate]
   uint32_t* reasons;       // [kFbReasons] counts of FP64 re-scoring reasons
-  const int64_t* nanrow;   // [candidate] first row where FP32 gave a NaN factor value
+  const int64_t* nanrow;   // [candidate] first row where a factor value was NaN in the table
+  double* cert_e;          // [candidate] certified rounds: per-row error bound for the residual-pass check
   double rank_tol, fallback_tol, pass2_tol, cert_tol;
   int certify;             // 1: RRG_MIXED_CERTIFIED decisions
 };
 
 // Host launchers (mixed.cu).
-bool launch_gram(int mmax, const MixedArgs& a, int grid, size_t smem, cudaStream_t st);
-bool launch_resid(int mmax, const MixedArgs& a, int grid, size_t smem, cudaStream_t st);
+bool launch_fac_probe(const uint32_t* code, const int2* meta, int32_t nf, const double* K64, const float* K32,
+                      const float* K32lo, const DevData& ds, FacProbe* out, cudaStream_t st);
+// cand_fac: [list index][kMixedMaxM] local factor ids; fcol: local factor -> table column
+bool launch_cand_probe(const rrg_cand* cands, const int32_t* list, int32_t n_list, const int32_t* cand_fac,
+                       const int32_t* fcol, const FacProbe* fp, const unsigned long long* fnan, ProbeOut* out,
+                       int64_t* nanrow, cudaStream_t st);
 bool launch_solve(const SolveArgs& a, cudaStream_t st);
-bool launch_probe(const DevBatch& b, const DevData& ds, const int32_t* list, int32_t n_list, ProbeOut* out,
-                  cudaStream_t st);
-int mixed_threads(int mmax);
-size_t mixed_smem(int mmax, int d, int tile, bool resid);
-int mixed_gram_entries(int mmax);
+// Certified rounds: residual-pass SSE of the listed candidates against their bound.
+bool launch_cert_resid(const int32_t* mlist, const int32_t* list2, int32_t n2, const double* sse_part, int nb,
+                       const double* cert_e, const DevData& ds, double cert_tol, int32_t* fallback,
+                       int32_t fallback_cap, uint32_t* reasons, cudaStream_t st);
 bool launch_to_f32(const double* src, float* dst, int64_t n, cudaStream_t st);
 bool launch_split_f32(const double* src, float* hi, float* lo, int64_t n, cudaStream_t st);
 
 }  // namespace rrd
-
-namespace rrd {
-bool mixed_allow_smem();
-}

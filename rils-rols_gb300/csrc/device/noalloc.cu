@@ -247,6 +247,7 @@ extern "C" rrg_status rrg_eval_plain_noalloc(const double* X_col, int64_t ld, co
   db.code = reinterpret_cast<const uint32_t*>(base + o_code);
   db.consts = reinterpret_cast<const double*>(base + o_const);
   db.consts32 = nullptr;
+  db.consts32lo = nullptr;
   db.n_cand = 1;
   db.n_factors = cd.n_factors;
   db.n_code = cd.code_len;
@@ -254,6 +255,7 @@ extern "C" rrg_status rrg_eval_plain_noalloc(const double* X_col, int64_t ld, co
   DevData dd;
   dd.X64 = X_col;
   dd.X32 = nullptr;
+  dd.X32lo = nullptr;
   dd.y64 = y;
   dd.y32 = nullptr;
   dd.y32lo = nullptr;
@@ -275,9 +277,9 @@ extern "C" rrg_status rrg_eval_plain_noalloc(const double* X_col, int64_t ld, co
   const int nb_eval = (int)std::min<int64_t>(1024, std::max<int64_t>(1, (n + 1023) / 1024));
   plain_eval_kernel<<<dim3(nb_eval, 1), 256, plain_eval_smem(), st>>>(db, dd, dpc, nullptr, 0, arena, arena,
                                                                        nullptr, 0, status);
-  plain_qr_kernel<<<1, 256, plain_qr_smem(), st>>>(db, dd, dpc, nullptr, 0, arena, arena, nullptr, 0, 1, cf, result,
-                                                   status, nullptr);
-  plain_resid_kernel<<<dim3(nb_res, 1), 256, 0, st>>>(db, dd, dpc, nullptr, 0, arena, cf, partial);
+  launch_plain_qr((int)k + 1, 1, st, db, dd, dpc, nullptr, 0, arena, arena, nullptr, 0, 1, cf, result, status, nullptr,
+                  nullptr);
+  plain_resid_kernel<<<dim3(nb_res, 1), 256, 0, st>>>(db, dd, dpc, nullptr, 0, arena, cf, partial, nullptr);
   finalize_kernel<<<1, 128, 0, st>>>(db, dd, nullptr, 0, 1, partial, nb_res, cf, result, 0u, nullptr);
   uint32_t dev_status = 0;
   if ((e = cudaGetLastError()) != cudaSuccess ||

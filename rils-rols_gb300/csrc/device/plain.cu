@@ -29,6 +29,13 @@ namespace {
 
 constexpr int kMaxK = RRG_MAX_TERMS;
 
+// Column j of candidate factor values: contiguous columns from a_col, or
+// through the column map (shared factor table) when one is given.
+__device__ __forceinline__ const double* factor_column(const double* A, int64_t n_pad, int64_t a_col, int j,
+                                                       const int32_t* colmap) {
+  return A + (colmap ? (int64_t)colmap[a_col + j] : a_col + j) * n_pad;
+}
+
 __device__ __forceinline__ double bin64(int base, double a, double b) {
   switch (base) {
     case RRG_ADD: return __dadd_rn(a, b);
@@ -214,11 +221,114 @@ __global__ void __launch_bounds__(256) plain_eval_kernel(DevBatch b, DevData ds,
   }
 }
 
-// One block per tuned candidate: column-pivoted QR least squares.
-__global__ void __launch_bounds__(256) plain_qr_kernel(DevBatch b, DevData ds, const PlainCand* pc,
-                                                        const int32_t* list, int cand0, const double* A, double* M,
-                                                        double* S, int tsqr, int nb, double* coefs, rrg_result* res,
-                                                        uint32_t* status, uint8_t* redo) {
+namespace {
+
+// Element-wise block sums of part[0..cnt) (register arrays of KB entries).
+template <int KB>
+__device__ __forceinline__ void block_sum_vec_t(const double (&part)[KB], int cnt, double* red, double* out) {
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
+  __syncthreads();
+#pragma unroll
+  for (int j = 0; j < KB; ++j)
+    if (j < cnt) {
+      const double v = warp_sum(part[j]);
+      if (l == 0) red[w * KB + j] = v;
+    }
+  __syncthreads();
+  for (int j = threadIdx.x; j < cnt; j += blockDim.x) {
+    double s = 0.0;
+    for (int i = 0; i < nw; ++i) s = __dadd_rn(s, red[i * KB + j]);
+    out[j] = s;
+  }
+  __syncthreads();
+}
+
+// Householder reflector of col[kk..rows) (Householder.h:67-96 semantics).
+// Returns tau; writes beta to col[kk] and the essential part below it.
+__device__ double make_householder_col(double* col, int64_t rows, int kk, double* red) {
+  double part = 0.0;
+  for (int64_t i = kk + 1 + threadIdx.x; i < rows; i += blockDim.x) part = __dadd_rn(part, __dmul_rn(col[i], col[i]));
+  const double tail_sq = (rows - kk == 1) ? 0.0 : block_sum(part, red);
+  const double c0 = col[kk];
+  double tau, beta;
+  __syncthreads();
+  if (tail_sq <= DBL_MIN) {
+    tau = 0.0;
+    beta = c0;
+    for (int64_t i = kk + 1 + threadIdx.x; i < rows; i += blockDim.x) col[i] = 0.0;
+  } else {
+    beta = __dsqrt_rn(__dadd_rn(__dmul_rn(c0, c0), tail_sq));
+    if (c0 >= 0.0) beta = -beta;
+    const double den = __dsub_rn(c0, beta);
+    for (int64_t i = kk + 1 + threadIdx.x; i < rows; i += blockDim.x) col[i] = __ddiv_rn(col[i], den);
+    tau = __ddiv_rn(__dsub_rn(beta, c0), beta);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) col[kk] = beta;
+  __syncthreads();
+  return tau;
+}
+
+// Applies H_kk = I - tau v v^T (v = [1, colp[kk][kk+1..]]) to the columns
+// colp[c_lo..c_hi) (rows kk..rows-1).  Householder.h:116-133 semantics.
+template <int KB>
+__device__ void apply_householder_cols(double* const* colp, int64_t rows, int kk, double tau, int c_lo, int c_hi,
+                                       double* red, double* sh_tmp) {
+  const int cnt = c_hi - c_lo;
+  if (cnt <= 0) return;
+  if (rows - kk == 1) {
+    for (int j = threadIdx.x; j < cnt; j += blockDim.x) {
+      double* q = colp[c_lo + j] + kk;
+      *q = __dmul_rn(*q, __dsub_rn(1.0, tau));
+    }
+    __syncthreads();
+    return;
+  }
+  if (tau == 0.0) return;
+  const double* v = colp[kk];
+  double* cp[KB];
+  double part[KB];
+#pragma unroll
+  for (int j = 0; j < KB; ++j) {
+    cp[j] = j < cnt ? colp[c_lo + j] : nullptr;
+    part[j] = 0.0;
+  }
+  for (int64_t i = kk + 1 + threadIdx.x; i < rows; i += blockDim.x) {
+    const double vi = v[i];
+#pragma unroll
+    for (int j = 0; j < KB; ++j)
+      if (j < cnt) part[j] = __dadd_rn(part[j], __dmul_rn(vi, cp[j][i]));
+  }
+  block_sum_vec_t<KB>(part, cnt, red, sh_tmp);
+  // tmp_j += Q[kk, j]; Q[kk, j] -= tau * tmp_j
+  if (threadIdx.x == 0) {
+    for (int j = 0; j < cnt; ++j) {
+      double* q = colp[c_lo + j] + kk;
+      sh_tmp[j] = __dadd_rn(sh_tmp[j], *q);
+      *q = __dsub_rn(*q, __dmul_rn(tau, sh_tmp[j]));
+    }
+  }
+  __syncthreads();
+  double t[KB];
+#pragma unroll
+  for (int j = 0; j < KB; ++j) t[j] = j < cnt ? sh_tmp[j] : 0.0;
+  for (int64_t i = kk + 1 + threadIdx.x; i < rows; i += blockDim.x) {
+    const double tv = __dmul_rn(tau, v[i]);
+#pragma unroll
+    for (int j = 0; j < KB; ++j)
+      if (j < cnt) cp[j][i] = __dsub_rn(cp[j][i], __dmul_rn(tv, t[j]));
+  }
+  __syncthreads();
+}
+
+// One block per tuned candidate: column-pivoted QR least squares.  KB bounds
+// the columns [A | 1 | y] (k + 1) so that per-column accumulators stay in
+// registers.  Pivoting swaps column pointers, not data.
+template <int KB>
+__global__ void __launch_bounds__(256) plain_qr_kernel_t(DevBatch b, DevData ds, const PlainCand* pc,
+                                                          const int32_t* list, int cand0, const double* A, double* M,
+                                                          double* S, int tsqr, int nb, double* coefs, rrg_result* res,
+                                                          uint32_t* status, uint8_t* redo, const int32_t* colmap) {
   extern __shared__ double smem[];
   const int c = list ? list[cand0 + blockIdx.x] : cand0 + blockIdx.x;
   const rrg_cand cd = b.cands[c];
@@ -226,7 +336,7 @@ __global__ void __launch_bounds__(256) plain_qr_kernel(DevBatch b, DevData ds, c
   // second pass of a tiled round: only the candidates the first pass flagged
   if (!tsqr && redo && !redo[c]) return;
   const int k = pc[c].k;
-  if (k > kMaxK) {
+  if (k + 1 > KB || k > kMaxK) {
     if (threadIdx.x == 0) atomicOr(status, ST_TOO_LARGE);
     return;
   }
@@ -237,37 +347,63 @@ __global__ void __launch_bounds__(256) plain_qr_kernel(DevBatch b, DevData ds, c
   double* hc = ndir + kMaxK;                // kMaxK
   int* perm = reinterpret_cast<int*>(hc + kMaxK);
   int* misc = perm + kMaxK;                 // [0] pivot, [1] nonzero, [2..] recompute flags
+  __shared__ double* colp[KB];              // current position -> column storage
 
-  double* Q;
   int64_t ld, rows;
+  double* Q;
+  double part[KB];
+#pragma unroll
+  for (int j = 0; j < KB; ++j) part[j] = 0.0;
   if (tsqr) {
     Q = S + pc[c].s_off;
     ld = (int64_t)nb * k;
     rows = ld;
+    for (int j = threadIdx.x; j <= k; j += blockDim.x) colp[j] = Q + (int64_t)j * ld;
+    __syncthreads();
+    // initial column norms
+    for (int64_t i = threadIdx.x; i < rows; i += blockDim.x) {
+#pragma unroll
+      for (int j = 0; j < KB; ++j)
+        if (j < k) {
+          const double q = colp[j][i];
+          part[j] = __dadd_rn(part[j], __dmul_rn(q, q));
+        }
+    }
   } else {
     Q = M + pc[c].m_col * ds.n_pad;
     ld = ds.n_pad;
     rows = ds.n;
-    const double* Ac = A + pc[c].a_col * ds.n_pad;
-    for (int j = 0; j <= k; ++j)
-      for (int64_t r = threadIdx.x; r < rows; r += blockDim.x)
-        Q[(int64_t)j * ld + r] = j < k - 1 ? Ac[(int64_t)j * ds.n_pad + r] : (j == k - 1 ? 1.0 : ds.y64[r]);
-    __syncthreads();
+    for (int j = threadIdx.x; j <= k; j += blockDim.x) colp[j] = Q + (int64_t)j * ld;
+    // [A | 1 | y] into the working columns; the initial norms on the way
+    // (each lane sums its rows in the same order as a separate pass would)
+#pragma unroll
+    for (int j = 0; j < KB; ++j) {
+      if (j > k) break;
+      double* dst = Q + (int64_t)j * ld;
+      if (j < k - 1) {
+        const double* src = factor_column(A, ds.n_pad, pc[c].a_col, j, colmap);
+        double acc = 0.0;
+        for (int64_t r = threadIdx.x; r < rows; r += blockDim.x) {
+          const double v = src[r];
+          dst[r] = v;
+          acc = __dadd_rn(acc, __dmul_rn(v, v));
+        }
+        part[j] = acc;
+      } else if (j == k - 1) {
+        double acc = 0.0;
+        for (int64_t r = threadIdx.x; r < rows; r += blockDim.x) {
+          dst[r] = 1.0;
+          acc = __dadd_rn(acc, 1.0);
+        }
+        part[j] = acc;
+      } else {
+        for (int64_t r = threadIdx.x; r < rows; r += blockDim.x) dst[r] = ds.y64[r];
+      }
+    }
   }
+  block_sum_vec_t<KB>(part, k, red, sh_tmp);
   const double rows_thr = (double)ds.n;
   const int size = (int)(rows < k ? rows : k);
-
-  // initial column norms
-  {
-    double part[kMaxK];
-    for (int j = 0; j < k; ++j) part[j] = 0.0;
-    for (int64_t i = threadIdx.x; i < rows; i += blockDim.x)
-      for (int j = 0; j < k; ++j) {
-        const double q = Q[(int64_t)j * ld + i];
-        part[j] = __dadd_rn(part[j], __dmul_rn(q, q));
-      }
-    block_sum_vec(part, k, red, sh_tmp);
-  }
   if (threadIdx.x == 0) {
     for (int j = 0; j < k; ++j) {
       ndir[j] = __dsqrt_rn(sh_tmp[j]);
@@ -298,32 +434,22 @@ __global__ void __launch_bounds__(256) plain_qr_kernel(DevBatch b, DevData ds, c
         double t = nupd[kk]; nupd[kk] = nupd[big]; nupd[big] = t;
         t = ndir[kk]; ndir[kk] = ndir[big]; ndir[big] = t;
         int p = perm[kk]; perm[kk] = perm[big]; perm[big] = p;
+        double* cq = colp[kk]; colp[kk] = colp[big]; colp[big] = cq;
       }
     }
     __syncthreads();
-    const int big = misc[0];
-    if (big != kk) {
-      double* ca = Q + (int64_t)kk * ld;
-      double* cb = Q + (int64_t)big * ld;
-      for (int64_t i = threadIdx.x; i < rows; i += blockDim.x) {
-        const double t = ca[i];
-        ca[i] = cb[i];
-        cb[i] = t;
-      }
-    }
-    __syncthreads();
-    const double tau = make_householder(Q, ld, rows, kk, red);
+    const double tau = make_householder_col(colp[kk], rows, kk, red);
     if (threadIdx.x == 0) hc[kk] = tau;
     // reflector kk reaches the right-hand side only while kk < rank
     const int c_hi = misc[1] == size ? k + 1 : k;
-    apply_householder(Q, ld, rows, kk, tau, kk + 1, c_hi, red, sh_tmp);
+    apply_householder_cols<KB>(colp, rows, kk, tau, kk + 1, c_hi, red, sh_tmp);
     // LAWN 176 norm down-dating (ColPivHouseholderQR.h:549-572)
     int* rec = misc + 2;
     if (threadIdx.x == 0) {
       for (int j = kk + 1; j < k; ++j) {
         rec[j] = 0;
         if (nupd[j] != 0.0) {
-          double temp = __ddiv_rn(fabs(Q[(int64_t)j * ld + kk]), nupd[j]);
+          double temp = __ddiv_rn(fabs(colp[j][kk]), nupd[j]);
           temp = __dmul_rn(__dadd_rn(1.0, temp), __dsub_rn(1.0, temp));
           temp = temp < 0.0 ? 0.0 : temp;
           const double ratio = __ddiv_rn(nupd[j], ndir[j]);
@@ -336,12 +462,13 @@ __global__ void __launch_bounds__(256) plain_qr_kernel(DevBatch b, DevData ds, c
     __syncthreads();
     for (int j = kk + 1; j < k; ++j) {
       if (!rec[j]) continue;  // uniform
-      double part = 0.0;
+      const double* cj = colp[j];
+      double p1 = 0.0;
       for (int64_t i = kk + 1 + threadIdx.x; i < rows; i += blockDim.x) {
-        const double q = Q[(int64_t)j * ld + i];
-        part = __dadd_rn(part, __dmul_rn(q, q));
+        const double q = cj[i];
+        p1 = __dadd_rn(p1, __dmul_rn(q, q));
       }
-      const double s = block_sum(part, red);
+      const double s = block_sum(p1, red);
       if (threadIdx.x == 0) {
         ndir[j] = __dsqrt_rn(s);
         nupd[j] = ndir[j];
@@ -353,10 +480,10 @@ __global__ void __launch_bounds__(256) plain_qr_kernel(DevBatch b, DevData ds, c
   if (threadIdx.x == 0) {
     const int r = misc[1];
     double cvec[kMaxK];
-    for (int i = 0; i < r; ++i) cvec[i] = Q[(int64_t)k * ld + i];
+    for (int i = 0; i < r; ++i) cvec[i] = colp[k][i];
     for (int kk = r - 1; kk >= 0; --kk) {
-      cvec[kk] = __ddiv_rn(cvec[kk], Q[(int64_t)kk * ld + kk]);
-      for (int i = 0; i < kk; ++i) cvec[i] = __dsub_rn(cvec[i], __dmul_rn(cvec[kk], Q[(int64_t)kk * ld + i]));
+      cvec[kk] = __ddiv_rn(cvec[kk], colp[kk][kk]);
+      for (int i = 0; i < kk; ++i) cvec[i] = __dsub_rn(cvec[i], __dmul_rn(cvec[kk], colp[kk][i]));
     }
     double* out = coefs + cd.coef_offset;
     for (int j = 0; j < k; ++j) out[j] = 0.0;
@@ -369,7 +496,7 @@ __global__ void __launch_bounds__(256) plain_qr_kernel(DevBatch b, DevData ds, c
       // candidate is re-solved by the direct column-pivoted QR on [A | 1 | y].
       double rmax = 0.0, rmin = 1e308;
       for (int i = 0; i < size; ++i) {
-        const double d = fabs(Q[(int64_t)i * ld + i]);
+        const double d = fabs(colp[i][i]);
         rmax = d > rmax ? d : rmax;
         rmin = d < rmin ? d : rmin;
       }
@@ -378,14 +505,37 @@ __global__ void __launch_bounds__(256) plain_qr_kernel(DevBatch b, DevData ds, c
   }
 }
 
+}  // namespace
+
+int plain_qr_bucket(int cols) { return cols <= 4 ? 4 : (cols <= 8 ? 8 : (cols <= 16 ? 16 : kMaxK + 1)); }
+
+bool launch_plain_qr(int max_cols, int grid, cudaStream_t st, DevBatch b, DevData ds, const PlainCand* pc,
+                     const int32_t* list, int cand0, const double* A, double* M, double* S, int tsqr, int nb,
+                     double* coefs, rrg_result* res, uint32_t* status, uint8_t* redo, const int32_t* colmap) {
+  if (grid <= 0) return true;
+  const size_t sm = plain_qr_smem();
+  if (max_cols <= 4)
+    plain_qr_kernel_t<4><<<grid, 256, sm, st>>>(b, ds, pc, list, cand0, A, M, S, tsqr, nb, coefs, res, status, redo, colmap);
+  else if (max_cols <= 8)
+    plain_qr_kernel_t<8><<<grid, 256, sm, st>>>(b, ds, pc, list, cand0, A, M, S, tsqr, nb, coefs, res, status, redo, colmap);
+  else if (max_cols <= 16)
+    plain_qr_kernel_t<16><<<grid, 256, sm, st>>>(b, ds, pc, list, cand0, A, M, S, tsqr, nb, coefs, res, status, redo, colmap);
+  else
+    plain_qr_kernel_t<kMaxK + 1><<<grid, 256, sm, st>>>(b, ds, pc, list, cand0, A, M, S, tsqr, nb, coefs, res, status,
+                                                        redo, colmap);
+  return cudaGetLastError() == cudaSuccess;
+}
+
 // grid (ceil(n / RR_CHUNK), candidates): SSE of the rebuilt sum per chunk of
 // RR_CHUNK rows in the fixed order of csrc/common/rr_sum.h
 __global__ void __launch_bounds__(256) plain_resid_kernel(DevBatch b, DevData ds, const PlainCand* pc,
                                                            const int32_t* list, int cand0, const double* A,
-                                                           const double* coefs, double* partial) {
+                                                           const double* coefs, double* partial,
+                                                           const int32_t* colmap) {
   __shared__ double red[32];
   __shared__ double cs[kMaxK];
   __shared__ int kind[kMaxK];  // 0 skip, 1 free term, 2 bare factor, 3 scaled factor
+  __shared__ const double* colp[kMaxK];
   const int c = list ? list[cand0 + blockIdx.y] : cand0 + blockIdx.y;
   const rrg_cand cd = b.cands[c];
   const int nb = gridDim.x;
@@ -400,8 +550,9 @@ __global__ void __launch_bounds__(256) plain_resid_kernel(DevBatch b, DevData ds
     }
   }
   __syncthreads();
+  for (int i = threadIdx.x; i < m; i += blockDim.x) colp[i] = factor_column(A, ds.n_pad, pc[c].a_col, i, colmap);
+  __syncthreads();
   const int64_t r0 = (int64_t)blockIdx.x * RR_CHUNK, r1 = min(ds.n, r0 + (int64_t)RR_CHUNK);
-  const double* Ac = A + pc[c].a_col * ds.n_pad;
   double acc = 0.0;
   for (int64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
     double yp;
@@ -411,13 +562,12 @@ __global__ void __launch_bounds__(256) plain_resid_kernel(DevBatch b, DevData ds
       for (int i = 0; i < k; ++i) {
         const int kd = kind[i];
         if (kd == 0) continue;
-        const double term = kd == 1 ? __dmul_rn(cs[i], 1.0)
-                                    : (kd == 2 ? Ac[(int64_t)i * ds.n_pad + r] : __dmul_rn(cs[i], Ac[(int64_t)i * ds.n_pad + r]));
+        const double term = kd == 1 ? __dmul_rn(cs[i], 1.0) : (kd == 2 ? colp[i][r] : __dmul_rn(cs[i], colp[i][r]));
         yp = have ? __dadd_rn(yp, term) : term;
         have = true;
       }
     } else {
-      yp = Ac[r];
+      yp = colp[0][r];
     }
     const double e = __dsub_rn(ds.y64[r], yp);
     acc = __dadd_rn(acc, __dmul_rn(e, e));
@@ -478,6 +628,12 @@ __global__ void finalize_kernel(DevBatch b, DevData ds, const int32_t* list, int
 }
 
 // ----------------------------------------------------------- launchers ----
+// Result records of the listed candidates back to zero before a re-scoring.
+__global__ void clear_results_kernel(const int32_t* list, int n, rrg_result* res) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) res[list[i]] = rrg_result{};
+}
+
 size_t plain_eval_smem() { return RRG_MAX_STACK * 256 * sizeof(double) + kMaxCodeSmem * sizeof(uint32_t); }
 size_t plain_qr_smem() {
   return (8 * (kMaxK + 1) + (kMaxK + 1) + 3 * kMaxK) * sizeof(double) + (kMaxK + 2 + kMaxK) * sizeof(int);

@@ -12,16 +12,24 @@ __global__ void plain_eval_kernel(DevBatch b, DevData ds, const PlainCand* pc, c
 // tsqr = 1: pivoted QR of the stacked slice triangles, and redo[c] = 1 when
 // the candidate must be re-solved directly; tsqr = 0 with redo != NULL: only
 // the flagged candidates, by the direct QR on [A | 1 | y].
-__global__ void plain_qr_kernel(DevBatch b, DevData ds, const PlainCand* pc, const int32_t* list, int cand0,
-                                const double* A, double* M, double* S, int tsqr, int nb, double* coefs,
-                                rrg_result* res, uint32_t* status, uint8_t* redo);
+// colmap (may be NULL): factor column j of candidate c is column
+// colmap[pc[c].a_col + j] of A (a shared factor table) instead of
+// column pc[c].a_col + j.
+// Column bucket (register footprint) of the QR kernel for k + 1 columns.
+int plain_qr_bucket(int cols);
+// One block per candidate of the launch; max_cols bounds k + 1 over them.
+bool launch_plain_qr(int max_cols, int grid, cudaStream_t st, DevBatch b, DevData ds, const PlainCand* pc,
+                     const int32_t* list, int cand0, const double* A, double* M, double* S, int tsqr, int nb,
+                     double* coefs, rrg_result* res, uint32_t* status, uint8_t* redo, const int32_t* colmap);
 __global__ void plain_resid_kernel(DevBatch b, DevData ds, const PlainCand* pc, const int32_t* list, int cand0,
-                                   const double* A, const double* coefs, double* partial);
+                                   const double* A, const double* coefs, double* partial, const int32_t* colmap);
 // partial[c * nb + j]: per-candidate squared-residual partial sums; when
 // sse_direct is given and sse_direct[c] >= 0 (or NaN) it is the SSE itself.
 __global__ void finalize_kernel(DevBatch b, DevData ds, const int32_t* list, int cand0, int cand1,
                                 const double* partial, int nb, const double* coefs, rrg_result* res,
                                 uint32_t flags_or, const double* sse_direct);
+
+__global__ void clear_results_kernel(const int32_t* list, int n, rrg_result* res);
 
 size_t plain_eval_smem();
 size_t plain_qr_smem();

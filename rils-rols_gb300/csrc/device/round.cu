@@ -1,0 +1,921 @@
+// Rounds over the shared factor table: the mixed round (FP32 table, pair
+// sums, solve, residual pass) and the FP64 scoring of candidate lists
+// (FP64 table, direct column-pivoted QR per candidate).
+//
+// A candidate's tuned form is a sum of top-level factors
+// (tune_constants, rils_rols_cpp.cpp:448-475); candidates of one round share
+// most factors, so factor programs are de-duplicated on the host (same
+// instructions, same constant values) and each distinct factor is evaluated
+// once per round.  The arithmetic of every factor value is that of the
+// per-candidate paths, so sharing changes no result.
+#include <algorithm>
+#include <cstring>
+#include <numeric>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "../common/error.h"
+#include "../common/rr_sum.h"
+#include "common.cuh"
+#include "ftable.cuh"
+#include "mixed.cuh"
+#include "plain.cuh"
+#include "runtime.cuh"
+
+using namespace rrd;
+
+namespace {
+
+bool cuda_ok(cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return true;
+  rrc::set_error(std::string(what) + ": " + cudaGetErrorString(e));
+  return false;
+}
+
+#define RRG_CUDA(call)                              \
+  do {                                              \
+    if (!cuda_ok((call), #call)) return RRG_E_CUDA; \
+  } while (0)
+
+bool const_arg(int op) {
+  if (op == RRG_OP_LDC || op == RRG_OP_PSC) return true;
+  if (op >= RRG_OP_BIN) return (((op - RRG_OP_BIN) & 7) >> 1) == RRG_SRC_C;
+  return false;
+}
+
+// Sections of one upload, each 256-byte aligned, copied into one pinned
+// buffer and sent with one host-to-device copy.
+struct Packer {
+  std::vector<std::pair<const void*, size_t>> parts;
+  std::vector<size_t> offs;
+  size_t total = 0;
+  size_t add(const void* p, size_t bytes) {
+    const size_t off = total;
+    parts.push_back({p, bytes});
+    offs.push_back(off);
+    total = (size_t)round_up((int64_t)(total + bytes), 256);
+    return off;
+  }
+  rrg_status send(HostBuf& h, DevBuf& d, cudaStream_t st) {
+    // the pinned buffer may still feed a copy queued earlier on the stream
+    RRG_CUDA(cudaStreamSynchronize(st));
+    if (!h.reserve(std::max<size_t>(total, 256)) || !d.reserve(std::max<size_t>(total, 256))) {
+      rrc::set_error("factor table: staging allocation failed");
+      return RRG_E_OOM;
+    }
+    char* hp = static_cast<char*>(h.ptr);
+    for (size_t i = 0; i < parts.size(); ++i)
+      if (parts[i].first && parts[i].second) std::memcpy(hp + offs[i], parts[i].first, parts[i].second);
+    if (total) RRG_CUDA(cudaMemcpyAsync(d.ptr, h.ptr, total, cudaMemcpyHostToDevice, st));
+    return RRG_OK;
+  }
+  template <class T>
+  T* at(DevBuf& d, size_t off) const {
+    return reinterpret_cast<T*>(static_cast<char*>(d.ptr) + off);
+  }
+};
+
+int cand_factors(const rrg_cand& cd) { return cd.mode == RRG_TUNED ? cd.n_factors : 1; }
+
+// ----------------------------------------------- shared subexpressions ----
+// Factor programs parsed back into trees: every distinct sin / cos / ln /
+// exp / pow subtree of a sub-round becomes a table column of its own,
+// evaluated once, and the programs that contain it read that column.
+struct PNode {
+  int8_t kind;  // 0 feature, 1 constant, 3 unary, 4 binary
+  int8_t op;    // unary opcode or binary base
+  int32_t arg;  // feature or constant index
+  int32_t a, b; // children
+};
+
+bool parse_program(const uint32_t* code, int len, std::vector<PNode>& nd, int32_t& root) {
+  std::vector<int32_t> st;
+  auto leaf = [&](int8_t kind, uint32_t arg) {
+    nd.push_back(PNode{kind, 0, (int32_t)arg, -1, -1});
+    return (int32_t)nd.size() - 1;
+  };
+  for (int pc = 0; pc < len; ++pc) {
+    const uint32_t w = code[pc];
+    const int op = (int)(w & 0xffu);
+    const uint32_t arg = w >> 8;
+    if (op == RRG_OP_LDV || op == RRG_OP_PSV) {
+      st.push_back(leaf(0, arg));
+    } else if (op == RRG_OP_LDC || op == RRG_OP_PSC) {
+      st.push_back(leaf(1, arg));
+    } else if (op >= RRG_OP_SIN && op <= RRG_OP_SQR) {
+      if (st.empty()) return false;
+      const int32_t x = st.back();
+      nd.push_back(PNode{3, (int8_t)op, 0, x, -1});
+      st.back() = (int32_t)nd.size() - 1;
+    } else if (op == RRG_OP_EMIT) {
+      if (st.size() != 1) return false;
+      root = st.back();
+      return true;
+    } else if (op >= RRG_OP_BIN) {
+      const int kk = op - RRG_OP_BIN;
+      const int base = kk >> 3, src = (kk & 7) >> 1, dir = kk & 1;
+      if (st.empty()) return false;
+      const int32_t tos = st.back();
+      st.pop_back();
+      int32_t other;
+      if (src == RRG_SRC_S) {
+        if (st.empty()) return false;
+        other = st.back();
+        st.pop_back();
+      } else {
+        other = leaf(src == RRG_SRC_V ? 0 : 1, arg);
+      }
+      nd.push_back(PNode{4, (int8_t)base, 0, dir == RRG_DIR_N ? other : tos, dir == RRG_DIR_N ? tos : other});
+      st.push_back((int32_t)nd.size() - 1);
+    } else {
+      return false;
+    }
+  }
+  return false;
+}
+
+bool shared_root(const PNode& n) {
+  return (n.kind == 3 && (n.op == RRG_OP_SIN || n.op == RRG_OP_COS || n.op == RRG_OP_LN || n.op == RRG_OP_EXP)) ||
+         (n.kind == 4 && n.op == RRG_POW);
+}
+
+struct TableProgs {
+  std::vector<uint32_t> code;      // column programs, contiguous, in column order
+  std::vector<int2> meta;          // [column] (code offset, length)
+  std::vector<int32_t> stack;      // [column] spill depth
+  std::vector<int32_t> level_end;  // columns of level L end at level_end[L] (levels ascending)
+  std::vector<int32_t> fcol;       // [local factor] table column
+};
+
+// Postfix encoder with the operand-source superinstructions and Sethi-Ullman
+// ordering; a node marked as a table column is read as a leaf.
+struct Encoder {
+  const std::vector<PNode>& nd;
+  const std::vector<int32_t>& col_of;  // [node] table column, -1 when computed inline
+  int32_t root = -1;
+  std::vector<int32_t> memo;
+  std::vector<uint32_t>* out = nullptr;
+  int sp = 0, maxsp = 0;
+  Encoder(const std::vector<PNode>& n, const std::vector<int32_t>& c) : nd(n), col_of(c), memo(n.size(), -1) {}
+  bool leaf(int32_t m) const { return nd[m].kind <= 1 || (m != root && col_of[m] >= 0); }
+  int need(int32_t m) {
+    if (leaf(m)) return 0;
+    if (m != root && memo[m] >= 0) return memo[m];
+    const PNode& n = nd[m];
+    int v;
+    if (n.kind == 3) {
+      v = need(n.a);
+    } else if (leaf(n.b)) {
+      v = need(n.a);
+    } else if (leaf(n.a)) {
+      v = need(n.b);
+    } else {
+      const int na = need(n.a), nb = need(n.b);
+      v = na >= nb ? std::max(na, nb + 1) : std::max(nb, na + 1);
+    }
+    if (m != root) memo[m] = v;
+    return v;
+  }
+  void src_of(int32_t m, int& src, uint32_t& arg) const {
+    if (nd[m].kind == 0) { src = RRG_SRC_V; arg = (uint32_t)nd[m].arg; }
+    else if (nd[m].kind == 1) { src = RRG_SRC_C; arg = (uint32_t)nd[m].arg; }
+    else { src = kSrcT; arg = (uint32_t)col_of[m]; }
+  }
+  void emit(int32_t m, bool live) {
+    if (leaf(m)) {
+      int src;
+      uint32_t arg;
+      src_of(m, src, arg);
+      int op = src == RRG_SRC_V ? (live ? RRG_OP_PSV : RRG_OP_LDV)
+                                : (src == RRG_SRC_C ? (live ? RRG_OP_PSC : RRG_OP_LDC) : (live ? kOpPST : kOpLDT));
+      if (live) maxsp = std::max(maxsp, ++sp);
+      out->push_back(RRG_INSN(op, arg));
+      return;
+    }
+    const PNode& n = nd[m];
+    if (n.kind == 3) {
+      emit(n.a, live);
+      out->push_back(RRG_INSN(n.op, 0));
+      return;
+    }
+    int src;
+    uint32_t arg;
+    if (leaf(n.b)) {
+      emit(n.a, live);
+      src_of(n.b, src, arg);
+      out->push_back(RRG_INSN(RRG_BIN_OP(n.op, src, RRG_DIR_R), arg));
+    } else if (leaf(n.a)) {
+      emit(n.b, live);
+      src_of(n.a, src, arg);
+      out->push_back(RRG_INSN(RRG_BIN_OP(n.op, src, RRG_DIR_N), arg));
+    } else if (need(n.a) >= need(n.b)) {
+      emit(n.a, live);
+      emit(n.b, true);
+      out->push_back(RRG_INSN(RRG_BIN_OP(n.op, RRG_SRC_S, RRG_DIR_N), 0));
+      --sp;
+    } else {
+      emit(n.b, live);
+      emit(n.a, true);
+      out->push_back(RRG_INSN(RRG_BIN_OP(n.op, RRG_SRC_S, RRG_DIR_R), 0));
+      --sp;
+    }
+  }
+  int encode(int32_t r, std::vector<uint32_t>& dst) {
+    root = r;
+    out = &dst;
+    sp = maxsp = 0;
+    emit(r, false);
+    dst.push_back(RRG_INSN(RRG_OP_EMIT, 0));
+    return maxsp;
+  }
+};
+
+// Table programs of the local factors (programs in lcode / lmeta).
+bool build_table_programs(const std::vector<uint32_t>& lcode, const std::vector<int2>& lmeta, const double* consts,
+                          TableProgs& tp) {
+  const int32_t nfl = (int32_t)lmeta.size();
+  std::vector<PNode> nd;
+  std::vector<int32_t> froot(nfl);
+  for (int32_t l = 0; l < nfl; ++l)
+    if (!parse_program(lcode.data() + lmeta[l].x, lmeta[l].y, nd, froot[l])) return false;
+  // canonical keys bottom-up (children precede parents)
+  std::vector<std::string> key(nd.size());
+  for (size_t i = 0; i < nd.size(); ++i) {
+    const PNode& n = nd[i];
+    std::string& k = key[i];
+    if (n.kind == 0) {
+      k = "V" + std::to_string(n.arg);
+    } else if (n.kind == 1) {
+      uint64_t bits;
+      std::memcpy(&bits, consts + n.arg, sizeof bits);
+      k = "C" + std::to_string(bits);
+    } else if (n.kind == 3) {
+      k = "U" + std::to_string(n.op) + "(" + key[n.a] + ")";
+    } else {
+      k = "B" + std::to_string(n.op) + "(" + key[n.a] + "," + key[n.b] + ")";
+    }
+  }
+  // shared subtrees and their levels (1 + the deepest shared subtree inside)
+  std::unordered_map<std::string, int32_t> aux_index;
+  std::vector<int32_t> aux_node, aux_level, aux_of(nd.size(), -1), lvl(nd.size(), 0);
+  for (size_t i = 0; i < nd.size(); ++i) {
+    const PNode& n = nd[i];
+    int inner = 0;
+    if (n.kind >= 3) inner = std::max(inner, lvl[n.a]);
+    if (n.kind == 4) inner = std::max(inner, lvl[n.b]);
+    lvl[i] = inner;
+    if (shared_root(n)) {
+      auto it = aux_index.find(key[i]);
+      int32_t id;
+      if (it == aux_index.end()) {
+        id = (int32_t)aux_node.size();
+        aux_index.emplace(key[i], id);
+        aux_node.push_back((int32_t)i);
+        aux_level.push_back(inner + 1);
+      } else {
+        id = it->second;
+      }
+      aux_of[i] = id;
+      lvl[i] = aux_level[id];
+    }
+  }
+  // column order: shared subtrees by level, then the factors not aliased to one
+  const int n_aux = (int)aux_node.size();
+  const int max_level = n_aux ? *std::max_element(aux_level.begin(), aux_level.end()) : 0;
+  std::vector<int32_t> aux_col(n_aux, -1);
+  std::vector<int32_t> col_nodes;  // node encoded for each column
+  tp.level_end.clear();
+  for (int L = 1; L <= max_level; ++L) {
+    for (int a = 0; a < n_aux; ++a)
+      if (aux_level[a] == L) {
+        aux_col[a] = (int32_t)col_nodes.size();
+        col_nodes.push_back(aux_node[a]);
+      }
+    tp.level_end.push_back((int32_t)col_nodes.size());
+  }
+  tp.fcol.assign(nfl, -1);
+  for (int32_t l = 0; l < nfl; ++l) {
+    const int32_t r = froot[l];
+    if (aux_of[r] >= 0) {
+      tp.fcol[l] = aux_col[aux_of[r]];
+    } else {
+      tp.fcol[l] = (int32_t)col_nodes.size();
+      col_nodes.push_back(r);
+    }
+  }
+  tp.level_end.push_back((int32_t)col_nodes.size());
+  std::vector<int32_t> col_of(nd.size(), -1);
+  for (size_t i = 0; i < nd.size(); ++i)
+    if (aux_of[i] >= 0) col_of[i] = aux_col[aux_of[i]];
+  Encoder enc(nd, col_of);
+  tp.code.clear();
+  tp.meta.assign(col_nodes.size(), make_int2(0, 0));
+  tp.stack.assign(col_nodes.size(), 0);
+  for (size_t c = 0; c < col_nodes.size(); ++c) {
+    const int off = (int)tp.code.size();
+    tp.stack[c] = enc.encode(col_nodes[c], tp.code);
+    tp.meta[c] = make_int2(off, (int)tp.code.size() - off);
+  }
+  return true;
+}
+
+}  // namespace
+
+void build_factor_table(const rrg_cand* cands, int32_t n_cand, const uint32_t* code, const double* consts,
+                        FactorTable& ft) {
+  ft.code.clear();
+  ft.meta.clear();
+  ft.stack.clear();
+  ft.occ.clear();
+  ft.ids.clear();
+  ft.cand_off.assign((size_t)n_cand + 1, 0);
+  std::unordered_map<std::string, int32_t> index;
+  index.reserve((size_t)n_cand * 2 + 16);
+  std::string key;
+  for (int32_t c = 0; c < n_cand; ++c) {
+    ft.cand_off[c] = (int32_t)ft.ids.size();
+    const rrg_cand& cd = cands[c];
+    int32_t start = cd.code_offset;
+    const int32_t end = cd.code_offset + cd.code_len;
+    int sp = 0, depth = 0;
+    key.clear();
+    for (int32_t pc = start; pc < end; ++pc) {
+      const uint32_t w = code[pc];
+      const int op = (int)(w & 0xffu);
+      if (op == RRG_OP_EMIT) {
+        auto it = index.find(key);
+        int32_t id;
+        if (it == index.end()) {
+          id = (int32_t)ft.meta.size();
+          index.emplace(key, id);
+          int2 mt;
+          mt.x = (int)ft.code.size();
+          mt.y = pc - start + 1;
+          ft.code.insert(ft.code.end(), code + start, code + pc);
+          ft.code.push_back(RRG_INSN(RRG_OP_EMIT, 0));
+          ft.meta.push_back(mt);
+          ft.stack.push_back(depth);
+          ft.occ.push_back(0);
+        } else {
+          id = it->second;
+        }
+        ft.occ[id] += 1;
+        ft.ids.push_back(id);
+        start = pc + 1;
+        sp = 0;
+        depth = 0;
+        key.clear();
+        continue;
+      }
+      if (const_arg(op)) {
+        const double v = consts[w >> 8];
+        key.push_back('C');
+        key.push_back((char)op);
+        key.append(reinterpret_cast<const char*>(&v), sizeof v);
+      } else {
+        key.push_back('W');
+        key.append(reinterpret_cast<const char*>(&w), sizeof w);
+      }
+      if (op == RRG_OP_PSV || op == RRG_OP_PSC) depth = std::max(depth, ++sp);
+      else if (op >= RRG_OP_BIN && (((op - RRG_OP_BIN) & 7) >> 1) == RRG_SRC_S) --sp;
+    }
+  }
+  ft.cand_off[n_cand] = (int32_t)ft.ids.size();
+}
+
+// --------------------------------------------------------- mixed round ----
+rrg_status rrg_context::run_mixed(const rrg_dataset* ds, int32_t n_cand, bool certify) {
+  const char* hb = static_cast<const char*>(h_batch.ptr);
+  build_factor_table(host_cands.data(), n_cand, reinterpret_cast<const uint32_t*>(hb + off_k),
+                     reinterpret_cast<const double*>(hb + off_d), ft);
+  // the mixed kernels take up to kMixedMaxM factors of spill depth <= kMixedStackCap
+  std::vector<int32_t> mixed, routed;
+  for (int32_t c = 0; c < n_cand; ++c) {
+    const rrg_cand& cd = host_cands[c];
+    const int m = cand_factors(cd);
+    bool ok = m <= kMixedMaxM;
+    for (int s = 0; s < m && ok; ++s) {
+      const int32_t id = ft.ids[ft.cand_off[c] + s];
+      ok = ft.stack[id] <= kMixedStackCap && ft.meta[id].y <= kFacCodeSmem;
+    }
+    (ok ? mixed : routed).push_back(c);
+  }
+  last_plain_routed = (int64_t)routed.size();
+  const int n_super = pair_row_blocks(ds->n_pad);
+  const int fb_cap = std::max(1, n_cand);
+  const size_t back_bytes = sizeof(int32_t) * (fb_cap + 1 + kFbReasons) + (size_t)fb_cap;
+  if (!d_terms.reserve(sizeof(MixedTerm) * fb_cap) || !d_sse1.reserve(sizeof(double) * fb_cap) ||
+      !d_cert_e.reserve(sizeof(double) * fb_cap) ||
+      !d_probe.reserve(sizeof(ProbeOut) * fb_cap) || !d_nanrow.reserve(sizeof(int64_t) * fb_cap) ||
+      !d_partial.reserve(sizeof(double) * (size_t)fb_cap * n_super) || !d_fallback.reserve(back_bytes) ||
+      !h_fallback.reserve(back_bytes)) {
+    rrc::set_error("mixed round: scratch allocation failed");
+    return RRG_E_OOM;
+  }
+  std::vector<int32_t> fb_all;
+  const size_t col_bytes = sizeof(float2) * (size_t)ds->n_pad;
+  const int64_t cap_f = std::max<int64_t>(16, (int64_t)(table_budget_bytes / col_bytes));
+  std::vector<int32_t> lid(ft.meta.size(), -1), lf;
+  size_t pos = 0;
+  while (pos < mixed.size()) {
+    lf.clear();
+    size_t end = pos;
+    while (end < mixed.size()) {
+      const int32_t c = mixed[end];
+      const int m = cand_factors(host_cands[c]);
+      int fresh = 0;
+      for (int s = 0; s < m; ++s) fresh += lid[ft.ids[ft.cand_off[c] + s]] < 0 ? 1 : 0;
+      if (end > pos && (int64_t)lf.size() + fresh > cap_f) break;
+      for (int s = 0; s < m; ++s) {
+        const int32_t g = ft.ids[ft.cand_off[c] + s];
+        if (lid[g] < 0) {
+          lid[g] = (int32_t)lf.size();
+          lf.push_back(g);
+        }
+      }
+      ++end;
+    }
+    const rrg_status st = mixed_subround(ds, mixed.data() + pos, (int32_t)(end - pos), lf, lid, certify, fb_all);
+    for (int32_t g : lf) lid[g] = -1;
+    if (st != RRG_OK) return st;
+    pos = end;
+  }
+  last_fallback = (int64_t)fb_all.size();
+  rrg_status st = RRG_OK;
+  if (!routed.empty()) st = run_fp64_table(ds, routed, 0u);
+  if (st == RRG_OK && !fb_all.empty()) {
+    std::sort(fb_all.begin(), fb_all.end());
+    st = run_fp64_table(ds, fb_all, RRG_F_QR_FALLBACK);
+  }
+  return st;
+}
+
+rrg_status rrg_context::mixed_subround(const rrg_dataset* ds, const int32_t* list, int32_t cnt,
+                                       const std::vector<int32_t>& lf, const std::vector<int32_t>& lid,
+                                       bool certify, std::vector<int32_t>& fb_all) {
+  const DevData dd = ds->view();
+  const int32_t nfl = (int32_t)lf.size();
+  // local programs, contiguous in local id order
+  std::vector<uint32_t> lcode;
+  std::vector<int2> lmeta(nfl);
+  for (int32_t i = 0; i < nfl; ++i) {
+    const int2 mt = ft.meta[lf[i]];
+    lmeta[i] = make_int2((int)lcode.size(), mt.y);
+    lcode.insert(lcode.end(), ft.code.begin() + mt.x, ft.code.begin() + mt.x + mt.y);
+  }
+  // table columns: shared transcendental subtrees (by level), then factors
+  TableProgs tp;
+  const char* hb = static_cast<const char*>(h_batch.ptr);
+  if (!build_table_programs(lcode, lmeta, reinterpret_cast<const double*>(hb + off_d), tp)) {
+    rrc::set_error("mixed round: a factor program could not be parsed");
+    return RRG_E_INVALID;
+  }
+  const int32_t ncol = (int32_t)tp.meta.size();
+  for (int32_t c = 0; c < ncol; ++c)
+    if (tp.stack[c] > kMixedStackCap || tp.meta[c].y > kFacCodeSmem) {
+      rrc::set_error("mixed round: a table program exceeds the evaluator's limits");
+      return RRG_E_INVALID;
+    }
+  // evaluator groups per level: consecutive columns whose programs fit the shared buffer
+  std::vector<int2> groups;
+  std::vector<int32_t> level_groups;  // groups of level L end at level_groups[L]
+  for (size_t L = 0, c0 = 0; L < tp.level_end.size(); ++L) {
+    const int32_t c1 = tp.level_end[L];
+    for (int32_t i = (int32_t)c0; i < c1;) {
+      int32_t j = i, words = 0;
+      while (j < c1 && j - i < kFacGroupMax && words + tp.meta[j].y <= kFacCodeSmem) words += tp.meta[j++].y;
+      groups.push_back(make_int2(i, j - i));
+      i = j;
+    }
+    level_groups.push_back((int32_t)groups.size());
+    c0 = c1;
+  }
+  // pair map over table columns: self pairs 3t..3t+2, cross pairs oriented
+  // so that `a` is the rarer factor (its partners are then the widely shared
+  // ones, hot in L2)
+  const int32_t n_self = 3 * ncol;
+  std::unordered_map<uint64_t, int32_t> cmap;
+  cmap.reserve((size_t)cnt * 4 + 16);
+  std::vector<std::pair<int32_t, int32_t>> cross;
+  std::vector<int32_t> pair_of((size_t)cnt * kMixedE, -1), cand_fac((size_t)cnt * kMixedMaxM, 0);
+  std::vector<int32_t> cand_col((size_t)cnt * kMixedMaxM, 0);
+  auto cross_id = [&](int32_t x, int32_t y) {
+    const int32_t gx = lf[x], gy = lf[y];
+    const bool xa = ft.occ[gx] < ft.occ[gy] || (ft.occ[gx] == ft.occ[gy] && gx < gy);
+    const int32_t a = tp.fcol[xa ? x : y], b = tp.fcol[xa ? y : x];
+    const uint64_t key = ((uint64_t)(uint32_t)a << 32) | (uint32_t)b;
+    auto it = cmap.find(key);
+    if (it != cmap.end()) return it->second;
+    const int32_t id = (int32_t)cross.size();
+    cmap.emplace(key, id);
+    cross.push_back({a, b});
+    return id;
+  };
+  constexpr int Gn = GramSize<kMixedMaxM>::G;
+  for (int32_t li = 0; li < cnt; ++li) {
+    const int32_t c = list[li];
+    const int m = cand_factors(host_cands[c]);
+    int32_t l[kMixedMaxM];
+    for (int s = 0; s < m; ++s) {
+      l[s] = lid[ft.ids[ft.cand_off[c] + s]];
+      cand_fac[(size_t)li * kMixedMaxM + s] = l[s];
+      cand_col[(size_t)li * kMixedMaxM + s] = tp.fcol[l[s]];
+    }
+    int32_t* po = pair_of.data() + (size_t)li * kMixedE;
+    int e = 0;
+    for (int i = 0; i < kMixedMaxM; ++i)
+      for (int j = i; j < kMixedMaxM; ++j, ++e)
+        if (i < m && j < m) po[e] = l[i] == l[j] ? 3 * tp.fcol[l[i]] : -2 - cross_id(l[i], l[j]);
+    for (int i = 0; i < m; ++i) {
+      po[Gn + i] = 3 * tp.fcol[l[i]] + 1;
+      po[Gn + kMixedMaxM + i] = 3 * tp.fcol[l[i]] + 2;
+    }
+  }
+  // cross pairs sorted by (a, b); units = runs of equal a
+  const int32_t n_cross = (int32_t)cross.size();
+  std::vector<int32_t> order(n_cross), rank(n_cross), partner(n_cross);
+  std::iota(order.begin(), order.end(), 0);
+  std::sort(order.begin(), order.end(), [&](int32_t x, int32_t y) { return cross[x] < cross[y]; });
+  for (int32_t k = 0; k < n_cross; ++k) {
+    rank[order[k]] = k;
+    partner[k] = cross[order[k]].second;
+  }
+  for (int32_t& p : pair_of)
+    if (p <= -2) p = n_self + rank[-2 - p];
+  std::vector<int4> units;
+  for (int32_t k = 0; k < n_cross;) {
+    const int32_t a = cross[order[k]].first;
+    int32_t e = k;
+    while (e < n_cross && cross[order[e]].first == a) ++e;
+    units.push_back(make_int4(a, k, e, 0));
+    k = e;
+  }
+  const int32_t n_pairs = n_self + n_cross;
+  // row chunks: the evaluator stages X and y (high and low parts) by TMA
+  // when a chunk of d + 1 columns fits; pair sums and the residual pass use
+  // kPairRows blocks
+  bool staged = (size_t)(ds->d + 1) * 2 * 1024 * sizeof(float) <= (size_t)kFacStageBytes;
+  int chunk = staged ? 1024 : 2048;
+  if ((ds->n_pad + chunk - 1) / chunk > 65535) {
+    staged = false;
+    chunk = (int)round_up((ds->n_pad + 65534) / 65535, kFacStep);
+  }
+  const int64_t n_chunks64 = (ds->n_pad + chunk - 1) / chunk;
+  const int n_chunks = (int)n_chunks64;
+  const int n_super = pair_row_blocks(ds->n_pad);
+  const int n_prow = std::max(n_chunks, n_super);
+  if (!d_F.reserve(sizeof(float2) * (size_t)ncol * ds->n_pad) ||
+      !d_P.reserve(sizeof(float2) * (size_t)n_prow * std::max(1, n_pairs)) ||
+      !d_psum.reserve(sizeof(double) * std::max(1, n_pairs)) || !d_fprobe.reserve(sizeof(FacProbe) * nfl) ||
+      !d_fnan.reserve(sizeof(unsigned long long) * ncol)) {
+    rrc::set_error("mixed round: factor table allocation failed");
+    return RRG_E_OOM;
+  }
+  Packer pk;
+  const size_t o_code = pk.add(lcode.data(), sizeof(uint32_t) * lcode.size());
+  const size_t o_meta = pk.add(lmeta.data(), sizeof(int2) * lmeta.size());
+  const size_t o_tcode = pk.add(tp.code.data(), sizeof(uint32_t) * tp.code.size());
+  const size_t o_tmeta = pk.add(tp.meta.data(), sizeof(int2) * tp.meta.size());
+  const size_t o_fcol = pk.add(tp.fcol.data(), sizeof(int32_t) * tp.fcol.size());
+  const size_t o_ccol = pk.add(cand_col.data(), sizeof(int32_t) * cand_col.size());
+  const size_t o_groups = pk.add(groups.data(), sizeof(int2) * groups.size());
+  const size_t o_units = pk.add(units.data(), sizeof(int4) * units.size());
+  const size_t o_partner = pk.add(partner.data(), sizeof(int32_t) * partner.size());
+  const size_t o_pair = pk.add(pair_of.data(), sizeof(int32_t) * pair_of.size());
+  const size_t o_list = pk.add(list, sizeof(int32_t) * cnt);
+  const size_t o_cfac = pk.add(cand_fac.data(), sizeof(int32_t) * cand_fac.size());
+  const size_t o_list2 = pk.add(nullptr, sizeof(int32_t) * cnt);  // filled after the solve
+  rrg_status pst = pk.send(h_ft, d_ft, stream);
+  if (pst != RRG_OK) return pst;
+  const uint32_t* d_code = pk.at<const uint32_t>(d_ft, o_code);
+  const int2* d_meta = pk.at<const int2>(d_ft, o_meta);
+  const int32_t* d_list = pk.at<const int32_t>(d_ft, o_list);
+  const int32_t* d_cfac = pk.at<const int32_t>(d_ft, o_cfac);
+  int32_t* d_list2 = pk.at<int32_t>(d_ft, o_list2);
+  float2* F = static_cast<float2*>(d_F.ptr);
+  float2* P = static_cast<float2*>(d_P.ptr);
+  double* psum = static_cast<double*>(d_psum.ptr);
+  FacProbe* fprobe = static_cast<FacProbe*>(d_fprobe.ptr);
+  unsigned long long* fnan = static_cast<unsigned long long*>(d_fnan.ptr);
+  uint32_t* status = static_cast<uint32_t*>(d_status.ptr);
+  const int fb_cap = std::max(1, (int)host_cands.size());
+  const size_t back_bytes = sizeof(int32_t) * (fb_cap + 1 + kFbReasons) + (size_t)fb_cap;
+  int32_t* fallback = static_cast<int32_t*>(d_fallback.ptr);
+  uint32_t* reasons = reinterpret_cast<uint32_t*>(fallback + fb_cap + 1);
+  uint8_t* pass2 = reinterpret_cast<uint8_t*>(fallback + fb_cap + 1 + kFbReasons);
+  RRG_CUDA(cudaMemsetAsync(d_fallback.ptr, 0, back_bytes, stream));
+  RRG_CUDA(cudaMemsetAsync(d_cert_e.ptr, 0xff, sizeof(double) * fb_cap, stream));  // NaN: no check
+  RRG_CUDA(cudaMemsetAsync(fnan, 0x7f, sizeof(unsigned long long) * ncol, stream));
+
+  cudaEvent_t t0 = mark_begin();
+  FacEvalArgs fa;
+  fa.ds = dd;
+  fa.code = pk.at<const uint32_t>(d_ft, o_tcode);
+  fa.meta = pk.at<const int2>(d_ft, o_tmeta);
+  fa.K = dev.consts32;
+  fa.Klo = dev.consts32lo;
+  fa.chunk = chunk;
+  fa.F = F;
+  fa.P = P;
+  fa.n_pairs = n_pairs;
+  fa.fnan = fnan;
+  fa.status = status;
+  // one launch per level: a level reads the columns of the levels before it
+  for (size_t L = 0, g0 = 0; L < level_groups.size(); ++L) {
+    fa.groups = pk.at<const int2>(d_ft, o_groups) + g0;
+    if (!launch_fac_eval(fa, level_groups[L] - (int)g0, n_chunks, staged, stream)) {
+      cuda_ok(cudaGetLastError(), "factor evaluation launch");
+      return RRG_E_CUDA;
+    }
+    ++launches;
+    g0 = level_groups[L];
+  }
+  mark_end(P_GRAM, t0);
+  t0 = mark_begin();
+  PairArgs pa;
+  pa.F = F;
+  pa.n_pad = ds->n_pad;
+  pa.units = pk.at<const int4>(d_ft, o_units);
+  pa.n_units = (int32_t)units.size();
+  pa.partner = pk.at<const int32_t>(d_ft, o_partner);
+  pa.P = P;
+  pa.n_pairs = n_pairs;
+  pa.cross0 = n_self;
+  if (!launch_pair_sum(pa, n_super, stream)) {
+    cuda_ok(cudaGetLastError(), "pair sum launch");
+    return RRG_E_CUDA;
+  }
+  mark_end(P_PAIRS, t0);
+  t0 = mark_begin();
+  if (!launch_pair_reduce(P, n_pairs, n_chunks, 0, n_self, psum, stream) ||
+      !launch_pair_reduce(P, n_pairs, n_super, n_self, n_pairs, psum, stream) ||
+      !launch_fac_probe(d_code, d_meta, nfl, dev.consts, dev.consts32, dev.consts32lo, dd, fprobe, stream) ||
+      !launch_cand_probe(dev.cands, d_list, cnt, d_cfac, pk.at<const int32_t>(d_ft, o_fcol), fprobe, fnan,
+                         static_cast<ProbeOut*>(d_probe.ptr), static_cast<int64_t*>(d_nanrow.ptr), stream)) {
+    cuda_ok(cudaGetLastError(), "mixed round launch");
+    return RRG_E_CUDA;
+  }
+  SolveArgs sa;
+  sa.b = dev;
+  sa.ds = dd;
+  sa.list = d_list;
+  sa.n_list = cnt;
+  sa.pair_of = pk.at<const int32_t>(d_ft, o_pair);
+  sa.psum = psum;
+  sa.coefs = static_cast<double*>(d_coefs.ptr);
+  sa.terms = static_cast<MixedTerm*>(d_terms.ptr);
+  sa.res = static_cast<rrg_result*>(d_res.ptr);
+  sa.fallback = fallback;
+  sa.fallback_cap = fb_cap;
+  sa.sse1 = static_cast<double*>(d_sse1.ptr);
+  sa.pass2 = pass2;
+  sa.probe = static_cast<const ProbeOut*>(d_probe.ptr);
+  sa.reasons = reasons;
+  sa.nanrow = static_cast<const int64_t*>(d_nanrow.ptr);
+  sa.cert_e = static_cast<double*>(d_cert_e.ptr);
+  sa.rank_tol = 1e-11;
+  sa.fallback_tol = 1e-7;
+  sa.pass2_tol = 1e-8;
+  sa.cert_tol = cert_tol;
+  sa.certify = certify ? 1 : 0;
+  if (!launch_solve(sa, stream)) {
+    cuda_ok(cudaGetLastError(), "mixed solve launch");
+    return RRG_E_CUDA;
+  }
+  mark_end(P_SOLVE, t0);
+  launches += 7;
+  // residual-pass flags (and the fallback list so far) back to the host
+  RRG_CUDA(cudaMemcpyAsync(h_fallback.ptr, d_fallback.ptr, back_bytes, cudaMemcpyDeviceToHost, stream));
+  RRG_CUDA(cudaStreamSynchronize(stream));
+  const int32_t* hf = static_cast<const int32_t*>(h_fallback.ptr);
+  const uint8_t* hp2 = reinterpret_cast<const uint8_t*>(hf + fb_cap + 1 + kFbReasons);
+  std::vector<int32_t> list2;
+  for (int32_t li = 0; li < cnt; ++li)
+    if (hp2[list[li]]) list2.push_back(li);
+  last_pass2 += (int64_t)list2.size();
+  double* sse = static_cast<double*>(d_partial.ptr);
+  if (!list2.empty()) {
+    if (!h_mlist.reserve(sizeof(int32_t) * list2.size())) {
+      rrc::set_error("mixed round: staging allocation failed");
+      return RRG_E_OOM;
+    }
+    std::memcpy(h_mlist.ptr, list2.data(), sizeof(int32_t) * list2.size());
+    RRG_CUDA(cudaMemcpyAsync(d_list2, h_mlist.ptr, sizeof(int32_t) * list2.size(), cudaMemcpyHostToDevice, stream));
+    ResidArgs ra;
+    ra.b = dev;
+    ra.ds = dd;
+    ra.F = F;
+    ra.mlist = d_list;
+    ra.list2 = d_list2;
+    ra.n2 = (int32_t)list2.size();
+    ra.cand_col = pk.at<const int32_t>(d_ft, o_ccol);
+    ra.terms = static_cast<const MixedTerm*>(d_terms.ptr);
+    ra.n_chunks = n_super;
+    ra.sse = sse;
+    t0 = mark_begin();
+    if (!launch_ftab_resid(ra, stream) ||
+        (certify && !launch_cert_resid(d_list, d_list2, ra.n2, sse, n_super, static_cast<const double*>(d_cert_e.ptr),
+                                       dd, cert_tol, fallback, fb_cap, reasons, stream))) {
+      cuda_ok(cudaGetLastError(), "mixed residual launch");
+      return RRG_E_CUDA;
+    }
+    mark_end(P_RESID, t0);
+    launches += certify ? 2 : 1;
+  }
+  t0 = mark_begin();
+  finalize_kernel<<<(cnt + 127) / 128, 128, 0, stream>>>(dev, dd, d_list, 0, cnt, sse, n_super,
+                                                         static_cast<const double*>(d_coefs.ptr),
+                                                         static_cast<rrg_result*>(d_res.ptr), 0u,
+                                                         static_cast<const double*>(d_sse1.ptr));
+  mark_end(P_FINAL, t0);
+  ++launches;
+  if (certify && !list2.empty()) {
+    // the residual-pass checks may have queued more
+    RRG_CUDA(cudaMemcpyAsync(h_fallback.ptr, d_fallback.ptr, sizeof(int32_t) * (fb_cap + 1 + kFbReasons),
+                             cudaMemcpyDeviceToHost, stream));
+    RRG_CUDA(cudaStreamSynchronize(stream));
+  }
+  const uint32_t* hr = reinterpret_cast<const uint32_t*>(hf + fb_cap + 1);
+  for (int i = 0; i < kFbReasons; ++i) last_reasons[i] += hr[i];
+  const int32_t nf = std::min(hf[0], fb_cap);
+  fb_all.insert(fb_all.end(), hf + 1, hf + 1 + nf);
+  RRG_CUDA(cudaGetLastError());
+  return RRG_OK;
+}
+
+// ------------------------------------------------- FP64 over the table ----
+// The listed candidates (absolute indices) scored by the plain FP64 path's
+// arithmetic: their distinct factors evaluated once into an FP64 table, then
+// per candidate the direct column-pivoted QR on [factors | 1 | y] (one block
+// each), the rebuilt sum's residual and the fitness.  `ft` must describe the
+// round's batch.
+rrg_status rrg_context::run_fp64_table(const rrg_dataset* ds, const std::vector<int32_t>& list_in,
+                                       uint32_t flags_or) {
+  if (list_in.empty()) return RRG_OK;
+  // candidates ordered by the QR kernel's column bucket, so that each launch
+  // uses the smallest register footprint its candidates allow
+  auto bucket = [&](int32_t c) {
+    const rrg_cand& cd = host_cands[c];
+    return plain_qr_bucket(cd.mode == RRG_TUNED ? cd.n_factors + 2 : 2);
+  };
+  std::vector<int32_t> list(list_in);
+  std::stable_sort(list.begin(), list.end(), [&](int32_t x, int32_t y) { return bucket(x) < bucket(y); });
+  const DevData dd = ds->view();
+  const size_t col8 = sizeof(double) * (size_t)ds->n_pad;
+  const int64_t fcap = std::max<int64_t>(2 * RRG_MAX_TERMS, (int64_t)(scratch_budget_bytes / 2 / col8));
+  const int64_t mcap = std::max<int64_t>(2 * RRG_MAX_TERMS + 2, (int64_t)(scratch_budget_bytes / 2 / col8));
+  const int nb_res = (int)((ds->n + RR_CHUNK - 1) / RR_CHUNK);
+  const size_t n_all = host_cands.size();
+  if (!d_partial.reserve(sizeof(double) * n_all * (size_t)nb_res)) {
+    rrc::set_error("FP64 round: scratch allocation failed");
+    return RRG_E_OOM;
+  }
+  std::vector<int32_t> lid(ft.meta.size(), -1), lf;
+  size_t pos = 0;
+  while (pos < list.size()) {
+    // candidates whose distinct factors fit the FP64 table
+    lf.clear();
+    size_t end = pos;
+    while (end < list.size()) {
+      const int32_t c = list[end];
+      const int m = cand_factors(host_cands[c]);
+      int fresh = 0;
+      for (int s = 0; s < m; ++s) fresh += lid[ft.ids[ft.cand_off[c] + s]] < 0 ? 1 : 0;
+      if (end > pos && (int64_t)lf.size() + fresh > fcap) break;
+      for (int s = 0; s < m; ++s) {
+        const int32_t g = ft.ids[ft.cand_off[c] + s];
+        if (lid[g] < 0) {
+          lid[g] = (int32_t)lf.size();
+          lf.push_back(g);
+        }
+      }
+      ++end;
+    }
+    const int32_t nfl = (int32_t)lf.size();
+    const int32_t ng = (int32_t)(end - pos);
+    // the factors as one-factor untuned pseudo-candidates writing column i
+    std::vector<uint32_t> fcode;
+    std::vector<rrg_cand> fc(std::max(1, nfl));
+    std::vector<PlainCand> fpc(std::max(1, nfl));
+    for (int32_t i = 0; i < nfl; ++i) {
+      const int2 mt = ft.meta[lf[i]];
+      rrg_cand& p = fc[i];
+      p.code_offset = (int32_t)fcode.size();
+      p.code_len = mt.y;
+      p.first_factor = 0;
+      p.n_factors = 1;
+      p.mode = RRG_UNTUNED;
+      p.coef_offset = 0;
+      p.stack_need = ft.stack[lf[i]];
+      p.reserved = 0;
+      fcode.insert(fcode.end(), ft.code.begin() + mt.x, ft.code.begin() + mt.x + mt.y);
+      fpc[i] = PlainCand{i, 0, 0, 1, 0};
+    }
+    // column map and QR working columns; QR sub-batches by the M budget
+    std::vector<int32_t> colmap;
+    std::vector<PlainCand> pcs(std::max<size_t>(1, n_all));
+    std::vector<std::pair<int32_t, int32_t>> subs;  // [first, end) positions in the group list
+    int64_t mcol = 0, mcols_max = 1;
+    int32_t sub0 = 0;
+    for (int32_t i = 0; i < ng; ++i) {
+      const int32_t c = list[pos + i];
+      const rrg_cand& cd = host_cands[c];
+      const int m = cand_factors(cd);
+      const int32_t k = cd.mode == RRG_TUNED ? cd.n_factors + 1 : 1;
+      const int64_t need = cd.mode == RRG_TUNED ? k + 1 : 0;
+      if (i > sub0 && (mcol + need > mcap || i - sub0 >= 65535)) {
+        subs.push_back({sub0, i});
+        sub0 = i;
+        mcol = 0;
+      }
+      PlainCand& p = pcs[c];
+      p.a_col = (int64_t)colmap.size();
+      p.m_col = mcol;
+      p.s_off = 0;
+      p.k = k;
+      p.pad = 0;
+      mcol += need;
+      mcols_max = std::max(mcols_max, mcol);
+      for (int s = 0; s < m; ++s) colmap.push_back(lid[ft.ids[ft.cand_off[c] + s]]);
+    }
+    subs.push_back({sub0, ng});
+    Packer pk;
+    const size_t o_fcode = pk.add(fcode.data(), sizeof(uint32_t) * fcode.size());
+    const size_t o_fc = pk.add(fc.data(), sizeof(rrg_cand) * fc.size());
+    const size_t o_fpc = pk.add(fpc.data(), sizeof(PlainCand) * fpc.size());
+    const size_t o_cmap = pk.add(colmap.data(), sizeof(int32_t) * std::max<size_t>(1, colmap.size()));
+    const size_t o_pcs = pk.add(pcs.data(), sizeof(PlainCand) * pcs.size());
+    const size_t o_list = pk.add(list.data() + pos, sizeof(int32_t) * ng);
+    rrg_status pst = pk.send(h_ft64, d_ft64, stream);
+    if (pst != RRG_OK) return pst;
+    if (!d_F64.reserve(col8 * std::max(1, nfl)) || !d_M.reserve(col8 * mcols_max)) {
+      rrc::set_error("FP64 round: table allocation failed");
+      return RRG_E_OOM;
+    }
+    double* F64 = static_cast<double*>(d_F64.ptr);
+    double* M = static_cast<double*>(d_M.ptr);
+    const int32_t* d_list = pk.at<const int32_t>(d_ft64, o_list);
+    const PlainCand* d_pcs = pk.at<const PlainCand>(d_ft64, o_pcs);
+    const int32_t* d_cmap = pk.at<const int32_t>(d_ft64, o_cmap);
+    double* coefs = static_cast<double*>(d_coefs.ptr);
+    rrg_result* res = static_cast<rrg_result*>(d_res.ptr);
+    uint32_t* status = static_cast<uint32_t*>(d_status.ptr);
+    double* partial = static_cast<double*>(d_partial.ptr);
+    clear_results_kernel<<<(ng + 255) / 256, 256, 0, stream>>>(d_list, ng, res);
+    // distinct factors, FP64, the plain evaluator (bit-identical values)
+    DevBatch fdev = dev;
+    fdev.cands = pk.at<const rrg_cand>(d_ft64, o_fc);
+    fdev.code = pk.at<const uint32_t>(d_ft64, o_fcode);
+    fdev.n_cand = nfl;
+    fdev.n_code = (int32_t)fcode.size();
+    cudaEvent_t t0 = mark_begin();
+    const int nb = (int)std::max<int64_t>(
+        1, std::min<int64_t>((4LL * sm_count + nfl - 1) / std::max(1, nfl), (ds->n + 1023) / 1024));
+    for (int32_t f0 = 0; f0 < nfl; f0 += 65535) {
+      const int32_t nfb = std::min<int32_t>(65535, nfl - f0);
+      plain_eval_kernel<<<dim3(nb, nfb), 256, plain_eval_smem(), stream>>>(
+          fdev, dd, pk.at<const PlainCand>(d_ft64, o_fpc), nullptr, f0, F64, F64, nullptr, 0, status);
+      ++launches;
+    }
+    mark_end(P_PLAIN_EVAL, t0);
+    ++launches;
+    for (const auto& sb : subs) {
+      const int32_t ns = sb.second - sb.first;
+      if (ns <= 0) continue;
+      t0 = mark_begin();
+      for (int32_t b0 = sb.first; b0 < sb.second;) {
+        const int bk = bucket(list[pos + b0]);
+        int32_t b1 = b0;
+        while (b1 < sb.second && bucket(list[pos + b1]) == bk) ++b1;
+        launch_plain_qr(bk, b1 - b0, stream, dev, dd, d_pcs, d_list, b0, F64, M, nullptr, 0, 1, coefs, res, status,
+                        nullptr, d_cmap);
+        ++launches;
+        b0 = b1;
+      }
+      mark_end(P_PLAIN_QR, t0);
+      t0 = mark_begin();
+      plain_resid_kernel<<<dim3(nb_res, ns), 256, 0, stream>>>(dev, dd, d_pcs, d_list, sb.first, F64, coefs, partial,
+                                                               d_cmap);
+      mark_end(P_PLAIN_RESID, t0);
+      t0 = mark_begin();
+      finalize_kernel<<<(ns + 127) / 128, 128, 0, stream>>>(dev, dd, d_list, sb.first, sb.second, partial, nb_res,
+                                                            coefs, res, flags_or, nullptr);
+      mark_end(P_FINAL, t0);
+      launches += 3;
+    }
+    RRG_CUDA(cudaGetLastError());
+    for (int32_t g : lf) lid[g] = -1;
+    pos = end;
+  }
+  return RRG_OK;
+}
+
+rrg_status rrg_context::run_plain_table(const rrg_dataset* ds, int32_t n_cand) {
+  const char* hb = static_cast<const char*>(h_batch.ptr);
+  build_factor_table(host_cands.data(), n_cand, reinterpret_cast<const uint32_t*>(hb + off_k),
+                     reinterpret_cast<const double*>(hb + off_d), ft);
+  std::vector<int32_t> all(n_cand);
+  std::iota(all.begin(), all.end(), 0);
+  return run_fp64_table(ds, all, 0u);
+}

@@ -16,8 +16,10 @@
 #include <vector>
 
 #include "../common/error.h"
+#include "../common/df32.h"
 #include "../common/rr_sum.h"
 #include "common.cuh"
+#include "ftable.cuh"
 #include "mixed.cuh"
 #include "plain.cuh"
 #include "runtime.cuh"
@@ -187,7 +189,8 @@ rrg_status rrg_context::stage_batch(const rrg_batch* b) {
   off_k = round_up(off_f + sz_f, 256);
   off_d = round_up(off_k + sz_k, 256);
   off_s = round_up(off_d + sz_d, 256);
-  batch_bytes = round_up(off_s + sz_s + 8, 256);
+  off_sl = round_up(off_s + sz_s, 256);
+  batch_bytes = round_up(off_sl + sz_s + 8, 256);
   if (!h_batch.reserve(batch_bytes) || !d_batch.reserve(batch_bytes)) {
     rrc::set_error("cannot reserve batch staging");
     return RRG_E_OOM;
@@ -197,14 +200,21 @@ rrg_status rrg_context::stage_batch(const rrg_batch* b) {
   if (sz_f) std::memcpy(h + off_f, b->factors, sz_f);
   if (sz_k) std::memcpy(h + off_k, b->code, sz_k);
   if (sz_d) std::memcpy(h + off_d, b->consts, sz_d);
+  // constants as double-floats (high part: the FP32 rounding)
   float* c32 = reinterpret_cast<float*>(h + off_s);
-  for (int32_t i = 0; i < b->n_consts; ++i) c32[i] = (float)b->consts[i];
+  float* c32lo = reinterpret_cast<float*>(h + off_sl);
+  for (int32_t i = 0; i < b->n_consts; ++i) {
+    const dfl v = dfl_from_double(b->consts[i]);
+    c32[i] = v.hi;
+    c32lo[i] = v.lo;
+  }
   char* d = static_cast<char*>(d_batch.ptr);
   dev.cands = reinterpret_cast<const rrg_cand*>(d + off_c);
   dev.factors = reinterpret_cast<const rrg_factor*>(d + off_f);
   dev.code = reinterpret_cast<const uint32_t*>(d + off_k);
   dev.consts = reinterpret_cast<const double*>(d + off_d);
   dev.consts32 = reinterpret_cast<const float*>(d + off_s);
+  dev.consts32lo = reinterpret_cast<const float*>(d + off_sl);
   dev.n_cand = b->n_cand;
   dev.n_factors = b->n_factors;
   dev.n_code = b->n_code;
@@ -306,15 +316,17 @@ rrg_status rrg_context::run_plain(const rrg_dataset* ds, int32_t lo, int32_t hi,
     if (predict_only) continue;
     t0 = mark_begin();
     uint8_t* redo = static_cast<uint8_t*>(d_redo.ptr);
-    plain_qr_kernel<<<ns, 256, plain_qr_smem(), stream>>>(dev, dd, pc, dl, sb.p, A, A, S, sb.tsqr ? 1 : 0, sb.nb,
-                                                          coefs, res, status,
-                                                          (sb.tsqr && redo_sensitive) ? redo : nullptr);
+    int kmax = 1;
+    for (int32_t i = sb.p; i < sb.e; ++i) kmax = std::max(kmax, pcs[(*list)[i]].k);
+    launch_plain_qr(kmax + 1, ns, stream, dev, dd, pc, dl, sb.p, A, A, S, sb.tsqr ? 1 : 0, sb.nb, coefs, res, status,
+                    (sb.tsqr && redo_sensitive) ? redo : nullptr, nullptr);
     if (sb.tsqr && redo_sensitive)
-      plain_qr_kernel<<<ns, 256, plain_qr_smem(), stream>>>(dev, dd, pc, dl, sb.p, A, A, S, 0, sb.nb, coefs, res,
-                                                            status, redo);
+      launch_plain_qr(kmax + 1, ns, stream, dev, dd, pc, dl, sb.p, A, A, S, 0, sb.nb, coefs, res, status, redo,
+                      nullptr);
     mark_end(P_PLAIN_QR, t0);
     t0 = mark_begin();
-    plain_resid_kernel<<<dim3(nb_res, ns), 256, 0, stream>>>(dev, dd, pc, dl, sb.p, A, coefs, partial);
+    plain_resid_kernel<<<dim3(nb_res, ns), 256, 0, stream>>>(dev, dd, pc, dl, sb.p, A, coefs, partial,
+                                                             nullptr);
     mark_end(P_PLAIN_RESID, t0);
     t0 = mark_begin();
     finalize_kernel<<<(ns + 127) / 128, 128, 0, stream>>>(dev, dd, dl, sb.p, sb.e, partial, nb_res, coefs, res,
@@ -324,211 +336,6 @@ rrg_status rrg_context::run_plain(const rrg_dataset* ds, int32_t lo, int32_t hi,
   }
   RRG_CUDA(cudaGetLastError());
   return RRG_OK;
-}
-
-// Mixed round.  Candidates are bucketed by factor count (untuned programs use
-// the 1-factor bucket) and sorted by program length within a bucket; programs
-// beyond the mixed kernels' limits go to the FP64 path.  Gram pass + solve for
-// every bucket; the residual pass only for candidates whose one-pass SSE is
-// not accurate enough; ill-conditioned systems are re-solved in FP64.
-rrg_status rrg_context::run_mixed(const rrg_dataset* ds, int32_t n_cand, bool certify) {
-  const DevData dd = ds->view();
-  static const int kBuckets[4] = {1, 2, 4, 8};
-  std::vector<int32_t> bucket[4], plain;
-  for (int32_t c = 0; c < n_cand; ++c) {
-    const rrg_cand& cd = host_cands[c];
-    const bool fits = cd.stack_need <= kMixedStackCap && (cd.mode != RRG_TUNED || cd.n_factors <= kMixedMaxM);
-    if (!fits) {
-      plain.push_back(c);
-      continue;
-    }
-    const int m = cd.mode == RRG_TUNED ? std::max(cd.n_factors, 1) : 1;
-    int b = 0;
-    while (kBuckets[b] < m) ++b;
-    bucket[b].push_back(c);
-  }
-  for (auto& v : bucket)  // longest programs first: the short ones fill the tail of each work unit
-    std::stable_sort(v.begin(), v.end(),
-                     [&](int32_t x, int32_t y) { return host_cands[x].code_len > host_cands[y].code_len; });
-  last_plain_routed = (int64_t)plain.size();
-  // one tile height for the round: the largest multiple of 128 (<= 4096) whose
-  // staging fits next to the stacks and code buffers of every bucket in use
-  int tile = 4096;
-  for (int b = 0; b < 4; ++b)
-    if (!bucket[b].empty())
-      while (tile > 128 && mixed_smem(kBuckets[b], ds->d, tile, true) > 227 * 1024) tile -= 128;
-  if (mixed_tile_override > 0) tile = mixed_tile_override;
-  tile = (int)std::min<int64_t>(tile, ds->n_pad);
-  const int n_tiles = (int)((ds->n_pad + tile - 1) / tile);
-  std::vector<int32_t> lists;
-  int32_t off[5];
-  for (int b = 0; b < 4; ++b) {
-    off[b] = (int32_t)lists.size();
-    lists.insert(lists.end(), bucket[b].begin(), bucket[b].end());
-  }
-  off[4] = (int32_t)lists.size();
-  const int32_t n_mixed = off[4];
-  size_t gram_elems = 0, goff[4];
-  for (int b = 0; b < 4; ++b) {
-    goff[b] = gram_elems;
-    gram_elems += bucket[b].size() * (size_t)n_tiles * mixed_gram_entries(kBuckets[b]);
-  }
-  const int fb_cap = std::max(1, n_cand);
-  const size_t list_bytes = sizeof(int32_t) * (lists.size() * 2 + 8);
-  // fallback list, reason counters, pass2 flags
-  const size_t back_bytes = sizeof(int32_t) * (fb_cap + 1 + kFbReasons) + (size_t)fb_cap;
-  if (!d_mlist.reserve(list_bytes) || !h_mlist.reserve(list_bytes) ||
-      !d_gram.reserve(sizeof(float2) * std::max<size_t>(1, gram_elems)) ||
-      !d_terms.reserve(sizeof(MixedTerm) * fb_cap) || !d_sse1.reserve(sizeof(double) * fb_cap) ||
-      !d_probe.reserve(sizeof(ProbeOut) * fb_cap) || !d_nanrow.reserve(sizeof(int64_t) * fb_cap) ||
-      !d_partial.reserve(sizeof(double) * (size_t)fb_cap * n_tiles) || !d_fallback.reserve(back_bytes) ||
-      !h_fallback.reserve(back_bytes)) {
-    rrc::set_error("mixed round: scratch allocation failed");
-    return RRG_E_OOM;
-  }
-  int32_t* hl = static_cast<int32_t*>(h_mlist.ptr);
-  std::memcpy(hl, lists.data(), sizeof(int32_t) * lists.size());
-  RRG_CUDA(cudaMemcpyAsync(d_mlist.ptr, hl, sizeof(int32_t) * std::max<size_t>(1, lists.size()), cudaMemcpyHostToDevice,
-                           stream));
-  RRG_CUDA(cudaMemsetAsync(d_fallback.ptr, 0, back_bytes, stream));
-  RRG_CUDA(cudaMemsetAsync(d_nanrow.ptr, 0x7f, sizeof(int64_t) * fb_cap, stream));  // "no NaN row"
-  int64_t* nanrow = static_cast<int64_t*>(d_nanrow.ptr);
-  const int32_t* dl = static_cast<const int32_t*>(d_mlist.ptr);
-  float2* gram = static_cast<float2*>(d_gram.ptr);
-  MixedTerm* terms = static_cast<MixedTerm*>(d_terms.ptr);
-  double* sse = static_cast<double*>(d_partial.ptr);
-  double* sse1 = static_cast<double*>(d_sse1.ptr);
-  int32_t* fallback = static_cast<int32_t*>(d_fallback.ptr);
-  uint32_t* reasons = reinterpret_cast<uint32_t*>(fallback + fb_cap + 1);
-  uint8_t* pass2 = reinterpret_cast<uint8_t*>(fallback + fb_cap + 1 + kFbReasons);
-  uint32_t* status = static_cast<uint32_t*>(d_status.ptr);
-  rrg_result* res = static_cast<rrg_result*>(d_res.ptr);
-  double* coefs = static_cast<double*>(d_coefs.ptr);
-
-  ProbeOut* probe = static_cast<ProbeOut*>(d_probe.ptr);
-  {
-    // FP32-versus-FP64 probe of every mixed candidate (certification input)
-    cudaEvent_t t0 = mark_begin();
-    if (!launch_probe(dev, dd, dl, n_mixed, probe, stream)) {
-      cuda_ok(cudaGetLastError(), "mixed probe launch");
-      return RRG_E_CUDA;
-    }
-    mark_end(P_SOLVE, t0);
-    ++launches;
-  }
-  auto make_args = [&](int mmax, const int32_t* list, int32_t cnt, float2* g) {
-    MixedArgs a;
-    a.b = dev;
-    a.ds = dd;
-    a.list = list;
-    a.n_list = cnt;
-    const int nw = mixed_threads(mmax) / 32;
-    const int want_groups = std::max(1, (int)((4LL * sm_count + n_tiles - 1) / n_tiles));
-    a.group = std::max(4 * nw, (cnt + want_groups - 1) / want_groups);
-    a.n_tiles = n_tiles;
-    a.tile = tile;
-    a.n_units = n_tiles * ((cnt + a.group - 1) / a.group);
-    a.gram = g;
-    a.sse = sse;
-    a.terms = terms;
-    a.status = status;
-    a.nanrow = nanrow;
-    return a;
-  };
-  for (int b = 0; b < 4; ++b) {
-    const int32_t cnt = (int32_t)bucket[b].size();
-    if (!cnt) continue;
-    MixedArgs a = make_args(kBuckets[b], dl + off[b], cnt, gram + goff[b]);
-    const int grid = std::min(a.n_units, sm_count);
-    cudaEvent_t t0 = mark_begin();
-    if (!launch_gram(kBuckets[b], a, grid, mixed_smem(kBuckets[b], ds->d, tile, false), stream)) {
-      cuda_ok(cudaGetLastError(), "mixed gram launch");
-      return RRG_E_CUDA;
-    }
-    mark_end(P_GRAM, t0);
-    SolveArgs sa;
-    sa.b = dev;
-    sa.ds = dd;
-    sa.list = dl + off[b];
-    sa.n_list = cnt;
-    sa.n_tiles = n_tiles;
-    sa.mmax = kBuckets[b];
-    sa.gram = gram + goff[b];
-    sa.coefs = coefs;
-    sa.terms = terms;
-    sa.res = res;
-    sa.fallback = fallback;
-    sa.fallback_cap = fb_cap;
-    sa.sse1 = sse1;
-    sa.pass2 = pass2;
-    sa.probe = probe;
-    sa.reasons = reasons;
-    sa.nanrow = nanrow;
-    sa.rank_tol = 1e-11;
-    sa.fallback_tol = 1e-7;
-    sa.pass2_tol = 1e-8;
-    sa.cert_tol = cert_tol;
-    sa.certify = certify ? 1 : 0;
-    t0 = mark_begin();
-    if (!launch_solve(sa, stream)) {
-      cuda_ok(cudaGetLastError(), "mixed solve launch");
-      return RRG_E_CUDA;
-    }
-    mark_end(P_SOLVE, t0);
-    launches += 2;
-  }
-  // fallback list and residual-pass flags back to the host
-  RRG_CUDA(cudaMemcpyAsync(h_fallback.ptr, d_fallback.ptr, back_bytes, cudaMemcpyDeviceToHost, stream));
-  RRG_CUDA(cudaStreamSynchronize(stream));
-  const int32_t* hf = static_cast<const int32_t*>(h_fallback.ptr);
-  const uint32_t* hr = reinterpret_cast<const uint32_t*>(hf + fb_cap + 1);
-  for (int i = 0; i < kFbReasons; ++i) last_reasons[i] = hr[i];
-  const uint8_t* hp2 = reinterpret_cast<const uint8_t*>(hf + fb_cap + 1 + kFbReasons);
-  const int32_t nf = std::min(hf[0], fb_cap);
-  std::vector<int32_t> fb(hf + 1, hf + 1 + nf);
-  std::sort(fb.begin(), fb.end());
-  last_fallback = nf;
-  // residual pass on the flagged candidates, bucket by bucket
-  int32_t* hl2 = hl + lists.size();
-  int32_t n2 = 0, off2[5];
-  for (int b = 0; b < 4; ++b) {
-    off2[b] = n2;
-    for (int32_t c : bucket[b])
-      if (hp2[c]) hl2[n2++] = c;
-  }
-  off2[4] = n2;
-  last_pass2 = n2;
-  if (n2 > 0) {
-    RRG_CUDA(cudaMemcpyAsync(const_cast<int32_t*>(dl) + lists.size(), hl2, sizeof(int32_t) * n2,
-                             cudaMemcpyHostToDevice, stream));
-    for (int b = 0; b < 4; ++b) {
-      const int32_t cnt = off2[b + 1] - off2[b];
-      if (!cnt) continue;
-      MixedArgs a = make_args(kBuckets[b], dl + lists.size() + off2[b], cnt, nullptr);
-      const int grid = std::min(a.n_units, sm_count);
-      cudaEvent_t t0 = mark_begin();
-      if (!launch_resid(kBuckets[b], a, grid, mixed_smem(kBuckets[b], ds->d, tile, true), stream)) {
-        cuda_ok(cudaGetLastError(), "mixed residual launch");
-        return RRG_E_CUDA;
-      }
-      mark_end(P_RESID, t0);
-      ++launches;
-    }
-  }
-  if (n_mixed > 0) {
-    cudaEvent_t t0 = mark_begin();
-    finalize_kernel<<<(n_mixed + 127) / 128, 128, 0, stream>>>(dev, dd, dl, 0, n_mixed, sse, n_tiles, coefs, res, 0u,
-                                                               sse1);
-    mark_end(P_FINAL, t0);
-    ++launches;
-  }
-  RRG_CUDA(cudaGetLastError());
-  rrg_status st = RRG_OK;
-  // FP64 re-scoring goes through the tiled QR on tall data; certified rounds
-  // re-solve its rounding-sensitive candidates by the direct QR
-  if (!plain.empty()) st = run_plain(ds, 0, 0, false, &plain, 0u, true, certify);
-  if (st == RRG_OK && !fb.empty()) st = run_plain(ds, 0, 0, false, &fb, RRG_F_QR_FALLBACK, true, certify);
-  return st;
 }
 
 rrg_status rrg_context::submit(rrg_dataset* ds, const rrg_batch* b, int32_t precision, rrg_result* results,
@@ -564,8 +371,14 @@ rrg_status rrg_context::submit(rrg_dataset* ds, const rrg_batch* b, int32_t prec
   RRG_CUDA(cudaMemsetAsync(d_res.ptr, 0, res_bytes, stream));
   RRG_CUDA(cudaMemsetAsync(d_coefs.ptr, 0, coef_bytes, stream));
   RRG_CUDA(cudaMemsetAsync(d_status.ptr, 0, 64, stream));
-  if (precision == RRG_PLAIN_FP64) st = run_plain(ds, 0, b->n_cand, false);
-  else st = run_mixed(ds, b->n_cand, precision == RRG_MIXED_CERTIFIED);
+  if (precision == RRG_PLAIN_FP64) {
+    // few candidates on tall data: the tiled QR spreads each over the GPU;
+    // otherwise one block per candidate over the shared FP64 factor table
+    if (ds->n >= 65536 && b->n_cand < 2 * sm_count) st = run_plain(ds, 0, b->n_cand, false);
+    else st = run_plain_table(ds, b->n_cand);
+  } else {
+    st = run_mixed(ds, b->n_cand, precision == RRG_MIXED_CERTIFIED);
+  }
   if (st != RRG_OK) return st;
   RRG_CUDA(cudaMemcpyAsync(h_res.ptr, d_res.ptr, res_bytes, cudaMemcpyDeviceToHost, stream));
   RRG_CUDA(cudaMemcpyAsync(h_coefs.ptr, d_coefs.ptr, coef_bytes, cudaMemcpyDeviceToHost, stream));
@@ -634,16 +447,17 @@ rrg_context::~rrg_context() {
   d_status.release();
   d_list.release();
   d_redo.release();
-  d_gram.release();
   d_terms.release();
-  d_mlist.release();
   d_fallback.release();
   d_sse1.release();
   d_probe.release();
   d_nanrow.release();
+  d_cert_e.release();
   h_mlist.release();
   h_fallback.release();
-  mixed_scratch.release();
+  for (DevBuf* bf : {&d_ft, &d_ft64, &d_F, &d_P, &d_psum, &d_fprobe, &d_fnan, &d_F64, &d_M}) bf->release();
+  h_ft.release();
+  h_ft64.release();
   h_batch.release();
   h_res.release();
   h_coefs.release();
@@ -658,6 +472,7 @@ DevData rrg_dataset::view() const {
   DevData v;
   v.X64 = X64;
   v.X32 = X32;
+  v.X32lo = X32lo;
   v.y64 = y64;
   v.y32 = y32;
   v.y32lo = y32lo;
@@ -695,7 +510,8 @@ rrg_status rrg_context_create(int32_t device, rrg_context** out) {
   ctx->sm_count = prop.multiProcessorCount;
   size_t free_b = 0, total_b = 0;
   cudaMemGetInfo(&free_b, &total_b);
-  ctx->scratch_budget_bytes = std::min<size_t>((size_t)8 << 30, free_b / 4);
+  ctx->scratch_budget_bytes = std::min<size_t>((size_t)64 << 30, free_b / 3);
+  ctx->table_budget_bytes = std::min<size_t>((size_t)32 << 30, free_b / 5);
   if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreateWithFlags(&ctx->done, cudaEventDisableTiming) != cudaSuccess) {
     cuda_ok(cudaGetLastError(), "stream creation");
@@ -704,7 +520,7 @@ rrg_status rrg_context_create(int32_t device, rrg_context** out) {
   }
   if (cudaFuncSetAttribute(plain_eval_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)plain_eval_smem()) !=
           cudaSuccess ||
-      !rrd::mixed_allow_smem()) {
+      !rrd::fac_allow_smem()) {
     cuda_ok(cudaGetLastError(), "kernel attributes");
     delete ctx;
     return RRG_E_CUDA;
@@ -747,6 +563,7 @@ rrg_status rrg_dataset_create(rrg_context* ctx, const double* X_col, const doubl
   const size_t b64 = sizeof(double) * ds->n_pad * cols, b32 = sizeof(float) * ds->n_pad * cols;
   const size_t y64b = sizeof(double) * ds->n_pad, y32b = sizeof(float) * ds->n_pad;
   if (cudaMalloc(&ds->X64, b64) != cudaSuccess || cudaMalloc(&ds->X32, b32) != cudaSuccess ||
+      cudaMalloc(&ds->X32lo, b32) != cudaSuccess ||
       cudaMalloc(&ds->y64, y64b) != cudaSuccess || cudaMalloc(&ds->y32, y32b) != cudaSuccess ||
       cudaMalloc(&ds->y32lo, y32b) != cudaSuccess) {
     cudaGetLastError();
@@ -769,7 +586,7 @@ rrg_status rrg_dataset_create(rrg_context* ctx, const double* X_col, const doubl
   bool ok = cudaMemcpyAsync(ds->X64, hx, b64, cudaMemcpyHostToDevice, st) == cudaSuccess &&
             cudaMemcpyAsync(ds->y64, hx + cols * ds->n_pad, y64b, cudaMemcpyHostToDevice, st) == cudaSuccess;
   if (ok)
-    ok = launch_to_f32(ds->X64, ds->X32, ds->n_pad * cols, st) &&
+    ok = launch_split_f32(ds->X64, ds->X32, ds->X32lo, ds->n_pad * cols, st) &&
          launch_split_f32(ds->y64, ds->y32, ds->y32lo, ds->n_pad, st);
   ok = ok && cudaStreamSynchronize(st) == cudaSuccess;
   stage.release();
@@ -788,6 +605,7 @@ rrg_status rrg_dataset_destroy(rrg_dataset* ds) {
   if (ds->ctx && ds->ctx->in_flight) cudaEventSynchronize(ds->ctx->done);
   if (ds->X64) cudaFree(ds->X64);
   if (ds->X32) cudaFree(ds->X32);
+  if (ds->X32lo) cudaFree(ds->X32lo);
   if (ds->y64) cudaFree(ds->y64);
   if (ds->y32) cudaFree(ds->y32);
   if (ds->y32lo) cudaFree(ds->y32lo);

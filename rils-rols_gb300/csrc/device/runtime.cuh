@@ -26,6 +26,7 @@ struct rrg_dataset {
   int32_t d = 0;
   double* X64 = nullptr;
   float* X32 = nullptr;
+  float* X32lo = nullptr;
   double* y64 = nullptr;
   float* y32 = nullptr;
   float* y32lo = nullptr;
@@ -33,25 +34,42 @@ struct rrg_dataset {
   rrd::DevData view() const;
 };
 
+// Distinct factor programs of a round's batch (host side), shared by the
+// candidates that use them.
+struct FactorTable {
+  std::vector<uint32_t> code;      // programs in id order, each ending in EMIT 0
+  std::vector<int2> meta;          // [f] (code offset, length)
+  std::vector<int32_t> stack;      // [f] spill depth
+  std::vector<int32_t> occ;        // [f] factor instances in the batch
+  std::vector<int32_t> cand_off;   // [c] first entry of candidate c in ids (n_cand + 1 entries)
+  std::vector<int32_t> ids;        // factor id of every factor slot, candidates in order
+};
+void build_factor_table(const rrg_cand* cands, int32_t n_cand, const uint32_t* code, const double* consts,
+                        FactorTable& ft);
+
 struct rrg_context {
   int device = 0;
   int sm_count = 0;
-  size_t scratch_budget_bytes = 0;
+  size_t scratch_budget_bytes = 0;  // FP64 tables and QR working columns
+  size_t table_budget_bytes = 0;    // FP32 factor table of a mixed round
   cudaStream_t stream = nullptr;
   cudaEvent_t done = nullptr;
   // batch staging
   HostBuf h_batch;
   DevBuf d_batch;
-  size_t off_c = 0, off_f = 0, off_k = 0, off_d = 0, off_s = 0, batch_bytes = 0;
+  size_t off_c = 0, off_f = 0, off_k = 0, off_d = 0, off_s = 0, off_sl = 0, batch_bytes = 0;
   rrd::DevBatch dev{};
   std::vector<rrg_cand> host_cands;
   // plain scratch
   DevBuf d_A, d_S, d_pc, d_partial, d_list, d_redo;
   HostBuf h_pc, h_list;
   // mixed scratch
-  DevBuf d_gram, d_terms, d_mlist, d_fallback, d_sse1, d_probe, d_nanrow;
+  DevBuf d_terms, d_fallback, d_sse1, d_probe, d_nanrow, d_cert_e;
   HostBuf h_mlist, h_fallback;
-  DevBuf mixed_scratch;
+  // factor tables
+  FactorTable ft;
+  HostBuf h_ft, h_ft64;
+  DevBuf d_ft, d_ft64, d_F, d_P, d_psum, d_fprobe, d_fnan, d_F64, d_M;
   // results
   DevBuf d_res, d_coefs, d_status;
   HostBuf h_res, h_coefs, h_status;
@@ -65,13 +83,12 @@ struct rrg_context {
   // mixed-round statistics of the last round
   int64_t last_fallback = 0, last_plain_routed = 0, last_pass2 = 0;
   int64_t last_reasons[16] = {0};
-  int32_t mixed_tile_override = 0;
   // certified bound on the relative fitness error of a mixed result; larger
   // bounds are re-scored by the FP64 path
   double cert_tol = 5e-7;
   // optional per-phase device timing (CUDA events on the context stream)
   bool timing = false;
-  enum Phase { P_GRAM = 0, P_SOLVE, P_RESID, P_FINAL, P_PLAIN_EVAL, P_PLAIN_QR, P_PLAIN_RESID, P_COUNT };
+  enum Phase { P_GRAM = 0, P_SOLVE, P_RESID, P_FINAL, P_PLAIN_EVAL, P_PLAIN_QR, P_PLAIN_RESID, P_PAIRS, P_COUNT };
   std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> marks;
   std::vector<cudaEvent_t> event_pool;
   size_t event_next = 0;
@@ -87,7 +104,15 @@ struct rrg_context {
   rrg_status run_plain(const rrg_dataset* ds, int32_t lo, int32_t hi, bool predict_only,
                        const std::vector<int32_t>* list = nullptr, uint32_t flags_or = 0, bool tiled_any = false,
                        bool redo_sensitive = true);
+  // mixed round over the shared FP32 factor table; FP64 re-scoring of the
+  // candidates it cannot decide
   rrg_status run_mixed(const rrg_dataset* ds, int32_t n_cand, bool certify);
+  rrg_status mixed_subround(const rrg_dataset* ds, const int32_t* list, int32_t cnt, const std::vector<int32_t>& lf,
+                            const std::vector<int32_t>& lid, bool certify, std::vector<int32_t>& fb_all);
+  // plain FP64 arithmetic over a shared FP64 factor table with the direct QR
+  // per candidate (bit-identical to run_plain's direct QR)
+  rrg_status run_fp64_table(const rrg_dataset* ds, const std::vector<int32_t>& list, uint32_t flags_or);
+  rrg_status run_plain_table(const rrg_dataset* ds, int32_t n_cand);
   rrg_status submit(rrg_dataset* ds, const rrg_batch* b, int32_t precision, rrg_result* results, double* coefs);
   rrg_status wait(int32_t timeout_ms);
   ~rrg_context();

@@ -131,15 +131,17 @@ class Context:
         d["rescore_reasons"] = {r: out[4 + i] for i, r in enumerate(self.REASONS) if out[4 + i]}
         return d
 
-    PHASES = ("mixed_gram", "mixed_solve", "mixed_residual", "finalize", "fp64_eval", "fp64_qr", "fp64_residual")
+    PHASES = ("factor_eval", "mixed_solve", "mixed_residual", "finalize", "fp64_eval", "fp64_qr", "fp64_residual",
+              "pair_sums")
 
     def set_timing(self, on: bool = True) -> None:
         check(self.lib.rrg_context_set_timing(self.h, int(on)), "rrg_context_set_timing")
 
     def last_round_timing(self) -> dict:
-        ms = (C.c_double * 7)()
-        cnt = (C.c_int64 * 7)()
-        self.lib.rrg_last_round_timing(self.h, ms, cnt, 7)
+        n = len(self.PHASES)
+        ms = (C.c_double * n)()
+        cnt = (C.c_int64 * n)()
+        self.lib.rrg_last_round_timing(self.h, ms, cnt, n)
         return {p: (ms[i], cnt[i]) for i, p in enumerate(self.PHASES)}
 
     def stream(self) -> int:
