@@ -1,17 +1,18 @@
 """Benchmark of the RILS-ROLS fitness path on GB300.
 
 Metric: candidate fitness evaluations per second (tune_constants + fitness of
-rils_rols_cpp.cpp:445-541 per candidate) at n = 1M rows.
+rils_rols_cpp.cpp:445-541 per candidate) at n = 1M rows, in the certified
+mixed-precision form: every fitness within 1e-6 relative of the FP64 path.
 
 Workload (one step): the local-search rounds of a search on the 1M-row,
 5-feature regression problem (X ~ U(-3, 3), y = 2.5 x1 x2 - sin(x3)/(1+x4^2) +
 0.7 exp(0.3 x5) + 0.5% noise): every local-search candidate (all_candidates,
 rils_rols_cpp.cpp:348-443) of the eight intermediate models in
 synth.REGRESSION_1M_TRAJECTORY, 7083 tuned candidates, scored in one batched
-round of the mixed-precision path.  Synthetic, seeded data; nothing is
-downloaded.  The same numbers are reported for 8192 random trees drawn like
-the standalone batched-fitness configuration (sizes 3..50 over
-+ - * / sin cos ln exp sqrt, leaves x_j or U(-5, 5)).
+round.  Synthetic, seeded data; nothing is downloaded.  The same numbers are
+reported for 8192 random trees drawn like the standalone batched-fitness
+configuration (sizes 3..50 over + - * / sin cos ln exp sqrt, leaves x_j or
+U(-5, 5)).
 
   value  device-resident: dataset in HBM, each step = one rrg_eval round
          (batch upload, kernels, result download), timed with CUDA events on
@@ -20,9 +21,10 @@ the standalone batched-fitness configuration (sizes 3..50 over
          flattened, X and y are uploaded from pinned host memory
          (rrg_dataset_create), the round runs and the results come back.
 
-Reported beside it: the plain FP64 path's unbatched launch (one candidate per
-round), the mixed-vs-FP64 fitness error of every candidate, the roofline of
-the dominant kernel, the CPU oracle timed on the host cores, clocks.
+Reported beside it: the uncertified mixed form, the plain FP64 path batched
+and unbatched (one candidate per round), the fitness error of every
+candidate against the FP64 path, the roofline of the dominant kernel, the
+CPU oracle timed on the host cores, clocks.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 """
@@ -44,7 +46,7 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT / "rils-rols_gb300"))
 sys.path.insert(0, str(ROOT))
 
-METRIC = "candidate fitness evals/s at n=1M (mixed precision, batched local-search round)"
+METRIC = "candidate fitness evals/s at n=1M (certified mixed precision, batched local-search round)"
 UNIT = "evals/s"
 N_ROWS = 1_000_000
 N_FEAT = 5
@@ -67,7 +69,8 @@ def config(n, batch):
                         f"x n={n} rows, d={N_FEAT}",
             "n_rows": n, "n_features": N_FEAT, "batch": batch,
             "candidates": "all_candidates(model, local_search) of 8 models on the way to the generating formula",
-            "precision": "RRG_MIXED: FP32 eval, exact-product Gram sums, FP64 Cholesky / SSE",
+            "precision": "RRG_MIXED_CERTIFIED: double-float factor table, FP64 Cholesky / SSE, every result within "
+                         "1e-6 of the FP64 path (rank-ambiguous and non-finite candidates re-scored by the exact QR)",
             "l2": "flushed (256 MB write on the round's stream) before every timed step"}
 
 
@@ -230,26 +233,28 @@ def run_ours(args):
     stream = torch.cuda.ExternalStream(ctx.stream(), device=torch.device("cuda", local))
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=torch.device("cuda", local))
 
-    for _ in range(args.warmup):
-        ds.evaluate(batch, MIXED)
-    ctx.set_timing(True)
-    phase_ms, phase_n = {}, {}
-    times = []
-    launches = 0
-    barrier(world)
-    torch.cuda.synchronize()
-    with ClockSampler(local) as clk:
-        for _ in range(args.steps):
-            dt, out = timed_round(ctx, ds, batch, MIXED, stream, flush)
+    def timed_rounds(prec, steps):
+        """(seconds per round list, last output, launches, phase ms sums, phase launch counts, stats)"""
+        ctx.set_timing(True)
+        phase_ms, phase_n, times, launches, out = {}, {}, [], 0, None
+        for _ in range(steps):
+            dt, out = timed_round(ctx, ds, batch, prec, stream, flush)
             times.append(dt)
             launches += ctx.last_round_launches()
             for k, (ms, cnt) in ctx.last_round_timing().items():
                 phase_ms[k] = phase_ms.get(k, 0.0) + ms
                 phase_n[k] = phase_n.get(k, 0) + cnt
+        ctx.set_timing(False)
+        return times, out, launches, phase_ms, phase_n, ctx.last_round_stats()
+
+    for _ in range(args.warmup):
+        ds.evaluate(batch, CERTIFIED)
+    barrier(world)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        times, cert, launches, phase_ms, phase_n, stats = timed_rounds(CERTIFIED, args.steps)
     torch.cuda.synchronize()
     barrier(world)
-    stats = ctx.last_round_stats()
-    ctx.set_timing(False)
     value, t_max = aggregate(B * args.steps, sum(times), world)
 
     # e2e: trees in, fitness out, through the C ABI from host buffers
@@ -261,7 +266,7 @@ def run_ours(args):
         t = time.perf_counter()
         b = encode(trees, tuned=True)
         d2 = ctx.dataset(Xp, yp)
-        d2.evaluate(b, MIXED)
+        d2.evaluate(b, CERTIFIED)
         d2.close()
         torch.cuda.synchronize()
         if step >= args.warmup:
@@ -274,37 +279,30 @@ def run_ours(args):
         return
     res = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps, "higher_is_better": True,
-           "scaling": "weak", "vs_baseline": None, "dtype": "f32/f64", "data": "synthetic (seeded)",
+           "scaling": "weak", "vs_baseline": None, "dtype": "df32/f64", "data": "synthetic (seeded)",
            "config": config(args.n, B),
            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
            "gpu_launches": int(launches), "round_stats": stats}
-    gram_ms, gram_n = phase_ms.get("factor_eval", 0.0), max(1, phase_n.get("factor_eval", 1))
-    avg_launch_s = gram_ms / 1e3 / gram_n
-    algo_bytes = args.n * (N_FEAT + 1) * 4  # X (FP32) and y read once per launch
-    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
-    peak = peaks.get("hbm_gbs", 6800.0)
-    achieved = algo_bytes / avg_launch_s / 1e9 if avg_launch_s > 0 else 0.0
-    res["roofline"] = {"kernel": "mixed_pass_kernel (gram pass)", "bound": "hbm", "achieved": achieved,
-                       "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                       "traffic": read_profile_traffic(), "peak_source": "measured" if peaks else "fallback",
-                       "note": "instruction-issue-bound interpreter (FP32 / ALU): far below the HBM roofline"}
     res["phase_ms_per_step"] = {k: v / args.steps for k, v in phase_ms.items() if v > 0}
+    res["roofline"] = roofline(res["phase_ms_per_step"], phase_n, args.steps, args.n)
     res["clocks"] = clk.summary()
     if args.quick:
         print(json.dumps(res))
         return
-    # certified mixed form: every fitness within 1e-6 of the FP64 path or re-scored in FP64
-    dt_c, cert = timed_round(ctx, ds, batch, CERTIFIED, stream, flush)
-    res["certified"] = {"evals_per_s": B / dt_c, "round_stats": ctx.last_round_stats()}
+    # uncertified mixed form: the same round without the FP64 re-scoring of
+    # rank-ambiguous candidates
+    mtimes, mixed, _, mphase, _, mstats = timed_rounds(MIXED, max(2, args.steps // 2))
+    res["mixed_uncertified"] = {"evals_per_s": B * len(mtimes) / sum(mtimes), "round_stats": mstats,
+                                "phase_ms_per_step": {k: v / len(mtimes) for k, v in mphase.items() if v > 0}}
     # random-tree batch (standalone batched-fitness generator) at the same n
     rb = encode(rand_trees, tuned=True)
-    ds.evaluate(rb, MIXED)
-    dt_r, _ = timed_round(ctx, ds, rb, MIXED, stream, flush)
-    rs = ctx.last_round_stats()
+    ds.evaluate(rb, CERTIFIED)
     dt_rc, _ = timed_round(ctx, ds, rb, CERTIFIED, stream, flush)
-    res["random_trees_8192"] = {"mixed_evals_per_s": len(rand_trees) / dt_r, "mixed_round_stats": rs,
-                                "certified_evals_per_s": len(rand_trees) / dt_rc,
-                                "certified_round_stats": ctx.last_round_stats()}
+    rcs = ctx.last_round_stats()
+    dt_r, _ = timed_round(ctx, ds, rb, MIXED, stream, flush)
+    res["random_trees_8192"] = {"certified_evals_per_s": len(rand_trees) / dt_rc, "certified_round_stats": rcs,
+                                "mixed_evals_per_s": len(rand_trees) / dt_r,
+                                "mixed_round_stats": ctx.last_round_stats()}
     # plain FP64: unbatched launches and the whole batch (accuracy reference)
     singles = [encode([t], tuned=True) for t in trees[:args.unbatched_sample]]
     ds.evaluate(singles[0], PLAIN)
@@ -318,27 +316,66 @@ def run_ours(args):
     plain = ds.evaluate(batch, PLAIN)
     res["plain_fp64_unbatched_evals_per_s"] = unbatched
     res["plain_fp64_batched_evals_per_s"] = B / (time.perf_counter() - t)
-    res["mixed_over_plain_unbatched"] = value / world / unbatched
-    res["certified_over_plain_unbatched"] = res["certified"]["evals_per_s"] / unbatched
-    res["accuracy_vs_fp64"] = {"mixed": accuracy(out, plain), "certified": accuracy(cert, plain),
+    res["certified_over_plain_unbatched"] = value / world / unbatched
+    res["mixed_over_plain_unbatched"] = res["mixed_uncertified"]["evals_per_s"] / unbatched
+    res["accuracy_vs_fp64"] = {"certified": accuracy(cert, plain), "mixed_uncertified": accuracy(mixed, plain),
                                "fitness": "(1 + (1 - R2)) (1 + RMSE) (1 + 0.001 size)"}
     res["cpu_baseline"] = cpu_baseline(X, y, trees, args.cpu_sample)
-    res["mixed_over_cpu_baseline"] = value / world / res["cpu_baseline"]["value"]
+    res["certified_over_cpu_baseline"] = value / world / res["cpu_baseline"]["value"]
     print(json.dumps(res))
 
 
-def read_profile_traffic():
-    """DRAM bytes per launch of the gram pass from the committed ncu summary."""
-    p = ROOT / "profiles" / "mixed_gram_pass.txt"
+# kernels behind the timed phases, with the algorithmic bytes of one launch
+PHASE_KERNELS = {
+    "factor_eval": "fac_eval_kernel (double-float factor table)",
+    "pair_sums": "pair_sum_kernel",
+    "mixed_residual": "ftab_resid_kernel",
+    "fp64_eval": "plain_eval_kernel (FP64 table)",
+    "fp64_qr": "plain_qr_kernel_t (direct column-pivoted QR, FP64)",
+}
+
+
+def roofline(phase_ms, phase_n, steps, n):
+    """Roofline of the phase with the largest time.  Its bytes are algorithmic:
+    the FP64 table written once (8 B per row and column) for the evaluators,
+    every column read once for the QR and the sums; these kernels are bound by
+    the FP32 / FP64 pipes (see profiles/), so the HBM fraction is small."""
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    peak = peaks.get("hbm_gbs", 6800.0)
+    cand = {k: v for k, v in phase_ms.items() if k in PHASE_KERNELS}
+    if not cand:
+        return None
+    top = max(cand, key=cand.get)
+    launches = max(1, phase_n.get(top, 1)) / steps
+    ms_per_launch = cand[top] / launches
+    traffic = read_profile_traffic(top)
+    algo = traffic.get("algorithmic_bytes_per_launch") if traffic else None
+    achieved = algo / (ms_per_launch / 1e3) / 1e9 if algo else None
+    return {"kernel": PHASE_KERNELS[top], "phase": top, "bound": "hbm", "achieved": achieved, "peak": peak,
+            "unit": "GB/s", "frac": (achieved / peak) if achieved else None,
+            "traffic": traffic.get("dram_bytes_per_launch") if traffic else None,
+            "ms_per_launch": ms_per_launch, "launches_per_step": launches,
+            "peak_source": "measured" if peaks else "fallback",
+            "compute_bound": traffic.get("pipe") if traffic else None}
+
+
+def read_profile_traffic(phase):
+    """Figures of the committed ncu summary of the phase's kernel at the
+    bench's size: lines `key=value` in profiles/<phase>_1m.txt."""
+    p = ROOT / "profiles" / f"{phase}_1m.txt"
     if not p.exists():
         return None
+    out = {}
     for line in p.read_text().splitlines():
-        if line.startswith("traffic_bytes_per_launch_full_size"):
+        if "=" in line and not line.startswith(" ") and line.split("=")[0] in (
+                "algorithmic_bytes_per_launch", "dram_bytes_per_launch", "pipe"):
+            k, v = line.split("=", 1)
+            v = v.strip().split()[0]
             try:
-                return float(line.split("=")[1].split()[0])
-            except (IndexError, ValueError):
-                return None
-    return None
+                out[k] = float(v)
+            except ValueError:
+                out[k] = v
+    return out
 
 
 # -------------------------------------------------------------- reference --

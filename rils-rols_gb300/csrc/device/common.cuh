@@ -48,6 +48,12 @@ struct PlainCand {
   int32_t pad;
 };
 
+// Internal instructions of table programs (never in a submitted batch: the
+// batch validation rejects them): read table column `arg` of the same rows.
+constexpr int kOpLDT = 12;   // TOS = T[arg]
+constexpr int kOpPST = 13;   // spill TOS; TOS = T[arg]
+constexpr int kSrcT = 3;     // binary operand from table column `arg`
+
 constexpr double kEps12 = 1e-12;  // value_zero / value_one threshold (node.h:13-14)
 
 __host__ __device__ inline int64_t round_up(int64_t a, int64_t b) { return (a + b - 1) / b * b; }

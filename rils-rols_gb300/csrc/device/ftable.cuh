@@ -22,11 +22,6 @@ constexpr int kPairBatch = 16;        // partners reduced together
 constexpr int kPairRows = 4096;       // rows per pair-sum / residual block
 constexpr int kResidThreads = 256;
 
-// Internal instructions of table programs (never in a submitted batch: the
-// batch validation rejects them): read table column `arg` of the same rows.
-constexpr int kOpLDT = 12;   // TOS = T[arg]
-constexpr int kOpPST = 13;   // spill TOS; TOS = T[arg]
-constexpr int kSrcT = 3;     // binary operand from table column `arg`
 
 // Self pairs of factor f sit at pair index 3f (f*f), 3f+1 (f*1), 3f+2 (f*y);
 // cross pairs follow from 3 * n_factors.

@@ -138,7 +138,11 @@ __global__ void __launch_bounds__(128) mixed_solve_kernel(SolveArgs a) {
   const rrg_cand cd = a.b.cands[c];
   const double* ent = red[warp];
   const double yy = a.ds.yy;
-  const double kU = 1e-11;  // relative accuracy of the double-float Gram sums
+  // Relative accuracy of the double-float Gram sums with respect to the sums
+  // of the absolute values of their terms: about 5u^2 per product and 3u^2
+  // per double-float addition (u = 2^-24) over at most ~90 sequential
+  // additions per sum, plus the FP64 sum of the chunk partials: about 4e-13.
+  const double kU = 1e-12;
   auto queue_fallback = [&](int why) {
     const int slot = atomicAdd(a.fallback, 1);
     if (slot < a.fallback_cap) a.fallback[1 + slot] = c;
@@ -176,7 +180,7 @@ __global__ void __launch_bounds__(128) mixed_solve_kernel(SolveArgs a) {
       sse = __longlong_as_double(0x7ff8000000000000ll);
     } else {
       sse = __dadd_rn(__dsub_rn(yy, __dmul_rn(2.0, fy)), ff);
-      const double bound = kU * (yy + 2.0 * fabs(fy) + ff);
+      const double bound = kU * (yy + 2.0 * sqrt(fabs(ff) * yy) + ff);
       if (!(sse > 0.0 && bound <= a.pass2_tol * sse)) {
         // the residual pass gives the SSE; certified rounds check it after
         p2 = 1;
@@ -398,13 +402,16 @@ __global__ void __launch_bounds__(128) mixed_solve_kernel(SolveArgs a) {
   if (has_nan || !finite) {
     sse = has_nan ? __longlong_as_double(0x7ff8000000000000ll) : -1.0;
   } else {
+    // mag bounds the sums of |terms| behind every entry used (Cauchy-Schwarz:
+    // sum |f_i f_j| <= sqrt(G_ii G_jj), sum |f_i y| <= sqrt(G_ii y'y))
     double lin = 0.0, quad = 0.0, mag = yy;
     for (int i = 0; i < k; ++i) {
+      const double si = sqrt(fabs(G[i][i]));
       lin += ceff[i] * bvec[i];
-      mag += 2.0 * fabs(ceff[i] * bvec[i]);
+      mag += 2.0 * fabs(ceff[i]) * si * sqrt(yy);
       for (int j = 0; j < k; ++j) {
         quad += ceff[i] * ceff[j] * G[i][j];
-        mag += fabs(ceff[i] * ceff[j] * G[i][j]);
+        mag += fabs(ceff[i] * ceff[j]) * si * sqrt(fabs(G[j][j]));
       }
     }
     sse = yy - 2.0 * lin + quad;

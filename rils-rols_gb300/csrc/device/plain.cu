@@ -54,8 +54,9 @@ __device__ __forceinline__ double bin64(int base, double a, double b) {
 
 // Runs the code of one candidate on `row`; factor slot s is written to
 // out[s * n_pad + row].  Spill stack in shared memory, stride blockDim.x.
+// Table programs also read columns of T (same rows, column stride n_pad).
 __device__ __forceinline__ void run_row64(const uint32_t* code, int len, const double* consts, const DevData& ds,
-                                          int64_t row, double* st, double* out, uint32_t* status) {
+                                          int64_t row, double* st, double* out, const double* T, uint32_t* status) {
   double tos = 0.0;
   int sp = 0;
   const int stride = blockDim.x;
@@ -82,6 +83,12 @@ __device__ __forceinline__ void run_row64(const uint32_t* code, int len, const d
       case RRG_OP_EXP: tos = rr_exp(tos); break;
       case RRG_OP_SQRT: tos = __dsqrt_rn(tos); break;
       case RRG_OP_SQR: tos = __dmul_rn(tos, tos); break;
+      case kOpLDT: tos = T[(int64_t)arg * ds.n_pad + row]; break;
+      case kOpPST:
+        if (sp >= RRG_MAX_STACK) { atomicOr(status, ST_STACK); return; }
+        st[sp++ * stride] = tos;
+        tos = T[(int64_t)arg * ds.n_pad + row];
+        break;
       case RRG_OP_EMIT:
         out[(int64_t)arg * ds.n_pad + row] = tos;
         sp = 0;
@@ -96,6 +103,8 @@ __device__ __forceinline__ void run_row64(const uint32_t* code, int len, const d
           other = st[--sp * stride];
         } else if (src == RRG_SRC_V) {
           other = ds.X64[(int64_t)arg * ds.n_pad + row];
+        } else if (src == kSrcT) {
+          other = T[(int64_t)arg * ds.n_pad + row];
         } else {
           other = consts[arg];
         }
@@ -195,7 +204,7 @@ __global__ void __launch_bounds__(256) plain_eval_kernel(DevBatch b, DevData ds,
   const uint32_t* code = staged ? code_s : b.code + cd.code_offset;
   double* Ac = A + pc[c].a_col * ds.n_pad;
   for (int64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x)
-    run_row64(code, cd.code_len, b.consts, ds, r, st, Ac, status);
+    run_row64(code, cd.code_len, b.consts, ds, r, st, Ac, A, status);
   if (!tsqr || cd.mode != RRG_TUNED) return;
 
   // TSQR: [A | 1 | y] of this slice -> R (k x (k+1)) into S block blockIdx.x
@@ -243,6 +252,30 @@ __device__ __forceinline__ void block_sum_vec_t(const double (&part)[KB], int cn
   __syncthreads();
 }
 
+// a / b correctly rounded (the value of __ddiv_rn), for many a and one b,
+// with y = RN(1 / b): q0 = RN(a y), Markstein's correction
+// q1 = RN(q0 + (a - q0 b) y), and q1 is accepted when its exact remainder
+// a - q1 b (one FMA) is below half an ulp of q1 times |b| in magnitude,
+// which makes q1 the correctly rounded quotient.  A power-of-two q1 (whose
+// lower neighbour is closer than half an ulp), a q1 outside the normal range
+// and a bound outside the normal range take __ddiv_rn.
+__device__ __forceinline__ double div_by(double a, double b, double y) {
+  const double q0 = __dmul_rn(a, y);
+  const double r = __fma_rn(-q0, b, a);
+  const double q1 = __fma_rn(r, y, q0);
+  const double r1 = __fma_rn(-q1, b, a);
+  const long long qb = __double_as_longlong(q1);
+  const int e = (int)((qb >> 52) & 0x7ff);
+  const long long bb = __double_as_longlong(b) & 0x7fffffffffffffffll;
+  const int eb = (int)(bb >> 52);
+  const int el = eb + e - 1023 - 53;  // biased exponent of |b| * 2^(E(q1) - 53)
+  if (e > 54 && e < 2045 && (qb & 0x000fffffffffffffll) != 0 && el > 1 && el < 2046) {
+    const double lim = __longlong_as_double(bb + ((long long)(e - 1023 - 53) << 52));
+    if (fabs(r1) < lim) return q1;
+  }
+  return __ddiv_rn(a, b);
+}
+
 // Householder reflector of col[kk..rows) (Householder.h:67-96 semantics).
 // Returns tau; writes beta to col[kk] and the essential part below it.
 __device__ double make_householder_col(double* col, int64_t rows, int kk, double* red) {
@@ -260,7 +293,8 @@ __device__ double make_householder_col(double* col, int64_t rows, int kk, double
     beta = __dsqrt_rn(__dadd_rn(__dmul_rn(c0, c0), tail_sq));
     if (c0 >= 0.0) beta = -beta;
     const double den = __dsub_rn(c0, beta);
-    for (int64_t i = kk + 1 + threadIdx.x; i < rows; i += blockDim.x) col[i] = __ddiv_rn(col[i], den);
+    const double rden = __drcp_rn(den);
+    for (int64_t i = kk + 1 + threadIdx.x; i < rows; i += blockDim.x) col[i] = div_by(col[i], den, rden);
     tau = __ddiv_rn(__dsub_rn(beta, c0), beta);
   }
   __syncthreads();

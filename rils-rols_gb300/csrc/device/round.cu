@@ -231,9 +231,12 @@ struct Encoder {
   }
 };
 
-// Table programs of the local factors (programs in lcode / lmeta).
+// Table programs of the local factors (programs in lcode / lmeta).  A
+// transcendental subtree becomes a column of its own only when it occurs at
+// least twice (a column costs a write and a read per use); share = false
+// keeps every factor a single program.
 bool build_table_programs(const std::vector<uint32_t>& lcode, const std::vector<int2>& lmeta, const double* consts,
-                          TableProgs& tp) {
+                          TableProgs& tp, bool share = true) {
   const int32_t nfl = (int32_t)lmeta.size();
   std::vector<PNode> nd;
   std::vector<int32_t> froot(nfl);
@@ -256,6 +259,11 @@ bool build_table_programs(const std::vector<uint32_t>& lcode, const std::vector<
       k = "B" + std::to_string(n.op) + "(" + key[n.a] + "," + key[n.b] + ")";
     }
   }
+  // occurrences of every transcendental subtree
+  std::unordered_map<std::string, int32_t> uses;
+  if (share)
+    for (size_t i = 0; i < nd.size(); ++i)
+      if (shared_root(nd[i])) ++uses[key[i]];
   // shared subtrees and their levels (1 + the deepest shared subtree inside)
   std::unordered_map<std::string, int32_t> aux_index;
   std::vector<int32_t> aux_node, aux_level, aux_of(nd.size(), -1), lvl(nd.size(), 0);
@@ -265,7 +273,7 @@ bool build_table_programs(const std::vector<uint32_t>& lcode, const std::vector<
     if (n.kind >= 3) inner = std::max(inner, lvl[n.a]);
     if (n.kind == 4) inner = std::max(inner, lvl[n.b]);
     lvl[i] = inner;
-    if (shared_root(n)) {
+    if (share && shared_root(n) && uses[key[i]] >= 2) {
       auto it = aux_index.find(key[i]);
       int32_t id;
       if (it == aux_index.end()) {
@@ -385,13 +393,11 @@ void build_factor_table(const rrg_cand* cands, int32_t n_cand, const uint32_t* c
 }
 
 // --------------------------------------------------------- mixed round ----
-rrg_status rrg_context::run_mixed(const rrg_dataset* ds, int32_t n_cand, bool certify) {
-  const char* hb = static_cast<const char*>(h_batch.ptr);
-  build_factor_table(host_cands.data(), n_cand, reinterpret_cast<const uint32_t*>(hb + off_k),
-                     reinterpret_cast<const double*>(hb + off_d), ft);
+rrg_status rrg_context::run_mixed(const rrg_dataset* ds, const std::vector<int32_t>& cands, bool certify) {
+  const int32_t n_cand = (int32_t)host_cands.size();
   // the mixed kernels take up to kMixedMaxM factors of spill depth <= kMixedStackCap
   std::vector<int32_t> mixed, routed;
-  for (int32_t c = 0; c < n_cand; ++c) {
+  for (int32_t c : cands) {
     const rrg_cand& cd = host_cands[c];
     const int m = cand_factors(cd);
     bool ok = m <= kMixedMaxM;
@@ -467,10 +473,14 @@ rrg_status rrg_context::mixed_subround(const rrg_dataset* ds, const int32_t* lis
   // table columns: shared transcendental subtrees (by level), then factors
   TableProgs tp;
   const char* hb = static_cast<const char*>(h_batch.ptr);
-  if (!build_table_programs(lcode, lmeta, reinterpret_cast<const double*>(hb + off_d), tp)) {
+  const double* consts64 = reinterpret_cast<const double*>(hb + off_d);
+  if (!build_table_programs(lcode, lmeta, consts64, tp)) {
     rrc::set_error("mixed round: a factor program could not be parsed");
     return RRG_E_INVALID;
   }
+  // shared columns on top of the factors must fit the table budget
+  if ((double)tp.meta.size() * sizeof(float2) * (double)ds->n_pad > (double)table_budget_bytes)
+    build_table_programs(lcode, lmeta, consts64, tp, false);
   const int32_t ncol = (int32_t)tp.meta.size();
   for (int32_t c = 0; c < ncol; ++c)
     if (tp.stack[c] > kMixedStackCap || tp.meta[c].y > kFacCodeSmem) {
@@ -759,11 +769,14 @@ rrg_status rrg_context::run_fp64_table(const rrg_dataset* ds, const std::vector<
     const rrg_cand& cd = host_cands[c];
     return plain_qr_bucket(cd.mode == RRG_TUNED ? cd.n_factors + 2 : 2);
   };
+  const char* hb = static_cast<const char*>(h_batch.ptr);
   std::vector<int32_t> list(list_in);
-  std::stable_sort(list.begin(), list.end(), [&](int32_t x, int32_t y) { return bucket(x) < bucket(y); });
+  // widest bucket first: its blocks are the longest, so they start first
+  std::stable_sort(list.begin(), list.end(), [&](int32_t x, int32_t y) { return bucket(x) > bucket(y); });
   const DevData dd = ds->view();
   const size_t col8 = sizeof(double) * (size_t)ds->n_pad;
-  const int64_t fcap = std::max<int64_t>(2 * RRG_MAX_TERMS, (int64_t)(scratch_budget_bytes / 2 / col8));
+  // factors per FP64 table (shared subtree columns come on top: keep room)
+  const int64_t fcap = std::max<int64_t>(2 * RRG_MAX_TERMS, (int64_t)(scratch_budget_bytes / 3 / col8));
   const int64_t mcap = std::max<int64_t>(2 * RRG_MAX_TERMS + 2, (int64_t)(scratch_budget_bytes / 2 / col8));
   const int nb_res = (int)((ds->n + RR_CHUNK - 1) / RR_CHUNK);
   const size_t n_all = host_cands.size();
@@ -794,22 +807,42 @@ rrg_status rrg_context::run_fp64_table(const rrg_dataset* ds, const std::vector<
     }
     const int32_t nfl = (int32_t)lf.size();
     const int32_t ng = (int32_t)(end - pos);
-    // the factors as one-factor untuned pseudo-candidates writing column i
-    std::vector<uint32_t> fcode;
-    std::vector<rrg_cand> fc(std::max(1, nfl));
-    std::vector<PlainCand> fpc(std::max(1, nfl));
+    // table columns (shared transcendental subtrees by level, then the
+    // factors), each a one-factor untuned pseudo-candidate writing its column;
+    // FP64 values are the same computed inline or through a shared column
+    std::vector<uint32_t> lcode;
+    std::vector<int2> lmeta(nfl);
     for (int32_t i = 0; i < nfl; ++i) {
       const int2 mt = ft.meta[lf[i]];
+      lmeta[i] = make_int2((int)lcode.size(), mt.y);
+      lcode.insert(lcode.end(), ft.code.begin() + mt.x, ft.code.begin() + mt.x + mt.y);
+    }
+    TableProgs tp;
+    const double* consts64 = reinterpret_cast<const double*>(hb + off_d);
+    if (!build_table_programs(lcode, lmeta, consts64, tp)) {
+      rrc::set_error("FP64 round: a factor program could not be parsed");
+      return RRG_E_INVALID;
+    }
+    if ((double)tp.meta.size() * (double)col8 > (double)scratch_budget_bytes / 2)
+      build_table_programs(lcode, lmeta, consts64, tp, false);
+    const int32_t ncol = (int32_t)tp.meta.size();
+    const std::vector<uint32_t>& fcode = tp.code;
+    std::vector<rrg_cand> fc(std::max(1, ncol));
+    std::vector<PlainCand> fpc(std::max(1, ncol));
+    for (int32_t i = 0; i < ncol; ++i) {
       rrg_cand& p = fc[i];
-      p.code_offset = (int32_t)fcode.size();
-      p.code_len = mt.y;
+      p.code_offset = tp.meta[i].x;
+      p.code_len = tp.meta[i].y;
       p.first_factor = 0;
       p.n_factors = 1;
       p.mode = RRG_UNTUNED;
       p.coef_offset = 0;
-      p.stack_need = ft.stack[lf[i]];
+      p.stack_need = tp.stack[i];
       p.reserved = 0;
-      fcode.insert(fcode.end(), ft.code.begin() + mt.x, ft.code.begin() + mt.x + mt.y);
+      if (tp.stack[i] > RRG_MAX_STACK) {
+        rrc::set_error("FP64 round: a table program exceeds the spill stack");
+        return RRG_E_INVALID;
+      }
       fpc[i] = PlainCand{i, 0, 0, 1, 0};
     }
     // column map and QR working columns; QR sub-batches by the M budget
@@ -837,7 +870,7 @@ rrg_status rrg_context::run_fp64_table(const rrg_dataset* ds, const std::vector<
       p.pad = 0;
       mcol += need;
       mcols_max = std::max(mcols_max, mcol);
-      for (int s = 0; s < m; ++s) colmap.push_back(lid[ft.ids[ft.cand_off[c] + s]]);
+      for (int s = 0; s < m; ++s) colmap.push_back(tp.fcol[lid[ft.ids[ft.cand_off[c] + s]]]);
     }
     subs.push_back({sub0, ng});
     Packer pk;
@@ -849,7 +882,7 @@ rrg_status rrg_context::run_fp64_table(const rrg_dataset* ds, const std::vector<
     const size_t o_list = pk.add(list.data() + pos, sizeof(int32_t) * ng);
     rrg_status pst = pk.send(h_ft64, d_ft64, stream);
     if (pst != RRG_OK) return pst;
-    if (!d_F64.reserve(col8 * std::max(1, nfl)) || !d_M.reserve(col8 * mcols_max)) {
+    if (!d_F64.reserve(col8 * std::max(1, ncol)) || !d_M.reserve(col8 * mcols_max)) {
       rrc::set_error("FP64 round: table allocation failed");
       return RRG_E_OOM;
     }
@@ -867,16 +900,22 @@ rrg_status rrg_context::run_fp64_table(const rrg_dataset* ds, const std::vector<
     DevBatch fdev = dev;
     fdev.cands = pk.at<const rrg_cand>(d_ft64, o_fc);
     fdev.code = pk.at<const uint32_t>(d_ft64, o_fcode);
-    fdev.n_cand = nfl;
+    fdev.n_cand = ncol;
     fdev.n_code = (int32_t)fcode.size();
     cudaEvent_t t0 = mark_begin();
-    const int nb = (int)std::max<int64_t>(
-        1, std::min<int64_t>((4LL * sm_count + nfl - 1) / std::max(1, nfl), (ds->n + 1023) / 1024));
-    for (int32_t f0 = 0; f0 < nfl; f0 += 65535) {
-      const int32_t nfb = std::min<int32_t>(65535, nfl - f0);
-      plain_eval_kernel<<<dim3(nb, nfb), 256, plain_eval_smem(), stream>>>(
-          fdev, dd, pk.at<const PlainCand>(d_ft64, o_fpc), nullptr, f0, F64, F64, nullptr, 0, status);
-      ++launches;
+    // one launch (or several of at most 65535 columns) per level
+    for (size_t L = 0, c0 = 0; L < tp.level_end.size(); ++L) {
+      const int32_t c1 = tp.level_end[L];
+      const int32_t nl = c1 - (int32_t)c0;
+      const int nb = (int)std::max<int64_t>(
+          1, std::min<int64_t>((4LL * sm_count + nl - 1) / std::max(1, nl), (ds->n + 1023) / 1024));
+      for (int32_t f0 = (int32_t)c0; f0 < c1; f0 += 65535) {
+        const int32_t nfb = std::min<int32_t>(65535, c1 - f0);
+        plain_eval_kernel<<<dim3(nb, nfb), 256, plain_eval_smem(), stream>>>(
+            fdev, dd, pk.at<const PlainCand>(d_ft64, o_fpc), nullptr, f0, F64, F64, nullptr, 0, status);
+        ++launches;
+      }
+      c0 = c1;
     }
     mark_end(P_PLAIN_EVAL, t0);
     ++launches;
@@ -884,14 +923,27 @@ rrg_status rrg_context::run_fp64_table(const rrg_dataset* ds, const std::vector<
       const int32_t ns = sb.second - sb.first;
       if (ns <= 0) continue;
       t0 = mark_begin();
+      // one launch per register bucket, side by side on the side streams
+      RRG_CUDA(cudaEventRecord(fork_ev, stream));
+      int used = 0;
       for (int32_t b0 = sb.first; b0 < sb.second;) {
         const int bk = bucket(list[pos + b0]);
         int32_t b1 = b0;
         while (b1 < sb.second && bucket(list[pos + b1]) == bk) ++b1;
-        launch_plain_qr(bk, b1 - b0, stream, dev, dd, d_pcs, d_list, b0, F64, M, nullptr, 0, 1, coefs, res, status,
-                        nullptr, d_cmap);
+        cudaStream_t s = side[used % kSide];
+        if (used < kSide) RRG_CUDA(cudaStreamWaitEvent(s, fork_ev, 0));
+        if (!launch_plain_qr(bk, b1 - b0, s, dev, dd, d_pcs, d_list, b0, F64, M, nullptr, 0, 1, coefs, res, status,
+                             nullptr, d_cmap)) {
+          cuda_ok(cudaGetLastError(), "QR launch");
+          return RRG_E_CUDA;
+        }
+        ++used;
         ++launches;
         b0 = b1;
+      }
+      for (int i = 0; i < std::min(used, (int)kSide); ++i) {
+        RRG_CUDA(cudaEventRecord(join_ev[i], side[i]));
+        RRG_CUDA(cudaStreamWaitEvent(stream, join_ev[i], 0));
       }
       mark_end(P_PLAIN_QR, t0);
       t0 = mark_begin();
@@ -911,11 +963,3 @@ rrg_status rrg_context::run_fp64_table(const rrg_dataset* ds, const std::vector<
   return RRG_OK;
 }
 
-rrg_status rrg_context::run_plain_table(const rrg_dataset* ds, int32_t n_cand) {
-  const char* hb = static_cast<const char*>(h_batch.ptr);
-  build_factor_table(host_cands.data(), n_cand, reinterpret_cast<const uint32_t*>(hb + off_k),
-                     reinterpret_cast<const double*>(hb + off_d), ft);
-  std::vector<int32_t> all(n_cand);
-  std::iota(all.begin(), all.end(), 0);
-  return run_fp64_table(ds, all, 0u);
-}

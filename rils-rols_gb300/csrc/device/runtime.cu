@@ -13,6 +13,7 @@
 #include <mutex>
 #include <string>
 #include <thread>
+#include <unordered_map>
 #include <vector>
 
 #include "../common/error.h"
@@ -338,6 +339,31 @@ rrg_status rrg_context::run_plain(const rrg_dataset* ds, int32_t lo, int32_t hi,
   return RRG_OK;
 }
 
+// dup_of[c]: the first candidate with c's mode and factor list (c itself
+// when none comes before); reps: those that are their own.
+void rrg_context::dedup_candidates(std::vector<int32_t>& reps) {
+  const int32_t n = (int32_t)host_cands.size();
+  dup_of.assign(n, 0);
+  reps.clear();
+  std::unordered_map<std::string, int32_t> seen;
+  seen.reserve((size_t)n * 2 + 16);
+  std::string key;
+  for (int32_t c = 0; c < n; ++c) {
+    const rrg_cand& cd = host_cands[c];
+    key.assign(reinterpret_cast<const char*>(&cd.mode), sizeof cd.mode);
+    key.append(reinterpret_cast<const char*>(ft.ids.data() + ft.cand_off[c]),
+               sizeof(int32_t) * (size_t)(ft.cand_off[c + 1] - ft.cand_off[c]));
+    auto it = seen.find(key);
+    if (it == seen.end()) {
+      seen.emplace(key, c);
+      dup_of[c] = c;
+      reps.push_back(c);
+    } else {
+      dup_of[c] = it->second;
+    }
+  }
+}
+
 rrg_status rrg_context::submit(rrg_dataset* ds, const rrg_batch* b, int32_t precision, rrg_result* results,
                                double* coefs) {
   if (in_flight) {
@@ -371,13 +397,18 @@ rrg_status rrg_context::submit(rrg_dataset* ds, const rrg_batch* b, int32_t prec
   RRG_CUDA(cudaMemsetAsync(d_res.ptr, 0, res_bytes, stream));
   RRG_CUDA(cudaMemsetAsync(d_coefs.ptr, 0, coef_bytes, stream));
   RRG_CUDA(cudaMemsetAsync(d_status.ptr, 0, 64, stream));
+  // distinct factor programs, and candidates with identical factor lists
+  // (same programs, same order, same mode) scored once
+  build_factor_table(host_cands.data(), b->n_cand, b->code, b->consts, ft);
+  std::vector<int32_t> reps;
+  dedup_candidates(reps);
   if (precision == RRG_PLAIN_FP64) {
     // few candidates on tall data: the tiled QR spreads each over the GPU;
     // otherwise one block per candidate over the shared FP64 factor table
-    if (ds->n >= 65536 && b->n_cand < 2 * sm_count) st = run_plain(ds, 0, b->n_cand, false);
-    else st = run_plain_table(ds, b->n_cand);
+    if (ds->n >= 65536 && (int64_t)reps.size() < 2 * sm_count) st = run_plain(ds, 0, 0, false, &reps);
+    else st = run_fp64_table(ds, reps, 0u);
   } else {
-    st = run_mixed(ds, b->n_cand, precision == RRG_MIXED_CERTIFIED);
+    st = run_mixed(ds, reps, precision == RRG_MIXED_CERTIFIED);
   }
   if (st != RRG_OK) return st;
   RRG_CUDA(cudaMemcpyAsync(h_res.ptr, d_res.ptr, res_bytes, cudaMemcpyDeviceToHost, stream));
@@ -431,6 +462,16 @@ rrg_status rrg_context::wait(int32_t timeout_ms) {
   }
   if (out_results) std::memcpy(out_results, h_res.ptr, sizeof(rrg_result) * out_n);
   if (out_coefs && out_ncoef > 0) std::memcpy(out_coefs, h_coefs.ptr, sizeof(double) * out_ncoef);
+  // candidates scored through an identical one
+  for (int32_t c = 0; c < out_n && c < (int32_t)dup_of.size(); ++c) {
+    const int32_t r = dup_of[c];
+    if (r == c) continue;
+    if (out_results) out_results[c] = out_results[r];
+    const rrg_cand& cd = host_cands[c];
+    if (out_coefs && cd.mode == RRG_TUNED)
+      std::memcpy(out_coefs + cd.coef_offset, out_coefs + host_cands[r].coef_offset,
+                  sizeof(double) * (size_t)(cd.n_factors + 1));
+  }
   last_launches = launches;
   return RRG_OK;
 }
@@ -466,6 +507,11 @@ rrg_context::~rrg_context() {
   for (cudaEvent_t e : event_pool) cudaEventDestroy(e);
   if (done) cudaEventDestroy(done);
   if (stream) cudaStreamDestroy(stream);
+  if (fork_ev) cudaEventDestroy(fork_ev);
+  for (int i = 0; i < kSide; ++i) {
+    if (join_ev[i]) cudaEventDestroy(join_ev[i]);
+    if (side[i]) cudaStreamDestroy(side[i]);
+  }
 }
 
 DevData rrg_dataset::view() const {
@@ -512,7 +558,11 @@ rrg_status rrg_context_create(int32_t device, rrg_context** out) {
   cudaMemGetInfo(&free_b, &total_b);
   ctx->scratch_budget_bytes = std::min<size_t>((size_t)64 << 30, free_b / 3);
   ctx->table_budget_bytes = std::min<size_t>((size_t)32 << 30, free_b / 5);
-  if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
+  bool side_ok = cudaEventCreateWithFlags(&ctx->fork_ev, cudaEventDisableTiming) == cudaSuccess;
+  for (int i = 0; i < rrg_context::kSide && side_ok; ++i)
+    side_ok = cudaStreamCreateWithFlags(&ctx->side[i], cudaStreamNonBlocking) == cudaSuccess &&
+              cudaEventCreateWithFlags(&ctx->join_ev[i], cudaEventDisableTiming) == cudaSuccess;
+  if (!side_ok || cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreateWithFlags(&ctx->done, cudaEventDisableTiming) != cudaSuccess) {
     cuda_ok(cudaGetLastError(), "stream creation");
     delete ctx;

@@ -54,6 +54,10 @@ struct rrg_context {
   size_t table_budget_bytes = 0;    // FP32 factor table of a mixed round
   cudaStream_t stream = nullptr;
   cudaEvent_t done = nullptr;
+  // side streams: QR launches of different register buckets run side by side
+  static constexpr int kSide = 4;
+  cudaStream_t side[kSide] = {nullptr};
+  cudaEvent_t fork_ev = nullptr, join_ev[kSide] = {nullptr};
   // batch staging
   HostBuf h_batch;
   DevBuf d_batch;
@@ -106,13 +110,15 @@ struct rrg_context {
                        bool redo_sensitive = true);
   // mixed round over the shared FP32 factor table; FP64 re-scoring of the
   // candidates it cannot decide
-  rrg_status run_mixed(const rrg_dataset* ds, int32_t n_cand, bool certify);
+  rrg_status run_mixed(const rrg_dataset* ds, const std::vector<int32_t>& cands, bool certify);
   rrg_status mixed_subround(const rrg_dataset* ds, const int32_t* list, int32_t cnt, const std::vector<int32_t>& lf,
                             const std::vector<int32_t>& lid, bool certify, std::vector<int32_t>& fb_all);
   // plain FP64 arithmetic over a shared FP64 factor table with the direct QR
   // per candidate (bit-identical to run_plain's direct QR)
   rrg_status run_fp64_table(const rrg_dataset* ds, const std::vector<int32_t>& list, uint32_t flags_or);
-  rrg_status run_plain_table(const rrg_dataset* ds, int32_t n_cand);
+  // candidates with identical factor lists: dup_of[c] = the one scored for c
+  std::vector<int32_t> dup_of;
+  void dedup_candidates(std::vector<int32_t>& reps);
   rrg_status submit(rrg_dataset* ds, const rrg_batch* b, int32_t precision, rrg_result* results, double* coefs);
   rrg_status wait(int32_t timeout_ms);
   ~rrg_context();
