@@ -224,6 +224,17 @@ int64_t rrg_last_round_launches(const rrg_context* ctx);
  * Returns the count written. */
 int32_t rrg_last_round_stats(const rrg_context* ctx, int64_t* out, int32_t n);
 
+/* Device-memory limits of this context's scratch: FP64 tables and QR working
+ * columns (scratch_bytes) and the mixed rounds' double-float factor table
+ * (table_bytes).  By default they are set from the free memory at creation;
+ * several contexts on one device (the serving loop) set them explicitly.
+ * No counterpart in the reference (single-threaded, one fit per process). */
+rrg_status rrg_context_set_limits(rrg_context* ctx, int64_t scratch_bytes, int64_t table_bytes);
+
+/* Free and total memory of a device (cudaMemGetInfo); RRG_E_NO_DEVICE without
+ * one.  No counterpart in the reference. */
+rrg_status rrg_device_memory(int32_t device, int64_t* free_bytes, int64_t* total_bytes);
+
 /* The CUDA stream (cudaStream_t) every kernel of this context runs on, so that
  * a caller can order or time its own work against the rounds. */
 void* rrg_context_stream(const rrg_context* ctx);

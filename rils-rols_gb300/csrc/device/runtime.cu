@@ -737,6 +737,32 @@ rrg_status rrg_context_set_timing(rrg_context* ctx, int32_t on) {
   return RRG_OK;
 }
 
+rrg_status rrg_context_set_limits(rrg_context* ctx, int64_t scratch_bytes, int64_t table_bytes) {
+  if (!ctx || scratch_bytes < (1 << 20) || table_bytes < (1 << 20)) {
+    rrc::set_error("rrg_context_set_limits: invalid arguments (each limit at least 1 MiB)");
+    return RRG_E_INVALID;
+  }
+  ctx->scratch_budget_bytes = (size_t)scratch_bytes;
+  ctx->table_budget_bytes = (size_t)table_bytes;
+  return RRG_OK;
+}
+
+rrg_status rrg_device_memory(int32_t device, int64_t* free_bytes, int64_t* total_bytes) {
+  if (!free_bytes || !total_bytes) return RRG_E_INVALID;
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || device < 0 || device >= count) {
+    cudaGetLastError();
+    rrc::set_error("no CUDA device available for the GB300 fitness path");
+    return RRG_E_NO_DEVICE;
+  }
+  RRG_CUDA(cudaSetDevice(device));
+  size_t f = 0, t = 0;
+  RRG_CUDA(cudaMemGetInfo(&f, &t));
+  *free_bytes = (int64_t)f;
+  *total_bytes = (int64_t)t;
+  return RRG_OK;
+}
+
 int32_t rrg_last_round_timing(const rrg_context* ctx, double* ms, int64_t* launches, int32_t n) {
   if (!ctx || !ms || n <= 0) return 0;
   const int32_t k = n < (int32_t)rrg_context::P_COUNT ? n : (int32_t)rrg_context::P_COUNT;

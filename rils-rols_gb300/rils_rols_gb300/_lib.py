@@ -1,5 +1,6 @@
 """ctypes binding of librils_rols_gb300.so: the C ABI of include/rils_rols_gb300.h
-(device fitness path) and include/rils_rols_host.h (host search driver).
+(device fitness path), include/rils_rols_host.h (host search driver) and
+include/rils_rols_serve.h (serving loop).
 
 The library is built in-tree by build.py.  Loading never falls back to
 anything else: a missing or unloadable library raises.
@@ -48,15 +49,37 @@ class Backend(C.Structure):
                 ("predict", C.c_void_p), ("dataset_destroy", C.c_void_p)]
 
 
-# Every symbol the two headers declare (checked by the CPU test suite).
+class JobParams(C.Structure):
+    _fields_ = [("classification", C.c_int32), ("max_fit_calls", C.c_int32), ("max_seconds", C.c_int32),
+                ("complexity_penalty", C.c_double), ("max_complexity", C.c_int32), ("sample_size", C.c_double),
+                ("random_state", C.c_int32), ("precision", C.c_int32)]
+
+
+class JobInfo(C.Structure):
+    _fields_ = [("state", C.c_int32), ("fit_calls", C.c_int32), ("queued_s", C.c_double), ("run_s", C.c_double),
+                ("time_to_model_s", C.c_double), ("best_time", C.c_double), ("footprint_bytes", C.c_int64),
+                ("device_rounds", C.c_int64), ("candidates", C.c_int64)]
+
+
+class ServeStats(C.Structure):
+    _fields_ = [("submitted", C.c_int64), ("done", C.c_int64), ("failed", C.c_int64), ("running", C.c_int64),
+                ("queued", C.c_int64), ("p50_time_to_model_s", C.c_double), ("p99_time_to_model_s", C.c_double),
+                ("mean_time_to_model_s", C.c_double), ("wall_s", C.c_double), ("candidates", C.c_int64),
+                ("peak_running", C.c_int64)]
+
+
+# Every symbol the headers declare (checked by the CPU test suite).
 EXPORTS = [
     "rrg_abi_version", "rrg_last_error", "rrg_context_create", "rrg_context_destroy", "rrg_dataset_create",
     "rrg_dataset_destroy", "rrg_round_submit", "rrg_round_wait", "rrg_eval", "rrg_predict", "rrg_batch_validate", "rrg_dataset_rows",
     "rrg_dataset_cols", "rrg_last_round_launches", "rrg_last_round_stats", "rrg_context_stream",
-    "rrg_context_set_timing", "rrg_last_round_timing", "rrg_eval_plain_noalloc",
+    "rrg_context_set_timing", "rrg_last_round_timing", "rrg_eval_plain_noalloc", "rrg_context_set_limits",
+    "rrg_device_memory",
     "rrh_create", "rrh_destroy", "rrh_set_backend", "rrh_set_precision", "rrh_fit", "rrh_predict",
     "rrh_model_string", "rrh_model_prefix", "rrh_best_time", "rrh_total_time", "rrh_fit_calls", "rrh_counter",
     "rrh_last_error", "rrh_candidates", "rrh_rewrite", "rrh_encode", "rrh_rebuild",
+    "rrs_create", "rrs_destroy", "rrs_set_backend", "rrs_submit", "rrs_wait", "rrs_result", "rrs_stats_get",
+    "rrs_last_error",
 ]
 
 _lock = threading.Lock()
@@ -87,6 +110,8 @@ def _declare(lib):
         "rrg_context_set_timing": (i32, [vp, i32]),
         "rrg_last_round_timing": (i32, [vp, dp, P(C.c_int64), i32]),
         "rrg_eval_plain_noalloc": (i32, [vp, i64, vp, i64, i32, P(Batch), vp, vp, vp]),
+        "rrg_context_set_limits": (i32, [vp, i64, i64]),
+        "rrg_device_memory": (i32, [i32, P(C.c_int64), P(C.c_int64)]),
         "rrh_create": (vp, [i32, i32, i32, dbl, i32, dbl, i32, i32]),
         "rrh_destroy": (None, [vp]),
         "rrh_set_backend": (i32, [vp, P(Backend)]),
@@ -104,6 +129,14 @@ def _declare(lib):
         "rrh_rewrite": (i32, [cp, i32, cp, i32]),
         "rrh_encode": (i32, [cp, i32, P(Batch)]),
         "rrh_rebuild": (i32, [cp, dp, i32, cp, i32]),
+        "rrs_create": (vp, [i32, i64, i32]),
+        "rrs_destroy": (None, [vp]),
+        "rrs_set_backend": (i32, [vp, P(Backend)]),
+        "rrs_submit": (i64, [vp, dp, dp, i32, i32, P(JobParams)]),
+        "rrs_wait": (i32, [vp, i64, i32]),
+        "rrs_result": (i32, [vp, i64, cp, i32, P(JobInfo)]),
+        "rrs_stats_get": (i32, [vp, P(ServeStats)]),
+        "rrs_last_error": (cp, []),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

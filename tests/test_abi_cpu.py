@@ -13,9 +13,9 @@ REPO = Path(__file__).resolve().parent.parent
 
 def test_exports_every_declared_symbol(lib):
     declared = set()
-    for h in ("rils_rols_gb300.h", "rils_rols_host.h"):
+    for h in ("rils_rols_gb300.h", "rils_rols_host.h", "rils_rols_serve.h"):
         text = (REPO / "include" / h).read_text()
-        declared |= set(re.findall(r"\b(rr[gh]_[a-z_]+)\s*\(", text))
+        declared |= set(re.findall(r"\b(rr[ghs]_[a-z_]+)\s*\(", text))
     assert declared == set(_lib.EXPORTS)
     for name in declared:
         assert hasattr(lib, name), name
