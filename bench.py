@@ -322,7 +322,58 @@ def run_ours(args):
                                "fitness": "(1 + (1 - R2)) (1 + RMSE) (1 + 0.001 size)"}
     res["cpu_baseline"] = cpu_baseline(X, y, trees, args.cpu_sample)
     res["certified_over_cpu_baseline"] = value / world / res["cpu_baseline"]["value"]
+    if args.serve_jobs > 0:
+        res["serving"] = serving_leg(args, local)
     print(json.dumps(res))
+
+
+# ------------------------------------------------------------- serving ----
+def serving_leg(args, device=0):
+    """The serving stream (Poisson arrivals, mean 5/s; n log-uniform in
+    [200, 1M], d in [1, 20], y a random 5-25-node tree + 1% noise,
+    max_fit_calls 1e5), first `serve_jobs` requests: every request submitted
+    at its arrival time to the serving loop (certified mixed form, jobs in
+    flight share the GPU), against the same requests run one after another
+    with the plain FP64 form."""
+    from rils_rols_gb300 import synth
+    from rils_rols_gb300._lib import RRG_MIXED_CERTIFIED, RRG_PLAIN_FP64
+    from rils_rols_gb300.serve import Server
+    jobs = synth.serving_stream(n_jobs=args.serve_jobs)
+    data = [synth.serving_job_data(j) for j in jobs]
+    params = dict(max_fit_calls=args.serve_fit_calls, max_seconds=1 << 30, complexity_penalty=0.001,
+                  max_complexity=50, sample_size=1.0)
+
+    def run(precision, max_active, paced):
+        with Server(device=device, max_active=max_active) as srv:
+            t0 = time.perf_counter()
+            ids = []
+            for j, (X, y) in zip(jobs, data):
+                if paced:
+                    delay = j["arrival"] - (time.perf_counter() - t0)
+                    if delay > 0:
+                        time.sleep(delay)
+                ids.append(srv.submit(X, y, random_state=j["seed"] % 100000, precision=precision, **params))
+            out = [srv.result(i) for i in ids]
+            wall = time.perf_counter() - t0
+            st = srv.stats()
+        return out, wall, st
+
+    conc, wall_c, st_c = run(RRG_MIXED_CERTIFIED, args.serve_active, True)
+    ser, wall_s, st_s = run(RRG_PLAIN_FP64, 1, False)
+    ttm = sorted(i["time_to_model_s"] for _, i in conc)
+    run_s = [i["run_s"] for _, i in ser]
+    return {
+        "requests": len(jobs), "arrivals": "Poisson, mean 5/s (first requests of the stream)",
+        "max_fit_calls": args.serve_fit_calls, "n_rows": [j["n"] for j in jobs], "n_features": [j["d"] for j in jobs],
+        "concurrent_certified": {"max_active": args.serve_active, "p50_time_to_model_s": st_c["p50_time_to_model_s"],
+                                 "p99_time_to_model_s": st_c["p99_time_to_model_s"], "wall_s": wall_c,
+                                 "fits_per_hour": 3600.0 * len(jobs) / wall_c,
+                                 "evals_per_s": st_c["candidates"] / wall_c, "peak_running": st_c["peak_running"],
+                                 "time_to_model_s": ttm},
+        "serial_plain_fp64": {"wall_s": wall_s, "sum_run_s": sum(run_s), "fits_per_hour": 3600.0 * len(jobs) / wall_s,
+                              "evals_per_s": st_s["candidates"] / wall_s},
+        "models_equal_plain": sum(a[0] == b[0] for a, b in zip(conc, ser)),
+    }
 
 
 # kernels behind the timed phases, with the algorithmic bytes of one launch
@@ -425,7 +476,14 @@ def main():
     ap.add_argument("--ref-sample", type=int, default=32)
     ap.add_argument("--unbatched-sample", type=int, default=64)
     ap.add_argument("--quick", action="store_true", help="skip the FP64 comparison and the CPU baseline")
+    ap.add_argument("--serve-jobs", type=int, default=8, help="requests of the serving stream (0: no serving leg)")
+    ap.add_argument("--serve-fit-calls", type=int, default=100000)
+    ap.add_argument("--serve-active", type=int, default=8)
+    ap.add_argument("--serve-only", action="store_true", help="only the serving leg")
     args = ap.parse_args()
+    if args.serve_only:
+        print(json.dumps(serving_leg(args)))
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

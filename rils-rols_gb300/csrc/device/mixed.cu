@@ -143,6 +143,9 @@ __global__ void __launch_bounds__(128) mixed_solve_kernel(SolveArgs a) {
   // per double-float addition (u = 2^-24) over at most ~90 sequential
   // additions per sum, plus the FP64 sum of the chunk partials: about 4e-13.
   const double kU = 1e-12;
+  // squared-norm ratio to the largest column below which the reference's
+  // rank cut (eps^2 ~ 5e-32) cannot be ruled out
+  const double kCutAbs = 1e-24;
   auto queue_fallback = [&](int why) {
     const int slot = atomicAdd(a.fallback, 1);
     if (slot < a.fallback_cap) a.fallback[1 + slot] = c;
@@ -260,9 +263,13 @@ __global__ void __launch_bounds__(128) mixed_solve_kernel(SolveArgs a) {
     int idx[kMixedMaxM + 1], kk2 = 0;
     for (int i = 0; i < k; ++i)
       if (i == m || !((nanmask >> i) & 1u)) idx[kk2++] = i;
-    double H[kMixedMaxM + 1][kMixedMaxM + 1];
-    for (int i = 0; i < kk2; ++i)
+    double H[kMixedMaxM + 1][kMixedMaxM + 1], hd0[kMixedMaxM + 1];
+    int hp[kMixedMaxM + 1];
+    for (int i = 0; i < kk2; ++i) {
       for (int j = 0; j < kk2; ++j) H[i][j] = G[idx[i]][idx[j]];
+      hd0[i] = H[i][i];
+      hp[i] = i;
+    }
     bool full = true;
     double hmax = 0.0;
     for (int i = 0; i < kk2; ++i) hmax = fmax(hmax, H[i][i]);
@@ -270,13 +277,15 @@ __global__ void __launch_bounds__(128) mixed_solve_kernel(SolveArgs a) {
       int p = s2;
       for (int j = s2 + 1; j < kk2; ++j)
         if (H[j][j] > H[p][p]) p = j;
-      if (!(H[p][p] > 1e-6 * hmax)) {
+      // well away from a cut: relative to the column's own norm and to the largest
+      if (!(H[p][p] > 1e-6 * hd0[hp[p]]) || !(H[p][p] > kCutAbs * hmax)) {
         full = false;
         break;
       }
       if (p != s2) {
         for (int j = 0; j < kk2; ++j) { const double t2 = H[s2][j]; H[s2][j] = H[p][j]; H[p][j] = t2; }
         for (int j = 0; j < kk2; ++j) { const double t2 = H[j][s2]; H[j][s2] = H[j][p]; H[j][p] = t2; }
+        const int t3 = hp[s2]; hp[s2] = hp[p]; hp[p] = t3;
       }
       const double l = sqrt(H[s2][s2]);
       for (int i = s2 + 1; i < kk2; ++i) H[i][s2] /= l;
@@ -317,7 +326,11 @@ __global__ void __launch_bounds__(128) mixed_solve_kernel(SolveArgs a) {
     for (int j = s2 + 1; j < k; ++j)
       if (L[j][j] > L[p][p]) p = j;
     const double dp = L[p][p];
-    if (!(dp > a.rank_tol * maxd)) {
+    // A pivot is cut when it is small against its own column's norm (the
+    // Gram sums cannot resolve it) or so small against the largest column
+    // that the reference's QR, whose cut is at eps^2 of the largest squared
+    // norm, may cut it.  A badly scaled but independent column is kept.
+    if (!(dp > a.rank_tol * d0[piv[p]]) || !(dp > kCutAbs * maxd)) {
       rank = s2;
       break;
     }
@@ -374,16 +387,30 @@ __global__ void __launch_bounds__(128) mixed_solve_kernel(SolveArgs a) {
   // rule works at eps^2 of the column norms), ill-conditioning, and
   // coefficients inside the ambiguity band of the drop (|c| < 1e-12) and
   // snap (|c - 1| < 1e-12) rules of the rebuilt tree.
-  const double yrms = sqrt(yy / n_d);
   int why = -1;
   if (!finite) why = FB_OTHER_NAN;
   else if (rank < k && a.certify) why = FB_RANK;
   else if (rank == k && min_ratio < a.fallback_tol) why = FB_ILL_COND;
-  for (int i = 0; i < k && why < 0 && a.certify; ++i) {
-    const double ci = coef[i];
-    const double scale = i == m ? 1.0 : fmax((double)pr.rms[i], 1e-300);
-    if (fabs(ci - 1.0) < 1e-8 && i < m) why = FB_SNAP;
-    else if (fabs(ci) * scale < 1e-9 * yrms) why = FB_DROP;
+  if (why < 0 && a.certify) {
+    // Coefficient error of the Gram solve: with relative errors u of the
+    // Gram entries (the sums, kU, and the table's evaluation, ferr / rms of
+    // each column) and the smallest relative pivot as the scaled
+    // conditioning,
+    //   |dc_i| <= u (|y| + sum_j |c_j| |f_j|) sqrt(k) / (lam |f_i|),  lam = min_ratio / k.
+    // The drop (|c| < 1e-12) and snap (|c - 1| < 1e-12) rules of the rebuilt
+    // tree are left to the FP64 path when c lies within 8 |dc_i| of them.
+    double u = kU, M = sqrt(yy);
+    for (int i = 0; i < k; ++i) {
+      M += fabs(coef[i]) * sqrt(fabs(G[i][i]));
+      if (i < m) u = fmax(u, ferr(i) / fmax((double)pr.rms[i], 1e-300));
+    }
+    const double lam = fmax(min_ratio, 1e-300) / k;
+    for (int i = 0; i < k && why < 0; ++i) {
+      const double ci = coef[i];
+      const double dc = 8.0 * u * M * sqrt((double)k) / (lam * fmax(sqrt(fabs(G[i][i])), 1e-300));
+      if (i < m && !(fabs(fabs(ci - 1.0) - kEps12) > dc)) why = FB_SNAP;
+      else if (!(fabs(fabs(ci) - kEps12) > dc)) why = FB_DROP;
+    }
   }
   double* out = a.coefs + cd.coef_offset;
   MixedTerm& tm = a.terms[c];

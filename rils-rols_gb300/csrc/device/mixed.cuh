@@ -74,7 +74,9 @@ struct SolveArgs {
   uint32_t* reasons;       // [kFbReasons] counts of FP64 re-scoring reasons
   const int64_t* nanrow;   // [candidate] first row where a factor value was NaN in the table
   double* cert_e;          // [candidate] certified rounds: per-row error bound for the residual-pass check
-  double rank_tol, fallback_tol, pass2_tol, cert_tol;
+  double rank_tol;         // pivot cut: squared pivot below rank_tol x its column's squared norm
+  double fallback_tol;     // smallest pivot ratio solved here; below it the FP64 path solves
+  double pass2_tol, cert_tol;
   int certify;             // 1: RRG_MIXED_CERTIFIED decisions
 };
 
