@@ -220,7 +220,9 @@ int64_t rrg_last_round_launches(const rrg_context* ctx);
  *   FP32/FP64 non-finite mismatch on a probe row, FP64 overflow, FP32
  *   overflow, NaN factor beside a rank-deficient rest, rank cut,
  *   ill-conditioning, coefficient near 1, coefficient near 0, one-pass SSE
- *   inaccurate, certified error bound too large, other NaN.
+ *   inaccurate, certified error bound too large, other NaN.  [15] FP64-path
+ *   candidates whose pivoted QR was not run: a non-finite column norm makes its
+ *   outcome certainly all-NaN coefficients (the fitness sentinel).
  * Returns the count written. */
 int32_t rrg_last_round_stats(const rrg_context* ctx, int64_t* out, int32_t n);
 

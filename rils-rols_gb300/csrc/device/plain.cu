@@ -366,7 +366,7 @@ __global__ void __launch_bounds__(256) plain_qr_kernel_t(DevBatch b, DevData ds,
   extern __shared__ double smem[];
   const int c = list ? list[cand0 + blockIdx.x] : cand0 + blockIdx.x;
   const rrg_cand cd = b.cands[c];
-  if (cd.mode != RRG_TUNED) return;
+  if (cd.mode != RRG_TUNED || (pc[c].pad & 1)) return;  // pad bit 0: outcome already written
   // second pass of a tiled round: only the candidates the first pass flagged
   if (!tsqr && redo && !redo[c]) return;
   const int k = pc[c].k;
@@ -574,6 +574,12 @@ __global__ void __launch_bounds__(256) plain_resid_kernel(DevBatch b, DevData ds
   const rrg_cand cd = b.cands[c];
   const int nb = gridDim.x;
   const bool tuned = cd.mode == RRG_TUNED;
+  if (tuned && (pc[c].pad & 1)) {
+    // all-NaN coefficients: every row's rebuilt sum is NaN
+    if (threadIdx.x == 0)
+      partial[(int64_t)c * nb + blockIdx.x] = blockIdx.x == 0 ? __longlong_as_double(0x7ff8000000000000ll) : 0.0;
+    return;
+  }
   const int k = pc[c].k;
   const int m = tuned ? k - 1 : 1;
   if (tuned) {
@@ -666,6 +672,77 @@ __global__ void finalize_kernel(DevBatch b, DevData ds, const int32_t* list, int
 __global__ void clear_results_kernel(const int32_t* list, int n, rrg_result* res) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) res[list[i]] = rrg_result{};
+}
+
+__global__ void __launch_bounds__(256) colstat_kernel(const double* T, int64_t n, int64_t n_pad, ColStat* out) {
+  const double* col = T + (int64_t)blockIdx.y * n_pad;
+  uint32_t f = 0;
+  unsigned long long mx = 0;
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+    const double v = col[r];
+    const double a = fabs(v);
+    if (v != v) {
+      f |= kCsNaN;
+    } else if (!(a <= 1.35e154)) {  // infinite, or its square overflows
+      f |= kCsBig;
+    } else {
+      const unsigned long long bits = (unsigned long long)__double_as_longlong(a);
+      mx = bits > mx ? bits : mx;
+    }
+    if (r >= 1 && !(a <= 1e-150)) f |= kCsTail;
+  }
+  f = __reduce_or_sync(0xffffffffu, f);
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long t = __shfl_xor_sync(0xffffffffu, mx, o);
+    mx = t > mx ? t : mx;
+  }
+  if ((threadIdx.x & 31) == 0) {
+    if (f) atomicOr(&out[blockIdx.y].flags, f);
+    if (mx) atomicMax(&out[blockIdx.y].maxabs, mx);
+  }
+}
+
+// The outcome of the column-pivoted QR (ColPivHouseholderQR.h:482-608, as
+// restated by the oracle) on [f_0 .. f_{m-1}, 1] when its first pivot has a
+// non-finite norm.  Pivot selection keeps the first maximum under '>', so a
+// NaN norm is chosen only when it heads the remaining columns and a +inf
+// norm beats every finite one: the first pivot is non-finite when column 0's
+// norm is NaN or some column's norm is +inf (an infinite value or an
+// overflowing square, without NaN).  With a non-trivial tail in every column
+// (some row after the first above 1e-150: the reflector is formed and every
+// norm is non-zero), that pivot yields tau = NaN, which turns every other
+// column and its norm NaN; no step cuts the rank (step 0 compares against an
+// infinite or NaN threshold, later steps against NaN norms), so all
+// coefficients are NaN at full rank.  A finite first pivot can leave a column
+// with an exactly zero norm that a later step cuts, so NaN columns further
+// on are left to the QR.
+__global__ void sentinel_classify_kernel(DevBatch b, const int32_t* list, int cand0, int cnt, PlainCand* pc,
+                                         const int32_t* colmap, const ColStat* cs, int64_t rows, double* coefs,
+                                         rrg_result* res, uint32_t* decided) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= cnt) return;
+  const int c = list[cand0 + i];
+  const rrg_cand cd = b.cands[c];
+  if (cd.mode != RRG_TUNED) return;
+  const int k = pc[c].k;
+  const int m = k - 1;
+  if (m < 1 || rows < (int64_t)k + 2) return;
+  bool tails = true, inf_norm = false, nan0 = false;
+  for (int j = 0; j < m; ++j) {
+    const ColStat st = cs[colmap[pc[c].a_col + j]];
+    if (!(st.flags & kCsTail)) tails = false;
+    if (st.flags & kCsNaN) {
+      if (j == 0) nan0 = true;
+    } else if (st.flags & kCsBig) {
+      inf_norm = true;
+    }
+  }
+  if (!tails || !(nan0 || inf_norm)) return;
+  double* out = coefs + cd.coef_offset;
+  for (int j = 0; j < k; ++j) out[j] = __longlong_as_double(0x7ff8000000000000ll);
+  res[c].rank = k;
+  pc[c].pad = 1;
+  atomicAdd(decided, 1u);
 }
 
 size_t plain_eval_smem() { return RRG_MAX_STACK * 256 * sizeof(double) + kMaxCodeSmem * sizeof(uint32_t); }

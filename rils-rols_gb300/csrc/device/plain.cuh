@@ -31,6 +31,26 @@ __global__ void finalize_kernel(DevBatch b, DevData ds, const int32_t* list, int
 
 __global__ void clear_results_kernel(const int32_t* list, int n, rrg_result* res);
 
+// Column statistics of an FP64 table, for deciding the column-pivoted QR's
+// outcome on non-finite data without running it.
+struct ColStat {
+  uint32_t flags;       // kCs* bits
+  uint32_t pad;
+  unsigned long long maxabs;  // bits of the largest finite |value| (non-negative doubles order as integers)
+};
+constexpr uint32_t kCsNaN = 1;   // a NaN value: the column's norm is NaN
+constexpr uint32_t kCsBig = 2;   // an infinite value or one whose square overflows
+constexpr uint32_t kCsTail = 4;  // a row after the first with |value| > 1e-150 or non-finite
+// grid (row blocks, columns); out zeroed before the launch
+__global__ void colstat_kernel(const double* T, int64_t n, int64_t n_pad, ColStat* out);
+// One thread per listed tuned candidate: where the QR's result is certain to
+// be all-NaN coefficients at full rank (the fitness sentinel), writes that
+// result, sets pc[c].pad = 1 (the QR and residual kernels skip it) and
+// counts it in *decided.
+__global__ void sentinel_classify_kernel(DevBatch b, const int32_t* list, int cand0, int cnt, PlainCand* pc,
+                                         const int32_t* colmap, const ColStat* cs, int64_t rows, double* coefs,
+                                         rrg_result* res, uint32_t* decided);
+
 size_t plain_eval_smem();
 size_t plain_qr_smem();
 

@@ -381,7 +381,7 @@ rrg_status rrg_context::submit(rrg_dataset* ds, const rrg_batch* b, int32_t prec
   if (n_coefs > 0 && !coefs) return RRG_E_INVALID;
   RRG_CUDA(cudaSetDevice(device));
   launches = 0;
-  last_plain_routed = last_fallback = last_pass2 = 0;
+  last_plain_routed = last_fallback = last_pass2 = last_sentinel = 0;
   for (auto& r : last_reasons) r = 0;
   marks.clear();
   event_next = 0;
@@ -449,6 +449,7 @@ rrg_status rrg_context::wait(int32_t timeout_ms) {
     rrc::set_error(msg);
     return RRG_E_DEVICE_FAULT;
   }
+  last_sentinel = static_cast<const uint32_t*>(h_status.ptr)[rrd::kStatusSentinel];
   for (int i = 0; i < P_COUNT; ++i) {
     phase_ms[i] = 0;
     phase_launches[i] = 0;
@@ -496,7 +497,8 @@ rrg_context::~rrg_context() {
   d_cert_e.release();
   h_mlist.release();
   h_fallback.release();
-  for (DevBuf* bf : {&d_ft, &d_ft64, &d_F, &d_P, &d_psum, &d_fprobe, &d_fnan, &d_F64, &d_M}) bf->release();
+  for (DevBuf* bf : {&d_ft, &d_ft64, &d_F, &d_P, &d_psum, &d_fprobe, &d_fnan, &d_F64, &d_M, &d_colstat})
+    bf->release();
   h_ft.release();
   h_ft64.release();
   h_batch.release();
@@ -722,9 +724,10 @@ int64_t rrg_last_round_launches(const rrg_context* ctx) { return ctx ? ctx->last
 
 int32_t rrg_last_round_stats(const rrg_context* ctx, int64_t* out, int32_t n) {
   if (!ctx || !out || n <= 0) return 0;
-  int64_t v[4 + kFbReasons] = {ctx->last_launches, ctx->last_plain_routed, ctx->last_fallback, ctx->last_pass2};
+  int64_t v[5 + kFbReasons] = {ctx->last_launches, ctx->last_plain_routed, ctx->last_fallback, ctx->last_pass2};
   for (int i = 0; i < kFbReasons; ++i) v[4 + i] = ctx->last_reasons[i];
-  const int32_t k = n < 4 + kFbReasons ? n : 4 + kFbReasons;
+  v[4 + kFbReasons] = ctx->last_sentinel;
+  const int32_t k = n < 5 + kFbReasons ? n : 5 + kFbReasons;
   for (int32_t i = 0; i < k; ++i) out[i] = v[i];
   return k;
 }

@@ -73,7 +73,7 @@ struct rrg_context {
   // factor tables
   FactorTable ft;
   HostBuf h_ft, h_ft64;
-  DevBuf d_ft, d_ft64, d_F, d_P, d_psum, d_fprobe, d_fnan, d_F64, d_M;
+  DevBuf d_ft, d_ft64, d_F, d_P, d_psum, d_fprobe, d_fnan, d_F64, d_M, d_colstat;
   // results
   DevBuf d_res, d_coefs, d_status;
   HostBuf h_res, h_coefs, h_status;
@@ -85,7 +85,7 @@ struct rrg_context {
   int64_t out_ncoef = 0;
   int64_t launches = 0, last_launches = 0;
   // mixed-round statistics of the last round
-  int64_t last_fallback = 0, last_plain_routed = 0, last_pass2 = 0;
+  int64_t last_fallback = 0, last_plain_routed = 0, last_pass2 = 0, last_sentinel = 0;
   int64_t last_reasons[16] = {0};
   // certified bound on the relative fitness error of a mixed result; larger
   // bounds are re-scored by the FP64 path

@@ -125,9 +125,10 @@ class Context:
                "one_pass", "cert", "other_nan")
 
     def last_round_stats(self) -> dict:
-        out = (C.c_int64 * 15)()
-        self.lib.rrg_last_round_stats(self.h, out, 15)
-        d = {"launches": out[0], "plain_routed": out[1], "fp64_rescored": out[2], "residual_pass": out[3]}
+        out = (C.c_int64 * 16)()
+        self.lib.rrg_last_round_stats(self.h, out, 16)
+        d = {"launches": out[0], "plain_routed": out[1], "fp64_rescored": out[2], "residual_pass": out[3],
+             "qr_skipped_sentinel": out[15]}
         d["rescore_reasons"] = {r: out[4 + i] for i, r in enumerate(self.REASONS) if out[4 + i]}
         return d
 

@@ -152,3 +152,33 @@ def test_round_is_deterministic_and_mix_independent(ctx):
             one = ds.evaluate(encode([trees[i]], tuned=True), prec)
             assert one["loss"][0] == full["loss"][i] or (np.isnan(one["loss"][0]) and np.isnan(full["loss"][i]))
             assert one["rmse"][0] == full["rmse"][i] or (np.isnan(one["rmse"][0]) and np.isnan(full["rmse"][i]))
+
+
+def test_nonfinite_outcomes_decided_from_column_statistics(ctx):
+    # Infinite and NaN factor values in various columns: where a column norm
+    # is non-finite the QR's outcome (all-NaN coefficients at full rank) is
+    # decided without running it; every result stays bit-identical to the
+    # oracle, whether decided or factorised.
+    rng = np.random.default_rng(11)
+    n = 3000
+    X = rng.uniform(-3, 3, (n, 3))
+    y = 2.0 * X[:, 0] * X[:, 1] + np.sin(X[:, 2])
+    X[5, 0] = 800.0    # exp(x0) overflows on one row
+    X[17, 2] = -0.5    # x2 stays mixed-sign: ln and sqrt give NaN on part of the rows
+    trees = ["add mul c:2 exp x0 mul c:3 x1", "add mul c:2 x1 mul c:3 exp x0",
+             "add mul c:2 ln x2 mul c:3 x1", "add mul c:2 x1 mul c:3 ln x2",
+             "add add mul c:2 x1 mul c:3 x0 mul c:4 sqrt x2", "add add mul c:2 sqrt x2 mul c:3 x0 exp x0",
+             "add add add mul c:2 x1 mul c:3 x0 mul c:4 sin x2 ln x2", "add mul c:2 x1 mul c:3 x0",
+             "mul exp x0 ln x2", "add exp mul c:1000 x1 x0"]
+    ds = ctx.dataset(X, y)
+    ods = pyoracle.OracleDataset(X, y)
+    b = encode(trees, tuned=True)
+    dev, ora = ds.evaluate(b, PLAIN), ods.evaluate(b)
+    stats = ctx.last_round_stats()
+    for key in ("loss", "rmse", "rank"):
+        assert same_bits(dev[key], ora[key]), key
+    assert np.array_equal(dev["size"], ora["size"])
+    for i in range(len(trees)):
+        assert same_bits(dev["coefs"][i], ora["coefs"][i]), trees[i]
+    n_sent = int((ora["loss"] == 1000).sum())
+    assert 1 <= stats["qr_skipped_sentinel"] <= n_sent
