@@ -14,6 +14,8 @@
 //   plain_resid  the rebuilt sum  sum_i c_i * f_i  with the drop / snap rules
 //                of rils_rols_cpp.cpp:488-517 and its squared residual;
 //   finalize     R2, RMSE and the NaN sentinel (rils_rols_cpp.cpp:40-49, 520-541).
+#include <cooperative_groups.h>
+
 #include <cfloat>
 #include <cstdint>
 
@@ -539,6 +541,351 @@ __global__ void __launch_bounds__(256) plain_qr_kernel_t(DevBatch b, DevData ds,
   }
 }
 
+// ------------------------------------------------- cluster-wide direct QR --
+// The same factorisation as plain_qr_kernel_t (direct, tsqr = 0), with the
+// 256 lanes of every RR256 sum spread over a cluster of kQrCluster CTAs of
+// one warp each: CTA w runs lanes 32w .. 32w + 31.  Each CTA folds its warp
+// and sends the total to every CTA of the cluster through distributed shared
+// memory; after the cluster barrier each CTA adds the eight totals in order,
+// so every sum is bit-identical to the one-block kernel's.  The scalar
+// bookkeeping (norms, pivots, permutation) is replicated in every CTA from
+// identical inputs; row kk of the working columns (the R entries) is written
+// by CTA 0 only, after every CTA has read the old values.  A lane touches the
+// rows kk + 1 + lane + 256 t within one step, which shift by one row per
+// step, so a cluster barrier closes each step; working-column loads bypass
+// L1 (ld.global.cg) since other SMs of the cluster wrote them.
+namespace cg = cooperative_groups;
+constexpr int kQrCluster = 8;
+
+template <int KB>
+struct ClRed {
+  double buf[2][kQrCluster * KB];
+  int parity;
+};
+
+// Element-wise RR256 sum of part[0..cnt) over the cluster; every lane of
+// every CTA gets out[0..cnt).
+template <int KB>
+__device__ __forceinline__ void cl_sum_vec(cg::cluster_group& cl, ClRed<KB>& r, const double (&part)[KB], int cnt,
+                                           double (&out)[KB]) {
+  const int w = (int)cl.block_rank(), lane = threadIdx.x & 31;
+  double* buf = r.buf[r.parity];
+#pragma unroll
+  for (int j = 0; j < KB; ++j)
+    if (j < cnt) {
+      const double v = __shfl_sync(0xffffffffu, warp_sum(part[j]), 0);  // lane 0's fold is the RR256 one
+      if (lane < kQrCluster) cl.map_shared_rank(buf, lane)[w * KB + j] = v;
+    }
+  cl.sync();
+#pragma unroll
+  for (int j = 0; j < KB; ++j) {
+    double s = 0.0;
+    if (j < cnt)
+      for (int i = 0; i < kQrCluster; ++i) s = __dadd_rn(s, buf[i * KB + j]);
+    out[j] = s;
+  }
+  __syncwarp();
+  if (lane == 0) r.parity ^= 1;
+  __syncwarp();
+}
+
+template <int KB>
+__device__ __forceinline__ double cl_sum(cg::cluster_group& cl, ClRed<KB>& r, double v) {
+  double part[KB], out[KB];
+#pragma unroll
+  for (int j = 0; j < KB; ++j) part[j] = j == 0 ? v : 0.0;
+  cl_sum_vec<KB>(cl, r, part, 1, out);
+  return out[0];
+}
+
+// One lane's share of an RR256 sum of squares over rows i0, i0 + 256, ...
+// (in row order), with the loads of kRowBatch rows issued together: a
+// cluster CTA is a single warp, so latency is hidden by in-flight loads.
+constexpr int kRowBatch = 8;
+__device__ __forceinline__ double lane_sumsq(const double* col, int64_t i0, int64_t rows) {
+  double ps = 0.0;
+  int64_t i = i0;
+  for (; i + 256 * (kRowBatch - 1) < rows; i += 256 * kRowBatch) {
+    double q[kRowBatch];
+#pragma unroll
+    for (int u = 0; u < kRowBatch; ++u) q[u] = __ldcg(col + i + 256 * u);
+#pragma unroll
+    for (int u = 0; u < kRowBatch; ++u) ps = __dadd_rn(ps, __dmul_rn(q[u], q[u]));
+  }
+  for (; i < rows; i += 256) {
+    const double q = __ldcg(col + i);
+    ps = __dadd_rn(ps, __dmul_rn(q, q));
+  }
+  return ps;
+}
+
+// rows per batch of the dot and update passes: KB columns each
+template <int KB>
+struct ColBatch {
+  static constexpr int U = KB <= 4 ? 8 : (KB <= 8 ? 4 : (KB <= 16 ? 2 : 1));
+};
+
+template <int KB>
+__global__ void __cluster_dims__(kQrCluster, 1, 1) __launch_bounds__(32)
+    plain_qr_cluster_kernel(DevBatch b, DevData ds, const PlainCand* pc, const int32_t* list, int cand0,
+                            const double* A, double* M, double* coefs, rrg_result* res, uint32_t* status,
+                            const int32_t* colmap) {
+  cg::cluster_group cl = cg::this_cluster();
+  const int w = (int)cl.block_rank();
+  const int lane = threadIdx.x;
+  const int L = w * 32 + lane;  // RR256 lane
+  const int ci = blockIdx.x / kQrCluster;
+  const int c = list ? list[cand0 + ci] : cand0 + ci;
+  const rrg_cand cd = b.cands[c];
+  // uniform over the cluster: every CTA takes the same exits
+  if (cd.mode != RRG_TUNED || (pc[c].pad & 1)) return;
+  const int k = pc[c].k;
+  if (k + 1 > KB || k > kMaxK) {
+    if (w == 0 && lane == 0) atomicOr(status, ST_TOO_LARGE);
+    return;
+  }
+  __shared__ ClRed<KB> red;
+  __shared__ double nupd[KB], ndir[KB];
+  __shared__ int perm[KB], rec[KB];
+  __shared__ double* colp[KB];
+  __shared__ int s_nonzero;
+  if (lane == 0) red.parity = 0;
+  cl.sync();  // every CTA of the cluster running before any distributed shared memory access
+  double* Q = M + pc[c].m_col * ds.n_pad;
+  const int64_t ld = ds.n_pad, rows = ds.n;
+  for (int j = lane; j <= k; j += 32) colp[j] = Q + (int64_t)j * ld;
+  __syncwarp();
+  // [A | 1 | y] into the working columns, the initial norms on the way
+  double part[KB], out[KB];
+#pragma unroll
+  for (int j = 0; j < KB; ++j) {
+    part[j] = 0.0;
+    if (j > k) continue;
+    double* dst = Q + (int64_t)j * ld;
+    if (j < k - 1) {
+      const double* src = factor_column(A, ds.n_pad, pc[c].a_col, j, colmap);
+      double acc = 0.0;
+      int64_t r = L;
+      for (; r + 256 * (kRowBatch - 1) < rows; r += 256 * kRowBatch) {
+        double v[kRowBatch];
+#pragma unroll
+        for (int u = 0; u < kRowBatch; ++u) v[u] = src[r + 256 * u];
+#pragma unroll
+        for (int u = 0; u < kRowBatch; ++u) {
+          __stcg(dst + r + 256 * u, v[u]);
+          acc = __dadd_rn(acc, __dmul_rn(v[u], v[u]));
+        }
+      }
+      for (; r < rows; r += 256) {
+        const double v = src[r];
+        __stcg(dst + r, v);
+        acc = __dadd_rn(acc, __dmul_rn(v, v));
+      }
+      part[j] = acc;
+    } else if (j == k - 1) {
+      double acc = 0.0;
+      for (int64_t r = L; r < rows; r += 256) {
+        __stcg(dst + r, 1.0);
+        acc = __dadd_rn(acc, 1.0);
+      }
+      part[j] = acc;
+    } else {
+      for (int64_t r = L; r < rows; r += 256) __stcg(dst + r, ds.y64[r]);
+    }
+  }
+  cl_sum_vec<KB>(cl, red, part, k, out);  // its barrier also publishes the copies
+  const double rows_thr = (double)ds.n;
+  const int size = (int)(rows < k ? rows : k);
+  if (lane == 0) {
+#pragma unroll
+    for (int j = 0; j < KB; ++j)
+      if (j < k) {
+        ndir[j] = __dsqrt_rn(out[j]);
+        nupd[j] = ndir[j];
+        perm[j] = j;
+      }
+    s_nonzero = size;
+  }
+  __syncwarp();
+  double maxn = nupd[0];
+  for (int j = 1; j < k; ++j)
+    if (nupd[j] > maxn) maxn = nupd[j];
+  const double thr_helper = __ddiv_rn(__dmul_rn(__dmul_rn(maxn, DBL_EPSILON), __dmul_rn(maxn, DBL_EPSILON)), rows_thr);
+  const double downdate_thr = 1.4901161193847656e-08;  // sqrt(DBL_EPSILON)
+
+  for (int kk = 0; kk < size; ++kk) {
+    if (lane == 0) {
+      int big = kk;
+      double bign = nupd[kk];
+      for (int j = kk + 1; j < k; ++j)
+        if (nupd[j] > bign) {
+          bign = nupd[j];
+          big = j;
+        }
+      if (s_nonzero == size && __dmul_rn(bign, bign) < __dmul_rn(thr_helper, rows_thr - kk)) s_nonzero = kk;
+      if (big != kk) {
+        double t = nupd[kk]; nupd[kk] = nupd[big]; nupd[big] = t;
+        t = ndir[kk]; ndir[kk] = ndir[big]; ndir[big] = t;
+        int p = perm[kk]; perm[kk] = perm[big]; perm[big] = p;
+        double* cq = colp[kk]; colp[kk] = colp[big]; colp[big] = cq;
+      }
+    }
+    __syncwarp();
+    // Householder reflector of the pivot column (Householder.h:67-96)
+    double* col = colp[kk];
+    double tau;
+    {
+      // c0 is read before the barrier of the tail sum, after which CTA 0 overwrites it with beta
+      const double c0 = __ldcg(col + kk);
+      const double ps = lane_sumsq(col, kk + 1 + L, rows);
+      const double tail_sq = (rows - kk == 1) ? 0.0 : cl_sum<KB>(cl, red, ps);
+      double beta;
+      if (tail_sq <= DBL_MIN) {
+        tau = 0.0;
+        beta = c0;
+        for (int64_t i = kk + 1 + L; i < rows; i += 256) __stcg(col + i, 0.0);
+      } else {
+        beta = __dsqrt_rn(__dadd_rn(__dmul_rn(c0, c0), tail_sq));
+        if (c0 >= 0.0) beta = -beta;
+        const double den = __dsub_rn(c0, beta);
+        const double rden = __drcp_rn(den);
+        int64_t i = kk + 1 + L;
+        for (; i + 256 * (kRowBatch - 1) < rows; i += 256 * kRowBatch) {
+          double q[kRowBatch];
+#pragma unroll
+          for (int u = 0; u < kRowBatch; ++u) q[u] = __ldcg(col + i + 256 * u);
+#pragma unroll
+          for (int u = 0; u < kRowBatch; ++u) __stcg(col + i + 256 * u, div_by(q[u], den, rden));
+        }
+        for (; i < rows; i += 256) __stcg(col + i, div_by(__ldcg(col + i), den, rden));
+        tau = __ddiv_rn(__dsub_rn(beta, c0), beta);
+      }
+      if (w == 0 && lane == 0) __stcg(col + kk, beta);
+    }
+    // apply H = I - tau v v^T to the columns after the pivot (Householder.h:116-133);
+    // the right-hand side only while kk < rank
+    const int c_lo = kk + 1, c_hi = s_nonzero == size ? k + 1 : k;
+    const int cnt = c_hi - c_lo;
+    if (cnt > 0) {
+      if (rows - kk == 1) {
+        if (w == 0)
+          for (int j = lane; j < cnt; j += 32) {
+            double* q = colp[c_lo + j] + kk;
+            __stcg(q, __dmul_rn(__ldcg(q), __dsub_rn(1.0, tau)));
+          }
+      } else if (tau != 0.0) {
+        const double* v = col;
+        double* cp[KB];
+        double qk[KB];
+#pragma unroll
+        for (int j = 0; j < KB; ++j) {
+          cp[j] = j < cnt ? colp[c_lo + j] : nullptr;
+          qk[j] = j < cnt ? __ldcg(cp[j] + kk) : 0.0;  // row kk, read before CTA 0 rewrites it
+          part[j] = 0.0;
+        }
+        constexpr int U = ColBatch<KB>::U;
+        {
+          int64_t i = kk + 1 + L;
+          for (; i + 256 * (U - 1) < rows; i += 256 * U) {
+            double vi[U], cv[U][KB];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+              vi[u] = __ldcg(v + i + 256 * u);
+#pragma unroll
+              for (int j = 0; j < KB; ++j) cv[u][j] = j < cnt ? __ldcg(cp[j] + i + 256 * u) : 0.0;
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u)
+#pragma unroll
+              for (int j = 0; j < KB; ++j)
+                if (j < cnt) part[j] = __dadd_rn(part[j], __dmul_rn(vi[u], cv[u][j]));
+          }
+          for (; i < rows; i += 256) {
+            const double vi = __ldcg(v + i);
+#pragma unroll
+            for (int j = 0; j < KB; ++j)
+              if (j < cnt) part[j] = __dadd_rn(part[j], __dmul_rn(vi, __ldcg(cp[j] + i)));
+          }
+        }
+        cl_sum_vec<KB>(cl, red, part, cnt, out);
+        // tmp_j += Q[kk, j]; Q[kk, j] -= tau * tmp_j
+#pragma unroll
+        for (int j = 0; j < KB; ++j) {
+          if (j >= cnt) continue;
+          out[j] = __dadd_rn(out[j], qk[j]);
+          if (w == 0 && lane == (j & 31)) __stcg(cp[j] + kk, __dsub_rn(qk[j], __dmul_rn(tau, out[j])));
+        }
+        {
+          int64_t i = kk + 1 + L;
+          for (; i + 256 * (U - 1) < rows; i += 256 * U) {
+            double tv[U], cv[U][KB];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+              tv[u] = __ldcg(v + i + 256 * u);
+#pragma unroll
+              for (int j = 0; j < KB; ++j) cv[u][j] = j < cnt ? __ldcg(cp[j] + i + 256 * u) : 0.0;
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+              const double t = __dmul_rn(tau, tv[u]);
+#pragma unroll
+              for (int j = 0; j < KB; ++j)
+                if (j < cnt) __stcg(cp[j] + i + 256 * u, __dsub_rn(cv[u][j], __dmul_rn(t, out[j])));
+            }
+          }
+          for (; i < rows; i += 256) {
+            const double t = __dmul_rn(tau, __ldcg(v + i));
+#pragma unroll
+            for (int j = 0; j < KB; ++j)
+              if (j < cnt) __stcg(cp[j] + i, __dsub_rn(__ldcg(cp[j] + i), __dmul_rn(t, out[j])));
+          }
+        }
+      }
+    }
+    cl.sync();  // the step's rows (and row kk) visible to every CTA
+    // LAWN 176 norm down-dating (ColPivHouseholderQR.h:549-572)
+    if (lane == 0) {
+      for (int j = kk + 1; j < k; ++j) {
+        rec[j] = 0;
+        if (nupd[j] != 0.0) {
+          double temp = __ddiv_rn(fabs(__ldcg(colp[j] + kk)), nupd[j]);
+          temp = __dmul_rn(__dadd_rn(1.0, temp), __dsub_rn(1.0, temp));
+          temp = temp < 0.0 ? 0.0 : temp;
+          const double ratio = __ddiv_rn(nupd[j], ndir[j]);
+          const double temp2 = __dmul_rn(temp, __dmul_rn(ratio, ratio));
+          if (temp2 <= downdate_thr) rec[j] = 1;
+          else nupd[j] = __dmul_rn(nupd[j], __dsqrt_rn(temp));
+        }
+      }
+    }
+    __syncwarp();
+    for (int j = kk + 1; j < k; ++j) {
+      if (!rec[j]) continue;  // uniform over the cluster
+      const double sq = cl_sum<KB>(cl, red, lane_sumsq(colp[j], kk + 1 + L, rows));
+      if (lane == 0) {
+        ndir[j] = __dsqrt_rn(sq);
+        nupd[j] = ndir[j];
+      }
+      __syncwarp();
+    }
+  }
+  if (w == 0 && lane == 0) {
+    const int r = s_nonzero;
+    double cvec[kMaxK];
+    for (int i = 0; i < r; ++i) cvec[i] = __ldcg(colp[k] + i);
+    for (int kk = r - 1; kk >= 0; --kk) {
+      cvec[kk] = __ddiv_rn(cvec[kk], __ldcg(colp[kk] + kk));
+      for (int i = 0; i < kk; ++i) cvec[i] = __dsub_rn(cvec[i], __dmul_rn(cvec[kk], __ldcg(colp[kk] + i)));
+    }
+    double* outc = coefs + cd.coef_offset;
+    for (int j = 0; j < k; ++j) outc[j] = 0.0;
+    for (int i = 0; i < r; ++i) outc[perm[i]] = cvec[i];
+    res[c].rank = r;
+  }
+  // no CTA leaves while another may still write into its shared memory
+  cl.sync();
+}
+
 }  // namespace
 
 int plain_qr_bucket(int cols) { return cols <= 4 ? 4 : (cols <= 8 ? 8 : (cols <= 16 ? 16 : kMaxK + 1)); }
@@ -557,6 +904,23 @@ bool launch_plain_qr(int max_cols, int grid, cudaStream_t st, DevBatch b, DevDat
   else
     plain_qr_kernel_t<kMaxK + 1><<<grid, 256, sm, st>>>(b, ds, pc, list, cand0, A, M, S, tsqr, nb, coefs, res, status,
                                                         redo, colmap);
+  return cudaGetLastError() == cudaSuccess;
+}
+
+bool launch_plain_qr_cluster(int max_cols, int n_cand, cudaStream_t st, DevBatch b, DevData ds, const PlainCand* pc,
+                             const int32_t* list, int cand0, const double* A, double* M, double* coefs,
+                             rrg_result* res, uint32_t* status, const int32_t* colmap) {
+  if (n_cand <= 0) return true;
+  const int grid = n_cand * kQrCluster;
+  if (max_cols <= 4)
+    plain_qr_cluster_kernel<4><<<grid, 32, 0, st>>>(b, ds, pc, list, cand0, A, M, coefs, res, status, colmap);
+  else if (max_cols <= 8)
+    plain_qr_cluster_kernel<8><<<grid, 32, 0, st>>>(b, ds, pc, list, cand0, A, M, coefs, res, status, colmap);
+  else if (max_cols <= 16)
+    plain_qr_cluster_kernel<16><<<grid, 32, 0, st>>>(b, ds, pc, list, cand0, A, M, coefs, res, status, colmap);
+  else
+    plain_qr_cluster_kernel<kMaxK + 1><<<grid, 32, 0, st>>>(b, ds, pc, list, cand0, A, M, coefs, res, status,
+                                                            colmap);
   return cudaGetLastError() == cudaSuccess;
 }
 

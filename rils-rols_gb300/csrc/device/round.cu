@@ -952,8 +952,7 @@ rrg_status rrg_context::run_fp64_table(const rrg_dataset* ds, const std::vector<
         while (b1 < sb.second && bucket(list[pos + b1]) == bk) ++b1;
         cudaStream_t s = side[used % kSide];
         if (used < kSide) RRG_CUDA(cudaStreamWaitEvent(s, fork_ev, 0));
-        if (!launch_plain_qr(bk, b1 - b0, s, dev, dd, d_pcs, d_list, b0, F64, M, nullptr, 0, 1, coefs, res, status,
-                             nullptr, d_cmap)) {
+        if (!launch_plain_qr_cluster(bk, b1 - b0, s, dev, dd, d_pcs, d_list, b0, F64, M, coefs, res, status, d_cmap)) {
           cuda_ok(cudaGetLastError(), "QR launch");
           return RRG_E_CUDA;
         }
