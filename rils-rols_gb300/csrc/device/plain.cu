@@ -543,15 +543,18 @@ __global__ void __launch_bounds__(256) plain_qr_kernel_t(DevBatch b, DevData ds,
 
 // ------------------------------------------------- cluster-wide direct QR --
 // The same factorisation as plain_qr_kernel_t (direct, tsqr = 0), with the
-// 256 lanes of every RR256 sum spread over a cluster of kQrCluster CTAs of
-// one warp each: CTA w runs lanes 32w .. 32w + 31.  Each CTA folds its warp
-// and sends the total to every CTA of the cluster through distributed shared
-// memory; after the cluster barrier each CTA adds the eight totals in order,
-// so every sum is bit-identical to the one-block kernel's.  The scalar
+// 256 lanes of every RR256 sum spread over a cluster of kQrCluster CTAs:
+// CTA w runs lanes 32w .. 32w + 31.  A CTA has W warps over the same 32
+// lanes; the columns of a pass are dealt to them (offset j to warp j mod W),
+// so each column's lane sums are formed by one warp exactly as in the
+// one-block kernel.  Each warp folds its columns and sends the totals to
+// every CTA of the cluster through distributed shared memory; after the
+// cluster barrier every CTA adds the eight totals of a column in order, so
+// every sum is bit-identical to the one-block kernel's.  The scalar
 // bookkeeping (norms, pivots, permutation) is replicated in every CTA from
 // identical inputs; row kk of the working columns (the R entries) is written
-// by CTA 0 only, after every CTA has read the old values.  A lane touches the
-// rows kk + 1 + lane + 256 t within one step, which shift by one row per
+// by CTA 0 only, after every CTA has read the old values.  A lane touches
+// the rows kk + 1 + lane + 256 t within one step, which shift by one row per
 // step, so a cluster barrier closes each step; working-column loads bypass
 // L1 (ld.global.cg) since other SMs of the cluster wrote them.
 namespace cg = cooperative_groups;
@@ -563,44 +566,53 @@ struct ClRed {
   int parity;
 };
 
-// Element-wise RR256 sum of part[0..cnt) over the cluster; every lane of
-// every CTA gets out[0..cnt).
-template <int KB>
-__device__ __forceinline__ void cl_sum_vec(cg::cluster_group& cl, ClRed<KB>& r, const double (&part)[KB], int cnt,
-                                           double (&out)[KB]) {
-  const int w = (int)cl.block_rank(), lane = threadIdx.x & 31;
+// RR256 sums of the columns a warp holds: slot s of warp wi is column
+// offset j = wi + s W (j < cnt); every lane of the warp gets out[s].
+template <int KB, int W, int CPW>
+__device__ __forceinline__ void cl_sum_cols(cg::cluster_group& cl, ClRed<KB>& r, const double (&part)[CPW], int cnt,
+                                            double (&out)[CPW]) {
+  const int w = (int)cl.block_rank(), lane = threadIdx.x & 31, wi = threadIdx.x >> 5;
   double* buf = r.buf[r.parity];
 #pragma unroll
-  for (int j = 0; j < KB; ++j)
+  for (int s = 0; s < CPW; ++s) {
+    const int j = wi + s * W;
     if (j < cnt) {
-      const double v = __shfl_sync(0xffffffffu, warp_sum(part[j]), 0);  // lane 0's fold is the RR256 one
+      const double v = __shfl_sync(0xffffffffu, warp_sum(part[s]), 0);  // lane 0's fold is the RR256 one
       if (lane < kQrCluster) cl.map_shared_rank(buf, lane)[w * KB + j] = v;
     }
+  }
   cl.sync();
 #pragma unroll
-  for (int j = 0; j < KB; ++j) {
-    double s = 0.0;
+  for (int s = 0; s < CPW; ++s) {
+    const int j = wi + s * W;
+    double t = 0.0;
     if (j < cnt)
-      for (int i = 0; i < kQrCluster; ++i) s = __dadd_rn(s, buf[i * KB + j]);
-    out[j] = s;
+      for (int i = 0; i < kQrCluster; ++i) t = __dadd_rn(t, buf[i * KB + j]);
+    out[s] = t;
   }
-  __syncwarp();
-  if (lane == 0) r.parity ^= 1;
-  __syncwarp();
+  __syncthreads();
+  if (threadIdx.x == 0) r.parity ^= 1;
+  __syncthreads();
 }
 
-template <int KB>
-__device__ __forceinline__ double cl_sum(cg::cluster_group& cl, ClRed<KB>& r, double v) {
-  double part[KB], out[KB];
+// One RR256 sum formed by warp 0 (the other warps pass 0 and only take part
+// in the barrier); every thread gets the total.
+template <int KB, int W, int CPW>
+__device__ __forceinline__ double cl_sum1(cg::cluster_group& cl, ClRed<KB>& r, double v) {
+  double part[CPW], out[CPW];
 #pragma unroll
-  for (int j = 0; j < KB; ++j) part[j] = j == 0 ? v : 0.0;
-  cl_sum_vec<KB>(cl, r, part, 1, out);
-  return out[0];
+  for (int s = 0; s < CPW; ++s) part[s] = s == 0 ? v : 0.0;
+  cl_sum_cols<KB, W, CPW>(cl, r, part, 1, out);
+  __shared__ double tot;
+  if (threadIdx.x == 0) tot = out[0];
+  __syncthreads();
+  const double t = tot;
+  __syncthreads();
+  return t;
 }
 
 // One lane's share of an RR256 sum of squares over rows i0, i0 + 256, ...
-// (in row order), with the loads of kRowBatch rows issued together: a
-// cluster CTA is a single warp, so latency is hidden by in-flight loads.
+// (in row order), with the loads of kRowBatch rows issued together.
 constexpr int kRowBatch = 8;
 __device__ __forceinline__ double lane_sumsq(const double* col, int64_t i0, int64_t rows) {
   double ps = 0.0;
@@ -619,20 +631,24 @@ __device__ __forceinline__ double lane_sumsq(const double* col, int64_t i0, int6
   return ps;
 }
 
-// rows per batch of the dot and update passes: KB columns each
+// Warps per CTA by column bucket, columns per warp and rows per batch of the
+// dot and update passes.
 template <int KB>
-struct ColBatch {
-  static constexpr int U = KB <= 4 ? 8 : (KB <= 8 ? 4 : (KB <= 16 ? 2 : 1));
+struct QrShape {
+  static constexpr int W = KB <= 4 ? 1 : (KB <= 8 ? 2 : (KB <= 16 ? 4 : 8));
+  static constexpr int CPW = (KB + W - 1) / W;
+  static constexpr int U = CPW <= 4 ? 8 : (CPW <= 8 ? 4 : 2);
 };
 
 template <int KB>
-__global__ void __cluster_dims__(kQrCluster, 1, 1) __launch_bounds__(32)
+__global__ void __cluster_dims__(kQrCluster, 1, 1) __launch_bounds__(32 * QrShape<KB>::W)
     plain_qr_cluster_kernel(DevBatch b, DevData ds, const PlainCand* pc, const int32_t* list, int cand0,
                             const double* A, double* M, double* coefs, rrg_result* res, uint32_t* status,
                             const int32_t* colmap) {
+  constexpr int W = QrShape<KB>::W, CPW = QrShape<KB>::CPW, U = QrShape<KB>::U;
   cg::cluster_group cl = cg::this_cluster();
   const int w = (int)cl.block_rank();
-  const int lane = threadIdx.x;
+  const int lane = threadIdx.x & 31, wi = threadIdx.x >> 5;
   const int L = w * 32 + lane;  // RR256 lane
   const int ci = blockIdx.x / kQrCluster;
   const int c = list ? list[cand0 + ci] : cand0 + ci;
@@ -641,7 +657,7 @@ __global__ void __cluster_dims__(kQrCluster, 1, 1) __launch_bounds__(32)
   if (cd.mode != RRG_TUNED || (pc[c].pad & 1)) return;
   const int k = pc[c].k;
   if (k + 1 > KB || k > kMaxK) {
-    if (w == 0 && lane == 0) atomicOr(status, ST_TOO_LARGE);
+    if (w == 0 && threadIdx.x == 0) atomicOr(status, ST_TOO_LARGE);
     return;
   }
   __shared__ ClRed<KB> red;
@@ -649,17 +665,19 @@ __global__ void __cluster_dims__(kQrCluster, 1, 1) __launch_bounds__(32)
   __shared__ int perm[KB], rec[KB];
   __shared__ double* colp[KB];
   __shared__ int s_nonzero;
-  if (lane == 0) red.parity = 0;
+  if (threadIdx.x == 0) red.parity = 0;
   cl.sync();  // every CTA of the cluster running before any distributed shared memory access
   double* Q = M + pc[c].m_col * ds.n_pad;
   const int64_t ld = ds.n_pad, rows = ds.n;
-  for (int j = lane; j <= k; j += 32) colp[j] = Q + (int64_t)j * ld;
-  __syncwarp();
-  // [A | 1 | y] into the working columns, the initial norms on the way
-  double part[KB], out[KB];
+  for (int j = threadIdx.x; j <= k; j += blockDim.x) colp[j] = Q + (int64_t)j * ld;
+  __syncthreads();
+  // [A | 1 | y] into the working columns (column j by warp j mod W), the
+  // initial norms on the way
+  double part[CPW], out[CPW];
 #pragma unroll
-  for (int j = 0; j < KB; ++j) {
-    part[j] = 0.0;
+  for (int s = 0; s < CPW; ++s) {
+    part[s] = 0.0;
+    const int j = wi + s * W;
     if (j > k) continue;
     double* dst = Q + (int64_t)j * ld;
     if (j < k - 1) {
@@ -681,32 +699,34 @@ __global__ void __cluster_dims__(kQrCluster, 1, 1) __launch_bounds__(32)
         __stcg(dst + r, v);
         acc = __dadd_rn(acc, __dmul_rn(v, v));
       }
-      part[j] = acc;
+      part[s] = acc;
     } else if (j == k - 1) {
       double acc = 0.0;
       for (int64_t r = L; r < rows; r += 256) {
         __stcg(dst + r, 1.0);
         acc = __dadd_rn(acc, 1.0);
       }
-      part[j] = acc;
+      part[s] = acc;
     } else {
       for (int64_t r = L; r < rows; r += 256) __stcg(dst + r, ds.y64[r]);
     }
   }
-  cl_sum_vec<KB>(cl, red, part, k, out);  // its barrier also publishes the copies
+  cl_sum_cols<KB, W, CPW>(cl, red, part, k, out);  // its barrier also publishes the copies
   const double rows_thr = (double)ds.n;
   const int size = (int)(rows < k ? rows : k);
   if (lane == 0) {
 #pragma unroll
-    for (int j = 0; j < KB; ++j)
+    for (int s = 0; s < CPW; ++s) {
+      const int j = wi + s * W;
       if (j < k) {
-        ndir[j] = __dsqrt_rn(out[j]);
+        ndir[j] = __dsqrt_rn(out[s]);
         nupd[j] = ndir[j];
         perm[j] = j;
       }
-    s_nonzero = size;
+    }
   }
-  __syncwarp();
+  if (threadIdx.x == 0) s_nonzero = size;
+  __syncthreads();
   double maxn = nupd[0];
   for (int j = 1; j < k; ++j)
     if (nupd[j] > maxn) maxn = nupd[j];
@@ -714,7 +734,7 @@ __global__ void __cluster_dims__(kQrCluster, 1, 1) __launch_bounds__(32)
   const double downdate_thr = 1.4901161193847656e-08;  // sqrt(DBL_EPSILON)
 
   for (int kk = 0; kk < size; ++kk) {
-    if (lane == 0) {
+    if (threadIdx.x == 0) {
       int big = kk;
       double bign = nupd[kk];
       for (int j = kk + 1; j < k; ++j)
@@ -730,37 +750,40 @@ __global__ void __cluster_dims__(kQrCluster, 1, 1) __launch_bounds__(32)
         double* cq = colp[kk]; colp[kk] = colp[big]; colp[big] = cq;
       }
     }
-    __syncwarp();
+    __syncthreads();
     // Householder reflector of the pivot column (Householder.h:67-96)
     double* col = colp[kk];
     double tau;
     {
       // c0 is read before the barrier of the tail sum, after which CTA 0 overwrites it with beta
       const double c0 = __ldcg(col + kk);
-      const double ps = lane_sumsq(col, kk + 1 + L, rows);
-      const double tail_sq = (rows - kk == 1) ? 0.0 : cl_sum<KB>(cl, red, ps);
+      const double ps = wi == 0 ? lane_sumsq(col, kk + 1 + L, rows) : 0.0;
+      const double tail_sq = (rows - kk == 1) ? 0.0 : cl_sum1<KB, W, CPW>(cl, red, ps);
       double beta;
       if (tail_sq <= DBL_MIN) {
         tau = 0.0;
         beta = c0;
-        for (int64_t i = kk + 1 + L; i < rows; i += 256) __stcg(col + i, 0.0);
+        for (int64_t i = kk + 1 + L + 256 * (int64_t)wi; i < rows; i += 256 * W) __stcg(col + i, 0.0);
       } else {
         beta = __dsqrt_rn(__dadd_rn(__dmul_rn(c0, c0), tail_sq));
         if (c0 >= 0.0) beta = -beta;
         const double den = __dsub_rn(c0, beta);
         const double rden = __drcp_rn(den);
-        int64_t i = kk + 1 + L;
-        for (; i + 256 * (kRowBatch - 1) < rows; i += 256 * kRowBatch) {
+        // element-wise: the lane's rows are dealt to the CTA's warps
+        int64_t i = kk + 1 + L + 256 * (int64_t)wi;
+        for (; i + 256 * W * (kRowBatch - 1) < rows; i += 256 * W * kRowBatch) {
           double q[kRowBatch];
 #pragma unroll
-          for (int u = 0; u < kRowBatch; ++u) q[u] = __ldcg(col + i + 256 * u);
+          for (int u = 0; u < kRowBatch; ++u) q[u] = __ldcg(col + i + 256 * W * u);
 #pragma unroll
-          for (int u = 0; u < kRowBatch; ++u) __stcg(col + i + 256 * u, div_by(q[u], den, rden));
+          for (int u = 0; u < kRowBatch; ++u) __stcg(col + i + 256 * W * u, div_by(q[u], den, rden));
         }
-        for (; i < rows; i += 256) __stcg(col + i, div_by(__ldcg(col + i), den, rden));
+        for (; i < rows; i += 256 * W) __stcg(col + i, div_by(__ldcg(col + i), den, rden));
         tau = __ddiv_rn(__dsub_rn(beta, c0), beta);
       }
-      if (w == 0 && lane == 0) __stcg(col + kk, beta);
+      if (w == 0 && threadIdx.x == 0) __stcg(col + kk, beta);
+      // the division pass wrote rows that other warps of this CTA read next
+      __syncthreads();
     }
     // apply H = I - tau v v^T to the columns after the pivot (Householder.h:116-133);
     // the right-hand side only while kk < rank
@@ -769,82 +792,82 @@ __global__ void __cluster_dims__(kQrCluster, 1, 1) __launch_bounds__(32)
     if (cnt > 0) {
       if (rows - kk == 1) {
         if (w == 0)
-          for (int j = lane; j < cnt; j += 32) {
+          for (int j = threadIdx.x; j < cnt; j += blockDim.x) {
             double* q = colp[c_lo + j] + kk;
             __stcg(q, __dmul_rn(__ldcg(q), __dsub_rn(1.0, tau)));
           }
       } else if (tau != 0.0) {
         const double* v = col;
-        double* cp[KB];
-        double qk[KB];
+        double* cp[CPW];
+        double qk[CPW];
 #pragma unroll
-        for (int j = 0; j < KB; ++j) {
-          cp[j] = j < cnt ? colp[c_lo + j] : nullptr;
-          qk[j] = j < cnt ? __ldcg(cp[j] + kk) : 0.0;  // row kk, read before CTA 0 rewrites it
-          part[j] = 0.0;
+        for (int s = 0; s < CPW; ++s) {
+          const int j = wi + s * W;
+          cp[s] = j < cnt ? colp[c_lo + j] : nullptr;
+          qk[s] = j < cnt ? __ldcg(cp[s] + kk) : 0.0;  // row kk, read before CTA 0 rewrites it
+          part[s] = 0.0;
         }
-        constexpr int U = ColBatch<KB>::U;
         {
           int64_t i = kk + 1 + L;
           for (; i + 256 * (U - 1) < rows; i += 256 * U) {
-            double vi[U], cv[U][KB];
+            double vi[U], cv[U][CPW];
 #pragma unroll
             for (int u = 0; u < U; ++u) {
               vi[u] = __ldcg(v + i + 256 * u);
 #pragma unroll
-              for (int j = 0; j < KB; ++j) cv[u][j] = j < cnt ? __ldcg(cp[j] + i + 256 * u) : 0.0;
+              for (int s = 0; s < CPW; ++s) cv[u][s] = cp[s] ? __ldcg(cp[s] + i + 256 * u) : 0.0;
             }
 #pragma unroll
             for (int u = 0; u < U; ++u)
 #pragma unroll
-              for (int j = 0; j < KB; ++j)
-                if (j < cnt) part[j] = __dadd_rn(part[j], __dmul_rn(vi[u], cv[u][j]));
+              for (int s = 0; s < CPW; ++s)
+                if (cp[s]) part[s] = __dadd_rn(part[s], __dmul_rn(vi[u], cv[u][s]));
           }
           for (; i < rows; i += 256) {
             const double vi = __ldcg(v + i);
 #pragma unroll
-            for (int j = 0; j < KB; ++j)
-              if (j < cnt) part[j] = __dadd_rn(part[j], __dmul_rn(vi, __ldcg(cp[j] + i)));
+            for (int s = 0; s < CPW; ++s)
+              if (cp[s]) part[s] = __dadd_rn(part[s], __dmul_rn(vi, __ldcg(cp[s] + i)));
           }
         }
-        cl_sum_vec<KB>(cl, red, part, cnt, out);
+        cl_sum_cols<KB, W, CPW>(cl, red, part, cnt, out);
         // tmp_j += Q[kk, j]; Q[kk, j] -= tau * tmp_j
 #pragma unroll
-        for (int j = 0; j < KB; ++j) {
-          if (j >= cnt) continue;
-          out[j] = __dadd_rn(out[j], qk[j]);
-          if (w == 0 && lane == (j & 31)) __stcg(cp[j] + kk, __dsub_rn(qk[j], __dmul_rn(tau, out[j])));
+        for (int s = 0; s < CPW; ++s) {
+          if (!cp[s]) continue;
+          out[s] = __dadd_rn(out[s], qk[s]);
+          if (w == 0 && lane == 0) __stcg(cp[s] + kk, __dsub_rn(qk[s], __dmul_rn(tau, out[s])));
         }
         {
           int64_t i = kk + 1 + L;
           for (; i + 256 * (U - 1) < rows; i += 256 * U) {
-            double tv[U], cv[U][KB];
+            double tv[U], cv[U][CPW];
 #pragma unroll
             for (int u = 0; u < U; ++u) {
               tv[u] = __ldcg(v + i + 256 * u);
 #pragma unroll
-              for (int j = 0; j < KB; ++j) cv[u][j] = j < cnt ? __ldcg(cp[j] + i + 256 * u) : 0.0;
+              for (int s = 0; s < CPW; ++s) cv[u][s] = cp[s] ? __ldcg(cp[s] + i + 256 * u) : 0.0;
             }
 #pragma unroll
             for (int u = 0; u < U; ++u) {
               const double t = __dmul_rn(tau, tv[u]);
 #pragma unroll
-              for (int j = 0; j < KB; ++j)
-                if (j < cnt) __stcg(cp[j] + i + 256 * u, __dsub_rn(cv[u][j], __dmul_rn(t, out[j])));
+              for (int s = 0; s < CPW; ++s)
+                if (cp[s]) __stcg(cp[s] + i + 256 * u, __dsub_rn(cv[u][s], __dmul_rn(t, out[s])));
             }
           }
           for (; i < rows; i += 256) {
             const double t = __dmul_rn(tau, __ldcg(v + i));
 #pragma unroll
-            for (int j = 0; j < KB; ++j)
-              if (j < cnt) __stcg(cp[j] + i, __dsub_rn(__ldcg(cp[j] + i), __dmul_rn(t, out[j])));
+            for (int s = 0; s < CPW; ++s)
+              if (cp[s]) __stcg(cp[s] + i, __dsub_rn(__ldcg(cp[s] + i), __dmul_rn(t, out[s])));
           }
         }
       }
     }
     cl.sync();  // the step's rows (and row kk) visible to every CTA
     // LAWN 176 norm down-dating (ColPivHouseholderQR.h:549-572)
-    if (lane == 0) {
+    if (threadIdx.x == 0) {
       for (int j = kk + 1; j < k; ++j) {
         rec[j] = 0;
         if (nupd[j] != 0.0) {
@@ -858,18 +881,32 @@ __global__ void __cluster_dims__(kQrCluster, 1, 1) __launch_bounds__(32)
         }
       }
     }
-    __syncwarp();
-    for (int j = kk + 1; j < k; ++j) {
-      if (!rec[j]) continue;  // uniform over the cluster
-      const double sq = cl_sum<KB>(cl, red, lane_sumsq(colp[j], kk + 1 + L, rows));
-      if (lane == 0) {
-        ndir[j] = __dsqrt_rn(sq);
-        nupd[j] = ndir[j];
+    __syncthreads();
+    // direct recomputation of the flagged norms: one barrier for all of them
+    // (column j by warp j mod W); every CTA takes the same branch
+    int any_rec = 0;
+    for (int j = kk + 1; j < k; ++j) any_rec |= rec[j];
+    if (any_rec) {
+#pragma unroll
+      for (int s = 0; s < CPW; ++s) {
+        const int j = wi + s * W;
+        part[s] = (j > kk && j < k && rec[j]) ? lane_sumsq(colp[j], kk + 1 + L, rows) : 0.0;
       }
-      __syncwarp();
+      cl_sum_cols<KB, W, CPW>(cl, red, part, k, out);
+      if (lane == 0) {
+#pragma unroll
+        for (int s = 0; s < CPW; ++s) {
+          const int j = wi + s * W;
+          if (j > kk && j < k && rec[j]) {
+            ndir[j] = __dsqrt_rn(out[s]);
+            nupd[j] = ndir[j];
+          }
+        }
+      }
+      __syncthreads();
     }
   }
-  if (w == 0 && lane == 0) {
+  if (w == 0 && threadIdx.x == 0) {
     const int r = s_nonzero;
     double cvec[kMaxK];
     for (int i = 0; i < r; ++i) cvec[i] = __ldcg(colp[k] + i);
@@ -912,15 +949,18 @@ bool launch_plain_qr_cluster(int max_cols, int n_cand, cudaStream_t st, DevBatch
                              rrg_result* res, uint32_t* status, const int32_t* colmap) {
   if (n_cand <= 0) return true;
   const int grid = n_cand * kQrCluster;
+#define RRG_QR_CLUSTER(KB)                                                                                   \
+  plain_qr_cluster_kernel<KB><<<grid, 32 * QrShape<KB>::W, 0, st>>>(b, ds, pc, list, cand0, A, M, coefs, res, \
+                                                                     status, colmap)
   if (max_cols <= 4)
-    plain_qr_cluster_kernel<4><<<grid, 32, 0, st>>>(b, ds, pc, list, cand0, A, M, coefs, res, status, colmap);
+    RRG_QR_CLUSTER(4);
   else if (max_cols <= 8)
-    plain_qr_cluster_kernel<8><<<grid, 32, 0, st>>>(b, ds, pc, list, cand0, A, M, coefs, res, status, colmap);
+    RRG_QR_CLUSTER(8);
   else if (max_cols <= 16)
-    plain_qr_cluster_kernel<16><<<grid, 32, 0, st>>>(b, ds, pc, list, cand0, A, M, coefs, res, status, colmap);
+    RRG_QR_CLUSTER(16);
   else
-    plain_qr_cluster_kernel<kMaxK + 1><<<grid, 32, 0, st>>>(b, ds, pc, list, cand0, A, M, coefs, res, status,
-                                                            colmap);
+    RRG_QR_CLUSTER(kMaxK + 1);
+#undef RRG_QR_CLUSTER
   return cudaGetLastError() == cudaSuccess;
 }
 
