@@ -236,23 +236,24 @@ def run_ours(args):
     def timed_rounds(prec, steps):
         """(seconds per round list, last output, launches, phase ms sums, phase launch counts, stats)"""
         ctx.set_timing(True)
-        phase_ms, phase_n, times, launches, out = {}, {}, [], 0, None
+        phase_ms, phase_b, times, launches, out = {}, {}, [], 0, None
         for _ in range(steps):
             dt, out = timed_round(ctx, ds, batch, prec, stream, flush)
             times.append(dt)
             launches += ctx.last_round_launches()
             for k, (ms, cnt) in ctx.last_round_timing().items():
                 phase_ms[k] = phase_ms.get(k, 0.0) + ms
-                phase_n[k] = phase_n.get(k, 0) + cnt
+            for k, b in ctx.last_round_bytes().items():
+                phase_b[k] = phase_b.get(k, 0.0) + b
         ctx.set_timing(False)
-        return times, out, launches, phase_ms, phase_n, ctx.last_round_stats()
+        return times, out, launches, phase_ms, phase_b, ctx.last_round_stats()
 
     for _ in range(args.warmup):
         ds.evaluate(batch, CERTIFIED)
     barrier(world)
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
-        times, cert, launches, phase_ms, phase_n, stats = timed_rounds(CERTIFIED, args.steps)
+        times, cert, launches, phase_ms, phase_b, stats = timed_rounds(CERTIFIED, args.steps)
     torch.cuda.synchronize()
     barrier(world)
     value, t_max = aggregate(B * args.steps, sum(times), world)
@@ -284,7 +285,8 @@ def run_ours(args):
            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
            "gpu_launches": int(launches), "round_stats": stats}
     res["phase_ms_per_step"] = {k: v / args.steps for k, v in phase_ms.items() if v > 0}
-    res["roofline"] = roofline(res["phase_ms_per_step"], phase_n, args.steps, args.n)
+    res["phase_bytes_per_step"] = {k: v / args.steps for k, v in phase_b.items() if v > 0}
+    res["roofline"] = roofline(res["phase_ms_per_step"], res["phase_bytes_per_step"])
     res["clocks"] = clk.summary()
     if args.quick:
         print(json.dumps(res))
@@ -376,54 +378,53 @@ def serving_leg(args, device=0):
     }
 
 
-# kernels behind the timed phases, with the algorithmic bytes of one launch
+# kernels behind the timed phases (the roofline candidates)
 PHASE_KERNELS = {
     "factor_eval": "fac_eval_kernel (double-float factor table)",
     "pair_sums": "pair_sum_kernel",
-    "mixed_residual": "ftab_resid_kernel",
     "fp64_eval": "plain_eval_kernel (FP64 table)",
-    "fp64_qr": "plain_qr_kernel_t (direct column-pivoted QR, FP64)",
+    "fp64_qr": "plain_qr_cluster_kernel (direct column-pivoted QR, FP64, 8-CTA clusters)",
 }
 
 
-def roofline(phase_ms, phase_n, steps, n):
-    """Roofline of the phase with the largest time.  Its bytes are algorithmic:
-    the FP64 table written once (8 B per row and column) for the evaluators,
-    every column read once for the QR and the sums; these kernels are bound by
-    the FP32 / FP64 pipes (see profiles/), so the HBM fraction is small."""
+def roofline(phase_ms, phase_bytes):
+    """Roofline of the phase with the largest device time in one round.  A
+    "launch" here is that phase's kernels of one round; its bytes are the
+    algorithmic ones the library counts (rrg_last_round_bytes), its time the
+    CUDA-event phase time on the library's stream.  `traffic` scales them by
+    the DRAM/algorithmic ratio of the committed ncu capture of the same
+    kernels (profiles/<phase>_1m.txt); these kernels are FP64- or
+    FP32-pipe-bound (the `pipe` figure of that capture), so their HBM
+    fraction is small by construction."""
     peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
     peak = peaks.get("hbm_gbs", 6800.0)
     cand = {k: v for k, v in phase_ms.items() if k in PHASE_KERNELS}
     if not cand:
         return None
     top = max(cand, key=cand.get)
-    launches = max(1, phase_n.get(top, 1)) / steps
-    ms_per_launch = cand[top] / launches
-    traffic = read_profile_traffic(top)
-    algo = traffic.get("algorithmic_bytes_per_launch") if traffic else None
-    achieved = algo / (ms_per_launch / 1e3) / 1e9 if algo else None
+    ms = cand[top]
+    algo = phase_bytes.get(top)
+    achieved = algo / (ms / 1e3) / 1e9 if algo else None
+    prof = read_profile(top) or {}
+    ratio = prof.get("dram_over_algorithmic")
     return {"kernel": PHASE_KERNELS[top], "phase": top, "bound": "hbm", "achieved": achieved, "peak": peak,
             "unit": "GB/s", "frac": (achieved / peak) if achieved else None,
-            "traffic": traffic.get("dram_bytes_per_launch") if traffic else None,
-            "ms_per_launch": ms_per_launch, "launches_per_step": launches,
-            "peak_source": "measured" if peaks else "fallback",
-            "compute_bound": traffic.get("pipe") if traffic else None}
+            "traffic": ratio * algo if (ratio and algo) else None, "algorithmic_bytes": algo, "ms_per_launch": ms,
+            "peak_source": "measured" if peaks else "fallback", "pipe": prof.get("pipe")}
 
 
-def read_profile_traffic(phase):
-    """Figures of the committed ncu summary of the phase's kernel at the
-    bench's size: lines `key=value` in profiles/<phase>_1m.txt."""
+def read_profile(phase):
+    """`key=value` lines of the committed ncu summary of the phase's kernels."""
     p = ROOT / "profiles" / f"{phase}_1m.txt"
     if not p.exists():
         return None
     out = {}
     for line in p.read_text().splitlines():
-        if "=" in line and not line.startswith(" ") and line.split("=")[0] in (
-                "algorithmic_bytes_per_launch", "dram_bytes_per_launch", "pipe"):
+        if "=" in line and not line.startswith(" ") and line.split("=")[0] in ("dram_over_algorithmic", "pipe"):
             k, v = line.split("=", 1)
-            v = v.strip().split()[0]
+            v = v.strip()
             try:
-                out[k] = float(v)
+                out[k] = float(v.split()[0])
             except ValueError:
                 out[k] = v
     return out

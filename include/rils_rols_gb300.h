@@ -250,6 +250,15 @@ rrg_status rrg_context_set_timing(rrg_context* ctx, int32_t on);
  * [3] finalize, [4] FP64 evaluation, [5] FP64 QR, [6] FP64 residual,
  * [7] mixed pair sums.  Returns the number of phases written. */
 int32_t rrg_last_round_timing(const rrg_context* ctx, double* ms, int64_t* launches, int32_t n);
+/* Algorithmic device-memory bytes of the last completed round, per phase (the
+ * phases of rrg_last_round_timing): [0] X and y read once plus the
+ * double-float table written once (8 B per row and column); [4] X read once
+ * plus the FP64 table written once; [5] per factorised candidate with K
+ * columns [A | 1 | y], the copy (K - 2 factor columns and y read, K written)
+ * and, per step, every remaining column read and written once; [7] every
+ * table column read once.  Phases without a count read 0.  Returns the
+ * number of phases written.  No counterpart in the reference. */
+int32_t rrg_last_round_bytes(const rrg_context* ctx, double* bytes, int32_t n);
 
 #ifdef __cplusplus
 }

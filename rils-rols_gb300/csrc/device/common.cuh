@@ -57,6 +57,8 @@ constexpr int kSrcT = 3;     // binary operand from table column `arg`
 // word of the round's 16-word status block counting candidates whose QR outcome
 // was decided from the table's column statistics (word 0 holds the error bits)
 constexpr int kStatusSentinel = 8;
+// words 10-11 of the status block: algorithmic bytes of the round's direct QRs (u64)
+constexpr int kStatusQrBytes = 10;
 constexpr double kEps12 = 1e-12;  // value_zero / value_one threshold (node.h:13-14)
 
 __host__ __device__ inline int64_t round_up(int64_t a, int64_t b) { return (a + b - 1) / b * b; }

@@ -918,6 +918,12 @@ __global__ void __cluster_dims__(kQrCluster, 1, 1) __launch_bounds__(32 * QrShap
     for (int j = 0; j < k; ++j) outc[j] = 0.0;
     for (int i = 0; i < r; ++i) outc[perm[i]] = cvec[i];
     res[c].rank = r;
+    // algorithmic bytes: the copy, then every remaining column (the right-hand
+    // side while kk < rank) read and written once per step
+    double cols = (double)(2 * k + 1);
+    for (int kk = 0; kk < size; ++kk) cols += 2.0 * (double)((kk < r ? k + 1 : k) - kk);
+    atomicAdd(reinterpret_cast<unsigned long long*>(status + kStatusQrBytes),
+              (unsigned long long)(cols * 8.0 * (double)rows));
   }
   // no CTA leaves while another may still write into its shared memory
   cl.sync();

@@ -642,6 +642,7 @@ rrg_status rrg_context::mixed_subround(const rrg_dataset* ds, const int32_t* lis
     g0 = level_groups[L];
   }
   mark_end(P_GRAM, t0);
+  phase_bytes[P_GRAM] += (double)ds->n * 8.0 * (double)(ds->d + 1 + ncol);
   t0 = mark_begin();
   PairArgs pa;
   pa.F = F;
@@ -657,6 +658,7 @@ rrg_status rrg_context::mixed_subround(const rrg_dataset* ds, const int32_t* lis
     return RRG_E_CUDA;
   }
   mark_end(P_PAIRS, t0);
+  phase_bytes[P_PAIRS] += (double)ds->n * 8.0 * (double)ncol;
   t0 = mark_begin();
   if (!launch_pair_reduce(P, n_pairs, n_chunks, 0, n_self, psum, stream) ||
       !launch_pair_reduce(P, n_pairs, n_super, n_self, n_pairs, psum, stream) ||
@@ -938,6 +940,7 @@ rrg_status rrg_context::run_fp64_table(const rrg_dataset* ds, const std::vector<
                                                                    pk.at<PlainCand>(d_ft64, o_pcs), d_cmap, cst,
                                                                    ds->n, coefs, res, status + kStatusSentinel);
     mark_end(P_PLAIN_EVAL, t0);
+    phase_bytes[P_PLAIN_EVAL] += (double)ds->n * 8.0 * (double)(ds->d + ncol);
     launches += 2;
     for (const auto& sb : subs) {
       const int32_t ns = sb.second - sb.first;

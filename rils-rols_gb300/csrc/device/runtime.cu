@@ -382,6 +382,7 @@ rrg_status rrg_context::submit(rrg_dataset* ds, const rrg_batch* b, int32_t prec
   RRG_CUDA(cudaSetDevice(device));
   launches = 0;
   last_plain_routed = last_fallback = last_pass2 = last_sentinel = 0;
+  for (double& v : phase_bytes) v = 0.0;
   for (auto& r : last_reasons) r = 0;
   marks.clear();
   event_next = 0;
@@ -450,6 +451,12 @@ rrg_status rrg_context::wait(int32_t timeout_ms) {
     return RRG_E_DEVICE_FAULT;
   }
   last_sentinel = static_cast<const uint32_t*>(h_status.ptr)[rrd::kStatusSentinel];
+  for (int i = 0; i < P_COUNT; ++i) last_phase_bytes[i] = phase_bytes[i];
+  {
+    unsigned long long qb = 0;
+    std::memcpy(&qb, static_cast<const uint32_t*>(h_status.ptr) + rrd::kStatusQrBytes, sizeof qb);
+    last_phase_bytes[P_PLAIN_QR] += (double)qb;
+  }
   for (int i = 0; i < P_COUNT; ++i) {
     phase_ms[i] = 0;
     phase_launches[i] = 0;
@@ -764,6 +771,13 @@ rrg_status rrg_device_memory(int32_t device, int64_t* free_bytes, int64_t* total
   *free_bytes = (int64_t)f;
   *total_bytes = (int64_t)t;
   return RRG_OK;
+}
+
+int32_t rrg_last_round_bytes(const rrg_context* ctx, double* bytes, int32_t n) {
+  if (!ctx || !bytes || n <= 0) return 0;
+  const int32_t k = n < (int32_t)rrg_context::P_COUNT ? n : (int32_t)rrg_context::P_COUNT;
+  for (int32_t i = 0; i < k; ++i) bytes[i] = ctx->last_phase_bytes[i];
+  return k;
 }
 
 int32_t rrg_last_round_timing(const rrg_context* ctx, double* ms, int64_t* launches, int32_t n) {

@@ -98,6 +98,8 @@ struct rrg_context {
   size_t event_next = 0;
   double phase_ms[P_COUNT] = {0};
   int64_t phase_launches[P_COUNT] = {0};
+  double phase_bytes[P_COUNT] = {0};      // algorithmic bytes (host-counted phases)
+  double last_phase_bytes[P_COUNT] = {0};
   cudaEvent_t mark_begin();
   void mark_end(int phase, cudaEvent_t begin);
 

@@ -73,7 +73,7 @@ EXPORTS = [
     "rrg_abi_version", "rrg_last_error", "rrg_context_create", "rrg_context_destroy", "rrg_dataset_create",
     "rrg_dataset_destroy", "rrg_round_submit", "rrg_round_wait", "rrg_eval", "rrg_predict", "rrg_batch_validate", "rrg_dataset_rows",
     "rrg_dataset_cols", "rrg_last_round_launches", "rrg_last_round_stats", "rrg_context_stream",
-    "rrg_context_set_timing", "rrg_last_round_timing", "rrg_eval_plain_noalloc", "rrg_context_set_limits",
+    "rrg_context_set_timing", "rrg_last_round_timing", "rrg_last_round_bytes", "rrg_eval_plain_noalloc", "rrg_context_set_limits",
     "rrg_device_memory",
     "rrh_create", "rrh_destroy", "rrh_set_backend", "rrh_set_precision", "rrh_fit", "rrh_predict",
     "rrh_model_string", "rrh_model_prefix", "rrh_best_time", "rrh_total_time", "rrh_fit_calls", "rrh_counter",
@@ -109,6 +109,7 @@ def _declare(lib):
         "rrg_context_stream": (vp, [vp]),
         "rrg_context_set_timing": (i32, [vp, i32]),
         "rrg_last_round_timing": (i32, [vp, dp, P(C.c_int64), i32]),
+        "rrg_last_round_bytes": (i32, [vp, dp, i32]),
         "rrg_eval_plain_noalloc": (i32, [vp, i64, vp, i64, i32, P(Batch), vp, vp, vp]),
         "rrg_context_set_limits": (i32, [vp, i64, i64]),
         "rrg_device_memory": (i32, [i32, P(C.c_int64), P(C.c_int64)]),

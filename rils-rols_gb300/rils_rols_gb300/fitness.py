@@ -145,6 +145,13 @@ class Context:
         self.lib.rrg_last_round_timing(self.h, ms, cnt, n)
         return {p: (ms[i], cnt[i]) for i, p in enumerate(self.PHASES)}
 
+    def last_round_bytes(self) -> dict:
+        """Algorithmic device-memory bytes of the last round per phase (0 where not counted)."""
+        n = len(self.PHASES)
+        b = (C.c_double * n)()
+        self.lib.rrg_last_round_bytes(self.h, b, n)
+        return {p: b[i] for i, p in enumerate(self.PHASES)}
+
     def stream(self) -> int:
         """cudaStream_t of this context, as an integer handle."""
         return int(self.lib.rrg_context_stream(self.h) or 0)
