@@ -9,10 +9,10 @@ Workload (one step): the local-search rounds of a search on the 1M-row,
 0.7 exp(0.3 x5) + 0.5% noise): every local-search candidate (all_candidates,
 rils_rols_cpp.cpp:348-443) of the eight intermediate models in
 synth.REGRESSION_1M_TRAJECTORY, 7083 tuned candidates, scored in one batched
-round.  Synthetic, seeded data; nothing is downloaded.  The same numbers are
-reported for 8192 random trees drawn like the standalone batched-fitness
-configuration (sizes 3..50 over + - * / sin cos ln exp sqrt, leaves x_j or
-U(-5, 5)).
+round.  Synthetic, seeded data; nothing is downloaded.  Also reported: the
+standalone batched-fitness configuration (8192 random trees, sizes 3..50
+over + - * / sin cos ln exp sqrt, leaves x_j or U(-5, 5), n = 100k, d = 10)
+and the serving stream (Poisson arrivals of whole fit jobs, first requests).
 
   value  device-resident: dataset in HBM, each step = one rrg_eval round
          (batch upload, kernels, result download), timed with CUDA events on
@@ -27,6 +27,7 @@ candidate against the FP64 path, the roofline of the dominant kernel, the
 CPU oracle timed on the host cores, clocks.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--serve-jobs J] [--serve-only] [--quick]
 """
 from __future__ import annotations
 
@@ -50,18 +51,14 @@ METRIC = "candidate fitness evals/s at n=1M (certified mixed precision, batched 
 UNIT = "evals/s"
 N_ROWS = 1_000_000
 N_FEAT = 5
-BATCH = 8192
 SEED = 12345
 
 
-def workload(n=N_ROWS, batch=BATCH, seed=SEED):
-    """(X, y, local-search candidates, random trees)"""
+def workload(n=N_ROWS, seed=SEED):
+    """(X, y, local-search candidates) of the 1M-row regression search"""
     from rils_rols_gb300 import synth
     X, y = synth.regression_1m(n=n, seed=seed)
-    ls = synth.ls_round_batch(d=N_FEAT)
-    rng = np.random.default_rng(seed + 1)
-    rand = [synth.random_tree(rng, int(rng.integers(3, 51)), N_FEAT) for _ in range(batch)]
-    return X, y, ls, rand
+    return X, y, synth.ls_round_batch(d=N_FEAT)
 
 
 def config(n, batch):
@@ -224,7 +221,7 @@ def run_ours(args):
 
     rank, world = dist_setup()
     local = int(os.environ.get("LOCAL_RANK", "0"))
-    X, y, ls_trees, rand_trees = workload(args.n, args.batch)
+    X, y, ls_trees = workload(args.n)
     trees = ls_trees
     B = len(trees)
     ctx = Context(local)
@@ -296,15 +293,31 @@ def run_ours(args):
     mtimes, mixed, _, mphase, _, mstats = timed_rounds(MIXED, max(2, args.steps // 2))
     res["mixed_uncertified"] = {"evals_per_s": B * len(mtimes) / sum(mtimes), "round_stats": mstats,
                                 "phase_ms_per_step": {k: v / len(mtimes) for k, v in mphase.items() if v > 0}}
-    # random-tree batch (standalone batched-fitness generator) at the same n
-    rb = encode(rand_trees, tuned=True)
-    ds.evaluate(rb, CERTIFIED)
-    dt_rc, _ = timed_round(ctx, ds, rb, CERTIFIED, stream, flush)
-    rcs = ctx.last_round_stats()
-    dt_r, _ = timed_round(ctx, ds, rb, MIXED, stream, flush)
-    res["random_trees_8192"] = {"certified_evals_per_s": len(rand_trees) / dt_rc, "certified_round_stats": rcs,
-                                "mixed_evals_per_s": len(rand_trees) / dt_r,
-                                "mixed_round_stats": ctx.last_round_stats()}
+    # standalone batched fitness: 8192 random trees (sizes 3..50 over + - * / sin
+    # cos ln exp sqrt, leaves x_j or U(-5, 5)) on n = 100k rows, d = 10, X ~ N(0,1),
+    # y = a random 15-node tree + 1% noise; certified and uncertified mixed
+    # against the FP64 path, per-candidate fitness error and ranking agreement
+    from rils_rols_gb300 import synth
+    X2, y2, rtrees, _ = synth.batched_fitness(n=100_000, d=10, n_trees=8192, seed=SEED)
+    ds2 = ctx.dataset(X2, y2)
+    rb = encode(rtrees, tuned=True)
+    ds2.evaluate(rb, CERTIFIED)
+    rt = {}
+    ctx.set_timing(True)
+    for name, prec in (("certified", CERTIFIED), ("mixed_uncertified", MIXED), ("plain_fp64", PLAIN)):
+        ts, out = [], None
+        for _ in range(3):
+            dt_, out = timed_round(ctx, ds2, rb, prec, stream, flush)
+            ts.append(dt_)
+        rt[name] = {"evals_per_s": len(rtrees) / min(ts), "out": out, "round_stats": ctx.last_round_stats(),
+                    "phase_ms": {k: v[0] for k, v in ctx.last_round_timing().items() if v[0] > 0}}
+    ctx.set_timing(False)
+    res["batched_fitness_8192_random_trees"] = {
+        "config": "n=100000, d=10, 8192 random trees, sizes 3..50, tuned (best of 3 rounds)",
+        **{k: {kk: v[kk] for kk in ("evals_per_s", "round_stats", "phase_ms")} for k, v in rt.items()},
+        "accuracy_vs_fp64": {"certified": accuracy(rt["certified"]["out"], rt["plain_fp64"]["out"]),
+                             "mixed_uncertified": accuracy(rt["mixed_uncertified"]["out"], rt["plain_fp64"]["out"])}}
+    ds2.close()
     # plain FP64: unbatched launches and the whole batch (accuracy reference)
     singles = [encode([t], tuned=True) for t in trees[:args.unbatched_sample]]
     ds.evaluate(singles[0], PLAIN)
@@ -361,6 +374,7 @@ def serving_leg(args, device=0):
         return out, wall, st
 
     conc, wall_c, st_c = run(RRG_MIXED_CERTIFIED, args.serve_active, True)
+    concp, wall_cp, st_cp = run(RRG_PLAIN_FP64, args.serve_active, True)
     ser, wall_s, st_s = run(RRG_PLAIN_FP64, 1, False)
     ttm = sorted(i["time_to_model_s"] for _, i in conc)
     run_s = [i["run_s"] for _, i in ser]
@@ -372,9 +386,15 @@ def serving_leg(args, device=0):
                                  "fits_per_hour": 3600.0 * len(jobs) / wall_c,
                                  "evals_per_s": st_c["candidates"] / wall_c, "peak_running": st_c["peak_running"],
                                  "time_to_model_s": ttm},
+        "concurrent_plain_fp64": {"max_active": args.serve_active, "p50_time_to_model_s": st_cp["p50_time_to_model_s"],
+                                  "p99_time_to_model_s": st_cp["p99_time_to_model_s"], "wall_s": wall_cp,
+                                  "fits_per_hour": 3600.0 * len(jobs) / wall_cp,
+                                  "evals_per_s": st_cp["candidates"] / wall_cp},
         "serial_plain_fp64": {"wall_s": wall_s, "sum_run_s": sum(run_s), "fits_per_hour": 3600.0 * len(jobs) / wall_s,
                               "evals_per_s": st_s["candidates"] / wall_s},
-        "models_equal_plain": sum(a[0] == b[0] for a, b in zip(conc, ser)),
+        # a job's model is the same alone and in the mix (plain FP64: bit-identical search)
+        "plain_models_same_alone_and_in_mix": sum(a[0] == b[0] for a, b in zip(concp, ser)),
+        "certified_models_equal_plain": sum(a[0] == b[0] for a, b in zip(conc, ser)),
     }
 
 
@@ -440,7 +460,7 @@ def run_reference(args):
         return
     from oracle import pyoracle
     from rils_rols_gb300.fitness import encode
-    X, y, trees, _ = workload(args.n, args.batch)
+    X, y, trees = workload(args.n)
     threads = os.cpu_count() or 1
     ods = pyoracle.OracleDataset(X, y)
     sample = args.ref_sample
@@ -472,7 +492,6 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=N_ROWS)
-    ap.add_argument("--batch", type=int, default=BATCH)
     ap.add_argument("--cpu-sample", type=int, default=96)
     ap.add_argument("--ref-sample", type=int, default=32)
     ap.add_argument("--unbatched-sample", type=int, default=64)

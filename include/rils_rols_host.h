@@ -42,8 +42,9 @@ void rrh_destroy(rrh_model* m);
 
 /* Install a backend (copied).  NULL restores the device backend. */
 int32_t rrh_set_backend(rrh_model* m, const rrh_backend* be);
-/* RRG_PLAIN_FP64 (default, the drop-in), RRG_MIXED_CERTIFIED (search
- * decisions equal to the FP64 path's) or RRG_MIXED. */
+/* RRG_PLAIN_FP64 (default, the drop-in), RRG_MIXED_CERTIFIED (every fitness
+ * within 1e-6 relative of the FP64 path's: decisions agree except between
+ * candidates whose fitness values lie that close) or RRG_MIXED. */
 int32_t rrh_set_precision(rrh_model* m, int32_t precision);
 
 /* fit(X, y, data_cnt, feat_cnt), X row-major n x d (rils_rols_cpp.cpp:717-728).
