@@ -339,6 +339,8 @@ def run_ours(args):
     res["certified_over_cpu_baseline"] = value / world / res["cpu_baseline"]["value"]
     if args.serve_jobs > 0:
         res["serving"] = serving_leg(args, local)
+    if args.cls_fit_calls > 0:
+        res["classifier"] = classifier_leg(args)
     print(json.dumps(res))
 
 
@@ -396,6 +398,41 @@ def serving_leg(args, device=0):
         "plain_models_same_alone_and_in_mix": sum(a[0] == b[0] for a, b in zip(concp, ser)),
         "certified_models_equal_plain": sum(a[0] == b[0] for a, b in zip(conc, ser)),
     }
+
+
+# ----------------------------------------------------------- classifier ----
+def classifier_leg(args):
+    """Binary classifier fits (d = 30 correlated lognormal features, labels =
+    a random 10-node tree > 0 with 5% flipped; max_complexity 20,
+    sample_size 1): n = 569 on the device in FP64 and certified form and on
+    the host with the oracle as fitness backend (the reference's CPU path);
+    n = 200k on the device, FP64 against certified."""
+    import rils_rols_cpp
+    from rils_rols_gb300 import synth
+    out = {}
+    for n, calls in ((569, 100000), (200_000, args.cls_fit_calls)):
+        X, lab, _ = synth.classifier(n=n, d=30, seed=SEED)
+        row = {"max_fit_calls": calls}
+        arms = [("plain_fp64", "plain", None), ("certified", "mixed", None)]
+        if n <= 5000:
+            from oracle import pyoracle
+            arms.append(("cpu_oracle", "plain", pyoracle.backend_struct()))
+        for name, prec, backend in arms:
+            m = rils_rols_cpp.rils_rols(True, calls, 1 << 30, 0.001, 20, 1.0, False, SEED % 100000)
+            m.set_precision(prec)
+            if backend is not None:
+                m.set_backend(backend)
+            t = time.perf_counter()
+            m.fit(X.reshape(-1), lab, n, X.shape[1])
+            dt = time.perf_counter() - t
+            pred = m.predict(X.reshape(-1), n, X.shape[1])
+            row[name] = {"fit_s": dt, "fit_calls": m.get_fit_calls(), "model": m.get_model_string(),
+                         "train_accuracy": float(np.mean(pred == lab))}
+        if "cpu_oracle" in row:
+            row["device_fp64_equals_cpu"] = row["plain_fp64"]["model"] == row["cpu_oracle"]["model"]
+        row["certified_equals_fp64"] = row["certified"]["model"] == row["plain_fp64"]["model"]
+        out[f"n={n}"] = row
+    return out
 
 
 # kernels behind the timed phases (the roofline candidates)
@@ -500,9 +537,15 @@ def main():
     ap.add_argument("--serve-fit-calls", type=int, default=100000)
     ap.add_argument("--serve-active", type=int, default=8)
     ap.add_argument("--serve-only", action="store_true", help="only the serving leg")
+    ap.add_argument("--cls-fit-calls", type=int, default=20000,
+                    help="max_fit_calls of the 200k-row classifier fits (0: no classifier leg)")
+    ap.add_argument("--cls-only", action="store_true", help="only the classifier leg")
     args = ap.parse_args()
     if args.serve_only:
         print(json.dumps(serving_leg(args)))
+        return
+    if args.cls_only:
+        print(json.dumps(classifier_leg(args)))
         return
     if args.impl == "reference":
         run_reference(args)

@@ -7,19 +7,22 @@
  * Basic operations follow the double-word algorithms analysed by Joldes,
  * Muller and Popescu ("Tight and rigorous error bounds for basic building
  * blocks of double-word arithmetic", ACM TOMS 44(2), 2017): addition
- * (their Algorithm 6), multiplication with FMA (Algorithm 12), division
- * (Algorithm 17 form), the square root by one Karp-Markstein correction of
- * the FP32 root.  Elementary functions are our own: exp by Cody-Waite
- * reduction by ln 2 (three-part split), a Taylor polynomial on r / 16 and
- * four squarings; log by one Newton step on the FP32 logarithm using exp;
- * sin / cos by Cody-Waite reduction by pi / 2 (four-part split, |k| < 4096)
- * and Taylor polynomials on |r| <= pi / 4.  The constants are the Taylor
- * coefficients 1 / k! and splits of ln 2 and pi / 2, each rounded to a
- * double-float.  Relative accuracy is about 1e-13 (absolute for results
- * near zero, and only absolute, about 1e-38, for magnitudes below 1e-31,
- * where the low part leaves FP32's normal range); arguments that the
- * reductions do not cover give NaN, so that a caller treats the value as
- * not computed.
+ * (their Algorithm 6), addition of a float (Algorithm 4), multiplication
+ * with FMA (Algorithm 12), division (Algorithm 17 form), the square root by
+ * one Karp-Markstein correction of the FP32 root.  Elementary functions are
+ * our own, table-driven: exp by reduction by ln 2 / 32 (four-part split,
+ * exact leading products), 2^(j/32) from a table and a short polynomial whose
+ * terms of order 4 and above are summed in FP32; log by m 2^e with
+ * m in [sqrt(1/2), sqrt(2)), c = 1 + j/64 nearest to m, log m = log c +
+ * log1p((m - c) / c) from a table of 1/c and log c and a short series (order
+ * 5 and above in FP32); sin / cos by Cody-Waite reduction by pi / 2
+ * (four-part split, |k| < 4096) and Taylor polynomials on |r| <= pi / 4 whose
+ * high-order tails are summed in FP32.  Table entries and constants are the
+ * double-floats nearest to their values (gen_df32_tables.py).  Relative
+ * accuracy is about 1e-13 (absolute for results near zero, and only
+ * absolute, about 1e-38, for magnitudes below 1e-31, where the low part
+ * leaves FP32's normal range); arguments that the reductions do not cover
+ * give NaN, so that a caller treats the value as not computed.
  *
  * Non-finite results carry lo = 0.  Host builds need -ffp-contract=off.
  */
@@ -152,6 +155,135 @@ DFN dfl dfl_sqrt(dfl x) {
 }
 DFN dfl dfl_scale(dfl x, float p2) { return dfl_make(DF_MUL(x.hi, p2), DF_MUL(x.lo, p2)); }
 
+/* ---- unguarded forms for finite operands (inside the elementary functions) ---- */
+DFN dfl dfl_add_nc(dfl x, dfl y) {
+  const dfl s = dfl_two_sum(x.hi, y.hi);
+  const dfl t = dfl_two_sum(x.lo, y.lo);
+  const float c = DF_ADD(s.lo, t.hi);
+  const dfl v = dfl_fast_two_sum(s.hi, c);
+  const float w = DF_ADD(t.lo, v.lo);
+  return dfl_fast_two_sum(v.hi, w);
+}
+DFN dfl dfl_mul_nc(dfl x, dfl y) {
+  const dfl c = dfl_two_prod(x.hi, y.hi);
+  const float tl0 = DF_MUL(x.lo, y.lo);
+  const float tl1 = DF_FMA(x.hi, y.lo, tl0);
+  const float cl2 = DF_FMA(x.lo, y.hi, tl1);
+  return dfl_fast_two_sum(c.hi, DF_ADD(c.lo, cl2));
+}
+/* x + a for a float a */
+DFN dfl dfl_add_fl(dfl x, float a) {
+  const dfl s = dfl_two_sum(x.hi, a);
+  return dfl_fast_two_sum(s.hi, DF_ADD(x.lo, s.lo));
+}
+/* x * a for a float a */
+DFN dfl dfl_mul_fl(dfl x, float a) {
+  const dfl c = dfl_two_prod(x.hi, a);
+  return dfl_fast_two_sum(c.hi, DF_FMA(x.lo, a, c.lo));
+}
+
+/* ---- tables ---- */
+#define DF_LN2_32_C1 0.02166748046875f
+#define DF_LN2_32_C2 -6.631016731262207e-06f
+#define DF_LN2_32_C3 -5.952044412893542e-11f
+#define DF_LN2_32_C4 -2.7447449183091686e-18f
+#define DFL_EXP2_TAB { \
+  {1.0f, 0.0f}, \
+  {1.0218971967697144f, -4.811559861650494e-08f}, \
+  {1.0442737340927124f, 4.8334701574503924e-08f}, \
+  {1.0671404600143433f, -5.9337519786595294e-08f}, \
+  {1.0905077457427979f, -1.3077539939843064e-08f}, \
+  {1.114386796951294f, -5.435540018083884e-08f}, \
+  {1.1387885808944702f, 5.386222312608879e-08f}, \
+  {1.1637248992919922f, -4.051441493402308e-08f}, \
+  {1.1892070770263672f, 3.797635272917432e-08f}, \
+  {1.215247392654419f, -3.267394887984665e-08f}, \
+  {1.2418577671051025f, 4.496838101886169e-08f}, \
+  {1.2690509557724f, 1.419333317542737e-09f}, \
+  {1.2968395948410034f, -4.018999533172973e-08f}, \
+  {1.3252366781234741f, -3.496373324196611e-08f}, \
+  {1.3542555570602417f, -1.0123349269974824e-08f}, \
+  {1.3839099407196045f, -5.875577357983275e-08f}, \
+  {1.4142135381698608f, 2.4203234971764687e-08f}, \
+  {1.4451807737350464f, 3.324199937537742e-08f}, \
+  {1.4768261909484863f, -4.500898853621038e-08f}, \
+  {1.5091644525527954f, -2.4959373234878512e-08f}, \
+  {1.5422108173370361f, 8.070904833346049e-09f}, \
+  {1.5759809017181396f, -5.661025426206834e-08f}, \
+  {1.610490322113037f, 9.836217174097328e-09f}, \
+  {1.6457555294036865f, -5.124972091152813e-08f}, \
+  {1.6817928552627563f, -2.4755326677450284e-08f}, \
+  {1.7186193466186523f, -4.8496175963919086e-08f}, \
+  {1.7562521696090698f, -9.235770370707996e-09f}, \
+  {1.7947090864181519f, -1.141504490931311e-08f}, \
+  {1.8340080976486206f, -1.1239277952768134e-08f}, \
+  {1.8741676807403564f, -4.663005626071026e-08f}, \
+  {1.9152065515518188f, 9.845328108326612e-09f}, \
+  {1.9571441411972046f, -1.7021804410433106e-08f}, \
+}
+#define DFL_LOG_TAB { \
+  {1.4222222566604614f, -3.443824070359369e-08f, -0.3522205948829651f, 1.2936129945018138e-09f}, \
+  {1.39130437374115f, -2.5915062096260044e-08f, -0.33024168014526367f, -6.725313195232729e-09f}, \
+  {1.3617020845413208f, 4.311825207992115e-08f, -0.3087354898452759f, 8.195662815069227e-09f}, \
+  {1.3333333730697632f, -3.973643103449831e-08f, -0.28768208622932434f, 1.3777543550475002e-08f}, \
+  {1.3061224222183228f, 2.676126875655882e-08f, -0.267062783241272f, -2.0077732809653526e-09f}, \
+  {1.2799999713897705f, 2.8610228852699038e-08f, -0.246860072016716f, -5.914809975138269e-09f}, \
+  {1.2549020051956177f, -4.441130485588474e-08f, -0.22705745697021484f, 6.334868629664925e-09f}, \
+  {1.2307692766189575f, -4.5849727570157484e-08f, -0.20763936638832092f, 1.610076405533789e-09f}, \
+  {1.2075471878051758f, -1.7993855294662353e-08f, -0.18859116733074188f, -2.476808091955718e-09f}, \
+  {1.185185194015503f, -8.830317810293309e-09f, -0.16989903151988983f, -5.275507586333106e-09f}, \
+  {1.163636326789856f, 3.684650806690115e-08f, -0.15154990553855896f, 7.411358193820661e-09f}, \
+  {1.1428571939468384f, -5.108969602929392e-08f, -0.133531391620636f, -1.0038866404826763e-09f}, \
+  {1.1228070259094238f, -8.365564241330503e-09f, -0.11583181470632553f, -8.187961975103519e-10f}, \
+  {1.1034482717514038f, 4.11066514161007e-09f, -0.09844007343053818f, 6.17285667026124e-10f}, \
+  {1.0847457647323608f, -2.020496436827557e-09f, -0.08134564012289047f, 6.689380716018434e-10f}, \
+  {1.0666667222976685f, -5.563100202721216e-08f, -0.06453852355480194f, 2.417230859919073e-09f}, \
+  {1.049180269241333f, 5.862752061602805e-08f, -0.04800922051072121f, 1.3243606211688075e-09f}, \
+  {1.0322580337524414f, 3.076368670917873e-08f, -0.0317486971616745f, -1.1529057708514756e-09f}, \
+  {1.0158730745315552f, -5.865853935915766e-08f, -0.01574835740029812f, 4.3215894751647e-10f}, \
+  {1.0f, 0.0f, 0.0f, 0.0f}, \
+  {0.9846153855323792f, -9.169945358600273e-10f, 0.015504186972975731f, -4.3701048335620385e-10f}, \
+  {0.9696969985961914f, -2.8899222570544225e-08f, 0.030771657824516296f, 8.422373909411363e-10f}, \
+  {0.9552238583564758f, 2.224053829991135e-08f, 0.045809537172317505f, -1.1410232758635175e-09f}, \
+  {0.9411764740943909f, -3.5061555880844253e-09f, 0.0606246218085289f, 7.905942393804377e-12f}, \
+  {0.9275362491607666f, -1.7276708064173363e-08f, 0.0752234235405922f, -2.303004675852094e-09f}, \
+  {0.9142857193946838f, -5.108969691747234e-09f, 0.08961215615272522f, 2.536961973831353e-09f}, \
+  {0.9014084339141846f, 1.6790041357239716e-08f, 0.10379679501056671f, -1.328923193710807e-09f}, \
+  {0.8888888955116272f, -6.622738357719982e-09f, 0.11778303235769272f, 3.2986906539633765e-09f}, \
+  {0.8767123222351074f, 6.532015817128922e-09f, 0.13157635927200317f, -1.4832839401179854e-09f}, \
+  {0.8648648858070374f, -2.0942172440641116e-08f, 0.14518201351165771f, -3.6671599090709606e-09f}, \
+  {0.8533333539962769f, -2.0662943356342112e-08f, 0.15860502421855927f, 5.9580793632108e-09f}, \
+  {0.8421052694320679f, -6.274173180997877e-09f, 0.1718502640724182f, -7.145759095550375e-09f}, \
+  {0.8311688303947449f, 7.740862950633698e-10f, 0.18492233753204346f, 9.619685048534166e-10f}, \
+  {0.8205128312110901f, -1.0698269825581974e-08f, 0.19782574474811554f, -1.4181956720094036e-09f}, \
+  {0.8101266026496887f, -2.037120694353689e-08f, 0.2105647623538971f, 6.753452463925669e-09f}, \
+  {0.800000011920929f, -1.1920929132713809e-08f, 0.2231435477733612f, 3.540848503291727e-09f}, \
+  {0.790123462677002f, -5.886878540195539e-09f, 0.23556606471538544f, 6.597381307926753e-09f}, \
+  {0.7804877758026123f, 2.907543716901273e-08f, 0.2478361576795578f, 6.225023607697722e-09f}, \
+  {0.7710843086242676f, 2.8725130718498804e-08f, 0.25995752215385437f, 2.283071731667974e-09f}, \
+  {0.761904776096344f, -1.419158213167293e-08f, 0.2719337046146393f, 1.086900258684409e-08f}, \
+  {0.7529411911964417f, -1.4725853425545665e-08f, 0.2837681770324707f, -3.9018259734291405e-09f}, \
+  {0.7441860437393188f, 2.772309048992838e-09f, 0.2954642176628113f, -4.768975436775236e-09f}, \
+  {0.7356321811676025f, 2.740443427740047e-09f, 0.3070250451564789f, -9.86156667437399e-09f}, \
+  {0.7272727489471436f, -2.167441692790817e-08f, 0.31845372915267944f, 1.9658552563583953e-09f}, \
+  {0.7191011309623718f, -7.3668662281534125e-09f, 0.3297532796859741f, 6.686494025132106e-09f}, \
+  {0.7111111283302307f, -1.7219120351796846e-08f, 0.3409265875816345f, -6.110413286464222e-10f}, \
+  {0.7032967209815979f, -1.7684895325942307e-08f, 0.3519764244556427f, -1.2984645580971232e-09f}, \
+}
+#if defined(__CUDACC__)
+static __device__ const float dfl_exp2_tab_d[32][2] = DFL_EXP2_TAB;  /* 2^(j/32) */
+static __device__ const float dfl_log_tab_d[47][4] = DFL_LOG_TAB;    /* c = 1 + j/64, j = -19..27: 1/c, log c */
+#endif
+static const float dfl_exp2_tab_h[32][2] = DFL_EXP2_TAB;
+static const float dfl_log_tab_h[47][4] = DFL_LOG_TAB;
+#if defined(__CUDA_ARCH__)
+#define DFL_EXP2(j, i) dfl_exp2_tab_d[j][i]
+#define DFL_LOGT(j, i) dfl_log_tab_d[j][i]
+#else
+#define DFL_EXP2(j, i) dfl_exp2_tab_h[j][i]
+#define DFL_LOGT(j, i) dfl_log_tab_h[j][i]
+#endif
+
 /* ---- comparisons (the semantics of the FP64 comparisons on hi + lo) ---- */
 DFN int dfl_lt(dfl a, dfl b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
 DFN int dfl_eq(dfl a, dfl b) { return a.hi == b.hi && a.lo == b.lo; }
@@ -161,29 +293,28 @@ DFN dfl dfl_exp(dfl x) {
   if (x.hi != x.hi) return dfl_make(dfl_nanf(), 0.0f);
   if (x.hi > 88.72f) return dfl_make(dfl_inff(), 0.0f);
   if (x.hi < -103.5f) return dfl_make(0.0f, 0.0f);
-  const float k = rintf(DF_MUL(x.hi, 1.4426950216293335f));
-  /* ln 2 = L1 + L2 + L3 (+ 9e-17): L1, L2 of 12 bits, k * L1 and k * L2 exact */
-  dfl r = dfl_sub(x, dfl_make(DF_MUL(k, 0.693115234375f), 0.0f));
-  r = dfl_sub(r, dfl_make(DF_MUL(k, 3.1948089599609375e-05f), 0.0f));
-  r = dfl_sub(r, dfl_two_prod(k, -1.9046542121259336e-09f)); /* k * L3 */
-  r = dfl_scale(r, 0.0625f);
-  /* expm1(r) = r (1 + r (1/2 + r (1/6 + ... + r / 7!))) on |r| <= 0.022 */
-  dfl p = dfl_make(0.00019841270113829523f, -2.725596874933456e-12f);
-  p = dfl_add(dfl_mul(p, r), dfl_make(0.0013888889225199819f, -3.3631094437103215e-11f));
-  p = dfl_add(dfl_mul(p, r), dfl_make(0.008333333767950535f, -4.34617203337595e-10f));
-  p = dfl_add(dfl_mul(p, r), dfl_make(0.0416666679084301f, -1.2417634698280722e-09f));
-  p = dfl_add(dfl_mul(p, r), dfl_make(0.1666666716337204f, -4.967053879312289e-09f));
-  p = dfl_add(dfl_mul(p, r), dfl_make(0.5f, 0.0f));
-  p = dfl_add(dfl_mul(p, r), dfl_make(1.0f, 0.0f));
-  dfl em = dfl_mul(p, r);
-  /* (1 + em)^2 - 1 = em (em + 2), four times */
-  for (int i = 0; i < 4; ++i) em = dfl_mul(em, dfl_add(em, dfl_make(2.0f, 0.0f)));
-  dfl e = dfl_add(em, dfl_make(1.0f, 0.0f));
-  /* times 2^k in two exact steps (k in [-150, 128]) */
-  const int ki = (int)k;
-  const int k1 = ki / 2, k2 = ki - k1;
-  e = dfl_scale(e, dfl_pow2(k1));
-  e = dfl_scale(e, dfl_pow2(k2));
+  const float kf = rintf(DF_MUL(x.hi, 46.16624130844683f)); /* 32 / ln 2; |k| < 2^13 */
+  /* r = x - k ln2/32, |r| <= ln2/64 (k C1 and k C2 exact: 11-bit constants) */
+  dfl r = dfl_add_fl(x, -DF_MUL(kf, DF_LN2_32_C1));
+  r = dfl_add_fl(r, -DF_MUL(kf, DF_LN2_32_C2));
+  r = dfl_add_nc(r, dfl_two_prod(-kf, DF_LN2_32_C3));
+  r = dfl_add_fl(r, -DF_MUL(kf, DF_LN2_32_C4));
+  /* expm1(r) = r + r^2 (1/2 + r/6) + r^4 (1/24 + r/120 + r^2/720), the last term in FP32 (< 6e-10) */
+  const float rf = r.hi, r2f = DF_MUL(rf, rf);
+  const float tail = DF_MUL(DF_MUL(r2f, r2f),
+                            DF_FMA(DF_FMA(rf, 1.3888889225e-3f, 8.333333768e-3f), rf, 4.166666791e-2f));
+  const dfl q = dfl_add_fl(dfl_mul_nc(r, dfl_make(0.1666666716337204f, -4.967053879312289e-09f)), 0.5f);
+  dfl em = dfl_add_nc(r, dfl_mul_nc(dfl_mul_nc(r, r), q));
+  em = dfl_add_fl(em, tail);
+  /* 2^(j/32) (1 + em) 2^m, k = 32 m + j */
+  const int k = (int)kf;
+  const int jj = k & 31, m = (k - jj) / 32;
+  const dfl t = dfl_make(DFL_EXP2(jj, 0), DFL_EXP2(jj, 1));
+  dfl e = dfl_add_nc(t, dfl_mul_nc(t, em));
+  /* times 2^m in two exact steps (m in [-150, 128]) */
+  const int m1 = m / 2, m2 = m - m1;
+  e = dfl_scale(e, dfl_pow2(m1));
+  e = dfl_scale(e, dfl_pow2(m2));
   if (!dfl_finite(e.hi)) e.lo = 0.0f;
   return e;
 }
@@ -217,12 +348,23 @@ DFN dfl dfl_log(dfl x) {
   }
   int e;
   const dfl m = dfl_split_exp(x, &e);
-  const float y0 = logf(m.hi);
-  /* log(m) = y0 + m exp(-y0) - 1, one Newton step */
-  const dfl t = dfl_mul(m, dfl_exp(dfl_make(-y0, 0.0f)));
-  const dfl lm = dfl_add(dfl_make(y0, 0.0f), dfl_add(t, dfl_make(-1.0f, 0.0f)));
+  /* c = 1 + j/64 nearest to m (j in [-19, 27]); t = (m - c) / c, |t| <= 0.011 */
+  const float jf = rintf(DF_MUL(DF_SUB(m.hi, 1.0f), 64.0f));
+  const int J = (int)jf + 19;
+  const dfl d = dfl_add_fl(m, -DF_FMA(jf, 0.015625f, 1.0f));
+  const dfl t = dfl_mul_nc(d, dfl_make(DFL_LOGT(J, 0), DFL_LOGT(J, 1)));
+  /* log1p(t) = t (1 - t (1/2 - t (1/3 - t/4))) + t^5 (1/5 - t/6 + t^2/7 - t^3/8), the last term in FP32 */
+  const float tf = t.hi, t2f = DF_MUL(tf, tf);
+  const float tail = DF_MUL(DF_MUL(t2f, DF_MUL(t2f, tf)),
+                            DF_FMA(DF_FMA(DF_FMA(tf, -0.125f, 0.1428571492433548f), tf, -0.1666666716337204f), tf,
+                                   0.2f));
+  dfl p = dfl_add_nc(dfl_make(0.3333333432674408f, -9.934107758624577e-09f), dfl_scale(t, -0.25f));
+  p = dfl_add_fl(dfl_neg(dfl_mul_nc(p, t)), 0.5f);
+  p = dfl_add_fl(dfl_neg(dfl_mul_nc(p, t)), 1.0f);
+  p = dfl_add_fl(dfl_mul_nc(p, t), tail);
+  const dfl lm = dfl_add_nc(dfl_make(DFL_LOGT(J, 2), DFL_LOGT(J, 3)), p);
   /* + (e - shift) ln 2 */
-  return dfl_add(lm, dfl_mul_f(dfl_make(0.6931471824645996f, -1.9046542121259336e-09f), (float)(e - shift)));
+  return dfl_add_nc(lm, dfl_mul_fl(dfl_make(0.6931471824645996f, -1.9046542121259336e-09f), (float)(e - shift)));
 }
 
 /* ---- sin / cos ---- */
@@ -231,39 +373,41 @@ DFN dfl dfl_log(dfl x) {
 DFN int dfl_reduce_half_pi(dfl x, dfl* r) {
   const float k = rintf(DF_MUL(x.hi, 0.6366197466850281f));
   if (!(fabsf(k) < 4096.0f)) return -1;
-  dfl t = dfl_sub(x, dfl_make(DF_MUL(k, 1.57080078125f), 0.0f));
-  t = dfl_sub(t, dfl_make(DF_MUL(k, -4.453584551811218e-06f), 0.0f));
-  t = dfl_sub(t, dfl_two_prod(k, -8.705515752716053e-10f));
-  t = dfl_sub(t, dfl_two_prod(k, 5.721188916458728e-18f));
+  dfl t = dfl_add_fl(x, -DF_MUL(k, 1.57080078125f));
+  t = dfl_add_fl(t, -DF_MUL(k, -4.453584551811218e-06f));
+  t = dfl_add_nc(t, dfl_two_prod(-k, -8.705515752716053e-10f));
+  t = dfl_add_nc(t, dfl_two_prod(-k, 5.721188916458728e-18f));
   *r = t;
   const int ki = (int)k;
   return ki & 3;
 }
+/* sin r = r (1 - z/3! + z^2/5! - z^3/7! + z^4/9! - z^5 T(z)), z = r^2 <= 0.617,
+ * T = 1/11! - z/13! + z^2/15! - z^3/17! in FP32 (the term is below 3e-9) */
 DFN dfl dfl_sin_kernel(dfl r) {
-  const dfl z = dfl_mul(r, r);
-  dfl p = dfl_make(2.8114573589663704e-15f, -1.0462084739763658e-22f);         /* 1/17! */
-  p = dfl_sub(dfl_make(7.647163609812713e-13f, 1.2200710471178288e-20f), dfl_mul(p, z));   /* 1/15! */
-  p = dfl_sub(dfl_make(1.6059044372074283e-10f, -5.352526511562726e-18f), dfl_mul(p, z));  /* 1/13! */
-  p = dfl_sub(dfl_make(2.5052107943679403e-08f, 4.4176230446483665e-16f), dfl_mul(p, z));  /* 1/11! */
-  p = dfl_sub(dfl_make(2.7557318844628753e-06f, 3.793571224297229e-14f), dfl_mul(p, z));   /* 1/9! */
-  p = dfl_sub(dfl_make(0.00019841270113829523f, -2.725596874933456e-12f), dfl_mul(p, z));  /* 1/7! */
-  p = dfl_sub(dfl_make(0.008333333767950535f, -4.34617203337595e-10f), dfl_mul(p, z));     /* 1/5! */
-  p = dfl_sub(dfl_make(0.1666666716337204f, -4.967053879312289e-09f), dfl_mul(p, z));      /* 1/3! */
-  p = dfl_sub(dfl_make(1.0f, 0.0f), dfl_mul(p, z));
-  return dfl_mul(p, r);
+  const dfl z = dfl_mul_nc(r, r);
+  const float zf = z.hi;
+  const float tz = DF_FMA(DF_FMA(DF_FMA(zf, -2.8114573589663704e-15f, 7.647163609812713e-13f), zf,
+                                 -1.6059044372074283e-10f), zf, 2.5052107943679403e-08f);
+  dfl p = dfl_add_nc(dfl_make(2.7557318844628753e-06f, 3.793571224297229e-14f), dfl_neg(dfl_mul_fl(z, tz)));
+  p = dfl_add_nc(dfl_make(0.00019841270113829523f, -2.725596874933456e-12f), dfl_neg(dfl_mul_nc(p, z)));
+  p = dfl_add_nc(dfl_make(0.008333333767950535f, -4.34617203337595e-10f), dfl_neg(dfl_mul_nc(p, z)));
+  p = dfl_add_nc(dfl_make(0.1666666716337204f, -4.967053879312289e-09f), dfl_neg(dfl_mul_nc(p, z)));
+  p = dfl_add_fl(dfl_neg(dfl_mul_nc(p, z)), 1.0f);
+  return dfl_mul_nc(p, r);
 }
+/* cos r = 1 - z/2 + z^2/4! - z^3/6! + z^4/8! - z^5 U(z),
+ * U = 1/10! - z/12! + z^2/14! - z^3/16! + z^4/18! in FP32 (the term is below 3e-8) */
 DFN dfl dfl_cos_kernel(dfl r) {
-  const dfl z = dfl_mul(r, r);
-  dfl p = dfl_make(1.5619206814541513e-16f, 1.5404471465941993e-24f);          /* 1/18! */
-  p = dfl_sub(dfl_make(4.7794772561329454e-14f, 7.62544404448643e-22f), dfl_mul(p, z));    /* 1/16! */
-  p = dfl_sub(dfl_make(1.147074536050896e-11f, 2.372207689231238e-19f), dfl_mul(p, z));    /* 1/14! */
-  p = dfl_sub(dfl_make(2.0876755879584152e-09f, 1.1082839147459852e-16f), dfl_mul(p, z));  /* 1/12! */
-  p = dfl_sub(dfl_make(2.755731998149713e-07f, -7.575112209051195e-15f), dfl_mul(p, z));   /* 1/10! */
-  p = dfl_sub(dfl_make(2.4801587642286904e-05f, -3.40699609366682e-13f), dfl_mul(p, z));   /* 1/8! */
-  p = dfl_sub(dfl_make(0.0013888889225199819f, -3.3631094437103215e-11f), dfl_mul(p, z));  /* 1/6! */
-  p = dfl_sub(dfl_make(0.0416666679084301f, -1.2417634698280722e-09f), dfl_mul(p, z));     /* 1/4! */
-  p = dfl_sub(dfl_make(0.5f, 0.0f), dfl_mul(p, z));                                         /* 1/2! */
-  return dfl_sub(dfl_make(1.0f, 0.0f), dfl_mul(p, z));
+  const dfl z = dfl_mul_nc(r, r);
+  const float zf = z.hi;
+  const float uz = DF_FMA(DF_FMA(DF_FMA(DF_FMA(zf, 1.5619206814541513e-16f, -4.7794772561329454e-14f), zf,
+                                        1.147074536050896e-11f), zf, -2.0876755879584152e-09f), zf,
+                          2.755731998149713e-07f);
+  dfl p = dfl_add_nc(dfl_make(2.4801587642286904e-05f, -3.40699609366682e-13f), dfl_neg(dfl_mul_fl(z, uz)));
+  p = dfl_add_nc(dfl_make(0.0013888889225199819f, -3.3631094437103215e-11f), dfl_neg(dfl_mul_nc(p, z)));
+  p = dfl_add_nc(dfl_make(0.0416666679084301f, -1.2417634698280722e-09f), dfl_neg(dfl_mul_nc(p, z)));
+  p = dfl_add_fl(dfl_neg(dfl_mul_nc(p, z)), 0.5f);
+  return dfl_add_fl(dfl_neg(dfl_mul_nc(p, z)), 1.0f);
 }
 DFN dfl dfl_sin(dfl x) {
   if (!dfl_finite(x.hi)) return dfl_make(dfl_nanf(), 0.0f);

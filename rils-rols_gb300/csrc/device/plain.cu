@@ -1147,8 +1147,149 @@ __global__ void sentinel_classify_kernel(DevBatch b, const int32_t* list, int ca
       inf_norm = true;
     }
   }
-  if (!tails || !(nan0 || inf_norm)) return;
-  double* out = coefs + cd.coef_offset;
+  if (!tails) return;
+  if (nan0 || inf_norm) {
+    double* out = coefs + cd.coef_offset;
+    for (int j = 0; j < k; ++j) out[j] = __longlong_as_double(0x7ff8000000000000ll);
+    res[c].rank = k;
+    pc[c].pad = 1;
+    atomicAdd(decided, 1u);
+    return;
+  }
+  // a NaN column further right: left to nan_gram_* (bit 1), which decides it
+  // when the finite columns are well conditioned
+  int nf = 0;
+  bool any_nan = false;
+  for (int j = 0; j < m; ++j) {
+    if (cs[colmap[pc[c].a_col + j]].flags & kCsNaN) any_nan = true;
+    else ++nf;
+  }
+  if (any_nan && nf + 1 <= kGramCols) pc[c].pad = 2;
+}
+
+// A NaN column at position q >= 1, column 0 finite, no infinite norm, every
+// tail non-trivial: step 0 pivots on a finite column (NaN norms never win the
+// '>' scan unless they head the remaining columns) with tau != 0, which turns
+// every NaN-holding column entirely NaN; NaN columns do not move before step
+// q, where the first of them heads the remaining columns and is chosen; its
+// tau is NaN and every later norm and coefficient NaN, so the result is
+// all-NaN coefficients at full rank, unless some step before q cut the rank.
+// Steps before q factor finite columns only, so no cut is possible when the
+// finite columns (the free term included) are well conditioned: every pivot
+// of their pivoted Cholesky above 1e-8 of its column's squared norm and
+// 1e-24 of the largest (the reference cuts at eps^2 ~ 5e-32 of the largest,
+// and a remaining norm that far above it cannot be rounded down to it).
+// nan_gram_kernel forms their FP64 Gram matrix (a certificate: any summation
+// order), nan_gram_decide_kernel factors it.
+constexpr int kGramE = kGramCols * (kGramCols + 1) / 2;
+
+__device__ __forceinline__ int gram_finite_cols(const PlainCand& p, const int32_t* colmap, const ColStat* cs,
+                                                const double* T, int64_t n_pad, const double* (&colp)[kGramCols]) {
+  const int m = p.k - 1;
+  int nf = 0;
+  for (int j = 0; j < m && nf < kGramCols - 1; ++j) {
+    const int32_t t = colmap[p.a_col + j];
+    if (!(cs[t].flags & kCsNaN)) colp[nf++] = T + (int64_t)t * n_pad;
+  }
+  return nf;
+}
+
+__global__ void __launch_bounds__(256) nan_gram_kernel(const int32_t* list, int cnt, const PlainCand* pc,
+                                                       const int32_t* colmap, const ColStat* cs, const double* T,
+                                                       int64_t n, int64_t n_pad, double* gpart) {
+  __shared__ double red[8][kGramE];
+  const int i = blockIdx.y;
+  if (i >= cnt) return;
+  const int c = list[i];
+  const PlainCand p = pc[c];
+  if (!(p.pad & 2)) return;
+  const double* colp[kGramCols];
+  const int nf = gram_finite_cols(p, colmap, cs, T, n_pad, colp);
+  const int K = nf + 1;  // the free term last
+  double part[kGramE];
+#pragma unroll
+  for (int e = 0; e < kGramE; ++e) part[e] = 0.0;
+  const int64_t r0 = n * (int64_t)blockIdx.x / gridDim.x, r1 = n * (int64_t)(blockIdx.x + 1) / gridDim.x;
+  for (int64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
+    double v[kGramCols];
+#pragma unroll
+    for (int a = 0; a < kGramCols; ++a) v[a] = a < nf ? colp[a][r] : 1.0;
+    int e = 0;
+#pragma unroll
+    for (int a = 0; a < kGramCols; ++a)
+#pragma unroll
+      for (int bb = a; bb < kGramCols; ++bb, ++e)
+        if (bb < K) part[e] = fma(v[a], v[bb], part[e]);
+  }
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+#pragma unroll
+  for (int e = 0; e < kGramE; ++e) {
+    const double t = warp_sum(part[e]);
+    if (l == 0) red[w][e] = t;
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < kGramE; e += blockDim.x) {
+    double t = 0.0;
+    for (int ww = 0; ww < 8; ++ww) t += red[ww][e];
+    gpart[((int64_t)i * gridDim.x + blockIdx.x) * kGramE + e] = t;
+  }
+}
+
+__global__ void nan_gram_decide_kernel(DevBatch b, const int32_t* list, int cnt, PlainCand* pc, const int32_t* colmap,
+                                       const ColStat* cs, int nbx, const double* gpart, double* coefs,
+                                       rrg_result* res, uint32_t* decided) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= cnt) return;
+  const int c = list[i];
+  if (!(pc[c].pad & 2)) return;
+  const int k = pc[c].k, m = k - 1;
+  int nf = 0;
+  for (int j = 0; j < m; ++j) nf += (cs[colmap[pc[c].a_col + j]].flags & kCsNaN) ? 0 : 1;
+  const int K = nf + 1;
+  double G[kGramCols][kGramCols];
+  for (int a = 0, e = 0; a < kGramCols; ++a)
+    for (int bb = a; bb < kGramCols; ++bb, ++e) {
+      double t = 0.0;
+      if (bb < K)
+        for (int x = 0; x < nbx; ++x) t += gpart[((int64_t)i * nbx + x) * kGramE + e];
+      G[a][bb] = t;
+      G[bb][a] = t;
+    }
+  double d0[kGramCols], maxd = 0.0;
+  for (int a = 0; a < K; ++a) {
+    d0[a] = G[a][a];
+    maxd = fmax(maxd, G[a][a]);
+  }
+  int piv[kGramCols];
+  for (int a = 0; a < K; ++a) piv[a] = a;
+  bool ok = maxd > 0.0 && maxd < 1e300;
+  for (int s2 = 0; s2 < K && ok; ++s2) {
+    int q = s2;
+    for (int j = s2 + 1; j < K; ++j)
+      if (G[j][j] > G[q][q]) q = j;
+    const double dp = G[q][q];
+    if (!(dp > 1e-8 * d0[piv[q]]) || !(dp > 1e-24 * maxd)) {
+      ok = false;
+      break;
+    }
+    if (q != s2) {
+      for (int j = 0; j < K; ++j) { const double t = G[s2][j]; G[s2][j] = G[q][j]; G[q][j] = t; }
+      for (int j = 0; j < K; ++j) { const double t = G[j][s2]; G[j][s2] = G[j][q]; G[j][q] = t; }
+      const int t = piv[s2]; piv[s2] = piv[q]; piv[q] = t;
+    }
+    const double l = sqrt(dp);
+    for (int a = s2 + 1; a < K; ++a) G[a][s2] /= l;
+    for (int a = s2 + 1; a < K; ++a)
+      for (int bb = s2 + 1; bb <= a; ++bb) {
+        G[a][bb] -= G[a][s2] * G[bb][s2];
+        G[bb][a] = G[a][bb];
+      }
+  }
+  if (!ok) {
+    pc[c].pad = 0;
+    return;
+  }
+  double* out = coefs + b.cands[c].coef_offset;
   for (int j = 0; j < k; ++j) out[j] = __longlong_as_double(0x7ff8000000000000ll);
   res[c].rank = k;
   pc[c].pad = 1;

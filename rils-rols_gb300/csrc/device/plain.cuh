@@ -53,6 +53,18 @@ __global__ void colstat_kernel(const double* T, int64_t n, int64_t n_pad, ColSta
 // be all-NaN coefficients at full rank (the fitness sentinel), writes that
 // result, sets pc[c].pad = 1 (the QR and residual kernels skip it) and
 // counts it in *decided.
+// Finite columns (the free term included) of the Gram certificate for a NaN
+// column beyond column 0; wider candidates are left to the QR.
+constexpr int kGramCols = 9;
+// grid (row blocks, listed candidates): per-block FP64 Gram sums of the finite
+// columns of the candidates sentinel_classify_kernel marked (pad bit 1)
+__global__ void nan_gram_kernel(const int32_t* list, int cnt, const PlainCand* pc, const int32_t* colmap,
+                                const ColStat* cs, const double* T, int64_t n, int64_t n_pad, double* gpart);
+// one thread per listed candidate: a well-conditioned Gram decides the
+// all-NaN outcome (written, pad = 1); otherwise pad = 0 and the QR runs
+__global__ void nan_gram_decide_kernel(DevBatch b, const int32_t* list, int cnt, PlainCand* pc, const int32_t* colmap,
+                                       const ColStat* cs, int nbx, const double* gpart, double* coefs,
+                                       rrg_result* res, uint32_t* decided);
 __global__ void sentinel_classify_kernel(DevBatch b, const int32_t* list, int cand0, int cnt, PlainCand* pc,
                                          const int32_t* colmap, const ColStat* cs, int64_t rows, double* coefs,
                                          rrg_result* res, uint32_t* decided);

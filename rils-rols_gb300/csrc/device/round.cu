@@ -939,6 +939,26 @@ rrg_status rrg_context::run_fp64_table(const rrg_dataset* ds, const std::vector<
     sentinel_classify_kernel<<<(ng + 127) / 128, 128, 0, stream>>>(dev, d_list, 0, ng,
                                                                    pk.at<PlainCand>(d_ft64, o_pcs), d_cmap, cst,
                                                                    ds->n, coefs, res, status + kStatusSentinel);
+    {
+      // NaN columns beyond column 0: the Gram certificate of the finite columns
+      const int nbx = (int)std::max<int64_t>(1, std::min<int64_t>(16, (ds->n + 32767) / 32768));
+      const size_t gbytes = sizeof(double) * (size_t)ng * nbx * (kGramCols * (kGramCols + 1) / 2);
+      if (!d_gram.reserve(gbytes)) {
+        rrc::set_error("FP64 round: scratch allocation failed");
+        return RRG_E_OOM;
+      }
+      double* gpart = static_cast<double*>(d_gram.ptr);
+      for (int32_t g0 = 0; g0 < ng; g0 += 65535) {
+        const int32_t gn = std::min<int32_t>(65535, ng - g0);
+        nan_gram_kernel<<<dim3(nbx, gn), 256, 0, stream>>>(d_list + g0, gn, d_pcs, d_cmap, cst, F64, ds->n,
+                                                           ds->n_pad, gpart + (size_t)g0 * nbx *
+                                                                                  (kGramCols * (kGramCols + 1) / 2));
+      }
+      nan_gram_decide_kernel<<<(ng + 127) / 128, 128, 0, stream>>>(dev, d_list, ng, pk.at<PlainCand>(d_ft64, o_pcs),
+                                                                   d_cmap, cst, nbx, gpart, coefs, res,
+                                                                   status + kStatusSentinel);
+      launches += 2;
+    }
     mark_end(P_PLAIN_EVAL, t0);
     phase_bytes[P_PLAIN_EVAL] += (double)ds->n * 8.0 * (double)(ds->d + ncol);
     launches += 2;
