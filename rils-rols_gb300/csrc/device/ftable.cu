@@ -200,12 +200,22 @@ __global__ void __launch_bounds__(kFacThreads) fac_eval_kernel(FacEvalArgs a, in
       *reinterpret_cast<float4*>(a.F + (int64_t)f * n_pad + gr) = make_float4(v0.hi, v0.lo, v1.hi, v1.lo);
       const float2 yhv = *reinterpret_cast<const float2*>(yh + r);
       const float2 ylv = *reinterpret_cast<const float2*>(yl + r);
-      ff = dfl_add(ff, dfl_mul(v0, v0));
-      ff = dfl_add(ff, dfl_mul(v1, v1));
-      fs = dfl_add(fs, v0);
-      fs = dfl_add(fs, v1);
-      fy = dfl_add(fy, dfl_mul(v0, dfl_make(yhv.x, ylv.x)));
-      fy = dfl_add(fy, dfl_mul(v1, dfl_make(yhv.y, ylv.y)));
+      const dfl y0 = dfl_make(yhv.x, ylv.x), y1 = dfl_make(yhv.y, ylv.y);
+      if (__all_sync(0xffffffffu, dfl_finite(v0.hi) && dfl_finite(v1.hi) && dfl_finite(ff.hi) &&
+                                      dfl_finite(fs.hi) && dfl_finite(fy.hi))) {
+        // finite values (the common case): the two rows' terms are added first,
+        // without the non-finite guards
+        ff = dfl_add_nc(ff, dfl_add_nc(dfl_mul_nc(v0, v0), dfl_mul_nc(v1, v1)));
+        fs = dfl_add_nc(fs, dfl_add_nc(v0, v1));
+        fy = dfl_add_nc(fy, dfl_add_nc(dfl_mul_nc(v0, y0), dfl_mul_nc(v1, y1)));
+      } else {
+        ff = dfl_add(ff, dfl_mul(v0, v0));
+        ff = dfl_add(ff, dfl_mul(v1, v1));
+        fs = dfl_add(fs, v0);
+        fs = dfl_add(fs, v1);
+        fy = dfl_add(fy, dfl_mul(v0, y0));
+        fy = dfl_add(fy, dfl_mul(v1, y1));
+      }
     }
     if (!ok) atomicOr(a.status, ST_STACK);
 #pragma unroll
