@@ -12,7 +12,8 @@ src="$ref/rils_rols_cpp"
 [ -f "$src/rils_rols_cpp.cpp" ] || { echo "reference sources not found under $src" >&2; exit 3; }
 mkdir -p "$here/_ref"
 pyinc="$(python3 -c 'import pybind11,sysconfig;print("-I"+pybind11.get_include()+" -I"+sysconfig.get_paths()["include"])')"
-# -ffp-contract=off: no FMA contraction, so x86 and Arm builds round alike.
+# -ffp-contract=off: no implicit FMA contraction (the explicit fma() calls of the
+# fixed-order sums stay), so x86 and Arm builds round alike.
 g++ -std=c++17 -O2 -ffp-contract=off -fPIC -shared -w \
     -include "$here/eigen_shim/rr_module_guards.h" -I "$here/eigen_shim" -I "$src" $pyinc \
     "$here/ref_harness.cpp" "$src/node.cpp" -o "$here/_ref/librr_ref.so"

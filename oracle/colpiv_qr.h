@@ -19,7 +19,10 @@
  *
  * Reduction order (the one thing the vendored, incomplete Eigen cannot pin):
  * every sum, dot product and norm here follows the fixed RR256 order of
- * rils-rols_gb300/csrc/common/rr_sum.h (the order of a 256-thread block).
+ * rils-rols_gb300/csrc/common/rr_sum.h (the order of a 256-thread block);
+ * products are accumulated, and the rank-1 updates applied, with fused
+ * multiply-adds, as Eigen's vectorised kernels do in the reference's
+ * -O3 -march=native build on FMA hardware.
  * The Eigen-subset shim that compiles the reference sources uses this same
  * header, so the oracle and the compiled reference agree bit for bit.
  *
@@ -116,7 +119,7 @@ static inline long rrq_lstsq(double* A, long lda, long rows, long cols,
                     double tmp = rr_dot256(col, cj, k + 1, rows);
                     tmp += cj[k];
                     cj[k] -= tau * tmp;
-                    for (i = k + 1; i < rows; ++i) cj[i] -= (tau * col[i]) * tmp;
+                    for (i = k + 1; i < rows; ++i) cj[i] = fma(-(tau * col[i]), tmp, cj[i]);
                 }
             }
         }
@@ -154,7 +157,7 @@ static inline long rrq_lstsq(double* A, long lda, long rows, long cols,
             double tmp = rr_dot256(v, c, k + 1, rows);
             tmp += c[k];
             c[k] -= tau * tmp;
-            for (i = k + 1; i < rows; ++i) c[i] -= (tau * v[i]) * tmp;
+            for (i = k + 1; i < rows; ++i) c[i] = fma(-(tau * v[i]), tmp, c[i]);
         }
     }
     /* back substitution with R[0:r, 0:r], column sweep */

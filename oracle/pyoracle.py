@@ -17,7 +17,9 @@ CFLAGS = ["-std=c99", "-O2", "-ffp-contract=off", "-fPIC", "-shared"]
 
 
 def build(force: bool = False) -> Path:
-    srcs = [SRC, HERE / "colpiv_qr.h", HERE.parent / "include" / "rils_rols_gb300.h"]
+    common = HERE.parent / "rils-rols_gb300" / "csrc" / "common"
+    srcs = [SRC, HERE / "colpiv_qr.h", HERE.parent / "include" / "rils_rols_gb300.h", common / "rr_sum.h",
+            common / "rr_math.h"]
     if not force and LIB.exists() and LIB.stat().st_mtime >= max(p.stat().st_mtime for p in srcs):
         return LIB
     LIB.parent.mkdir(parents=True, exist_ok=True)

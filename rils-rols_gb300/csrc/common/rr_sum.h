@@ -10,10 +10,14 @@
  * CSUM: a whole column of n rows is summed as consecutive chunks of
  * RR_CHUNK rows, each by RR256, the chunk totals added in order from 0.
  * Every sum, mean, dot product and norm of the plain FP64 path uses one of
- * these (host code must be built with -ffp-contract=off).
+ * these (host code must be built with -ffp-contract=off).  Dot products and
+ * sums of squares accumulate each product with a fused multiply-add, as the
+ * reference's Eigen kernels do in its -O3 -march=native build on FMA hardware.
  */
 #ifndef RR_SUM_H
 #define RR_SUM_H
+
+#include <math.h>
 
 #define RR_LANES 256
 #define RR_CHUNK 16384
@@ -37,13 +41,19 @@ static inline double rr_sum256(const double* x, long start, long end) {
 
 static inline double rr_sumsq256(const double* x, long start, long end) {
   double p[RR_LANES] = {0};
-  for (long i = start; i < end; ++i) p[(i - start) & (RR_LANES - 1)] += x[i] * x[i];
+  for (long i = start; i < end; ++i) {
+    double* q = &p[(i - start) & (RR_LANES - 1)];
+    *q = fma(x[i], x[i], *q);
+  }
   return rrs_fold(p);
 }
 
 static inline double rr_dot256(const double* a, const double* b, long start, long end) {
   double p[RR_LANES] = {0};
-  for (long i = start; i < end; ++i) p[(i - start) & (RR_LANES - 1)] += a[i] * b[i];
+  for (long i = start; i < end; ++i) {
+    double* q = &p[(i - start) & (RR_LANES - 1)];
+    *q = fma(a[i], b[i], *q);
+  }
   return rrs_fold(p);
 }
 

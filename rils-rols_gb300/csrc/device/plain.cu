@@ -282,7 +282,7 @@ __device__ __forceinline__ double div_by(double a, double b, double y) {
 // Returns tau; writes beta to col[kk] and the essential part below it.
 __device__ double make_householder_col(double* col, int64_t rows, int kk, double* red) {
   double part = 0.0;
-  for (int64_t i = kk + 1 + threadIdx.x; i < rows; i += blockDim.x) part = __dadd_rn(part, __dmul_rn(col[i], col[i]));
+  for (int64_t i = kk + 1 + threadIdx.x; i < rows; i += blockDim.x) part = __fma_rn(col[i], col[i], part);
   const double tail_sq = (rows - kk == 1) ? 0.0 : block_sum(part, red);
   const double c0 = col[kk];
   double tau, beta;
@@ -333,7 +333,7 @@ __device__ void apply_householder_cols(double* const* colp, int64_t rows, int kk
     const double vi = v[i];
 #pragma unroll
     for (int j = 0; j < KB; ++j)
-      if (j < cnt) part[j] = __dadd_rn(part[j], __dmul_rn(vi, cp[j][i]));
+      if (j < cnt) part[j] = __fma_rn(vi, cp[j][i], part[j]);
   }
   block_sum_vec_t<KB>(part, cnt, red, sh_tmp);
   // tmp_j += Q[kk, j]; Q[kk, j] -= tau * tmp_j
@@ -352,7 +352,7 @@ __device__ void apply_householder_cols(double* const* colp, int64_t rows, int kk
     const double tv = __dmul_rn(tau, v[i]);
 #pragma unroll
     for (int j = 0; j < KB; ++j)
-      if (j < cnt) cp[j][i] = __dsub_rn(cp[j][i], __dmul_rn(tv, t[j]));
+      if (j < cnt) cp[j][i] = __fma_rn(-tv, t[j], cp[j][i]);
   }
   __syncthreads();
 }
@@ -402,7 +402,7 @@ __global__ void __launch_bounds__(256) plain_qr_kernel_t(DevBatch b, DevData ds,
       for (int j = 0; j < KB; ++j)
         if (j < k) {
           const double q = colp[j][i];
-          part[j] = __dadd_rn(part[j], __dmul_rn(q, q));
+          part[j] = __fma_rn(q, q, part[j]);
         }
     }
   } else {
@@ -422,7 +422,7 @@ __global__ void __launch_bounds__(256) plain_qr_kernel_t(DevBatch b, DevData ds,
         for (int64_t r = threadIdx.x; r < rows; r += blockDim.x) {
           const double v = src[r];
           dst[r] = v;
-          acc = __dadd_rn(acc, __dmul_rn(v, v));
+          acc = __fma_rn(v, v, acc);
         }
         part[j] = acc;
       } else if (j == k - 1) {
@@ -502,7 +502,7 @@ __global__ void __launch_bounds__(256) plain_qr_kernel_t(DevBatch b, DevData ds,
       double p1 = 0.0;
       for (int64_t i = kk + 1 + threadIdx.x; i < rows; i += blockDim.x) {
         const double q = cj[i];
-        p1 = __dadd_rn(p1, __dmul_rn(q, q));
+        p1 = __fma_rn(q, q, p1);
       }
       const double s = block_sum(p1, red);
       if (threadIdx.x == 0) {
@@ -622,11 +622,11 @@ __device__ __forceinline__ double lane_sumsq(const double* col, int64_t i0, int6
 #pragma unroll
     for (int u = 0; u < kRowBatch; ++u) q[u] = __ldcg(col + i + 256 * u);
 #pragma unroll
-    for (int u = 0; u < kRowBatch; ++u) ps = __dadd_rn(ps, __dmul_rn(q[u], q[u]));
+    for (int u = 0; u < kRowBatch; ++u) ps = __fma_rn(q[u], q[u], ps);
   }
   for (; i < rows; i += 256) {
     const double q = __ldcg(col + i);
-    ps = __dadd_rn(ps, __dmul_rn(q, q));
+    ps = __fma_rn(q, q, ps);
   }
   return ps;
 }
@@ -692,13 +692,13 @@ __global__ void __cluster_dims__(kQrCluster, 1, 1) __launch_bounds__(32 * QrShap
 #pragma unroll
         for (int u = 0; u < kRowBatch; ++u) {
           __stcg(dst + r + 256 * u, v[u]);
-          acc = __dadd_rn(acc, __dmul_rn(v[u], v[u]));
+          acc = __fma_rn(v[u], v[u], acc);
         }
       }
       for (; r < rows; r += 256) {
         const double v = src[r];
         __stcg(dst + r, v);
-        acc = __dadd_rn(acc, __dmul_rn(v, v));
+        acc = __fma_rn(v, v, acc);
       }
       part[s] = acc;
     } else if (j == k - 1) {
@@ -822,13 +822,13 @@ __global__ void __cluster_dims__(kQrCluster, 1, 1) __launch_bounds__(32 * QrShap
             for (int u = 0; u < U; ++u)
 #pragma unroll
               for (int s = 0; s < CPW; ++s)
-                if (cp[s]) part[s] = __dadd_rn(part[s], __dmul_rn(vi[u], cv[u][s]));
+                if (cp[s]) part[s] = __fma_rn(vi[u], cv[u][s], part[s]);
           }
           for (; i < rows; i += 256) {
             const double vi = __ldcg(v + i);
 #pragma unroll
             for (int s = 0; s < CPW; ++s)
-              if (cp[s]) part[s] = __dadd_rn(part[s], __dmul_rn(vi, __ldcg(cp[s] + i)));
+              if (cp[s]) part[s] = __fma_rn(vi, __ldcg(cp[s] + i), part[s]);
           }
         }
         cl_sum_cols<KB, W, CPW>(cl, red, part, cnt, out);
@@ -854,14 +854,14 @@ __global__ void __cluster_dims__(kQrCluster, 1, 1) __launch_bounds__(32 * QrShap
               const double t = __dmul_rn(tau, tv[u]);
 #pragma unroll
               for (int s = 0; s < CPW; ++s)
-                if (cp[s]) __stcg(cp[s] + i + 256 * u, __dsub_rn(cv[u][s], __dmul_rn(t, out[s])));
+                if (cp[s]) __stcg(cp[s] + i + 256 * u, __fma_rn(-t, out[s], cv[u][s]));
             }
           }
           for (; i < rows; i += 256) {
             const double t = __dmul_rn(tau, __ldcg(v + i));
 #pragma unroll
             for (int s = 0; s < CPW; ++s)
-              if (cp[s]) __stcg(cp[s] + i, __dsub_rn(__ldcg(cp[s] + i), __dmul_rn(t, out[s])));
+              if (cp[s]) __stcg(cp[s] + i, __fma_rn(-t, out[s], __ldcg(cp[s] + i)));
           }
         }
       }
