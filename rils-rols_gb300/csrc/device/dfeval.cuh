@@ -47,6 +47,55 @@ __device__ __forceinline__ dfl df_bin(int base, dfl a, dfl b) {
   }
 }
 
+// Two rows at once (one dispatch).  Addition, subtraction, multiplication and
+// squaring run without the non-finite guards first; a non-finite leading
+// part means an operand or the result is not finite, and only then are the
+// guarded operations (whose results are identical on finite values) run.
+__device__ __forceinline__ void df_bin2(int base, dfl a0, dfl b0, dfl a1, dfl b1, dfl& r0, dfl& r1) {
+  switch (base) {
+    case RRG_ADD:
+    case RRG_SUB:
+      if (base == RRG_SUB) {
+        b0 = dfl_neg(b0);
+        b1 = dfl_neg(b1);
+      }
+      r0 = dfl_add_nc(a0, b0);
+      r1 = dfl_add_nc(a1, b1);
+      if (!(dfl_finite(r0.hi) && dfl_finite(r1.hi))) {
+        r0 = dfl_add(a0, b0);
+        r1 = dfl_add(a1, b1);
+      }
+      return;
+    case RRG_MUL:
+      r0 = dfl_mul_nc(a0, b0);
+      r1 = dfl_mul_nc(a1, b1);
+      if (!(dfl_finite(r0.hi) && dfl_finite(r1.hi))) {
+        r0 = dfl_mul(a0, b0);
+        r1 = dfl_mul(a1, b1);
+      }
+      return;
+    default:
+      r0 = df_bin(base, a0, b0);
+      r1 = df_bin(base, a1, b1);
+  }
+}
+
+__device__ __forceinline__ void df_unary2(int op, dfl& t0, dfl& t1) {
+  if (op == RRG_OP_SQR) {
+    const dfl r0 = dfl_mul_nc(t0, t0), r1 = dfl_mul_nc(t1, t1);
+    if (dfl_finite(r0.hi) && dfl_finite(r1.hi)) {
+      t0 = r0;
+      t1 = r1;
+    } else {
+      t0 = dfl_mul(t0, t0);
+      t1 = dfl_mul(t1, t1);
+    }
+    return;
+  }
+  t0 = df_unary(op, t0);
+  t1 = df_unary(op, t1);
+}
+
 // Scalar interpreter (one row) over double-float X and constants; false on
 // a spill-stack violation.
 __device__ inline bool eval_row_df(const uint32_t* code, int len, const float* K, const float* Klo,

@@ -90,8 +90,7 @@ __device__ __forceinline__ bool eval_fac2(const uint32_t* code, int len, const f
         break;
       default:
         if (op >= RRG_OP_SIN && op <= RRG_OP_SQR) {
-          t0 = df_unary(op, t0);
-          t1 = df_unary(op, t1);
+          df_unary2(op, t0, t1);
         } else {
           const int kk = op - RRG_OP_BIN;
           const int base = kk >> 3, src = (kk & 7) >> 1, dir = kk & 1;
@@ -108,13 +107,8 @@ __device__ __forceinline__ bool eval_fac2(const uint32_t* code, int len, const f
           } else {
             u0 = u1 = dfl_make(__ldg(K + arg), __ldg(Klo + arg));
           }
-          if (dir == RRG_DIR_N) {
-            t0 = df_bin(base, u0, t0);
-            t1 = df_bin(base, u1, t1);
-          } else {
-            t0 = df_bin(base, t0, u0);
-            t1 = df_bin(base, t1, u1);
-          }
+          if (dir == RRG_DIR_N) df_bin2(base, u0, t0, u1, t1, t0, t1);
+          else df_bin2(base, t0, u0, t1, u1, t0, t1);
         }
     }
   }
