@@ -260,8 +260,11 @@ __global__ void __launch_bounds__(kPairThreads) pair_sum_kernel(PairArgs a) {
         const int r = 2 * tid + 2 * kPairThreads * s;
         if (r < rows) {
           const float4 bv = *reinterpret_cast<const float4*>(fb + r);
-          acc = dfl_add(acc, dfl_mul(dfl_make(av[s].x, av[s].y), dfl_make(bv.x, bv.y)));
-          acc = dfl_add(acc, dfl_mul(dfl_make(av[s].z, av[s].w), dfl_make(bv.z, bv.w)));
+          // without the non-finite guards: a non-finite factor value turns the
+          // sum NaN instead of +-inf, and the solve sends every candidate with a
+          // non-finite cross sum (NaN or inf alike) to the FP64 path
+          acc = dfl_add_nc(acc, dfl_add_nc(dfl_mul_nc(dfl_make(av[s].x, av[s].y), dfl_make(bv.x, bv.y)),
+                                           dfl_mul_nc(dfl_make(av[s].z, av[s].w), dfl_make(bv.z, bv.w))));
         }
       }
       const dfl v = warp_dfl_sum(acc);
