@@ -296,6 +296,8 @@ __global__ void pair_reduce_kernel(const float2* P, int32_t n_pairs, int32_t n_c
   psum[p] = s;
 }
 
+// The candidates of the residual pass have finite table values (the solve sends
+// every non-finite one to the FP64 path), so the unguarded operations apply.
 __global__ void __launch_bounds__(kResidThreads) ftab_resid_kernel(ResidArgs a) {
   __shared__ float red[kResidThreads / 32][2];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -338,16 +340,16 @@ __global__ void __launch_bounds__(kResidThreads) ftab_resid_kernel(ResidArgs a) 
           for (int s = 0; s < kMixedMaxM; ++s)
             if (s == t) f = u == 0 ? dfl_make(fv[s].x, fv[s].y) : dfl_make(fv[s].z, fv[s].w);
           const dfl cf = dfl_make(tm.hi[t], tm.lo[t]);
-          const dfl term = kd == 1 ? cf : (kd == 2 ? f : dfl_mul(cf, f));
-          yp = have ? dfl_add(yp, term) : term;
+          const dfl term = kd == 1 ? cf : (kd == 2 ? f : dfl_mul_nc(cf, f));
+          yp = have ? dfl_add_nc(yp, term) : term;
           have = true;
         }
       } else {
         yp = u == 0 ? dfl_make(fv[0].x, fv[0].y) : dfl_make(fv[0].z, fv[0].w);
       }
       const dfl y = u == 0 ? dfl_make(yh.x, yl.x) : dfl_make(yh.y, yl.y);
-      const dfl e = dfl_sub(y, yp);
-      if (gr + u < n) acc = dfl_add(acc, dfl_mul(e, e));
+      const dfl e = dfl_add_nc(y, dfl_neg(yp));
+      if (gr + u < n) acc = dfl_add_nc(acc, dfl_mul_nc(e, e));
     }
   }
   const dfl v = warp_dfl_sum(acc);
