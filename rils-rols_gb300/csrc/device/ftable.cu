@@ -40,75 +40,99 @@ __device__ __forceinline__ dfl warp_dfl_sum(dfl v) {
   return v;
 }
 
-// One table program on 2 consecutive rows (r, r + 1 of the chunk); X column
-// j has its high parts at xh + j * ldx and its low parts at xl + j * ldx;
-// table column t (an earlier level) at tb + t * ldtab.
-__device__ __forceinline__ bool eval_fac2(const uint32_t* code, int len, const float* __restrict__ K,
+// One table program on 4 consecutive rows (r .. r + 3 of the chunk), as two
+// pairs A (r, r + 1) and B (r + 2, r + 3) sharing one dispatch; X column j has
+// its high parts at xh + j * ldx and its low parts at xl + j * ldx; table
+// column t (an earlier level) at tb + t * ldtab.  A spill level holds the
+// four values in two float4 slots.
+__device__ __forceinline__ bool eval_fac4(const uint32_t* code, int len, const float* __restrict__ K,
                                           const float* __restrict__ Klo, const float* xh, const float* xl,
                                           int64_t ldx, const float2* tb, int64_t ldtab, int r, float4* st,
-                                          dfl& o0, dfl& o1) {
-  dfl t0 = dfl_make(0.f, 0.f), t1 = t0;
+                                          dfl (&o)[4]) {
+  dfl t0 = dfl_make(0.f, 0.f), t1 = t0, t2 = t0, t3 = t0;
   int sp = 0;
-  auto ldv = [&](uint32_t j, dfl& u0, dfl& u1) {
-    const float2 h = *reinterpret_cast<const float2*>(xh + (int64_t)j * ldx + r);
-    const float2 l = *reinterpret_cast<const float2*>(xl + (int64_t)j * ldx + r);
+  auto ldv = [&](uint32_t j, dfl& u0, dfl& u1, dfl& u2, dfl& u3) {
+    const float4 h = *reinterpret_cast<const float4*>(xh + (int64_t)j * ldx + r);
+    const float4 l = *reinterpret_cast<const float4*>(xl + (int64_t)j * ldx + r);
     u0 = dfl_make(h.x, l.x);
     u1 = dfl_make(h.y, l.y);
+    u2 = dfl_make(h.z, l.z);
+    u3 = dfl_make(h.w, l.w);
   };
-  auto ldt = [&](uint32_t t, dfl& u0, dfl& u1) {
+  auto ldt = [&](uint32_t t, dfl& u0, dfl& u1, dfl& u2, dfl& u3) {
     const float4 v = *reinterpret_cast<const float4*>(tb + (int64_t)t * ldtab + r);
+    const float4 w = *reinterpret_cast<const float4*>(tb + (int64_t)t * ldtab + r + 2);
     u0 = dfl_make(v.x, v.y);
     u1 = dfl_make(v.z, v.w);
+    u2 = dfl_make(w.x, w.y);
+    u3 = dfl_make(w.z, w.w);
+  };
+  auto push = [&]() {
+    st[32 * (2 * sp)] = make_float4(t0.hi, t0.lo, t1.hi, t1.lo);
+    st[32 * (2 * sp + 1)] = make_float4(t2.hi, t2.lo, t3.hi, t3.lo);
+    ++sp;
   };
   for (int pc = 0; pc < len; ++pc) {
     const uint32_t w = code[pc];
     const int op = (int)(w & 0xffu);
     const uint32_t arg = w >> 8;
     switch (op) {
-      case RRG_OP_LDV: ldv(arg, t0, t1); break;
-      case RRG_OP_LDC: t0 = t1 = dfl_make(__ldg(K + arg), __ldg(Klo + arg)); break;
+      case RRG_OP_LDV: ldv(arg, t0, t1, t2, t3); break;
+      case RRG_OP_LDC: t0 = t1 = t2 = t3 = dfl_make(__ldg(K + arg), __ldg(Klo + arg)); break;
       case RRG_OP_PSV:
         if (sp >= kMixedStackCap) return false;
-        st[32 * sp++] = make_float4(t0.hi, t0.lo, t1.hi, t1.lo);
-        ldv(arg, t0, t1);
+        push();
+        ldv(arg, t0, t1, t2, t3);
         break;
       case RRG_OP_PSC:
         if (sp >= kMixedStackCap) return false;
-        st[32 * sp++] = make_float4(t0.hi, t0.lo, t1.hi, t1.lo);
-        t0 = t1 = dfl_make(__ldg(K + arg), __ldg(Klo + arg));
+        push();
+        t0 = t1 = t2 = t3 = dfl_make(__ldg(K + arg), __ldg(Klo + arg));
         break;
-      case kOpLDT: ldt(arg, t0, t1); break;
+      case kOpLDT: ldt(arg, t0, t1, t2, t3); break;
       case kOpPST:
         if (sp >= kMixedStackCap) return false;
-        st[32 * sp++] = make_float4(t0.hi, t0.lo, t1.hi, t1.lo);
-        ldt(arg, t0, t1);
+        push();
+        ldt(arg, t0, t1, t2, t3);
         break;
       case RRG_OP_EMIT:
-        o0 = t0;
-        o1 = t1;
+        o[0] = t0;
+        o[1] = t1;
+        o[2] = t2;
+        o[3] = t3;
         sp = 0;
         break;
       default:
         if (op >= RRG_OP_SIN && op <= RRG_OP_SQR) {
           df_unary2(op, t0, t1);
+          df_unary2(op, t2, t3);
         } else {
           const int kk = op - RRG_OP_BIN;
           const int base = kk >> 3, src = (kk & 7) >> 1, dir = kk & 1;
-          dfl u0, u1;
+          dfl u0, u1, u2, u3;
           if (src == RRG_SRC_S) {
             if (sp <= 0) return false;
-            const float4 v = st[32 * --sp];
+            --sp;
+            const float4 v = st[32 * (2 * sp)];
+            const float4 v2 = st[32 * (2 * sp + 1)];
             u0 = dfl_make(v.x, v.y);
             u1 = dfl_make(v.z, v.w);
+            u2 = dfl_make(v2.x, v2.y);
+            u3 = dfl_make(v2.z, v2.w);
           } else if (src == RRG_SRC_V) {
-            ldv(arg, u0, u1);
+            ldv(arg, u0, u1, u2, u3);
           } else if (src == kSrcT) {
-            ldt(arg, u0, u1);
+            ldt(arg, u0, u1, u2, u3);
           } else {
-            u0 = u1 = dfl_make(__ldg(K + arg), __ldg(Klo + arg));
+            u0 = u1 = u2 = u3 = dfl_make(__ldg(K + arg), __ldg(Klo + arg));
           }
-          if (dir == RRG_DIR_N) df_bin2(base, u0, t0, u1, t1, t0, t1);
-          else df_bin2(base, t0, u0, t1, u1, t0, t1);
+          if (dir == RRG_DIR_N) {
+            df_bin2(base, u0, t0, u1, t1, t0, t1);
+            df_bin2(base, u2, t2, u3, t3, t2, t3);
+          } else {
+            df_bin2(base, t0, u0, t1, u1, t0, t1);
+            df_bin2(base, t2, u2, t3, u3, t2, t3);
+          }
         }
     }
   }
@@ -119,7 +143,7 @@ __device__ __forceinline__ bool eval_fac2(const uint32_t* code, int len, const f
 constexpr size_t kFacRedOff = 128;                                   // [warp][6] floats
 constexpr size_t kFacCodeOff = kFacRedOff + 256;
 constexpr size_t kFacStackOff = kFacCodeOff + sizeof(uint32_t) * kFacCodeSmem;
-constexpr size_t kFacXOff = kFacStackOff + sizeof(float4) * (kFacThreads / 32) * kMixedStackCap * 32;
+constexpr size_t kFacXOff = kFacStackOff + sizeof(float4) * (kFacThreads / 32) * kMixedStackCap * 32 * 2;
 
 }  // namespace
 
@@ -175,7 +199,7 @@ __global__ void __launch_bounds__(kFacThreads) fac_eval_kernel(FacEvalArgs a, in
   const float* yh = staged ? xs + (size_t)(2 * d) * a.chunk : a.ds.y32 + row0;
   const float* yl = staged ? xs + (size_t)(2 * d + 1) * a.chunk : a.ds.y32lo + row0;
   const float2* tb = a.F + row0;
-  float4* st = stk + (size_t)warp * kMixedStackCap * 32 + lane;
+  float4* st = stk + (size_t)warp * kMixedStackCap * 32 * 2 + lane;
   for (int i = 0; i < grp.y; ++i) {
     const int f = grp.x + i;
     const int2 mt = a.meta[f];
@@ -183,32 +207,39 @@ __global__ void __launch_bounds__(kFacThreads) fac_eval_kernel(FacEvalArgs a, in
     dfl ff = dfl_make(0.f, 0.f), fs = ff, fy = ff;
     unsigned long long first = ~0ull;
     bool ok = true;
-    for (int r = 2 * tid; r < rows; r += kFacStep) {
-      dfl v0 = dfl_make(0.f, 0.f), v1 = v0;
-      ok = eval_fac2(code, mt.y, a.K, a.Klo, xh, xl, ldx, tb, n_pad, r, st, v0, v1) && ok;
+    for (int r = 4 * tid; r < rows; r += kFacStep) {
+      dfl v[4];
+      ok = eval_fac4(code, mt.y, a.K, a.Klo, xh, xl, ldx, tb, n_pad, r, st, v) && ok;
       const int64_t gr = row0 + r;
-      if (gr >= n) v0 = dfl_make(0.f, 0.f);
-      if (gr + 1 >= n) v1 = dfl_make(0.f, 0.f);
-      if (v0.hi != v0.hi) first = min(first, (unsigned long long)gr);
-      else if (v1.hi != v1.hi) first = min(first, (unsigned long long)(gr + 1));
-      *reinterpret_cast<float4*>(a.F + (int64_t)f * n_pad + gr) = make_float4(v0.hi, v0.lo, v1.hi, v1.lo);
-      const float2 yhv = *reinterpret_cast<const float2*>(yh + r);
-      const float2 ylv = *reinterpret_cast<const float2*>(yl + r);
-      const dfl y0 = dfl_make(yhv.x, ylv.x), y1 = dfl_make(yhv.y, ylv.y);
-      if (__all_sync(0xffffffffu, dfl_finite(v0.hi) && dfl_finite(v1.hi) && dfl_finite(ff.hi) &&
-                                      dfl_finite(fs.hi) && dfl_finite(fy.hi))) {
-        // finite values (the common case): the two rows' terms are added first,
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        if (gr + u >= n) v[u] = dfl_make(0.f, 0.f);
+        if (v[u].hi != v[u].hi) first = min(first, (unsigned long long)(gr + u));
+      }
+      *reinterpret_cast<float4*>(a.F + (int64_t)f * n_pad + gr) = make_float4(v[0].hi, v[0].lo, v[1].hi, v[1].lo);
+      *reinterpret_cast<float4*>(a.F + (int64_t)f * n_pad + gr + 2) = make_float4(v[2].hi, v[2].lo, v[3].hi, v[3].lo);
+      const float4 yhv = *reinterpret_cast<const float4*>(yh + r);
+      const float4 ylv = *reinterpret_cast<const float4*>(yl + r);
+      const dfl y[4] = {dfl_make(yhv.x, ylv.x), dfl_make(yhv.y, ylv.y), dfl_make(yhv.z, ylv.z),
+                        dfl_make(yhv.w, ylv.w)};
+      bool fin = dfl_finite(ff.hi) && dfl_finite(fs.hi) && dfl_finite(fy.hi);
+#pragma unroll
+      for (int u = 0; u < 4; ++u) fin = fin && dfl_finite(v[u].hi);
+      if (__all_sync(0xffffffffu, fin)) {
+        // finite values (the common case): the rows' terms are added first,
         // without the non-finite guards
-        ff = dfl_add_nc(ff, dfl_add_nc(dfl_mul_nc(v0, v0), dfl_mul_nc(v1, v1)));
-        fs = dfl_add_nc(fs, dfl_add_nc(v0, v1));
-        fy = dfl_add_nc(fy, dfl_add_nc(dfl_mul_nc(v0, y0), dfl_mul_nc(v1, y1)));
+        ff = dfl_add_nc(ff, dfl_add_nc(dfl_add_nc(dfl_mul_nc(v[0], v[0]), dfl_mul_nc(v[1], v[1])),
+                                       dfl_add_nc(dfl_mul_nc(v[2], v[2]), dfl_mul_nc(v[3], v[3]))));
+        fs = dfl_add_nc(fs, dfl_add_nc(dfl_add_nc(v[0], v[1]), dfl_add_nc(v[2], v[3])));
+        fy = dfl_add_nc(fy, dfl_add_nc(dfl_add_nc(dfl_mul_nc(v[0], y[0]), dfl_mul_nc(v[1], y[1])),
+                                       dfl_add_nc(dfl_mul_nc(v[2], y[2]), dfl_mul_nc(v[3], y[3]))));
       } else {
-        ff = dfl_add(ff, dfl_mul(v0, v0));
-        ff = dfl_add(ff, dfl_mul(v1, v1));
-        fs = dfl_add(fs, v0);
-        fs = dfl_add(fs, v1);
-        fy = dfl_add(fy, dfl_mul(v0, y0));
-        fy = dfl_add(fy, dfl_mul(v1, y1));
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          ff = dfl_add(ff, dfl_mul(v[u], v[u]));
+          fs = dfl_add(fs, v[u]);
+          fy = dfl_add(fy, dfl_mul(v[u], y[u]));
+        }
       }
     }
     if (!ok) atomicOr(a.status, ST_STACK);

@@ -12,11 +12,11 @@
 
 namespace rrd {
 
-constexpr int kFacThreads = 256;      // evaluator block: 2 rows per thread
-constexpr int kFacStep = 2 * kFacThreads;
+constexpr int kFacThreads = 256;      // evaluator block: 4 rows per thread
+constexpr int kFacStep = 4 * kFacThreads;
 constexpr int kFacCodeSmem = 2048;    // program words of one evaluator group in shared memory
 constexpr int kFacGroupMax = 64;      // factors per evaluator group
-constexpr int kFacStageBytes = 64 * 1024;  // X and y chunk (hi and lo) staged by TMA when it fits
+constexpr int kFacStageBytes = 74 * 1024;  // largest staged evaluator block: three per SM
 constexpr int kPairThreads = 256;
 constexpr int kPairBatch = 16;        // partners reduced together
 constexpr int kPairRows = 4096;       // rows per pair-sum / residual block

@@ -563,9 +563,12 @@ rrg_status rrg_context::mixed_subround(const rrg_dataset* ds, const int32_t* lis
   }
   const int32_t n_pairs = n_self + n_cross;
   // row chunks: the evaluator stages X and y (high and low parts) by TMA
-  // when a chunk of d + 1 columns fits; pair sums and the residual pass use
+  // only while the staged block still fits three blocks per SM (the register
+  // limit), i.e. for few features; otherwise it reads them from L2, where
+  // they stay resident (measured: staging d = 5 cost 24% of the evaluator's
+  // time through the lost occupancy); pair sums and the residual pass use
   // kPairRows blocks
-  bool staged = (size_t)(ds->d + 1) * 2 * 1024 * sizeof(float) <= (size_t)kFacStageBytes;
+  bool staged = fac_eval_smem(ds->d, 1024, true) <= (size_t)kFacStageBytes;
   int chunk = staged ? 1024 : 2048;
   if ((ds->n_pad + chunk - 1) / chunk > 65535) {
     staged = false;
