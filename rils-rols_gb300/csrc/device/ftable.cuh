@@ -17,6 +17,7 @@ constexpr int kFacStep = 4 * kFacThreads;
 constexpr int kFacCodeSmem = 2048;    // program words of one evaluator group in shared memory
 constexpr int kFacGroupMax = 64;      // factors per evaluator group
 constexpr int kFacStageBytes = 74 * 1024;  // largest staged evaluator block: three per SM
+constexpr int kFacChunk = 8192;           // rows per evaluator block (a multiple of kFacStep)
 constexpr int kPairThreads = 256;
 constexpr int kPairBatch = 16;        // partners reduced together
 constexpr int kPairRows = 4096;       // rows per pair-sum / residual block

@@ -562,14 +562,16 @@ rrg_status rrg_context::mixed_subround(const rrg_dataset* ds, const int32_t* lis
     k = e;
   }
   const int32_t n_pairs = n_self + n_cross;
-  // row chunks: the evaluator stages X and y (high and low parts) by TMA
-  // only while the staged block still fits three blocks per SM (the register
-  // limit), i.e. for few features; otherwise it reads them from L2, where
-  // they stay resident (measured: staging d = 5 cost 24% of the evaluator's
-  // time through the lost occupancy); pair sums and the residual pass use
-  // kPairRows blocks
-  bool staged = fac_eval_smem(ds->d, 1024, true) <= (size_t)kFacStageBytes;
-  int chunk = staged ? 1024 : 2048;
+  // row chunks of kFacChunk rows (the self sums' partials are per chunk); the
+  // evaluator stages X and y (high and low parts) by TMA only while the
+  // staged block still fits three blocks per SM (the register limit), i.e.
+  // for one feature; otherwise it reads them from L2, where they stay
+  // resident (measured at d = 5, n = 1M: staged 1024-row chunks 73 ms per
+  // round, L2 reads of 1024 / 2048 / 4096 / 8192-row chunks 66 / 59 / 55 /
+  // 53 ms: larger chunks spread each block's per-factor reductions over more
+  // rows); pair sums and the residual pass use kPairRows blocks
+  int chunk = kFacChunk;
+  bool staged = fac_eval_smem(ds->d, chunk, true) <= (size_t)kFacStageBytes;
   if ((ds->n_pad + chunk - 1) / chunk > 65535) {
     staged = false;
     chunk = (int)round_up((ds->n_pad + 65534) / 65535, kFacStep);
