@@ -1,5 +1,6 @@
 // Candidate flattening and the tune_constants split/rebuild; see encode.h.
 #include "encode.h"
+#include "parallel.h"
 
 #include <cstring>
 #include <stdexcept>
@@ -92,9 +93,8 @@ namespace {
 
 struct Emitter {
   std::vector<uint32_t>& code;
-  std::unordered_map<const Node*, int> depth;
-  BatchBuilder* bb;
-  int (BatchBuilder::*cidx)(double);
+  std::unordered_map<const Node*, int>& depth;
+  std::vector<double>& pool;  // constants of this candidate; code holds local indices
 
   static bool leaf(const Node* n) { return n->type == CONST || n->type == VAR; }
 
@@ -143,7 +143,9 @@ struct Emitter {
   }
 
   uint32_t leaf_arg(const Node* n) {
-    return n->type == VAR ? (uint32_t)n->var : (uint32_t)(bb->*cidx)(n->val);
+    if (n->type == VAR) return (uint32_t)n->var;
+    pool.push_back(n->val);
+    return (uint32_t)(pool.size() - 1);
   }
 
   void emit(const Node* n, bool push) {
@@ -203,38 +205,65 @@ struct Emitter {
 
 }  // namespace
 
-int BatchBuilder::encode_factor(const Flat& f, int slot) {
-  arena_.reset();
-  Node* t = thaw(f, arena_);
-  Emitter e{code_, {}, this, &BatchBuilder::const_index};
-  int d = e.D(t);
-  e.emit(t, false);
-  code_.push_back(RRG_INSN(RRG_OP_EMIT, slot));
-  return d;
-}
-
-int BatchBuilder::add(const std::vector<Flat>& factors, int mode) {
-  rrg_cand c;
-  std::memset(&c, 0, sizeof c);
-  c.code_offset = (int32_t)code_.size();
-  c.first_factor = (int32_t)factors_.size();
-  c.n_factors = (int32_t)factors.size();
-  c.mode = mode;
-  c.coef_offset = mode == RRG_TUNED ? n_coefs_ : 0;
-  c.stack_need = 0;
+void encode_local(const std::vector<Flat>& factors, int mode, Arena& arena,
+                  std::unordered_map<const Node*, int>& depth, EncodedCand& out) {
+  out.code.clear();
+  out.consts.clear();
+  out.n_nodes.clear();
+  out.stack_need = 0;
+  out.mode = mode;
   if (mode == RRG_TUNED && (int)factors.size() + 1 > RRG_MAX_TERMS)
     throw std::runtime_error("candidate has more than RRG_MAX_TERMS terms");
   if (mode == RRG_UNTUNED && factors.size() != 1) throw std::runtime_error("untuned candidate needs one program");
   for (size_t i = 0; i < factors.size(); ++i) {
-    int d = encode_factor(factors[i], (int)i);
-    if (d > c.stack_need) c.stack_need = d;
-    factors_.push_back(rrg_factor{(int32_t)factors[i].size(), 0});
+    arena.reset();
+    depth.clear();
+    Node* t = thaw(factors[i], arena);
+    Emitter e{out.code, depth, out.consts};
+    const int d = e.D(t);
+    e.emit(t, false);
+    out.code.push_back(RRG_INSN(RRG_OP_EMIT, (uint32_t)i));
+    out.stack_need = std::max(out.stack_need, d);
+    out.n_nodes.push_back((int32_t)factors[i].size());
   }
-  if (c.stack_need > RRG_MAX_STACK) throw std::runtime_error("candidate exceeds RRG_MAX_STACK spill depth");
+  if (out.stack_need > RRG_MAX_STACK) throw std::runtime_error("candidate exceeds RRG_MAX_STACK spill depth");
+}
+
+int BatchBuilder::merge(const EncodedCand& e) {
+  rrg_cand c;
+  std::memset(&c, 0, sizeof c);
+  c.code_offset = (int32_t)code_.size();
+  c.first_factor = (int32_t)factors_.size();
+  c.n_factors = (int32_t)e.n_nodes.size();
+  c.mode = e.mode;
+  c.coef_offset = e.mode == RRG_TUNED ? n_coefs_ : 0;
+  c.stack_need = e.stack_need;
+  for (uint32_t w : e.code) {
+    const int op = (int)(w & 0xffu);
+    const bool cst = op == RRG_OP_LDC || op == RRG_OP_PSC ||
+                     (op >= RRG_OP_BIN && (((op - RRG_OP_BIN) & 7) >> 1) == RRG_SRC_C);
+    code_.push_back(cst ? RRG_INSN(op, (uint32_t)const_index(e.consts[w >> 8])) : w);
+  }
+  for (int32_t nn : e.n_nodes) factors_.push_back(rrg_factor{nn, 0});
   c.code_len = (int32_t)code_.size() - c.code_offset;
-  if (mode == RRG_TUNED) n_coefs_ += (int)factors.size() + 1;
+  if (e.mode == RRG_TUNED) n_coefs_ += c.n_factors + 1;
   cands_.push_back(c);
   return (int)cands_.size() - 1;
+}
+
+int BatchBuilder::add(const std::vector<Flat>& factors, int mode) {
+  encode_local(factors, mode, arena_, depth_, scratch_);
+  return merge(scratch_);
+}
+
+void BatchBuilder::add_all(const std::vector<const std::vector<Flat>*>& cands, int mode) {
+  std::vector<EncodedCand> enc(cands.size());
+  parallel_slices(cands.size(), 256, [&](size_t b, size_t e) {
+    Arena arena;
+    std::unordered_map<const Node*, int> depth;
+    for (size_t i = b; i < e; ++i) encode_local(*cands[i], mode, arena, depth, enc[i]);
+  });
+  for (const EncodedCand& e : enc) merge(e);
 }
 
 rrg_batch BatchBuilder::view() const {

@@ -26,10 +26,26 @@ Flat rebuild(const std::vector<Flat>& factors, const double* coefs);
 // Node count of the rebuilt tree without building it.
 int rebuilt_size(const std::vector<Flat>& factors, const double* coefs);
 
+// One candidate's postfix code with constant-pool indices local to it, as
+// encoded on its own (any thread); BatchBuilder::merge pools the constants.
+struct EncodedCand {
+  std::vector<uint32_t> code;
+  std::vector<double> consts;
+  std::vector<int32_t> n_nodes;  // per factor
+  int stack_need = 0;
+  int mode = 0;
+};
+void encode_local(const std::vector<Flat>& factors, int mode, Arena& arena,
+                  std::unordered_map<const Node*, int>& depth, EncodedCand& out);
+
 // Accumulates candidates into one rrg_batch.
 class BatchBuilder {
  public:
   void clear();
+  // every candidate of `cands` (the same mode), encoded on the host threads
+  // and appended in order
+  void add_all(const std::vector<const std::vector<Flat>*>& cands, int mode);
+  int merge(const EncodedCand& e);
   // mode RRG_TUNED: `factors` are the non-constant factors; RRG_UNTUNED:
   // factors has exactly one entry, the whole tree.  Returns the candidate
   // index; sets *too_large if the candidate cannot be encoded.
@@ -40,7 +56,6 @@ class BatchBuilder {
   const std::vector<rrg_cand>& cands() const { return cands_; }
 
  private:
-  int encode_factor(const Flat& f, int slot);  // returns spill depth
   int const_index(double v);
   std::vector<rrg_cand> cands_;
   std::vector<rrg_factor> factors_;
@@ -49,6 +64,8 @@ class BatchBuilder {
   std::unordered_map<uint64_t, int> const_map_;
   int n_coefs_ = 0;
   Arena arena_;
+  std::unordered_map<const Node*, int> depth_;
+  EncodedCand scratch_;
 };
 
 }  // namespace rrh

@@ -8,6 +8,7 @@
 #include "../../../include/rils_rols_host.h"
 #include "../common/error.h"
 #include "encode.h"
+#include "parallel.h"
 #include "search.h"
 
 struct rrh_model {
@@ -171,17 +172,26 @@ int32_t rrh_encode(const char* trees, int32_t mode, rrg_batch* out) {
     g_encoded.clear();
     std::istringstream in(trees);
     std::string line;
-    rrh::Arena a;
-    while (std::getline(in, line)) {
-      if (line.empty()) continue;
-      rrh::Flat f = rrh::from_prefix(line);
-      if (mode == RRG_TUNED) {
-        a.reset();
-        g_encoded.add(rrh::tune_factors(f, a), RRG_TUNED);
-      } else {
-        g_encoded.add(std::vector<rrh::Flat>{f}, RRG_UNTUNED);
+    std::vector<std::string> lines;
+    while (std::getline(in, line))
+      if (!line.empty()) lines.push_back(line);
+    // parse and split on the host threads, encode in order
+    std::vector<std::vector<rrh::Flat>> parts(lines.size());
+    rrh::parallel_slices(lines.size(), 256, [&](size_t b, size_t e) {
+      rrh::Arena a;
+      for (size_t i = b; i < e; ++i) {
+        rrh::Flat f = rrh::from_prefix(lines[i]);
+        if (mode == RRG_TUNED) {
+          a.reset();
+          parts[i] = rrh::tune_factors(f, a);
+        } else {
+          parts[i] = std::vector<rrh::Flat>{f};
+        }
       }
-    }
+    });
+    std::vector<const std::vector<rrh::Flat>*> ptrs(parts.size());
+    for (size_t i = 0; i < parts.size(); ++i) ptrs[i] = &parts[i];
+    g_encoded.add_all(ptrs, mode == RRG_TUNED ? RRG_TUNED : RRG_UNTUNED);
     *out = g_encoded.view();
     return (int32_t)RRG_OK;
   });

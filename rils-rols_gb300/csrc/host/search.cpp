@@ -1,4 +1,5 @@
 // Host search driver; see search.h.
+#include "parallel.h"
 #include "search.h"
 
 #include "../common/rr_sum.h"
@@ -228,22 +229,27 @@ std::vector<Flat> CandidateGen::all_candidates(const Flat& S, bool local_search)
       }
     }
   }
-  // clean-up loop (rils_rols_cpp.cpp:413-425)
-  for (auto& f : all) {
-    arena_.reset();
-    Node* t = thaw(f, arena_);
-    int it_max = 5;
-    while (it_max > 0) {
-      const int sz = size(t);
-      expand(t, arena_);
-      normalize_factor_constants(t, NONE, false);
-      simplify(t);
-      if (size(t) == sz) break;
-      it_max--;
+  // clean-up loop (rils_rols_cpp.cpp:413-425), each candidate on its own, on
+  // the host threads
+  parallel_slices(all.size(), 128, [&](size_t b, size_t e) {
+    Arena arena;
+    for (size_t i = b; i < e; ++i) {
+      Flat& f = all[i];
+      arena.reset();
+      Node* t = thaw(f, arena);
+      int it_max = 5;
+      while (it_max > 0) {
+        const int sz = size(t);
+        expand(t, arena);
+        normalize_factor_constants(t, NONE, false);
+        simplify(t);
+        if (size(t) == sz) break;
+        it_max--;
+      }
+      f.clear();
+      freeze_into(t, f);
     }
-    f.clear();
-    freeze_into(t, f);
-  }
+  });
   std::vector<Flat> filtered;
   filtered.reserve(all.size());
   seen.clear();
@@ -373,10 +379,19 @@ std::vector<Fit> Search::score_untuned(const std::vector<const Flat*>& trees) {
 std::vector<Search::Tuned> Search::score_tuned(const std::vector<const Flat*>& trees) {
   bb_.clear();
   std::vector<Tuned> out(trees.size());
-  for (size_t i = 0; i < trees.size(); ++i) {
-    arena_.reset();
-    out[i].factors = tune_factors(*trees[i], arena_);
-    bb_.add(out[i].factors, RRG_TUNED);
+  // the factor split of tune_constants (expand, simplify, top-level factors)
+  // of every candidate, on the host threads; encoded in candidate order
+  parallel_slices(trees.size(), 256, [&](size_t b, size_t e) {
+    Arena arena;
+    for (size_t i = b; i < e; ++i) {
+      arena.reset();
+      out[i].factors = tune_factors(*trees[i], arena);
+    }
+  });
+  {
+    std::vector<const std::vector<Flat>*> parts(trees.size());
+    for (size_t i = 0; i < trees.size(); ++i) parts[i] = &out[i].factors;
+    bb_.add_all(parts, RRG_TUNED);
   }
   std::vector<rrg_result> res;
   std::vector<double> coefs;
