@@ -15,15 +15,6 @@ static __device__ __noinline__ dfl df_sin_call(dfl a) { return dfl_sin(a); }
 static __device__ __noinline__ dfl df_cos_call(dfl a) { return dfl_cos(a); }
 static __device__ __noinline__ dfl df_log_call(dfl a) { return dfl_log(a); }
 static __device__ __noinline__ dfl df_exp_call(dfl a) { return dfl_exp(a); }
-// two rows per call: one call's overhead, and the two independent
-// evaluations interleave
-struct dfl_pair {
-  dfl a, b;
-};
-static __device__ __noinline__ dfl_pair df_sin_call2(dfl a, dfl b) { return dfl_pair{dfl_sin(a), dfl_sin(b)}; }
-static __device__ __noinline__ dfl_pair df_cos_call2(dfl a, dfl b) { return dfl_pair{dfl_cos(a), dfl_cos(b)}; }
-static __device__ __noinline__ dfl_pair df_log_call2(dfl a, dfl b) { return dfl_pair{dfl_log(a), dfl_log(b)}; }
-static __device__ __noinline__ dfl_pair df_exp_call2(dfl a, dfl b) { return dfl_pair{dfl_exp(a), dfl_exp(b)}; }
 // pow is rare: evaluated in FP64 (the plain path's rr_pow) and rounded back
 static __device__ __noinline__ dfl df_pow_call(dfl a, dfl b) {
   return dfl_from_double(rr_pow(dfl_to_double(a), dfl_to_double(b)));
@@ -101,19 +92,8 @@ __device__ __forceinline__ void df_unary2(int op, dfl& t0, dfl& t1) {
     }
     return;
   }
-  dfl_pair r;
-  switch (op) {
-    case RRG_OP_SIN: r = df_sin_call2(t0, t1); break;
-    case RRG_OP_COS: r = df_cos_call2(t0, t1); break;
-    case RRG_OP_LN: r = df_log_call2(t0, t1); break;
-    case RRG_OP_EXP: r = df_exp_call2(t0, t1); break;
-    default:
-      t0 = df_unary(op, t0);
-      t1 = df_unary(op, t1);
-      return;
-  }
-  t0 = r.a;
-  t1 = r.b;
+  t0 = df_unary(op, t0);
+  t1 = df_unary(op, t1);
 }
 
 // Scalar interpreter (one row) over double-float X and constants; false on

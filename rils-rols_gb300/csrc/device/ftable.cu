@@ -1,12 +1,15 @@
 // Factor table of a mixed round: double-float evaluation of the distinct
 // factor programs, Gram sums per distinct pair, and the residual pass.
 //
-//   fac_eval      block = (group of factors, row chunk).  The chunk of X and
-//                 y (high and low parts) is staged in shared memory by TMA
-//                 bulk copies (cp.async.bulk + mbarrier, bounded wait) when
-//                 it fits, and every factor of the group is interpreted on
-//                 it in double-float arithmetic, 2 rows per thread, with the
-//                 semantics of node::evaluate_inner (node.cpp:23-95).
+//   fac_eval      block = (group of factors, row chunk).  Every factor of
+//                 the group is interpreted on the chunk in double-float
+//                 arithmetic, 4 rows per thread for short shallow programs
+//                 and 2 for the others, with the semantics of
+//                 node::evaluate_inner (node.cpp:23-95); X and y (high and
+//                 low parts) are read from L2, where they stay resident
+//                 (staging each chunk in shared memory by TMA bulk copies
+//                 was measured slower: the shared memory it takes costs
+//                 more occupancy than the loads it saves).
 //                 Values go to the table F in HBM (rows >= n set to 0); the
 //                 self sums  sum f*f, sum f, sum f*y  of the chunk are formed
 //                 on the way;
@@ -23,7 +26,6 @@
 #include "common.cuh"
 #include "dfeval.cuh"
 #include "ftable.cuh"
-#include "tma.cuh"
 
 namespace rrd {
 
@@ -38,6 +40,81 @@ __device__ __forceinline__ dfl warp_dfl_sum(dfl v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v = dfl_add(v, shfl_dfl(v, o));
   return v;
+}
+
+// One table program on 2 consecutive rows (r, r + 1 of the chunk); X column
+// j has its high parts at xh + j * ldx and its low parts at xl + j * ldx;
+// table column t (an earlier level) at tb + t * ldtab.
+__device__ __forceinline__ bool eval_fac2(const uint32_t* code, int len, const float* __restrict__ K,
+                                          const float* __restrict__ Klo, const float* xh, const float* xl,
+                                          int64_t ldx, const float2* tb, int64_t ldtab, int r, float4* st,
+                                          dfl& o0, dfl& o1) {
+  dfl t0 = dfl_make(0.f, 0.f), t1 = t0;
+  int sp = 0;
+  auto ldv = [&](uint32_t j, dfl& u0, dfl& u1) {
+    const float2 h = *reinterpret_cast<const float2*>(xh + (int64_t)j * ldx + r);
+    const float2 l = *reinterpret_cast<const float2*>(xl + (int64_t)j * ldx + r);
+    u0 = dfl_make(h.x, l.x);
+    u1 = dfl_make(h.y, l.y);
+  };
+  auto ldt = [&](uint32_t t, dfl& u0, dfl& u1) {
+    const float4 v = *reinterpret_cast<const float4*>(tb + (int64_t)t * ldtab + r);
+    u0 = dfl_make(v.x, v.y);
+    u1 = dfl_make(v.z, v.w);
+  };
+  for (int pc = 0; pc < len; ++pc) {
+    const uint32_t w = code[pc];
+    const int op = (int)(w & 0xffu);
+    const uint32_t arg = w >> 8;
+    switch (op) {
+      case RRG_OP_LDV: ldv(arg, t0, t1); break;
+      case RRG_OP_LDC: t0 = t1 = dfl_make(__ldg(K + arg), __ldg(Klo + arg)); break;
+      case RRG_OP_PSV:
+        if (sp >= kMixedStackCap) return false;
+        st[32 * sp++] = make_float4(t0.hi, t0.lo, t1.hi, t1.lo);
+        ldv(arg, t0, t1);
+        break;
+      case RRG_OP_PSC:
+        if (sp >= kMixedStackCap) return false;
+        st[32 * sp++] = make_float4(t0.hi, t0.lo, t1.hi, t1.lo);
+        t0 = t1 = dfl_make(__ldg(K + arg), __ldg(Klo + arg));
+        break;
+      case kOpLDT: ldt(arg, t0, t1); break;
+      case kOpPST:
+        if (sp >= kMixedStackCap) return false;
+        st[32 * sp++] = make_float4(t0.hi, t0.lo, t1.hi, t1.lo);
+        ldt(arg, t0, t1);
+        break;
+      case RRG_OP_EMIT:
+        o0 = t0;
+        o1 = t1;
+        sp = 0;
+        break;
+      default:
+        if (op >= RRG_OP_SIN && op <= RRG_OP_SQR) {
+          df_unary2(op, t0, t1);
+        } else {
+          const int kk = op - RRG_OP_BIN;
+          const int base = kk >> 3, src = (kk & 7) >> 1, dir = kk & 1;
+          dfl u0, u1;
+          if (src == RRG_SRC_S) {
+            if (sp <= 0) return false;
+            const float4 v = st[32 * --sp];
+            u0 = dfl_make(v.x, v.y);
+            u1 = dfl_make(v.z, v.w);
+          } else if (src == RRG_SRC_V) {
+            ldv(arg, u0, u1);
+          } else if (src == kSrcT) {
+            ldt(arg, u0, u1);
+          } else {
+            u0 = u1 = dfl_make(__ldg(K + arg), __ldg(Klo + arg));
+          }
+          if (dir == RRG_DIR_N) df_bin2(base, u0, t0, u1, t1, t0, t1);
+          else df_bin2(base, t0, u0, t1, u1, t0, t1);
+        }
+    }
+  }
+  return true;
 }
 
 // One table program on 4 consecutive rows (r .. r + 3 of the chunk), as two
@@ -143,11 +220,14 @@ __device__ __forceinline__ bool eval_fac4(const uint32_t* code, int len, const f
 constexpr size_t kFacRedOff = 128;                                   // [warp][6] floats
 constexpr size_t kFacCodeOff = kFacRedOff + 256;
 constexpr size_t kFacStackOff = kFacCodeOff + sizeof(uint32_t) * kFacCodeSmem;
-constexpr size_t kFacXOff = kFacStackOff + sizeof(float4) * (kFacThreads / 32) * kMixedStackCap * 32 * 2;
+constexpr size_t kFacXOff = kFacStackOff + sizeof(float4) * (kFacThreads / 32) * kMixedStackCap * 32 * 2;  // end
 
 }  // namespace
 
-__global__ void __launch_bounds__(kFacThreads) fac_eval_kernel(FacEvalArgs a, int staged) {
+// R = 4 rows per thread for short, shallow programs (one dispatch per op for
+// four rows), R = 2 for the others (less spill traffic per thread).
+template <int R>
+__global__ void __launch_bounds__(kFacThreads) fac_eval_kernel(FacEvalArgs a) {
   extern __shared__ __align__(128) unsigned char smem[];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int2 grp = a.groups[blockIdx.x];
@@ -156,48 +236,20 @@ __global__ void __launch_bounds__(kFacThreads) fac_eval_kernel(FacEvalArgs a, in
   const int64_t n = a.ds.n, n_pad = a.ds.n_pad;
   const int64_t row0 = (int64_t)q * a.chunk;
   const int rows = (int)min((int64_t)a.chunk, n_pad - row0);  // a multiple of 256
-  uint64_t* bar = reinterpret_cast<uint64_t*>(smem);
-  int* abort_flag = reinterpret_cast<int*>(smem + 16);
   float* red = reinterpret_cast<float*>(smem + kFacRedOff);
   uint32_t* code_s = reinterpret_cast<uint32_t*>(smem + kFacCodeOff);
   float4* stk = reinterpret_cast<float4*>(smem + kFacStackOff);
-  // staged: column j high parts at xs + 2j * chunk, low parts chunk later; y after the d columns
-  float* xs = reinterpret_cast<float*>(smem + kFacXOff);
-  if (staged) {
-    if (tid == 0) {
-      mbar_init(bar, 1);
-      *abort_flag = 0;
-    }
-    fence_proxy_async();
-    __syncthreads();
-    if (tid == 0) {
-      const uint32_t bytes = (uint32_t)rows * (uint32_t)sizeof(float);
-      fence_proxy_async();
-      mbar_expect_tx(bar, bytes * 2u * (uint32_t)(d + 1));
-      for (int j = 0; j < d; ++j) {
-        tma_bulk_g2s(xs + (size_t)(2 * j) * a.chunk, a.ds.X32 + (int64_t)j * n_pad + row0, bytes, bar);
-        tma_bulk_g2s(xs + (size_t)(2 * j + 1) * a.chunk, a.ds.X32lo + (int64_t)j * n_pad + row0, bytes, bar);
-      }
-      tma_bulk_g2s(xs + (size_t)(2 * d) * a.chunk, a.ds.y32 + row0, bytes, bar);
-      tma_bulk_g2s(xs + (size_t)(2 * d + 1) * a.chunk, a.ds.y32lo + row0, bytes, bar);
-    }
-  }
   // the group's programs are contiguous: stage them
   const int base = a.meta[grp.x].x;
   const int2 last = a.meta[grp.x + grp.y - 1];
   const int total = last.x + last.y - base;
   for (int i = tid; i < total; i += kFacThreads) code_s[i] = a.code[base + i];
-  if (staged && !mbar_wait_bounded(bar, 0)) atomicExch(abort_flag, 1);
   __syncthreads();
-  if (staged && *abort_flag) {
-    if (tid == 0) atomicOr(a.status, ST_WAIT_TIMEOUT);
-    return;
-  }
-  const float* xh = staged ? xs : a.ds.X32 + row0;
-  const float* xl = staged ? xs + a.chunk : a.ds.X32lo + row0;
-  const int64_t ldx = staged ? 2 * (int64_t)a.chunk : n_pad;
-  const float* yh = staged ? xs + (size_t)(2 * d) * a.chunk : a.ds.y32 + row0;
-  const float* yl = staged ? xs + (size_t)(2 * d + 1) * a.chunk : a.ds.y32lo + row0;
+  const float* xh = a.ds.X32 + row0;
+  const float* xl = a.ds.X32lo + row0;
+  const int64_t ldx = n_pad;
+  const float* yh = a.ds.y32 + row0;
+  const float* yl = a.ds.y32lo + row0;
   const float2* tb = a.F + row0;
   float4* st = stk + (size_t)warp * kMixedStackCap * 32 * 2 + lane;
   for (int i = 0; i < grp.y; ++i) {
@@ -207,35 +259,58 @@ __global__ void __launch_bounds__(kFacThreads) fac_eval_kernel(FacEvalArgs a, in
     dfl ff = dfl_make(0.f, 0.f), fs = ff, fy = ff;
     unsigned long long first = ~0ull;
     bool ok = true;
-    for (int r = 4 * tid; r < rows; r += kFacStep) {
+    for (int r = R * tid; r < rows; r += R * kFacThreads) {
       dfl v[4];
-      ok = eval_fac4(code, mt.y, a.K, a.Klo, xh, xl, ldx, tb, n_pad, r, st, v) && ok;
+      if constexpr (R == 4) {
+        ok = eval_fac4(code, mt.y, a.K, a.Klo, xh, xl, ldx, tb, n_pad, r, st, v) && ok;
+      } else {
+        ok = eval_fac2(code, mt.y, a.K, a.Klo, xh, xl, ldx, tb, n_pad, r, st, v[0], v[1]) && ok;
+        v[2] = v[3] = dfl_make(0.f, 0.f);
+      }
       const int64_t gr = row0 + r;
 #pragma unroll
-      for (int u = 0; u < 4; ++u) {
+      for (int u = 0; u < R; ++u) {
         if (gr + u >= n) v[u] = dfl_make(0.f, 0.f);
         if (v[u].hi != v[u].hi) first = min(first, (unsigned long long)(gr + u));
       }
       *reinterpret_cast<float4*>(a.F + (int64_t)f * n_pad + gr) = make_float4(v[0].hi, v[0].lo, v[1].hi, v[1].lo);
-      *reinterpret_cast<float4*>(a.F + (int64_t)f * n_pad + gr + 2) = make_float4(v[2].hi, v[2].lo, v[3].hi, v[3].lo);
-      const float4 yhv = *reinterpret_cast<const float4*>(yh + r);
-      const float4 ylv = *reinterpret_cast<const float4*>(yl + r);
-      const dfl y[4] = {dfl_make(yhv.x, ylv.x), dfl_make(yhv.y, ylv.y), dfl_make(yhv.z, ylv.z),
-                        dfl_make(yhv.w, ylv.w)};
+      if constexpr (R == 4)
+        *reinterpret_cast<float4*>(a.F + (int64_t)f * n_pad + gr + 2) = make_float4(v[2].hi, v[2].lo, v[3].hi, v[3].lo);
+      dfl y[4];
+      if constexpr (R == 4) {
+        const float4 yhv = *reinterpret_cast<const float4*>(yh + r);
+        const float4 ylv = *reinterpret_cast<const float4*>(yl + r);
+        y[0] = dfl_make(yhv.x, ylv.x);
+        y[1] = dfl_make(yhv.y, ylv.y);
+        y[2] = dfl_make(yhv.z, ylv.z);
+        y[3] = dfl_make(yhv.w, ylv.w);
+      } else {
+        const float2 yhv = *reinterpret_cast<const float2*>(yh + r);
+        const float2 ylv = *reinterpret_cast<const float2*>(yl + r);
+        y[0] = dfl_make(yhv.x, ylv.x);
+        y[1] = dfl_make(yhv.y, ylv.y);
+        y[2] = y[3] = dfl_make(0.f, 0.f);
+      }
       bool fin = dfl_finite(ff.hi) && dfl_finite(fs.hi) && dfl_finite(fy.hi);
 #pragma unroll
-      for (int u = 0; u < 4; ++u) fin = fin && dfl_finite(v[u].hi);
+      for (int u = 0; u < R; ++u) fin = fin && dfl_finite(v[u].hi);
       if (__all_sync(0xffffffffu, fin)) {
         // finite values (the common case): the rows' terms are added first,
         // without the non-finite guards
-        ff = dfl_add_nc(ff, dfl_add_nc(dfl_add_nc(dfl_mul_nc(v[0], v[0]), dfl_mul_nc(v[1], v[1])),
-                                       dfl_add_nc(dfl_mul_nc(v[2], v[2]), dfl_mul_nc(v[3], v[3]))));
-        fs = dfl_add_nc(fs, dfl_add_nc(dfl_add_nc(v[0], v[1]), dfl_add_nc(v[2], v[3])));
-        fy = dfl_add_nc(fy, dfl_add_nc(dfl_add_nc(dfl_mul_nc(v[0], y[0]), dfl_mul_nc(v[1], y[1])),
-                                       dfl_add_nc(dfl_mul_nc(v[2], y[2]), dfl_mul_nc(v[3], y[3]))));
+        dfl sq = dfl_add_nc(dfl_mul_nc(v[0], v[0]), dfl_mul_nc(v[1], v[1]));
+        dfl sv = dfl_add_nc(v[0], v[1]);
+        dfl sy = dfl_add_nc(dfl_mul_nc(v[0], y[0]), dfl_mul_nc(v[1], y[1]));
+        if constexpr (R == 4) {
+          sq = dfl_add_nc(sq, dfl_add_nc(dfl_mul_nc(v[2], v[2]), dfl_mul_nc(v[3], v[3])));
+          sv = dfl_add_nc(sv, dfl_add_nc(v[2], v[3]));
+          sy = dfl_add_nc(sy, dfl_add_nc(dfl_mul_nc(v[2], y[2]), dfl_mul_nc(v[3], y[3])));
+        }
+        ff = dfl_add_nc(ff, sq);
+        fs = dfl_add_nc(fs, sv);
+        fy = dfl_add_nc(fy, sy);
       } else {
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
+        for (int u = 0; u < R; ++u) {
           ff = dfl_add(ff, dfl_mul(v[u], v[u]));
           fs = dfl_add(fs, v[u]);
           fy = dfl_add(fy, dfl_mul(v[u], y[u]));
@@ -397,17 +472,18 @@ __global__ void __launch_bounds__(kResidThreads) ftab_resid_kernel(ResidArgs a) 
 }
 
 // ----------------------------------------------------------- launchers ----
-size_t fac_eval_smem(int d, int chunk, bool staged) {
-  return kFacXOff + (staged ? sizeof(float) * 2 * (size_t)(d + 1) * chunk : 0);
-}
+size_t fac_eval_smem() { return kFacXOff; }
 bool fac_allow_smem() {
-  return cudaFuncSetAttribute(fac_eval_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) ==
-         cudaSuccess;
+  return cudaFuncSetAttribute(fac_eval_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) ==
+             cudaSuccess &&
+         cudaFuncSetAttribute(fac_eval_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) ==
+             cudaSuccess;
 }
-bool launch_fac_eval(const FacEvalArgs& a, int n_groups, int n_chunks, bool staged, cudaStream_t st) {
+bool launch_fac_eval(const FacEvalArgs& a, int n_groups, int n_chunks, bool light, cudaStream_t st) {
   if (n_groups <= 0 || n_chunks <= 0) return true;
-  fac_eval_kernel<<<dim3(n_groups, n_chunks), kFacThreads, fac_eval_smem(a.ds.d, a.chunk, staged), st>>>(
-      a, staged ? 1 : 0);
+  const size_t sm = fac_eval_smem();
+  if (light) fac_eval_kernel<4><<<dim3(n_groups, n_chunks), kFacThreads, sm, st>>>(a);
+  else fac_eval_kernel<2><<<dim3(n_groups, n_chunks), kFacThreads, sm, st>>>(a);
   return cudaGetLastError() == cudaSuccess;
 }
 int pair_row_blocks(int64_t n_pad) { return (int)((n_pad + kPairRows - 1) / kPairRows); }

@@ -12,12 +12,22 @@
 
 namespace rrd {
 
-constexpr int kFacThreads = 256;      // evaluator block: 4 rows per thread
+constexpr int kFacThreads = 256;      // evaluator block: 2 or 4 rows per thread
 constexpr int kFacStep = 4 * kFacThreads;
 constexpr int kFacCodeSmem = 2048;    // program words of one evaluator group in shared memory
 constexpr int kFacGroupMax = 64;      // factors per evaluator group
-constexpr int kFacStageBytes = 74 * 1024;  // largest staged evaluator block: three per SM
-constexpr int kFacChunk = 8192;           // rows per evaluator block (a multiple of kFacStep)
+// Rows per evaluator block (a power of two, multiple of kFacStep): larger
+// chunks spread each block's per-factor reductions over more rows, smaller
+// ones keep the X rows that the resident blocks read within L2; about
+// 24K (rows x features) per block, in [1024, 8192].  Measured per 1M-row
+// round: d = 5, 2048 / 4096 / 8192 rows 56.8 / 52.4 / 51.9 ms; 100k rows,
+// d = 10 (deeper programs): 92.3 / 98.1 / 110.9 ms.  It fixes the grouping
+// of the self sums, so it depends on the data shape only.
+inline int fac_chunk(int d) {
+  int c = 8192;
+  while (c > 1024 && (int64_t)c * (d + 1) > 24576) c >>= 1;
+  return c;
+}
 constexpr int kPairThreads = 256;
 constexpr int kPairBatch = 16;        // partners reduced together
 constexpr int kPairRows = 4096;       // rows per pair-sum / residual block
@@ -65,8 +75,12 @@ struct ResidArgs {
   double* sse;               // [candidate][row block]
 };
 
-bool launch_fac_eval(const FacEvalArgs& a, int n_groups, int n_chunks, bool staged, cudaStream_t st);
-size_t fac_eval_smem(int d, int chunk, bool staged);
+// light: the groups' programs are short and shallow (4 rows per thread);
+// otherwise 2 rows per thread
+bool launch_fac_eval(const FacEvalArgs& a, int n_groups, int n_chunks, bool light, cudaStream_t st);
+// The rows-per-thread class of a table program.
+inline bool fac_light(int code_len, int stack) { return stack <= 1 && code_len <= 16; }
+size_t fac_eval_smem();
 bool fac_allow_smem();
 // Row blocks of the pair sums and the residual pass.
 int pair_row_blocks(int64_t n_pad);

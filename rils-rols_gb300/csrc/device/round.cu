@@ -487,17 +487,32 @@ rrg_status rrg_context::mixed_subround(const rrg_dataset* ds, const int32_t* lis
       rrc::set_error("mixed round: a table program exceeds the evaluator's limits");
       return RRG_E_INVALID;
     }
-  // evaluator groups per level: consecutive columns whose programs fit the shared buffer
+  // evaluator groups per level: consecutive columns of one rows-per-thread
+  // class whose programs fit the shared buffer; per level the light groups
+  // first, then the others
   std::vector<int2> groups;
   std::vector<int32_t> level_groups;  // groups of level L end at level_groups[L]
+  std::vector<int32_t> level_light;   // ... of which the first level_light[L] are light
   for (size_t L = 0, c0 = 0; L < tp.level_end.size(); ++L) {
     const int32_t c1 = tp.level_end[L];
+    std::vector<int2> heavy;
+    int32_t n_light = 0;
     for (int32_t i = (int32_t)c0; i < c1;) {
+      const bool light = fac_light(tp.meta[i].y, tp.stack[i]);
       int32_t j = i, words = 0;
-      while (j < c1 && j - i < kFacGroupMax && words + tp.meta[j].y <= kFacCodeSmem) words += tp.meta[j++].y;
-      groups.push_back(make_int2(i, j - i));
+      while (j < c1 && j - i < kFacGroupMax && words + tp.meta[j].y <= kFacCodeSmem &&
+             fac_light(tp.meta[j].y, tp.stack[j]) == light)
+        words += tp.meta[j++].y;
+      if (light) {
+        groups.push_back(make_int2(i, j - i));
+        ++n_light;
+      } else {
+        heavy.push_back(make_int2(i, j - i));
+      }
       i = j;
     }
+    groups.insert(groups.end(), heavy.begin(), heavy.end());
+    level_light.push_back(n_light);
     level_groups.push_back((int32_t)groups.size());
     c0 = c1;
   }
@@ -562,20 +577,10 @@ rrg_status rrg_context::mixed_subround(const rrg_dataset* ds, const int32_t* lis
     k = e;
   }
   const int32_t n_pairs = n_self + n_cross;
-  // row chunks of kFacChunk rows (the self sums' partials are per chunk); the
-  // evaluator stages X and y (high and low parts) by TMA only while the
-  // staged block still fits three blocks per SM (the register limit), i.e.
-  // for one feature; otherwise it reads them from L2, where they stay
-  // resident (measured at d = 5, n = 1M: staged 1024-row chunks 73 ms per
-  // round, L2 reads of 1024 / 2048 / 4096 / 8192-row chunks 66 / 59 / 55 /
-  // 53 ms: larger chunks spread each block's per-factor reductions over more
-  // rows); pair sums and the residual pass use kPairRows blocks
-  int chunk = kFacChunk;
-  bool staged = fac_eval_smem(ds->d, chunk, true) <= (size_t)kFacStageBytes;
-  if ((ds->n_pad + chunk - 1) / chunk > 65535) {
-    staged = false;
-    chunk = (int)round_up((ds->n_pad + 65534) / 65535, kFacStep);
-  }
+  // row chunks of fac_chunk(d) rows (the self sums' partials are per chunk);
+  // pair sums and the residual pass use kPairRows blocks
+  int chunk = fac_chunk(ds->d);
+  if ((ds->n_pad + chunk - 1) / chunk > 65535) chunk = (int)round_up((ds->n_pad + 65534) / 65535, kFacStep);
   const int64_t n_chunks64 = (ds->n_pad + chunk - 1) / chunk;
   const int n_chunks = (int)n_chunks64;
   const int n_super = pair_row_blocks(ds->n_pad);
@@ -638,12 +643,16 @@ rrg_status rrg_context::mixed_subround(const rrg_dataset* ds, const int32_t* lis
   fa.status = status;
   // one launch per level: a level reads the columns of the levels before it
   for (size_t L = 0, g0 = 0; L < level_groups.size(); ++L) {
+    const int gl = (int)g0 + level_light[L];
     fa.groups = pk.at<const int2>(d_ft, o_groups) + g0;
-    if (!launch_fac_eval(fa, level_groups[L] - (int)g0, n_chunks, staged, stream)) {
+    bool ok = launch_fac_eval(fa, gl - (int)g0, n_chunks, true, stream);
+    fa.groups = pk.at<const int2>(d_ft, o_groups) + gl;
+    ok = ok && launch_fac_eval(fa, level_groups[L] - gl, n_chunks, false, stream);
+    if (!ok) {
       cuda_ok(cudaGetLastError(), "factor evaluation launch");
       return RRG_E_CUDA;
     }
-    ++launches;
+    launches += (gl > (int)g0) + (level_groups[L] > gl);
     g0 = level_groups[L];
   }
   mark_end(P_GRAM, t0);
