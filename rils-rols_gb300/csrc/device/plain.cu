@@ -272,8 +272,9 @@ __device__ __forceinline__ double div_by(double a, double b, double y) {
   const int eb = (int)(bb >> 52);
   const int el = eb + e - 1023 - 53;  // biased exponent of |b| * 2^(E(q1) - 53)
   if (e > 54 && e < 2045 && (qb & 0x000fffffffffffffll) != 0 && el > 1 && el < 2046) {
-    const double lim = __longlong_as_double(bb + ((long long)(e - 1023 - 53) << 52));
-    if (fabs(r1) < lim) return q1;
+    // |r1| < lim on the bit patterns (both non-negative; a NaN r1 compares above)
+    const long long lim = bb + ((long long)(e - 1023 - 53) << 52);
+    if ((__double_as_longlong(r1) & 0x7fffffffffffffffll) < lim) return q1;
   }
   return __ddiv_rn(a, b);
 }
@@ -665,6 +666,7 @@ __global__ void __cluster_dims__(kQrCluster, 1, 1) __launch_bounds__(32 * QrShap
   __shared__ double nupd[KB], ndir[KB];
   __shared__ int perm[KB], rec[KB];
   __shared__ double* colp[KB];
+  __shared__ double ntmp[KB];
   __shared__ int s_nonzero;
   if (threadIdx.x == 0) red.parity = 0;
   cl.sync();  // every CTA of the cluster running before any distributed shared memory access
@@ -808,7 +810,7 @@ __global__ void __cluster_dims__(kQrCluster, 1, 1) __launch_bounds__(32 * QrShap
           qk[s] = j < cnt ? __ldcg(cp[s] + kk) : 0.0;  // row kk, read before CTA 0 rewrites it
           part[s] = 0.0;
         }
-        {
+        if (cp[0]) {  // a warp without columns has no dot share
           int64_t i = kk + 1 + L;
           for (; i + 256 * (U - 1) < rows; i += 256 * U) {
             double vi[U], cv[U][CPW];
@@ -832,36 +834,58 @@ __global__ void __cluster_dims__(kQrCluster, 1, 1) __launch_bounds__(32 * QrShap
           }
         }
         cl_sum_cols<KB, W, CPW>(cl, red, part, cnt, out);
-        // tmp_j += Q[kk, j]; Q[kk, j] -= tau * tmp_j
+        // tmp_j += Q[kk, j]; Q[kk, j] -= tau * tmp_j; -tmp_j to every warp of the CTA
 #pragma unroll
         for (int s = 0; s < CPW; ++s) {
           if (!cp[s]) continue;
           out[s] = __dadd_rn(out[s], qk[s]);
           if (w == 0 && lane == 0) __stcg(cp[s] + kk, __dsub_rn(qk[s], __dmul_rn(tau, out[s])));
+          if (lane == 0) ntmp[wi + s * W] = -out[s];
         }
+        __syncthreads();
+        // element-wise Q[i, j] -= (tau v_i) tmp_j: the lane's rows are dealt to
+        // the CTA's warps as in the division pass (the same thread wrote v_i),
+        // each warp updating every column, so tau v_i is formed once per row
         {
-          int64_t i = kk + 1 + L;
-          for (; i + 256 * (U - 1) < rows; i += 256 * U) {
-            double tv[U], cv[U][CPW];
+          constexpr int UR = 4;
+          int64_t i = kk + 1 + L + 256 * (int64_t)wi;
+          for (; i + 256 * W * (UR - 1) < rows; i += 256 * W * UR) {
+            double t[UR];
 #pragma unroll
-            for (int u = 0; u < U; ++u) {
-              tv[u] = __ldcg(v + i + 256 * u);
+            for (int u = 0; u < UR; ++u) t[u] = __dmul_rn(tau, __ldcg(v + i + 256 * W * u));
+            int j = 0;
+            for (; j + 1 < cnt; j += 2) {
+              double* q0 = colp[c_lo + j] + i;
+              double* q1 = colp[c_lo + j + 1] + i;
+              const double n0 = ntmp[j], n1 = ntmp[j + 1];
+              double a0[UR], a1[UR];
 #pragma unroll
-              for (int s = 0; s < CPW; ++s) cv[u][s] = cp[s] ? __ldcg(cp[s] + i + 256 * u) : 0.0;
+              for (int u = 0; u < UR; ++u) {
+                a0[u] = __ldcg(q0 + 256 * W * u);
+                a1[u] = __ldcg(q1 + 256 * W * u);
+              }
+#pragma unroll
+              for (int u = 0; u < UR; ++u) {
+                __stcg(q0 + 256 * W * u, __fma_rn(t[u], n0, a0[u]));
+                __stcg(q1 + 256 * W * u, __fma_rn(t[u], n1, a1[u]));
+              }
             }
+            if (j < cnt) {
+              double* q0 = colp[c_lo + j] + i;
+              const double n0 = ntmp[j];
+              double a0[UR];
 #pragma unroll
-            for (int u = 0; u < U; ++u) {
-              const double t = __dmul_rn(tau, tv[u]);
+              for (int u = 0; u < UR; ++u) a0[u] = __ldcg(q0 + 256 * W * u);
 #pragma unroll
-              for (int s = 0; s < CPW; ++s)
-                if (cp[s]) __stcg(cp[s] + i + 256 * u, __fma_rn(-t, out[s], cv[u][s]));
+              for (int u = 0; u < UR; ++u) __stcg(q0 + 256 * W * u, __fma_rn(t[u], n0, a0[u]));
             }
           }
-          for (; i < rows; i += 256) {
+          for (; i < rows; i += 256 * W) {
             const double t = __dmul_rn(tau, __ldcg(v + i));
-#pragma unroll
-            for (int s = 0; s < CPW; ++s)
-              if (cp[s]) __stcg(cp[s] + i, __fma_rn(-t, out[s], __ldcg(cp[s] + i)));
+            for (int j = 0; j < cnt; ++j) {
+              double* q = colp[c_lo + j] + i;
+              __stcg(q, __fma_rn(t, ntmp[j], __ldcg(q)));
+            }
           }
         }
       }
