@@ -133,12 +133,14 @@ def cpu_baseline(X, y, trees, sample, threads=None):
     from rils_rols_gb300.fitness import encode
     threads = threads or os.cpu_count() or 1
     ods = pyoracle.OracleDataset(X, y)
-    b = encode(trees[:sample], tuned=True)
+    sample = min(sample, len(trees))
+    idx = np.sort(np.random.default_rng(5).choice(len(trees), sample, replace=False))
+    b = encode([trees[i] for i in idx], tuned=True)
     t = time.perf_counter()
     ods.evaluate(b, threads=threads)
     dt = time.perf_counter() - t
     return {"value": sample / dt, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{sample} of the {len(trees)} candidates at n={len(y)} (oracle/rrg_oracle.c, FP64, "
+            "sample": f"{sample} random candidates of the {len(trees)} at n={len(y)} (oracle/rrg_oracle.c, FP64, "
                       f"{threads} threads, {dt:.1f} s)"}
 
 
@@ -217,7 +219,7 @@ def accuracy(test, ref):
 def run_ours(args):
     import torch
 
-    from rils_rols_gb300.fitness import CERTIFIED, MIXED, PLAIN, Context, encode
+    from rils_rols_gb300.fitness import CERTIFIED, MIXED, PLAIN, Context, encode, tune_report
 
     rank, world = dist_setup()
     local = int(os.environ.get("LOCAL_RANK", "0"))
@@ -284,7 +286,12 @@ def run_ours(args):
     res["phase_ms_per_step"] = {k: v / args.steps for k, v in phase_ms.items() if v > 0}
     res["phase_bytes_per_step"] = {k: v / args.steps for k, v in phase_b.items() if v > 0}
     res["roofline"] = roofline(res["phase_ms_per_step"], res["phase_bytes_per_step"])
+    # secondary throughput: rows x tree nodes per second (nodes of each
+    # candidate tree as submitted, every row)
+    nodes = sum(len(t.split()) for t in trees)
+    res["rows_nodes_per_s"] = nodes * float(args.n) * args.steps * world / t_max
     res["clocks"] = clk.summary()
+    res["autotune"] = tune_report()
     if args.quick:
         print(json.dumps(res))
         return
@@ -529,8 +536,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=N_ROWS)
-    ap.add_argument("--cpu-sample", type=int, default=96)
-    ap.add_argument("--ref-sample", type=int, default=32)
+    ap.add_argument("--cpu-sample", type=int, default=4800)
+    ap.add_argument("--ref-sample", type=int, default=1024)
     ap.add_argument("--unbatched-sample", type=int, default=64)
     ap.add_argument("--quick", action="store_true", help="skip the FP64 comparison and the CPU baseline")
     ap.add_argument("--serve-jobs", type=int, default=8, help="requests of the serving stream (0: no serving leg)")

@@ -260,6 +260,31 @@ int32_t rrg_last_round_timing(const rrg_context* ctx, double* ms, int64_t* launc
  * number of phases written.  No counterpart in the reference. */
 int32_t rrg_last_round_bytes(const rrg_context* ctx, double* bytes, int32_t n);
 
+/* Launch-shape tuner.  Only launch shapes that leave every result bit
+ * unchanged are tuned: the warps per CTA of the FP64 QR by column bucket
+ * (RRG_KNOB_QR_WARPS; buckets 4, 8, 16, 65 columns) and the FP64 evaluator's
+ * blocks per level launch in SM waves (RRG_KNOB_EVAL_WAVES; bucket 0).  With
+ * RRG_TUNE_ON (the default) the first launch of a (knob, bucket, row class
+ * floor(log2 n)) that carries enough work is timed in every shape, and the
+ * fastest is kept for the process (and in the file named by the environment
+ * variable RRG_TUNE_CACHE, when set); RRG_TUNE_OFF uses the built-in shapes.
+ * No counterpart in the reference. */
+#define RRG_TUNE_OFF 0
+#define RRG_TUNE_ON 1
+#define RRG_KNOB_QR_WARPS 0
+#define RRG_KNOB_EVAL_WAVES 1
+rrg_status rrg_tune_set_mode(int32_t mode);
+/* Fix a knob's value in a bucket (value 0 releases it); RRG_E_INVALID for a
+ * knob, bucket or value the kernels are not built for. */
+rrg_status rrg_tune_pin(int32_t knob, int32_t bucket, int32_t value);
+/* Forget every tuned choice and pin. */
+rrg_status rrg_tune_reset(void);
+/* The tuner's choices as text, one line per (knob, bucket, row class) with the
+ * timed shapes ("qr_warps bucket=8 row_class=19 value=4 ms=4:1.2,2:1.4,8:1.3"),
+ * then the pins.  Writes at most cap bytes (NUL-terminated) and returns the
+ * size needed. */
+int64_t rrg_tune_report(char* buf, int64_t cap);
+
 #ifdef __cplusplus
 }
 #endif

@@ -22,11 +22,17 @@ bool launch_plain_qr(int max_cols, int grid, cudaStream_t st, DevBatch b, DevDat
                      const int32_t* list, int cand0, const double* A, double* M, double* S, int tsqr, int nb,
                      double* coefs, rrg_result* res, uint32_t* status, uint8_t* redo, const int32_t* colmap);
 // The direct QR (tsqr = 0, no redo) of each listed candidate on a cluster of
-// eight one-warp CTAs: bit-identical results, a candidate's work spread over
-// eight SMs.
-bool launch_plain_qr_cluster(int max_cols, int n_cand, cudaStream_t st, DevBatch b, DevData ds, const PlainCand* pc,
-                             const int32_t* list, int cand0, const double* A, double* M, double* coefs,
-                             rrg_result* res, uint32_t* status, const int32_t* colmap);
+// eight CTAs of `warps` warps (qr_cluster.cu): bit-identical results for every
+// shape, a candidate's work spread over eight SMs.  warps = 0 takes the
+// bucket's default; a shape the kernel is not built for returns false.
+// count_bytes = false leaves the algorithmic-bytes counter alone (a timing trial).
+bool launch_plain_qr_cluster(int max_cols, int warps, int n_cand, cudaStream_t st, DevBatch b, DevData ds,
+                             const PlainCand* pc, const int32_t* list, int cand0, const double* A, double* M,
+                             double* coefs, rrg_result* res, uint32_t* status, const int32_t* colmap,
+                             bool count_bytes);
+// Warps per CTA the cluster QR is built for in a column bucket, the default
+// first; returns how many (0 for an unknown bucket).
+int qr_warp_variants(int bucket, int* out);
 __global__ void plain_resid_kernel(DevBatch b, DevData ds, const PlainCand* pc, const int32_t* list, int cand0,
                                    const double* A, const double* coefs, double* partial, const int32_t* colmap);
 // partial[c * nb + j]: per-candidate squared-residual partial sums; when

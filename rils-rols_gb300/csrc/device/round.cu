@@ -22,6 +22,7 @@
 #include "mixed.cuh"
 #include "plain.cuh"
 #include "runtime.cuh"
+#include "tune.cuh"
 
 using namespace rrd;
 
@@ -919,17 +920,43 @@ rrg_status rrg_context::run_fp64_table(const rrg_dataset* ds, const std::vector<
     fdev.n_cand = ncol;
     fdev.n_code = (int32_t)fcode.size();
     cudaEvent_t t0 = mark_begin();
-    // one launch (or several of at most 65535 columns) per level
+    // one launch (or several of at most 65535 columns) per level; blocks per
+    // column from the tuner's SM waves (any value gives the same columns)
+    bool wave_trial = false;
+    int waves = tune_pick(TK_EVAL_WAVES, 0, ds->n, &wave_trial);
+    size_t wave_level = 0;  // a trial times the widest level
+    for (size_t L = 0, c0 = 0, widest = 0; L < tp.level_end.size(); c0 = tp.level_end[L++])
+      if ((size_t)tp.level_end[L] - c0 > widest) {
+        widest = (size_t)tp.level_end[L] - c0;
+        wave_level = L;
+      }
     for (size_t L = 0, c0 = 0; L < tp.level_end.size(); ++L) {
       const int32_t c1 = tp.level_end[L];
       const int32_t nl = c1 - (int32_t)c0;
-      const int nb = (int)std::max<int64_t>(
-          1, std::min<int64_t>((4LL * sm_count + nl - 1) / std::max(1, nl), (ds->n + 1023) / 1024));
-      for (int32_t f0 = (int32_t)c0; f0 < c1; f0 += 65535) {
-        const int32_t nfb = std::min<int32_t>(65535, c1 - f0);
-        plain_eval_kernel<<<dim3(nb, nfb), 256, plain_eval_smem(), stream>>>(
-            fdev, dd, pk.at<const PlainCand>(d_ft64, o_fpc), nullptr, f0, F64, F64, nullptr, 0, status);
-        ++launches;
+      auto eval_level = [&](int wv) {
+        const int nb = (int)std::max<int64_t>(
+            1, std::min<int64_t>(((int64_t)wv * sm_count + nl - 1) / std::max(1, nl), (ds->n + 1023) / 1024));
+        for (int32_t f0 = (int32_t)c0; f0 < c1; f0 += 65535) {
+          const int32_t nfb = std::min<int32_t>(65535, c1 - f0);
+          plain_eval_kernel<<<dim3(nb, nfb), 256, plain_eval_smem(), stream>>>(
+              fdev, dd, pk.at<const PlainCand>(d_ft64, o_fpc), nullptr, f0, F64, F64, nullptr, 0, status);
+          ++launches;
+        }
+      };
+      if (wave_trial && L == wave_level && (int64_t)nl * ds->n >= kTuneMinWork) {
+        // re-evaluating a level rewrites the same columns: time every shape
+        int vals[4];
+        float ms[4];
+        const int nv = tune_variants(TK_EVAL_WAVES, 0, vals);
+        for (int v = 0; v < nv; ++v) {
+          rrg_status ts = time_trial([&] { eval_level(vals[v]); }, ms[v]);
+          if (ts != RRG_OK) return ts;
+        }
+        tune_store(TK_EVAL_WAVES, 0, ds->n, vals, ms, nv);
+        wave_trial = false;
+        waves = tune_pick(TK_EVAL_WAVES, 0, ds->n, &wave_trial);
+      } else {
+        eval_level(waves);
       }
       c0 = c1;
     }
@@ -979,23 +1006,58 @@ rrg_status rrg_context::run_fp64_table(const rrg_dataset* ds, const std::vector<
     for (const auto& sb : subs) {
       const int32_t ns = sb.second - sb.first;
       if (ns <= 0) continue;
-      t0 = mark_begin();
-      // one launch per register bucket, side by side on the side streams
-      RRG_CUDA(cudaEventRecord(fork_ev, stream));
-      int used = 0;
+      // register buckets of the sub-batch, each with the tuner's warps per CTA;
+      // a bucket the tuner has no choice for is timed in every shape first, on
+      // the round's stream alone (the factorisation restarts from the table
+      // columns, so a repeat gives the same bits)
+      struct QrRun {
+        int32_t b0, b1;
+        int bk, warps;
+      };
+      std::vector<QrRun> runs;
       for (int32_t b0 = sb.first; b0 < sb.second;) {
         const int bk = bucket(list[pos + b0]);
         int32_t b1 = b0;
         while (b1 < sb.second && bucket(list[pos + b1]) == bk) ++b1;
+        bool trial = false;
+        int warps = tune_pick(TK_QR_WARPS, bk, ds->n, &trial);
+        if (trial && (int64_t)(b1 - b0) * ds->n >= kTuneMinWork) {
+          int vals[4];
+          float ms[4];
+          const int nv = tune_variants(TK_QR_WARPS, bk, vals);
+          for (int v = 0; v < nv; ++v) {
+            bool ok = true;
+            rrg_status ts = time_trial([&] {
+              ok = launch_plain_qr_cluster(bk, vals[v], b1 - b0, stream, dev, dd, d_pcs, d_list, b0, F64, M, coefs,
+                                           res, status, d_cmap, false);
+              ++launches;
+            }, ms[v]);
+            if (!ok) {
+              cuda_ok(cudaGetLastError(), "QR launch");
+              return RRG_E_CUDA;
+            }
+            if (ts != RRG_OK) return ts;
+          }
+          tune_store(TK_QR_WARPS, bk, ds->n, vals, ms, nv);
+          warps = tune_pick(TK_QR_WARPS, bk, ds->n, &trial);
+        }
+        runs.push_back({b0, b1, bk, warps});
+        b0 = b1;
+      }
+      t0 = mark_begin();
+      // one launch per register bucket, side by side on the side streams
+      RRG_CUDA(cudaEventRecord(fork_ev, stream));
+      int used = 0;
+      for (const QrRun& r : runs) {
         cudaStream_t s = side[used % kSide];
         if (used < kSide) RRG_CUDA(cudaStreamWaitEvent(s, fork_ev, 0));
-        if (!launch_plain_qr_cluster(bk, b1 - b0, s, dev, dd, d_pcs, d_list, b0, F64, M, coefs, res, status, d_cmap)) {
+        if (!launch_plain_qr_cluster(r.bk, r.warps, r.b1 - r.b0, s, dev, dd, d_pcs, d_list, r.b0, F64, M, coefs, res,
+                                     status, d_cmap, true)) {
           cuda_ok(cudaGetLastError(), "QR launch");
           return RRG_E_CUDA;
         }
         ++used;
         ++launches;
-        b0 = b1;
       }
       for (int i = 0; i < std::min(used, (int)kSide); ++i) {
         RRG_CUDA(cudaEventRecord(join_ev[i], side[i]));

@@ -517,10 +517,17 @@ rrg_context::~rrg_context() {
   if (done) cudaEventDestroy(done);
   if (stream) cudaStreamDestroy(stream);
   if (fork_ev) cudaEventDestroy(fork_ev);
+  for (cudaEvent_t e : tune_ev)
+    if (e) cudaEventDestroy(e);
   for (int i = 0; i < kSide; ++i) {
     if (join_ev[i]) cudaEventDestroy(join_ev[i]);
     if (side[i]) cudaStreamDestroy(side[i]);
   }
+}
+
+rrg_status rrg_context::trial_error() {
+  rrc::set_error(std::string("launch-shape trial: ") + cudaGetErrorString(cudaGetLastError()));
+  return RRG_E_CUDA;
 }
 
 DevData rrg_dataset::view() const {
@@ -568,6 +575,7 @@ rrg_status rrg_context_create(int32_t device, rrg_context** out) {
   ctx->scratch_budget_bytes = std::min<size_t>((size_t)64 << 30, free_b / 3);
   ctx->table_budget_bytes = std::min<size_t>((size_t)32 << 30, free_b / 5);
   bool side_ok = cudaEventCreateWithFlags(&ctx->fork_ev, cudaEventDisableTiming) == cudaSuccess;
+  side_ok = side_ok && cudaEventCreate(&ctx->tune_ev[0]) == cudaSuccess && cudaEventCreate(&ctx->tune_ev[1]) == cudaSuccess;
   for (int i = 0; i < rrg_context::kSide && side_ok; ++i)
     side_ok = cudaStreamCreateWithFlags(&ctx->side[i], cudaStreamNonBlocking) == cudaSuccess &&
               cudaEventCreateWithFlags(&ctx->join_ev[i], cudaEventDisableTiming) == cudaSuccess;

@@ -58,6 +58,7 @@ struct rrg_context {
   static constexpr int kSide = 4;
   cudaStream_t side[kSide] = {nullptr};
   cudaEvent_t fork_ev = nullptr, join_ev[kSide] = {nullptr};
+  cudaEvent_t tune_ev[2] = {nullptr, nullptr};  // launch-shape trials (timing events)
   // batch staging
   HostBuf h_batch;
   DevBuf d_batch;
@@ -102,6 +103,18 @@ struct rrg_context {
   double last_phase_bytes[P_COUNT] = {0};
   cudaEvent_t mark_begin();
   void mark_end(int phase, cudaEvent_t begin);
+  // device milliseconds of the launches fn() makes on the context stream
+  // (the host waits for them): one shape of a launch-shape trial
+  template <class F>
+  rrg_status time_trial(F&& fn, float& ms) {
+    if (cudaEventRecord(tune_ev[0], stream) != cudaSuccess) return trial_error();
+    fn();
+    if (cudaEventRecord(tune_ev[1], stream) != cudaSuccess || cudaEventSynchronize(tune_ev[1]) != cudaSuccess ||
+        cudaEventElapsedTime(&ms, tune_ev[0], tune_ev[1]) != cudaSuccess)
+      return trial_error();
+    return RRG_OK;
+  }
+  rrg_status trial_error();
 
   rrg_status stage_batch(const rrg_batch* b);
   // plain FP64 over `list` (absolute candidate indices) or over [lo, hi) when list is empty

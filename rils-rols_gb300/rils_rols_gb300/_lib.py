@@ -18,6 +18,8 @@ RRG_PLAIN_FP64, RRG_MIXED, RRG_MIXED_CERTIFIED = 0, 1, 2
 RRG_UNTUNED, RRG_TUNED = 0, 1
 RRG_F_NONFINITE, RRG_F_RANK_DEFICIENT, RRG_F_QR_FALLBACK, RRG_F_VERIFIED_FP64, RRG_F_TOO_LARGE = 1, 2, 4, 8, 16
 RRG_MAX_TERMS = 64
+RRG_TUNE_OFF, RRG_TUNE_ON = 0, 1
+RRG_KNOB_QR_WARPS, RRG_KNOB_EVAL_WAVES = 0, 1
 
 STATUS_NAMES = {0: "RRG_OK", 1: "RRG_E_INVALID", 2: "RRG_E_CUDA", 3: "RRG_E_NO_DEVICE", 4: "RRG_E_TIMEOUT",
                 5: "RRG_E_TOO_LARGE", 6: "RRG_E_OOM", 7: "RRG_E_DEVICE_FAULT"}
@@ -74,7 +76,7 @@ EXPORTS = [
     "rrg_dataset_destroy", "rrg_round_submit", "rrg_round_wait", "rrg_eval", "rrg_predict", "rrg_batch_validate", "rrg_dataset_rows",
     "rrg_dataset_cols", "rrg_last_round_launches", "rrg_last_round_stats", "rrg_context_stream",
     "rrg_context_set_timing", "rrg_last_round_timing", "rrg_last_round_bytes", "rrg_eval_plain_noalloc", "rrg_context_set_limits",
-    "rrg_device_memory",
+    "rrg_device_memory", "rrg_tune_set_mode", "rrg_tune_pin", "rrg_tune_reset", "rrg_tune_report",
     "rrh_create", "rrh_destroy", "rrh_set_backend", "rrh_set_precision", "rrh_fit", "rrh_predict",
     "rrh_model_string", "rrh_model_prefix", "rrh_best_time", "rrh_total_time", "rrh_fit_calls", "rrh_counter",
     "rrh_last_error", "rrh_candidates", "rrh_rewrite", "rrh_encode", "rrh_rebuild",
@@ -113,6 +115,10 @@ def _declare(lib):
         "rrg_eval_plain_noalloc": (i32, [vp, i64, vp, i64, i32, P(Batch), vp, vp, vp]),
         "rrg_context_set_limits": (i32, [vp, i64, i64]),
         "rrg_device_memory": (i32, [i32, P(C.c_int64), P(C.c_int64)]),
+        "rrg_tune_set_mode": (i32, [i32]),
+        "rrg_tune_pin": (i32, [i32, i32, i32]),
+        "rrg_tune_reset": (i32, []),
+        "rrg_tune_report": (i64, [cp, i64]),
         "rrh_create": (vp, [i32, i32, i32, dbl, i32, dbl, i32, i32]),
         "rrh_destroy": (None, [vp]),
         "rrh_set_backend": (i32, [vp, P(Backend)]),

@@ -225,3 +225,47 @@ class Dataset:
 
 def result_dtype() -> np.dtype:
     return _RES_DT
+
+
+# ------------------------------------------------------ launch-shape tuner --
+QR_WARPS = _lib.RRG_KNOB_QR_WARPS
+EVAL_WAVES = _lib.RRG_KNOB_EVAL_WAVES
+
+
+def tune_mode(on: bool) -> None:
+    """Time every result-invariant launch shape on first use (on, the default)
+    or keep the built-in shapes (off)."""
+    lib = _lib.load()
+    check(lib.rrg_tune_set_mode(_lib.RRG_TUNE_ON if on else _lib.RRG_TUNE_OFF), "rrg_tune_set_mode")
+
+
+def tune_pin(knob: int, bucket: int, value: int) -> None:
+    """Fix a knob's value in a bucket (0 releases it)."""
+    lib = _lib.load()
+    check(lib.rrg_tune_pin(knob, bucket, value), "rrg_tune_pin")
+
+
+def tune_reset() -> None:
+    lib = _lib.load()
+    check(lib.rrg_tune_reset(), "rrg_tune_reset")
+
+
+def tune_report() -> list[dict]:
+    """The tuner's choices: knob, bucket, row class, value and the timed shapes (ms)."""
+    lib = _lib.load()
+    need = lib.rrg_tune_report(None, 0)
+    buf = C.create_string_buffer(int(need))
+    lib.rrg_tune_report(buf, need)
+    out = []
+    for line in buf.value.decode().splitlines():
+        parts = line.split()
+        e = {"knob": parts[0]}
+        for kv in parts[1:]:
+            k, v = kv.split("=", 1)
+            if k == "ms":
+                e["ms"] = {int(a): float(b) for a, b in (t.split(":") for t in v.split(","))}
+            else:
+                e[k] = int(v)
+        out.append(e)
+    return out
+

@@ -1,0 +1,114 @@
+"""Launch-shape tuner on the device: every shape of a knob (warps per CTA of
+the FP64 QR by column bucket, FP64 evaluator waves) gives the same bits, and
+the tuner times every shape once per (knob, bucket, row class) and keeps the
+fastest."""
+import numpy as np
+import pytest
+
+from oracle import pyoracle
+from rils_rols_gb300.fitness import (CERTIFIED, EVAL_WAVES, PLAIN, QR_WARPS, Context, encode, tune_mode, tune_pin,
+                                     tune_report, tune_reset)
+
+pytestmark = pytest.mark.gpu
+
+TERMS = ["x0", "x1", "x2", "sin x0", "sin x1", "sin x2", "cos x0", "cos x1", "cos x2", "exp mul c:0.3 x0",
+         "exp mul c:0.3 x1", "exp mul c:0.3 x2", "mul x0 x1", "mul x0 x2", "mul x1 x2", "sqr x0", "sqr x1", "sqr x2",
+         "ln add c:4 x2", "div x0 add c:2 sqr x2", "mul x1 sin x2", "sqrt add c:5 x0", "cos mul x0 x2", "exp x1",
+         "mul x0 cos x1"]
+
+
+def sums(rng, count, lo, hi):
+    out = []
+    for _ in range(count):
+        m = int(rng.integers(lo, hi + 1))
+        t = [TERMS[i] for i in rng.choice(len(TERMS), m, replace=False)]
+        out.append("add " * (m - 1) + " ".join(t))
+    return out
+
+
+@pytest.fixture(scope="module")
+def data():
+    rng = np.random.default_rng(11)
+    n = 400_000
+    X = rng.uniform(-2, 2, (n, 3))
+    y = 1.5 * X[:, 0] * X[:, 1] - np.sin(X[:, 2]) + 0.1 * rng.standard_normal(n)
+    # buckets of k + 1 columns: <= 4 (1-2 terms), <= 8 (3-6), <= 16 (7-14);
+    # over 2 x 152 distinct candidates, so that the batch takes the shared
+    # FP64 table and the cluster QR (fewer go to the tiled QR on tall data)
+    trees = sums(rng, 160, 1, 2) + sums(rng, 160, 3, 6) + sums(rng, 140, 7, 14)
+    return X, y, trees
+
+
+def same(a, b):
+    for k in ("loss", "rmse", "size", "rank", "flags"):
+        assert np.array_equal(a[k], b[k], equal_nan=True), k
+    for ca, cb in zip(a["coefs"], b["coefs"]):
+        assert np.array_equal(ca, cb, equal_nan=True)
+
+
+def test_every_shape_gives_the_same_bits(data):
+    X, y, trees = data
+    ctx = Context(0)
+    ds = ctx.dataset(X, y)
+    batch = encode(trees, tuned=True)
+    try:
+        tune_mode(False)
+        ref = ds.evaluate(batch, PLAIN)
+        for bucket, shapes in ((4, (1, 2, 4)), (8, (2, 4, 8)), (16, (4, 8, 16))):
+            for w in shapes:
+                tune_pin(QR_WARPS, bucket, w)
+                same(ds.evaluate(batch, PLAIN), ref)
+            tune_pin(QR_WARPS, bucket, 0)
+        for wv in (2, 4, 8, 16):
+            tune_pin(EVAL_WAVES, 0, wv)
+            same(ds.evaluate(batch, PLAIN), ref)
+        tune_pin(EVAL_WAVES, 0, 0)
+        # and the oracle agrees on a sample (a few candidates on tall data take
+        # the tiled QR: within 1e-10 relative, as in the parity tests)
+        sub = encode(trees[::9], tuned=True)
+        ora = pyoracle.OracleDataset(X, y).evaluate(sub)
+        dev = ds.evaluate(sub, PLAIN)
+        assert np.array_equal(dev["size"], ora["size"])
+        np.testing.assert_allclose(dev["loss"], ora["loss"], rtol=1e-10, atol=0)
+        np.testing.assert_allclose(dev["rmse"], ora["rmse"], rtol=1e-10, atol=0)
+        # the batch itself (direct QR) against the oracle on the same sample
+        idx = np.arange(0, len(trees), 9)
+        np.testing.assert_allclose(ref["loss"][idx], ora["loss"], rtol=1e-10, atol=0)
+    finally:
+        tune_reset()
+        tune_mode(True)
+        ds.close()
+        ctx.close()
+
+
+def test_tuner_times_every_shape_once(data):
+    X, y, trees = data
+    ctx = Context(0)
+    ds = ctx.dataset(X, y)
+    batch = encode(trees, tuned=True)
+    try:
+        tune_mode(False)
+        ref = ds.evaluate(batch, PLAIN)
+        tune_reset()
+        tune_mode(True)
+        got = ds.evaluate(batch, PLAIN)
+        same(got, ref)
+        rep = {(e["knob"], e["bucket"]): e for e in tune_report()}
+        rc = int(np.floor(np.log2(len(y))))
+        for bucket, shapes in ((4, (1, 2, 4)), (8, (2, 4, 8)), (16, (4, 8, 16))):
+            e = rep[("qr_warps", bucket)]
+            assert e["row_class"] == rc
+            assert set(e["ms"]) == set(shapes) and e["value"] in shapes
+            assert e["ms"][e["value"]] == min(e["ms"].values())
+        assert set(rep[("eval_waves", 0)]["ms"]) == {2, 4, 8, 16}
+        # the choices stand: a second round times nothing new and gives the same bits
+        before = tune_report()
+        same(ds.evaluate(batch, PLAIN), ref)
+        assert tune_report() == before
+        # the certified mixed form runs its FP64 re-scoring through the same tuned launches
+        cert = ds.evaluate(batch, CERTIFIED)
+        assert np.array_equal(cert["size"], ref["size"])
+    finally:
+        tune_reset()
+        ds.close()
+        ctx.close()
