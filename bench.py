@@ -184,17 +184,26 @@ def aggregate(units_per_rank: float, seconds: float, world: int) -> tuple[float,
 
 # ------------------------------------------------------------------- ours --
 def timed_round(ctx, ds, batch, prec, stream, flush):
+    """One round through the C ABI (rrg_round_submit + rrg_round_wait: host
+    staging, every launch, results back in host memory), bracketed by CUDA
+    events on the library's stream after an L2 flush; the results are turned
+    into Python objects after the timed region."""
     import torch
+
+    from rils_rols_gb300.fitness import decode_results, result_dtype
+    res = np.zeros(len(batch), dtype=result_dtype())
+    coefs = np.zeros(max(1, batch.n_coefs), dtype=np.float64)
     with torch.cuda.stream(stream):
         flush.zero_()
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-    out = ds.evaluate(batch, prec)
+    ds.submit(batch, prec, res, coefs)
+    ds.wait()
     with torch.cuda.stream(stream):
         e1.record(stream)
     e1.synchronize()
-    return e0.elapsed_time(e1) / 1e3, out
+    return e0.elapsed_time(e1) / 1e3, decode_results(res, coefs, batch)
 
 
 def fv(r):

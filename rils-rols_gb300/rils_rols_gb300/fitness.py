@@ -95,14 +95,13 @@ def candidates(tree: str, d: int, local_search: bool = True, classification: boo
 
 
 def decode_results(res: np.ndarray, coefs: np.ndarray, batch: EncodedBatch) -> dict:
+    """Per-candidate fields, and each candidate's coefficients as a view into
+    `coefs` (free term last; empty for untuned candidates)."""
     out = {k: res[k].copy() for k in ("loss", "rmse", "size", "rank", "flags")}
-    cl = []
-    for c in batch.cands:
-        if c["mode"] == RRG_TUNED:
-            cl.append(coefs[c["coef_offset"]:c["coef_offset"] + c["n_factors"] + 1].copy())
-        else:
-            cl.append(np.zeros(0))
-    out["coefs"] = cl
+    c = batch.cands
+    lo = c["coef_offset"].astype(np.int64)
+    hi = np.where(c["mode"] == RRG_TUNED, lo + c["n_factors"] + 1, lo)
+    out["coefs"] = [coefs[a:b] for a, b in zip(lo.tolist(), hi.tolist())]
     return out
 
 
