@@ -58,9 +58,9 @@ struct Packer {
     total = (size_t)round_up((int64_t)(total + bytes), 256);
     return off;
   }
-  rrg_status send(HostBuf& h, DevBuf& d, cudaStream_t st) {
+  rrg_status send(HostBuf& h, DevBuf& d, cudaStream_t st, bool wait = true) {
     // the pinned buffer may still feed a copy queued earlier on the stream
-    RRG_CUDA(cudaStreamSynchronize(st));
+    if (wait) RRG_CUDA(cudaStreamSynchronize(st));
     if (!h.reserve(std::max<size_t>(total, 256)) || !d.reserve(std::max<size_t>(total, 256))) {
       rrc::set_error("factor table: staging allocation failed");
       return RRG_E_OOM;
@@ -240,33 +240,52 @@ bool build_table_programs(const std::vector<uint32_t>& lcode, const std::vector<
                           TableProgs& tp, bool share = true) {
   const int32_t nfl = (int32_t)lmeta.size();
   std::vector<PNode> nd;
+  nd.reserve(lcode.size() + 16);
   std::vector<int32_t> froot(nfl);
   for (int32_t l = 0; l < nfl; ++l)
     if (!parse_program(lcode.data() + lmeta[l].x, lmeta[l].y, nd, froot[l])) return false;
-  // canonical keys bottom-up (children precede parents)
-  std::vector<std::string> key(nd.size());
+  // structural class of every node, bottom-up (children precede parents):
+  // equal classes are equal subtrees (features by index, constants by bits)
+  struct ClassKey {
+    uint64_t arg;
+    int32_t a, b;
+    int8_t kind, op;
+    bool operator==(const ClassKey& o) const {
+      return arg == o.arg && a == o.a && b == o.b && kind == o.kind && op == o.op;
+    }
+  };
+  struct ClassHash {
+    size_t operator()(const ClassKey& k) const {
+      uint64_t h = k.arg * 0x9e3779b97f4a7c15ull;
+      h ^= ((uint64_t)(uint32_t)k.a << 32 | (uint32_t)k.b) + 0x7f4a7c159e3779b9ull + (h << 6) + (h >> 2);
+      h ^= ((uint64_t)(uint8_t)k.kind << 8 | (uint8_t)k.op) + (h << 6) + (h >> 2);
+      return (size_t)(h ^ (h >> 29));
+    }
+  };
+  std::unordered_map<ClassKey, int32_t, ClassHash> classes;
+  classes.reserve(nd.size() + 16);
+  std::vector<int32_t> cls(nd.size());
   for (size_t i = 0; i < nd.size(); ++i) {
     const PNode& n = nd[i];
-    std::string& k = key[i];
+    ClassKey k{0, -1, -1, n.kind, 0};
     if (n.kind == 0) {
-      k = "V" + std::to_string(n.arg);
+      k.arg = (uint64_t)n.arg;
     } else if (n.kind == 1) {
-      uint64_t bits;
-      std::memcpy(&bits, consts + n.arg, sizeof bits);
-      k = "C" + std::to_string(bits);
-    } else if (n.kind == 3) {
-      k = "U" + std::to_string(n.op) + "(" + key[n.a] + ")";
+      std::memcpy(&k.arg, consts + n.arg, sizeof k.arg);
     } else {
-      k = "B" + std::to_string(n.op) + "(" + key[n.a] + "," + key[n.b] + ")";
+      k.op = n.op;
+      k.a = cls[n.a];
+      if (n.kind == 4) k.b = cls[n.b];
     }
+    cls[i] = classes.emplace(k, (int32_t)classes.size()).first->second;
   }
   // occurrences of every transcendental subtree
-  std::unordered_map<std::string, int32_t> uses;
+  std::vector<int32_t> uses(classes.size(), 0);
   if (share)
     for (size_t i = 0; i < nd.size(); ++i)
-      if (shared_root(nd[i])) ++uses[key[i]];
+      if (shared_root(nd[i])) ++uses[cls[i]];
   // shared subtrees and their levels (1 + the deepest shared subtree inside)
-  std::unordered_map<std::string, int32_t> aux_index;
+  std::vector<int32_t> aux_index(classes.size(), -1);
   std::vector<int32_t> aux_node, aux_level, aux_of(nd.size(), -1), lvl(nd.size(), 0);
   for (size_t i = 0; i < nd.size(); ++i) {
     const PNode& n = nd[i];
@@ -274,16 +293,13 @@ bool build_table_programs(const std::vector<uint32_t>& lcode, const std::vector<
     if (n.kind >= 3) inner = std::max(inner, lvl[n.a]);
     if (n.kind == 4) inner = std::max(inner, lvl[n.b]);
     lvl[i] = inner;
-    if (share && shared_root(n) && uses[key[i]] >= 2) {
-      auto it = aux_index.find(key[i]);
-      int32_t id;
-      if (it == aux_index.end()) {
+    if (share && shared_root(n) && uses[cls[i]] >= 2) {
+      int32_t id = aux_index[cls[i]];
+      if (id < 0) {
         id = (int32_t)aux_node.size();
-        aux_index.emplace(key[i], id);
+        aux_index[cls[i]] = id;
         aux_node.push_back((int32_t)i);
         aux_level.push_back(inner + 1);
-      } else {
-        id = it->second;
       }
       aux_of[i] = id;
       lvl[i] = aux_level[id];
@@ -517,10 +533,64 @@ rrg_status rrg_context::mixed_subround(const rrg_dataset* ds, const int32_t* lis
     level_groups.push_back((int32_t)groups.size());
     c0 = c1;
   }
+  // row chunks of fac_chunk(d) rows (the self sums' partials are per chunk);
+  // pair sums and the residual pass use kPairRows blocks
+  const int32_t n_self = 3 * ncol;
+  int chunk = fac_chunk(ds->d);
+  if ((ds->n_pad + chunk - 1) / chunk > 65535) chunk = (int)round_up((ds->n_pad + 65534) / 65535, kFacStep);
+  const int64_t n_chunks64 = (ds->n_pad + chunk - 1) / chunk;
+  const int n_chunks = (int)n_chunks64;
+  const int n_super = pair_row_blocks(ds->n_pad);
+  if (!d_F.reserve(sizeof(float2) * (size_t)ncol * ds->n_pad) ||
+      !d_P.reserve(sizeof(float2) * (size_t)n_chunks * std::max(1, n_self)) ||
+      !d_fnan.reserve(sizeof(unsigned long long) * ncol)) {
+    rrc::set_error("mixed round: factor table allocation failed");
+    return RRG_E_OOM;
+  }
+  // the table programs go up first and the evaluator starts; the host builds
+  // the pair map while it runs
+  Packer pkt;
+  const size_t o_tcode = pkt.add(tp.code.data(), sizeof(uint32_t) * tp.code.size());
+  const size_t o_tmeta = pkt.add(tp.meta.data(), sizeof(int2) * tp.meta.size());
+  const size_t o_groups = pkt.add(groups.data(), sizeof(int2) * groups.size());
+  rrg_status pst = pkt.send(h_ftp, d_ftp, stream);
+  if (pst != RRG_OK) return pst;
+  float2* F = static_cast<float2*>(d_F.ptr);
+  float2* Pself = static_cast<float2*>(d_P.ptr);  // [chunk][3 ncol]
+  unsigned long long* fnan = static_cast<unsigned long long*>(d_fnan.ptr);
+  uint32_t* status = static_cast<uint32_t*>(d_status.ptr);
+  RRG_CUDA(cudaMemsetAsync(fnan, 0x7f, sizeof(unsigned long long) * ncol, stream));
+
+  cudaEvent_t t0 = mark_begin();
+  FacEvalArgs fa;
+  fa.ds = dd;
+  fa.code = pkt.at<const uint32_t>(d_ftp, o_tcode);
+  fa.meta = pkt.at<const int2>(d_ftp, o_tmeta);
+  fa.K = dev.consts32;
+  fa.Klo = dev.consts32lo;
+  fa.chunk = chunk;
+  fa.F = F;
+  fa.P = Pself;
+  fa.n_pairs = n_self;
+  fa.fnan = fnan;
+  fa.status = status;
+  // one launch per level: a level reads the columns of the levels before it
+  for (size_t L = 0, g0 = 0; L < level_groups.size(); ++L) {
+    const int gl = (int)g0 + level_light[L];
+    fa.groups = pkt.at<const int2>(d_ftp, o_groups) + g0;
+    bool ok = launch_fac_eval(fa, gl - (int)g0, n_chunks, true, stream);
+    fa.groups = pkt.at<const int2>(d_ftp, o_groups) + gl;
+    ok = ok && launch_fac_eval(fa, level_groups[L] - gl, n_chunks, false, stream);
+    if (!ok) {
+      cuda_ok(cudaGetLastError(), "factor evaluation launch");
+      return RRG_E_CUDA;
+    }
+    launches += (gl > (int)g0) + (level_groups[L] > gl);
+    g0 = level_groups[L];
+  }
   // pair map over table columns: self pairs 3t..3t+2, cross pairs oriented
   // so that `a` is the rarer factor (its partners are then the widely shared
   // ones, hot in L2)
-  const int32_t n_self = 3 * ncol;
   std::unordered_map<uint64_t, int32_t> cmap;
   cmap.reserve((size_t)cnt * 4 + 16);
   std::vector<std::pair<int32_t, int32_t>> cross;
@@ -578,48 +648,34 @@ rrg_status rrg_context::mixed_subround(const rrg_dataset* ds, const int32_t* lis
     k = e;
   }
   const int32_t n_pairs = n_self + n_cross;
-  // row chunks of fac_chunk(d) rows (the self sums' partials are per chunk);
-  // pair sums and the residual pass use kPairRows blocks
-  int chunk = fac_chunk(ds->d);
-  if ((ds->n_pad + chunk - 1) / chunk > 65535) chunk = (int)round_up((ds->n_pad + 65534) / 65535, kFacStep);
-  const int64_t n_chunks64 = (ds->n_pad + chunk - 1) / chunk;
-  const int n_chunks = (int)n_chunks64;
-  const int n_super = pair_row_blocks(ds->n_pad);
-  const int n_prow = std::max(n_chunks, n_super);
-  if (!d_F.reserve(sizeof(float2) * (size_t)ncol * ds->n_pad) ||
-      !d_P.reserve(sizeof(float2) * (size_t)n_prow * std::max(1, n_pairs)) ||
-      !d_psum.reserve(sizeof(double) * std::max(1, n_pairs)) || !d_fprobe.reserve(sizeof(FacProbe) * nfl) ||
-      !d_fnan.reserve(sizeof(unsigned long long) * ncol)) {
+  if (!d_Pc.reserve(sizeof(float2) * (size_t)n_super * std::max(1, n_cross)) ||
+      !d_psum.reserve(sizeof(double) * std::max(1, n_pairs)) || !d_fprobe.reserve(sizeof(FacProbe) * nfl)) {
     rrc::set_error("mixed round: factor table allocation failed");
     return RRG_E_OOM;
   }
   Packer pk;
   const size_t o_code = pk.add(lcode.data(), sizeof(uint32_t) * lcode.size());
   const size_t o_meta = pk.add(lmeta.data(), sizeof(int2) * lmeta.size());
-  const size_t o_tcode = pk.add(tp.code.data(), sizeof(uint32_t) * tp.code.size());
-  const size_t o_tmeta = pk.add(tp.meta.data(), sizeof(int2) * tp.meta.size());
   const size_t o_fcol = pk.add(tp.fcol.data(), sizeof(int32_t) * tp.fcol.size());
   const size_t o_ccol = pk.add(cand_col.data(), sizeof(int32_t) * cand_col.size());
-  const size_t o_groups = pk.add(groups.data(), sizeof(int2) * groups.size());
   const size_t o_units = pk.add(units.data(), sizeof(int4) * units.size());
   const size_t o_partner = pk.add(partner.data(), sizeof(int32_t) * partner.size());
   const size_t o_pair = pk.add(pair_of.data(), sizeof(int32_t) * pair_of.size());
   const size_t o_list = pk.add(list, sizeof(int32_t) * cnt);
   const size_t o_cfac = pk.add(cand_fac.data(), sizeof(int32_t) * cand_fac.size());
   const size_t o_list2 = pk.add(nullptr, sizeof(int32_t) * cnt);  // filled after the solve
-  rrg_status pst = pk.send(h_ft, d_ft, stream);
+  // its pinned buffer fed no copy since the last read-back: no need to wait
+  // for the evaluator
+  pst = pk.send(h_ft, d_ft, stream, false);
   if (pst != RRG_OK) return pst;
   const uint32_t* d_code = pk.at<const uint32_t>(d_ft, o_code);
   const int2* d_meta = pk.at<const int2>(d_ft, o_meta);
   const int32_t* d_list = pk.at<const int32_t>(d_ft, o_list);
   const int32_t* d_cfac = pk.at<const int32_t>(d_ft, o_cfac);
   int32_t* d_list2 = pk.at<int32_t>(d_ft, o_list2);
-  float2* F = static_cast<float2*>(d_F.ptr);
-  float2* P = static_cast<float2*>(d_P.ptr);
+  float2* Pcross = static_cast<float2*>(d_Pc.ptr);  // [row block][cross pairs]
   double* psum = static_cast<double*>(d_psum.ptr);
   FacProbe* fprobe = static_cast<FacProbe*>(d_fprobe.ptr);
-  unsigned long long* fnan = static_cast<unsigned long long*>(d_fnan.ptr);
-  uint32_t* status = static_cast<uint32_t*>(d_status.ptr);
   const int fb_cap = std::max(1, (int)host_cands.size());
   const size_t back_bytes = sizeof(int32_t) * (fb_cap + 1 + kFbReasons) + (size_t)fb_cap;
   int32_t* fallback = static_cast<int32_t*>(d_fallback.ptr);
@@ -627,35 +683,6 @@ rrg_status rrg_context::mixed_subround(const rrg_dataset* ds, const int32_t* lis
   uint8_t* pass2 = reinterpret_cast<uint8_t*>(fallback + fb_cap + 1 + kFbReasons);
   RRG_CUDA(cudaMemsetAsync(d_fallback.ptr, 0, back_bytes, stream));
   RRG_CUDA(cudaMemsetAsync(d_cert_e.ptr, 0xff, sizeof(double) * fb_cap, stream));  // NaN: no check
-  RRG_CUDA(cudaMemsetAsync(fnan, 0x7f, sizeof(unsigned long long) * ncol, stream));
-
-  cudaEvent_t t0 = mark_begin();
-  FacEvalArgs fa;
-  fa.ds = dd;
-  fa.code = pk.at<const uint32_t>(d_ft, o_tcode);
-  fa.meta = pk.at<const int2>(d_ft, o_tmeta);
-  fa.K = dev.consts32;
-  fa.Klo = dev.consts32lo;
-  fa.chunk = chunk;
-  fa.F = F;
-  fa.P = P;
-  fa.n_pairs = n_pairs;
-  fa.fnan = fnan;
-  fa.status = status;
-  // one launch per level: a level reads the columns of the levels before it
-  for (size_t L = 0, g0 = 0; L < level_groups.size(); ++L) {
-    const int gl = (int)g0 + level_light[L];
-    fa.groups = pk.at<const int2>(d_ft, o_groups) + g0;
-    bool ok = launch_fac_eval(fa, gl - (int)g0, n_chunks, true, stream);
-    fa.groups = pk.at<const int2>(d_ft, o_groups) + gl;
-    ok = ok && launch_fac_eval(fa, level_groups[L] - gl, n_chunks, false, stream);
-    if (!ok) {
-      cuda_ok(cudaGetLastError(), "factor evaluation launch");
-      return RRG_E_CUDA;
-    }
-    launches += (gl > (int)g0) + (level_groups[L] > gl);
-    g0 = level_groups[L];
-  }
   mark_end(P_GRAM, t0);
   phase_bytes[P_GRAM] += (double)ds->n * 8.0 * (double)(ds->d + 1 + ncol);
   t0 = mark_begin();
@@ -665,9 +692,9 @@ rrg_status rrg_context::mixed_subround(const rrg_dataset* ds, const int32_t* lis
   pa.units = pk.at<const int4>(d_ft, o_units);
   pa.n_units = (int32_t)units.size();
   pa.partner = pk.at<const int32_t>(d_ft, o_partner);
-  pa.P = P;
-  pa.n_pairs = n_pairs;
-  pa.cross0 = n_self;
+  pa.P = Pcross;
+  pa.n_pairs = n_cross;
+  pa.cross0 = 0;
   if (!launch_pair_sum(pa, n_super, stream)) {
     cuda_ok(cudaGetLastError(), "pair sum launch");
     return RRG_E_CUDA;
@@ -675,8 +702,8 @@ rrg_status rrg_context::mixed_subround(const rrg_dataset* ds, const int32_t* lis
   mark_end(P_PAIRS, t0);
   phase_bytes[P_PAIRS] += (double)ds->n * 8.0 * (double)ncol;
   t0 = mark_begin();
-  if (!launch_pair_reduce(P, n_pairs, n_chunks, 0, n_self, psum, stream) ||
-      !launch_pair_reduce(P, n_pairs, n_super, n_self, n_pairs, psum, stream) ||
+  if (!launch_pair_reduce(Pself, n_self, n_chunks, 0, n_self, psum, stream) ||
+      !launch_pair_reduce(Pcross, n_cross, n_super, 0, n_cross, psum + n_self, stream) ||
       !launch_fac_probe(d_code, d_meta, nfl, dev.consts, dev.consts32, dev.consts32lo, dd, fprobe, stream) ||
       !launch_cand_probe(dev.cands, d_list, cnt, d_cfac, pk.at<const int32_t>(d_ft, o_fcol), fprobe, fnan,
                          static_cast<ProbeOut*>(d_probe.ptr), static_cast<int64_t*>(d_nanrow.ptr), stream)) {

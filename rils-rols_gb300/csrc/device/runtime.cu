@@ -504,9 +504,11 @@ rrg_context::~rrg_context() {
   d_cert_e.release();
   h_mlist.release();
   h_fallback.release();
-  for (DevBuf* bf : {&d_ft, &d_ft64, &d_F, &d_P, &d_psum, &d_fprobe, &d_fnan, &d_F64, &d_M, &d_colstat, &d_gram})
+  for (DevBuf* bf : {&d_ft, &d_ftp, &d_ft64, &d_F, &d_P, &d_Pc, &d_psum, &d_fprobe, &d_fnan, &d_F64, &d_M, &d_colstat,
+                      &d_gram})
     bf->release();
   h_ft.release();
+  h_ftp.release();
   h_ft64.release();
   h_batch.release();
   h_res.release();

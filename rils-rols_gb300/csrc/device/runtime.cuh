@@ -73,8 +73,8 @@ struct rrg_context {
   HostBuf h_mlist, h_fallback;
   // factor tables
   FactorTable ft;
-  HostBuf h_ft, h_ft64;
-  DevBuf d_ft, d_ft64, d_F, d_P, d_psum, d_fprobe, d_fnan, d_F64, d_M, d_colstat, d_gram;
+  HostBuf h_ft, h_ftp, h_ft64;
+  DevBuf d_ft, d_ftp, d_ft64, d_F, d_P, d_Pc, d_psum, d_fprobe, d_fnan, d_F64, d_M, d_colstat, d_gram;
   // results
   DevBuf d_res, d_coefs, d_status;
   HostBuf h_res, h_coefs, h_status;
