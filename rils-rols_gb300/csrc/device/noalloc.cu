@@ -276,7 +276,7 @@ extern "C" rrg_status rrg_eval_plain_noalloc(const double* X_col, int64_t ld, co
   // residual, fitness), pointed at the scratch
   const int nb_eval = (int)std::min<int64_t>(1024, std::max<int64_t>(1, (n + 1023) / 1024));
   plain_eval_kernel<<<dim3(nb_eval, 1), 256, plain_eval_smem(), st>>>(db, dd, dpc, nullptr, 0, arena, arena,
-                                                                       nullptr, 0, status);
+                                                                       nullptr, 0, status, nullptr);
   launch_plain_qr((int)k + 1, 1, st, db, dd, dpc, nullptr, 0, arena, arena, nullptr, 0, 1, cf, result, status, nullptr,
                   nullptr);
   plain_resid_kernel<<<dim3(nb_res, 1), 256, 0, st>>>(db, dd, dpc, nullptr, 0, arena, cf, partial, nullptr);

@@ -183,7 +183,7 @@ __device__ void apply_householder(double* Q, int64_t ld, int64_t rows, int kk, d
 // grid (blocks per candidate, candidates); rows of block b: [b*n/nb, (b+1)*n/nb)
 __global__ void __launch_bounds__(256) plain_eval_kernel(DevBatch b, DevData ds, const PlainCand* pc,
                                                           const int32_t* list, int cand0, double* A, double* M,
-                                                          double* S, int tsqr, uint32_t* status) {
+                                                          double* S, int tsqr, uint32_t* status, ColStat* cst) {
   extern __shared__ double smem[];
   const int c = list ? list[cand0 + blockIdx.y] : cand0 + blockIdx.y;
   const rrg_cand cd = b.cands[c];
@@ -197,6 +197,35 @@ __global__ void __launch_bounds__(256) plain_eval_kernel(DevBatch b, DevData ds,
   __syncthreads();
   const uint32_t* code = staged ? code_s : b.code + cd.code_offset;
   double* Ac = A + pc[c].a_col * ds.n_pad;
+  if (cst) {
+    // one-column table programs: the column's statistics on the way
+    uint32_t f = 0;
+    unsigned long long mx = 0;
+    for (int64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
+      run_row64(code, cd.code_len, b.consts, ds, r, st, Ac, A, status);
+      const double v = Ac[r];
+      const double a = fabs(v);
+      if (v != v) {
+        f |= kCsNaN;
+      } else if (!(a <= 1.35e154)) {  // infinite, or its square overflows
+        f |= kCsBig;
+      } else {
+        const unsigned long long bits = (unsigned long long)__double_as_longlong(a);
+        mx = bits > mx ? bits : mx;
+      }
+      if (r >= 1 && !(a <= 1e-150)) f |= kCsTail;
+    }
+    f = __reduce_or_sync(0xffffffffu, f);
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long t = __shfl_xor_sync(0xffffffffu, mx, o);
+      mx = t > mx ? t : mx;
+    }
+    if ((threadIdx.x & 31) == 0) {
+      if (f) atomicOr(&cst[pc[c].a_col].flags, f);
+      if (mx) atomicMax(&cst[pc[c].a_col].maxabs, mx);
+    }
+    return;
+  }
   for (int64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x)
     run_row64(code, cd.code_len, b.consts, ds, r, st, Ac, A, status);
   if (!tsqr || cd.mode != RRG_TUNED) return;
@@ -644,34 +673,6 @@ __global__ void finalize_kernel(DevBatch b, DevData ds, const int32_t* list, int
 __global__ void clear_results_kernel(const int32_t* list, int n, rrg_result* res) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) res[list[i]] = rrg_result{};
-}
-
-__global__ void __launch_bounds__(256) colstat_kernel(const double* T, int64_t n, int64_t n_pad, ColStat* out) {
-  const double* col = T + (int64_t)blockIdx.y * n_pad;
-  uint32_t f = 0;
-  unsigned long long mx = 0;
-  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
-    const double v = col[r];
-    const double a = fabs(v);
-    if (v != v) {
-      f |= kCsNaN;
-    } else if (!(a <= 1.35e154)) {  // infinite, or its square overflows
-      f |= kCsBig;
-    } else {
-      const unsigned long long bits = (unsigned long long)__double_as_longlong(a);
-      mx = bits > mx ? bits : mx;
-    }
-    if (r >= 1 && !(a <= 1e-150)) f |= kCsTail;
-  }
-  f = __reduce_or_sync(0xffffffffu, f);
-  for (int o = 16; o > 0; o >>= 1) {
-    const unsigned long long t = __shfl_xor_sync(0xffffffffu, mx, o);
-    mx = t > mx ? t : mx;
-  }
-  if ((threadIdx.x & 31) == 0) {
-    if (f) atomicOr(&out[blockIdx.y].flags, f);
-    if (mx) atomicMax(&out[blockIdx.y].maxabs, mx);
-  }
 }
 
 // The outcome of the column-pivoted QR (ColPivHouseholderQR.h:482-608, as

@@ -6,9 +6,12 @@ namespace rrd {
 
 constexpr int kMaxCodeSmem = 4096;  // program words staged in shared memory per block
 
+struct ColStat;
 // `list` (may be NULL) maps grid positions to candidates: candidate = list[cand0 + i].
+// cst (may be NULL; one-column programs, no TSQR): column statistics of every
+// written column, merged into cst[pc[c].a_col] (zeroed before the launch).
 __global__ void plain_eval_kernel(DevBatch b, DevData ds, const PlainCand* pc, const int32_t* list, int cand0,
-                                  double* A, double* M, double* S, int tsqr, uint32_t* status);
+                                  double* A, double* M, double* S, int tsqr, uint32_t* status, ColStat* cst);
 // tsqr = 1: pivoted QR of the stacked slice triangles, and redo[c] = 1 when
 // the candidate must be re-solved directly; tsqr = 0 with redo != NULL: only
 // the flagged candidates, by the direct QR on [A | 1 | y].
@@ -43,8 +46,8 @@ __global__ void finalize_kernel(DevBatch b, DevData ds, const int32_t* list, int
 
 __global__ void clear_results_kernel(const int32_t* list, int n, rrg_result* res);
 
-// Column statistics of an FP64 table, for deciding the column-pivoted QR's
-// outcome on non-finite data without running it.
+// Column statistics of an FP64 table (gathered by plain_eval_kernel), for
+// deciding the column-pivoted QR's outcome on non-finite data without running it.
 struct ColStat {
   uint32_t flags;       // kCs* bits
   uint32_t pad;
@@ -53,8 +56,6 @@ struct ColStat {
 constexpr uint32_t kCsNaN = 1;   // a NaN value: the column's norm is NaN
 constexpr uint32_t kCsBig = 2;   // an infinite value or one whose square overflows
 constexpr uint32_t kCsTail = 4;  // a row after the first with |value| > 1e-150 or non-finite
-// grid (row blocks, columns); out zeroed before the launch
-__global__ void colstat_kernel(const double* T, int64_t n, int64_t n_pad, ColStat* out);
 // One thread per listed tuned candidate: where the QR's result is certain to
 // be all-NaN coefficients at full rank (the fitness sentinel), writes that
 // result, sets pc[c].pad = 1 (the QR and residual kernels skip it) and

@@ -946,6 +946,15 @@ rrg_status rrg_context::run_fp64_table(const rrg_dataset* ds, const std::vector<
     fdev.code = pk.at<const uint32_t>(d_ft64, o_fcode);
     fdev.n_cand = ncol;
     fdev.n_code = (int32_t)fcode.size();
+    // column statistics of the table, gathered by the evaluator, then the
+    // candidates whose QR outcome is certainly the all-NaN sentinel (their
+    // QR and residual work is skipped)
+    if (!d_colstat.reserve(sizeof(ColStat) * (size_t)std::max(1, ncol))) {
+      rrc::set_error("FP64 round: scratch allocation failed");
+      return RRG_E_OOM;
+    }
+    ColStat* cst = static_cast<ColStat*>(d_colstat.ptr);
+    RRG_CUDA(cudaMemsetAsync(cst, 0, sizeof(ColStat) * (size_t)std::max(1, ncol), stream));
     cudaEvent_t t0 = mark_begin();
     // one launch (or several of at most 65535 columns) per level; blocks per
     // column from the tuner's SM waves (any value gives the same columns)
@@ -966,7 +975,7 @@ rrg_status rrg_context::run_fp64_table(const rrg_dataset* ds, const std::vector<
         for (int32_t f0 = (int32_t)c0; f0 < c1; f0 += 65535) {
           const int32_t nfb = std::min<int32_t>(65535, c1 - f0);
           plain_eval_kernel<<<dim3(nb, nfb), 256, plain_eval_smem(), stream>>>(
-              fdev, dd, pk.at<const PlainCand>(d_ft64, o_fpc), nullptr, f0, F64, F64, nullptr, 0, status);
+              fdev, dd, pk.at<const PlainCand>(d_ft64, o_fpc), nullptr, f0, F64, F64, nullptr, 0, status, cst);
           ++launches;
         }
       };
@@ -986,23 +995,6 @@ rrg_status rrg_context::run_fp64_table(const rrg_dataset* ds, const std::vector<
         eval_level(waves);
       }
       c0 = c1;
-    }
-    // column statistics of the table, then the candidates whose QR outcome
-    // is certainly the all-NaN sentinel (their QR and residual work is skipped)
-    if (!d_colstat.reserve(sizeof(ColStat) * (size_t)std::max(1, ncol))) {
-      rrc::set_error("FP64 round: scratch allocation failed");
-      return RRG_E_OOM;
-    }
-    ColStat* cst = static_cast<ColStat*>(d_colstat.ptr);
-    RRG_CUDA(cudaMemsetAsync(cst, 0, sizeof(ColStat) * (size_t)std::max(1, ncol), stream));
-    {
-      const int bx = (int)std::max<int64_t>(
-          1, std::min<int64_t>((4LL * sm_count + ncol - 1) / std::max(1, ncol), (ds->n + 2047) / 2048));
-      for (int32_t f0 = 0; f0 < ncol; f0 += 65535) {
-        const int32_t nfb = std::min<int32_t>(65535, ncol - f0);
-        colstat_kernel<<<dim3(bx, nfb), 256, 0, stream>>>(F64 + (int64_t)f0 * ds->n_pad, ds->n, ds->n_pad, cst + f0);
-        ++launches;
-      }
     }
     sentinel_classify_kernel<<<(ng + 127) / 128, 128, 0, stream>>>(dev, d_list, 0, ng,
                                                                    pk.at<PlainCand>(d_ft64, o_pcs), d_cmap, cst,

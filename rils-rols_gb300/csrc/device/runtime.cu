@@ -311,7 +311,7 @@ rrg_status rrg_context::run_plain(const rrg_dataset* ds, int32_t lo, int32_t hi,
     const int32_t ns = sb.e - sb.p;
     cudaEvent_t t0 = mark_begin();
     plain_eval_kernel<<<dim3(sb.nb, ns), 256, plain_eval_smem(), stream>>>(dev, dd, pc, dl, sb.p, A, A, S,
-                                                                            sb.tsqr ? 1 : 0, status);
+                                                                            sb.tsqr ? 1 : 0, status, nullptr);
     mark_end(P_PLAIN_EVAL, t0);
     ++launches;
     if (predict_only) continue;
