@@ -6,18 +6,26 @@
  * so that the same input gives the same bits on x86, Arm and GB300.  This is
  * what lets the FP64 device path reproduce the CPU oracle bit for bit.
  * Methods (all published; constants are mathematical constants computed for
- * this file, rounded to double):
- *   exp  Cody & Waite argument reduction x = k ln2 + r (ln2 split in a 32-bit
- *        head and a tail), Taylor polynomial of e^r - 1 to degree 13,
- *        scaling by 2^k through the exponent field;
- *   log  x = m 2^e with m in (sqrt(1/2), sqrt(2)], log m = 2 atanh(s),
- *        s = (m-1)/(m+1), atanh series to s^23;
+ * this file by gen_rr_math_tables.py, rounded to double):
+ *   exp  table-driven (Tang): x = (64 k' + j) ln2/64 + r with ln2/64 split in
+ *        a 36-bit head and a tail (Cody & Waite), |r| <= ln2/128; e^x =
+ *        2^k' 2^(j/64) (1 + p(r)), 2^(j/64) from a table of double-double
+ *        values, p the Taylor polynomial of e^r - 1 to degree 6; scaling by
+ *        2^k' through the exponent field;
+ *   log  table-driven (Tang): x = m 2^e with m in [sqrt(1/2), sqrt(2)), c =
+ *        1 + j/64 the grid point nearest m, log x = e ln2 + log c +
+ *        log1p(r), r = (m - c)/c formed as r_hi + r_lo (m - c exact, r_hi =
+ *        (m - c) RN(1/c), r_lo from the exact remainder), log1p by its
+ *        Taylor series to degree 9; e ln2 + log c summed exactly (heads on
+ *        a 2^-42 grid), the rest by Fast2Sum;
  *   sin, cos  Cody & Waite reduction by pi/2 (three-term split, FMA) for
  *        |x| < 2^20, Payne & Hanek reduction with the binary expansion of 2/pi
  *        above; Taylor polynomials of sin (to r^19) and cos (to r^20) on
  *        |r| <= pi/4 with a first-order correction for the reduced tail;
- *   pow  exp(b log|a|) with the sign and special-value rules of C's pow.
- * Accuracy: a few ulp (checked against the host libm by the CPU tests).
+ *   pow  exp(b log|a|) with log|a| and the product b log|a| carried as
+ *        double-doubles, and the sign and special-value rules of C's pow.
+ * Accuracy: exp, log and pow within 1 ulp (measured 0.51), sin and cos within
+ * 2 ulp (checked against 60-digit arithmetic by tests/test_rr_math_cpu.py).
  */
 #ifndef RR_MATH_H
 #define RR_MATH_H
@@ -78,76 +86,257 @@ RRM_FN double rrm_rint(double x) {
   return RRM_SUB(RRM_ADD(x, shift), shift);
 }
 
+/* ------------------------------------------------------ exp / log tables -- */
+/* exp: x = k ln2/64 + r; 64/ln2, ln2/64 = C1 + C2 (C1: 36 bits) */
+#define RR_EXP_INV_L64 0x1.71547652b82fep+6
+#define RR_EXP_C1 0x1.62e42fefa0000p-7
+#define RR_EXP_C2 0x1.cf79abc9e3b3ap-46
+/* 1/n!, n = 2..6 */
+#define RR_EXP_F2 0x1.0000000000000p-1
+#define RR_EXP_F3 0x1.5555555555555p-3
+#define RR_EXP_F4 0x1.5555555555555p-5
+#define RR_EXP_F5 0x1.1111111111111p-7
+#define RR_EXP_F6 0x1.6c16c16c16c17p-10
+/* 2^(j/64) = hi + lo, j = 0..63 */
+#define RR_EXP_TAB { \
+  {0x1.0000000000000p+0, 0x0.0p+0}, \
+  {0x1.02c9a3e778061p+0, -0x1.19083535b085dp-56}, \
+  {0x1.059b0d3158574p+0, 0x1.d73e2a475b465p-55}, \
+  {0x1.0874518759bc8p+0, 0x1.186be4bb284ffp-57}, \
+  {0x1.0b5586cf9890fp+0, 0x1.8a62e4adc610bp-54}, \
+  {0x1.0e3ec32d3d1a2p+0, 0x1.03a1727c57b53p-59}, \
+  {0x1.11301d0125b51p+0, -0x1.6c51039449b3ap-54}, \
+  {0x1.1429aaea92de0p+0, -0x1.32fbf9af1369ep-54}, \
+  {0x1.172b83c7d517bp+0, -0x1.19041b9d78a76p-55}, \
+  {0x1.1a35beb6fcb75p+0, 0x1.e5b4c7b4968e4p-55}, \
+  {0x1.1d4873168b9aap+0, 0x1.e016e00a2643cp-54}, \
+  {0x1.2063b88628cd6p+0, 0x1.dc775814a8495p-55}, \
+  {0x1.2387a6e756238p+0, 0x1.9b07eb6c70573p-54}, \
+  {0x1.26b4565e27cddp+0, 0x1.2bd339940e9d9p-55}, \
+  {0x1.29e9df51fdee1p+0, 0x1.612e8afad1255p-55}, \
+  {0x1.2d285a6e4030bp+0, 0x1.0024754db41d5p-54}, \
+  {0x1.306fe0a31b715p+0, 0x1.6f46ad23182e4p-55}, \
+  {0x1.33c08b26416ffp+0, 0x1.32721843659a6p-54}, \
+  {0x1.371a7373aa9cbp+0, -0x1.63aeabf42eae2p-54}, \
+  {0x1.3a7db34e59ff7p+0, -0x1.5e436d661f5e3p-56}, \
+  {0x1.3dea64c123422p+0, 0x1.ada0911f09ebcp-55}, \
+  {0x1.4160a21f72e2ap+0, -0x1.ef3691c309278p-58}, \
+  {0x1.44e086061892dp+0, 0x1.89b7a04ef80d0p-59}, \
+  {0x1.486a2b5c13cd0p+0, 0x1.3c1a3b69062f0p-56}, \
+  {0x1.4bfdad5362a27p+0, 0x1.d4397afec42e2p-56}, \
+  {0x1.4f9b2769d2ca7p+0, -0x1.4b309d25957e3p-54}, \
+  {0x1.5342b569d4f82p+0, -0x1.07abe1db13cadp-55}, \
+  {0x1.56f4736b527dap+0, 0x1.9bb2c011d93adp-54}, \
+  {0x1.5ab07dd485429p+0, 0x1.6324c054647adp-54}, \
+  {0x1.5e76f15ad2148p+0, 0x1.ba6f93080e65ep-54}, \
+  {0x1.6247eb03a5585p+0, -0x1.383c17e40b497p-54}, \
+  {0x1.6623882552225p+0, -0x1.bb60987591c34p-54}, \
+  {0x1.6a09e667f3bcdp+0, -0x1.bdd3413b26456p-54}, \
+  {0x1.6dfb23c651a2fp+0, -0x1.bbe3a683c88abp-57}, \
+  {0x1.71f75e8ec5f74p+0, -0x1.16e4786887a99p-55}, \
+  {0x1.75feb564267c9p+0, -0x1.0245957316dd3p-54}, \
+  {0x1.7a11473eb0187p+0, -0x1.41577ee04992fp-55}, \
+  {0x1.7e2f336cf4e62p+0, 0x1.05d02ba15797ep-56}, \
+  {0x1.82589994cce13p+0, -0x1.d4c1dd41532d8p-54}, \
+  {0x1.868d99b4492edp+0, -0x1.fc6f89bd4f6bap-54}, \
+  {0x1.8ace5422aa0dbp+0, 0x1.6e9f156864b27p-54}, \
+  {0x1.8f1ae99157736p+0, 0x1.5cc13a2e3976cp-55}, \
+  {0x1.93737b0cdc5e5p+0, -0x1.75fc781b57ebcp-57}, \
+  {0x1.97d829fde4e50p+0, -0x1.d185b7c1b85d1p-54}, \
+  {0x1.9c49182a3f090p+0, 0x1.c7c46b071f2bep-56}, \
+  {0x1.a0c667b5de565p+0, -0x1.359495d1cd533p-54}, \
+  {0x1.a5503b23e255dp+0, -0x1.d2f6edb8d41e1p-54}, \
+  {0x1.a9e6b5579fdbfp+0, 0x1.0fac90ef7fd31p-54}, \
+  {0x1.ae89f995ad3adp+0, 0x1.7a1cd345dcc81p-54}, \
+  {0x1.b33a2b84f15fbp+0, -0x1.2805e3084d708p-57}, \
+  {0x1.b7f76f2fb5e47p+0, -0x1.5584f7e54ac3bp-56}, \
+  {0x1.bcc1e904bc1d2p+0, 0x1.23dd07a2d9e84p-55}, \
+  {0x1.c199bdd85529cp+0, 0x1.11065895048ddp-55}, \
+  {0x1.c67f12e57d14bp+0, 0x1.2884dff483cadp-54}, \
+  {0x1.cb720dcef9069p+0, 0x1.503cbd1e949dbp-56}, \
+  {0x1.d072d4a07897cp+0, -0x1.cbc3743797a9cp-54}, \
+  {0x1.d5818dcfba487p+0, 0x1.2ed02d75b3707p-55}, \
+  {0x1.da9e603db3285p+0, 0x1.c2300696db532p-54}, \
+  {0x1.dfc97337b9b5fp+0, -0x1.1a5cd4f184b5cp-54}, \
+  {0x1.e502ee78b3ff6p+0, 0x1.39e8980a9cc8fp-55}, \
+  {0x1.ea4afa2a490dap+0, -0x1.e9c23179c2893p-54}, \
+  {0x1.efa1bee615a27p+0, 0x1.dc7f486a4b6b0p-54}, \
+  {0x1.f50765b6e4540p+0, 0x1.9d3e12dd8a18bp-54}, \
+  {0x1.fa7c1819e90d8p+0, 0x1.74853f3a5931ep-55}, \
+}
+/* log: ln2 = HI + LO (HI a multiple of 2^-42) */
+#define RR_LOG_LN2_HI 0x1.62e42fefa3800p-1
+#define RR_LOG_LN2_LO 0x1.ef35793c76730p-45
+/* (-1)^(n+1) / n, n = 2..9 */
+#define RR_LOG_P2 -0x1.0000000000000p-1
+#define RR_LOG_P3 0x1.5555555555555p-2
+#define RR_LOG_P4 -0x1.0000000000000p-2
+#define RR_LOG_P5 0x1.999999999999ap-3
+#define RR_LOG_P6 -0x1.5555555555555p-3
+#define RR_LOG_P7 0x1.2492492492492p-3
+#define RR_LOG_P8 -0x1.0000000000000p-3
+#define RR_LOG_P9 0x1.c71c71c71c71cp-4
+/* c = 1 + j/64, j = -19..27: RN(1/c), log(c) = hi + lo (hi a multiple of 2^-42) */
+#define RR_LOG_TAB { \
+  {0x1.6c16c16c16c17p+0, -0x1.68ac83e9c7000p-2, 0x1.7af966c548a30p-44}, \
+  {0x1.642c8590b2164p+0, -0x1.522ae0738a000p-2, -0x1.ebe708164c759p-45}, \
+  {0x1.5c9882b931057p+0, -0x1.3c25277333000p-2, -0x1.83b54b606bd5cp-46}, \
+  {0x1.5555555555555p+0, -0x1.269621134e000p-2, 0x1.1b61f10522625p-44}, \
+  {0x1.4e5e0a72f0539p+0, -0x1.1178e8227e000p-2, -0x1.1ef78ce2d07f2p-44}, \
+  {0x1.47ae147ae147bp+0, -0x1.f991c6cb3c000p-3, 0x1.90d04cd7cc834p-44}, \
+  {0x1.4141414141414p+0, -0x1.d1037f2656000p-3, 0x1.84a7e75b6f6e4p-47}, \
+  {0x1.3b13b13b13b14p+0, -0x1.a93ed3c8ae000p-3, 0x1.8724350562169p-45}, \
+  {0x1.3521cfb2b78c1p+0, -0x1.823c16551a000p-3, -0x1.e0ddb9a631e83p-46}, \
+  {0x1.2f684bda12f68p+0, -0x1.5bf406b544000p-3, 0x1.27023eb68981cp-46}, \
+  {0x1.29e4129e4129ep+0, -0x1.365fcb015a000p-3, 0x1.fd3a0afb9691bp-44}, \
+  {0x1.2492492492492p+0, -0x1.1178e8227e000p-3, -0x1.1ef78ce2d07f2p-45}, \
+  {0x1.1f7047dc11f70p+0, -0x1.da72763844000p-4, -0x1.a89401fa71733p-46}, \
+  {0x1.1a7b9611a7b96p+0, -0x1.9335e5d594000p-4, -0x1.3115c3abd47dap-45}, \
+  {0x1.15b1e5f75270dp+0, -0x1.4d3115d208000p-4, 0x1.53a2582f4e1efp-48}, \
+  {0x1.1111111111111p+0, -0x1.08598b59e4000p-4, 0x1.7e5dd7009902cp-46}, \
+  {0x1.0c9714fbcda3bp+0, -0x1.894aa149f8000p-5, -0x1.9a19a8be97661p-44}, \
+  {0x1.0842108421084p+0, -0x1.0415d89e78000p-5, 0x1.dddc7f461c516p-44}, \
+  {0x1.0410410410410p+0, -0x1.0205658930000p-6, -0x1.611d27c8e8417p-44}, \
+  {0x1.0000000000000p+0, 0x0.0p+0, 0x0.0p+0}, \
+  {0x1.f81f81f81f820p-1, 0x1.fc0a8b0fc0000p-7, 0x1.f1e7cf6d3a69cp-50}, \
+  {0x1.f07c1f07c1f08p-1, 0x1.f829b0e780000p-6, 0x1.980267c7e09e4p-45}, \
+  {0x1.e9131abf0b767p-1, 0x1.77458f6330000p-5, -0x1.181dce586af09p-44}, \
+  {0x1.e1e1e1e1e1e1ep-1, 0x1.f0a30c0118000p-5, -0x1.d599e83368e91p-45}, \
+  {0x1.dae6076b981dbp-1, 0x1.341d7961bc000p-4, 0x1.1d09299837610p-44}, \
+  {0x1.d41d41d41d41dp-1, 0x1.6f0d28ae58000p-4, -0x1.4b4641b664613p-44}, \
+  {0x1.cd85689039b0bp-1, 0x1.a926d3a4ac000p-4, 0x1.563650bd22a9cp-44}, \
+  {0x1.c71c71c71c71cp-1, 0x1.e27076e2b0000p-4, -0x1.a342c2af0003cp-45}, \
+  {0x1.c0e070381c0e0p-1, 0x1.0d77e7cd08000p-3, 0x1.cb2cd2ee2f482p-44}, \
+  {0x1.bacf914c1bad0p-1, 0x1.29552f8200000p-3, -0x1.5b967f4471dfcp-44}, \
+  {0x1.b4e81b4e81b4fp-1, 0x1.44d2b6ccb8000p-3, -0x1.70cc16135783cp-46}, \
+  {0x1.af286bca1af28p-1, 0x1.5ff3070a7a000p-3, -0x1.8586f183bebf2p-44}, \
+  {0x1.a98ef606a63bep-1, 0x1.7ab890210e000p-3, -0x1.bdb9072534a58p-45}, \
+  {0x1.a41a41a41a41ap-1, 0x1.9525a9cf46000p-3, -0x1.297137d9f158fp-44}, \
+  {0x1.9ec8e951033d9p-1, 0x1.af3c94e80c000p-3, -0x1.a4e633fcd9066p-52}, \
+  {0x1.999999999999ap-1, 0x1.c8ff7c79aa000p-3, -0x1.7794f689f8434p-45}, \
+  {0x1.948b0fcd6e9e0p-1, 0x1.e27076e2b0000p-3, -0x1.a342c2af0003cp-44}, \
+  {0x1.8f9c18f9c18fap-1, 0x1.fb9186d5e4000p-3, -0x1.d572aab993c87p-47}, \
+  {0x1.8acb90f6bf3aap-1, 0x1.0a324e2739000p-2, 0x1.c6bee7ef4030ep-47}, \
+  {0x1.8618618618618p-1, 0x1.1675cababa000p-2, 0x1.8380e731f55c4p-44}, \
+  {0x1.8181818181818p-1, 0x1.22941fbcf8000p-2, -0x1.a6976f5eb0963p-44}, \
+  {0x1.7d05f417d05f4p-1, 0x1.2e8e2bae12000p-2, -0x1.67b1e99b72bd8p-45}, \
+  {0x1.78a4c8178a4c8p-1, 0x1.3a64c55694000p-2, 0x1.7a71cbcd735d0p-44}, \
+  {0x1.745d1745d1746p-1, 0x1.4618bc21c6000p-2, -0x1.3d82f484c84ccp-46}, \
+  {0x1.702e05c0b8170p-1, 0x1.51aad872e0000p-2, -0x1.f4bd8db0a7cc1p-44}, \
+  {0x1.6c16c16c16c17p-1, 0x1.5d1bdbf581000p-2, -0x1.8d6bdc9c7c238p-44}, \
+  {0x1.6816816816817p-1, 0x1.686c81e9b1000p-2, 0x1.2bb110af84054p-44}, \
+}
+
+#if defined(__CUDACC__)
+static __device__ const double RR_EXP_T_D[64][2] = RR_EXP_TAB;
+static __device__ const double RR_LOG_T_D[47][3] = RR_LOG_TAB;
+#endif
+static const double RR_EXP_T_H[64][2] = RR_EXP_TAB;
+static const double RR_LOG_T_H[47][3] = RR_LOG_TAB;
+#if defined(__CUDA_ARCH__)
+#define RR_EXP_T(j, i) RR_EXP_T_D[j][i]
+#define RR_LOG_T(j, i) RR_LOG_T_D[j][i]
+#else
+#define RR_EXP_T(j, i) RR_EXP_T_H[j][i]
+#define RR_LOG_T(j, i) RR_LOG_T_H[j][i]
+#endif
+
 /* ------------------------------------------------------------------ exp -- */
-RRM_FN double rr_exp(double x) {
-  if (rrm_isnan(x)) return x;
-  if (x > 0x1.62e42fefa39efp+9) return rrm_inf(); /* > log(DBL_MAX) */
-  if (x < -0x1.74910d52d3052p+9) return 0.0;      /* < log of the least subnormal / 2 */
-  const double kd = rrm_rint(RRM_MUL(x, 0x1.71547652b82fep+0));
-  double r = RRM_FMA(-kd, 0x1.62e42fee00000p-1, x);
-  r = RRM_FMA(-kd, 0x1.a39ef35793c76p-33, r);
-  /* p = sum_{j=2}^{13} r^(j-2) / j! */
-  double p = 0x1.6124613a86d09p-33;
-  p = RRM_FMA(p, r, 0x1.1eed8eff8d898p-29);
-  p = RRM_FMA(p, r, 0x1.ae64567f544e4p-26);
-  p = RRM_FMA(p, r, 0x1.27e4fb7789f5cp-22);
-  p = RRM_FMA(p, r, 0x1.71de3a556c734p-19);
-  p = RRM_FMA(p, r, 0x1.a01a01a01a01ap-16);
-  p = RRM_FMA(p, r, 0x1.a01a01a01a01ap-13);
-  p = RRM_FMA(p, r, 0x1.6c16c16c16c17p-10);
-  p = RRM_FMA(p, r, 0x1.1111111111111p-7);
-  p = RRM_FMA(p, r, 0x1.5555555555555p-5);
-  p = RRM_FMA(p, r, 0x1.5555555555555p-3);
-  p = RRM_FMA(p, r, 0.5);
-  const double em1 = RRM_FMA(RRM_MUL(r, r), p, r);
-  double y = RRM_ADD(1.0, em1);
-  int k = (int)kd;
+/* y * 2^k for y in [0.99, 2.02], any k, with one rounding */
+RRM_FN double rrm_scale(double y, int k) {
+  if (k >= -1020 && k <= 1020) return rrm_from_bits(rrm_bits(y) + ((uint64_t)(int64_t)k << 52));
   if (k > 1023) {
     y = RRM_MUL(y, rrm_pow2(1023));
     k -= 1023;
+    return k > 1023 ? rrm_inf() : RRM_MUL(y, rrm_pow2(k));
   }
   if (k < -1000) return RRM_MUL(RRM_MUL(y, rrm_pow2(k + 1000)), rrm_pow2(-1000));
   return RRM_MUL(y, rrm_pow2(k));
 }
 
+/* e^(x + xl) for |x| <= 745.2, xl a small correction used when has_lo */
+RRM_FN double rrm_exp_core(double x, double xl, int has_lo) {
+  /* kd = nearest integer to 64 x / ln2, read back from the low bits of the shifted sum */
+  const double t = RRM_FMA(x, RR_EXP_INV_L64, 0x1.8p52);
+  const int kd = (int)(int32_t)(uint32_t)rrm_bits(t);
+  const double kdd = RRM_SUB(t, 0x1.8p52);
+  double r = RRM_FMA(-kdd, RR_EXP_C1, x);
+  r = RRM_FMA(-kdd, RR_EXP_C2, r);
+  if (has_lo) r = RRM_ADD(r, xl);
+  /* e^r - 1 = r + r^2 (1/2 + r/6 + r^2/24 + r^3/120 + r^4/720) */
+  double q = RRM_FMA(r, RR_EXP_F6, RR_EXP_F5);
+  q = RRM_FMA(q, r, RR_EXP_F4);
+  q = RRM_FMA(q, r, RR_EXP_F3);
+  q = RRM_FMA(q, r, RR_EXP_F2);
+  const double p = RRM_FMA(RRM_MUL(r, r), q, r);
+  const int j = kd & 63;
+  const double th = RR_EXP_T(j, 0), tl = RR_EXP_T(j, 1);
+  const double y = RRM_ADD(th, RRM_FMA(th, p, tl));
+  return rrm_scale(y, (kd - j) / 64);
+}
+
+RRM_FN double rr_exp(double x) {
+  if ((rrm_bits(x) & 0x7fffffffffffffffull) >= 0x4086200000000000ull) { /* |x| >= 708, inf or NaN */
+    if (rrm_isnan(x)) return x;
+    if (x > 0x1.62e42fefa39efp+9) return rrm_inf(); /* > log(DBL_MAX) */
+    if (x < -0x1.74910d52d3052p+9) return 0.0;      /* < log of the least subnormal / 2 */
+  }
+  return rrm_exp_core(x, 0.0, 0);
+}
+
 /* ------------------------------------------------------------------ log -- */
-RRM_FN double rr_log(double x) {
-  if (rrm_isnan(x)) return x;
-  if (x < 0.0) return rrm_nan();
-  if (x == 0.0) return -rrm_inf();
-  if (x > 0x1.fffffffffffffp+1023) return x; /* +inf */
-  uint64_t b = rrm_bits(x);
-  int e = (int)((b >> 52) & 0x7ff);
-  if (e == 0) { /* subnormal */
-    x = RRM_MUL(x, 0x1p54);
-    b = rrm_bits(x);
-    e = (int)((b >> 52) & 0x7ff) - 54;
-  }
-  e -= 1023;
-  double m = rrm_from_bits((b & 0x000fffffffffffffull) | 0x3ff0000000000000ull);
-  if (m > 0x1.6a09e667f3bcdp+0) {
-    m = RRM_MUL(m, 0.5);
+/* log x = s + u for a positive normal x with its bits b and exponent offset e0
+ * (|u| well below |s| unless s = 0) */
+RRM_FN void rrm_log_parts(uint64_t b, int e0, double* s_out, double* u_out) {
+  const uint64_t mant = b & 0x000fffffffffffffull;
+  int e = e0 + (int)(b >> 52) - 1023;
+  int j;
+  double m;
+  if (mant > 0x6a09e667f3bccull) { /* 1.mant > sqrt(2): m = 1.mant / 2 */
+    m = rrm_from_bits(mant | 0x3fe0000000000000ull);
     e += 1;
+    j = (int)((mant + (1ull << 46)) >> 47) - 32;
+  } else {
+    m = rrm_from_bits(mant | 0x3ff0000000000000ull);
+    j = (int)((mant + (1ull << 45)) >> 46);
   }
-  const double f = RRM_SUB(m, 1.0);
-  const double s = RRM_DIV(f, RRM_ADD(2.0, f));
-  const double z = RRM_MUL(s, s);
-  /* q = sum_{j=1}^{11} z^(j-1) / (2j+1) */
-  double q = 1.0 / 23.0;
-  q = RRM_FMA(q, z, 1.0 / 21.0);
-  q = RRM_FMA(q, z, 1.0 / 19.0);
-  q = RRM_FMA(q, z, 1.0 / 17.0);
-  q = RRM_FMA(q, z, 1.0 / 15.0);
-  q = RRM_FMA(q, z, 1.0 / 13.0);
-  q = RRM_FMA(q, z, 1.0 / 11.0);
-  q = RRM_FMA(q, z, 1.0 / 9.0);
-  q = RRM_FMA(q, z, 1.0 / 7.0);
-  q = RRM_FMA(q, z, 1.0 / 5.0);
-  q = RRM_FMA(q, z, 1.0 / 3.0);
-  const double hs = RRM_ADD(s, s);
-  const double lm = RRM_FMA(RRM_MUL(hs, z), q, hs);
+  const double c = 1.0 + (double)j * 0x1p-6;
+  const double invc = RR_LOG_T(j + 19, 0);
+  const double f = RRM_SUB(m, c); /* exact */
+  const double rh = RRM_MUL(f, invc);
+  const double rl = RRM_MUL(RRM_FMA(-rh, c, f), invc);
+  /* log1p(r) - r = r^2 (-1/2 + r/3 - r^2/4 + ... + r^7/9) */
+  double q = RRM_FMA(rh, RR_LOG_P9, RR_LOG_P8);
+  q = RRM_FMA(q, rh, RR_LOG_P7);
+  q = RRM_FMA(q, rh, RR_LOG_P6);
+  q = RRM_FMA(q, rh, RR_LOG_P5);
+  q = RRM_FMA(q, rh, RR_LOG_P4);
+  q = RRM_FMA(q, rh, RR_LOG_P3);
+  q = RRM_FMA(q, rh, RR_LOG_P2);
+  const double tail = RRM_FMA(RRM_MUL(rh, rh), q, rl);
   const double ed = (double)e;
-  return RRM_FMA(ed, 0x1.62e42fee00000p-1, RRM_FMA(ed, 0x1.a39ef35793c76p-33, lm));
+  const double a = RRM_FMA(ed, RR_LOG_LN2_HI, RR_LOG_T(j + 19, 1)); /* exact */
+  const double b0 = RRM_FMA(ed, RR_LOG_LN2_LO, RR_LOG_T(j + 19, 2));
+  const double s = RRM_ADD(a, rh);
+  const double t = RRM_ADD(RRM_SUB(a, s), rh); /* |a| >= |rh| or a = 0 */
+  *s_out = s;
+  *u_out = RRM_ADD(RRM_ADD(t, tail), b0);
+}
+
+RRM_FN double rr_log(double x) {
+  uint64_t b = rrm_bits(x);
+  int e0 = 0;
+  if (b - 0x0010000000000000ull >= 0x7fe0000000000000ull) { /* not a positive normal number */
+    if (rrm_isnan(x)) return x;
+    if (x < 0.0) return rrm_nan();
+    if (x == 0.0) return -rrm_inf();
+    if (x > 0x1.fffffffffffffp+1023) return x; /* +inf */
+    b = rrm_bits(RRM_MUL(x, 0x1p54));          /* subnormal */
+    e0 = -54;
+  }
+  double s, u;
+  rrm_log_parts(b, e0, &s, &u);
+  return RRM_ADD(s, u);
 }
 
 /* ------------------------------------------------------------ sin / cos -- */
@@ -301,7 +490,7 @@ RRM_FN double rrm_cos_k(double r, double rl) {
 }
 
 RRM_FN double rr_sin(double x) {
-  if (rrm_isnan(x)) return x;
+  if (rrm_isnan(x) || x == 0.0) return x; /* sin(-0) = -0 */
   const double ax = rrm_fabs(x);
   if (ax > 0x1.fffffffffffffp+1023) return rrm_nan();
   double rh, rl;
@@ -353,7 +542,23 @@ RRM_FN double rr_pow(double a, double b) {
     if (!rrm_is_int(b)) return rrm_nan();
     if (bodd) sign = -1.0;
   }
-  return sign * rr_exp(RRM_MUL(b, rr_log(ab)));
+  /* e^(b log|a|) with log|a| and the product carried as double-doubles */
+  uint64_t bits = rrm_bits(ab);
+  int e0 = 0;
+  if (bits < 0x0010000000000000ull) { /* subnormal */
+    bits = rrm_bits(RRM_MUL(ab, 0x1p54));
+    e0 = -54;
+  }
+  double s, u;
+  rrm_log_parts(bits, e0, &s, &u);
+  const double lh = RRM_ADD(s, u);
+  const double ll = RRM_ADD(RRM_SUB(s, lh), u);
+  const double yh = RRM_MUL(b, lh);
+  const double yl = RRM_FMA(b, ll, RRM_FMA(b, lh, -yh));
+  if (rrm_isnan(yh)) return rrm_nan();
+  if (yh > 0x1.62e42fefa39efp+9) return sign * rrm_inf();
+  if (yh < -0x1.74910d52d3052p+9) return sign * 0.0;
+  return sign * rrm_exp_core(yh, yl, 1);
 }
 
 #endif
