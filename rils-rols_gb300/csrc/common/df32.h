@@ -270,18 +270,81 @@ DFN dfl dfl_mul_fl(dfl x, float a) {
   {0.7111111283302307f, -1.7219120351796846e-08f, 0.3409265875816345f, -6.110413286464222e-10f}, \
   {0.7032967209815979f, -1.7684895325942307e-08f, 0.3519764244556427f, -1.2984645580971232e-09f}, \
 }
+/* a = j/32, j = -26..26: sin a and cos a */
+#define DFL_SC_TAB { \
+  {-0.7260086536407471f, -1.6199654950810327e-09f, 0.6876855492591858f, 1.2961319129090043e-08f}, \
+  {-0.7041674852371216f, -2.6217412241180682e-08f, 0.7100338935852051f, -1.0019125085136693e-08f}, \
+  {-0.681638777256012f, 1.723267750719515e-08f, 0.7316888570785522f, 1.1795268761716216e-08f}, \
+  {-0.6584444046020508f, 4.691483201924029e-09f, 0.7526293992996216f, -2.6881554759938808e-08f}, \
+  {-0.6346070766448975f, -3.37037175945909e-09f, 0.7728349566459656f, -1.0493494073671172e-08f}, \
+  {-0.6101500988006592f, 2.1724867238503975e-08f, 0.7922858595848083f, 9.237019482633002e-11f}, \
+  {-0.5850972533226013f, -1.9617861113374602e-08f, 0.8109630942344666f, 2.5270750825256982e-08f}, \
+  {-0.5594731569290161f, 2.568164880756285e-08f, 0.8288484811782837f, 6.431041921217684e-09f}, \
+  {-0.5333026647567749f, -8.779244886625293e-09f, 0.8459244966506958f, 2.5803721381834066e-09f}, \
+  {-0.5066114664077759f, 1.1593518145502912e-08f, 0.8621744513511658f, 2.858371495051415e-08f}, \
+  {-0.4794255495071411f, 1.0902938107903992e-08f, 0.8775825500488281f, 1.1841544633739431e-08f}, \
+  {-0.45177146792411804f, -3.5675657983347264e-09f, 0.8921337127685547f, -1.3401559861847545e-08f}, \
+  {-0.4236762523651123f, -4.838825784503342e-09f, 0.9058136940002441f, -1.0574307651722847e-08f}, \
+  {-0.3951673209667206f, -9.274213397247877e-09f, 0.9186091423034668f, 1.3491451511526975e-08f}, \
+  {-0.36627253890037537f, 9.814328016943819e-09f, 0.9305076003074646f, 2.1604849465006737e-08f}, \
+  {-0.33702006936073303f, 3.384799662775606e-10f, 0.9414974451065063f, 1.8021374614818342e-08f}, \
+  {-0.30743852257728577f, 7.996904471951893e-09f, 0.9515679478645325f, 1.8363972842383447e-10f}, \
+  {-0.27755674719810486f, -4.448231560871818e-09f, 0.9607092142105103f, 2.880505078906026e-08f}, \
+  {-0.24740396440029144f, 5.145768700032249e-09f, 0.9689124226570129f, -9.463682060228962e-10f}, \
+  {-0.21700957417488098f, -6.920129358434224e-09f, 0.9761694669723511f, 6.896283988311325e-09f}, \
+  {-0.186403289437294f, -7.324975737077466e-09f, 0.9824733138084412f, -7.071859209339948e-10f}, \
+  {-0.15561498701572418f, -5.757831988972839e-09f, 0.9878177642822266f, 1.9534246220587193e-08f}, \
+  {-0.1246747300028801f, -3.3823475131811165e-09f, 0.9921976923942566f, -2.516492791926339e-08f}, \
+  {-0.09361273050308228f, -7.324306161571315e-10f, 0.9956086874008179f, -9.428161584779104e-10f}, \
+  {-0.0624593161046505f, -1.737729737882887e-09f, 0.9980475306510925f, -1.9950993745965206e-08f}, \
+  {-0.03124491311609745f, -8.69228633515462e-10f, 0.9995117783546448f, -1.9869508705028238e-08f}, \
+  {0.0f, 0.0f, 1.0f, 0.0f}, \
+  {0.03124491311609745f, 8.69228633515462e-10f, 0.9995117783546448f, -1.9869508705028238e-08f}, \
+  {0.0624593161046505f, 1.737729737882887e-09f, 0.9980475306510925f, -1.9950993745965206e-08f}, \
+  {0.09361273050308228f, 7.324306161571315e-10f, 0.9956086874008179f, -9.428161584779104e-10f}, \
+  {0.1246747300028801f, 3.3823475131811165e-09f, 0.9921976923942566f, -2.516492791926339e-08f}, \
+  {0.15561498701572418f, 5.757831988972839e-09f, 0.9878177642822266f, 1.9534246220587193e-08f}, \
+  {0.186403289437294f, 7.324975737077466e-09f, 0.9824733138084412f, -7.071859209339948e-10f}, \
+  {0.21700957417488098f, 6.920129358434224e-09f, 0.9761694669723511f, 6.896283988311325e-09f}, \
+  {0.24740396440029144f, -5.145768700032249e-09f, 0.9689124226570129f, -9.463682060228962e-10f}, \
+  {0.27755674719810486f, 4.448231560871818e-09f, 0.9607092142105103f, 2.880505078906026e-08f}, \
+  {0.30743852257728577f, -7.996904471951893e-09f, 0.9515679478645325f, 1.8363972842383447e-10f}, \
+  {0.33702006936073303f, -3.384799662775606e-10f, 0.9414974451065063f, 1.8021374614818342e-08f}, \
+  {0.36627253890037537f, -9.814328016943819e-09f, 0.9305076003074646f, 2.1604849465006737e-08f}, \
+  {0.3951673209667206f, 9.274213397247877e-09f, 0.9186091423034668f, 1.3491451511526975e-08f}, \
+  {0.4236762523651123f, 4.838825784503342e-09f, 0.9058136940002441f, -1.0574307651722847e-08f}, \
+  {0.45177146792411804f, 3.5675657983347264e-09f, 0.8921337127685547f, -1.3401559861847545e-08f}, \
+  {0.4794255495071411f, -1.0902938107903992e-08f, 0.8775825500488281f, 1.1841544633739431e-08f}, \
+  {0.5066114664077759f, -1.1593518145502912e-08f, 0.8621744513511658f, 2.858371495051415e-08f}, \
+  {0.5333026647567749f, 8.779244886625293e-09f, 0.8459244966506958f, 2.5803721381834066e-09f}, \
+  {0.5594731569290161f, -2.568164880756285e-08f, 0.8288484811782837f, 6.431041921217684e-09f}, \
+  {0.5850972533226013f, 1.9617861113374602e-08f, 0.8109630942344666f, 2.5270750825256982e-08f}, \
+  {0.6101500988006592f, -2.1724867238503975e-08f, 0.7922858595848083f, 9.237019482633002e-11f}, \
+  {0.6346070766448975f, 3.37037175945909e-09f, 0.7728349566459656f, -1.0493494073671172e-08f}, \
+  {0.6584444046020508f, -4.691483201924029e-09f, 0.7526293992996216f, -2.6881554759938808e-08f}, \
+  {0.681638777256012f, -1.723267750719515e-08f, 0.7316888570785522f, 1.1795268761716216e-08f}, \
+  {0.7041674852371216f, 2.6217412241180682e-08f, 0.7100338935852051f, -1.0019125085136693e-08f}, \
+  {0.7260086536407471f, 1.6199654950810327e-09f, 0.6876855492591858f, 1.2961319129090043e-08f}, \
+}
+/* 1/6 */
+#define DF_INV6_HI 0.1666666716337204f
+#define DF_INV6_LO -4.967053879312289e-09f
 #if defined(__CUDACC__)
 static __device__ const float dfl_exp2_tab_d[32][2] = DFL_EXP2_TAB;  /* 2^(j/32) */
 static __device__ const float dfl_log_tab_d[47][4] = DFL_LOG_TAB;    /* c = 1 + j/64, j = -19..27: 1/c, log c */
+static __device__ const float dfl_sc_tab_d[53][4] = DFL_SC_TAB;      /* a = j/32, j = -26..26: sin a, cos a */
 #endif
 static const float dfl_exp2_tab_h[32][2] = DFL_EXP2_TAB;
 static const float dfl_log_tab_h[47][4] = DFL_LOG_TAB;
+static const float dfl_sc_tab_h[53][4] = DFL_SC_TAB;
 #if defined(__CUDA_ARCH__)
 #define DFL_EXP2(j, i) dfl_exp2_tab_d[j][i]
 #define DFL_LOGT(j, i) dfl_log_tab_d[j][i]
+#define DFL_SCT(j, i) dfl_sc_tab_d[j][i]
 #else
 #define DFL_EXP2(j, i) dfl_exp2_tab_h[j][i]
 #define DFL_LOGT(j, i) dfl_log_tab_h[j][i]
+#define DFL_SCT(j, i) dfl_sc_tab_h[j][i]
 #endif
 
 /* ---- comparisons (the semantics of the FP64 comparisons on hi + lo) ---- */
@@ -381,49 +444,34 @@ DFN int dfl_reduce_half_pi(dfl x, dfl* r) {
   const int ki = (int)k;
   return ki & 3;
 }
-/* sin r = r (1 - z/3! + z^2/5! - z^3/7! + z^4/9! - z^5 T(z)), z = r^2 <= 0.617,
- * T = 1/11! - z/13! + z^2/15! - z^3/17! in FP32 (the term is below 3e-9) */
-DFN dfl dfl_sin_kernel(dfl r) {
-  const dfl z = dfl_mul_nc(r, r);
-  const float zf = z.hi;
-  const float tz = DF_FMA(DF_FMA(DF_FMA(zf, -2.8114573589663704e-15f, 7.647163609812713e-13f), zf,
-                                 -1.6059044372074283e-10f), zf, 2.5052107943679403e-08f);
-  dfl p = dfl_add_nc(dfl_make(2.7557318844628753e-06f, 3.793571224297229e-14f), dfl_neg(dfl_mul_fl(z, tz)));
-  p = dfl_add_nc(dfl_make(0.00019841270113829523f, -2.725596874933456e-12f), dfl_neg(dfl_mul_nc(p, z)));
-  p = dfl_add_nc(dfl_make(0.008333333767950535f, -4.34617203337595e-10f), dfl_neg(dfl_mul_nc(p, z)));
-  p = dfl_add_nc(dfl_make(0.1666666716337204f, -4.967053879312289e-09f), dfl_neg(dfl_mul_nc(p, z)));
-  p = dfl_add_fl(dfl_neg(dfl_mul_nc(p, z)), 1.0f);
-  return dfl_mul_nc(p, r);
-}
-/* cos r = 1 - z/2 + z^2/4! - z^3/6! + z^4/8! - z^5 U(z),
- * U = 1/10! - z/12! + z^2/14! - z^3/16! + z^4/18! in FP32 (the term is below 3e-8) */
-DFN dfl dfl_cos_kernel(dfl r) {
-  const dfl z = dfl_mul_nc(r, r);
-  const float zf = z.hi;
-  const float uz = DF_FMA(DF_FMA(DF_FMA(DF_FMA(zf, 1.5619206814541513e-16f, -4.7794772561329454e-14f), zf,
-                                        1.147074536050896e-11f), zf, -2.0876755879584152e-09f), zf,
-                          2.755731998149713e-07f);
-  dfl p = dfl_add_nc(dfl_make(2.4801587642286904e-05f, -3.40699609366682e-13f), dfl_neg(dfl_mul_fl(z, uz)));
-  p = dfl_add_nc(dfl_make(0.0013888889225199819f, -3.3631094437103215e-11f), dfl_neg(dfl_mul_nc(p, z)));
-  p = dfl_add_nc(dfl_make(0.0416666679084301f, -1.2417634698280722e-09f), dfl_neg(dfl_mul_nc(p, z)));
-  p = dfl_add_fl(dfl_neg(dfl_mul_nc(p, z)), 0.5f);
-  return dfl_add_fl(dfl_neg(dfl_mul_nc(p, z)), 1.0f);
-}
-DFN dfl dfl_sin(dfl x) {
+/* sin(x + shift pi/2), shift 0 (sin) or 1 (cos), in one path for every
+ * quadrant: x = k pi/2 + r, r = j/32 + s with |s| <= 1/64, sin(j/32) and
+ * cos(j/32) from a table, and sin(x + shift pi/2) = A cos s + B sin s with
+ * (A, B) = (S, C), (C, -S), (-S, -C), (-C, S) for the quadrant k + shift;
+ * sin s = s - s^3/6 + s^5 (1/120 - s^2/5040) and cos s - 1 = -s^2/2 +
+ * s^4 (1/24 - s^2/720), the s^5 and s^4 terms in FP32 */
+DFN dfl dfl_sincos(dfl x, int shift) {
   if (!dfl_finite(x.hi)) return dfl_make(dfl_nanf(), 0.0f);
   dfl r;
-  const int q = dfl_reduce_half_pi(x, &r);
-  if (q < 0) return dfl_make(dfl_nanf(), 0.0f);
-  const dfl v = (q & 1) ? dfl_cos_kernel(r) : dfl_sin_kernel(r);
-  return (q & 2) ? dfl_neg(v) : v;
+  const int q0 = dfl_reduce_half_pi(x, &r);
+  if (q0 < 0) return dfl_make(dfl_nanf(), 0.0f);
+  const int q = (q0 + shift) & 3;
+  const float jf = rintf(DF_MUL(r.hi, 32.0f));
+  const int J = (int)jf + 26;
+  const dfl s = dfl_add_fl(r, -DF_MUL(jf, 0.03125f));
+  const dfl z = dfl_mul_nc(s, s);
+  const float zf = z.hi;
+  const float s5 = DF_MUL(DF_MUL(s.hi, DF_MUL(zf, zf)), DF_FMA(zf, -1.9841270113829523e-04f, 8.333333767950535e-03f));
+  const dfl sins = dfl_add_fl(dfl_add_nc(s, dfl_neg(dfl_mul_nc(dfl_mul_nc(s, z), dfl_make(DF_INV6_HI, DF_INV6_LO)))), s5);
+  const float z4 = DF_MUL(DF_MUL(zf, zf), DF_FMA(zf, -1.3888889225199819e-03f, 4.1666667908430099e-02f));
+  const dfl cm1 = dfl_add_fl(dfl_scale(z, -0.5f), z4);
+  const dfl S = dfl_make(DFL_SCT(J, 0), DFL_SCT(J, 1)), C = dfl_make(DFL_SCT(J, 2), DFL_SCT(J, 3));
+  dfl A = (q & 1) ? C : S, B = (q & 1) ? S : C;
+  if (q & 2) A = dfl_neg(A);
+  if ((q + 1) & 2) B = dfl_neg(B);
+  return dfl_add_nc(A, dfl_add_nc(dfl_mul_nc(A, cm1), dfl_mul_nc(B, sins)));
 }
-DFN dfl dfl_cos(dfl x) {
-  if (!dfl_finite(x.hi)) return dfl_make(dfl_nanf(), 0.0f);
-  dfl r;
-  const int q = dfl_reduce_half_pi(x, &r);
-  if (q < 0) return dfl_make(dfl_nanf(), 0.0f);
-  const dfl v = (q & 1) ? dfl_sin_kernel(r) : dfl_cos_kernel(r);
-  return ((q + 1) & 2) ? dfl_neg(v) : v;
-}
+DFN dfl dfl_sin(dfl x) { return dfl_sincos(x, 0); }
+DFN dfl dfl_cos(dfl x) { return dfl_sincos(x, 1); }
 
 #endif
