@@ -149,6 +149,12 @@ rrg_status rrg_context_destroy(rrg_context* ctx);
  */
 rrg_status rrg_dataset_create(rrg_context* ctx, const double* X_col, const double* y, int64_t n, int32_t d,
                               rrg_dataset** out);
+/* The same dataset from X given row-major (n rows of d values, the buffer the
+ * reference's pybind fit receives before get_x splits it into columns,
+ * rils_rols_cpp.cpp:675-698); the transposition runs on the device.  A pinned
+ * X (or y) is copied by DMA straight from the caller's memory. */
+rrg_status rrg_dataset_create_rows(rrg_context* ctx, const double* X_rows, const double* y, int64_t n, int32_t d,
+                                   rrg_dataset** out);
 rrg_status rrg_dataset_destroy(rrg_dataset* ds);
 
 /*

@@ -551,6 +551,76 @@ DevData rrg_dataset::view() const {
 }
 
 // ------------------------------------------------------------------ ABI ----
+namespace {
+
+// X given row-major (n x d) into the padded column layout (rows >= n zero)
+__global__ void rows_to_cols_kernel(const double* __restrict__ rows, int64_t n, int32_t d, int64_t n_pad,
+                                    double* __restrict__ cols) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_pad; i += (int64_t)gridDim.x * blockDim.x)
+    for (int32_t j = 0; j < d; ++j) cols[(int64_t)j * n_pad + i] = i < n ? rows[i * d + j] : 0.0;
+}
+
+// Shared part of the two entry points: device buffers, the copies queued by
+// `upload` on the context stream, the FP32 splits, and meanwhile the sums of
+// y in the fixed CSUM order on the host.
+template <class Upload>
+rrg_status make_dataset(rrg_context* ctx, const double* y, int64_t n, int32_t d, rrg_dataset** out, Upload upload) {
+  *out = nullptr;
+  RRG_CUDA(cudaSetDevice(ctx->device));
+  rrg_dataset* ds = new rrg_dataset();
+  ds->ctx = ctx;
+  ds->n = n;
+  ds->d = d;
+  ds->n_pad = round_up(n, 256);
+  const int64_t cols = std::max(d, 1);
+  const size_t b64 = sizeof(double) * ds->n_pad * cols, b32 = sizeof(float) * ds->n_pad * cols;
+  const size_t y64b = sizeof(double) * ds->n_pad, y32b = sizeof(float) * ds->n_pad;
+  if (cudaMalloc(&ds->X64, b64) != cudaSuccess || cudaMalloc(&ds->X32, b32) != cudaSuccess ||
+      cudaMalloc(&ds->X32lo, b32) != cudaSuccess ||
+      cudaMalloc(&ds->y64, y64b) != cudaSuccess || cudaMalloc(&ds->y32, y32b) != cudaSuccess ||
+      cudaMalloc(&ds->y32lo, y32b) != cudaSuccess) {
+    cudaGetLastError();
+    rrg_dataset_destroy(ds);
+    rrc::set_error("rrg_dataset_create: out of device memory");
+    return RRG_E_OOM;
+  }
+  cudaStream_t st = ctx->stream;
+  bool ok = cudaMemsetAsync(ds->X64, 0, b64, st) == cudaSuccess && upload(ds, st) &&
+            cudaMemcpyAsync(ds->y64, y, sizeof(double) * n, cudaMemcpyHostToDevice, st) == cudaSuccess &&
+            cudaMemsetAsync(ds->y64 + n, 0, sizeof(double) * (ds->n_pad - n), st) == cudaSuccess &&
+            launch_split_f32(ds->X64, ds->X32, ds->X32lo, ds->n_pad * cols, st) &&
+            launch_split_f32(ds->y64, ds->y32, ds->y32lo, ds->n_pad, st);
+  // mean and total sum of squares of y (rils_rols_cpp.cpp:41-43) in the fixed
+  // CSUM order, while the copies run
+  ds->ysum = rr_csum(y, (long)n);
+  ds->ymean = ds->ysum / (double)n;
+  rr_csum_acc acc;
+  rr_csum_init(&acc);
+  for (int64_t i = 0; i < n; ++i) rr_csum_add(&acc, (y[i] - ds->ymean) * (y[i] - ds->ymean));
+  ds->sst = rr_csum_total(&acc);
+  rr_csum_init(&acc);
+  for (int64_t i = 0; i < n; ++i) rr_csum_add(&acc, y[i] * y[i]);
+  ds->yy = rr_csum_total(&acc);
+  ok = ok && cudaStreamSynchronize(st) == cudaSuccess;
+  if (!ok) {
+    cuda_ok(cudaGetLastError(), "dataset upload");
+    rrg_dataset_destroy(ds);
+    return RRG_E_CUDA;
+  }
+  *out = ds;
+  return RRG_OK;
+}
+
+bool dataset_args_ok(rrg_context* ctx, const double* X, const double* y, int64_t n, int32_t d, rrg_dataset** out) {
+  if (!ctx || !out || !y || n <= 0 || d < 0 || (d > 0 && !X) || n > (int64_t)1 << 40) {
+    rrc::set_error("rrg_dataset_create: invalid arguments");
+    return false;
+  }
+  return true;
+}
+
+}  // namespace
+
 extern "C" {
 
 rrg_status rrg_context_create(int32_t device, rrg_context** out) {
@@ -605,67 +675,35 @@ rrg_status rrg_context_destroy(rrg_context* ctx) {
   return RRG_OK;
 }
 
+
 rrg_status rrg_dataset_create(rrg_context* ctx, const double* X_col, const double* y, int64_t n, int32_t d,
                               rrg_dataset** out) {
-  if (!ctx || !out || !y || n <= 0 || d < 0 || (d > 0 && !X_col) || n > (int64_t)1 << 40) {
-    rrc::set_error("rrg_dataset_create: invalid arguments");
-    return RRG_E_INVALID;
-  }
-  *out = nullptr;
-  RRG_CUDA(cudaSetDevice(ctx->device));
-  rrg_dataset* ds = new rrg_dataset();
-  ds->ctx = ctx;
-  ds->n = n;
-  ds->d = d;
-  ds->n_pad = round_up(n, 256);
-  const int64_t cols = std::max(d, 1);
-  // mean and total sum of squares of y (rils_rols_cpp.cpp:41-43) in the fixed CSUM order
-  ds->ysum = rr_csum(y, (long)n);
-  ds->ymean = ds->ysum / (double)n;
-  rr_csum_acc acc;
-  rr_csum_init(&acc);
-  for (int64_t i = 0; i < n; ++i) rr_csum_add(&acc, (y[i] - ds->ymean) * (y[i] - ds->ymean));
-  ds->sst = rr_csum_total(&acc);
-  rr_csum_init(&acc);
-  for (int64_t i = 0; i < n; ++i) rr_csum_add(&acc, y[i] * y[i]);
-  ds->yy = rr_csum_total(&acc);
-  const size_t b64 = sizeof(double) * ds->n_pad * cols, b32 = sizeof(float) * ds->n_pad * cols;
-  const size_t y64b = sizeof(double) * ds->n_pad, y32b = sizeof(float) * ds->n_pad;
-  if (cudaMalloc(&ds->X64, b64) != cudaSuccess || cudaMalloc(&ds->X32, b32) != cudaSuccess ||
-      cudaMalloc(&ds->X32lo, b32) != cudaSuccess ||
-      cudaMalloc(&ds->y64, y64b) != cudaSuccess || cudaMalloc(&ds->y32, y32b) != cudaSuccess ||
-      cudaMalloc(&ds->y32lo, y32b) != cudaSuccess) {
-    cudaGetLastError();
-    rrg_dataset_destroy(ds);
-    rrc::set_error("rrg_dataset_create: out of device memory");
-    return RRG_E_OOM;
-  }
-  // pinned staging of the padded columns; FP32 copies are converted on the device
-  HostBuf stage;
-  if (!stage.reserve(b64 + y64b)) {
-    rrg_dataset_destroy(ds);
-    rrc::set_error("rrg_dataset_create: cannot pin staging memory");
-    return RRG_E_OOM;
-  }
-  double* hx = static_cast<double*>(stage.ptr);
-  std::memset(hx, 0, b64 + y64b);
-  for (int64_t j = 0; j < d; ++j) std::memcpy(hx + j * ds->n_pad, X_col + j * n, sizeof(double) * n);
-  std::memcpy(hx + cols * ds->n_pad, y, sizeof(double) * n);
-  cudaStream_t st = ctx->stream;
-  bool ok = cudaMemcpyAsync(ds->X64, hx, b64, cudaMemcpyHostToDevice, st) == cudaSuccess &&
-            cudaMemcpyAsync(ds->y64, hx + cols * ds->n_pad, y64b, cudaMemcpyHostToDevice, st) == cudaSuccess;
-  if (ok)
-    ok = launch_split_f32(ds->X64, ds->X32, ds->X32lo, ds->n_pad * cols, st) &&
-         launch_split_f32(ds->y64, ds->y32, ds->y32lo, ds->n_pad, st);
-  ok = ok && cudaStreamSynchronize(st) == cudaSuccess;
-  stage.release();
-  if (!ok) {
-    cuda_ok(cudaGetLastError(), "dataset upload");
-    rrg_dataset_destroy(ds);
-    return RRG_E_CUDA;
-  }
-  *out = ds;
-  return RRG_OK;
+  if (!dataset_args_ok(ctx, X_col, y, n, d, out)) return RRG_E_INVALID;
+  // each column straight into its padded place (one 2-D copy)
+  return make_dataset(ctx, y, n, d, out, [&](rrg_dataset* ds, cudaStream_t st) {
+    return d == 0 || cudaMemcpy2DAsync(ds->X64, sizeof(double) * ds->n_pad, X_col, sizeof(double) * n,
+                                       sizeof(double) * n, d, cudaMemcpyHostToDevice, st) == cudaSuccess;
+  });
+}
+
+rrg_status rrg_dataset_create_rows(rrg_context* ctx, const double* X_rows, const double* y, int64_t n, int32_t d,
+                                   rrg_dataset** out) {
+  if (!dataset_args_ok(ctx, X_rows, y, n, d, out)) return RRG_E_INVALID;
+  // the rows as given, then transposed on the device (a stream-ordered
+  // temporary)
+  return make_dataset(ctx, y, n, d, out, [&](rrg_dataset* ds, cudaStream_t st) {
+    if (d == 0) return true;
+    void* raw = nullptr;
+    const size_t bytes = sizeof(double) * (size_t)n * d;
+    if (cudaMallocAsync(&raw, bytes, st) != cudaSuccess) return false;
+    bool ok = cudaMemcpyAsync(raw, X_rows, bytes, cudaMemcpyHostToDevice, st) == cudaSuccess;
+    if (ok) {
+      const int64_t blocks = std::min<int64_t>((ds->n_pad + 255) / 256, 8LL * ctx->sm_count);
+      rows_to_cols_kernel<<<(int)blocks, 256, 0, st>>>(static_cast<const double*>(raw), n, d, ds->n_pad, ds->X64);
+      ok = cudaGetLastError() == cudaSuccess;
+    }
+    return cudaFreeAsync(raw, st) == cudaSuccess && ok;
+  });
 }
 
 rrg_status rrg_dataset_destroy(rrg_dataset* ds) {

@@ -73,6 +73,7 @@ class ServeStats(C.Structure):
 # Every symbol the headers declare (checked by the CPU test suite).
 EXPORTS = [
     "rrg_abi_version", "rrg_last_error", "rrg_context_create", "rrg_context_destroy", "rrg_dataset_create",
+    "rrg_dataset_create_rows",
     "rrg_dataset_destroy", "rrg_round_submit", "rrg_round_wait", "rrg_eval", "rrg_predict", "rrg_batch_validate", "rrg_dataset_rows",
     "rrg_dataset_cols", "rrg_last_round_launches", "rrg_last_round_stats", "rrg_context_stream",
     "rrg_context_set_timing", "rrg_last_round_timing", "rrg_last_round_bytes", "rrg_eval_plain_noalloc", "rrg_context_set_limits",
@@ -98,6 +99,7 @@ def _declare(lib):
         "rrg_context_create": (i32, [i32, P(vp)]),
         "rrg_context_destroy": (i32, [vp]),
         "rrg_dataset_create": (i32, [vp, dp, dp, i64, i32, P(vp)]),
+        "rrg_dataset_create_rows": (i32, [vp, dp, dp, i64, i32, P(vp)]),
         "rrg_dataset_destroy": (i32, [vp]),
         "rrg_round_submit": (i32, [vp, P(Batch), i32, P(Result), dp]),
         "rrg_round_wait": (i32, [vp, i32]),

@@ -176,14 +176,20 @@ class Dataset:
         if X.ndim == 1:
             X = X[:, None]
         self.n, self.d = X.shape
-        Xcol = np.ascontiguousarray(X.T)
         yv = np.ascontiguousarray(np.asarray(y, dtype=np.float64).reshape(-1))
         if len(yv) != self.n:
             raise ValueError("X and y disagree on the number of rows")
         h = C.c_void_p()
         dp = C.POINTER(C.c_double)
-        check(ctx.lib.rrg_dataset_create(ctx.h, Xcol.ctypes.data_as(dp), yv.ctypes.data_as(dp), self.n, self.d,
-                                         C.byref(h)), "rrg_dataset_create")
+        if X.flags.f_contiguous and not X.flags.c_contiguous:
+            # columns already contiguous
+            check(ctx.lib.rrg_dataset_create(ctx.h, X.ctypes.data_as(dp), yv.ctypes.data_as(dp), self.n, self.d,
+                                             C.byref(h)), "rrg_dataset_create")
+        else:
+            # rows as given (the device transposes)
+            Xr = np.ascontiguousarray(X)
+            check(ctx.lib.rrg_dataset_create_rows(ctx.h, Xr.ctypes.data_as(dp), yv.ctypes.data_as(dp), self.n,
+                                                  self.d, C.byref(h)), "rrg_dataset_create_rows")
         self.h = h
 
     def evaluate(self, batch: EncodedBatch, precision: int = PLAIN) -> dict:
