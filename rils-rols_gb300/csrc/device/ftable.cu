@@ -42,6 +42,24 @@ __device__ __forceinline__ dfl warp_dfl_sum(dfl v) {
   return v;
 }
 
+// Running sum s += p + e in the manner of Sum2 (Ogita, Rump and Oishi, 2005):
+// p joins the high part by an exact two-sum (Knuth), its rounding error and
+// the small term e join the low part, which is not renormalised per step.
+__device__ __forceinline__ void acc2(dfl& s, float p, float e) {
+  const float t = DF_ADD(s.hi, p);
+  const float bp = DF_SUB(t, s.hi);
+  const float err = DF_ADD(DF_SUB(s.hi, DF_SUB(t, bp)), DF_SUB(p, bp));
+  s.hi = t;
+  s.lo = DF_ADD(s.lo, DF_ADD(err, e));
+}
+// hi + lo as a normalised double-float (|lo| small against |hi|, or hi = 0);
+// non-finite parts pass through
+__device__ __forceinline__ dfl dfl_renorm(dfl s) {
+  if (!dfl_finite(s.hi) || !dfl_finite(s.lo)) return s;
+  const float t = DF_ADD(s.hi, s.lo);
+  return dfl_make(t, DF_SUB(s.lo, DF_SUB(t, s.hi)));
+}
+
 // One table program on 2 consecutive rows (r, r + 1 of the chunk); X column
 // j has its high parts at xh + j * ldx and its low parts at xl + j * ldx;
 // table column t (an earlier level) at tb + t * ldtab.
@@ -232,7 +250,6 @@ __global__ void __launch_bounds__(kFacThreads) fac_eval_kernel(FacEvalArgs a) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int2 grp = a.groups[blockIdx.x];
   const int q = blockIdx.y;
-  const int d = a.ds.d;
   const int64_t n = a.ds.n, n_pad = a.ds.n_pad;
   const int64_t row0 = (int64_t)q * a.chunk;
   const int rows = (int)min((int64_t)a.chunk, n_pad - row0);  // a multiple of 256
@@ -295,19 +312,17 @@ __global__ void __launch_bounds__(kFacThreads) fac_eval_kernel(FacEvalArgs a) {
 #pragma unroll
       for (int u = 0; u < R; ++u) fin = fin && dfl_finite(v[u].hi);
       if (__all_sync(0xffffffffu, fin)) {
-        // finite values (the common case): the rows' terms are added first,
-        // without the non-finite guards
-        dfl sq = dfl_add_nc(dfl_mul_nc(v[0], v[0]), dfl_mul_nc(v[1], v[1]));
-        dfl sv = dfl_add_nc(v[0], v[1]);
-        dfl sy = dfl_add_nc(dfl_mul_nc(v[0], y[0]), dfl_mul_nc(v[1], y[1]));
-        if constexpr (R == 4) {
-          sq = dfl_add_nc(sq, dfl_add_nc(dfl_mul_nc(v[2], v[2]), dfl_mul_nc(v[3], v[3])));
-          sv = dfl_add_nc(sv, dfl_add_nc(v[2], v[3]));
-          sy = dfl_add_nc(sy, dfl_add_nc(dfl_mul_nc(v[2], y[2]), dfl_mul_nc(v[3], y[3])));
+        // finite values (the common case): each product's high part joins
+        // the running high part by an exact two-sum; its low part and the
+        // two-sum's error join the low part (renormalised after the loop)
+#pragma unroll
+        for (int u = 0; u < R; ++u) {
+          const float p2 = DF_MUL(v[u].hi, v[u].hi);
+          acc2(ff, p2, DF_FMA(DF_ADD(v[u].hi, v[u].hi), v[u].lo, DF_FMA(v[u].hi, v[u].hi, -p2)));
+          acc2(fs, v[u].hi, v[u].lo);
+          const float py = DF_MUL(v[u].hi, y[u].hi);
+          acc2(fy, py, DF_FMA(v[u].lo, y[u].hi, DF_FMA(v[u].hi, y[u].lo, DF_FMA(v[u].hi, y[u].hi, -py))));
         }
-        ff = dfl_add_nc(ff, sq);
-        fs = dfl_add_nc(fs, sv);
-        fy = dfl_add_nc(fy, sy);
       } else {
 #pragma unroll
         for (int u = 0; u < R; ++u) {
@@ -324,7 +339,7 @@ __global__ void __launch_bounds__(kFacThreads) fac_eval_kernel(FacEvalArgs a) {
       first = other < first ? other : first;
     }
     if (lane == 0 && first != ~0ull) atomicMin(a.fnan + f, first);
-    const dfl s0 = warp_dfl_sum(ff), s1 = warp_dfl_sum(fs), s2 = warp_dfl_sum(fy);
+    const dfl s0 = warp_dfl_sum(dfl_renorm(ff)), s1 = warp_dfl_sum(dfl_renorm(fs)), s2 = warp_dfl_sum(dfl_renorm(fy));
     if (lane == 0) {
       float* rw = red + warp * 6;
       rw[0] = s0.hi; rw[1] = s0.lo;
@@ -369,11 +384,13 @@ __global__ void __launch_bounds__(kPairThreads) pair_sum_kernel(PairArgs a) {
           // without the non-finite guards: a non-finite factor value turns the
           // sum NaN instead of +-inf, and the solve sends every candidate with a
           // non-finite cross sum (NaN or inf alike) to the FP64 path
-          acc = dfl_add_nc(acc, dfl_add_nc(dfl_mul_nc(dfl_make(av[s].x, av[s].y), dfl_make(bv.x, bv.y)),
-                                           dfl_mul_nc(dfl_make(av[s].z, av[s].w), dfl_make(bv.z, bv.w))));
+          const float p0v = DF_MUL(av[s].x, bv.x);
+          acc2(acc, p0v, DF_FMA(av[s].y, bv.x, DF_FMA(av[s].x, bv.y, DF_FMA(av[s].x, bv.x, -p0v))));
+          const float p1v = DF_MUL(av[s].z, bv.z);
+          acc2(acc, p1v, DF_FMA(av[s].w, bv.z, DF_FMA(av[s].z, bv.w, DF_FMA(av[s].z, bv.z, -p1v))));
         }
       }
-      const dfl v = warp_dfl_sum(acc);
+      const dfl v = warp_dfl_sum(dfl_renorm(acc));
       if (lane == 0) {
         red[j][warp][0] = v.hi;
         red[j][warp][1] = v.lo;
