@@ -431,16 +431,22 @@ DFN dfl dfl_log(dfl x) {
 }
 
 /* ---- sin / cos ---- */
-/* r = x - k pi/2 with pi/2 = P1 + P2 + P3 + P4; returns the quadrant k mod 4,
- * or -1 when |k| >= 4096 (the reduction is not exact there) */
+/* r = x - k pi/2 with pi/2 = P1 + P2 + P3 + P4 (P1, P2 of 12 bits); returns
+ * the quadrant k mod 4, or -1 when |k| >= 4096 (the reduction is not exact
+ * there).  x.hi - k P1 is exact (both are multiples of the smaller one's ulp
+ * and the difference is below 0.8), k P2 and k P3 are exact products, the
+ * sums of the leading parts are exact two-sums, and only terms below 2^-24
+ * of r are added in rounded arithmetic. */
 DFN int dfl_reduce_half_pi(dfl x, dfl* r) {
   const float k = rintf(DF_MUL(x.hi, 0.6366197466850281f));
   if (!(fabsf(k) < 4096.0f)) return -1;
-  dfl t = dfl_add_fl(x, -DF_MUL(k, 1.57080078125f));
-  t = dfl_add_fl(t, -DF_MUL(k, -4.453584551811218e-06f));
-  t = dfl_add_nc(t, dfl_two_prod(-k, -8.705515752716053e-10f));
-  t = dfl_add_nc(t, dfl_two_prod(-k, 5.721188916458728e-18f));
-  *r = t;
+  const float a1 = DF_FMA(-k, 1.57080078125f, x.hi);
+  const dfl a2 = dfl_two_sum(a1, DF_MUL(k, 4.453584551811218e-06f));
+  const dfl p3 = dfl_two_prod(-k, -8.705515752716053e-10f);
+  const dfl a3 = dfl_two_sum(a2.hi, p3.hi);
+  const dfl a4 = dfl_two_sum(a3.hi, x.lo);
+  const float rl = DF_ADD(DF_ADD(DF_ADD(a2.lo, a3.lo), DF_ADD(p3.lo, a4.lo)), DF_MUL(-k, 5.721188916458728e-18f));
+  *r = dfl_fast_two_sum(a4.hi, rl);
   const int ki = (int)k;
   return ki & 3;
 }
@@ -448,8 +454,12 @@ DFN int dfl_reduce_half_pi(dfl x, dfl* r) {
  * quadrant: x = k pi/2 + r, r = j/32 + s with |s| <= 1/64, sin(j/32) and
  * cos(j/32) from a table, and sin(x + shift pi/2) = A cos s + B sin s with
  * (A, B) = (S, C), (C, -S), (-S, -C), (-C, S) for the quadrant k + shift;
- * sin s = s - s^3/6 + s^5 (1/120 - s^2/5040) and cos s - 1 = -s^2/2 +
- * s^4 (1/24 - s^2/720), the s^5 and s^4 terms in FP32 */
+ * sin s = s + s q with q = -s^2/6 + s^4 (1/120 - s^2/5040) and cos s - 1 =
+ * -s^2/2 + s^4 (1/24 - s^2/720).  Intermediates are unnormalised pairs: a
+ * rounded leading part, and a low part gathering the exact product and sum
+ * errors with the small terms (s^2/6 and s^2/2 carried as pairs, the s^4
+ * terms in FP32); the relative weight of every rounded low-part term is
+ * below 2^-40, so the result keeps about 2^-47. */
 DFN dfl dfl_sincos(dfl x, int shift) {
   if (!dfl_finite(x.hi)) return dfl_make(dfl_nanf(), 0.0f);
   dfl r;
@@ -458,18 +468,35 @@ DFN dfl dfl_sincos(dfl x, int shift) {
   const int q = (q0 + shift) & 3;
   const float jf = rintf(DF_MUL(r.hi, 32.0f));
   const int J = (int)jf + 26;
-  const dfl s = dfl_add_fl(r, -DF_MUL(jf, 0.03125f));
-  const dfl z = dfl_mul_nc(s, s);
-  const float zf = z.hi;
-  const float s5 = DF_MUL(DF_MUL(s.hi, DF_MUL(zf, zf)), DF_FMA(zf, -1.9841270113829523e-04f, 8.333333767950535e-03f));
-  const dfl sins = dfl_add_fl(dfl_add_nc(s, dfl_neg(dfl_mul_nc(dfl_mul_nc(s, z), dfl_make(DF_INV6_HI, DF_INV6_LO)))), s5);
-  const float z4 = DF_MUL(DF_MUL(zf, zf), DF_FMA(zf, -1.3888889225199819e-03f, 4.1666667908430099e-02f));
-  const dfl cm1 = dfl_add_fl(dfl_scale(z, -0.5f), z4);
+  const dfl s = dfl_two_sum(DF_FMA(-jf, 0.03125f, r.hi), r.lo); /* r.hi - j/32 is exact */
+  /* z = s^2 */
+  const float zh = DF_MUL(s.hi, s.hi);
+  const float zl = DF_FMA(DF_ADD(s.hi, s.hi), s.lo, DF_FMA(s.hi, s.hi, -zh));
+  /* q = -z/6 + z^2 (1/120 - z/5040) */
+  const float qh = DF_MUL(-zh, DF_INV6_HI);
+  const float ql = DF_FMA(-zl, DF_INV6_HI, DF_FMA(-zh, DF_INV6_LO, DF_FMA(-zh, DF_INV6_HI, -qh)));
+  const float q4 = DF_MUL(DF_MUL(zh, zh), DF_FMA(zh, -1.9841270113829523e-04f, 8.333333767950535e-03f));
+  /* sin s = s + s q, |s q| <= 4.1e-5 |s| */
+  const float sqh = DF_MUL(s.hi, qh);
+  const float sql = DF_FMA(s.lo, qh, DF_FMA(s.hi, DF_ADD(ql, q4), DF_FMA(s.hi, qh, -sqh)));
+  const dfl sn = dfl_fast_two_sum(s.hi, sqh);
+  const float snl = DF_ADD(sn.lo, DF_ADD(s.lo, sql));
+  /* cos s - 1 = ch + cl */
+  const float ch = DF_MUL(-0.5f, zh);
+  const float cl = DF_FMA(-0.5f, zl, DF_MUL(DF_MUL(zh, zh), DF_FMA(zh, -1.3888889225199819e-03f, 4.1666667908430099e-02f)));
   const dfl S = dfl_make(DFL_SCT(J, 0), DFL_SCT(J, 1)), C = dfl_make(DFL_SCT(J, 2), DFL_SCT(J, 3));
   dfl A = (q & 1) ? C : S, B = (q & 1) ? S : C;
   if (q & 2) A = dfl_neg(A);
   if ((q + 1) & 2) B = dfl_neg(B);
-  return dfl_add_nc(A, dfl_add_nc(dfl_mul_nc(A, cm1), dfl_mul_nc(B, sins)));
+  /* T = A (cos s - 1) + B sin s, then A + T */
+  const float ah = DF_MUL(A.hi, ch);
+  const float al = DF_FMA(A.lo, ch, DF_FMA(A.hi, cl, DF_FMA(A.hi, ch, -ah)));
+  const float bh = DF_MUL(B.hi, sn.hi);
+  const float bl = DF_FMA(B.lo, sn.hi, DF_FMA(B.hi, snl, DF_FMA(B.hi, sn.hi, -bh)));
+  const dfl t = dfl_two_sum(bh, ah);
+  const float tl = DF_ADD(t.lo, DF_ADD(al, bl));
+  const dfl u = dfl_two_sum(A.hi, t.hi);
+  return dfl_fast_two_sum(u.hi, DF_ADD(u.lo, DF_ADD(A.lo, tl)));
 }
 DFN dfl dfl_sin(dfl x) { return dfl_sincos(x, 0); }
 DFN dfl dfl_cos(dfl x) { return dfl_sincos(x, 1); }
