@@ -53,6 +53,23 @@
 #define DF_SQRT(a) sqrtf(a)
 #endif
 
+/* an approximate reciprocal (within a few ulp; a Newton step follows every
+ * use): the special-function unit's on the device, the exact quotient on the
+ * host */
+static
+#if defined(__CUDACC__)
+    __host__ __device__
+#endif
+    inline float df_rcp_approx(float y) {
+#if defined(__CUDA_ARCH__)
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(y));
+  return r;
+#else
+  return 1.0f / y;
+#endif
+}
+
 typedef struct {
   float hi, lo;
 } dfl;
@@ -180,6 +197,18 @@ DFN dfl dfl_add_fl(dfl x, float a) {
 DFN dfl dfl_mul_fl(dfl x, float a) {
   const dfl c = dfl_two_prod(x.hi, a);
   return dfl_fast_two_sum(c.hi, DF_FMA(x.lo, a, c.lo));
+}
+/* x / y for finite operands and a finite quotient: 1/y.hi from the
+ * approximate reciprocal and one Newton step (relative error near 2^-44),
+ * th = x.hi / y.hi rounded, then the remainder x - th y (its leading part
+ * by FMA, exact for a faithful th) times 1/y.hi as the low part.  A
+ * non-finite leading part means the guarded dfl_div has to run. */
+DFN dfl dfl_div_nc(dfl x, dfl y) {
+  const float r0 = df_rcp_approx(y.hi);
+  const float r1 = DF_FMA(r0, DF_FMA(-y.hi, r0, 1.0f), r0);
+  const float th = DF_MUL(x.hi, r1);
+  const float rem = DF_ADD(DF_FMA(-th, y.lo, DF_FMA(-th, y.hi, x.hi)), x.lo);
+  return dfl_fast_two_sum(th, DF_MUL(rem, r1));
 }
 
 /* ---- tables ---- */
@@ -357,23 +386,38 @@ DFN dfl dfl_exp(dfl x) {
   if (x.hi > 88.72f) return dfl_make(dfl_inff(), 0.0f);
   if (x.hi < -103.5f) return dfl_make(0.0f, 0.0f);
   const float kf = rintf(DF_MUL(x.hi, 46.16624130844683f)); /* 32 / ln 2; |k| < 2^13 */
-  /* r = x - k ln2/32, |r| <= ln2/64 (k C1 and k C2 exact: 11-bit constants) */
-  dfl r = dfl_add_fl(x, -DF_MUL(kf, DF_LN2_32_C1));
-  r = dfl_add_fl(r, -DF_MUL(kf, DF_LN2_32_C2));
-  r = dfl_add_nc(r, dfl_two_prod(-kf, DF_LN2_32_C3));
-  r = dfl_add_fl(r, -DF_MUL(kf, DF_LN2_32_C4));
-  /* expm1(r) = r + r^2 (1/2 + r/6) + r^4 (1/24 + r/120 + r^2/720), the last term in FP32 (< 6e-10) */
-  const float rf = r.hi, r2f = DF_MUL(rf, rf);
-  const float tail = DF_MUL(DF_MUL(r2f, r2f),
-                            DF_FMA(DF_FMA(rf, 1.3888889225e-3f, 8.333333768e-3f), rf, 4.166666791e-2f));
-  const dfl q = dfl_add_fl(dfl_mul_nc(r, dfl_make(0.1666666716337204f, -4.967053879312289e-09f)), 0.5f);
-  dfl em = dfl_add_nc(r, dfl_mul_nc(dfl_mul_nc(r, r), q));
-  em = dfl_add_fl(em, tail);
+  /* r = x - k ln2/32, |r| <= ln2/64: x.hi - k C1 is exact (C1 and C2 have 11
+   * bits), the leading sums are exact two-sums, only terms below 2^-24 of r
+   * are added rounded */
+  const float a1 = DF_FMA(-kf, DF_LN2_32_C1, x.hi);
+  const dfl a2 = dfl_two_sum(a1, DF_MUL(-kf, DF_LN2_32_C2));
+  const dfl p3 = dfl_two_prod(-kf, DF_LN2_32_C3);
+  const dfl a3 = dfl_two_sum(a2.hi, p3.hi);
+  const dfl a4 = dfl_two_sum(a3.hi, x.lo);
+  const float rlo = DF_ADD(DF_ADD(DF_ADD(a2.lo, a3.lo), DF_ADD(p3.lo, a4.lo)), DF_MUL(-kf, DF_LN2_32_C4));
+  const dfl r = dfl_fast_two_sum(a4.hi, rlo);
+  /* expm1(r) = r + z P, z = r^2, P = 1/2 + r/6 + z (1/24 + r/120 + z/720):
+   * z and r/6 as unnormalised pairs, 1/2 + r/6 by an exact two-sum, the z
+   * term of P in FP32 (below 5e-6) */
+  const float zh = DF_MUL(r.hi, r.hi);
+  const float zl = DF_FMA(DF_ADD(r.hi, r.hi), r.lo, DF_FMA(r.hi, r.hi, -zh));
+  const float p6h = DF_MUL(r.hi, DF_INV6_HI);
+  const float p6l = DF_FMA(r.lo, DF_INV6_HI, DF_FMA(r.hi, DF_INV6_LO, DF_FMA(r.hi, DF_INV6_HI, -p6h)));
+  const float pz = DF_MUL(zh, DF_FMA(zh, 1.3888889225e-3f, DF_FMA(r.hi, 8.333333768e-3f, 4.166666791e-2f)));
+  const dfl ph = dfl_two_sum(0.5f, p6h);
+  const float pl = DF_ADD(ph.lo, DF_ADD(p6l, pz));
+  const float zph = DF_MUL(zh, ph.hi);
+  const float zpl = DF_FMA(zl, ph.hi, DF_FMA(zh, pl, DF_FMA(zh, ph.hi, -zph)));
+  const dfl e0 = dfl_fast_two_sum(r.hi, zph); /* |z P| <= 0.0055 |r| */
+  const float eml = DF_ADD(e0.lo, DF_ADD(r.lo, zpl));
   /* 2^(j/32) (1 + em) 2^m, k = 32 m + j */
   const int k = (int)kf;
   const int jj = k & 31, m = (k - jj) / 32;
   const dfl t = dfl_make(DFL_EXP2(jj, 0), DFL_EXP2(jj, 1));
-  dfl e = dfl_add_nc(t, dfl_mul_nc(t, em));
+  const float teh = DF_MUL(t.hi, e0.hi);
+  const float tel = DF_FMA(t.lo, e0.hi, DF_FMA(t.hi, eml, DF_FMA(t.hi, e0.hi, -teh)));
+  const dfl u = dfl_two_sum(t.hi, teh);
+  dfl e = dfl_fast_two_sum(u.hi, DF_ADD(u.lo, DF_ADD(t.lo, tel)));
   /* times 2^m in two exact steps (m in [-150, 128]) */
   const int m1 = m / 2, m2 = m - m1;
   e = dfl_scale(e, dfl_pow2(m1));
@@ -414,20 +458,39 @@ DFN dfl dfl_log(dfl x) {
   /* c = 1 + j/64 nearest to m (j in [-19, 27]); t = (m - c) / c, |t| <= 0.011 */
   const float jf = rintf(DF_MUL(DF_SUB(m.hi, 1.0f), 64.0f));
   const int J = (int)jf + 19;
-  const dfl d = dfl_add_fl(m, -DF_FMA(jf, 0.015625f, 1.0f));
-  const dfl t = dfl_mul_nc(d, dfl_make(DFL_LOGT(J, 0), DFL_LOGT(J, 1)));
-  /* log1p(t) = t (1 - t (1/2 - t (1/3 - t/4))) + t^5 (1/5 - t/6 + t^2/7 - t^3/8), the last term in FP32 */
-  const float tf = t.hi, t2f = DF_MUL(tf, tf);
-  const float tail = DF_MUL(DF_MUL(t2f, DF_MUL(t2f, tf)),
-                            DF_FMA(DF_FMA(DF_FMA(tf, -0.125f, 0.1428571492433548f), tf, -0.1666666716337204f), tf,
-                                   0.2f));
-  dfl p = dfl_add_nc(dfl_make(0.3333333432674408f, -9.934107758624577e-09f), dfl_scale(t, -0.25f));
-  p = dfl_add_fl(dfl_neg(dfl_mul_nc(p, t)), 0.5f);
-  p = dfl_add_fl(dfl_neg(dfl_mul_nc(p, t)), 1.0f);
-  p = dfl_add_fl(dfl_mul_nc(p, t), tail);
-  const dfl lm = dfl_add_nc(dfl_make(DFL_LOGT(J, 2), DFL_LOGT(J, 3)), p);
-  /* + (e - shift) ln 2 */
-  return dfl_add_nc(lm, dfl_mul_fl(dfl_make(0.6931471824645996f, -1.9046542121259336e-09f), (float)(e - shift)));
+  /* t = (m - c)/c: m.hi - c is exact, m - c normalised by a two-sum, times
+   * 1/c (a pair) */
+  const float c = DF_FMA(jf, 0.015625f, 1.0f);
+  const dfl d = dfl_two_sum(DF_SUB(m.hi, c), m.lo);
+  const float ih = DFL_LOGT(J, 0), il = DFL_LOGT(J, 1);
+  const float th0 = DF_MUL(d.hi, ih);
+  const dfl t = dfl_fast_two_sum(th0, DF_FMA(d.lo, ih, DF_FMA(d.hi, il, DF_FMA(d.hi, ih, -th0))));
+  /* log1p(t) = t + z Q, z = t^2, Q = -1/2 + t/3 - z/4 + t z (1/5 - t/6 + z/7 - t z/8 + z^2/9):
+   * z and t/3 as unnormalised pairs, -1/2 + t/3 - z/4 by exact two-sums, the
+   * t z term in FP32 (below 3e-7) */
+  const float zh = DF_MUL(t.hi, t.hi);
+  const float zl = DF_FMA(DF_ADD(t.hi, t.hi), t.lo, DF_FMA(t.hi, t.hi, -zh));
+  const float p3h = DF_MUL(t.hi, 0.3333333432674408f);
+  const float p3l = DF_FMA(t.lo, 0.3333333432674408f,
+                           DF_FMA(t.hi, -9.934107758624577e-09f, DF_FMA(t.hi, 0.3333333432674408f, -p3h)));
+  const dfl q1 = dfl_two_sum(-0.5f, p3h);
+  const dfl q2 = dfl_two_sum(q1.hi, DF_MUL(-0.25f, zh));
+  const float inner = DF_FMA(DF_FMA(DF_FMA(DF_FMA(t.hi, 0.1111111119389534f, -0.125f), t.hi, 0.1428571492433548f),
+                                    t.hi, -0.1666666716337204f),
+                             t.hi, 0.2f);
+  const float qt = DF_MUL(DF_MUL(t.hi, zh), inner);
+  const float ql = DF_ADD(DF_ADD(q1.lo, q2.lo), DF_ADD(DF_FMA(-0.25f, zl, p3l), qt));
+  const float zqh = DF_MUL(zh, q2.hi);
+  const float zql = DF_FMA(zl, q2.hi, DF_FMA(zh, ql, DF_FMA(zh, q2.hi, -zqh)));
+  const dfl l0 = dfl_fast_two_sum(t.hi, zqh); /* |z Q| <= 0.0057 |t| */
+  /* + log c + (e - shift) ln 2: the leading parts by exact steps */
+  const float ef = (float)(e - shift);
+  const dfl a = dfl_two_prod(ef, 0.6931471824645996f);
+  const dfl b = dfl_two_sum(a.hi, DFL_LOGT(J, 2));
+  const dfl s = dfl_two_sum(b.hi, l0.hi);
+  const float lo = DF_ADD(DF_ADD(DF_ADD(s.lo, b.lo), DF_ADD(a.lo, DF_MUL(ef, -1.9046542121259336e-09f))),
+                          DF_ADD(DFL_LOGT(J, 3), DF_ADD(l0.lo, DF_ADD(t.lo, zql))));
+  return dfl_fast_two_sum(s.hi, lo);
 }
 
 /* ---- sin / cos ---- */

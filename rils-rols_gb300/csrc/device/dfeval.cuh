@@ -31,12 +31,22 @@ __device__ __forceinline__ dfl df_unary(int op, dfl a) {
   }
 }
 
+// Division: the reciprocal form (dfl_div_nc) first; a zero, tiny or
+// non-finite divisor or a non-finite quotient gives a non-finite leading part,
+// and then the guarded dfl_div decides the row.  The two forms agree to about
+// 2^-47 on finite quotients, and every evaluator (table and probe) takes the
+// same form for the same row.
+__device__ __forceinline__ dfl df_div(dfl a, dfl b) {
+  const dfl r = dfl_div_nc(a, b);
+  return dfl_finite(r.hi) ? r : dfl_div(a, b);
+}
+
 __device__ __forceinline__ dfl df_bin(int base, dfl a, dfl b) {
   switch (base) {
     case RRG_ADD: return dfl_add(a, b);
     case RRG_SUB: return dfl_sub(a, b);
     case RRG_MUL: return dfl_mul(a, b);
-    case RRG_DIV: return dfl_div(a, b);
+    case RRG_DIV: return df_div(a, b);
     case RRG_POW: return df_pow_call(a, b);
     case RRG_LT: return dfl_make(dfl_lt(a, b) ? 1.f : 0.f, 0.f);
     case RRG_EQ: return dfl_make(dfl_eq(a, b) ? 1.f : 0.f, 0.f);
@@ -73,6 +83,10 @@ __device__ __forceinline__ void df_bin2(int base, dfl a0, dfl b0, dfl a1, dfl b1
         r0 = dfl_mul(a0, b0);
         r1 = dfl_mul(a1, b1);
       }
+      return;
+    case RRG_DIV:
+      r0 = df_div(a0, b0);
+      r1 = df_div(a1, b1);
       return;
     default:
       r0 = df_bin(base, a0, b0);
