@@ -441,9 +441,13 @@ def classifier_leg(args):
             t = time.perf_counter()
             m.fit(X.reshape(-1), lab, n, X.shape[1])
             dt = time.perf_counter() - t
+            cnt = m.counters()
             pred = m.predict(X.reshape(-1), n, X.shape[1])
             row[name] = {"fit_s": dt, "fit_calls": m.get_fit_calls(), "model": m.get_model_string(),
-                         "train_accuracy": float(np.mean(pred == lab))}
+                         "train_accuracy": float(np.mean(pred == lab)),
+                         # wall time inside the fitness backend; the rest is the host search
+                         "backend_s": cnt["backend_ns"] / 1e9, "rounds": cnt["device_rounds"],
+                         "candidates": cnt["candidates_scored"]}
         if "cpu_oracle" in row:
             row["device_fp64_equals_cpu"] = row["plain_fp64"]["model"] == row["cpu_oracle"]["model"]
         row["certified_equals_fp64"] = row["certified"]["model"] == row["plain_fp64"]["model"]

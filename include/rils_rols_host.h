@@ -61,7 +61,9 @@ int32_t rrh_model_prefix(const rrh_model* m, char* buf, int32_t cap);
 double rrh_best_time(const rrh_model* m);
 double rrh_total_time(const rrh_model* m);
 int32_t rrh_fit_calls(const rrh_model* m);
-/* Counters beyond the reference's: LS calls, device rounds, candidates scored. */
+/* Counters beyond the reference's: [0] LS calls, [1] main-loop iterations,
+ * [2] backend rounds, [3] candidates scored, [4] skipped and [5] all
+ * perturbations, [6] nanoseconds spent in the fitness backend. */
 int64_t rrh_counter(const rrh_model* m, int32_t which);
 const char* rrh_last_error(void);
 

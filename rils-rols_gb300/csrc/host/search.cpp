@@ -355,7 +355,9 @@ void Search::run_batch(std::vector<rrg_result>& res, std::vector<double>& coefs)
   rrg_batch b = bb_.view();
   res.assign(b.n_cand, rrg_result{});
   coefs.assign(bb_.n_coefs() > 0 ? bb_.n_coefs() : 1, 0.0);
+  const auto t0 = std::chrono::steady_clock::now();
   int32_t st = backend_.eval(dataset_, &b, precision_, res.data(), coefs.data());
+  backend_ns_ += std::chrono::duration_cast<std::chrono::nanoseconds>(std::chrono::steady_clock::now() - t0).count();
   if (st != RRG_OK) throw std::runtime_error(std::string("fitness backend failed: ") + rrg_last_error());
   ++n_rounds_;
   n_scored_ += b.n_cand;
@@ -597,6 +599,7 @@ int64_t Search::counter(int which) const {
     case 3: return n_scored_;
     case 4: return skipped_perts_;
     case 5: return total_perts_;
+    case 6: return backend_ns_;
     default: return -1;
   }
 }

@@ -112,6 +112,7 @@ class Search {
   BatchBuilder bb_;
   Arena arena_;
   int64_t n_rounds_ = 0, n_scored_ = 0;
+  int64_t backend_ns_ = 0;  // wall time inside the fitness backend (device rounds)
 };
 
 }  // namespace rrh

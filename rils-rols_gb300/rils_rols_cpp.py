@@ -40,7 +40,8 @@ class rils_rols:  # noqa: N801 - name of the reference class
         _lib.check(self._lib.rrh_set_precision(self._h, int(p)), "rrh_set_precision")
 
     def counters(self) -> dict:
-        names = ["ls_calls", "main_it", "device_rounds", "candidates_scored", "skipped_perts", "total_perts"]
+        names = ["ls_calls", "main_it", "device_rounds", "candidates_scored", "skipped_perts", "total_perts",
+                 "backend_ns"]
         return {n: int(self._lib.rrh_counter(self._h, i)) for i, n in enumerate(names)}
 
     def get_model_prefix(self) -> str:
