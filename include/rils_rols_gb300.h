@@ -239,6 +239,13 @@ int32_t rrg_last_round_stats(const rrg_context* ctx, int64_t* out, int32_t n);
  * No counterpart in the reference (single-threaded, one fit per process). */
 rrg_status rrg_context_set_limits(rrg_context* ctx, int64_t scratch_bytes, int64_t table_bytes);
 
+/* Rounds in RRG_MIXED / RRG_MIXED_CERTIFIED on datasets with fewer than
+ * `rows` rows (default 8192) are computed in FP64 instead: there the mixed
+ * form's probes, pair sums and read-backs cost more than the FP64 arithmetic
+ * they replace, and FP64 results meet any certified bound.  0 always takes
+ * the mixed form.  No counterpart in the reference. */
+rrg_status rrg_context_set_mixed_min_rows(rrg_context* ctx, int64_t rows);
+
 /* Free and total memory of a device (cudaMemGetInfo); RRG_E_NO_DEVICE without
  * one.  No counterpart in the reference. */
 rrg_status rrg_device_memory(int32_t device, int64_t* free_bytes, int64_t* total_bytes);

@@ -268,6 +268,7 @@ __global__ void __launch_bounds__(kFacThreads) fac_eval_kernel(FacEvalArgs a) {
   const float* yh = a.ds.y32 + row0;
   const float* yl = a.ds.y32lo + row0;
   const float2* tb = a.F + row0;
+  const bool tail = row0 + rows > n;  // the chunk holds padding rows (set to 0)
   float4* st = stk + (size_t)warp * kMixedStackCap * 32 * 2 + lane;
   for (int i = 0; i < grp.y; ++i) {
     const int f = grp.x + i;
@@ -285,10 +286,10 @@ __global__ void __launch_bounds__(kFacThreads) fac_eval_kernel(FacEvalArgs a) {
         v[2] = v[3] = dfl_make(0.f, 0.f);
       }
       const int64_t gr = row0 + r;
+      if (tail) {
 #pragma unroll
-      for (int u = 0; u < R; ++u) {
-        if (gr + u >= n) v[u] = dfl_make(0.f, 0.f);
-        if (v[u].hi != v[u].hi) first = min(first, (unsigned long long)(gr + u));
+        for (int u = 0; u < R; ++u)
+          if (gr + u >= n) v[u] = dfl_make(0.f, 0.f);
       }
       *reinterpret_cast<float4*>(a.F + (int64_t)f * n_pad + gr) = make_float4(v[0].hi, v[0].lo, v[1].hi, v[1].lo);
       if constexpr (R == 4)
@@ -324,8 +325,10 @@ __global__ void __launch_bounds__(kFacThreads) fac_eval_kernel(FacEvalArgs a) {
           acc2(fy, py, DF_FMA(v[u].lo, y[u].hi, DF_FMA(v[u].hi, y[u].lo, DF_FMA(v[u].hi, y[u].hi, -py))));
         }
       } else {
+        // a non-finite value in the warp: guarded sums, and the first NaN row
 #pragma unroll
         for (int u = 0; u < R; ++u) {
+          if (v[u].hi != v[u].hi) first = min(first, (unsigned long long)(gr + u));
           ff = dfl_add(ff, dfl_mul(v[u], v[u]));
           fs = dfl_add(fs, v[u]);
           fy = dfl_add(fy, dfl_mul(v[u], y[u]));

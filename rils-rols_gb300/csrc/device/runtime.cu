@@ -403,7 +403,10 @@ rrg_status rrg_context::submit(rrg_dataset* ds, const rrg_batch* b, int32_t prec
   build_factor_table(host_cands.data(), b->n_cand, b->code, b->consts, ft);
   std::vector<int32_t> reps;
   dedup_candidates(reps);
-  if (precision == RRG_PLAIN_FP64) {
+  // on small datasets the mixed form's probes, pair sums and read-backs cost
+  // more than the FP64 arithmetic they replace: such rounds run in FP64
+  // (exact, so within any certified bound)
+  if (precision == RRG_PLAIN_FP64 || ds->n < mixed_min_rows) {
     // few candidates on tall data: the tiled QR spreads each over the GPU;
     // otherwise one block per candidate over the shared FP64 factor table
     if (ds->n >= 65536 && (int64_t)reps.size() < 2 * sm_count) st = run_plain(ds, 0, 0, false, &reps);
@@ -792,6 +795,15 @@ void* rrg_context_stream(const rrg_context* ctx) { return ctx ? (void*)ctx->stre
 rrg_status rrg_context_set_timing(rrg_context* ctx, int32_t on) {
   if (!ctx) return RRG_E_INVALID;
   ctx->timing = on != 0;
+  return RRG_OK;
+}
+
+rrg_status rrg_context_set_mixed_min_rows(rrg_context* ctx, int64_t rows) {
+  if (!ctx || rows < 0) {
+    rrc::set_error("rrg_context_set_mixed_min_rows: invalid arguments");
+    return RRG_E_INVALID;
+  }
+  ctx->mixed_min_rows = rows;
   return RRG_OK;
 }
 

@@ -137,6 +137,11 @@ class Context:
     def set_timing(self, on: bool = True) -> None:
         check(self.lib.rrg_context_set_timing(self.h, int(on)), "rrg_context_set_timing")
 
+    def set_mixed_min_rows(self, rows: int) -> None:
+        """Datasets with fewer rows run mixed-precision rounds in FP64 (default
+        8192; 0 always takes the mixed form)."""
+        check(self.lib.rrg_context_set_mixed_min_rows(self.h, int(rows)), "rrg_context_set_mixed_min_rows")
+
     def last_round_timing(self) -> dict:
         n = len(self.PHASES)
         ms = (C.c_double * n)()

@@ -22,8 +22,38 @@ REL_PLAIN = 1e-10
 @pytest.fixture(scope="module")
 def ctx():
     c = Context(0)
+    c.set_mixed_min_rows(0)  # the mixed kernels on every dataset size
     yield c
     c.close()
+
+
+def test_small_datasets_take_fp64_in_mixed_rounds():
+    # below the row threshold a mixed or certified round is the FP64 round,
+    # bit for bit; at threshold 0 the mixed kernels run (within tolerance)
+    rng = np.random.default_rng(4)
+    n = 3000
+    X = rng.uniform(-3, 3, (n, 3))
+    y = X[:, 0] * np.exp(0.3 * X[:, 1]) - np.cos(X[:, 2])
+    trees = [synth.random_tree(rng, int(rng.integers(3, 20)), 3) for _ in range(80)]
+    b = encode(trees, tuned=True)
+    c = Context(0)
+    try:
+        ds = c.dataset(X, y)
+        plain = ds.evaluate(b, PLAIN)
+        for prec in (MIXED, CERTIFIED):
+            got = ds.evaluate(b, prec)
+            for key in ("loss", "rmse", "size", "rank"):
+                assert np.array_equal(got[key], plain[key], equal_nan=True), key
+        launches_fp64 = c.last_round_launches()
+        c.set_mixed_min_rows(0)
+        cert = ds.evaluate(b, CERTIFIED)
+        assert c.last_round_launches() != launches_fp64
+        ok = plain["loss"] != 1000
+        np.testing.assert_allclose(fitness_value(cert["loss"], cert["rmse"], cert["size"])[ok],
+                                   fitness_value(plain["loss"], plain["rmse"], plain["size"])[ok], rtol=1e-6)
+        ds.close()
+    finally:
+        c.close()
 
 
 def rel_err(a, b):
