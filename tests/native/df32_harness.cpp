@@ -6,7 +6,8 @@
 
 extern "C" {
 
-// op: 0 add, 1 sub, 2 mul, 3 div, 4 sqrt, 5 exp, 6 log, 7 sin, 8 cos
+// op: 0 add, 1 sub, 2 mul, 3 div, 4 sqrt, 5 exp, 6 log, 7 sin, 8 cos,
+// 9 div by the reciprocal form (dfl_div_nc)
 // a, b: n doubles each, converted to double-floats; out: n doubles (hi + lo)
 void df32_apply(int op, const double* a, const double* b, int64_t n, double* out) {
   for (int64_t i = 0; i < n; ++i) {
@@ -22,6 +23,7 @@ void df32_apply(int op, const double* a, const double* b, int64_t n, double* out
       case 5: r = dfl_exp(x); break;
       case 6: r = dfl_log(x); break;
       case 7: r = dfl_sin(x); break;
+      case 9: r = dfl_div_nc(x, y); break;
       default: r = dfl_cos(x); break;
     }
     out[i] = dfl_to_double(r);

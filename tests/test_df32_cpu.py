@@ -10,7 +10,7 @@ import numpy as np
 import pytest
 
 HERE = Path(__file__).resolve().parent
-OPS = {"add": 0, "sub": 1, "mul": 2, "div": 3, "sqrt": 4, "exp": 5, "log": 6, "sin": 7, "cos": 8}
+OPS = {"add": 0, "sub": 1, "mul": 2, "div": 3, "sqrt": 4, "exp": 5, "log": 6, "sin": 7, "cos": 8, "div_nc": 9}
 
 
 @pytest.fixture(scope="module")
@@ -54,6 +54,12 @@ def test_basic_operations(df32):
     assert rel(df32("sub", a, b), al - bl) < 3e-14
     assert rel(df32("mul", a, b), al * bl) < 3e-14
     assert rel(df32("div", a, b), al / bl) < 6e-14
+    # the evaluator's division: approximate reciprocal (here one ulp off) and
+    # one Newton step; a zero divisor gives a non-finite leading part, which
+    # sends the row to the guarded division
+    assert rel(df32("div_nc", a, b), al / bl) < 6e-14
+    z = df32("div_nc", np.array([1.0, 0.0, -2.0]), np.array([0.0, 0.0, 0.0]))
+    assert not np.isfinite(z).any()
     assert rel(df32("sqrt", np.abs(a)), np.sqrt(np.abs(al))) < 3e-14
 
 
