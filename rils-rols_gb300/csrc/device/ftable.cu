@@ -453,9 +453,10 @@ __global__ void __launch_bounds__(kResidThreads) ftab_resid_kernel(ResidArgs a) 
     const float2 yl = *reinterpret_cast<const float2*>(a.ds.y32lo + gr);
 #pragma unroll
     for (int u = 0; u < 2; ++u) {
+      // the rebuilt sum in term order, Sum2-style (each term's high part by
+      // an exact two-sum, the errors and low parts gathered), then normalised
       dfl yp = dfl_make(0.f, 0.f);
       if (tuned) {
-        bool have = false;
 #pragma unroll
         for (int t = 0; t <= kMixedMaxM; ++t) {
           if (t > m) break;
@@ -466,19 +467,29 @@ __global__ void __launch_bounds__(kResidThreads) ftab_resid_kernel(ResidArgs a) 
           for (int s = 0; s < kMixedMaxM; ++s)
             if (s == t) f = u == 0 ? dfl_make(fv[s].x, fv[s].y) : dfl_make(fv[s].z, fv[s].w);
           const dfl cf = dfl_make(tm.hi[t], tm.lo[t]);
-          const dfl term = kd == 1 ? cf : (kd == 2 ? f : dfl_mul_nc(cf, f));
-          yp = have ? dfl_add_nc(yp, term) : term;
-          have = true;
+          if (kd == 3) {
+            const float p = DF_MUL(cf.hi, f.hi);
+            acc2(yp, p, DF_FMA(cf.lo, f.hi, DF_FMA(cf.hi, f.lo, DF_FMA(cf.hi, f.hi, -p))));
+          } else {
+            const dfl term = kd == 1 ? cf : f;
+            acc2(yp, term.hi, term.lo);
+          }
         }
+        yp = dfl_two_sum(yp.hi, yp.lo);
       } else {
         yp = u == 0 ? dfl_make(fv[0].x, fv[0].y) : dfl_make(fv[0].z, fv[0].w);
       }
       const dfl y = u == 0 ? dfl_make(yh.x, yl.x) : dfl_make(yh.y, yl.y);
-      const dfl e = dfl_add_nc(y, dfl_neg(yp));
-      if (gr + u < n) acc = dfl_add_nc(acc, dfl_mul_nc(e, e));
+      // e = y - yp (exact two-sum of the high parts), e^2 into the running sum
+      const dfl dh = dfl_two_sum(y.hi, -yp.hi);
+      const dfl e = dfl_fast_two_sum(dh.hi, DF_ADD(dh.lo, DF_SUB(y.lo, yp.lo)));
+      if (gr + u < n) {
+        const float p = DF_MUL(e.hi, e.hi);
+        acc2(acc, p, DF_FMA(DF_ADD(e.hi, e.hi), e.lo, DF_FMA(e.hi, e.hi, -p)));
+      }
     }
   }
-  const dfl v = warp_dfl_sum(acc);
+  const dfl v = warp_dfl_sum(dfl_renorm(acc));
   if (lane == 0) {
     red[warp][0] = v.hi;
     red[warp][1] = v.lo;
