@@ -405,8 +405,10 @@ rrg_status rrg_context::submit(rrg_dataset* ds, const rrg_batch* b, int32_t prec
   dedup_candidates(reps);
   // on small datasets the mixed form's probes, pair sums and read-backs cost
   // more than the FP64 arithmetic they replace: such rounds run in FP64
-  // (exact, so within any certified bound)
-  if (precision == RRG_PLAIN_FP64 || ds->n < mixed_min_rows) {
+  // (exact, so within any certified bound).  So do rounds on a constant y
+  // (SST = 0): R2 = 1 - SSE/SST is then decided by whether the SSE is exactly
+  // zero (0/0 gives the NaN sentinel), which only the exact path settles.
+  if (precision == RRG_PLAIN_FP64 || ds->n < mixed_min_rows || !(ds->sst > 0.0)) {
     // few candidates on tall data: the tiled QR spreads each over the GPU;
     // otherwise one block per candidate over the shared FP64 factor table
     if (ds->n >= 65536 && (int64_t)reps.size() < 2 * sm_count) st = run_plain(ds, 0, 0, false, &reps);
