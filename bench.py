@@ -353,6 +353,9 @@ def run_ours(args):
                                "fitness": "(1 + (1 - R2)) (1 + RMSE) (1 + 0.001 size)"}
     res["cpu_baseline"] = cpu_baseline(X, y, trees, args.cpu_sample)
     res["certified_over_cpu_baseline"] = value / world / res["cpu_baseline"]["value"]
+    # the reference runs single-threaded: the same oracle on one core
+    res["cpu_baseline_1core"] = cpu_baseline(X, y, trees, max(1, args.cpu_sample // 48), threads=1)
+    res["certified_over_cpu_1core"] = value / world / res["cpu_baseline_1core"]["value"]
     if args.serve_jobs > 0:
         res["serving"] = serving_leg(args, local)
     if args.cls_fit_calls > 0:
