@@ -24,6 +24,6 @@ int tune_row_class(int64_t n);
 int tune_pick(int knob, int bucket, int64_t n, bool* trial);
 void tune_store(int knob, int bucket, int64_t n, const int* vals, const float* ms, int cnt);
 // Device work below which a launch is not timed for the tuner (row-candidates).
-constexpr int64_t kTuneMinWork = int64_t(1) << 22;
+constexpr int64_t kTuneMinWork = int64_t(1) << 20;
 
 }  // namespace rrd
