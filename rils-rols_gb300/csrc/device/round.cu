@@ -355,53 +355,67 @@ void build_factor_table(const rrg_cand* cands, int32_t n_cand, const uint32_t* c
   ft.occ.clear();
   ft.ids.clear();
   ft.cand_off.assign((size_t)n_cand + 1, 0);
-  std::unordered_map<std::string, int32_t> index;
+  // factors are equal when their words are, except that a constant operand
+  // is compared by its value (two candidates may hold the same constant at
+  // different pool indices): a 64-bit hash of that sequence picks the
+  // candidates, a word-by-word comparison decides
+  auto const_bits = [&](uint32_t w) {
+    uint64_t b;
+    std::memcpy(&b, consts + (w >> 8), sizeof b);
+    return b;
+  };
+  auto same = [&](const uint32_t* a, const uint32_t* b, int len) {
+    for (int i = 0; i < len; ++i) {
+      const uint32_t wa = a[i], wb = b[i];
+      const int oa = (int)(wa & 0xffu);
+      if (oa != (int)(wb & 0xffu)) return false;
+      if (const_arg(oa) ? const_bits(wa) != const_bits(wb) : wa != wb) return false;
+    }
+    return true;
+  };
+  std::unordered_map<uint64_t, int32_t> index;  // hash -> latest factor with it
+  std::vector<int32_t> next_same;               // earlier factors with the same hash
   index.reserve((size_t)n_cand * 2 + 16);
-  std::string key;
   for (int32_t c = 0; c < n_cand; ++c) {
     ft.cand_off[c] = (int32_t)ft.ids.size();
     const rrg_cand& cd = cands[c];
     int32_t start = cd.code_offset;
     const int32_t end = cd.code_offset + cd.code_len;
     int sp = 0, depth = 0;
-    key.clear();
+    uint64_t h = 0x9e3779b97f4a7c15ull;
     for (int32_t pc = start; pc < end; ++pc) {
       const uint32_t w = code[pc];
       const int op = (int)(w & 0xffu);
       if (op == RRG_OP_EMIT) {
-        auto it = index.find(key);
-        int32_t id;
-        if (it == index.end()) {
+        const int len = pc - start;
+        auto it = index.find(h);
+        int32_t id = it == index.end() ? -1 : it->second;
+        while (id >= 0 && !(ft.meta[id].y == len + 1 && same(ft.code.data() + ft.meta[id].x, code + start, len)))
+          id = next_same[id];
+        if (id < 0) {
           id = (int32_t)ft.meta.size();
-          index.emplace(key, id);
+          next_same.push_back(it == index.end() ? -1 : it->second);
+          index[h] = id;
           int2 mt;
           mt.x = (int)ft.code.size();
-          mt.y = pc - start + 1;
+          mt.y = len + 1;
           ft.code.insert(ft.code.end(), code + start, code + pc);
           ft.code.push_back(RRG_INSN(RRG_OP_EMIT, 0));
           ft.meta.push_back(mt);
           ft.stack.push_back(depth);
           ft.occ.push_back(0);
-        } else {
-          id = it->second;
         }
         ft.occ[id] += 1;
         ft.ids.push_back(id);
         start = pc + 1;
         sp = 0;
         depth = 0;
-        key.clear();
+        h = 0x9e3779b97f4a7c15ull;
         continue;
       }
-      if (const_arg(op)) {
-        const double v = consts[w >> 8];
-        key.push_back('C');
-        key.push_back((char)op);
-        key.append(reinterpret_cast<const char*>(&v), sizeof v);
-      } else {
-        key.push_back('W');
-        key.append(reinterpret_cast<const char*>(&w), sizeof w);
-      }
+      const uint64_t v = const_arg(op) ? (const_bits(w) ^ ((uint64_t)op << 56)) : (uint64_t)w;
+      h = (h ^ v) * 0x100000001b3ull;
+      h ^= h >> 29;
       if (op == RRG_OP_PSV || op == RRG_OP_PSC) depth = std::max(depth, ++sp);
       else if (op >= RRG_OP_BIN && (((op - RRG_OP_BIN) & 7) >> 1) == RRG_SRC_S) --sp;
     }

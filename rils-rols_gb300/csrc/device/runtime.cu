@@ -345,21 +345,33 @@ void rrg_context::dedup_candidates(std::vector<int32_t>& reps) {
   const int32_t n = (int32_t)host_cands.size();
   dup_of.assign(n, 0);
   reps.clear();
-  std::unordered_map<std::string, int32_t> seen;
+  // key: the mode and the factor ids in order; a 64-bit hash picks earlier
+  // candidates, a comparison of the id lists decides
+  std::unordered_map<uint64_t, int32_t> seen;  // hash -> latest representative with it
+  std::vector<int32_t> next_same(n, -1);       // earlier representatives with the same hash
   seen.reserve((size_t)n * 2 + 16);
-  std::string key;
+  auto same = [&](int32_t a, int32_t b) {
+    const int32_t la = ft.cand_off[a + 1] - ft.cand_off[a], lb = ft.cand_off[b + 1] - ft.cand_off[b];
+    return host_cands[a].mode == host_cands[b].mode && la == lb &&
+           std::equal(ft.ids.begin() + ft.cand_off[a], ft.ids.begin() + ft.cand_off[a + 1],
+                      ft.ids.begin() + ft.cand_off[b]);
+  };
   for (int32_t c = 0; c < n; ++c) {
-    const rrg_cand& cd = host_cands[c];
-    key.assign(reinterpret_cast<const char*>(&cd.mode), sizeof cd.mode);
-    key.append(reinterpret_cast<const char*>(ft.ids.data() + ft.cand_off[c]),
-               sizeof(int32_t) * (size_t)(ft.cand_off[c + 1] - ft.cand_off[c]));
-    auto it = seen.find(key);
-    if (it == seen.end()) {
-      seen.emplace(key, c);
+    uint64_t h = 0x9e3779b97f4a7c15ull ^ (uint64_t)(uint32_t)host_cands[c].mode;
+    for (int32_t i = ft.cand_off[c]; i < ft.cand_off[c + 1]; ++i) {
+      h = (h ^ (uint64_t)(uint32_t)ft.ids[i]) * 0x100000001b3ull;
+      h ^= h >> 29;
+    }
+    auto it = seen.find(h);
+    int32_t r = it == seen.end() ? -1 : it->second;
+    while (r >= 0 && !same(r, c)) r = next_same[r];
+    if (r < 0) {
+      next_same[c] = it == seen.end() ? -1 : it->second;
+      seen[h] = c;
       dup_of[c] = c;
       reps.push_back(c);
     } else {
-      dup_of[c] = it->second;
+      dup_of[c] = r;
     }
   }
 }
