@@ -258,7 +258,7 @@ int BatchBuilder::add(const std::vector<Flat>& factors, int mode) {
 
 void BatchBuilder::add_all(const std::vector<const std::vector<Flat>*>& cands, int mode) {
   std::vector<EncodedCand> enc(cands.size());
-  parallel_slices(cands.size(), 256, [&](size_t b, size_t e) {
+  parallel_slices(cands.size(), 32, [&](size_t b, size_t e) {
     Arena arena;
     std::unordered_map<const Node*, int> depth;
     for (size_t i = b; i < e; ++i) encode_local(*cands[i], mode, arena, depth, enc[i]);

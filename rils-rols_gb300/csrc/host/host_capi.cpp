@@ -177,7 +177,7 @@ int32_t rrh_encode(const char* trees, int32_t mode, rrg_batch* out) {
       if (!line.empty()) lines.push_back(line);
     // parse and split on the host threads, encode in order
     std::vector<std::vector<rrh::Flat>> parts(lines.size());
-    rrh::parallel_slices(lines.size(), 256, [&](size_t b, size_t e) {
+    rrh::parallel_slices(lines.size(), 32, [&](size_t b, size_t e) {
       rrh::Arena a;
       for (size_t i = b; i < e; ++i) {
         rrh::Flat f = rrh::from_prefix(lines[i]);

@@ -231,7 +231,7 @@ std::vector<Flat> CandidateGen::all_candidates(const Flat& S, bool local_search)
   }
   // clean-up loop (rils_rols_cpp.cpp:413-425), each candidate on its own, on
   // the host threads
-  parallel_slices(all.size(), 128, [&](size_t b, size_t e) {
+  parallel_slices(all.size(), 32, [&](size_t b, size_t e) {
     Arena arena;
     for (size_t i = b; i < e; ++i) {
       Flat& f = all[i];
@@ -383,7 +383,7 @@ std::vector<Search::Tuned> Search::score_tuned(const std::vector<const Flat*>& t
   std::vector<Tuned> out(trees.size());
   // the factor split of tune_constants (expand, simplify, top-level factors)
   // of every candidate, on the host threads; encoded in candidate order
-  parallel_slices(trees.size(), 256, [&](size_t b, size_t e) {
+  parallel_slices(trees.size(), 32, [&](size_t b, size_t e) {
     Arena arena;
     for (size_t i = b; i < e; ++i) {
       arena.reset();
