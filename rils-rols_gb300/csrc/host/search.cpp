@@ -183,54 +183,78 @@ void CandidateGen::perturb_candidates(const FNode* t, size_t n, std::vector<Flat
   add_change_binary_to_another(t, n, out);
 }
 
+namespace {
+// a candidate's to_string key with its hash, computed on the slice threads so
+// that the order-keeping de-duplication below only compares
+struct KeyRef {
+  const std::string* s;
+  size_t h;
+  bool operator==(const KeyRef& o) const { return h == o.h && *s == *o.s; }
+};
+struct KeyRefHash {
+  size_t operator()(const KeyRef& k) const { return k.h; }
+};
+}  // namespace
+
 std::vector<Flat> CandidateGen::all_candidates(const Flat& S, bool local_search) {
-  std::vector<Flat> all;
-  all.reserve(3000);
-  std::unordered_set<std::string> seen;
-  seen.reserve(3000);
-  std::string key;
-  auto push_unique = [&](Flat&& f) {
-    key.clear();
-    to_string(f.data(), f.size(), key);
-    if (seen.insert(key).second) all.push_back(std::move(f));
-  };
-  std::vector<Flat> cands;
-  auto gen = [&](const FNode* t, size_t n) {
-    cands.clear();
-    if (local_search) change_candidates(t, n, cands);
-    else perturb_candidates(t, n, cands);
-  };
-  auto splice = [&](size_t p, size_t len, const Flat& c) {
-    Flat f;
-    f.reserve(S.size() - len + c.size());
-    f.insert(f.end(), S.begin(), S.begin() + p);
-    f.insert(f.end(), c.begin(), c.end());
-    f.insert(f.end(), S.begin() + p + len, S.end());
-    return f;
-  };
+  // The candidates of one subtree position are those of change/perturb on
+  // that subtree spliced into S; positions are visited in breadth-first
+  // order, the root's candidates taken whole (rils_rols_cpp.cpp:348-411).
+  // Positions are independent, so they are generated on the host threads and
+  // concatenated in position order, which is the sequential order.
   std::vector<size_t> pos{0};
   for (size_t i = 0; i < pos.size(); ++i) {
     const size_t p = pos[i];
-    if (p == 0) {
-      gen(S.data(), S.size());
-      for (auto& c : cands) push_unique(std::move(c));
-    }
     const int ar = arity_of(S[p].type);
     if (ar >= 1) {
-      const size_t lp = p + 1, ln = subtree_len(S.data(), lp);
-      gen(S.data() + lp, ln);
-      for (auto& c : cands) push_unique(splice(lp, ln, c));
+      const size_t lp = p + 1;
       pos.push_back(lp);
-      if (ar >= 2) {
-        const size_t rp = lp + ln, rn = subtree_len(S.data(), rp);
-        gen(S.data() + rp, rn);
-        for (auto& c : cands) push_unique(splice(rp, rn, c));
-        pos.push_back(rp);
-      }
+      if (ar >= 2) pos.push_back(lp + subtree_len(S.data(), lp));
     }
   }
+  std::vector<std::vector<Flat>> unit(pos.size());
+  std::vector<std::vector<std::string>> ukey(pos.size());
+  parallel_slices(pos.size(), 1, [&](size_t b, size_t e) {
+    std::vector<Flat> cands;
+    for (size_t i = b; i < e; ++i) {
+      const size_t p = pos[i], len = subtree_len(S.data(), p);
+      cands.clear();
+      if (local_search) change_candidates(S.data() + p, len, cands);
+      else perturb_candidates(S.data() + p, len, cands);
+      auto& out = unit[i];
+      auto& keys = ukey[i];
+      out.reserve(cands.size());
+      keys.resize(cands.size());
+      for (size_t c = 0; c < cands.size(); ++c) {
+        if (p == 0) {
+          out.push_back(std::move(cands[c]));
+        } else {
+          Flat f;
+          f.reserve(S.size() - len + cands[c].size());
+          f.insert(f.end(), S.begin(), S.begin() + p);
+          f.insert(f.end(), cands[c].begin(), cands[c].end());
+          f.insert(f.end(), S.begin() + p + len, S.end());
+          out.push_back(std::move(f));
+        }
+        to_string(out.back().data(), out.back().size(), keys[c]);
+      }
+    }
+  });
+  // first de-duplication by to_string, keeping the first occurrence
+  std::hash<std::string> hs;
+  std::unordered_set<KeyRef, KeyRefHash> seen;
+  std::vector<Flat> all;
+  size_t raw = 0;
+  for (auto& u : unit) raw += u.size();
+  all.reserve(raw);
+  seen.reserve(raw);
+  for (size_t i = 0; i < unit.size(); ++i)
+    for (size_t c = 0; c < unit[i].size(); ++c)
+      if (seen.insert(KeyRef{&ukey[i][c], hs(ukey[i][c])}).second) all.push_back(std::move(unit[i][c]));
   // clean-up loop (rils_rols_cpp.cpp:413-425), each candidate on its own, on
-  // the host threads
+  // the host threads, with the key of the cleaned candidate
+  std::vector<std::string> key2(all.size());
+  std::vector<size_t> hash2(all.size());
   parallel_slices(all.size(), 32, [&](size_t b, size_t e) {
     Arena arena;
     for (size_t i = b; i < e; ++i) {
@@ -248,16 +272,15 @@ std::vector<Flat> CandidateGen::all_candidates(const Flat& S, bool local_search)
       }
       f.clear();
       freeze_into(t, f);
+      to_string(f.data(), f.size(), key2[i]);
+      hash2[i] = hs(key2[i]);
     }
   });
   std::vector<Flat> filtered;
   filtered.reserve(all.size());
   seen.clear();
-  for (auto& f : all) {
-    key.clear();
-    to_string(f.data(), f.size(), key);
-    if (seen.insert(key).second) filtered.push_back(std::move(f));
-  }
+  for (size_t i = 0; i < all.size(); ++i)
+    if (seen.insert(KeyRef{&key2[i], hash2[i]}).second) filtered.push_back(std::move(all[i]));
   return filtered;
 }
 
