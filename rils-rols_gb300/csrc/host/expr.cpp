@@ -5,6 +5,7 @@
 #include <limits>
 #include <cmath>
 #include <cstdio>
+#include <cstring>
 #include <sstream>
 #include <stdexcept>
 
@@ -176,25 +177,37 @@ std::string to_prefix(const Flat& f) {
 }
 
 Flat from_prefix(const std::string& s) {
-  std::istringstream in(s);
-  std::string tok;
+  // whitespace-separated tokens, scanned in place (a round encodes thousands
+  // of trees, so no stream or per-token string for operators and constants)
+  auto is_space = [](char c) { return c == ' ' || c == '\t' || c == '\n' || c == '\r' || c == '\v' || c == '\f'; };
   Flat f;
   size_t need = 1;
-  while (in >> tok) {
+  const char* p = s.c_str();
+  const char* const end = p + s.size();
+  for (;;) {
+    while (p < end && is_space(*p)) ++p;
+    if (p == end) break;
+    const char* q = p;
+    while (q < end && !is_space(*q)) ++q;
+    const size_t len = (size_t)(q - p);
     if (need == 0) throw std::runtime_error("trailing tokens in tree: " + s);
-    if (tok[0] == 'x') {
-      f.push_back(FNode{VAR, std::stoi(tok.substr(1)), 0.0});
-    } else if (tok.rfind("c:", 0) == 0) {
-      f.push_back(FNode{CONST, -1, std::strtod(tok.c_str() + 2, nullptr)});
+    if (p[0] == 'x') {
+      f.push_back(FNode{VAR, std::stoi(std::string(p + 1, len - 1)), 0.0});
+    } else if (len >= 2 && p[0] == 'c' && p[1] == ':') {
+      // strtod stops at the whitespace that ends the token
+      f.push_back(FNode{CONST, -1, std::strtod(p + 2, nullptr)});
     } else {
       uint8_t op = NONE;
-      for (uint8_t t = PLUS; t < N_OPS; ++t)
-        if (tok == prefix_name(t)) op = t;
-      if (op == NONE) throw std::runtime_error("bad token in tree: " + tok);
+      for (uint8_t t = PLUS; t < N_OPS; ++t) {
+        const char* nm = prefix_name(t);
+        if (std::strlen(nm) == len && std::memcmp(nm, p, len) == 0) op = t;
+      }
+      if (op == NONE) throw std::runtime_error("bad token in tree: " + std::string(p, len));
       f.push_back(FNode{op, -1, 0.0});
     }
     need += arity_of(f.back().type);
     --need;
+    p = q;
   }
   if (need != 0) throw std::runtime_error("truncated tree: " + s);
   return f;
