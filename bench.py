@@ -4,27 +4,29 @@ Metric: candidate fitness evaluations per second (tune_constants + fitness of
 rils_rols_cpp.cpp:445-541 per candidate) at n = 1M rows, in the certified
 mixed-precision form: every fitness within 1e-6 relative of the FP64 path.
 
-Workload (one step): the local-search rounds of a search on the 1M-row,
+Workload (one step): the eight local-search rounds of a search on the 1M-row,
 5-feature regression problem (X ~ U(-3, 3), y = 2.5 x1 x2 - sin(x3)/(1+x4^2) +
-0.7 exp(0.3 x5) + 0.5% noise): every local-search candidate (all_candidates,
-rils_rols_cpp.cpp:348-443) of the eight intermediate models in
-synth.REGRESSION_1M_TRAJECTORY, 7083 tuned candidates, scored in one batched
-round.  Synthetic, seeded data; nothing is downloaded.  Also reported: the
-standalone batched-fitness configuration (8192 random trees, sizes 3..50
-over + - * / sin cos ln exp sqrt, leaves x_j or U(-5, 5), n = 100k, d = 10)
-and the serving stream (Poisson arrivals of whole fit jobs, first requests).
+0.7 exp(0.3 x5) + 0.5% noise), submitted the way the search submits them:
+one rrg_round_submit / rrg_round_wait per round, in order.  Round r holds the
+local-search candidates (all_candidates, rils_rols_cpp.cpp:348-443) of the
+r-th model of synth.REGRESSION_1M_TRAJECTORY, 264 to 1469 tuned candidates,
+7083 in all (tests/golden/ls_rounds_regression_1m.txt.gz, made by the
+reference's own generator).  Synthetic, seeded data; nothing is downloaded.
 
-  value  device-resident: dataset in HBM, each step = one rrg_eval round
-         (batch upload, kernels, result download), timed with CUDA events on
-         the library's stream, L2 flushed (256 MB write) before every step;
-  e2e    through the C ABI from host buffers: per step the trees are
-         flattened, X and y are uploaded from pinned host memory
-         (rrg_dataset_create), the round runs and the results come back.
+  value  device-resident: dataset in HBM, each step = the eight rounds (batch
+         upload, kernels and results back per round), timed with CUDA events
+         on the library's stream, L2 flushed (256 MB write) before every step;
+  e2e    through the C ABI from host buffers: per step X and y are uploaded
+         from pinned host memory (rrg_dataset_create) and every round's trees
+         are flattened, scored and their results read back.
 
-Reported beside it: the uncertified mixed form, the plain FP64 path batched
-and unbatched (one candidate per round), the fitness error of every
-candidate against the FP64 path, the roofline of the dominant kernel, the
-CPU oracle timed on the host cores, clocks.
+Reported beside it: the eight rounds concatenated into one batch, the
+uncertified mixed form, the plain FP64 path batched and unbatched, the
+fitness of a seeded sample of the candidates against the oracle (plain FP64
+bit for bit, certified within 1e-6), a capped regression fit at n = 1M
+through the drop-in module, the standalone batched-fitness configuration,
+the classifier fits and the serving stream, the roofline of the dominant
+kernel, the CPU oracle timed on the host cores, clocks.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
                   [--serve-jobs J] [--serve-only] [--quick]
@@ -32,6 +34,7 @@ CPU oracle timed on the host cores, clocks.
 from __future__ import annotations
 
 import argparse
+import gzip
 import json
 import os
 import subprocess
@@ -47,27 +50,37 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT / "rils-rols_gb300"))
 sys.path.insert(0, str(ROOT))
 
-METRIC = "candidate fitness evals/s at n=1M (certified mixed precision, batched local-search round)"
+METRIC = "candidate fitness evals/s at n=1M (certified mixed precision, local-search rounds)"
 UNIT = "evals/s"
 N_ROWS = 1_000_000
 N_FEAT = 5
 SEED = 12345
+ROUNDS_FILE = ROOT / "tests" / "golden" / "ls_rounds_regression_1m.txt.gz"
 
 
-def workload(n=N_ROWS, seed=SEED):
-    """(X, y, local-search candidates) of the 1M-row regression search"""
-    from rils_rols_gb300 import synth
-    X, y = synth.regression_1m(n=n, seed=seed)
-    return X, y, synth.ls_round_batch(d=N_FEAT)
+def load_rounds() -> list[list[str]]:
+    """The eight local-search rounds (prefix trees), in order."""
+    rounds: dict[int, list[str]] = {}
+    for line in gzip.open(ROUNDS_FILE, "rt").read().splitlines():
+        r, tree = line.split("\t")
+        rounds.setdefault(int(r), []).append(tree)
+    return [rounds[k] for k in sorted(rounds)]
 
 
-def config(n, batch):
-    return {"workload": f"local-search rounds of the 1M-row regression search: {batch} tuned candidates "
-                        f"x n={n} rows, d={N_FEAT}",
-            "n_rows": n, "n_features": N_FEAT, "batch": batch,
-            "candidates": "all_candidates(model, local_search) of 8 models on the way to the generating formula",
+def regression_data(n=N_ROWS, seed=SEED):
+    from rils_rols_gb300 import synth  # numpy only: the product library is not loaded
+    return synth.regression_1m(n=n, seed=seed)
+
+
+def config(n, rounds):
+    sizes = [len(r) for r in rounds]
+    return {"workload": f"the 8 local-search rounds of the 1M-row regression search, one call per round "
+                        f"({min(sizes)}..{max(sizes)} tuned candidates, {sum(sizes)} in all) x n={n} rows, "
+                        f"d={N_FEAT}",
+            "n_rows": n, "n_features": N_FEAT, "rounds": len(rounds), "round_sizes": sizes,
+            "candidates": "all_candidates(model, local_search) of the 8 models on the way to the generating formula",
             "precision": "RRG_MIXED_CERTIFIED: double-float factor table, FP64 Cholesky / SSE, every result within "
-                         "1e-6 of the FP64 path (rank-ambiguous and non-finite candidates re-scored by the exact QR)",
+                         "1e-6 of the FP64 path (rank-ambiguous and non-finite candidates re-scored in FP64)",
             "l2": "flushed (256 MB write on the round's stream) before every timed step"}
 
 
@@ -126,22 +139,54 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------ CPU baseline --
-def cpu_baseline(X, y, trees, sample, threads=None):
-    """The oracle (CPU restatement of the reference's path, FP64) on `sample`
-    candidates with all host threads."""
-    from oracle import pyoracle
-    from rils_rols_gb300.fitness import encode
+def sample_index(total: int, sample: int, seed: int = 5) -> np.ndarray:
+    return np.sort(np.random.default_rng(seed).choice(total, min(sample, total), replace=False))
+
+
+def cpu_baseline(X, y, trees, idx, threads=None):
+    """The oracle (oracle/rrg_oracle.c, FP64; trees flattened by the oracle's
+    own encoder, oracle/tree_encode.py) on the candidates `idx` of `trees`
+    with `threads` host threads.  Returns the baseline record and the
+    oracle's results (kept for the accuracy comparison)."""
+    from oracle import pyoracle, tree_encode
     threads = threads or os.cpu_count() or 1
     ods = pyoracle.OracleDataset(X, y)
-    sample = min(sample, len(trees))
-    idx = np.sort(np.random.default_rng(5).choice(len(trees), sample, replace=False))
-    b = encode([trees[i] for i in idx], tuned=True)
+    b = tree_encode.encode([trees[i] for i in idx], tuned=True)
     t = time.perf_counter()
-    ods.evaluate(b, threads=threads)
+    out = ods.evaluate(b, threads=threads)
     dt = time.perf_counter() - t
-    return {"value": sample / dt, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{sample} random candidates of the {len(trees)} at n={len(y)} (oracle/rrg_oracle.c, FP64, "
-                      f"{threads} threads, {dt:.1f} s)"}
+    rec = {"value": len(idx) / dt, "unit": UNIT, "cores": threads, "kind": "port",
+           "sample": f"{len(idx)} seeded random candidates of the {len(trees)} at n={len(y)} "
+                     f"(oracle/rrg_oracle.c via oracle/tree_encode.py, FP64, {threads} threads, {dt:.1f} s)"}
+    return rec, out
+
+
+def fv(r):
+    return (1 + r["loss"]) * (1 + r["rmse"]) * (1 + r["size"] * 1e-3)
+
+
+def accuracy(test, ref):
+    """Per-candidate fitness of `test` against `ref` (dicts of arrays)."""
+    ok = (ref["loss"] != 1000) & np.isfinite(fv(ref))
+    with np.errstate(all="ignore"):
+        err = np.abs(fv(test)[ok] - fv(ref)[ok]) / fv(ref)[ok]
+    err = np.where(np.isfinite(err), err, np.inf)
+    best = lambda r: int(np.argmin(np.where(ok, fv(r), np.inf)))  # noqa: E731
+    top = lambda r: set(np.argsort(np.where(ok, fv(r), np.inf))[:100].tolist())  # noqa: E731
+    same = ((test["loss"] == ref["loss"]) & (test["rmse"] == ref["rmse"]) & (test["size"] == ref["size"]))
+    return {"candidates_compared": int(len(ok)), "finite": int(ok.sum()),
+            "bit_identical": int(same.sum()),
+            "sentinel_agreement": float(np.mean((test["loss"] == 1000) == (ref["loss"] == 1000))),
+            "size_agreement": float(np.mean(test["size"] == ref["size"])),
+            "fitness_rel_err_median": float(np.median(err)) if len(err) else 0.0,
+            "fitness_rel_err_p99": float(np.quantile(err, 0.99)) if len(err) else 0.0,
+            "fitness_rel_err_max": float(err.max()) if len(err) else 0.0,
+            "frac_within_1e-6": float(np.mean(err <= 1e-6)) if len(err) else 1.0,
+            "argbest_same": best(test) == best(ref), "top100_overlap": len(top(test) & top(ref)) / 100.0}
+
+
+def subset(out: dict, idx) -> dict:
+    return {k: v[idx] for k, v in out.items() if k != "coefs"}
 
 
 # ----------------------------------------------------------- multi-rank --
@@ -183,46 +228,32 @@ def aggregate(units_per_rank: float, seconds: float, world: int) -> tuple[float,
 
 
 # ------------------------------------------------------------------- ours --
-def timed_round(ctx, ds, batch, prec, stream, flush):
-    """One round through the C ABI (rrg_round_submit + rrg_round_wait: host
-    staging, every launch, results back in host memory), bracketed by CUDA
-    events on the library's stream after an L2 flush; the results are turned
-    into Python objects after the timed region."""
+def timed_rounds(ctx, ds, batches, prec, stream, flush):
+    """One step: the rounds in order, each through the C ABI
+    (rrg_round_submit + rrg_round_wait: host staging, every launch, results
+    back in host memory), the whole step bracketed by CUDA events on the
+    library's stream after an L2 flush; results are turned into Python
+    objects after the timed region."""
     import torch
 
     from rils_rols_gb300.fitness import decode_results, result_dtype
-    res = np.zeros(len(batch), dtype=result_dtype())
-    coefs = np.zeros(max(1, batch.n_coefs), dtype=np.float64)
+    bufs = [(np.zeros(len(b), dtype=result_dtype()), np.zeros(max(1, b.n_coefs), dtype=np.float64)) for b in batches]
     with torch.cuda.stream(stream):
         flush.zero_()
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-    ds.submit(batch, prec, res, coefs)
-    ds.wait()
+    for b, (res, coefs) in zip(batches, bufs):
+        ds.submit(b, prec, res, coefs)
+        ds.wait()
     with torch.cuda.stream(stream):
         e1.record(stream)
     e1.synchronize()
-    return e0.elapsed_time(e1) / 1e3, decode_results(res, coefs, batch)
+    return e0.elapsed_time(e1) / 1e3, [decode_results(r, c, b) for b, (r, c) in zip(batches, bufs)]
 
 
-def fv(r):
-    return (1 + r["loss"]) * (1 + r["rmse"]) * (1 + r["size"] * 1e-3)
-
-
-def accuracy(test, ref):
-    ok = (ref["loss"] != 1000) & np.isfinite(fv(ref))
-    with np.errstate(all="ignore"):
-        err = np.abs(fv(test)[ok] - fv(ref)[ok]) / fv(ref)[ok]
-    err = np.where(np.isfinite(err), err, np.inf)
-    best = lambda r: int(np.argmin(np.where(ok, fv(r), np.inf)))  # noqa: E731
-    top = lambda r: set(np.argsort(np.where(ok, fv(r), np.inf))[:100].tolist())  # noqa: E731
-    return {"candidates_compared": int(ok.sum()),
-            "sentinel_agreement": float(np.mean((test["loss"] == 1000) == (ref["loss"] == 1000))),
-            "size_agreement": float(np.mean(test["size"] == ref["size"])),
-            "fitness_rel_err_median": float(np.median(err)), "fitness_rel_err_p99": float(np.quantile(err, 0.99)),
-            "fitness_rel_err_max": float(err.max()), "frac_within_1e-6": float(np.mean(err <= 1e-6)),
-            "argbest_same": best(test) == best(ref), "top100_overlap": len(top(test) & top(ref)) / 100.0}
+def concat_results(outs: list[dict]) -> dict:
+    return {k: np.concatenate([o[k] for o in outs]) for k in ("loss", "rmse", "size", "rank", "flags")}
 
 
 def run_ours(args):
@@ -232,39 +263,47 @@ def run_ours(args):
 
     rank, world = dist_setup()
     local = int(os.environ.get("LOCAL_RANK", "0"))
-    X, y, ls_trees = workload(args.n)
-    trees = ls_trees
+    X, y = regression_data(args.n)
+    rounds = load_rounds()
+    trees = [t for r in rounds for t in r]
     B = len(trees)
     ctx = Context(local)
     ds = ctx.dataset(X, y)
-    batch = encode(trees, tuned=True)
+    batches = [encode(r, tuned=True) for r in rounds]
     stream = torch.cuda.ExternalStream(ctx.stream(), device=torch.device("cuda", local))
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=torch.device("cuda", local))
 
-    def timed_rounds(prec, steps):
-        """(seconds per round list, last output, launches, phase ms sums, phase launch counts, stats)"""
+    def phases_of_step(prec, bs=batches):
+        """Per-phase device time, bytes, launches and statistics of one step,
+        round by round (a separate, untimed pass with per-launch events)."""
         ctx.set_timing(True)
-        phase_ms, phase_b, times, launches, out = {}, {}, [], 0, None
-        for _ in range(steps):
-            dt, out = timed_round(ctx, ds, batch, prec, stream, flush)
-            times.append(dt)
+        pm, pb, launches, stats = {}, {}, 0, []
+        for b in bs:
+            ds.evaluate(b, prec)
             launches += ctx.last_round_launches()
             for k, (ms, cnt) in ctx.last_round_timing().items():
-                phase_ms[k] = phase_ms.get(k, 0.0) + ms
-            for k, b in ctx.last_round_bytes().items():
-                phase_b[k] = phase_b.get(k, 0.0) + b
+                pm[k] = pm.get(k, 0.0) + ms
+            for k, v in ctx.last_round_bytes().items():
+                pb[k] = pb.get(k, 0.0) + v
+            stats.append(ctx.last_round_stats())
         ctx.set_timing(False)
-        return times, out, launches, phase_ms, phase_b, ctx.last_round_stats()
+        return pm, pb, launches, stats
 
     for _ in range(args.warmup):
-        ds.evaluate(batch, CERTIFIED)
+        for b in batches:
+            ds.evaluate(b, CERTIFIED)
     barrier(world)
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
-        times, cert, launches, phase_ms, phase_b, stats = timed_rounds(CERTIFIED, args.steps)
+        times = []
+        cert_rounds = None
+        for _ in range(args.steps):
+            dt, cert_rounds = timed_rounds(ctx, ds, batches, CERTIFIED, stream, flush)
+            times.append(dt)
     torch.cuda.synchronize()
     barrier(world)
     value, t_max = aggregate(B * args.steps, sum(times), world)
+    cert = concat_results(cert_rounds)
 
     # e2e: trees in, fitness out, through the C ABI from host buffers
     Xp = torch.from_numpy(np.ascontiguousarray(X)).pin_memory().numpy()
@@ -273,27 +312,37 @@ def run_ours(args):
     for step in range(args.warmup + args.steps):
         torch.cuda.synchronize()
         t = time.perf_counter()
-        b = encode(trees, tuned=True)
         d2 = ctx.dataset(Xp, yp)
-        d2.evaluate(b, CERTIFIED)
+        for r in rounds:
+            d2.evaluate(encode(r, tuned=True), CERTIFIED)
         d2.close()
         torch.cuda.synchronize()
         if step >= args.warmup:
             e2e_times.append(time.perf_counter() - t)
     e2e_value, _ = aggregate(B * args.steps, sum(e2e_times), world)
-    h2d = X.nbytes + y.nbytes + batch.cands.nbytes + batch.factors.nbytes + batch.code.nbytes + batch.consts.nbytes
-    d2h = B * 32 + batch.n_coefs * 8
+    h2d = X.nbytes + y.nbytes + sum(b.cands.nbytes + b.factors.nbytes + b.code.nbytes + b.consts.nbytes
+                                    for b in batches)
+    d2h = B * 32 + sum(b.n_coefs for b in batches) * 8
 
+    # phases, launches and statistics of one step (untimed pass, per-launch events)
+    phase_ms, phase_b, launches, stats = phases_of_step(CERTIFIED)
     if rank != 0:
         return
     res = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "df32/f64", "data": "synthetic (seeded)",
-           "config": config(args.n, B),
+           "config": config(args.n, rounds),
            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
-           "gpu_launches": int(launches), "round_stats": stats}
-    res["phase_ms_per_step"] = {k: v / args.steps for k, v in phase_ms.items() if v > 0}
-    res["phase_bytes_per_step"] = {k: v / args.steps for k, v in phase_b.items() if v > 0}
+           "gpu_launches": int(launches * args.steps), "gpu_launches_per_step": int(launches),
+           "round_ms": [1e3 * t for t in times],
+           "round_stats": {"fp64_rescored": sum(st["fp64_rescored"] for st in stats),
+                           "plain_routed": sum(st["plain_routed"] for st in stats),
+                           "residual_pass": sum(st["residual_pass"] for st in stats),
+                           "qr_skipped_sentinel": sum(st["qr_skipped_sentinel"] for st in stats),
+                           "rescore_reasons": {k: sum(st["rescore_reasons"].get(k, 0) for st in stats)
+                                               for k in ctx.REASONS if any(k in st["rescore_reasons"] for st in stats)}}}
+    res["phase_ms_per_step"] = {k: v for k, v in phase_ms.items() if v > 0}
+    res["phase_bytes_per_step"] = {k: v for k, v in phase_b.items() if v > 0}
     res["roofline"] = roofline(res["phase_ms_per_step"], res["phase_bytes_per_step"])
     # secondary throughput: rows x tree nodes per second (nodes of each
     # candidate tree as submitted, every row)
@@ -304,15 +353,60 @@ def run_ours(args):
     if args.quick:
         print(json.dumps(res))
         return
-    # uncertified mixed form: the same round without the FP64 re-scoring of
-    # rank-ambiguous candidates
-    mtimes, mixed, _, mphase, _, mstats = timed_rounds(MIXED, max(2, args.steps // 2))
-    res["mixed_uncertified"] = {"evals_per_s": B * len(mtimes) / sum(mtimes), "round_stats": mstats,
-                                "phase_ms_per_step": {k: v / len(mtimes) for k, v in mphase.items() if v > 0}}
+    # the eight rounds concatenated into one batch (one call)
+    allb = encode(trees, tuned=True)
+    ctimes = [timed_rounds(ctx, ds, [allb], CERTIFIED, stream, flush)[0] for _ in range(max(2, args.steps // 2))]
+    res["concatenated_round_evals_per_s"] = B * len(ctimes) / sum(ctimes)
+    # uncertified mixed form: the same rounds without the FP64 re-scoring of
+    # rank-ambiguous candidates (does not meet the 1e-6 bar: reported only)
+    mtimes = []
+    for _ in range(max(2, args.steps // 2)):
+        dt, mixed_rounds = timed_rounds(ctx, ds, batches, MIXED, stream, flush)
+        mtimes.append(dt)
+    mixed = concat_results(mixed_rounds)
+    res["mixed_uncertified"] = {"evals_per_s": B * len(mtimes) / sum(mtimes),
+                                "note": "no FP64 re-scoring: fitness errors above 1e-6 occur, see accuracy_vs_fp64"}
+    # plain FP64: unbatched launches (one candidate per round) and the rounds
+    singles = [encode([t], tuned=True) for t in trees[:args.unbatched_sample]]
+    ds.evaluate(singles[0], PLAIN)
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    for s1 in singles:
+        ds.evaluate(s1, PLAIN)
+    torch.cuda.synchronize()
+    unbatched = len(singles) / (time.perf_counter() - t)
+    ptimes = []
+    for _ in range(2):
+        dt, plain_rounds = timed_rounds(ctx, ds, batches, PLAIN, stream, flush)
+        ptimes.append(dt)
+    plain = concat_results(plain_rounds)
+    res["plain_fp64_unbatched_evals_per_s"] = unbatched
+    res["plain_fp64_rounds_evals_per_s"] = B * len(ptimes) / sum(ptimes)
+    res["certified_over_plain_unbatched"] = value / world / unbatched
+    res["accuracy_vs_fp64"] = {"certified": accuracy(cert, plain), "mixed_uncertified": accuracy(mixed, plain),
+                               "fitness": "(1 + (1 - R2)) (1 + RMSE) (1 + 0.001 size)"}
+    # the CPU oracle on a seeded sample of the same candidates: its time is
+    # the CPU baseline, its results the accuracy reference
+    idx = sample_index(B, args.cpu_sample)
+    res["cpu_baseline"], ora = cpu_baseline(X, y, trees, idx)
+    res["accuracy_vs_oracle"] = {
+        "sample": f"{len(idx)} seeded random candidates of the {B} (the CPU baseline's)",
+        "plain_fp64": accuracy(subset(plain, idx), ora),
+        "certified": accuracy(subset(cert, idx), ora),
+        "mixed_uncertified": accuracy(subset(mixed, idx), ora)}
+    res["certified_over_cpu_baseline"] = value / world / res["cpu_baseline"]["value"]
+    # the reference runs single-threaded: the same oracle on one core
+    one, _ = cpu_baseline(X, y, trees, sample_index(B, max(1, args.cpu_sample // 48), seed=6), threads=1)
+    res["cpu_baseline_1core"] = one
+    res["certified_over_cpu_1core"] = value / world / one["value"]
+    res["target_500x_cpu"] = {"all_cores": res["certified_over_cpu_baseline"] >= 500,
+                              "one_core": res["certified_over_cpu_1core"] >= 500}
+    if args.fit_calls_1m > 0:
+        res["regression_fit_1m"] = regression_fit_leg(X, y, args.fit_calls_1m)
     # standalone batched fitness: 8192 random trees (sizes 3..50 over + - * / sin
     # cos ln exp sqrt, leaves x_j or U(-5, 5)) on n = 100k rows, d = 10, X ~ N(0,1),
     # y = a random 15-node tree + 1% noise; certified and uncertified mixed
-    # against the FP64 path, per-candidate fitness error and ranking agreement
+    # against the FP64 path and, on a sample, the oracle
     from rils_rols_gb300 import synth
     X2, y2, rtrees, _ = synth.batched_fitness(n=100_000, d=10, n_trees=8192, seed=SEED)
     ds2 = ctx.dataset(X2, y2)
@@ -323,44 +417,50 @@ def run_ours(args):
     for name, prec in (("certified", CERTIFIED), ("mixed_uncertified", MIXED), ("plain_fp64", PLAIN)):
         ts, out = [], None
         for _ in range(3):
-            dt_, out = timed_round(ctx, ds2, rb, prec, stream, flush)
+            dt_, outs = timed_rounds(ctx, ds2, [rb], prec, stream, flush)
             ts.append(dt_)
+            out = outs[0]
         rt[name] = {"evals_per_s": len(rtrees) / min(ts), "out": out, "round_stats": ctx.last_round_stats(),
                     "phase_ms": {k: v[0] for k, v in ctx.last_round_timing().items() if v[0] > 0}}
     ctx.set_timing(False)
+    idx2 = sample_index(len(rtrees), args.cpu_sample // 2, seed=9)
+    _, ora2 = cpu_baseline(X2, y2, rtrees, idx2)
     res["batched_fitness_8192_random_trees"] = {
         "config": "n=100000, d=10, 8192 random trees, sizes 3..50, tuned (best of 3 rounds)",
         **{k: {kk: v[kk] for kk in ("evals_per_s", "round_stats", "phase_ms")} for k, v in rt.items()},
         "accuracy_vs_fp64": {"certified": accuracy(rt["certified"]["out"], rt["plain_fp64"]["out"]),
-                             "mixed_uncertified": accuracy(rt["mixed_uncertified"]["out"], rt["plain_fp64"]["out"])}}
+                             "mixed_uncertified": accuracy(rt["mixed_uncertified"]["out"], rt["plain_fp64"]["out"])},
+        "accuracy_vs_oracle": {"sample": f"{len(idx2)} seeded random trees of the 8192",
+                               "plain_fp64": accuracy(subset(rt["plain_fp64"]["out"], idx2), ora2),
+                               "certified": accuracy(subset(rt["certified"]["out"], idx2), ora2)}}
     ds2.close()
-    # plain FP64: unbatched launches and the whole batch (accuracy reference)
-    singles = [encode([t], tuned=True) for t in trees[:args.unbatched_sample]]
-    ds.evaluate(singles[0], PLAIN)
-    torch.cuda.synchronize()
-    t = time.perf_counter()
-    for s1 in singles:
-        ds.evaluate(s1, PLAIN)
-    torch.cuda.synchronize()
-    unbatched = len(singles) / (time.perf_counter() - t)
-    t = time.perf_counter()
-    plain = ds.evaluate(batch, PLAIN)
-    res["plain_fp64_unbatched_evals_per_s"] = unbatched
-    res["plain_fp64_batched_evals_per_s"] = B / (time.perf_counter() - t)
-    res["certified_over_plain_unbatched"] = value / world / unbatched
-    res["mixed_over_plain_unbatched"] = res["mixed_uncertified"]["evals_per_s"] / unbatched
-    res["accuracy_vs_fp64"] = {"certified": accuracy(cert, plain), "mixed_uncertified": accuracy(mixed, plain),
-                               "fitness": "(1 + (1 - R2)) (1 + RMSE) (1 + 0.001 size)"}
-    res["cpu_baseline"] = cpu_baseline(X, y, trees, args.cpu_sample)
-    res["certified_over_cpu_baseline"] = value / world / res["cpu_baseline"]["value"]
-    # the reference runs single-threaded: the same oracle on one core
-    res["cpu_baseline_1core"] = cpu_baseline(X, y, trees, max(1, args.cpu_sample // 48), threads=1)
-    res["certified_over_cpu_1core"] = value / world / res["cpu_baseline_1core"]["value"]
     if args.serve_jobs > 0:
         res["serving"] = serving_leg(args, local)
     if args.cls_fit_calls > 0:
         res["classifier"] = classifier_leg(args)
     print(json.dumps(res))
+
+
+def regression_fit_leg(X, y, calls):
+    """A regression fit on the 1M-row data through the drop-in module
+    (rils_rols_cpp.rils_rols, certified mixed precision), max_fit_calls =
+    `calls`: the search submits its own rounds, so evals/s here is what a fit
+    sees (host search included in the wall time)."""
+    import rils_rols_cpp
+    n, d = X.shape
+    m = rils_rols_cpp.rils_rols(False, calls, 1 << 30, 0.001, 50, 1.0, False, SEED % 100000)
+    m.set_precision("mixed")
+    t = time.perf_counter()
+    m.fit(X.reshape(-1), y, n, d)
+    wall = time.perf_counter() - t
+    cnt = m.counters()
+    pred = m.predict(X.reshape(-1), n, d)
+    r2 = 1 - float(np.sum((y - pred) ** 2) / np.sum((y - y.mean()) ** 2))
+    return {"max_fit_calls": calls, "n_rows": n, "fit_s": wall, "fit_calls": m.get_fit_calls(),
+            "rounds": cnt["device_rounds"], "candidates_scored": cnt["candidates_scored"],
+            "backend_s": cnt["backend_ns"] / 1e9,
+            "evals_per_s_backend": cnt["candidates_scored"] / max(1e-9, cnt["backend_ns"] / 1e9),
+            "evals_per_s_wall": cnt["candidates_scored"] / wall, "model": m.get_model_string(), "train_r2": r2}
 
 
 # ------------------------------------------------------------- serving ----
@@ -511,37 +611,81 @@ def read_profile(phase):
 
 
 # -------------------------------------------------------------- reference --
+REF_LIB = ROOT / "oracle" / "_ref" / "librr_ref.so"
+
+
+def reference_scorer(X, y, threads):
+    """A function scoring a list of prefix trees on the CPU with `threads`
+    host threads and a description of what it runs: the reference's own
+    tune_constants + fitness (oracle/_ref/librr_ref.so, compiled from the
+    reference's sources, where this host built it), else the oracle port
+    (oracle/rrg_oracle.c with the oracle's own encoder).  Neither loads the
+    product library."""
+    import ctypes as C
+    from concurrent.futures import ThreadPoolExecutor
+    n, d = X.shape
+    lib = None
+    if REF_LIB.exists():
+        try:
+            lib = C.CDLL(str(REF_LIB))
+        except OSError:
+            lib = None
+    if lib is not None:
+        Xc = np.ascontiguousarray(X.T)
+        yc = np.ascontiguousarray(y)
+        dp = C.POINTER(C.c_double)
+
+        def one(tree):
+            out3 = (C.c_double * 3)()
+            buf = C.create_string_buffer(1 << 16)
+            # ctypes releases the GIL for the call: the threads run in parallel
+            lib.ref_tune_fitness(Xc.ctypes.data_as(dp), yc.ctypes.data_as(dp), n, d, tree.encode(), 1, 0, out3,
+                                 buf, len(buf))
+            return out3[0]
+
+        pool = ThreadPoolExecutor(threads)
+
+        def score(trees):
+            list(pool.map(one, trees))
+        return score, "reference", "the reference's own tune_constants + fitness (oracle/_ref/librr_ref.so)"
+    from oracle import pyoracle, tree_encode
+    ods = pyoracle.OracleDataset(X, y)
+
+    def score(trees):
+        ods.evaluate(tree_encode.encode(trees, tuned=True), threads=threads)
+    return score, "port", "the oracle (oracle/rrg_oracle.c, trees flattened by oracle/tree_encode.py)"
+
+
 def run_reference(args):
-    """The reference's CPU path for this workload: the oracle restatement
-    (oracle/rrg_oracle.c; the reference harness only builds where the
-    reference checkout exists), all host threads, a bounded sample per step."""
+    """The reference's CPU path on this workload, all host threads, a bounded
+    seeded sample of the rounds' candidates per step (no product code is
+    loaded in this process)."""
     rank, world = dist_setup()
     if rank != 0:
         return
-    from oracle import pyoracle
-    from rils_rols_gb300.fitness import encode
-    X, y, trees = workload(args.n)
+    X, y = regression_data(args.n)
+    rounds = load_rounds()
+    trees = [t for r in rounds for t in r]
     threads = os.cpu_count() or 1
-    ods = pyoracle.OracleDataset(X, y)
-    sample = args.ref_sample
+    score, kind, what = reference_scorer(X, y, threads)
+    sample = min(args.ref_sample, len(trees))
     rng = np.random.default_rng(7)
     times = []
     for step in range(args.warmup + args.steps):
-        idx = rng.choice(len(trees), sample, replace=False)
-        b = encode([trees[i] for i in idx], tuned=True)
+        pick = [trees[i] for i in rng.choice(len(trees), sample, replace=False)]
         t = time.perf_counter()
-        ods.evaluate(b, threads=threads)
+        score(pick)
         dt = time.perf_counter() - t
         if step >= args.warmup:
             times.append(dt)
     value = sample * len(times) / sum(times)
-    desc = f"{sample} random candidates of the batch per step at n={args.n}, FP64, {threads} threads"
+    desc = (f"{sample} seeded random candidates of the {len(trees)} per step at n={args.n}, FP64, {threads} threads; "
+            f"{what}")
     print(json.dumps({"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
                       "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
                       "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-                      "data": "synthetic (seeded)", "config": config(args.n, len(trees)),
-                      "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                                       "sample": desc},
+                      "data": "synthetic (seeded)", "config": config(args.n, rounds),
+                      "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind, "sample": desc},
                       "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
 
 
@@ -552,8 +696,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=N_ROWS)
-    ap.add_argument("--cpu-sample", type=int, default=4800)
-    ap.add_argument("--ref-sample", type=int, default=1024)
+    ap.add_argument("--cpu-sample", type=int, default=2400, help="oracle sample of the CPU baseline")
+    ap.add_argument("--ref-sample", type=int, default=384, help="candidates per step of the reference arm")
+    ap.add_argument("--fit-calls-1m", type=int, default=100000,
+                    help="max_fit_calls of the regression fit at n = 1M (0: no fit leg)")
     ap.add_argument("--unbatched-sample", type=int, default=64)
     ap.add_argument("--quick", action="store_true", help="skip the FP64 comparison and the CPU baseline")
     ap.add_argument("--serve-jobs", type=int, default=8, help="requests of the serving stream (0: no serving leg)")

@@ -187,8 +187,8 @@ rrg_status rrg_predict(rrg_dataset* ds, const rrg_batch* batch, double* values);
  * FP64 path, for callers that may not allocate device memory or have a
  * library allocate it for them (a framework that owns every device byte
  * through its own pool; a loop that cannot take cudaMalloc / cudaFree
- * stalls).  No counterpart in the reference: it is the per-candidate
- * tune_constants + fitness pair (rils_rols_cpp.cpp:445-541) without a
+ * stalls).  It has no counterpart in the reference.  It scores one tuned or
+ * untuned candidate on data the caller already holds on the device, with no
  * context or dataset object.
  *   X_col: device, d columns of ld >= n FP64 values (column j at X_col + j*ld);
  *   y: device, n values; result: device, one rrg_result; coefs: device,

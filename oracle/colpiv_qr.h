@@ -36,6 +36,12 @@
 
 #include "../rils-rols_gb300/csrc/common/rr_sum.h"
 
+/* rank-1 update step c - (tau v_i) t: one fused multiply-add (a stock,
+ * unvectorised build redefines it as a multiply and an add) */
+#ifndef RRQ_UPDATE
+#define RRQ_UPDATE(a, b, c) fma((a), (b), (c))
+#endif
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -119,7 +125,7 @@ static inline long rrq_lstsq(double* A, long lda, long rows, long cols,
                     double tmp = rr_dot256(col, cj, k + 1, rows);
                     tmp += cj[k];
                     cj[k] -= tau * tmp;
-                    for (i = k + 1; i < rows; ++i) cj[i] = fma(-(tau * col[i]), tmp, cj[i]);
+                    for (i = k + 1; i < rows; ++i) cj[i] = RRQ_UPDATE(-(tau * col[i]), tmp, cj[i]);
                 }
             }
         }
@@ -157,7 +163,7 @@ static inline long rrq_lstsq(double* A, long lda, long rows, long cols,
             double tmp = rr_dot256(v, c, k + 1, rows);
             tmp += c[k];
             c[k] -= tau * tmp;
-            for (i = k + 1; i < rows; ++i) c[i] = fma(-(tau * v[i]), tmp, c[i]);
+            for (i = k + 1; i < rows; ++i) c[i] = RRQ_UPDATE(-(tau * v[i]), tmp, c[i]);
         }
     }
     /* back substitution with R[0:r, 0:r], column sweep */

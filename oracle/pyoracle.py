@@ -29,6 +29,21 @@ def build(force: bool = False) -> Path:
     return LIB
 
 
+# rrg_result of include/rils_rols_gb300.h
+RESULT_DT = np.dtype([("loss", np.float64), ("rmse", np.float64), ("size", np.int32), ("rank", np.int32),
+                      ("flags", np.uint32), ("n_coef", np.int32)])
+TUNED = 1
+
+
+def decode(res: np.ndarray, coefs: np.ndarray, batch) -> dict:
+    out = {k: res[k].copy() for k in ("loss", "rmse", "size", "rank", "flags")}
+    c = batch.cands
+    lo = c["coef_offset"].astype(np.int64)
+    hi = np.where(c["mode"] == TUNED, lo + c["n_factors"] + 1, lo)
+    out["coefs"] = [coefs[a:b] for a, b in zip(lo.tolist(), hi.tolist())]
+    return out
+
+
 _lib = None
 
 
@@ -63,15 +78,17 @@ class OracleDataset:
             raise MemoryError("oracle dataset")
 
     def evaluate(self, batch, threads: int = 1) -> dict:
-        """Same output as rils_rols_gb300.fitness.Dataset.evaluate."""
-        from rils_rols_gb300.fitness import decode_results, result_dtype
-        res = np.zeros(len(batch), dtype=result_dtype())
+        """Per-candidate loss, rmse, size, rank, flags and coefficients (the
+        fields of rils_rols_gb300.fitness.Dataset.evaluate).  `batch` is any
+        object with the rrg_batch arrays (cands, n_coefs) and a struct()
+        method: oracle.tree_encode.encode makes one without the product."""
+        res = np.zeros(len(batch), dtype=RESULT_DT)
         coefs = np.zeros(max(1, batch.n_coefs), dtype=np.float64)
         b = batch.struct()
         st = load().oracle_eval_threads(self.h, C.addressof(b), res.ctypes.data, coefs.ctypes.data, threads)
         if st != 0:
             raise RuntimeError(f"oracle_eval failed with status {st}")
-        return decode_results(res, coefs, batch)
+        return decode(res, coefs, batch)
 
     def predict(self, batch) -> np.ndarray:
         out = np.zeros(self.n)

@@ -319,11 +319,16 @@ rrg_status rrg_context::run_plain(const rrg_dataset* ds, int32_t lo, int32_t hi,
     uint8_t* redo = static_cast<uint8_t*>(d_redo.ptr);
     int kmax = 1;
     for (int32_t i = sb.p; i < sb.e; ++i) kmax = std::max(kmax, pcs[(*list)[i]].k);
-    launch_plain_qr(kmax + 1, ns, stream, dev, dd, pc, dl, sb.p, A, A, S, sb.tsqr ? 1 : 0, sb.nb, coefs, res, status,
-                    (sb.tsqr && redo_sensitive) ? redo : nullptr, nullptr);
-    if (sb.tsqr && redo_sensitive)
-      launch_plain_qr(kmax + 1, ns, stream, dev, dd, pc, dl, sb.p, A, A, S, 0, sb.nb, coefs, res, status, redo,
-                      nullptr);
+    // launch_plain_qr reads (and so clears) the launch error itself: check
+    // its return value
+    if (!launch_plain_qr(kmax + 1, ns, stream, dev, dd, pc, dl, sb.p, A, A, S, sb.tsqr ? 1 : 0, sb.nb, coefs, res,
+                         status, (sb.tsqr && redo_sensitive) ? redo : nullptr, nullptr) ||
+        (sb.tsqr && redo_sensitive &&
+         !launch_plain_qr(kmax + 1, ns, stream, dev, dd, pc, dl, sb.p, A, A, S, 0, sb.nb, coefs, res, status, redo,
+                          nullptr))) {
+      rrc::set_error("plain round: QR launch failed");
+      return RRG_E_CUDA;
+    }
     mark_end(P_PLAIN_QR, t0);
     t0 = mark_begin();
     plain_resid_kernel<<<dim3(nb_res, ns), 256, 0, stream>>>(dev, dd, pc, dl, sb.p, A, coefs, partial,

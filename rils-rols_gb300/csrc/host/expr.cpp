@@ -338,7 +338,7 @@ double fold_raw(uint8_t type, double a, double b) {
     case NOT_EQUAL: return a != b ? 1 : 0;
     case MIN: return a < b ? a : b;
     case MAX: return a > b ? a : b;
-    default: throw std::runtime_error("Simplification is not supported for this binary operator!");
+    default: throw std::runtime_error("constant folding: unknown binary opcode");
   }
 }
 // A NaN made by an invalid operation on non-NaN operands gets the sign of the

@@ -1,6 +1,6 @@
 """Generates the golden fixtures of tests/golden/ from the reference itself.
 
-Runs only where the reference checkout exists (default /root/reference): it
+Runs only where the reference checkout exists (see oracle/build_ref.sh): it
 builds oracle/_ref/librr_ref.so with oracle/build_ref.sh (the reference's own
 rils_rols_cpp.cpp and node.cpp, unmodified, against the self-written Eigen
 subset in oracle/eigen_shim/) and records, for seeded inputs:
@@ -26,8 +26,9 @@ REPO = HERE.parent.parent
 sys.path.insert(0, str(REPO / "rils-rols_gb300"))
 from rils_rols_gb300 import synth  # noqa: E402
 
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
-subprocess.run([str(REPO / "oracle" / "build_ref.sh"), REF], check=True)
+# the reference checkout: first argument, else what oracle/build_ref.sh finds
+# (environment variable RILS_ROLS_REFERENCE or the recipe's default)
+subprocess.run([str(REPO / "oracle" / "build_ref.sh")] + sys.argv[1:2], check=True)
 lib = C.CDLL(str(REPO / "oracle" / "_ref" / "librr_ref.so"))
 dp = C.POINTER(C.c_double)
 BUF = C.create_string_buffer(1 << 26)
