@@ -162,7 +162,11 @@ rrg_status rrg_dataset_destroy(rrg_dataset* ds);
  * batch is copied into pinned staging before the call returns, so the caller
  * may reuse its buffers at once; `results` (n_cand entries) and `coefs` (the
  * sum of n_coef over tuned candidates, may be NULL) are written when
- * rrg_round_wait returns RRG_OK.  One round in flight per context.
+ * rrg_round_wait returns RRG_OK.  One round in flight per context.  The
+ * call returns once every launch of the round is queued: it waits on the
+ * device only for a launch-shape trial (the first launch of a shape class,
+ * see rrg_tune_set_mode) and for mixed rounds that need table sub-rounds or
+ * run with rrg_context_set_async off.
  * Replaces, per candidate j: tune_constants (rils_rols_cpp.cpp:615) followed
  * by fitness (:616), or fitness alone (:828, :842) for RRG_UNTUNED.
  */
@@ -228,7 +232,14 @@ int64_t rrg_last_round_launches(const rrg_context* ctx);
  *   ill-conditioning, coefficient near 1, coefficient near 0, one-pass SSE
  *   inaccurate, certified error bound too large, other NaN.  [15] FP64-path
  *   candidates whose pivoted QR was not run: a non-finite column norm makes its
- *   outcome certainly all-NaN coefficients (the fitness sentinel).
+ *   outcome certainly all-NaN coefficients (the fitness sentinel).  [16]
+ *   candidates scored after merging those with identical factor lists.
+ *   [17] 1 when the round solved by the tiled QR (a plain round of fewer
+ *   than twice as many distinct candidates as the device has SMs, on 65536
+ *   rows or more): results within 1e-10 relative of the direct QR, same
+ *   rank, size and sentinel; 0 when by the direct QR (bit-identical to the
+ *   oracle).  [18] 1 when the last round ran as a CUDA graph
+ *   (rrg_context_set_graph).
  * Returns the count written. */
 int32_t rrg_last_round_stats(const rrg_context* ctx, int64_t* out, int32_t n);
 
@@ -238,6 +249,29 @@ int32_t rrg_last_round_stats(const rrg_context* ctx, int64_t* out, int32_t n);
  * several contexts on one device (the serving loop) set them explicitly.
  * No counterpart in the reference (single-threaded, one fit per process). */
 rrg_status rrg_context_set_limits(rrg_context* ctx, int64_t scratch_bytes, int64_t table_bytes);
+
+/* How a mixed or certified round decides its second half.  On (the
+ * default): on the device, from the solve's flags (the residual-pass list,
+ * which candidates the FP64 path re-scores, which table columns it
+ * evaluates), so that rrg_round_submit returns with the whole round queued
+ * and the host reads nothing back before the results.  Off: the host reads
+ * the flags back twice in mid-round and builds the FP64 path's programs for
+ * the re-scored candidates only.  Results are the same bits either way; a
+ * round whose double-float table needs sub-rounds always takes the second
+ * form.  RRG_E_INVALID while a round is in flight.  No counterpart in the
+ * reference. */
+rrg_status rrg_context_set_async(rrg_context* ctx, int32_t on);
+
+/* Run every round as a CUDA graph (off by default): the round's launches,
+ * copies and stream forks are captured from the context stream and launched
+ * as one graph, the previous round's graph updated in place when the shapes
+ * allow (rrg_last_round_stats [18] tells whether the last round ran so).  A
+ * round that waits on the device in mid-round (a launch-shape trial, table
+ * sub-rounds, rrg_context_set_async off) cannot be captured and is launched
+ * directly; so are rounds with per-phase timing on.  Results are the same
+ * bits either way.  RRG_E_INVALID while a round is in flight.  No
+ * counterpart in the reference. */
+rrg_status rrg_context_set_graph(rrg_context* ctx, int32_t on);
 
 /* Rounds in RRG_MIXED / RRG_MIXED_CERTIFIED on datasets with fewer than
  * `rows` rows (default 8192) are computed in FP64 instead: there the mixed

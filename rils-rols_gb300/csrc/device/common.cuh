@@ -63,4 +63,9 @@ constexpr double kEps12 = 1e-12;  // value_zero / value_one threshold (node.h:13
 
 __host__ __device__ inline int64_t round_up(int64_t a, int64_t b) { return (a + b - 1) / b * b; }
 
+// After a kernel launch: true when it was accepted; otherwise the launch
+// error is recorded as the thread's error text (rrg_last_error) and cleared,
+// so the caller's own checks see it through the return value.
+bool launch_ok(const char* what);
+
 }  // namespace rrd

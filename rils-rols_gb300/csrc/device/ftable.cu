@@ -20,6 +20,7 @@
 //   ftab_resid    the rebuilt sum  sum_i c_i f_i  (drop / snap rules of
 //                 rils_rols_cpp.cpp:488-517) from the table, its residual
 //                 against y and the squared residuals, all double-float.
+#include <algorithm>
 #include <cfloat>
 #include <cstdint>
 
@@ -424,11 +425,19 @@ __global__ void pair_reduce_kernel(const float2* P, int32_t n_pairs, int32_t n_c
 
 // The candidates of the residual pass have finite table values (the solve sends
 // every non-finite one to the FP64 path), so the unguarded operations apply.
+__device__ __forceinline__ void ftab_resid_item(const ResidArgs& a, int i, int qs);
+
+// Items (candidate i of list2, row block qs), i = item % n2, qs = item / n2,
+// walked by the grid in any shape: each item's partial sum is the same.
 __global__ void __launch_bounds__(kResidThreads) ftab_resid_kernel(ResidArgs a) {
+  const int n2 = a.n2_dev ? min(*a.n2_dev, a.n2) : a.n2;
+  const int64_t items = (int64_t)n2 * a.n_chunks;
+  for (int64_t w = blockIdx.x; w < items; w += gridDim.x) ftab_resid_item(a, (int)(w % n2), (int)(w / n2));
+}
+
+__device__ __forceinline__ void ftab_resid_item(const ResidArgs& a, int i, int qs) {
   __shared__ float red[kResidThreads / 32][2];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int i = blockIdx.x % a.n2;
-  const int qs = blockIdx.x / a.n2;
   const int li = a.list2[i];
   const int c = a.mlist[li];
   const rrg_cand cd = a.b.cands[c];
@@ -500,6 +509,7 @@ __global__ void __launch_bounds__(kResidThreads) ftab_resid_kernel(ResidArgs a) 
     for (int w = 0; w < kResidThreads / 32; ++w) s = dfl_add(s, dfl_make(red[w][0], red[w][1]));
     a.sse[(size_t)c * a.n_chunks + qs] = (double)s.hi + (double)s.lo;
   }
+  __syncthreads();  // red is reused by the block's next item
 }
 
 // ----------------------------------------------------------- launchers ----
@@ -515,24 +525,26 @@ bool launch_fac_eval(const FacEvalArgs& a, int n_groups, int n_chunks, bool ligh
   const size_t sm = fac_eval_smem();
   if (light) fac_eval_kernel<4><<<dim3(n_groups, n_chunks), kFacThreads, sm, st>>>(a);
   else fac_eval_kernel<2><<<dim3(n_groups, n_chunks), kFacThreads, sm, st>>>(a);
-  return cudaGetLastError() == cudaSuccess;
+  return launch_ok("launch_fac_eval");
 }
 int pair_row_blocks(int64_t n_pad) { return (int)((n_pad + kPairRows - 1) / kPairRows); }
 bool launch_pair_sum(const PairArgs& a, int n_super, cudaStream_t st) {
   if (a.n_units <= 0 || n_super <= 0) return true;
   pair_sum_kernel<<<a.n_units * n_super, kPairThreads, 0, st>>>(a);
-  return cudaGetLastError() == cudaSuccess;
+  return launch_ok("launch_pair_sum");
 }
 bool launch_pair_reduce(const float2* P, int32_t n_pairs, int32_t n_chunks, int32_t p0, int32_t p1, double* psum,
                         cudaStream_t st) {
   if (p1 <= p0) return true;
   pair_reduce_kernel<<<(p1 - p0 + 255) / 256, 256, 0, st>>>(P, n_pairs, n_chunks, p0, p1, psum);
-  return cudaGetLastError() == cudaSuccess;
+  return launch_ok("launch_pair_reduce");
 }
-bool launch_ftab_resid(const ResidArgs& a, cudaStream_t st) {
+bool launch_ftab_resid(const ResidArgs& a, cudaStream_t st, int max_blocks) {
   if (a.n2 <= 0 || a.n_chunks <= 0) return true;
-  ftab_resid_kernel<<<a.n2 * a.n_chunks, kResidThreads, 0, st>>>(a);
-  return cudaGetLastError() == cudaSuccess;
+  const int64_t items = (int64_t)a.n2 * a.n_chunks;
+  const int grid = (int)(max_blocks > 0 ? std::min<int64_t>(items, max_blocks) : items);
+  ftab_resid_kernel<<<grid, kResidThreads, 0, st>>>(a);
+  return launch_ok("launch_ftab_resid");
 }
 
 }  // namespace rrd

@@ -68,7 +68,8 @@ struct ResidArgs {
   const float2* F;
   const int32_t* mlist;      // mixed list: list index -> candidate
   const int32_t* list2;      // [i] list index of a candidate that needs the residual pass
-  int32_t n2;
+  int32_t n2;                // entries of list2 the grid covers
+  const int32_t* n2_dev;     // may be NULL: the device-decided length of list2 (<= n2)
   const int32_t* cand_col;   // [list index][kMixedMaxM] table column of each factor
   const MixedTerm* terms;    // [candidate]
   int32_t n_chunks;          // row blocks of pair_row_blocks(n_pad)
@@ -88,6 +89,8 @@ bool launch_pair_sum(const PairArgs& a, int n_row_blocks, cudaStream_t st);
 // psum[p] for p in [p0, p1): FP64 sum over the first n_chunks rows of P.
 bool launch_pair_reduce(const float2* P, int32_t n_pairs, int32_t n_chunks, int32_t p0, int32_t p1, double* psum,
                         cudaStream_t st);
-bool launch_ftab_resid(const ResidArgs& a, cudaStream_t st);
+// max_blocks > 0: at most that many blocks walk the items (the grid shape
+// changes no result); otherwise one block per item.
+bool launch_ftab_resid(const ResidArgs& a, cudaStream_t st, int max_blocks = 0);
 
 }  // namespace rrd

@@ -557,9 +557,9 @@ __global__ void cand_probe_kernel(const rrg_cand* cands, const int32_t* list, in
 // the order of finalize_kernel); above the tolerance it is queued for FP64.
 __global__ void cert_resid_kernel(const int32_t* mlist, const int32_t* list2, int32_t n2, const double* sse_part,
                                   int nb, const double* cert_e, DevData ds, double cert_tol, int32_t* fallback,
-                                  int32_t fallback_cap, uint32_t* reasons) {
+                                  int32_t fallback_cap, uint32_t* reasons, const int32_t* n2_dev) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n2) return;
+  if (i >= n2 || (n2_dev && i >= *n2_dev)) return;
   const int c = mlist[list2[i]];
   const double E = cert_e[c];
   if (!(E >= 0.0)) return;
@@ -589,7 +589,7 @@ bool launch_fac_probe(const uint32_t* code, const int2* meta, int32_t nf, const 
                       const float* K32lo, const DevData& ds, FacProbe* out, cudaStream_t st) {
   if (nf <= 0) return true;
   fac_probe_kernel<<<(nf + 3) / 4, 128, 0, st>>>(code, meta, nf, K64, K32, K32lo, ds, out);
-  return cudaGetLastError() == cudaSuccess;
+  return launch_ok("launch_fac_probe");
 }
 bool launch_cand_probe(const rrg_cand* cands, const int32_t* list, int32_t n_list, const int32_t* cand_fac,
                        const int32_t* fcol, const FacProbe* fp, const unsigned long long* fnan, ProbeOut* out,
@@ -597,28 +597,28 @@ bool launch_cand_probe(const rrg_cand* cands, const int32_t* list, int32_t n_lis
   if (n_list <= 0) return true;
   cand_probe_kernel<<<(n_list + 127) / 128, 128, 0, st>>>(cands, list, n_list, cand_fac, fcol, fp, fnan, out,
                                                           nanrow);
-  return cudaGetLastError() == cudaSuccess;
+  return launch_ok("launch_cand_probe");
 }
 bool launch_cert_resid(const int32_t* mlist, const int32_t* list2, int32_t n2, const double* sse_part, int nb,
                        const double* cert_e, const DevData& ds, double cert_tol, int32_t* fallback,
-                       int32_t fallback_cap, uint32_t* reasons, cudaStream_t st) {
+                       int32_t fallback_cap, uint32_t* reasons, cudaStream_t st, const int32_t* n2_dev) {
   if (n2 <= 0) return true;
   cert_resid_kernel<<<(n2 + 127) / 128, 128, 0, st>>>(mlist, list2, n2, sse_part, nb, cert_e, ds, cert_tol, fallback,
-                                                      fallback_cap, reasons);
-  return cudaGetLastError() == cudaSuccess;
+                                                      fallback_cap, reasons, n2_dev);
+  return launch_ok("launch_cert_resid");
 }
 bool launch_solve(const SolveArgs& a, cudaStream_t st) {
   if (a.n_list <= 0) return true;
   mixed_solve_kernel<<<(a.n_list + 3) / 4, 128, 0, st>>>(a);
-  return cudaGetLastError() == cudaSuccess;
+  return launch_ok("launch_solve");
 }
 bool launch_to_f32(const double* src, float* dst, int64_t n, cudaStream_t st) {
   to_f32_kernel<<<1024, 256, 0, st>>>(src, dst, n);
-  return cudaGetLastError() == cudaSuccess;
+  return launch_ok("launch_to_f32");
 }
 bool launch_split_f32(const double* src, float* hi, float* lo, int64_t n, cudaStream_t st) {
   split_f32_kernel<<<1024, 256, 0, st>>>(src, hi, lo, n);
-  return cudaGetLastError() == cudaSuccess;
+  return launch_ok("launch_split_f32");
 }
 
 }  // namespace rrd

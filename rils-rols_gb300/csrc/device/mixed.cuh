@@ -89,9 +89,10 @@ bool launch_cand_probe(const rrg_cand* cands, const int32_t* list, int32_t n_lis
                        int64_t* nanrow, cudaStream_t st);
 bool launch_solve(const SolveArgs& a, cudaStream_t st);
 // Certified rounds: residual-pass SSE of the listed candidates against their bound.
+// n2_dev (may be NULL): the device-decided length of list2 (<= n2).
 bool launch_cert_resid(const int32_t* mlist, const int32_t* list2, int32_t n2, const double* sse_part, int nb,
                        const double* cert_e, const DevData& ds, double cert_tol, int32_t* fallback,
-                       int32_t fallback_cap, uint32_t* reasons, cudaStream_t st);
+                       int32_t fallback_cap, uint32_t* reasons, cudaStream_t st, const int32_t* n2_dev = nullptr);
 bool launch_to_f32(const double* src, float* dst, int64_t n, cudaStream_t st);
 bool launch_split_f32(const double* src, float* hi, float* lo, int64_t n, cudaStream_t st);
 

@@ -148,6 +148,9 @@ extern "C" rrg_status rrg_eval_plain_noalloc(const double* X_col, int64_t ld, co
     rrc::set_error("rrg_eval_plain_noalloc: a tuned candidate needs a device coefficient output");
     return RRG_E_INVALID;
   }
+  // an error another library left pending on this thread is not this
+  // call's: clear it so the launch checks below see only their own
+  cudaGetLastError();
   int device = 0;
   cudaError_t e = cudaGetDevice(&device);
   if (e != cudaSuccess) {

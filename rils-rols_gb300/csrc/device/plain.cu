@@ -177,9 +177,69 @@ __device__ void apply_householder(double* Q, int64_t ld, int64_t rows, int kk, d
   __syncthreads();
 }
 
+// One-column table program on rows [r0, r1) of this block, written to Ac;
+// the column's statistics (NaN, infinite or overflowing square, non-trivial
+// tail, largest finite magnitude) merged into *cs.
+__device__ __forceinline__ void eval_column_stats(const uint32_t* code, int len, const double* consts,
+                                                  const DevData& ds, int64_t r0, int64_t r1, double* st, double* Ac,
+                                                  const double* T, uint32_t* status, ColStat* cs) {
+  uint32_t f = 0;
+  unsigned long long mx = 0;
+  for (int64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
+    run_row64(code, len, consts, ds, r, st, Ac, T, status);
+    const double v = Ac[r];
+    const double a = fabs(v);
+    if (v != v) {
+      f |= kCsNaN;
+    } else if (!(a <= 1.35e154)) {  // infinite, or its square overflows
+      f |= kCsBig;
+    } else {
+      const unsigned long long bits = (unsigned long long)__double_as_longlong(a);
+      mx = bits > mx ? bits : mx;
+    }
+    if (r >= 1 && !(a <= 1e-150)) f |= kCsTail;
+  }
+  f = __reduce_or_sync(0xffffffffu, f);
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long t = __shfl_xor_sync(0xffffffffu, mx, o);
+    mx = t > mx ? t : mx;
+  }
+  if ((threadIdx.x & 31) == 0) {
+    if (f) atomicOr(&cs->flags, f);
+    if (mx) atomicMax(&cs->maxabs, mx);
+  }
+}
+
 }  // namespace
 
 // ------------------------------------------------------------- kernels ----
+__global__ void __launch_bounds__(256) table_eval_list_kernel(DevBatch b, DevData ds, const PlainCand* pc,
+                                                               const int32_t* cols, const int32_t* count,
+                                                               int max_nbc, double* A, uint32_t* status,
+                                                               ColStat* cst) {
+  extern __shared__ double smem[];
+  const int cnt = *count;
+  if (cnt <= 0) return;
+  const int nbc = (int)max(1, min(max_nbc, (int)((gridDim.x + cnt - 1) / cnt)));
+  const int64_t items = (int64_t)cnt * nbc;
+  double* st = smem + threadIdx.x;
+  uint32_t* code_s = reinterpret_cast<uint32_t*>(smem + RRG_MAX_STACK * blockDim.x);
+  for (int64_t w = blockIdx.x; w < items; w += gridDim.x) {
+    const int c = cols[w / nbc];
+    const int bi = (int)(w % nbc);
+    const rrg_cand cd = b.cands[c];
+    const int64_t r0 = ds.n * (int64_t)bi / nbc, r1 = ds.n * (int64_t)(bi + 1) / nbc;
+    const bool staged = cd.code_len <= kMaxCodeSmem;
+    __syncthreads();  // the previous item's program is no longer read
+    if (staged)
+      for (int i = threadIdx.x; i < cd.code_len; i += blockDim.x) code_s[i] = b.code[cd.code_offset + i];
+    __syncthreads();
+    const uint32_t* code = staged ? code_s : b.code + cd.code_offset;
+    eval_column_stats(code, cd.code_len, b.consts, ds, r0, r1, st, A + pc[c].a_col * ds.n_pad, A, status,
+                      &cst[pc[c].a_col]);
+  }
+}
+
 // grid (blocks per candidate, candidates); rows of block b: [b*n/nb, (b+1)*n/nb)
 __global__ void __launch_bounds__(256) plain_eval_kernel(DevBatch b, DevData ds, const PlainCand* pc,
                                                           const int32_t* list, int cand0, double* A, double* M,
@@ -198,32 +258,7 @@ __global__ void __launch_bounds__(256) plain_eval_kernel(DevBatch b, DevData ds,
   const uint32_t* code = staged ? code_s : b.code + cd.code_offset;
   double* Ac = A + pc[c].a_col * ds.n_pad;
   if (cst) {
-    // one-column table programs: the column's statistics on the way
-    uint32_t f = 0;
-    unsigned long long mx = 0;
-    for (int64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
-      run_row64(code, cd.code_len, b.consts, ds, r, st, Ac, A, status);
-      const double v = Ac[r];
-      const double a = fabs(v);
-      if (v != v) {
-        f |= kCsNaN;
-      } else if (!(a <= 1.35e154)) {  // infinite, or its square overflows
-        f |= kCsBig;
-      } else {
-        const unsigned long long bits = (unsigned long long)__double_as_longlong(a);
-        mx = bits > mx ? bits : mx;
-      }
-      if (r >= 1 && !(a <= 1e-150)) f |= kCsTail;
-    }
-    f = __reduce_or_sync(0xffffffffu, f);
-    for (int o = 16; o > 0; o >>= 1) {
-      const unsigned long long t = __shfl_xor_sync(0xffffffffu, mx, o);
-      mx = t > mx ? t : mx;
-    }
-    if ((threadIdx.x & 31) == 0) {
-      if (f) atomicOr(&cst[pc[c].a_col].flags, f);
-      if (mx) atomicMax(&cst[pc[c].a_col].maxabs, mx);
-    }
+    eval_column_stats(code, cd.code_len, b.consts, ds, r0, r1, st, Ac, A, status, &cst[pc[c].a_col]);
     return;
   }
   for (int64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x)
@@ -557,7 +592,7 @@ bool launch_plain_qr(int max_cols, int grid, cudaStream_t st, DevBatch b, DevDat
   else
     plain_qr_kernel_t<kMaxK + 1><<<grid, 256, sm, st>>>(b, ds, pc, list, cand0, A, M, S, tsqr, nb, coefs, res, status,
                                                         redo, colmap);
-  return cudaGetLastError() == cudaSuccess;
+  return launch_ok("launch_plain_qr");
 }
 
 
@@ -566,7 +601,8 @@ bool launch_plain_qr(int max_cols, int grid, cudaStream_t st, DevBatch b, DevDat
 __global__ void __launch_bounds__(256) plain_resid_kernel(DevBatch b, DevData ds, const PlainCand* pc,
                                                            const int32_t* list, int cand0, const double* A,
                                                            const double* coefs, double* partial,
-                                                           const int32_t* colmap) {
+                                                           const int32_t* colmap, const int32_t* dcount) {
+  if (dcount && cand0 + (int)blockIdx.y >= *dcount) return;
   __shared__ double red[32];
   __shared__ double cs[kMaxK];
   __shared__ int kind[kMaxK];  // 0 skip, 1 free term, 2 bare factor, 3 scaled factor
@@ -620,9 +656,9 @@ __global__ void __launch_bounds__(256) plain_resid_kernel(DevBatch b, DevData ds
 // one thread per candidate: R2, RMSE, sentinel, rebuilt size
 __global__ void finalize_kernel(DevBatch b, DevData ds, const int32_t* list, int cand0, int cand1,
                                 const double* partial, int nb, const double* coefs, rrg_result* res,
-                                uint32_t flags_or, const double* sse_direct) {
+                                uint32_t flags_or, const double* sse_direct, const int32_t* dcount) {
   const int i = cand0 + blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= cand1) return;
+  if (i >= cand1 || (dcount && i >= *dcount)) return;
   const int c = list ? list[i] : i;
   const rrg_cand cd = b.cands[c];
   double ssr = 0.0;
@@ -670,9 +706,9 @@ __global__ void finalize_kernel(DevBatch b, DevData ds, const int32_t* list, int
 
 // ----------------------------------------------------------- launchers ----
 // Result records of the listed candidates back to zero before a re-scoring.
-__global__ void clear_results_kernel(const int32_t* list, int n, rrg_result* res) {
+__global__ void clear_results_kernel(const int32_t* list, int n, rrg_result* res, const int32_t* dcount) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) res[list[i]] = rrg_result{};
+  if (i < n && !(dcount && i >= *dcount)) res[list[i]] = rrg_result{};
 }
 
 // The outcome of the column-pivoted QR (ColPivHouseholderQR.h:482-608, as
@@ -691,9 +727,9 @@ __global__ void clear_results_kernel(const int32_t* list, int n, rrg_result* res
 // on are left to the QR.
 __global__ void sentinel_classify_kernel(DevBatch b, const int32_t* list, int cand0, int cnt, PlainCand* pc,
                                          const int32_t* colmap, const ColStat* cs, int64_t rows, double* coefs,
-                                         rrg_result* res, uint32_t* decided) {
+                                         rrg_result* res, uint32_t* decided, const int32_t* dcount) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= cnt) return;
+  if (i >= cnt || (dcount && cand0 + i >= *dcount)) return;
   const int c = list[cand0 + i];
   const rrg_cand cd = b.cands[c];
   if (cd.mode != RRG_TUNED) return;
@@ -759,10 +795,11 @@ __device__ __forceinline__ int gram_finite_cols(const PlainCand& p, const int32_
 
 __global__ void __launch_bounds__(256) nan_gram_kernel(const int32_t* list, int cnt, const PlainCand* pc,
                                                        const int32_t* colmap, const ColStat* cs, const double* T,
-                                                       int64_t n, int64_t n_pad, double* gpart) {
+                                                       int64_t n, int64_t n_pad, double* gpart,
+                                                       const int32_t* dcount) {
   __shared__ double red[8][kGramE];
   const int i = blockIdx.y;
-  if (i >= cnt) return;
+  if (i >= cnt || (dcount && i >= *dcount)) return;
   const int c = list[i];
   const PlainCand p = pc[c];
   if (!(p.pad & 2)) return;
@@ -800,9 +837,9 @@ __global__ void __launch_bounds__(256) nan_gram_kernel(const int32_t* list, int 
 
 __global__ void nan_gram_decide_kernel(DevBatch b, const int32_t* list, int cnt, PlainCand* pc, const int32_t* colmap,
                                        const ColStat* cs, int nbx, const double* gpart, double* coefs,
-                                       rrg_result* res, uint32_t* decided) {
+                                       rrg_result* res, uint32_t* decided, const int32_t* dcount) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= cnt) return;
+  if (i >= cnt || (dcount && i >= *dcount)) return;
   const int c = list[i];
   if (!(pc[c].pad & 2)) return;
   const int k = pc[c].k, m = k - 1;

@@ -36,15 +36,28 @@ bool launch_plain_qr_cluster(int max_cols, int warps, int n_cand, cudaStream_t s
 // Warps per CTA the cluster QR is built for in a column bucket, the default
 // first; returns how many (0 for an unknown bucket).
 int qr_warp_variants(int bucket, int* out);
+// The list form of the cluster QR: n_clusters clusters take the candidates
+// list[0 .. *count) from the counter *next (zero before the launch), each
+// factorising in working slot (cluster index) of slot_cols >= bucket columns
+// of M.  Bit-identical to launch_plain_qr_cluster.
+bool launch_plain_qr_cluster_list(int bucket, int warps, int n_clusters, cudaStream_t st, DevBatch b, DevData ds,
+                                  const PlainCand* pc, const int32_t* list, const int32_t* count, int32_t* next,
+                                  const double* A, double* M, int slot_cols, double* coefs, rrg_result* res,
+                                  uint32_t* status, const int32_t* colmap, bool count_bytes);
+// Clusters of the list form that fit on the device at once (0 when unknown).
+int qr_cluster_list_clusters(int bucket, int warps);
+// dcount (may be NULL): grid positions at or beyond *dcount do nothing (a
+// list whose length the device decided; the grid covers its capacity).
 __global__ void plain_resid_kernel(DevBatch b, DevData ds, const PlainCand* pc, const int32_t* list, int cand0,
-                                   const double* A, const double* coefs, double* partial, const int32_t* colmap);
+                                   const double* A, const double* coefs, double* partial, const int32_t* colmap,
+                                   const int32_t* dcount = nullptr);
 // partial[c * nb + j]: per-candidate squared-residual partial sums; when
 // sse_direct is given and sse_direct[c] >= 0 (or NaN) it is the SSE itself.
 __global__ void finalize_kernel(DevBatch b, DevData ds, const int32_t* list, int cand0, int cand1,
                                 const double* partial, int nb, const double* coefs, rrg_result* res,
-                                uint32_t flags_or, const double* sse_direct);
+                                uint32_t flags_or, const double* sse_direct, const int32_t* dcount = nullptr);
 
-__global__ void clear_results_kernel(const int32_t* list, int n, rrg_result* res);
+__global__ void clear_results_kernel(const int32_t* list, int n, rrg_result* res, const int32_t* dcount = nullptr);
 
 // Column statistics of an FP64 table (gathered by plain_eval_kernel), for
 // deciding the column-pivoted QR's outcome on non-finite data without running it.
@@ -66,15 +79,23 @@ constexpr int kGramCols = 9;
 // grid (row blocks, listed candidates): per-block FP64 Gram sums of the finite
 // columns of the candidates sentinel_classify_kernel marked (pad bit 1)
 __global__ void nan_gram_kernel(const int32_t* list, int cnt, const PlainCand* pc, const int32_t* colmap,
-                                const ColStat* cs, const double* T, int64_t n, int64_t n_pad, double* gpart);
+                                const ColStat* cs, const double* T, int64_t n, int64_t n_pad, double* gpart,
+                                const int32_t* dcount = nullptr);
 // one thread per listed candidate: a well-conditioned Gram decides the
 // all-NaN outcome (written, pad = 1); otherwise pad = 0 and the QR runs
 __global__ void nan_gram_decide_kernel(DevBatch b, const int32_t* list, int cnt, PlainCand* pc, const int32_t* colmap,
                                        const ColStat* cs, int nbx, const double* gpart, double* coefs,
-                                       rrg_result* res, uint32_t* decided);
+                                       rrg_result* res, uint32_t* decided, const int32_t* dcount = nullptr);
 __global__ void sentinel_classify_kernel(DevBatch b, const int32_t* list, int cand0, int cnt, PlainCand* pc,
                                          const int32_t* colmap, const ColStat* cs, int64_t rows, double* coefs,
-                                         rrg_result* res, uint32_t* decided);
+                                         rrg_result* res, uint32_t* decided, const int32_t* dcount = nullptr);
+// Table columns listed in cols[0 .. *count) (one-column programs, pc[c].a_col
+// = the column), with their column statistics into cst: a persistent grid of
+// any size walks (column, row block) items, each column split into
+// min(max_nbc, ceil(gridDim.x / count)) row blocks.  The values and
+// statistics are those of plain_eval_kernel's one-column form.
+__global__ void table_eval_list_kernel(DevBatch b, DevData ds, const PlainCand* pc, const int32_t* cols,
+                                       const int32_t* count, int max_nbc, double* A, uint32_t* status, ColStat* cst);
 
 size_t plain_eval_smem();
 size_t plain_qr_smem();

@@ -11,6 +11,7 @@
 #include <cfloat>
 #include <cstdint>
 
+#include "../common/error.h"
 #include "../common/rr_sum.h"
 #include "common.cuh"
 #include "plain.cuh"
@@ -120,18 +121,18 @@ struct QrShape {
   static constexpr int U = CPW <= 4 ? 8 : (CPW <= 8 ? 4 : 2);
 };
 
+// The factorisation and solve of candidate c on this cluster, in the working
+// columns Q (k + 1 columns of n_pad doubles).  Every CTA of the cluster calls
+// it with the same c and takes the same exits.
 template <int KB, int W>
-__global__ void __cluster_dims__(kQrCluster, 1, 1) __launch_bounds__(32 * W)
-    plain_qr_cluster_kernel(DevBatch b, DevData ds, const PlainCand* pc, const int32_t* list, int cand0,
-                            const double* A, double* M, double* coefs, rrg_result* res, uint32_t* status,
-                            const int32_t* colmap, int count_bytes) {
+__device__ __forceinline__ void qr_cluster_one(cg::cluster_group& cl, const DevBatch& b, const DevData& ds,
+                                               const PlainCand* pc, int c, const double* A, double* Q, double* coefs,
+                                               rrg_result* res, uint32_t* status, const int32_t* colmap,
+                                               int count_bytes) {
   constexpr int CPW = QrShape<KB, W>::CPW, U = QrShape<KB, W>::U;
-  cg::cluster_group cl = cg::this_cluster();
   const int w = (int)cl.block_rank();
   const int lane = threadIdx.x & 31, wi = threadIdx.x >> 5;
   const int L = w * 32 + lane;  // RR256 lane
-  const int ci = blockIdx.x / kQrCluster;
-  const int c = list ? list[cand0 + ci] : cand0 + ci;
   const rrg_cand cd = b.cands[c];
   // uniform over the cluster: every CTA takes the same exits
   if (cd.mode != RRG_TUNED || (pc[c].pad & 1)) return;
@@ -148,7 +149,6 @@ __global__ void __cluster_dims__(kQrCluster, 1, 1) __launch_bounds__(32 * W)
   __shared__ int s_nonzero;
   if (threadIdx.x == 0) red.parity = 0;
   cl.sync();  // every CTA of the cluster running before any distributed shared memory access
-  double* Q = M + pc[c].m_col * ds.n_pad;
   const int64_t ld = ds.n_pad, rows = ds.n;
   for (int j = threadIdx.x; j <= k; j += blockDim.x) colp[j] = Q + (int64_t)j * ld;
   __syncthreads();
@@ -433,6 +433,48 @@ __global__ void __cluster_dims__(kQrCluster, 1, 1) __launch_bounds__(32 * W)
   cl.sync();
 }
 
+template <int KB, int W>
+__global__ void __cluster_dims__(kQrCluster, 1, 1) __launch_bounds__(32 * W)
+    plain_qr_cluster_kernel(DevBatch b, DevData ds, const PlainCand* pc, const int32_t* list, int cand0,
+                            const double* A, double* M, double* coefs, rrg_result* res, uint32_t* status,
+                            const int32_t* colmap, int count_bytes) {
+  cg::cluster_group cl = cg::this_cluster();
+  const int ci = blockIdx.x / kQrCluster;
+  const int c = list ? list[cand0 + ci] : cand0 + ci;
+  qr_cluster_one<KB, W>(cl, b, ds, pc, c, A, M + pc[c].m_col * ds.n_pad, coefs, res, status, colmap, count_bytes);
+}
+
+// Persistent form over a list whose length the device decided: the clusters
+// of the grid take the candidates list[0 .. *count) one at a time from a
+// shared counter (*next, zero before the launch), each factorising in its own
+// working slot of slot_cols columns of M.  Same bits as the per-candidate
+// kernel: only the placement of the working columns differs.
+template <int KB, int W>
+__global__ void __cluster_dims__(kQrCluster, 1, 1) __launch_bounds__(32 * W)
+    plain_qr_cluster_list_kernel(DevBatch b, DevData ds, const PlainCand* pc, const int32_t* list,
+                                 const int32_t* count, int32_t* next, const double* A, double* M, int slot_cols,
+                                 double* coefs, rrg_result* res, uint32_t* status, const int32_t* colmap,
+                                 int count_bytes) {
+  cg::cluster_group cl = cg::this_cluster();
+  __shared__ int s_take;
+  const int slot = blockIdx.x / kQrCluster;
+  double* Q = M + (int64_t)slot * slot_cols * ds.n_pad;
+  const int cnt = *count;
+  for (;;) {
+    // CTA 0 takes the next candidate and every CTA reads it from CTA 0's
+    // shared memory after the barrier; CTA 0 takes another only after the
+    // factorisation's closing barrier, when every CTA has read this one
+    if (cl.block_rank() == 0 && threadIdx.x == 0) s_take = atomicAdd(next, 1);
+    cl.sync();
+    const int t = *cl.map_shared_rank(&s_take, 0);
+    if (t >= cnt) break;
+    qr_cluster_one<KB, W>(cl, b, ds, pc, list[t], A, Q, coefs, res, status, colmap, count_bytes);
+    cl.sync();
+  }
+  // no CTA leaves while CTA 0's counter slot may still be read
+  cl.sync();
+}
+
 }  // namespace
 
 int qr_warp_variants(int bucket, int* out) {
@@ -457,12 +499,15 @@ bool launch_plain_qr_cluster(int max_cols, int warps, int n_cand, cudaStream_t s
   if (warps == 0) warps = v[0];
   bool known = false;
   for (int i = 0; i < nv; ++i) known = known || v[i] == warps;
-  if (!known) return false;
+  if (!known) {
+    rrc::set_error("QR launch: no kernel built for this column bucket and warps per CTA");
+    return false;
+  }
 #define RRG_QR_CLUSTER(KB, W)                                                                               \
   if (bk == KB && warps == W) {                                                                             \
     plain_qr_cluster_kernel<KB, W><<<grid, 32 * W, 0, st>>>(b, ds, pc, list, cand0, A, M, coefs, res, status, \
                                                             colmap, count_bytes ? 1 : 0);                   \
-    return cudaGetLastError() == cudaSuccess;                                                               \
+    return launch_ok("launch_plain_qr_cluster");                                                               \
   }
   RRG_QR_CLUSTER(4, 1)
   RRG_QR_CLUSTER(4, 2)
@@ -476,6 +521,95 @@ bool launch_plain_qr_cluster(int max_cols, int warps, int n_cand, cudaStream_t s
   RRG_QR_CLUSTER(kMaxK + 1, 8)
   RRG_QR_CLUSTER(kMaxK + 1, 16)
 #undef RRG_QR_CLUSTER
+  rrc::set_error("QR launch: no kernel built for this column bucket and warps per CTA");
+  return false;
+}
+
+namespace {
+// Kernel of a (bucket, warps) pair of the list form, or nullptr.
+template <int KB, int W>
+const void* list_kernel_of() {
+  return reinterpret_cast<const void*>(&plain_qr_cluster_list_kernel<KB, W>);
+}
+bool list_kernel(int bk, int warps, const void** fn) {
+#define RRG_QR_LIST(KB, W) \
+  if (bk == KB && warps == W) { *fn = list_kernel_of<KB, W>(); return true; }
+  RRG_QR_LIST(4, 1)
+  RRG_QR_LIST(4, 2)
+  RRG_QR_LIST(4, 4)
+  RRG_QR_LIST(8, 2)
+  RRG_QR_LIST(8, 4)
+  RRG_QR_LIST(8, 8)
+  RRG_QR_LIST(16, 4)
+  RRG_QR_LIST(16, 8)
+  RRG_QR_LIST(16, 16)
+  RRG_QR_LIST(kMaxK + 1, 8)
+  RRG_QR_LIST(kMaxK + 1, 16)
+#undef RRG_QR_LIST
+  return false;
+}
+}  // namespace
+
+int qr_cluster_list_clusters(int bucket, int warps) {
+  if (warps == 0) {
+    int v[4];
+    if (qr_warp_variants(bucket, v) == 0) return 0;
+    warps = v[0];
+  }
+  const void* fn = nullptr;
+  if (!list_kernel(bucket, warps, &fn)) return 0;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(kQrCluster, 1, 1);
+  cfg.blockDim = dim3(32 * warps, 1, 1);
+  cfg.dynamicSmemBytes = 0;
+  cudaLaunchAttribute attr;
+  attr.id = cudaLaunchAttributeClusterDimension;
+  attr.val.clusterDim.x = kQrCluster;
+  attr.val.clusterDim.y = 1;
+  attr.val.clusterDim.z = 1;
+  cfg.attrs = &attr;
+  cfg.numAttrs = 1;
+  int clusters = 0;
+  if (cudaOccupancyMaxActiveClusters(&clusters, fn, &cfg) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return clusters;
+}
+
+bool launch_plain_qr_cluster_list(int bucket, int warps, int n_clusters, cudaStream_t st, DevBatch b, DevData ds,
+                                  const PlainCand* pc, const int32_t* list, const int32_t* count, int32_t* next,
+                                  const double* A, double* M, int slot_cols, double* coefs, rrg_result* res,
+                                  uint32_t* status, const int32_t* colmap, bool count_bytes) {
+  if (n_clusters <= 0) return true;
+  int v[4];
+  const int nv = qr_warp_variants(bucket, v);
+  if (nv == 0) {
+    rrc::set_error("QR launch: unknown column bucket");
+    return false;
+  }
+  if (warps == 0) warps = v[0];
+  const int grid = n_clusters * kQrCluster;
+#define RRG_QR_LIST(KB, W)                                                                                 \
+  if (bucket == KB && warps == W) {                                                                        \
+    plain_qr_cluster_list_kernel<KB, W><<<grid, 32 * W, 0, st>>>(b, ds, pc, list, count, next, A, M,       \
+                                                                 slot_cols, coefs, res, status, colmap,   \
+                                                                 count_bytes ? 1 : 0);                    \
+    return launch_ok("launch_plain_qr_cluster_list");                                                              \
+  }
+  RRG_QR_LIST(4, 1)
+  RRG_QR_LIST(4, 2)
+  RRG_QR_LIST(4, 4)
+  RRG_QR_LIST(8, 2)
+  RRG_QR_LIST(8, 4)
+  RRG_QR_LIST(8, 8)
+  RRG_QR_LIST(16, 4)
+  RRG_QR_LIST(16, 8)
+  RRG_QR_LIST(16, 16)
+  RRG_QR_LIST(kMaxK + 1, 8)
+  RRG_QR_LIST(kMaxK + 1, 16)
+#undef RRG_QR_LIST
+  rrc::set_error("QR launch: no list kernel built for this column bucket and warps per CTA");
   return false;
 }
 

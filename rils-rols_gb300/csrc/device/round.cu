@@ -21,6 +21,7 @@
 #include "ftable.cuh"
 #include "mixed.cuh"
 #include "plain.cuh"
+#include "rescore.cuh"
 #include "runtime.cuh"
 #include "tune.cuh"
 
@@ -58,9 +59,12 @@ struct Packer {
     total = (size_t)round_up((int64_t)(total + bytes), 256);
     return off;
   }
-  rrg_status send(HostBuf& h, DevBuf& d, cudaStream_t st, bool wait = true) {
-    // the pinned buffer may still feed a copy queued earlier on the stream
-    if (wait) RRG_CUDA(cudaStreamSynchronize(st));
+  // `round`: the context's round sequence number.  The previous round has
+  // completed before a round is submitted, so a pinned buffer waits only when
+  // it already fed a copy earlier in this round (that copy may be queued).
+  rrg_status send(HostBuf& h, DevBuf& d, cudaStream_t st, uint64_t round) {
+    if (h.used_in == round) RRG_CUDA(cudaStreamSynchronize(st));
+    h.used_in = round;
     if (!h.reserve(std::max<size_t>(total, 256)) || !d.reserve(std::max<size_t>(total, 256))) {
       rrc::set_error("factor table: staging allocation failed");
       return RRG_E_OOM;
@@ -473,7 +477,12 @@ rrg_status rrg_context::run_mixed(const rrg_dataset* ds, const std::vector<int32
       }
       ++end;
     }
-    const rrg_status st = mixed_subround(ds, mixed.data() + pos, (int32_t)(end - pos), lf, lid, certify, fb_all);
+    // one sub-round (the table budget holds the whole round): its second
+    // half is decided on the device, with no read-back
+    const bool async = async_rounds && pos == 0 && end == mixed.size();
+    bool async_done = false;
+    const rrg_status st = mixed_subround(ds, mixed.data() + pos, (int32_t)(end - pos), lf, lid, certify, fb_all,
+                                         async, &async_done);
     for (int32_t g : lf) lid[g] = -1;
     if (st != RRG_OK) return st;
     pos = end;
@@ -490,7 +499,9 @@ rrg_status rrg_context::run_mixed(const rrg_dataset* ds, const std::vector<int32
 
 rrg_status rrg_context::mixed_subround(const rrg_dataset* ds, const int32_t* list, int32_t cnt,
                                        const std::vector<int32_t>& lf, const std::vector<int32_t>& lid,
-                                       bool certify, std::vector<int32_t>& fb_all) {
+                                       bool certify, std::vector<int32_t>& fb_all, bool async,
+                                       bool* async_done) {
+  if (async_done) *async_done = false;
   const DevData dd = ds->view();
   const int32_t nfl = (int32_t)lf.size();
   // local programs, contiguous in local id order
@@ -567,7 +578,7 @@ rrg_status rrg_context::mixed_subround(const rrg_dataset* ds, const int32_t* lis
   const size_t o_tcode = pkt.add(tp.code.data(), sizeof(uint32_t) * tp.code.size());
   const size_t o_tmeta = pkt.add(tp.meta.data(), sizeof(int2) * tp.meta.size());
   const size_t o_groups = pkt.add(groups.data(), sizeof(int2) * groups.size());
-  rrg_status pst = pkt.send(h_ftp, d_ftp, stream);
+  rrg_status pst = pkt.send(h_ftp, d_ftp, stream, round_seq);
   if (pst != RRG_OK) return pst;
   float2* F = static_cast<float2*>(d_F.ptr);
   float2* Pself = static_cast<float2*>(d_P.ptr);  // [chunk][3 ncol]
@@ -678,9 +689,7 @@ rrg_status rrg_context::mixed_subround(const rrg_dataset* ds, const int32_t* lis
   const size_t o_list = pk.add(list, sizeof(int32_t) * cnt);
   const size_t o_cfac = pk.add(cand_fac.data(), sizeof(int32_t) * cand_fac.size());
   const size_t o_list2 = pk.add(nullptr, sizeof(int32_t) * cnt);  // filled after the solve
-  // its pinned buffer fed no copy since the last read-back: no need to wait
-  // for the evaluator
-  pst = pk.send(h_ft, d_ft, stream, false);
+  pst = pk.send(h_ft, d_ft, stream, round_seq);
   if (pst != RRG_OK) return pst;
   const uint32_t* d_code = pk.at<const uint32_t>(d_ft, o_code);
   const int2* d_meta = pk.at<const int2>(d_ft, o_meta);
@@ -753,6 +762,326 @@ rrg_status rrg_context::mixed_subround(const rrg_dataset* ds, const int32_t* lis
   }
   mark_end(P_SOLVE, t0);
   launches += 7;
+  if (async && cnt <= 65535) {
+    // ------------------------------------------------------------------
+    // Second half decided on the device: no read-back before the results.
+    // The residual-pass list is compacted from the solve's flags; the FP64
+    // re-scoring lane evaluates, from the round's own table programs, only
+    // the columns its candidates read, decides the certain sentinels, and
+    // factorises the rest with the list form of the cluster QR.  Every value
+    // is computed by the same arithmetic as the host-driven path.
+    // ------------------------------------------------------------------
+    const size_t col8 = sizeof(double) * (size_t)ds->n_pad;
+    const size_t n_all = host_cands.size();
+    static const int kBucketCols[kQrBuckets] = {4, 8, 16, RRG_MAX_TERMS + 1};
+    int bucket_cap[kQrBuckets] = {0, 0, 0, 0};
+    for (int32_t li = 0; li < cnt; ++li) {
+      const rrg_cand& cd = host_cands[list[li]];
+      if (cd.mode != RRG_TUNED) continue;
+      const int cols = cd.n_factors + 2;
+      ++bucket_cap[cols <= 4 ? 0 : (cols <= 8 ? 1 : (cols <= 16 ? 2 : 3))];
+    }
+    int qwarps[kQrBuckets] = {0, 0, 0, 0}, nclus[kQrBuckets] = {0, 0, 0, 0};
+    for (int q = 0; q < kQrBuckets; ++q) {
+      if (!bucket_cap[q]) continue;
+      bool trial = false;
+      qwarps[q] = tune_pick(TK_QR_WARPS, kBucketCols[q], ds->n, &trial);
+      int occ = qr_cluster_list_clusters(kBucketCols[q], qwarps[q]);
+      if (occ <= 0) occ = std::max(1, sm_count / 8);
+      nclus[q] = std::min(bucket_cap[q], occ);
+    }
+    // working slots of the QR within half the scratch budget (the FP64
+    // table takes the other half): the widest buckets give up clusters first
+    auto slot_bytes = [&]() {
+      double t = 0.0;
+      for (int q = 0; q < kQrBuckets; ++q) t += (double)nclus[q] * kBucketCols[q] * (double)col8;
+      return t;
+    };
+    for (int q = kQrBuckets - 1; q >= 0 && slot_bytes() > (double)scratch_budget_bytes / 2; --q)
+      while (nclus[q] > 1 && slot_bytes() > (double)scratch_budget_bytes / 2) nclus[q] = (nclus[q] + 1) / 2;
+    const bool fits = slot_bytes() <= (double)scratch_budget_bytes / 2 &&
+                      (double)ncol * (double)col8 <= (double)scratch_budget_bytes / 2;
+    if (fits) {
+      // host records of the lane: one-column pseudo-candidates of the table
+      // programs, the shared-column closure of every column, placements of
+      // the round's candidates (factor columns through cand_col)
+      std::vector<rrg_cand> fc(std::max(1, ncol));
+      std::vector<PlainCand> fpc(std::max(1, ncol));
+      std::vector<int32_t> dep_off(ncol + 1, 0), deps;
+      std::vector<std::vector<int32_t>> closure(ncol);
+      for (int32_t i = 0; i < ncol; ++i) {
+        rrg_cand& p = fc[i];
+        p.code_offset = tp.meta[i].x;
+        p.code_len = tp.meta[i].y;
+        p.first_factor = 0;
+        p.n_factors = 1;
+        p.mode = RRG_UNTUNED;
+        p.coef_offset = 0;
+        p.stack_need = tp.stack[i];
+        p.reserved = 0;
+        fpc[i] = PlainCand{i, 0, 0, 1, 0};
+        std::vector<int32_t>& cl = closure[i];
+        for (int pc = 0; pc < tp.meta[i].y; ++pc) {
+          const uint32_t w = tp.code[tp.meta[i].x + pc];
+          const int op = (int)(w & 0xffu);
+          const bool tref = op == kOpLDT || op == kOpPST ||
+                            (op >= RRG_OP_BIN && (((op - RRG_OP_BIN) & 7) >> 1) == kSrcT);
+          if (!tref) continue;
+          const int32_t a = (int32_t)(w >> 8);
+          cl.push_back(a);
+          cl.insert(cl.end(), closure[a].begin(), closure[a].end());  // a is of a lower level
+        }
+        std::sort(cl.begin(), cl.end());
+        cl.erase(std::unique(cl.begin(), cl.end()), cl.end());
+        dep_off[i + 1] = dep_off[i] + (int32_t)cl.size();
+        deps.insert(deps.end(), cl.begin(), cl.end());
+      }
+      std::vector<int32_t> li_of(n_all, -1);
+      std::vector<PlainCand> pcs(std::max<size_t>(1, n_all));
+      for (int32_t li = 0; li < cnt; ++li) {
+        const int32_t c = list[li];
+        const rrg_cand& cd = host_cands[c];
+        li_of[c] = li;
+        pcs[c] = PlainCand{(int64_t)li * kMixedMaxM, 0, 0, cd.mode == RRG_TUNED ? cd.n_factors + 1 : 1, 0};
+      }
+      const int32_t n_levels = (int32_t)tp.level_end.size();
+      Packer pf;
+      const size_t o_fc = pf.add(fc.data(), sizeof(rrg_cand) * fc.size());
+      const size_t o_fpc = pf.add(fpc.data(), sizeof(PlainCand) * fpc.size());
+      const size_t o_doff = pf.add(dep_off.data(), sizeof(int32_t) * dep_off.size());
+      const size_t o_deps = pf.add(deps.data(), sizeof(int32_t) * std::max<size_t>(1, deps.size()));
+      const size_t o_liof = pf.add(li_of.data(), sizeof(int32_t) * li_of.size());
+      const size_t o_pcs = pf.add(pcs.data(), sizeof(PlainCand) * pcs.size());
+      const size_t o_lend = pf.add(tp.level_end.data(), sizeof(int32_t) * tp.level_end.size());
+      pst = pf.send(h_fbpack, d_fbpack, stream, round_seq);
+      if (pst != RRG_OK) return pst;
+      const int nb_res = (int)((ds->n + RR_CHUNK - 1) / RR_CHUNK);
+      const int nbx = (int)std::max<int64_t>(1, std::min<int64_t>(16, (ds->n + 32767) / 32768));
+      size_t m_cols = 0;
+      for (int q = 0; q < kQrBuckets; ++q) m_cols += (size_t)nclus[q] * kBucketCols[q];
+      const size_t stat_words = 2 + kFbReasons + (size_t)n_levels;
+      if (!d_rlist2.reserve(sizeof(int32_t) * (cnt + 1)) || !d_fbneed.reserve(std::max(1, ncol)) ||
+          !d_fbcols.reserve(sizeof(int32_t) * (ncol + n_levels + 1)) ||
+          !d_fbF64.reserve(col8 * std::max(1, ncol)) || !d_fbcst.reserve(sizeof(ColStat) * std::max(1, ncol)) ||
+          !d_fbgram.reserve(sizeof(double) * (size_t)cnt * nbx * (kGramCols * (kGramCols + 1) / 2)) ||
+          !d_fbblist.reserve(sizeof(int32_t) * ((size_t)kQrBuckets * cnt + 2 * kQrBuckets)) ||
+          !d_fbM.reserve(col8 * std::max<size_t>(1, m_cols)) ||
+          !h_fbstat.reserve(sizeof(int32_t) * stat_words)) {
+        rrc::set_error("mixed round: re-scoring lane allocation failed");
+        return RRG_E_OOM;
+      }
+      int32_t* list2 = static_cast<int32_t*>(d_rlist2.ptr);
+      int32_t* count2 = list2 + cnt;
+      uint8_t* need = static_cast<uint8_t*>(d_fbneed.ptr);
+      int32_t* lvl_cols = static_cast<int32_t*>(d_fbcols.ptr);
+      int32_t* lvl_count = lvl_cols + ncol;
+      double* F64 = static_cast<double*>(d_fbF64.ptr);
+      ColStat* cst = static_cast<ColStat*>(d_fbcst.ptr);
+      double* gpart = static_cast<double*>(d_fbgram.ptr);
+      int32_t* blist = static_cast<int32_t*>(d_fbblist.ptr);
+      int32_t* bcount = blist + (size_t)kQrBuckets * cnt;
+      int32_t* qnext = bcount + kQrBuckets;
+      double* Mq = static_cast<double*>(d_fbM.ptr);
+      const int32_t* d_ccol = pk.at<const int32_t>(d_ft, o_ccol);
+      PlainCand* d_pcs = pf.at<PlainCand>(d_fbpack, o_pcs);
+      const int32_t* fb_count = fallback;  // fallback[0]: entries queued so far
+      const int32_t* fb_list = fallback + 1;
+      double* coefs = static_cast<double*>(d_coefs.ptr);
+      rrg_result* res = static_cast<rrg_result*>(d_res.ptr);
+      double* sse = static_cast<double*>(d_partial.ptr);
+      // residual pass of the mixed candidates whose one-pass SSE is not
+      // accurate enough, over the device-compacted list
+      if (!launch_pass2_compact(d_list, cnt, pass2, list2, count2, stream)) {
+        cuda_ok(cudaGetLastError(), "residual list launch");
+        return RRG_E_CUDA;
+      }
+      ResidArgs ra;
+      ra.b = dev;
+      ra.ds = dd;
+      ra.F = F;
+      ra.mlist = d_list;
+      ra.list2 = list2;
+      ra.n2 = cnt;
+      ra.n2_dev = count2;
+      ra.cand_col = d_ccol;
+      ra.terms = static_cast<const MixedTerm*>(d_terms.ptr);
+      ra.n_chunks = n_super;
+      ra.sse = sse;
+      t0 = mark_begin();
+      if (!launch_ftab_resid(ra, stream, 16 * sm_count) ||
+          (certify && !launch_cert_resid(d_list, list2, cnt, sse, n_super, static_cast<const double*>(d_cert_e.ptr),
+                                         dd, cert_tol, fallback, fb_cap, reasons, stream, count2))) {
+        cuda_ok(cudaGetLastError(), "mixed residual launch");
+        return RRG_E_CUDA;
+      }
+      mark_end(P_RESID, t0);
+      t0 = mark_begin();
+      finalize_kernel<<<(cnt + 127) / 128, 128, 0, stream>>>(dev, dd, d_list, 0, cnt, sse, n_super,
+                                                             static_cast<const double*>(d_coefs.ptr), res, 0u,
+                                                             static_cast<const double*>(d_sse1.ptr));
+      mark_end(P_FINAL, t0);
+      launches += 3 + (certify ? 1 : 0);
+      // FP64 re-scoring lane over fallback[1 .. 1 + fallback[0])
+      t0 = mark_begin();
+      RRG_CUDA(cudaMemsetAsync(need, 0, std::max(1, ncol), stream));
+      RRG_CUDA(cudaMemsetAsync(cst, 0, sizeof(ColStat) * std::max(1, ncol), stream));
+      RRG_CUDA(cudaMemsetAsync(bcount, 0, sizeof(int32_t) * 2 * kQrBuckets, stream));
+      DevBatch fdev = dev;
+      fdev.cands = pf.at<const rrg_cand>(d_fbpack, o_fc);
+      fdev.code = pkt.at<const uint32_t>(d_ftp, o_tcode);
+      fdev.n_cand = ncol;
+      fdev.n_code = (int32_t)tp.code.size();
+      clear_results_kernel<<<(cnt + 255) / 256, 256, 0, stream>>>(fb_list, cnt, res, fb_count);
+      if (!launch_rescore_mark(dev.cands, fallback, cnt, pf.at<const int32_t>(d_fbpack, o_liof), d_ccol,
+                               pf.at<const int32_t>(d_fbpack, o_doff), pf.at<const int32_t>(d_fbpack, o_deps), need,
+                               stream) ||
+          !launch_rescore_levels(need, pf.at<const int32_t>(d_fbpack, o_lend), n_levels, lvl_cols, lvl_count,
+                                 stream)) {
+        cuda_ok(cudaGetLastError(), "re-scoring list launch");
+        return RRG_E_CUDA;
+      }
+      bool wave_trial = false;
+      int waves = tune_pick(TK_EVAL_WAVES, 0, ds->n, &wave_trial);
+      const int max_nbc = (int)std::max<int64_t>(1, (ds->n + 1023) / 1024);
+      auto eval_level = [&](int32_t L, int wv) {
+        const int32_t lo = L == 0 ? 0 : tp.level_end[L - 1];
+        table_eval_list_kernel<<<std::max(1, wv * sm_count), 256, plain_eval_smem(), stream>>>(
+            fdev, dd, pf.at<const PlainCand>(d_fbpack, o_fpc), lvl_cols + lo, lvl_count + L, max_nbc, F64, status,
+            cst);
+      };
+      if (wave_trial && !capturing && n_levels > 0) {
+        // the first round of this row class: read the per-level counts back
+        // once and time every shape on the widest level (re-evaluating a
+        // level rewrites the same columns and statistics)
+        std::vector<int32_t> hc(n_levels);
+        RRG_CUDA(cudaMemcpyAsync(hc.data(), lvl_count, sizeof(int32_t) * n_levels, cudaMemcpyDeviceToHost, stream));
+        RRG_CUDA(cudaStreamSynchronize(stream));
+        int32_t widest = 0;
+        for (int32_t L = 1; L < n_levels; ++L)
+          if (hc[L] > hc[widest]) widest = L;
+        if ((int64_t)hc[widest] * ds->n >= kTuneMinWork) {
+          for (int32_t L = 0; L < widest; ++L) eval_level(L, waves);  // the columns the widest level reads
+          int vals[4];
+          float ms[4];
+          const int nv = tune_variants(TK_EVAL_WAVES, 0, vals);
+          for (int v = 0; v < nv; ++v) {
+            rrg_status ts = time_trial([&] { eval_level(widest, vals[v]); }, ms[v]);
+            if (ts != RRG_OK) return ts;
+          }
+          tune_store(TK_EVAL_WAVES, 0, ds->n, vals, ms, nv);
+          waves = tune_pick(TK_EVAL_WAVES, 0, ds->n, &wave_trial);
+        }
+      }
+      for (int32_t L = 0; L < n_levels; ++L) eval_level(L, waves);
+      sentinel_classify_kernel<<<(cnt + 127) / 128, 128, 0, stream>>>(dev, fb_list, 0, cnt, d_pcs, d_ccol, cst,
+                                                                     ds->n, coefs, res, status + kStatusSentinel,
+                                                                     fb_count);
+      nan_gram_kernel<<<dim3(nbx, cnt), 256, 0, stream>>>(fb_list, cnt, d_pcs, d_ccol, cst, F64, ds->n, ds->n_pad,
+                                                          gpart, fb_count);
+      nan_gram_decide_kernel<<<(cnt + 127) / 128, 128, 0, stream>>>(dev, fb_list, cnt, d_pcs, d_ccol, cst, nbx, gpart,
+                                                                    coefs, res, status + kStatusSentinel, fb_count);
+      if (!launch_rescore_buckets(dev.cands, fallback, cnt, d_pcs, blist, bcount, stream)) {
+        cuda_ok(cudaGetLastError(), "re-scoring bucket launch");
+        return RRG_E_CUDA;
+      }
+      mark_end(P_PLAIN_EVAL, t0);
+      launches += n_levels + 6;
+      // launch-shape trials of the QR (the first round of a bucket and row
+      // class): the bucket counts are read back once so that a trial times
+      // real work; a repeat restarts from the table columns (same results)
+      {
+        bool qtrial[kQrBuckets] = {false, false, false, false}, any = false;
+        for (int q = 0; q < kQrBuckets; ++q) {
+          if (!nclus[q] || capturing) continue;
+          bool tr = false;
+          tune_pick(TK_QR_WARPS, kBucketCols[q], ds->n, &tr);
+          qtrial[q] = tr;
+          any = any || tr;
+        }
+        if (any) {
+          int32_t hb[kQrBuckets] = {0, 0, 0, 0};
+          RRG_CUDA(cudaMemcpyAsync(hb, bcount, sizeof hb, cudaMemcpyDeviceToHost, stream));
+          RRG_CUDA(cudaStreamSynchronize(stream));
+          size_t off = 0;
+          for (int q = 0; q < kQrBuckets; ++q) {
+            double* Mb = Mq + off * ds->n_pad;
+            off += (size_t)nclus[q] * kBucketCols[q];
+            if (!qtrial[q] || (int64_t)hb[q] * ds->n < kTuneMinWork) continue;
+            int vals[4];
+            float ms[4];
+            const int nv = tune_variants(TK_QR_WARPS, kBucketCols[q], vals);
+            for (int v = 0; v < nv; ++v) {
+              const int nc = std::min(nclus[q], std::max(1, qr_cluster_list_clusters(kBucketCols[q], vals[v])));
+              bool ok = true;
+              rrg_status ts = time_trial([&] {
+                ok = cudaMemsetAsync(qnext + q, 0, sizeof(int32_t), stream) == cudaSuccess &&
+                     launch_plain_qr_cluster_list(kBucketCols[q], vals[v], nc, stream, dev, dd, d_pcs,
+                                                  blist + (size_t)q * cnt, bcount + q, qnext + q, F64, Mb,
+                                                  kBucketCols[q], coefs, res, status, d_ccol, false);
+              }, ms[v]);
+              if (!ok) return RRG_E_CUDA;
+              if (ts != RRG_OK) return ts;
+              launches += 1;
+            }
+            tune_store(TK_QR_WARPS, kBucketCols[q], ds->n, vals, ms, nv);
+            bool tr = false;
+            qwarps[q] = tune_pick(TK_QR_WARPS, kBucketCols[q], ds->n, &tr);
+            nclus[q] = std::min(nclus[q], std::max(1, qr_cluster_list_clusters(kBucketCols[q], qwarps[q])));
+          }
+          RRG_CUDA(cudaMemsetAsync(qnext, 0, sizeof(int32_t) * kQrBuckets, stream));
+        }
+      }
+      // one list-form QR per column bucket, side by side on the side streams
+      t0 = mark_begin();
+      RRG_CUDA(cudaEventRecord(fork_ev, stream));
+      int used = 0;
+      size_t m_off = 0;
+      for (int q = 0; q < kQrBuckets; ++q) {
+        if (!nclus[q]) continue;
+        cudaStream_t sq = side[used % kSide];
+        if (used < kSide) RRG_CUDA(cudaStreamWaitEvent(sq, fork_ev, 0));
+        if (!launch_plain_qr_cluster_list(kBucketCols[q], qwarps[q], nclus[q], sq, dev, dd, d_pcs,
+                                          blist + (size_t)q * cnt, bcount + q, qnext + q, F64, Mq + m_off * ds->n_pad,
+                                          kBucketCols[q], coefs, res, status, d_ccol, true)) {
+          cuda_ok(cudaGetLastError(), "QR launch");
+          return RRG_E_CUDA;
+        }
+        m_off += (size_t)nclus[q] * kBucketCols[q];
+        ++used;
+        ++launches;
+      }
+      for (int i = 0; i < std::min(used, (int)kSide); ++i) {
+        RRG_CUDA(cudaEventRecord(join_ev[i], side[i]));
+        RRG_CUDA(cudaStreamWaitEvent(stream, join_ev[i], 0));
+      }
+      mark_end(P_PLAIN_QR, t0);
+      t0 = mark_begin();
+      plain_resid_kernel<<<dim3(nb_res, cnt), 256, 0, stream>>>(dev, dd, d_pcs, fb_list, 0, F64, coefs, sse, d_ccol,
+                                                               fb_count);
+      mark_end(P_PLAIN_RESID, t0);
+      t0 = mark_begin();
+      finalize_kernel<<<(cnt + 127) / 128, 128, 0, stream>>>(dev, dd, fb_list, 0, cnt, sse, nb_res, coefs, res,
+                                                             RRG_F_QR_FALLBACK, nullptr, fb_count);
+      mark_end(P_FINAL, t0);
+      launches += 2;
+      // statistics for rrg_last_round_stats: re-scored count, residual-pass
+      // count, reasons, columns evaluated per level
+      int32_t* hs = static_cast<int32_t*>(h_fbstat.ptr);
+      RRG_CUDA(cudaMemcpyAsync(hs, fallback, sizeof(int32_t), cudaMemcpyDeviceToHost, stream));
+      RRG_CUDA(cudaMemcpyAsync(hs + 1, count2, sizeof(int32_t), cudaMemcpyDeviceToHost, stream));
+      RRG_CUDA(cudaMemcpyAsync(hs + 2, reasons, sizeof(uint32_t) * kFbReasons, cudaMemcpyDeviceToHost, stream));
+      if (n_levels)
+        RRG_CUDA(cudaMemcpyAsync(hs + 2 + kFbReasons, lvl_count, sizeof(int32_t) * n_levels, cudaMemcpyDeviceToHost,
+                                 stream));
+      fbstat_pending = true;
+      fbstat_levels = n_levels;
+      fbstat_rows = (double)ds->n;
+      fbstat_d = ds->d;
+      RRG_CUDA(cudaGetLastError());
+      if (async_done) *async_done = true;
+      return RRG_OK;
+    }
+  }
   // residual-pass flags (and the fallback list so far) back to the host
   RRG_CUDA(cudaMemcpyAsync(h_fallback.ptr, d_fallback.ptr, back_bytes, cudaMemcpyDeviceToHost, stream));
   RRG_CUDA(cudaStreamSynchronize(stream));
@@ -777,6 +1106,7 @@ rrg_status rrg_context::mixed_subround(const rrg_dataset* ds, const int32_t* lis
     ra.mlist = d_list;
     ra.list2 = d_list2;
     ra.n2 = (int32_t)list2.size();
+    ra.n2_dev = nullptr;
     ra.cand_col = pk.at<const int32_t>(d_ft, o_ccol);
     ra.terms = static_cast<const MixedTerm*>(d_terms.ptr);
     ra.n_chunks = n_super;
@@ -938,7 +1268,7 @@ rrg_status rrg_context::run_fp64_table(const rrg_dataset* ds, const std::vector<
     const size_t o_cmap = pk.add(colmap.data(), sizeof(int32_t) * std::max<size_t>(1, colmap.size()));
     const size_t o_pcs = pk.add(pcs.data(), sizeof(PlainCand) * pcs.size());
     const size_t o_list = pk.add(list.data() + pos, sizeof(int32_t) * ng);
-    rrg_status pst = pk.send(h_ft64, d_ft64, stream);
+    rrg_status pst = pk.send(h_ft64, d_ft64, stream, round_seq);
     if (pst != RRG_OK) return pst;
     if (!d_F64.reserve(col8 * std::max(1, ncol)) || !d_M.reserve(col8 * mcols_max)) {
       rrc::set_error("FP64 round: table allocation failed");
@@ -993,7 +1323,7 @@ rrg_status rrg_context::run_fp64_table(const rrg_dataset* ds, const std::vector<
           ++launches;
         }
       };
-      if (wave_trial && L == wave_level && (int64_t)nl * ds->n >= kTuneMinWork) {
+      if (wave_trial && !capturing && L == wave_level && (int64_t)nl * ds->n >= kTuneMinWork) {
         // re-evaluating a level rewrites the same columns: time every shape
         int vals[4];
         float ms[4];
@@ -1054,7 +1384,7 @@ rrg_status rrg_context::run_fp64_table(const rrg_dataset* ds, const std::vector<
         while (b1 < sb.second && bucket(list[pos + b1]) == bk) ++b1;
         bool trial = false;
         int warps = tune_pick(TK_QR_WARPS, bk, ds->n, &trial);
-        if (trial && (int64_t)(b1 - b0) * ds->n >= kTuneMinWork) {
+        if (trial && !capturing && (int64_t)(b1 - b0) * ds->n >= kTuneMinWork) {
           int vals[4];
           float ms[4];
           const int nv = tune_variants(TK_QR_WARPS, bk, vals);

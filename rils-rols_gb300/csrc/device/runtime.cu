@@ -90,6 +90,15 @@ void HostBuf::release() {
 }
 
 // --------------------------------------------------------------- timing ----
+namespace rrd {
+bool launch_ok(const char* what) {
+  const cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) return true;
+  rrc::set_error(std::string(what) + ": " + cudaGetErrorString(e));
+  return false;
+}
+}  // namespace rrd
+
 cudaEvent_t rrg_context::mark_begin() {
   if (!timing) return nullptr;
   if (event_next >= event_pool.size()) {
@@ -293,7 +302,8 @@ rrg_status rrg_context::run_plain(const rrg_dataset* ds, int32_t lo, int32_t hi,
     return RRG_E_OOM;
   }
   // h_pc may still feed a copy queued by an earlier call of this round
-  RRG_CUDA(cudaStreamSynchronize(stream));
+  if (h_pc.used_in == round_seq) RRG_CUDA(cudaStreamSynchronize(stream));
+  h_pc.used_in = round_seq;
   std::memcpy(h_pc.ptr, pcs.data(), pc_bytes);
   std::memcpy(static_cast<char*>(h_pc.ptr) + pc_bytes, list->data(), list_bytes);
   RRG_CUDA(cudaMemcpyAsync(d_pc.ptr, h_pc.ptr, pc_bytes, cudaMemcpyHostToDevice, stream));
@@ -397,6 +407,70 @@ rrg_status rrg_context::submit(rrg_dataset* ds, const rrg_batch* b, int32_t prec
     return RRG_E_INVALID;
   if (n_coefs > 0 && !coefs) return RRG_E_INVALID;
   RRG_CUDA(cudaSetDevice(device));
+  last_graph = false;
+  if (graph_rounds && !timing) {
+    // the round's work captured from the context stream (and the side
+    // streams it forks) into a graph, then launched as one; the graph of the
+    // previous round is updated in place when the shapes allow.  A round
+    // that cannot be captured (a host wait inside it: a launch-shape trial,
+    // a reused staging buffer, table sub-rounds) is enqueued directly.
+    cudaGraph_t g = nullptr;
+    rrg_status cst = RRG_E_CUDA;
+    if (cudaStreamBeginCapture(stream, cudaStreamCaptureModeRelaxed) == cudaSuccess) {
+      capturing = true;
+      cst = enqueue_round(ds, b, precision, n_coefs);
+      capturing = false;
+      const cudaError_t ec = cudaStreamEndCapture(stream, &g);
+      if (ec != cudaSuccess) cst = RRG_E_CUDA;
+    }
+    bool launched = false;
+    if (cst == RRG_OK && g) {
+      bool ready = false;
+      if (graph_exec) {
+        cudaGraphExecUpdateResultInfo info;
+        ready = cudaGraphExecUpdate(graph_exec, g, &info) == cudaSuccess;
+        if (!ready) {
+          cudaGetLastError();
+          cudaGraphExecDestroy(graph_exec);
+          graph_exec = nullptr;
+        }
+      }
+      if (!ready) ready = cudaGraphInstantiate(&graph_exec, g, 0) == cudaSuccess;
+      launched = ready && cudaGraphLaunch(graph_exec, stream) == cudaSuccess;
+    }
+    if (g) cudaGraphDestroy(g);
+    if (launched) {
+      last_graph = true;
+      st = RRG_OK;
+    } else {
+      cudaGetLastError();
+      ++graph_fallbacks;
+      st = enqueue_round(ds, b, precision, n_coefs);
+    }
+  } else {
+    st = enqueue_round(ds, b, precision, n_coefs);
+  }
+  if (st != RRG_OK) return st;
+  RRG_CUDA(cudaEventRecord(done, stream));
+  in_flight = true;
+  out_results = results;
+  out_coefs = coefs;
+  out_n = b->n_cand;
+  out_ncoef = n_coefs;
+  return RRG_OK;
+}
+
+// The device work of one round on the context stream: batch upload, the
+// precision's kernels, the results back into pinned staging.  Everything
+// that reaches the device goes through the stream (or side streams forked
+// from it), so it can run under stream capture.
+rrg_status rrg_context::enqueue_round(rrg_dataset* ds, const rrg_batch* b, int32_t precision, int64_t n_coefs) {
+  rrg_status st = RRG_OK;
+  // an error another library left pending on this thread is not this
+  // round's: clear it so the launch checks below see only their own
+  cudaGetLastError();
+  ++round_seq;
+  fbstat_pending = false;
   launches = 0;
   last_plain_routed = last_fallback = last_pass2 = last_sentinel = 0;
   for (double& v : phase_bytes) v = 0.0;
@@ -420,6 +494,8 @@ rrg_status rrg_context::submit(rrg_dataset* ds, const rrg_batch* b, int32_t prec
   build_factor_table(host_cands.data(), b->n_cand, b->code, b->consts, ft);
   std::vector<int32_t> reps;
   dedup_candidates(reps);
+  last_distinct = (int64_t)reps.size();
+  last_tiled = false;
   // on small datasets the mixed form's probes, pair sums and read-backs cost
   // more than the FP64 arithmetic they replace: such rounds run in FP64
   // (exact, so within any certified bound).  So do rounds on a constant y
@@ -428,7 +504,10 @@ rrg_status rrg_context::submit(rrg_dataset* ds, const rrg_batch* b, int32_t prec
   if (precision == RRG_PLAIN_FP64 || ds->n < mixed_min_rows || !(ds->sst > 0.0)) {
     // few candidates on tall data: the tiled QR spreads each over the GPU;
     // otherwise one block per candidate over the shared FP64 factor table
-    if (ds->n >= 65536 && (int64_t)reps.size() < 2 * sm_count) st = run_plain(ds, 0, 0, false, &reps);
+    if (ds->n >= 65536 && (int64_t)reps.size() < 2 * sm_count) {
+      last_tiled = true;
+      st = run_plain(ds, 0, 0, false, &reps);
+    }
     else st = run_fp64_table(ds, reps, 0u);
   } else {
     st = run_mixed(ds, reps, precision == RRG_MIXED_CERTIFIED);
@@ -437,12 +516,6 @@ rrg_status rrg_context::submit(rrg_dataset* ds, const rrg_batch* b, int32_t prec
   RRG_CUDA(cudaMemcpyAsync(h_res.ptr, d_res.ptr, res_bytes, cudaMemcpyDeviceToHost, stream));
   RRG_CUDA(cudaMemcpyAsync(h_coefs.ptr, d_coefs.ptr, coef_bytes, cudaMemcpyDeviceToHost, stream));
   RRG_CUDA(cudaMemcpyAsync(h_status.ptr, d_status.ptr, 64, cudaMemcpyDeviceToHost, stream));
-  RRG_CUDA(cudaEventRecord(done, stream));
-  in_flight = true;
-  out_results = results;
-  out_coefs = coefs;
-  out_n = b->n_cand;
-  out_ncoef = n_coefs;
   return RRG_OK;
 }
 
@@ -474,6 +547,17 @@ rrg_status rrg_context::wait(int32_t timeout_ms) {
   }
   last_sentinel = static_cast<const uint32_t*>(h_status.ptr)[rrd::kStatusSentinel];
   for (int i = 0; i < P_COUNT; ++i) last_phase_bytes[i] = phase_bytes[i];
+  if (fbstat_pending) {
+    // statistics of a mixed round whose second half the device decided
+    const int32_t* hs = static_cast<const int32_t*>(h_fbstat.ptr);
+    last_fallback += hs[0];
+    last_pass2 += hs[1];
+    for (int i = 0; i < kFbReasons && i < 16; ++i) last_reasons[i] += static_cast<const uint32_t*>(h_fbstat.ptr)[2 + i];
+    int64_t cols = 0;
+    for (int32_t L = 0; L < fbstat_levels; ++L) cols += hs[2 + kFbReasons + L];
+    last_phase_bytes[P_PLAIN_EVAL] += fbstat_rows * 8.0 * (double)(fbstat_d + cols);
+    fbstat_pending = false;
+  }
   {
     unsigned long long qb = 0;
     std::memcpy(&qb, static_cast<const uint32_t*>(h_status.ptr) + rrd::kStatusQrBytes, sizeof qb);
@@ -508,6 +592,7 @@ rrg_status rrg_context::wait(int32_t timeout_ms) {
 
 rrg_context::~rrg_context() {
   if (in_flight) cudaEventSynchronize(done);
+  if (graph_exec) cudaGraphExecDestroy(graph_exec);
   d_batch.release();
   d_A.release();
   d_S.release();
@@ -527,8 +612,11 @@ rrg_context::~rrg_context() {
   h_mlist.release();
   h_fallback.release();
   for (DevBuf* bf : {&d_ft, &d_ftp, &d_ft64, &d_F, &d_P, &d_Pc, &d_psum, &d_fprobe, &d_fnan, &d_F64, &d_M, &d_colstat,
-                      &d_gram})
+                      &d_gram, &d_rlist2, &d_fbpack, &d_fbneed, &d_fbcols, &d_fbF64, &d_fbcst, &d_fbgram, &d_fbblist,
+                      &d_fbM, &d_fbctr})
     bf->release();
+  h_fbpack.release();
+  h_fbstat.release();
   h_ft.release();
   h_ftp.release();
   h_ft64.release();
@@ -772,6 +860,8 @@ rrg_status rrg_predict(rrg_dataset* ds, const rrg_batch* batch, double* values) 
     return RRG_E_INVALID;
   }
   RRG_CUDA(cudaSetDevice(ctx->device));
+  cudaGetLastError();  // not this call's: an error left pending on this thread by other code
+  ++ctx->round_seq;
   st = ctx->stage_batch(&one);
   if (st != RRG_OK) return st;
   if (!ctx->d_status.reserve(64) || !ctx->h_status.reserve(64)) return RRG_E_OOM;
@@ -801,10 +891,13 @@ int64_t rrg_last_round_launches(const rrg_context* ctx) { return ctx ? ctx->last
 
 int32_t rrg_last_round_stats(const rrg_context* ctx, int64_t* out, int32_t n) {
   if (!ctx || !out || n <= 0) return 0;
-  int64_t v[5 + kFbReasons] = {ctx->last_launches, ctx->last_plain_routed, ctx->last_fallback, ctx->last_pass2};
+  int64_t v[8 + kFbReasons] = {ctx->last_launches, ctx->last_plain_routed, ctx->last_fallback, ctx->last_pass2};
   for (int i = 0; i < kFbReasons; ++i) v[4 + i] = ctx->last_reasons[i];
   v[4 + kFbReasons] = ctx->last_sentinel;
-  const int32_t k = n < 5 + kFbReasons ? n : 5 + kFbReasons;
+  v[5 + kFbReasons] = ctx->last_distinct;
+  v[6 + kFbReasons] = ctx->last_tiled ? 1 : 0;
+  v[7 + kFbReasons] = ctx->last_graph ? 1 : 0;
+  const int32_t k = n < 8 + kFbReasons ? n : 8 + kFbReasons;
   for (int32_t i = 0; i < k; ++i) out[i] = v[i];
   return k;
 }
@@ -814,6 +907,26 @@ void* rrg_context_stream(const rrg_context* ctx) { return ctx ? (void*)ctx->stre
 rrg_status rrg_context_set_timing(rrg_context* ctx, int32_t on) {
   if (!ctx) return RRG_E_INVALID;
   ctx->timing = on != 0;
+  return RRG_OK;
+}
+
+rrg_status rrg_context_set_graph(rrg_context* ctx, int32_t on) {
+  if (!ctx) return RRG_E_INVALID;
+  if (ctx->in_flight) {
+    rrc::set_error("rrg_context_set_graph: a round is in flight");
+    return RRG_E_INVALID;
+  }
+  ctx->graph_rounds = on != 0;
+  return RRG_OK;
+}
+
+rrg_status rrg_context_set_async(rrg_context* ctx, int32_t on) {
+  if (!ctx) return RRG_E_INVALID;
+  if (ctx->in_flight) {
+    rrc::set_error("rrg_context_set_async: a round is in flight");
+    return RRG_E_INVALID;
+  }
+  ctx->async_rounds = on != 0;
   return RRG_OK;
 }
 

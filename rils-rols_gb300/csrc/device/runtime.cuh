@@ -16,6 +16,7 @@ struct DevBuf {
 struct HostBuf {
   void* ptr = nullptr;
   size_t cap = 0;
+  uint64_t used_in = 0;  // round sequence number of its last upload (0: none)
   bool reserve(size_t bytes);
   void release();
 };
@@ -71,6 +72,22 @@ struct rrg_context {
   // mixed scratch
   DevBuf d_terms, d_fallback, d_sse1, d_probe, d_nanrow, d_cert_e;
   HostBuf h_mlist, h_fallback;
+  // device-decided second half of a mixed round (residual-pass list, FP64
+  // re-scoring lane): its buffers, and the read-back of its statistics
+  DevBuf d_rlist2, d_fbpack, d_fbneed, d_fbcols, d_fbF64, d_fbcst, d_fbgram, d_fbblist, d_fbM, d_fbctr;
+  HostBuf h_fbpack, h_fbstat;
+  bool fbstat_pending = false;
+  int32_t fbstat_levels = 0;
+  double fbstat_rows = 0.0;
+  int32_t fbstat_d = 0;
+  bool async_rounds = true;  // mixed rounds decide their second half on the device
+  uint64_t round_seq = 0;    // rounds submitted on this context
+  // CUDA graph form of a round (rrg_context_set_graph)
+  bool graph_rounds = false;
+  bool capturing = false;            // the context stream is being captured: no host waits
+  bool last_graph = false;           // the last round ran as a graph
+  int64_t graph_fallbacks = 0;       // rounds that could not be captured
+  cudaGraphExec_t graph_exec = nullptr;
   // factor tables
   FactorTable ft;
   HostBuf h_ft, h_ftp, h_ft64;
@@ -87,6 +104,8 @@ struct rrg_context {
   int64_t launches = 0, last_launches = 0;
   // mixed-round statistics of the last round
   int64_t last_fallback = 0, last_plain_routed = 0, last_pass2 = 0, last_sentinel = 0;
+  int64_t last_distinct = 0;  // candidates scored after merging identical factor lists
+  bool last_tiled = false;    // the round solved by the tiled QR (within 1e-10 of the direct one)
   int64_t last_reasons[16] = {0};
   // certified bound on the relative fitness error of a mixed result; larger
   // bounds are re-scored by the FP64 path
@@ -130,8 +149,12 @@ struct rrg_context {
   // mixed round over the shared FP32 factor table; FP64 re-scoring of the
   // candidates it cannot decide
   rrg_status run_mixed(const rrg_dataset* ds, const std::vector<int32_t>& cands, bool certify);
+  // async: decide the residual-pass list and the FP64 re-scoring on the
+  // device (no read-back); returns with *async_done = false when this
+  // sub-round could not (then the re-scored candidates are in fb_all)
   rrg_status mixed_subround(const rrg_dataset* ds, const int32_t* list, int32_t cnt, const std::vector<int32_t>& lf,
-                            const std::vector<int32_t>& lid, bool certify, std::vector<int32_t>& fb_all);
+                            const std::vector<int32_t>& lid, bool certify, std::vector<int32_t>& fb_all,
+                            bool async, bool* async_done);
   // plain FP64 arithmetic over a shared FP64 factor table with the direct QR
   // per candidate (bit-identical to run_plain's direct QR)
   rrg_status run_fp64_table(const rrg_dataset* ds, const std::vector<int32_t>& list, uint32_t flags_or);
@@ -139,6 +162,7 @@ struct rrg_context {
   std::vector<int32_t> dup_of;
   void dedup_candidates(std::vector<int32_t>& reps);
   rrg_status submit(rrg_dataset* ds, const rrg_batch* b, int32_t precision, rrg_result* results, double* coefs);
+  rrg_status enqueue_round(rrg_dataset* ds, const rrg_batch* b, int32_t precision, int64_t n_coefs);
   rrg_status wait(int32_t timeout_ms);
   ~rrg_context();
 };

@@ -124,10 +124,10 @@ class Context:
                "one_pass", "cert", "other_nan")
 
     def last_round_stats(self) -> dict:
-        out = (C.c_int64 * 16)()
-        self.lib.rrg_last_round_stats(self.h, out, 16)
+        out = (C.c_int64 * 19)()
+        self.lib.rrg_last_round_stats(self.h, out, 19)
         d = {"launches": out[0], "plain_routed": out[1], "fp64_rescored": out[2], "residual_pass": out[3],
-             "qr_skipped_sentinel": out[15]}
+             "qr_skipped_sentinel": out[15], "distinct": out[16], "tiled_qr": bool(out[17]), "graph": bool(out[18])}
         d["rescore_reasons"] = {r: out[4 + i] for i, r in enumerate(self.REASONS) if out[4 + i]}
         return d
 
@@ -141,6 +141,17 @@ class Context:
         """Datasets with fewer rows run mixed-precision rounds in FP64 (default
         8192; 0 always takes the mixed form)."""
         check(self.lib.rrg_context_set_mixed_min_rows(self.h, int(rows)), "rrg_context_set_mixed_min_rows")
+
+    def set_async(self, on: bool = True) -> None:
+        """Mixed rounds decide their second half on the device (on, the
+        default) or read their flags back to the host twice (off); the same
+        results either way."""
+        check(self.lib.rrg_context_set_async(self.h, int(on)), "rrg_context_set_async")
+
+    def set_graph(self, on: bool = True) -> None:
+        """Run every round as a CUDA graph (rounds that cannot be captured are
+        launched directly); the same results either way."""
+        check(self.lib.rrg_context_set_graph(self.h, int(on)), "rrg_context_set_graph")
 
     def last_round_timing(self) -> dict:
         n = len(self.PHASES)

@@ -10,7 +10,7 @@ import numpy as np
 import pytest
 
 from rils_rols_gb300 import _lib, synth
-from rils_rols_gb300.fitness import PLAIN, Context, encode, result_dtype
+from rils_rols_gb300.fitness import CERTIFIED, PLAIN, Context, encode, result_dtype
 
 from conftest import GOLDEN
 
@@ -23,7 +23,7 @@ def rounds_1m():
     return trees
 
 
-@pytest.mark.parametrize("precision", [PLAIN])
+@pytest.mark.parametrize("precision", [PLAIN, CERTIFIED])
 def test_wait_times_out_then_completes(precision):
     X, y = synth.regression_1m()
     ctx = Context(0)
