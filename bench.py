@@ -532,13 +532,18 @@ def classifier_leg(args):
     for n, calls in ((569, 100000), (200_000, args.cls_fit_calls)):
         X, lab, _ = synth.classifier(n=n, d=30, seed=SEED)
         row = {"max_fit_calls": calls}
-        arms = [("plain_fp64", "plain", None), ("certified", "mixed", None)]
+        # the device FP64 fit with its rounds as CUDA graphs beside the
+        # directly launched one (same search, same model)
+        arms = [("plain_fp64", "plain", None, False), ("plain_fp64_graph", "plain", None, True),
+                ("certified", "mixed", None, False)]
         if n <= 5000:
             from oracle import pyoracle
-            arms.append(("cpu_oracle", "plain", pyoracle.backend_struct()))
-        for name, prec, backend in arms:
+            arms.append(("cpu_oracle", "plain", pyoracle.backend_struct(), False))
+        for name, prec, backend, graph in arms:
             m = rils_rols_cpp.rils_rols(True, calls, 1 << 30, 0.001, 20, 1.0, False, SEED % 100000)
             m.set_precision(prec)
+            if graph:
+                m.set_graph(True)
             if backend is not None:
                 m.set_backend(backend)
             t = time.perf_counter()
@@ -554,6 +559,7 @@ def classifier_leg(args):
         if "cpu_oracle" in row:
             row["device_fp64_equals_cpu"] = row["plain_fp64"]["model"] == row["cpu_oracle"]["model"]
         row["certified_equals_fp64"] = row["certified"]["model"] == row["plain_fp64"]["model"]
+        row["graph_equals_fp64"] = row["plain_fp64_graph"]["model"] == row["plain_fp64"]["model"]
         out[f"n={n}"] = row
     return out
 

@@ -280,6 +280,12 @@ rrg_status rrg_context_set_graph(rrg_context* ctx, int32_t on);
  * the mixed form.  No counterpart in the reference. */
 rrg_status rrg_context_set_mixed_min_rows(rrg_context* ctx, int64_t rows);
 
+/* Device bytes a context's scratch holds (the buffers only grow; datasets
+ * not included), or -1 for NULL.  For callers that keep a context across
+ * jobs and account its memory (the serving loop).  No counterpart in the
+ * reference. */
+int64_t rrg_context_memory(rrg_context* ctx);
+
 /* Free and total memory of a device (cudaMemGetInfo); RRG_E_NO_DEVICE without
  * one.  No counterpart in the reference. */
 rrg_status rrg_device_memory(int32_t device, int64_t* free_bytes, int64_t* total_bytes);

@@ -46,6 +46,10 @@ int32_t rrh_set_backend(rrh_model* m, const rrh_backend* be);
  * within 1e-6 relative of the FP64 path's: decisions agree except between
  * candidates whose fitness values lie that close) or RRG_MIXED. */
 int32_t rrh_set_precision(rrh_model* m, int32_t precision);
+/* Run the device backend's rounds as CUDA graphs (rrg_context_set_graph);
+ * off by default.  The same search and results either way.  No counterpart
+ * in the reference. */
+int32_t rrh_set_graph(rrh_model* m, int32_t on);
 
 /* fit(X, y, data_cnt, feat_cnt), X row-major n x d (rils_rols_cpp.cpp:717-728).
  * Returns RRG_OK or an rrg_status; never exits the process. */

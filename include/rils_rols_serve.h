@@ -10,9 +10,12 @@
  * on its own CUDA stream, so the rounds of the jobs in flight overlap on the
  * device (continuous batching at round granularity).  A job is admitted when
  * a slot is free and its device-memory footprint (dataset plus working
- * tables, sized from n and d) fits the server's budget; jobs wait in arrival
- * order otherwise.  A job's result does not depend on the other jobs: the
- * same search, on the same data, in the same arithmetic.
+ * tables, sized from n and d) fits the server's budget.  Jobs start in
+ * arrival order, except that when the head of the queue does not fit, a
+ * job among the next 16 that does fit may start first, at most 8 times past
+ * the same head.  A worker keeps its device context (and its scratch) from
+ * job to job.  A job's result does not depend on the other jobs: the same
+ * search, on the same data, in the same arithmetic.
  */
 #ifndef RILS_ROLS_SERVE_H
 #define RILS_ROLS_SERVE_H

@@ -45,16 +45,22 @@ bool cuda_ok(cudaError_t e, const char* what) {
 // ------------------------------------------------------------- buffers ----
 bool DevBuf::reserve(size_t bytes) {
   if (bytes <= cap) return true;
+  if (frozen && *frozen) return false;  // an allocation would become part of the captured graph
   if (ptr) {
-    cudaDeviceSynchronize();  // queued kernels may still use the old buffer
-    cudaFree(ptr);
+    if (st) {
+      cudaFreeAsync(ptr, st);  // after the queued kernels that may still use it
+    } else {
+      cudaDeviceSynchronize();  // queued kernels may still use the old buffer
+      cudaFree(ptr);
+    }
   }
   ptr = nullptr;
   cap = 0;
   size_t want = round_up((int64_t)bytes, 1 << 20);
-  if (cudaMalloc(&ptr, want) != cudaSuccess) {
+  auto alloc = [&](size_t b) { return (st ? cudaMallocAsync(&ptr, b, st) : cudaMalloc(&ptr, b)) == cudaSuccess; };
+  if (!alloc(want)) {
     cudaGetLastError();
-    if (cudaMalloc(&ptr, bytes) != cudaSuccess) {
+    if (!alloc(bytes)) {
       cudaGetLastError();
       ptr = nullptr;
       return false;
@@ -65,7 +71,10 @@ bool DevBuf::reserve(size_t bytes) {
   return true;
 }
 void DevBuf::release() {
-  if (ptr) cudaFree(ptr);
+  if (ptr) {
+    if (st) cudaFreeAsync(ptr, st);
+    else cudaFree(ptr);
+  }
   ptr = nullptr;
   cap = 0;
 }
@@ -590,31 +599,26 @@ rrg_status rrg_context::wait(int32_t timeout_ms) {
   return RRG_OK;
 }
 
+std::vector<DevBuf*> rrg_context::all_bufs() {
+  return {&d_batch, &d_A, &d_S, &d_pc, &d_partial, &d_list, &d_redo, &d_terms, &d_fallback, &d_sse1, &d_probe,
+          &d_nanrow, &d_cert_e, &d_ft, &d_ftp, &d_ft64, &d_F, &d_P, &d_Pc, &d_psum, &d_fprobe, &d_fnan, &d_F64, &d_M,
+          &d_colstat, &d_gram, &d_rlist2, &d_fbpack, &d_fbneed, &d_fbcols, &d_fbF64, &d_fbcst, &d_fbgram, &d_fbblist,
+          &d_fbM, &d_fbctr, &d_res, &d_coefs, &d_status};
+}
+
+int64_t rrg_context::device_bytes() {
+  int64_t t = 0;
+  for (DevBuf* b : all_bufs()) t += (int64_t)b->cap;
+  return t;
+}
+
 rrg_context::~rrg_context() {
   if (in_flight) cudaEventSynchronize(done);
   if (graph_exec) cudaGraphExecDestroy(graph_exec);
-  d_batch.release();
-  d_A.release();
-  d_S.release();
-  d_pc.release();
-  d_partial.release();
-  d_res.release();
-  d_coefs.release();
-  d_status.release();
-  d_list.release();
-  d_redo.release();
-  d_terms.release();
-  d_fallback.release();
-  d_sse1.release();
-  d_probe.release();
-  d_nanrow.release();
-  d_cert_e.release();
+  for (DevBuf* bf : all_bufs()) bf->release();
   h_mlist.release();
   h_fallback.release();
-  for (DevBuf* bf : {&d_ft, &d_ftp, &d_ft64, &d_F, &d_P, &d_Pc, &d_psum, &d_fprobe, &d_fnan, &d_F64, &d_M, &d_colstat,
-                      &d_gram, &d_rlist2, &d_fbpack, &d_fbneed, &d_fbcols, &d_fbF64, &d_fbcst, &d_fbgram, &d_fbblist,
-                      &d_fbM, &d_fbctr})
-    bf->release();
+  h_list.release();
   h_fbpack.release();
   h_fbstat.release();
   h_ft.release();
@@ -685,16 +689,17 @@ rrg_status make_dataset(rrg_context* ctx, const double* y, int64_t n, int32_t d,
   const int64_t cols = std::max(d, 1);
   const size_t b64 = sizeof(double) * ds->n_pad * cols, b32 = sizeof(float) * ds->n_pad * cols;
   const size_t y64b = sizeof(double) * ds->n_pad, y32b = sizeof(float) * ds->n_pad;
-  if (cudaMalloc(&ds->X64, b64) != cudaSuccess || cudaMalloc(&ds->X32, b32) != cudaSuccess ||
-      cudaMalloc(&ds->X32lo, b32) != cudaSuccess ||
-      cudaMalloc(&ds->y64, y64b) != cudaSuccess || cudaMalloc(&ds->y32, y32b) != cudaSuccess ||
-      cudaMalloc(&ds->y32lo, y32b) != cudaSuccess) {
+  // stream-ordered on the context stream (no device-wide wait when a
+  // dataset comes or goes while other contexts' rounds run)
+  cudaStream_t st = ctx->stream;
+  auto alloc = [&](void** p, size_t b) { return cudaMallocAsync(p, b, st) == cudaSuccess; };
+  if (!alloc((void**)&ds->X64, b64) || !alloc((void**)&ds->X32, b32) || !alloc((void**)&ds->X32lo, b32) ||
+      !alloc((void**)&ds->y64, y64b) || !alloc((void**)&ds->y32, y32b) || !alloc((void**)&ds->y32lo, y32b)) {
     cudaGetLastError();
     rrg_dataset_destroy(ds);
     rrc::set_error("rrg_dataset_create: out of device memory");
     return RRG_E_OOM;
   }
-  cudaStream_t st = ctx->stream;
   bool ok = cudaMemsetAsync(ds->X64, 0, b64, st) == cudaSuccess && upload(ds, st) &&
             cudaMemcpyAsync(ds->y64, y, sizeof(double) * n, cudaMemcpyHostToDevice, st) == cudaSuccess &&
             cudaMemsetAsync(ds->y64 + n, 0, sizeof(double) * (ds->n_pad - n), st) == cudaSuccess &&
@@ -774,6 +779,20 @@ rrg_status rrg_context_create(int32_t device, rrg_context** out) {
     delete ctx;
     return RRG_E_CUDA;
   }
+  // scratch from the device's memory pool, ordered on the context stream:
+  // growing a buffer or freeing it never waits for the device (other
+  // contexts' rounds keep running); the pool keeps freed memory for reuse
+  // by this process instead of returning it at every synchronisation
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+    uint64_t keep = UINT64_MAX;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    for (DevBuf* b : ctx->all_bufs()) {
+      b->st = ctx->stream;
+      b->frozen = &ctx->capturing;
+    }
+  }
+  cudaGetLastError();
   *out = ctx;
   return RRG_OK;
 }
@@ -820,12 +839,12 @@ rrg_status rrg_dataset_destroy(rrg_dataset* ds) {
   if (!ds) return RRG_E_INVALID;
   if (ds->ctx) cudaSetDevice(ds->ctx->device);
   if (ds->ctx && ds->ctx->in_flight) cudaEventSynchronize(ds->ctx->done);
-  if (ds->X64) cudaFree(ds->X64);
-  if (ds->X32) cudaFree(ds->X32);
-  if (ds->X32lo) cudaFree(ds->X32lo);
-  if (ds->y64) cudaFree(ds->y64);
-  if (ds->y32) cudaFree(ds->y32);
-  if (ds->y32lo) cudaFree(ds->y32lo);
+  // freed behind the context stream's queued work (every round of this
+  // dataset ran on that stream or joined it)
+  cudaStream_t st = ds->ctx ? ds->ctx->stream : nullptr;
+  for (void* p : {(void*)ds->X64, (void*)ds->X32, (void*)ds->X32lo, (void*)ds->y64, (void*)ds->y32,
+                  (void*)ds->y32lo})
+    if (p) cudaFreeAsync(p, st);
   delete ds;
   return RRG_OK;
 }
@@ -909,6 +928,8 @@ rrg_status rrg_context_set_timing(rrg_context* ctx, int32_t on) {
   ctx->timing = on != 0;
   return RRG_OK;
 }
+
+int64_t rrg_context_memory(rrg_context* ctx) { return ctx ? ctx->device_bytes() : -1; }
 
 rrg_status rrg_context_set_graph(rrg_context* ctx, int32_t on) {
   if (!ctx) return RRG_E_INVALID;

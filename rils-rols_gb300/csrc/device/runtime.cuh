@@ -5,10 +5,16 @@
 
 #include "common.cuh"
 
-// Device allocation that only grows.
+// Device allocation that only grows.  With an owner stream, allocation and
+// release are stream-ordered (the device's memory pool, kept cached): the
+// old allocation is freed behind the work already queued on that stream and
+// nothing waits for the device; the owner's side streams only touch it
+// after forking from that stream.
 struct DevBuf {
   void* ptr = nullptr;
   size_t cap = 0;
+  cudaStream_t st = nullptr;      // owner stream (nullptr: plain cudaMalloc / cudaFree)
+  const bool* frozen = nullptr;   // while *frozen (a graph capture), growth is refused
   bool reserve(size_t bytes);
   void release();
 };
@@ -164,5 +170,7 @@ struct rrg_context {
   rrg_status submit(rrg_dataset* ds, const rrg_batch* b, int32_t precision, rrg_result* results, double* coefs);
   rrg_status enqueue_round(rrg_dataset* ds, const rrg_batch* b, int32_t precision, int64_t n_coefs);
   rrg_status wait(int32_t timeout_ms);
+  std::vector<DevBuf*> all_bufs();  // every device buffer the context owns
+  int64_t device_bytes();           // device memory they hold
   ~rrg_context();
 };

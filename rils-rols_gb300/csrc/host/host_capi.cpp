@@ -14,6 +14,7 @@
 struct rrh_model {
   rrh::Search search;
   rrg_context* ctx = nullptr;  // owned; created on first use of the device backend
+  bool graph = false;          // device rounds as CUDA graphs (rrh_set_graph)
   rrh_model(bool c, int mfc, int ms, double cp, int mc, double ss, bool v, int rs) : search(c, mfc, ms, cp, mc, ss, v, rs) {}
   ~rrh_model() {
     if (ctx) rrg_context_destroy(ctx);
@@ -25,7 +26,10 @@ namespace {
 // ---- default backend: the device path of include/rils_rols_gb300.h ----
 void* dev_dataset_create(void* self, const double* X, const double* y, int64_t n, int32_t d) {
   rrh_model* m = static_cast<rrh_model*>(self);
-  if (!m->ctx && rrg_context_create(0, &m->ctx) != RRG_OK) return nullptr;
+  if (!m->ctx) {
+    if (rrg_context_create(0, &m->ctx) != RRG_OK) return nullptr;
+    if (m->graph) rrg_context_set_graph(m->ctx, 1);
+  }
   rrg_dataset* ds = nullptr;
   if (rrg_dataset_create(m->ctx, X, y, n, d, &ds) != RRG_OK) return nullptr;
   return ds;
@@ -87,6 +91,12 @@ int32_t rrh_set_backend(rrh_model* m, const rrh_backend* be) {
   if (!m) return RRG_E_INVALID;
   m->search.set_backend(be ? *be : device_backend(m));
   return RRG_OK;
+}
+
+int32_t rrh_set_graph(rrh_model* m, int32_t on) {
+  if (!m) return RRG_E_INVALID;
+  m->graph = on != 0;
+  return m->ctx ? rrg_context_set_graph(m->ctx, on) : RRG_OK;
 }
 
 int32_t rrh_set_precision(rrh_model* m, int32_t p) {

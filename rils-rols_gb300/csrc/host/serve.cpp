@@ -1,14 +1,20 @@
-// Serving loop (include/rils_rols_serve.h): fit jobs admitted in arrival
-// order by device-memory footprint, each run as one search with its own
-// device context on its own streams.
+// Serving loop (include/rils_rols_serve.h): fit jobs admitted by
+// device-memory footprint, each run as one search on the device context of
+// its worker, on that context's streams.
 //
 // The workers are max_active threads.  A free worker takes the job at the
 // head of the queue once its footprint fits what the jobs in flight leave of
-// the budget; the head job blocks the ones behind it, so jobs start in
-// arrival order and a large job is not starved by small ones.  A job holds
-// its context (dataset, FP64 scratch, double-float factor table) from
-// admission to its model and releases it before its memory is returned to
-// the budget.
+// the budget.  When the head does not fit, one of the next kBypassWindow
+// jobs that does fit may start instead, but the head is passed over at most
+// kMaxBypass times: jobs start in arrival order within a window, and a large
+// job waits for a bounded number of smaller ones.
+//
+// A worker keeps its context from job to job (its scratch buffers only grow,
+// and come from the device's stream-ordered pool, so a job's start and end
+// cost no device-wide wait).  It is charged the larger of the job's
+// footprint and what its context already holds; a context holding more than
+// twice a new job's footprint is released first, so that one large job does
+// not pin its memory for every later small one.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -55,8 +61,12 @@ Footprint job_footprint(int64_t n, int64_t d) {
   return f;
 }
 
+constexpr int kBypassWindow = 16;  // queue positions a free worker looks at
+constexpr int kMaxBypass = 8;      // times the head of the queue may be passed over
+
 struct Job {
   int64_t id = 0;
+  int32_t bypassed = 0;  // jobs admitted ahead of it while it headed the queue
   rrs_job_params p{};
   int32_t n = 0, d = 0;
   std::vector<double> X, y;
@@ -69,26 +79,25 @@ struct Job {
   int64_t rounds = 0, candidates = 0;
 };
 
-// Device backend of one job: its own context, created on the server's device
-// with the job's scratch limits.
+// Device backend of one job: its worker's context (created on the server's
+// device when the worker has none), with the job's scratch limits.
 struct JobDevice {
   int32_t device;
   Footprint fp;
-  rrg_context* ctx = nullptr;
-  ~JobDevice() {
-    if (ctx) rrg_context_destroy(ctx);
-  }
+  rrg_context** ctx;  // the worker's context slot
 };
 void* jd_dataset_create(void* self, const double* X, const double* y, int64_t n, int32_t d) {
   JobDevice* j = static_cast<JobDevice*>(self);
-  if (!j->ctx) {
-    if (rrg_context_create(j->device, &j->ctx) != RRG_OK) return nullptr;
-    if (rrg_context_set_limits(j->ctx, j->fp.scratch, j->fp.table) != RRG_OK) return nullptr;
-  }
+  if (!*j->ctx && rrg_context_create(j->device, j->ctx) != RRG_OK) return nullptr;
+  if (rrg_context_set_limits(*j->ctx, j->fp.scratch, j->fp.table) != RRG_OK) return nullptr;
   rrg_dataset* ds = nullptr;
-  if (rrg_dataset_create(j->ctx, X, y, n, d, &ds) != RRG_OK) return nullptr;
+  if (rrg_dataset_create(*j->ctx, X, y, n, d, &ds) != RRG_OK) return nullptr;
   return ds;
 }
+
+// What a worker whose context holds `held` bytes is charged for a job of
+// footprint `fp`: a context more than twice the job's size is released first.
+int64_t charge_for(int64_t fp, int64_t held) { return held > 2 * fp ? fp : std::max(fp, held); }
 int32_t jd_eval(void* ds, const rrg_batch* b, int32_t p, rrg_result* r, double* c) {
   return rrg_eval(static_cast<rrg_dataset*>(ds), b, p, r, c);
 }
@@ -114,14 +123,27 @@ struct rrs_server {
   std::vector<std::thread> workers;
 
   void worker();
-  void run(Job& j);
+  void run(Job& j, rrg_context** ctx);
+  // the queue position a worker whose context holds `held` bytes may
+  // admit, or -1
+  int pick(int64_t held);
 };
 
-void rrs_server::run(Job& j) {
+int rrs_server::pick(int64_t held) {
+  const int w = (int)std::min<size_t>(queue.size(), kBypassWindow);
+  for (int i = 0; i < w; ++i) {
+    const Job& j = *jobs[queue[i]];
+    if (used + charge_for(j.fp.total, held) <= budget) return i;
+    if (i == 0 && j.bypassed >= kMaxBypass) return -1;  // the head waits for no more jobs
+  }
+  return -1;
+}
+
+void rrs_server::run(Job& j, rrg_context** ctx) {
   rrh::Search search(j.p.classification != 0, j.p.max_fit_calls, j.p.max_seconds, j.p.complexity_penalty,
                      j.p.max_complexity, j.p.sample_size, false, j.p.random_state);
   search.set_precision(j.p.precision);
-  JobDevice dev{device, j.fp};
+  JobDevice dev{device, j.fp, ctx};
   if (has_backend) {
     search.set_backend(backend);
   } else {
@@ -145,44 +167,56 @@ void rrs_server::run(Job& j) {
     j.error = e.what();
     j.state = RRS_FAILED;
   }
-  // the search's dataset is gone with `search`; the context goes with `dev`
+  // the search's dataset is gone with `search`; the context stays with the worker
 }
 
 void rrs_server::worker() {
+  rrg_context* ctx = nullptr;  // kept from job to job
+  int64_t held = 0;            // device bytes its scratch holds
   std::unique_lock<std::mutex> lk(mu);
   for (;;) {
+    int at = -1;
     cv_work.wait(lk, [&] {
       if (stopping) return true;
       if (queue.empty()) return false;
-      const Job& head = *jobs[queue.front()];
-      return used + head.fp.total <= budget;
+      at = pick(held);
+      return at >= 0;
     });
-    if (stopping) return;
-    Job& j = *jobs[queue.front()];
-    queue.pop_front();
-    used += j.fp.total;
+    if (stopping) break;
+    Job& j = *jobs[queue[at]];
+    if (at > 0) jobs[queue.front()]->bypassed += 1;
+    queue.erase(queue.begin() + at);
+    if (ctx && held > 2 * j.fp.total) {
+      // far larger than this job needs: its memory goes back first
+      rrg_context_destroy(ctx);
+      ctx = nullptr;
+      held = 0;
+    }
+    const int64_t charge = charge_for(j.fp.total, held);
+    used += charge;
     ++running;
     peak_running = std::max(peak_running, running);
     j.state = RRS_RUNNING;
     j.t_start = Clock::now();
     lk.unlock();
-    {
-      // the job's search and context live in this scope only
-      run(j);
-    }
+    run(j, &ctx);
+    const int64_t now_held = ctx ? rrg_context_memory(ctx) : 0;
     lk.lock();
     j.t_end = Clock::now();
     j.X.clear();
     j.X.shrink_to_fit();
     j.y.clear();
     j.y.shrink_to_fit();
-    used -= j.fp.total;
+    used -= charge;
+    held = std::max<int64_t>(now_held, 0);
     --running;
     t_last = j.t_end;
     any_done = true;
     cv_done.notify_all();
     cv_work.notify_all();
   }
+  lk.unlock();
+  if (ctx) rrg_context_destroy(ctx);
 }
 
 extern "C" {

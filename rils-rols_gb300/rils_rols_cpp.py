@@ -39,6 +39,10 @@ class rils_rols:  # noqa: N801 - name of the reference class
              "mixed_uncertified": RRG_MIXED}.get(precision, precision)
         _lib.check(self._lib.rrh_set_precision(self._h, int(p)), "rrh_set_precision")
 
+    def set_graph(self, on: bool = True) -> None:
+        """Run the device rounds as CUDA graphs (the same search and results)."""
+        _lib.check(self._lib.rrh_set_graph(self._h, int(bool(on))), "rrh_set_graph")
+
     def counters(self) -> dict:
         names = ["ls_calls", "main_it", "device_rounds", "candidates_scored", "skipped_perts", "total_perts",
                  "backend_ns"]

@@ -78,8 +78,8 @@ EXPORTS = [
     "rrg_dataset_cols", "rrg_last_round_launches", "rrg_last_round_stats", "rrg_context_stream",
     "rrg_context_set_timing", "rrg_last_round_timing", "rrg_last_round_bytes", "rrg_eval_plain_noalloc", "rrg_context_set_limits",
     "rrg_device_memory", "rrg_tune_set_mode", "rrg_tune_pin", "rrg_tune_reset", "rrg_tune_report",
-    "rrg_context_set_mixed_min_rows", "rrg_context_set_async", "rrg_context_set_graph",
-    "rrh_create", "rrh_destroy", "rrh_set_backend", "rrh_set_precision", "rrh_fit", "rrh_predict",
+    "rrg_context_set_mixed_min_rows", "rrg_context_set_async", "rrg_context_set_graph", "rrg_context_memory",
+    "rrh_create", "rrh_destroy", "rrh_set_backend", "rrh_set_precision", "rrh_set_graph", "rrh_fit", "rrh_predict",
     "rrh_model_string", "rrh_model_prefix", "rrh_best_time", "rrh_total_time", "rrh_fit_calls", "rrh_counter",
     "rrh_last_error", "rrh_candidates", "rrh_rewrite", "rrh_encode", "rrh_rebuild",
     "rrs_create", "rrs_destroy", "rrs_set_backend", "rrs_submit", "rrs_wait", "rrs_result", "rrs_stats_get",
@@ -121,6 +121,7 @@ def _declare(lib):
         "rrg_context_set_mixed_min_rows": (i32, [vp, i64]),
         "rrg_context_set_async": (i32, [vp, i32]),
         "rrg_context_set_graph": (i32, [vp, i32]),
+        "rrg_context_memory": (i64, [vp]),
         "rrg_tune_set_mode": (i32, [i32]),
         "rrg_tune_pin": (i32, [i32, i32, i32]),
         "rrg_tune_reset": (i32, []),
@@ -129,6 +130,7 @@ def _declare(lib):
         "rrh_destroy": (None, [vp]),
         "rrh_set_backend": (i32, [vp, P(Backend)]),
         "rrh_set_precision": (i32, [vp, i32]),
+        "rrh_set_graph": (i32, [vp, i32]),
         "rrh_fit": (i32, [vp, dp, dp, i32, i32]),
         "rrh_predict": (i32, [vp, dp, i32, i32, dp]),
         "rrh_model_string": (i32, [vp, cp, i32]),

@@ -91,3 +91,36 @@ def test_invalid_arguments(lib):
         with pytest.raises(ServeError):
             srv.result(12345)
     assert lib.rrs_set_backend(None, None) == _lib.RRG_E_INVALID
+
+
+def test_bounded_bypass_of_a_blocked_head():
+    # a budget for one large job and one small one: while the first large job
+    # runs, the second (the head of the queue) does not fit, and the small jobs
+    # behind it start first, but at most 8 of them pass it
+    import time
+    rng = np.random.default_rng(5)
+    XL = rng.uniform(-2, 2, (40_000, 1))
+    yL = np.sin(XL[:, 0]) + 0.5 * XL[:, 0]
+    XS = rng.uniform(-2, 2, (300, 1))
+    yS = XS[:, 0] ** 2 - XS[:, 0]
+    with Server(max_active=4, backend=pyoracle.backend_struct(), memory_budget=1 << 40) as srv:
+        fl = srv.info(srv.submit(XL, yL, max_fit_calls=50, max_seconds=1 << 30))["footprint_bytes"]
+        fs = srv.info(srv.submit(XS, yS, max_fit_calls=50, max_seconds=1 << 30))["footprint_bytes"]
+    assert fl > fs
+    with Server(max_active=4, backend=pyoracle.backend_struct(), memory_budget=fl + fs + (fl - fs) // 2) as srv:
+        t0 = time.perf_counter()
+        submitted = {}
+        l1 = srv.submit(XL, yL, max_fit_calls=3000, max_seconds=1 << 30, random_state=1)
+        submitted[l1] = time.perf_counter() - t0
+        l2 = srv.submit(XL, yL, max_fit_calls=200, max_seconds=1 << 30, random_state=2)
+        submitted[l2] = time.perf_counter() - t0
+        small = []
+        for s in range(12):
+            j = srv.submit(XS, yS, max_fit_calls=600, max_seconds=1 << 30, random_state=10 + s)
+            submitted[j] = time.perf_counter() - t0
+            small.append(j)
+        infos = {j: srv.result(j)[1] for j in [l1, l2] + small}
+    start = {j: submitted[j] + infos[j]["queued_s"] for j in infos}
+    ahead = sum(start[j] < start[l2] for j in small)
+    assert 1 <= ahead <= 8, ahead
+    assert all(i["state"] == "done" for i in infos.values())
