@@ -315,8 +315,18 @@ int32_t rrg_last_round_bytes(const rrg_context* ctx, double* bytes, int32_t n);
 
 /* Launch-shape tuner.  Only launch shapes that leave every result bit
  * unchanged are tuned: the warps per CTA of the FP64 QR by column bucket
- * (RRG_KNOB_QR_WARPS; buckets 4, 8, 16, 65 columns) and the FP64 evaluator's
- * blocks per level launch in SM waves (RRG_KNOB_EVAL_WAVES; bucket 0).  With
+ * (RRG_KNOB_QR_WARPS; buckets 4, 8, 16, 65 columns), the FP64 evaluator's
+ * blocks per level launch in SM waves (RRG_KNOB_EVAL_WAVES; bucket 0), and
+ * in mixed rounds the double-float evaluator's factors per block
+ * (RRG_KNOB_FAC_GROUP: 64, 32, 16; bucket 0) and the pair sums' partners per
+ * block (RRG_KNOB_PAIR_UNIT: 65536, 512, 128; bucket 0) -- every factor's
+ * values and every pair's sum are formed alone, whatever shares its block --
+ * and whether that evaluator reads X and y from global memory (1) or stages
+ * each block's rows of them in shared memory by tensor copies (2)
+ * (RRG_KNOB_FAC_STAGE; bucket: the feature count d, 1..64); and the warps
+ * per CTA of the QR of a mixed round's FP64 re-scoring, where few
+ * candidates make latency matter more than throughput
+ * (RRG_KNOB_QR_LIST_WARPS; buckets as RRG_KNOB_QR_WARPS).  With
  * RRG_TUNE_ON (the default) the first launch of a (knob, bucket, row class
  * floor(log2 n)) that carries enough work is timed in every shape, and the
  * fastest is kept for the process (and in the file named by the environment
@@ -326,6 +336,10 @@ int32_t rrg_last_round_bytes(const rrg_context* ctx, double* bytes, int32_t n);
 #define RRG_TUNE_ON 1
 #define RRG_KNOB_QR_WARPS 0
 #define RRG_KNOB_EVAL_WAVES 1
+#define RRG_KNOB_FAC_GROUP 2
+#define RRG_KNOB_PAIR_UNIT 3
+#define RRG_KNOB_FAC_STAGE 4
+#define RRG_KNOB_QR_LIST_WARPS 5
 rrg_status rrg_tune_set_mode(int32_t mode);
 /* Fix a knob's value in a bucket (value 0 releases it); RRG_E_INVALID for a
  * knob, bucket or value the kernels are not built for. */

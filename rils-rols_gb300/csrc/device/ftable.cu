@@ -240,13 +240,53 @@ constexpr size_t kFacRedOff = 128;                                   // [warp][6
 constexpr size_t kFacCodeOff = kFacRedOff + 256;
 constexpr size_t kFacStackOff = kFacCodeOff + sizeof(uint32_t) * kFacCodeSmem;
 constexpr size_t kFacXOff = kFacStackOff + sizeof(float4) * (kFacThreads / 32) * kMixedStackCap * 32 * 2;  // end
+// staged form: the copy barrier, then the staged rows (hi of every slot, lo
+// of every slot, y hi, y lo; `chunk` floats each)
+constexpr size_t kFacBarOff = kFacXOff;
+constexpr size_t kFacStageOff = kFacXOff + 128;
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t* m, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(m)), "r"(count) : "memory");
+}
+// the barrier's initialisation visible to the tensor-copy (async) proxy
+__device__ __forceinline__ void mbar_init_fence() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* m, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(m)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* m, uint32_t parity) {
+  uint32_t done;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(done)
+      : "r"(smem_addr(m)), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+// Waits for the barrier's phase `parity` to complete, at most `tries` times.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* m, uint32_t parity, int tries) {
+  for (int i = 0; i < tries; ++i)
+    if (mbar_try_wait(m, parity)) return true;
+  return false;
+}
+// Tensor copy of the box at (x, y) of `map` into dst, completing on m.
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y, uint64_t* m) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          smem_addr(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_addr(m))
+      : "memory");
+}
+constexpr int kStageWaitTries = 1 << 20;  // bounded wait for the staged rows
 
 }  // namespace
 
 // R = 4 rows per thread for short, shallow programs (one dispatch per op for
 // four rows), R = 2 for the others (less spill traffic per thread).
-template <int R>
-__global__ void __launch_bounds__(kFacThreads) fac_eval_kernel(FacEvalArgs a) {
+template <int R, bool STAGED>
+__global__ void __launch_bounds__(kFacThreads) fac_eval_kernel(const __grid_constant__ FacEvalArgs a) {
   extern __shared__ __align__(128) unsigned char smem[];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int2 grp = a.groups[blockIdx.x];
@@ -257,17 +297,73 @@ __global__ void __launch_bounds__(kFacThreads) fac_eval_kernel(FacEvalArgs a) {
   float* red = reinterpret_cast<float*>(smem + kFacRedOff);
   uint32_t* code_s = reinterpret_cast<uint32_t*>(smem + kFacCodeOff);
   float4* stk = reinterpret_cast<float4*>(smem + kFacStackOff);
-  // the group's programs are contiguous: stage them
+  const float* xh = a.ds.X32 + row0;
+  const float* xl = a.ds.X32lo + row0;
+  int64_t ldx = n_pad;
+  const float* yh = a.ds.y32 + row0;
+  const float* yl = a.ds.y32lo + row0;
+  int f0 = 0, nf = 0;
+  if constexpr (STAGED) {
+    // the chunk's rows of the group's features and of y into shared memory:
+    // one thread arms the barrier with the byte count and issues the tensor
+    // copies; every thread waits for them (a bounded wait)
+    f0 = a.gfeat_off[blockIdx.x];
+    nf = a.gfeat_off[blockIdx.x + 1] - f0;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + kFacBarOff);
+    float* stg = reinterpret_cast<float*>(smem + kFacStageOff);
+    if (tid == 0) {
+      mbar_init(bar, 1);
+      mbar_init_fence();
+    }
+    __syncthreads();
+    if (tid == 0) {
+      mbar_expect_tx(bar, (uint32_t)((2 * nf + 2) * rows * (int)sizeof(float)));
+      for (int b = 0; b < rows; b += kTmaRows) {
+        const int x = (int)(row0 + b);  // a multiple of kTmaRows: 16-byte aligned
+        for (int s = 0; s < nf; ++s) {
+          const int j = a.gfeat[f0 + s];
+          tma_load_2d(stg + (size_t)s * rows + b, &a.tm_xh, x, j, bar);
+          tma_load_2d(stg + (size_t)(nf + s) * rows + b, &a.tm_xl, x, j, bar);
+        }
+        tma_load_2d(stg + (size_t)(2 * nf) * rows + b, &a.tm_yh, x, 0, bar);
+        tma_load_2d(stg + (size_t)(2 * nf + 1) * rows + b, &a.tm_yl, x, 0, bar);
+      }
+    }
+    if (!mbar_wait_bounded(bar, 0, kStageWaitTries)) {
+      // the copies did not complete: report it, give them a second bounded
+      // wait (they write this block's shared memory) and leave
+      if (tid == 0) atomicOr(a.status, ST_WAIT_TIMEOUT);
+      mbar_wait_bounded(bar, 0, kStageWaitTries);
+      return;
+    }
+    xh = stg;
+    xl = stg + (size_t)nf * rows;
+    ldx = rows;
+    yh = stg + (size_t)(2 * nf) * rows;
+    yl = stg + (size_t)(2 * nf + 1) * rows;
+  }
+  // the group's programs are contiguous: stage them (staged form: feature
+  // operands renumbered to their shared-memory slots)
   const int base = a.meta[grp.x].x;
   const int2 last = a.meta[grp.x + grp.y - 1];
   const int total = last.x + last.y - base;
-  for (int i = tid; i < total; i += kFacThreads) code_s[i] = a.code[base + i];
+  for (int i = tid; i < total; i += kFacThreads) {
+    uint32_t w = a.code[base + i];
+    if constexpr (STAGED) {
+      const int op = (int)(w & 0xffu);
+      const bool feat = op == RRG_OP_LDV || op == RRG_OP_PSV ||
+                        (op >= RRG_OP_BIN && (((op - RRG_OP_BIN) & 7) >> 1) == RRG_SRC_V);
+      if (feat) {
+        const int j = (int)(w >> 8);
+        int slot = 0;
+        for (int s = 0; s < nf; ++s)
+          if (a.gfeat[f0 + s] == j) slot = s;
+        w = (w & 0xffu) | ((uint32_t)slot << 8);
+      }
+    }
+    code_s[i] = w;
+  }
   __syncthreads();
-  const float* xh = a.ds.X32 + row0;
-  const float* xl = a.ds.X32lo + row0;
-  const int64_t ldx = n_pad;
-  const float* yh = a.ds.y32 + row0;
-  const float* yl = a.ds.y32lo + row0;
   const float2* tb = a.F + row0;
   const bool tail = row0 + rows > n;  // the chunk holds padding rows (set to 0)
   float4* st = stk + (size_t)warp * kMixedStackCap * 32 * 2 + lane;
@@ -514,17 +610,70 @@ __device__ __forceinline__ void ftab_resid_item(const ResidArgs& a, int i, int q
 
 // ----------------------------------------------------------- launchers ----
 size_t fac_eval_smem() { return kFacXOff; }
+size_t fac_eval_smem_staged(int chunk, int slots) {
+  return kFacStageOff + sizeof(float) * (size_t)(2 * slots + 2) * (size_t)chunk;
+}
 bool fac_allow_smem() {
-  return cudaFuncSetAttribute(fac_eval_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) ==
+  const int big = 227 * 1024;
+  return cudaFuncSetAttribute(fac_eval_kernel<4, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, big) ==
              cudaSuccess &&
-         cudaFuncSetAttribute(fac_eval_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) ==
+         cudaFuncSetAttribute(fac_eval_kernel<2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, big) ==
+             cudaSuccess &&
+         cudaFuncSetAttribute(fac_eval_kernel<4, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, big) ==
+             cudaSuccess &&
+         cudaFuncSetAttribute(fac_eval_kernel<2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, big) ==
              cudaSuccess;
 }
+
+namespace {
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiledFn encode_tiled() {
+  static EncodeTiledFn fn = [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess) {
+      cudaGetLastError();
+      return (EncodeTiledFn) nullptr;
+    }
+    return reinterpret_cast<EncodeTiledFn>(p);
+  }();
+  return fn;
+}
+// a [rows_dim][n_pad] float array (rows of n_pad floats) as a 2D tensor with
+// boxes of kTmaRows x 1
+bool encode_2d(CUtensorMap* m, const float* base, int64_t n_pad, int64_t outer) {
+  EncodeTiledFn fn = encode_tiled();
+  if (!fn || !base || (reinterpret_cast<uintptr_t>(base) & 15) || (n_pad * 4) % 16 != 0) return false;
+  const cuuint64_t dims[2] = {(cuuint64_t)n_pad, (cuuint64_t)outer};
+  const cuuint64_t strides[1] = {(cuuint64_t)n_pad * sizeof(float)};
+  const cuuint32_t box[2] = {(cuuint32_t)kTmaRows, 1};
+  const cuuint32_t estr[2] = {1, 1};
+  return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims, strides, box, estr,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+}  // namespace
+
+bool fac_stage_maps(FacEvalArgs& a, const DevData& ds) {
+  return encode_2d(&a.tm_xh, ds.X32, ds.n_pad, std::max(ds.d, 1)) &&
+         encode_2d(&a.tm_xl, ds.X32lo, ds.n_pad, std::max(ds.d, 1)) && encode_2d(&a.tm_yh, ds.y32, ds.n_pad, 1) &&
+         encode_2d(&a.tm_yl, ds.y32lo, ds.n_pad, 1);
+}
+
 bool launch_fac_eval(const FacEvalArgs& a, int n_groups, int n_chunks, bool light, cudaStream_t st) {
   if (n_groups <= 0 || n_chunks <= 0) return true;
+  if (a.stage) {
+    const size_t sm = fac_eval_smem_staged(a.chunk, a.stage_slots);
+    if (light) fac_eval_kernel<4, true><<<dim3(n_groups, n_chunks), kFacThreads, sm, st>>>(a);
+    else fac_eval_kernel<2, true><<<dim3(n_groups, n_chunks), kFacThreads, sm, st>>>(a);
+    return launch_ok("launch_fac_eval");
+  }
   const size_t sm = fac_eval_smem();
-  if (light) fac_eval_kernel<4><<<dim3(n_groups, n_chunks), kFacThreads, sm, st>>>(a);
-  else fac_eval_kernel<2><<<dim3(n_groups, n_chunks), kFacThreads, sm, st>>>(a);
+  if (light) fac_eval_kernel<4, false><<<dim3(n_groups, n_chunks), kFacThreads, sm, st>>>(a);
+  else fac_eval_kernel<2, false><<<dim3(n_groups, n_chunks), kFacThreads, sm, st>>>(a);
   return launch_ok("launch_fac_eval");
 }
 int pair_row_blocks(int64_t n_pad) { return (int)((n_pad + kPairRows - 1) / kPairRows); }

@@ -7,6 +7,8 @@
 // in double-float arithmetic (csrc/common/df32.h) into HBM, and each
 // distinct pair of factors is summed once.
 #pragma once
+#include <cuda.h>  // CUtensorMap: the tensor maps of the staged evaluator
+
 #include "common.cuh"
 #include "mixed.cuh"
 
@@ -34,6 +36,13 @@ constexpr int kPairRows = 4096;       // rows per pair-sum / residual block
 constexpr int kResidThreads = 256;
 
 
+// Staged evaluation (FacEvalArgs::stage): a block copies the rows of its
+// chunk of the features its group reads, and of y, into shared memory with
+// tensor copies (cp.async.bulk.tensor, boxes of kTmaRows rows of one
+// feature) and evaluates from there; the same arithmetic on the same rows.
+constexpr int kFacStageMax = 16;  // features one staged group may read
+constexpr int kTmaRows = 256;     // rows per tensor-copy box
+
 // Self pairs of factor f sit at pair index 3f (f*f), 3f+1 (f*1), 3f+2 (f*y);
 // cross pairs follow from 3 * n_factors.
 struct FacEvalArgs {
@@ -50,7 +59,20 @@ struct FacEvalArgs {
   int32_t n_pairs;
   unsigned long long* fnan;  // [f] first row with a NaN value
   uint32_t* status;
+  // staging: 0 reads X and y from global memory (L2); 1 stages them.  The
+  // features group g reads (of this launch's groups) are
+  // gfeat[gfeat_off[g] .. gfeat_off[g + 1]), at most stage_slots of them.
+  int32_t stage;
+  int32_t stage_slots;
+  const int32_t* gfeat_off;
+  const int32_t* gfeat;
+  CUtensorMap tm_xh, tm_xl, tm_yh, tm_yl;  // X hi / lo as [d][n_pad], y hi / lo as [1][n_pad]
 };
+// Shared memory of the staged evaluator for `slots` features of a chunk.
+size_t fac_eval_smem_staged(int chunk, int slots);
+// Encodes the four tensor maps of a dataset into a; false when the driver
+// offers no tensor-map encoder or the layout is not copyable.
+bool fac_stage_maps(FacEvalArgs& a, const DevData& ds);
 
 struct PairArgs {
   const float2* F;

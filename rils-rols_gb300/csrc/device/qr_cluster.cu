@@ -449,8 +449,15 @@ __global__ void __cluster_dims__(kQrCluster, 1, 1) __launch_bounds__(32 * W)
 // shared counter (*next, zero before the launch), each factorising in its own
 // working slot of slot_cols columns of M.  Same bits as the per-candidate
 // kernel: only the placement of the working columns differs.
+// Resident blocks the list form is compiled for: about the register
+// footprint of the per-candidate form (72 registers a thread; 64 at 16 warps).
+template <int W>
+struct ListMinBlocks {
+  static constexpr int value = W >= 16 ? 2 : 65536 / (32 * W * 72);
+};
+
 template <int KB, int W>
-__global__ void __cluster_dims__(kQrCluster, 1, 1) __launch_bounds__(32 * W)
+__global__ void __cluster_dims__(kQrCluster, 1, 1) __launch_bounds__(32 * W, ListMinBlocks<W>::value)
     plain_qr_cluster_list_kernel(DevBatch b, DevData ds, const PlainCand* pc, const int32_t* list,
                                  const int32_t* count, int32_t* next, const double* A, double* M, int slot_cols,
                                  double* coefs, rrg_result* res, uint32_t* status, const int32_t* colmap,

@@ -529,35 +529,71 @@ rrg_status rrg_context::mixed_subround(const rrg_dataset* ds, const int32_t* lis
       rrc::set_error("mixed round: a table program exceeds the evaluator's limits");
       return RRG_E_INVALID;
     }
-  // evaluator groups per level: consecutive columns of one rows-per-thread
-  // class whose programs fit the shared buffer; per level the light groups
-  // first, then the others
-  std::vector<int2> groups;
-  std::vector<int32_t> level_groups;  // groups of level L end at level_groups[L]
-  std::vector<int32_t> level_light;   // ... of which the first level_light[L] are light
-  for (size_t L = 0, c0 = 0; L < tp.level_end.size(); ++L) {
-    const int32_t c1 = tp.level_end[L];
-    std::vector<int2> heavy;
-    int32_t n_light = 0;
-    for (int32_t i = (int32_t)c0; i < c1;) {
-      const bool light = fac_light(tp.meta[i].y, tp.stack[i]);
-      int32_t j = i, words = 0;
-      while (j < c1 && j - i < kFacGroupMax && words + tp.meta[j].y <= kFacCodeSmem &&
-             fac_light(tp.meta[j].y, tp.stack[j]) == light)
-        words += tp.meta[j++].y;
-      if (light) {
-        groups.push_back(make_int2(i, j - i));
-        ++n_light;
-      } else {
-        heavy.push_back(make_int2(i, j - i));
+  // evaluator groups per level, of at most `gmax` factors: consecutive
+  // columns of one rows-per-thread class whose programs fit the shared
+  // buffer; per level the light groups first, then the others.  The group
+  // size is a launch shape only (each factor is evaluated and summed alone):
+  // the tuner's TK_FAC_GROUP.
+  struct GroupSet {
+    std::vector<int2> groups;
+    std::vector<int32_t> level_groups;  // groups of level L end at level_groups[L]
+    std::vector<int32_t> level_light;   // ... of which the first level_light[L] are light
+    std::vector<int32_t> feat_off{0};   // [group + 1]: the features each group reads (staged form)
+    std::vector<int32_t> feat;
+    int32_t slots = 0;                  // most features one group reads
+    size_t off = 0, off_foff = 0, off_feat = 0;
+  };
+  auto build_groups = [&](int gmax, GroupSet& gs) {
+    for (size_t L = 0, c0 = 0; L < tp.level_end.size(); ++L) {
+      const int32_t c1 = tp.level_end[L];
+      std::vector<int2> heavy;
+      int32_t n_light = 0;
+      for (int32_t i = (int32_t)c0; i < c1;) {
+        const bool light = fac_light(tp.meta[i].y, tp.stack[i]);
+        int32_t j = i, words = 0;
+        while (j < c1 && j - i < gmax && words + tp.meta[j].y <= kFacCodeSmem &&
+               fac_light(tp.meta[j].y, tp.stack[j]) == light)
+          words += tp.meta[j++].y;
+        if (light) {
+          gs.groups.push_back(make_int2(i, j - i));
+          ++n_light;
+        } else {
+          heavy.push_back(make_int2(i, j - i));
+        }
+        i = j;
       }
-      i = j;
+      gs.groups.insert(gs.groups.end(), heavy.begin(), heavy.end());
+      gs.level_light.push_back(n_light);
+      gs.level_groups.push_back((int32_t)gs.groups.size());
+      c0 = c1;
     }
-    groups.insert(groups.end(), heavy.begin(), heavy.end());
-    level_light.push_back(n_light);
-    level_groups.push_back((int32_t)groups.size());
-    c0 = c1;
-  }
+    // the features each group's programs read, ascending
+    std::vector<uint8_t> used(std::max(1, ds->d));
+    for (const int2& g : gs.groups) {
+      std::fill(used.begin(), used.end(), 0);
+      for (int32_t c = g.x; c < g.x + g.y; ++c)
+        for (int pc = 0; pc < tp.meta[c].y; ++pc) {
+          const uint32_t w = tp.code[tp.meta[c].x + pc];
+          const int op = (int)(w & 0xffu);
+          if (op == RRG_OP_LDV || op == RRG_OP_PSV || (op >= RRG_OP_BIN && (((op - RRG_OP_BIN) & 7) >> 1) == RRG_SRC_V))
+            used[w >> 8] = 1;
+        }
+      int32_t k = 0;
+      for (int32_t j = 0; j < ds->d; ++j)
+        if (used[j]) {
+          gs.feat.push_back(j);
+          ++k;
+        }
+      gs.slots = std::max(gs.slots, k);
+      gs.feat_off.push_back((int32_t)gs.feat.size());
+    }
+  };
+  bool gtrial = false;
+  int gvals[4] = {tune_pick(TK_FAC_GROUP, 0, ds->n, &gtrial), 0, 0, 0};
+  gtrial = gtrial && !capturing && (int64_t)ncol * ds->n >= kTuneMinWork;
+  const int ngv = gtrial ? tune_variants(TK_FAC_GROUP, 0, gvals) : 1;
+  std::vector<GroupSet> gsets(ngv);
+  for (int v = 0; v < ngv; ++v) build_groups(std::min(gvals[v], kFacGroupMax), gsets[v]);
   // row chunks of fac_chunk(d) rows (the self sums' partials are per chunk);
   // pair sums and the residual pass use kPairRows blocks
   const int32_t n_self = 3 * ncol;
@@ -577,7 +613,11 @@ rrg_status rrg_context::mixed_subround(const rrg_dataset* ds, const int32_t* lis
   Packer pkt;
   const size_t o_tcode = pkt.add(tp.code.data(), sizeof(uint32_t) * tp.code.size());
   const size_t o_tmeta = pkt.add(tp.meta.data(), sizeof(int2) * tp.meta.size());
-  const size_t o_groups = pkt.add(groups.data(), sizeof(int2) * groups.size());
+  for (GroupSet& gs : gsets) {
+    gs.off = pkt.add(gs.groups.data(), sizeof(int2) * gs.groups.size());
+    gs.off_foff = pkt.add(gs.feat_off.data(), sizeof(int32_t) * gs.feat_off.size());
+    gs.off_feat = pkt.add(gs.feat.data(), sizeof(int32_t) * std::max<size_t>(1, gs.feat.size()));
+  }
   rrg_status pst = pkt.send(h_ftp, d_ftp, stream, round_seq);
   if (pst != RRG_OK) return pst;
   float2* F = static_cast<float2*>(d_F.ptr);
@@ -599,19 +639,68 @@ rrg_status rrg_context::mixed_subround(const rrg_dataset* ds, const int32_t* lis
   fa.n_pairs = n_self;
   fa.fnan = fnan;
   fa.status = status;
+  fa.stage = 0;
+  fa.stage_slots = 0;
+  // X and y staged in shared memory by tensor copies (the tuner's
+  // TK_FAC_STAGE, per feature count): possible when every group's features
+  // and y fit the shared memory of one block and the tensor maps encode
+  const int stage_bucket = std::min(std::max(ds->d, 1), 64);
+  bool strial = false;
+  const bool stage_pick = tune_pick(TK_FAC_STAGE, stage_bucket, ds->n, &strial) == 2;
+  auto can_stage = [&](const GroupSet& gs) {
+    return chunk % kTmaRows == 0 && gs.slots <= kFacStageMax &&
+           fac_eval_smem_staged(chunk, gs.slots) <= (size_t)227 * 1024;
+  };
+  const bool maps_ok = fac_stage_maps(fa, dd);
   // one launch per level: a level reads the columns of the levels before it
-  for (size_t L = 0, g0 = 0; L < level_groups.size(); ++L) {
-    const int gl = (int)g0 + level_light[L];
-    fa.groups = pkt.at<const int2>(d_ftp, o_groups) + g0;
-    bool ok = launch_fac_eval(fa, gl - (int)g0, n_chunks, true, stream);
-    fa.groups = pkt.at<const int2>(d_ftp, o_groups) + gl;
-    ok = ok && launch_fac_eval(fa, level_groups[L] - gl, n_chunks, false, stream);
-    if (!ok) {
-      cuda_ok(cudaGetLastError(), "factor evaluation launch");
-      return RRG_E_CUDA;
+  auto eval_all = [&](const GroupSet& gs, bool stage) {
+    fa.stage = stage ? 1 : 0;
+    fa.stage_slots = gs.slots;
+    fa.gfeat = pkt.at<const int32_t>(d_ftp, gs.off_feat);
+    for (size_t L = 0, g0 = 0; L < gs.level_groups.size(); ++L) {
+      const int gl = (int)g0 + gs.level_light[L];
+      fa.groups = pkt.at<const int2>(d_ftp, gs.off) + g0;
+      fa.gfeat_off = pkt.at<const int32_t>(d_ftp, gs.off_foff) + g0;
+      bool ok = launch_fac_eval(fa, gl - (int)g0, n_chunks, true, stream);
+      fa.groups = pkt.at<const int2>(d_ftp, gs.off) + gl;
+      fa.gfeat_off = pkt.at<const int32_t>(d_ftp, gs.off_foff) + gl;
+      ok = ok && launch_fac_eval(fa, gs.level_groups[L] - gl, n_chunks, false, stream);
+      if (!ok) return false;
+      launches += (gl > (int)g0) + (gs.level_groups[L] > gl);
+      g0 = gs.level_groups[L];
     }
-    launches += (gl > (int)g0) + (level_groups[L] > gl);
-    g0 = level_groups[L];
+    return true;
+  };
+  int gbest = 0;  // the group set in use
+  if (gtrial) {
+    // the first round of this row class: every group size timed on the
+    // real launches (a repeat rewrites the same columns and sums)
+    float ms[4];
+    for (int v = 0; v < ngv; ++v) {
+      bool ok = true;
+      const bool st = stage_pick && maps_ok && can_stage(gsets[v]);
+      const rrg_status ts = time_trial([&] { ok = eval_all(gsets[v], st); }, ms[v]);
+      if (!ok) return RRG_E_CUDA;
+      if (ts != RRG_OK) return ts;
+      if (ms[v] < ms[gbest]) gbest = v;
+    }
+    tune_store(TK_FAC_GROUP, 0, ds->n, gvals, ms, ngv);
+  }
+  const bool stage_ok = maps_ok && can_stage(gsets[gbest]);
+  if (strial && !capturing && stage_ok && (int64_t)ncol * ds->n >= kTuneMinWork) {
+    // the first round of this feature count: reading X from global memory
+    // and staging it, both timed on the real launches
+    int vals[2] = {1, 2};
+    float ms[2];
+    for (int v = 0; v < 2; ++v) {
+      bool ok = true;
+      const rrg_status ts = time_trial([&] { ok = eval_all(gsets[gbest], vals[v] == 2); }, ms[v]);
+      if (!ok) return RRG_E_CUDA;
+      if (ts != RRG_OK) return ts;
+    }
+    tune_store(TK_FAC_STAGE, stage_bucket, ds->n, vals, ms, 2);
+  } else if (!gtrial && !eval_all(gsets[0], stage_pick && stage_ok)) {
+    return RRG_E_CUDA;
   }
   // pair map over table columns: self pairs 3t..3t+2, cross pairs oriented
   // so that `a` is the rarer factor (its partners are then the widely shared
@@ -664,14 +753,23 @@ rrg_status rrg_context::mixed_subround(const rrg_dataset* ds, const int32_t* lis
   }
   for (int32_t& p : pair_of)
     if (p <= -2) p = n_self + rank[-2 - p];
-  std::vector<int4> units;
-  for (int32_t k = 0; k < n_cross;) {
-    const int32_t a = cross[order[k]].first;
-    int32_t e = k;
-    while (e < n_cross && cross[order[e]].first == a) ++e;
-    units.push_back(make_int4(a, k, e, 0));
-    k = e;
-  }
+  // units of at most `maxp` partners (a launch shape only: each pair's sum
+  // is formed alone; the tuner's TK_PAIR_UNIT)
+  auto build_units = [&](int maxp, std::vector<int4>& units) {
+    for (int32_t k = 0; k < n_cross;) {
+      const int32_t a = cross[order[k]].first;
+      int32_t e = k;
+      while (e < n_cross && cross[order[e]].first == a) ++e;
+      for (int32_t s0 = k; s0 < e; s0 += maxp) units.push_back(make_int4(a, s0, std::min(e, s0 + maxp), 0));
+      k = e;
+    }
+  };
+  bool ptrial = false;
+  int pvals[4] = {tune_pick(TK_PAIR_UNIT, 0, ds->n, &ptrial), 0, 0, 0};
+  ptrial = ptrial && !capturing && (int64_t)n_cross * ds->n >= kTuneMinWork;
+  const int npv = ptrial ? tune_variants(TK_PAIR_UNIT, 0, pvals) : 1;
+  std::vector<std::vector<int4>> usets(npv);
+  for (int v = 0; v < npv; ++v) build_units(pvals[v], usets[v]);
   const int32_t n_pairs = n_self + n_cross;
   if (!d_Pc.reserve(sizeof(float2) * (size_t)n_super * std::max(1, n_cross)) ||
       !d_psum.reserve(sizeof(double) * std::max(1, n_pairs)) || !d_fprobe.reserve(sizeof(FacProbe) * nfl)) {
@@ -683,7 +781,8 @@ rrg_status rrg_context::mixed_subround(const rrg_dataset* ds, const int32_t* lis
   const size_t o_meta = pk.add(lmeta.data(), sizeof(int2) * lmeta.size());
   const size_t o_fcol = pk.add(tp.fcol.data(), sizeof(int32_t) * tp.fcol.size());
   const size_t o_ccol = pk.add(cand_col.data(), sizeof(int32_t) * cand_col.size());
-  const size_t o_units = pk.add(units.data(), sizeof(int4) * units.size());
+  std::vector<size_t> o_units(npv);
+  for (int v = 0; v < npv; ++v) o_units[v] = pk.add(usets[v].data(), sizeof(int4) * usets[v].size());
   const size_t o_partner = pk.add(partner.data(), sizeof(int32_t) * partner.size());
   const size_t o_pair = pk.add(pair_of.data(), sizeof(int32_t) * pair_of.size());
   const size_t o_list = pk.add(list, sizeof(int32_t) * cnt);
@@ -712,14 +811,27 @@ rrg_status rrg_context::mixed_subround(const rrg_dataset* ds, const int32_t* lis
   PairArgs pa;
   pa.F = F;
   pa.n_pad = ds->n_pad;
-  pa.units = pk.at<const int4>(d_ft, o_units);
-  pa.n_units = (int32_t)units.size();
   pa.partner = pk.at<const int32_t>(d_ft, o_partner);
   pa.P = Pcross;
   pa.n_pairs = n_cross;
   pa.cross0 = 0;
-  if (!launch_pair_sum(pa, n_super, stream)) {
-    cuda_ok(cudaGetLastError(), "pair sum launch");
+  auto pair_all = [&](int v) {
+    pa.units = pk.at<const int4>(d_ft, o_units[v]);
+    pa.n_units = (int32_t)usets[v].size();
+    return launch_pair_sum(pa, n_super, stream);
+  };
+  if (ptrial) {
+    // every unit size timed on the real launch (a repeat rewrites the same sums)
+    float ms[4];
+    for (int v = 0; v < npv; ++v) {
+      bool ok = true;
+      const rrg_status ts = time_trial([&] { ok = pair_all(v); }, ms[v]);
+      if (!ok) return RRG_E_CUDA;
+      if (ts != RRG_OK) return ts;
+      ++launches;
+    }
+    tune_store(TK_PAIR_UNIT, 0, ds->n, pvals, ms, npv);
+  } else if (!pair_all(0)) {
     return RRG_E_CUDA;
   }
   mark_end(P_PAIRS, t0);
@@ -785,7 +897,7 @@ rrg_status rrg_context::mixed_subround(const rrg_dataset* ds, const int32_t* lis
     for (int q = 0; q < kQrBuckets; ++q) {
       if (!bucket_cap[q]) continue;
       bool trial = false;
-      qwarps[q] = tune_pick(TK_QR_WARPS, kBucketCols[q], ds->n, &trial);
+      qwarps[q] = tune_pick(TK_QR_LIST_WARPS, kBucketCols[q], ds->n, &trial);
       int occ = qr_cluster_list_clusters(kBucketCols[q], qwarps[q]);
       if (occ <= 0) occ = std::max(1, sm_count / 8);
       nclus[q] = std::min(bucket_cap[q], occ);
@@ -994,7 +1106,7 @@ rrg_status rrg_context::mixed_subround(const rrg_dataset* ds, const int32_t* lis
         for (int q = 0; q < kQrBuckets; ++q) {
           if (!nclus[q] || capturing) continue;
           bool tr = false;
-          tune_pick(TK_QR_WARPS, kBucketCols[q], ds->n, &tr);
+          tune_pick(TK_QR_LIST_WARPS, kBucketCols[q], ds->n, &tr);
           qtrial[q] = tr;
           any = any || tr;
         }
@@ -1009,7 +1121,7 @@ rrg_status rrg_context::mixed_subround(const rrg_dataset* ds, const int32_t* lis
             if (!qtrial[q] || (int64_t)hb[q] * ds->n < kTuneMinWork) continue;
             int vals[4];
             float ms[4];
-            const int nv = tune_variants(TK_QR_WARPS, kBucketCols[q], vals);
+            const int nv = tune_variants(TK_QR_LIST_WARPS, kBucketCols[q], vals);
             for (int v = 0; v < nv; ++v) {
               const int nc = std::min(nclus[q], std::max(1, qr_cluster_list_clusters(kBucketCols[q], vals[v])));
               bool ok = true;
@@ -1023,9 +1135,9 @@ rrg_status rrg_context::mixed_subround(const rrg_dataset* ds, const int32_t* lis
               if (ts != RRG_OK) return ts;
               launches += 1;
             }
-            tune_store(TK_QR_WARPS, kBucketCols[q], ds->n, vals, ms, nv);
+            tune_store(TK_QR_LIST_WARPS, kBucketCols[q], ds->n, vals, ms, nv);
             bool tr = false;
-            qwarps[q] = tune_pick(TK_QR_WARPS, kBucketCols[q], ds->n, &tr);
+            qwarps[q] = tune_pick(TK_QR_LIST_WARPS, kBucketCols[q], ds->n, &tr);
             nclus[q] = std::min(nclus[q], std::max(1, qr_cluster_list_clusters(kBucketCols[q], qwarps[q])));
           }
           RRG_CUDA(cudaMemsetAsync(qnext, 0, sizeof(int32_t) * kQrBuckets, stream));

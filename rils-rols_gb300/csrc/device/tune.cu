@@ -82,18 +82,50 @@ void save_locked(const Tuner& t) {
   std::rename(tmp.c_str(), path);
 }
 
-const char* knob_name(int knob) { return knob == TK_QR_WARPS ? "qr_warps" : "eval_waves"; }
+const char* knob_name(int knob) {
+  switch (knob) {
+    case TK_QR_WARPS: return "qr_warps";
+    case TK_EVAL_WAVES: return "eval_waves";
+    case TK_FAC_GROUP: return "fac_group";
+    case TK_PAIR_UNIT: return "pair_unit";
+    case TK_FAC_STAGE: return "fac_stage";
+    default: return "qr_list_warps";
+  }
+}
 
 }  // namespace
 
 int tune_variants(int knob, int bucket, int* out) {
   if (knob == TK_QR_WARPS) return qr_warp_variants(bucket, out);
+  if (knob == TK_QR_LIST_WARPS) {
+    // the same shapes, the widest first (few candidates: latency)
+    const int nv = qr_warp_variants(bucket, out);
+    std::sort(out, out + nv, [](int x, int y) { return x > y; });
+    return nv;
+  }
   if (knob == TK_EVAL_WAVES && bucket == 0) {
     out[0] = 4;
     out[1] = 2;
     out[2] = 8;
     out[3] = 16;
     return 4;
+  }
+  if (knob == TK_FAC_GROUP && bucket == 0) {
+    out[0] = 64;
+    out[1] = 32;
+    out[2] = 16;
+    return 3;
+  }
+  if (knob == TK_FAC_STAGE && bucket >= 1 && bucket <= 64) {
+    out[0] = 1;  // X and y read from global memory (L2) (the first shape)
+    out[1] = 2;  // staged in shared memory by tensor copies
+    return 2;
+  }
+  if (knob == TK_PAIR_UNIT && bucket == 0) {
+    out[0] = 1 << 16;  // a factor's whole partner list in one block (the first shape)
+    out[1] = 512;
+    out[2] = 128;
+    return 3;
   }
   return 0;
 }

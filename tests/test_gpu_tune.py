@@ -1,13 +1,15 @@
 """Launch-shape tuner on the device: every shape of a knob (warps per CTA of
-the FP64 QR by column bucket, FP64 evaluator waves) gives the same bits, and
-the tuner times every shape once per (knob, bucket, row class) and keeps the
-fastest."""
+the FP64 QR by column bucket, FP64 evaluator waves, and in mixed rounds the
+double-float evaluator's factors per block, whether it stages X and y in
+shared memory by tensor copies, and the pair sums' partners per block)
+gives the same bits, and the tuner times every shape once per (knob,
+bucket, row class) and keeps the fastest."""
 import numpy as np
 import pytest
 
 from oracle import pyoracle
-from rils_rols_gb300.fitness import (CERTIFIED, EVAL_WAVES, PLAIN, QR_WARPS, Context, encode, tune_mode, tune_pin,
-                                     tune_report, tune_reset)
+from rils_rols_gb300.fitness import (CERTIFIED, EVAL_WAVES, FAC_GROUP, FAC_STAGE, MIXED, PAIR_UNIT, PLAIN, QR_WARPS,
+                                     Context, encode, tune_mode, tune_pin, tune_report, tune_reset)
 
 pytestmark = pytest.mark.gpu
 
@@ -110,5 +112,44 @@ def test_tuner_times_every_shape_once(data):
         assert np.array_equal(cert["size"], ref["size"])
     finally:
         tune_reset()
+        ds.close()
+        ctx.close()
+
+
+def test_mixed_path_shapes_give_the_same_bits(data):
+    X, y, trees = data
+    ctx = Context(0)
+    ds = ctx.dataset(X, y)
+    batch = encode(trees, tuned=True)
+    try:
+        tune_mode(False)
+        for prec in (MIXED, CERTIFIED):
+            ref = ds.evaluate(batch, prec)
+            for g in (64, 32, 16):
+                tune_pin(FAC_GROUP, 0, g)
+                same(ds.evaluate(batch, prec), ref)
+            tune_pin(FAC_GROUP, 0, 0)
+            for u in (1 << 16, 512, 128):
+                tune_pin(PAIR_UNIT, 0, u)
+                same(ds.evaluate(batch, prec), ref)
+            tune_pin(PAIR_UNIT, 0, 0)
+            # X and y staged in shared memory by tensor copies, or read from L2
+            for st in (2, 1):
+                tune_pin(FAC_STAGE, X.shape[1], st)
+                same(ds.evaluate(batch, prec), ref)
+            tune_pin(FAC_STAGE, X.shape[1], 0)
+        # with the tuner on, the first mixed round times both knobs' shapes
+        # on its real launches and the results stay the same
+        tune_reset()
+        tune_mode(True)
+        same(ds.evaluate(batch, CERTIFIED), ref)
+        rep = {e["knob"]: e for e in tune_report()}
+        assert set(rep["fac_group"]["ms"]) == {64, 32, 16}
+        assert set(rep["pair_unit"]["ms"]) == {1 << 16, 512, 128}
+        assert rep["pair_unit"]["ms"][rep["pair_unit"]["value"]] == min(rep["pair_unit"]["ms"].values())
+        assert set(rep["fac_stage"]["ms"]) == {1, 2} and rep["fac_stage"]["bucket"] == X.shape[1]
+    finally:
+        tune_reset()
+        tune_mode(True)
         ds.close()
         ctx.close()
