@@ -136,7 +136,11 @@ int32_t rrg_abi_version(void);
 /* Text of the last error on this thread (never NULL). */
 const char* rrg_last_error(void);
 
-/* One context per device: owns a stream, pinned staging and scratch arenas. */
+/* One context per device: owns a stream, pinned staging and scratch arenas.
+ * Destroying a context also releases the device memory of the datasets
+ * created on it; their handles stay valid for rrg_dataset_destroy only (any
+ * other call on them returns RRG_E_INVALID), so the two may be destroyed in
+ * either order (garbage-collected bindings cannot always choose). */
 rrg_status rrg_context_create(int32_t device, rrg_context** out);
 rrg_status rrg_context_destroy(rrg_context* ctx);
 

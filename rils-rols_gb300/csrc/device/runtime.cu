@@ -612,8 +612,33 @@ int64_t rrg_context::device_bytes() {
   return t;
 }
 
+namespace {
+
+// the dataset's device columns, freed in the order of `st`
+void release_dataset_memory(rrg_dataset* ds, cudaStream_t st) {
+  for (void** p : {(void**)&ds->X64, (void**)&ds->X32, (void**)&ds->X32lo, (void**)&ds->y64, (void**)&ds->y32,
+                   (void**)&ds->y32lo}) {
+    if (*p) cudaFreeAsync(*p, st);
+    *p = nullptr;
+  }
+}
+
+// a dataset whose context was destroyed first has no device data left
+bool detached_ok(const rrg_dataset* ds) {
+  if (ds->ctx) return true;
+  rrc::set_error("the dataset's context was destroyed");
+  return false;
+}
+
+}  // namespace
+
 rrg_context::~rrg_context() {
   if (in_flight) cudaEventSynchronize(done);
+  for (rrg_dataset* ds : datasets) {
+    release_dataset_memory(ds, stream);
+    ds->ctx = nullptr;
+  }
+  datasets.clear();
   if (graph_exec) cudaGraphExecDestroy(graph_exec);
   for (DevBuf* bf : all_bufs()) bf->release();
   h_mlist.release();
@@ -683,6 +708,7 @@ rrg_status make_dataset(rrg_context* ctx, const double* y, int64_t n, int32_t d,
   RRG_CUDA(cudaSetDevice(ctx->device));
   rrg_dataset* ds = new rrg_dataset();
   ds->ctx = ctx;
+  ctx->datasets.push_back(ds);
   ds->n = n;
   ds->d = d;
   ds->n_pad = round_up(n, 256);
@@ -837,14 +863,16 @@ rrg_status rrg_dataset_create_rows(rrg_context* ctx, const double* X_rows, const
 
 rrg_status rrg_dataset_destroy(rrg_dataset* ds) {
   if (!ds) return RRG_E_INVALID;
-  if (ds->ctx) cudaSetDevice(ds->ctx->device);
-  if (ds->ctx && ds->ctx->in_flight) cudaEventSynchronize(ds->ctx->done);
-  // freed behind the context stream's queued work (every round of this
-  // dataset ran on that stream or joined it)
-  cudaStream_t st = ds->ctx ? ds->ctx->stream : nullptr;
-  for (void* p : {(void*)ds->X64, (void*)ds->X32, (void*)ds->X32lo, (void*)ds->y64, (void*)ds->y32,
-                  (void*)ds->y32lo})
-    if (p) cudaFreeAsync(p, st);
+  rrg_context* ctx = ds->ctx;
+  if (ctx) {
+    cudaSetDevice(ctx->device);
+    if (ctx->in_flight) cudaEventSynchronize(ctx->done);
+    // freed behind the context stream's queued work (every round of this
+    // dataset ran on that stream or joined it)
+    release_dataset_memory(ds, ctx->stream);
+    auto it = std::find(ctx->datasets.begin(), ctx->datasets.end(), ds);
+    if (it != ctx->datasets.end()) ctx->datasets.erase(it);
+  }
   delete ds;
   return RRG_OK;
 }
@@ -852,6 +880,7 @@ rrg_status rrg_dataset_destroy(rrg_dataset* ds) {
 rrg_status rrg_round_submit(rrg_dataset* ds, const rrg_batch* batch, int32_t precision, rrg_result* results,
                             double* coefs) {
   if (!ds || !batch || (!results && batch->n_cand > 0)) return RRG_E_INVALID;
+  if (!detached_ok(ds)) return RRG_E_INVALID;
   return ds->ctx->submit(ds, batch, precision, results, coefs);
 }
 
@@ -868,6 +897,7 @@ rrg_status rrg_eval(rrg_dataset* ds, const rrg_batch* batch, int32_t precision, 
 
 rrg_status rrg_predict(rrg_dataset* ds, const rrg_batch* batch, double* values) {
   if (!ds || !batch || !values || batch->n_cand < 1) return RRG_E_INVALID;
+  if (!detached_ok(ds)) return RRG_E_INVALID;
   rrg_context* ctx = ds->ctx;
   if (ctx->in_flight) return RRG_E_INVALID;
   int64_t n_coefs = 0;

@@ -170,6 +170,10 @@ struct rrg_context {
   rrg_status submit(rrg_dataset* ds, const rrg_batch* b, int32_t precision, rrg_result* results, double* coefs);
   rrg_status enqueue_round(rrg_dataset* ds, const rrg_batch* b, int32_t precision, int64_t n_coefs);
   rrg_status wait(int32_t timeout_ms);
+  // datasets created on this context and not yet destroyed: destroying the
+  // context first releases their device memory and leaves their handles
+  // detached (rrg_dataset_destroy then only frees the handle)
+  std::vector<rrg_dataset*> datasets;
   std::vector<DevBuf*> all_bufs();  // every device buffer the context owns
   int64_t device_bytes();           // device memory they hold
   ~rrg_context();

@@ -67,3 +67,32 @@ def test_invalid_upload_arguments():
         assert lib.rrg_dataset_create_rows(ctx.h, y.ctypes.data_as(dp), y.ctypes.data_as(dp), 0, 1, C.byref(h)) != 0
     finally:
         ctx.close()
+
+
+def test_context_destroyed_before_its_datasets():
+    """Garbage collection may finalise a context before the datasets that
+    reference it (objects that die together are finalised in any order): the
+    context then releases their device memory, the handles only accept
+    rrg_dataset_destroy, and other calls on them fail cleanly."""
+    from rils_rols_gb300._lib import RRGError
+    rng = np.random.default_rng(11)
+    X = rng.uniform(-1, 1, (5000, 2))
+    y = X[:, 0] * 2.0 + X[:, 1]
+    ctx = Context(0)
+    ds_a = ctx.dataset(X, y)
+    ds_b = ctx.dataset(X, y)
+    batch = encode(["add x0 x1"], tuned=True)
+    ref = ds_a.evaluate(batch, PLAIN)
+    ds_b.close()  # the usual order for one of them
+    ctx.close()   # the other outlives its context
+    with pytest.raises(RRGError):
+        ds_a.evaluate(batch, PLAIN)
+    ds_a.close()
+    # a fresh context works as before
+    ctx2 = Context(0)
+    try:
+        ds = ctx2.dataset(X, y)
+        same(ds.evaluate(batch, PLAIN), ref)
+        ds.close()
+    finally:
+        ctx2.close()
