@@ -209,8 +209,7 @@ rrg_status rrg_predict(rrg_dataset* ds, const rrg_batch* batch, double* values);
  * device looks up the scratch address: make it before any stream capture
  * begins on that device.  Calls share the scratch, so calls that overlap on
  * a device race: serialise them.  Results equal rrg_eval(RRG_PLAIN_FP64) on
- * the same data when that call solves directly (n < 65536); above that
- * rrg_eval may solve by tiled QR, which agrees within 1e-10 relative.
+ * the same data bit for bit (the same QR in the same summation order).
  */
 rrg_status rrg_eval_plain_noalloc(const double* X_col, int64_t ld, const double* y, int64_t n, int32_t d,
                                   const rrg_batch* batch, rrg_result* result, double* coefs, void* stream);
@@ -238,12 +237,9 @@ int64_t rrg_last_round_launches(const rrg_context* ctx);
  *   candidates whose pivoted QR was not run: a non-finite column norm makes its
  *   outcome certainly all-NaN coefficients (the fitness sentinel).  [16]
  *   candidates scored after merging those with identical factor lists.
- *   [17] 1 when the round solved by the tiled QR (a plain round of fewer
- *   than twice as many distinct candidates as the device has SMs, on 65536
- *   rows or more): results within 1e-10 relative of the direct QR, same
- *   rank, size and sentinel; 0 when by the direct QR (bit-identical to the
- *   oracle).  [18] 1 when the last round ran as a CUDA graph
- *   (rrg_context_set_graph).
+ *   [17] 0 (formerly a tiled-QR flag: every round now solves by the direct
+ *   column-pivoted QR, bit-identical to the oracle).  [18] 1 when the last
+ *   round ran as a CUDA graph (rrg_context_set_graph).
  * Returns the count written. */
 int32_t rrg_last_round_stats(const rrg_context* ctx, int64_t* out, int32_t n);
 
@@ -318,19 +314,16 @@ int32_t rrg_last_round_timing(const rrg_context* ctx, double* ms, int64_t* launc
 int32_t rrg_last_round_bytes(const rrg_context* ctx, double* bytes, int32_t n);
 
 /* Launch-shape tuner.  Only launch shapes that leave every result bit
- * unchanged are tuned: the warps per CTA of the FP64 QR by column bucket
- * (RRG_KNOB_QR_WARPS; buckets 4, 8, 16, 65 columns), the FP64 evaluator's
- * blocks per level launch in SM waves (RRG_KNOB_EVAL_WAVES; bucket 0), and
- * in mixed rounds the double-float evaluator's factors per block
- * (RRG_KNOB_FAC_GROUP: 64, 32, 16; bucket 0) and the pair sums' partners per
- * block (RRG_KNOB_PAIR_UNIT: 65536, 512, 128; bucket 0) -- every factor's
- * values and every pair's sum are formed alone, whatever shares its block --
- * and whether that evaluator reads X and y from global memory (1) or stages
- * each block's rows of them in shared memory by tensor copies (2)
- * (RRG_KNOB_FAC_STAGE; bucket: the feature count d, 1..64); and the warps
- * per CTA of the QR of a mixed round's FP64 re-scoring, where few
- * candidates make latency matter more than throughput
- * (RRG_KNOB_QR_LIST_WARPS; buckets as RRG_KNOB_QR_WARPS).  With
+ * unchanged are tuned: the FP64 evaluator's blocks per level launch in SM
+ * waves (RRG_KNOB_EVAL_WAVES; bucket 0), and in mixed rounds the
+ * double-float evaluator's factors per block (RRG_KNOB_FAC_GROUP: 64, 32,
+ * 16; bucket 0) and the pair sums' partners per block (RRG_KNOB_PAIR_UNIT:
+ * 65536, 512, 128; bucket 0) -- every factor's values and every pair's sum
+ * are formed alone, whatever shares its block -- and whether that evaluator
+ * reads X and y from global memory (1) or stages each block's rows of them
+ * in shared memory by tensor copies (2) (RRG_KNOB_FAC_STAGE; bucket: the
+ * feature count d, 1..64).  Knobs 0 and 5 (the warps per CTA of an earlier
+ * cluster QR) are retired: the QR's passes have one shape.  With
  * RRG_TUNE_ON (the default) the first launch of a (knob, bucket, row class
  * floor(log2 n)) that carries enough work is timed in every shape, and the
  * fastest is kept for the process (and in the file named by the environment
@@ -338,12 +331,10 @@ int32_t rrg_last_round_bytes(const rrg_context* ctx, double* bytes, int32_t n);
  * No counterpart in the reference. */
 #define RRG_TUNE_OFF 0
 #define RRG_TUNE_ON 1
-#define RRG_KNOB_QR_WARPS 0
 #define RRG_KNOB_EVAL_WAVES 1
 #define RRG_KNOB_FAC_GROUP 2
 #define RRG_KNOB_PAIR_UNIT 3
 #define RRG_KNOB_FAC_STAGE 4
-#define RRG_KNOB_QR_LIST_WARPS 5
 rrg_status rrg_tune_set_mode(int32_t mode);
 /* Fix a knob's value in a bucket (value 0 releases it); RRG_E_INVALID for a
  * knob, bucket or value the kernels are not built for. */
@@ -351,7 +342,7 @@ rrg_status rrg_tune_pin(int32_t knob, int32_t bucket, int32_t value);
 /* Forget every tuned choice and pin. */
 rrg_status rrg_tune_reset(void);
 /* The tuner's choices as text, one line per (knob, bucket, row class) with the
- * timed shapes ("qr_warps bucket=8 row_class=19 value=4 ms=4:1.2,2:1.4,8:1.3"),
+ * timed shapes ("fac_group bucket=0 row_class=19 value=16 ms=64:2.5,32:2.3,16:2.1"),
  * then the pins.  Writes at most cap bytes (NUL-terminated) and returns the
  * size needed. */
 int64_t rrg_tune_report(char* buf, int64_t cap);

@@ -18,8 +18,9 @@
  *   (makeHouseholder) and :116-133 (applyHouseholderOnTheLeft).
  *
  * Reduction order (the one thing the vendored, incomplete Eigen cannot pin):
- * every sum, dot product and norm here follows the fixed RR256 order of
- * rils-rols_gb300/csrc/common/rr_sum.h (the order of a 256-thread block);
+ * every sum, dot product and norm here follows the fixed QSUM order of
+ * rils-rols_gb300/csrc/common/rr_sum.h (256 lanes by row index, chunks of
+ * RR_CHUNK rows at absolute row multiples, chunk totals in order);
  * products are accumulated, and the rank-1 updates applied, with fused
  * multiply-adds, as Eigen's vectorised kernels do in the reference's
  * -O3 -march=native build on FMA hardware.
@@ -68,7 +69,7 @@ static inline long rrq_lstsq(double* A, long lda, long rows, long cols,
     long k, j, i;
 
     for (k = 0; k < cols; ++k) {
-        norm_dir[k] = sqrt(rr_sumsq256(A + k * lda, 0, rows));
+        norm_dir[k] = sqrt(rr_qsumsq(A + k * lda, 0, rows));
         norm_upd[k] = norm_dir[k];
         permf[k] = (double)k;
     }
@@ -98,7 +99,7 @@ static inline long rrq_lstsq(double* A, long lda, long rows, long cols,
         /* Householder reflector of A[k:rows, k] */
         double* col = A + k * lda;
         const long m = rows - k;
-        const double tail_sq = (m == 1) ? 0.0 : rr_sumsq256(col, k + 1, rows);
+        const double tail_sq = (m == 1) ? 0.0 : rr_qsumsq(col, k + 1, rows);
         const double c0 = col[k];
         double tau, beta;
         if (tail_sq <= DBL_MIN) {
@@ -122,7 +123,7 @@ static inline long rrq_lstsq(double* A, long lda, long rows, long cols,
             } else if (tau != 0.0) {
                 for (j = k + 1; j < cols; ++j) {
                     double* cj = A + j * lda;
-                    double tmp = rr_dot256(col, cj, k + 1, rows);
+                    double tmp = rr_qdot(col, cj, k + 1, rows);
                     tmp += cj[k];
                     cj[k] -= tau * tmp;
                     for (i = k + 1; i < rows; ++i) cj[i] = RRQ_UPDATE(-(tau * col[i]), tmp, cj[i]);
@@ -139,7 +140,7 @@ static inline long rrq_lstsq(double* A, long lda, long rows, long cols,
                 const double ratio = norm_upd[j] / norm_dir[j];
                 const double temp2 = temp * (ratio * ratio);
                 if (temp2 <= downdate_thr) {
-                    norm_dir[j] = sqrt(rr_sumsq256(A + j * lda, k + 1, rows));
+                    norm_dir[j] = sqrt(rr_qsumsq(A + j * lda, k + 1, rows));
                     norm_upd[j] = norm_dir[j];
                 } else {
                     norm_upd[j] *= sqrt(temp);
@@ -160,7 +161,7 @@ static inline long rrq_lstsq(double* A, long lda, long rows, long cols,
         if (m == 1) {
             c[k] *= (1.0 - tau);
         } else if (tau != 0.0) {
-            double tmp = rr_dot256(v, c, k + 1, rows);
+            double tmp = rr_qdot(v, c, k + 1, rows);
             tmp += c[k];
             c[k] -= tau * tmp;
             for (i = k + 1; i < rows; ++i) c[i] = RRQ_UPDATE(-(tau * v[i]), tmp, c[i]);

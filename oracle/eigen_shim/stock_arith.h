@@ -48,6 +48,10 @@ static inline double rr_dot256(const double* a, const double* b, long start, lon
   }
   return s;
 }
+static inline double rr_qsumsq(const double* x, long start, long end) { return rr_sumsq256(x, start, end); }
+static inline double rr_qdot(const double* a, const double* b, long start, long end) {
+  return rr_dot256(a, b, start, end);
+}
 typedef struct {
   double total;
 } rr_csum_acc;

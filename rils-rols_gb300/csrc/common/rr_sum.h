@@ -9,6 +9,13 @@
  * across warps, so device and host results agree bit for bit.
  * CSUM: a whole column of n rows is summed as consecutive chunks of
  * RR_CHUNK rows, each by RR256, the chunk totals added in order from 0.
+ * QSUM (the sums of the column-pivoted QR): a row range [start, end) is cut
+ * at the absolute row multiples of RR_CHUNK; within a chunk, lane t takes
+ * the rows i with i mod 256 = t in increasing order, the lanes are folded as
+ * in RR256, and the chunk totals are added in order from 0.  A range from
+ * row 0 is summed exactly as CSUM sums it.  The fixed lane of every row and
+ * the independent chunks let a device spread one sum over as many blocks as
+ * the range has chunks.
  * Every sum, mean, dot product and norm of the plain FP64 path uses one of
  * these (host code must be built with -ffp-contract=off).  Dot products and
  * sums of squares accumulate each product with a fused multiply-add, as the
@@ -83,6 +90,35 @@ static inline double rr_csum_total(rr_csum_acc* a) {
     a->i = (a->i / RR_CHUNK + 1) * RR_CHUNK;
   }
   return a->total;
+}
+
+/* QSUM sum of squares and dot product over rows [start, end) */
+static inline double rr_qsumsq(const double* x, long start, long end) {
+  double total = 0.0;
+  for (long c0 = (start / RR_CHUNK) * RR_CHUNK; c0 < end; c0 += RR_CHUNK) {
+    const long lo = c0 > start ? c0 : start, hi = c0 + RR_CHUNK < end ? c0 + RR_CHUNK : end;
+    double p[RR_LANES] = {0};
+    for (long i = lo; i < hi; ++i) {
+      double* q = &p[i & (RR_LANES - 1)];
+      *q = fma(x[i], x[i], *q);
+    }
+    total = total + rrs_fold(p);
+  }
+  return total;
+}
+
+static inline double rr_qdot(const double* a, const double* b, long start, long end) {
+  double total = 0.0;
+  for (long c0 = (start / RR_CHUNK) * RR_CHUNK; c0 < end; c0 += RR_CHUNK) {
+    const long lo = c0 > start ? c0 : start, hi = c0 + RR_CHUNK < end ? c0 + RR_CHUNK : end;
+    double p[RR_LANES] = {0};
+    for (long i = lo; i < hi; ++i) {
+      double* q = &p[i & (RR_LANES - 1)];
+      *q = fma(a[i], b[i], *q);
+    }
+    total = total + rrs_fold(p);
+  }
+  return total;
 }
 
 static inline double rr_csum(const double* x, long n) {

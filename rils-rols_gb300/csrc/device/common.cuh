@@ -12,7 +12,8 @@ enum : uint32_t {
   ST_BAD_CODE = 0x1,       // unknown opcode or argument out of range
   ST_STACK = 0x2,          // spill stack over/underflow
   ST_WAIT_TIMEOUT = 0x4,   // a bounded mbarrier / flag wait ran out
-  ST_TOO_LARGE = 0x8       // candidate beyond the kernel's term limit
+  ST_TOO_LARGE = 0x8,      // candidate beyond the kernel's term limit
+  ST_QR_STATE = 0x10       // a QR pass found its state inconsistent (a bug, never data)
 };
 
 // Batch of one round, resident on the device.

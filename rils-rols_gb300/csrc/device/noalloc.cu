@@ -278,13 +278,12 @@ extern "C" rrg_status rrg_eval_plain_noalloc(const double* X_col, int64_t ld, co
   // the plain FP64 kernels (factor evaluation, direct column-pivoted QR,
   // residual, fitness), pointed at the scratch
   const int nb_eval = (int)std::min<int64_t>(1024, std::max<int64_t>(1, (n + 1023) / 1024));
-  plain_eval_kernel<<<dim3(nb_eval, 1), 256, plain_eval_smem(), st>>>(db, dd, dpc, nullptr, 0, arena, arena,
-                                                                       nullptr, 0, status, nullptr);
+  plain_eval_kernel<<<dim3(nb_eval, 1), 256, plain_eval_smem(), st>>>(db, dd, dpc, nullptr, 0, arena, status,
+                                                                       nullptr);
   if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail("factor evaluation launch", e);
   // launch_plain_qr reads (and so clears) the launch error itself: a failed
   // QR launch is only visible through its return value
-  if (!launch_plain_qr((int)k + 1, 1, st, db, dd, dpc, nullptr, 0, arena, arena, nullptr, 0, 1, cf, result, status,
-                       nullptr, nullptr))
+  if (!launch_plain_qr((int)k + 1, 1, st, db, dd, dpc, nullptr, 0, arena, arena, cf, result, status, nullptr))
     return cuda_fail("QR launch", cudaErrorLaunchFailure);
   plain_resid_kernel<<<dim3(nb_res, 1), 256, 0, st>>>(db, dd, dpc, nullptr, 0, arena, cf, partial, nullptr);
   finalize_kernel<<<1, 128, 0, st>>>(db, dd, nullptr, 0, 1, partial, nb_res, cf, result, 0u, nullptr);

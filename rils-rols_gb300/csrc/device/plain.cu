@@ -2,15 +2,13 @@
 // (rils_rols_cpp/rils_rols_cpp.cpp:445-541).
 //
 //   plain_eval   evaluates every factor program of a candidate on every row
-//                (node::evaluate_all, node.cpp:5-95) into the A arena and,
-//                for tall tiled (TSQR) rounds, reduces each row slice of
-//                [A | 1 | y] to a k x (k+1) triangle by Householder QR;
+//                (node::evaluate_all, node.cpp:5-95) into the A arena;
 //   plain_qr     column-pivoted Householder least squares with the pivot,
 //                rank and norm-down-dating rules of Eigen's
-//                ColPivHouseholderQR (eigen/Eigen/src/QR/ColPivHouseholderQR.h:482-608),
-//                on [A | 1 | y] directly (one slice) or on the stacked
-//                triangles (TSQR; the column norms, pivots and least-squares
-//                solution are those of A up to rounding);
+//                ColPivHouseholderQR (eigen/Eigen/src/QR/ColPivHouseholderQR.h:482-608)
+//                on [A | 1 | y], one block per candidate (small row counts
+//                and the allocation-free entry; qr_chunk.cu spreads larger
+//                ones over the GPU with the same bits);
 //   plain_resid  the rebuilt sum  sum_i c_i * f_i  with the drop / snap rules
 //                of rils_rols_cpp.cpp:488-517 and its squared residual;
 //   finalize     R2, RMSE and the NaN sentinel (rils_rols_cpp.cpp:40-49, 520-541).
@@ -108,75 +106,6 @@ __device__ __forceinline__ void run_row64(const uint32_t* code, int len, const d
   }
 }
 
-// Householder reflector of Q[kk.., kk] (Householder.h:67-96 semantics).
-// Returns tau; writes beta to Q[kk,kk] and the essential part below it.
-__device__ double make_householder(double* Q, int64_t ld, int64_t rows, int kk, double* red) {
-  double* col = Q + (int64_t)kk * ld;
-  double part = 0.0;
-  for (int64_t i = kk + 1 + threadIdx.x; i < rows; i += blockDim.x) part = __dadd_rn(part, __dmul_rn(col[i], col[i]));
-  const double tail_sq = (rows - kk == 1) ? 0.0 : block_sum(part, red);
-  const double c0 = col[kk];
-  double tau, beta;
-  __syncthreads();
-  if (tail_sq <= DBL_MIN) {
-    tau = 0.0;
-    beta = c0;
-    for (int64_t i = kk + 1 + threadIdx.x; i < rows; i += blockDim.x) col[i] = 0.0;
-  } else {
-    beta = __dsqrt_rn(__dadd_rn(__dmul_rn(c0, c0), tail_sq));
-    if (c0 >= 0.0) beta = -beta;
-    const double den = __dsub_rn(c0, beta);
-    for (int64_t i = kk + 1 + threadIdx.x; i < rows; i += blockDim.x) col[i] = __ddiv_rn(col[i], den);
-    tau = __ddiv_rn(__dsub_rn(beta, c0), beta);
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) col[kk] = beta;
-  __syncthreads();
-  return tau;
-}
-
-// Applies H_kk = I - tau v v^T (v = [1, Q[kk+1.., kk]]) to columns
-// [c_lo, c_hi) of Q (rows kk..rows-1).  Householder.h:116-133 semantics.
-__device__ void apply_householder(double* Q, int64_t ld, int64_t rows, int kk, double tau, int c_lo, int c_hi,
-                                  double* red, double* sh_tmp) {
-  const int cnt = c_hi - c_lo;
-  if (cnt <= 0) return;
-  if (rows - kk == 1) {
-    for (int j = threadIdx.x; j < cnt; j += blockDim.x) {
-      double* q = Q + (int64_t)(c_lo + j) * ld + kk;
-      *q = __dmul_rn(*q, __dsub_rn(1.0, tau));
-    }
-    __syncthreads();
-    return;
-  }
-  if (tau == 0.0) return;
-  const double* v = Q + (int64_t)kk * ld;
-  double part[kMaxK + 1];
-  for (int j = 0; j < cnt; ++j) part[j] = 0.0;
-  for (int64_t i = kk + 1 + threadIdx.x; i < rows; i += blockDim.x) {
-    const double vi = v[i];
-    for (int j = 0; j < cnt; ++j) part[j] = __dadd_rn(part[j], __dmul_rn(vi, Q[(int64_t)(c_lo + j) * ld + i]));
-  }
-  block_sum_vec(part, cnt, red, sh_tmp);
-  // tmp_j += Q[kk, j]; Q[kk, j] -= tau * tmp_j
-  if (threadIdx.x == 0) {
-    for (int j = 0; j < cnt; ++j) {
-      double* q = Q + (int64_t)(c_lo + j) * ld + kk;
-      sh_tmp[j] = __dadd_rn(sh_tmp[j], *q);
-      *q = __dsub_rn(*q, __dmul_rn(tau, sh_tmp[j]));
-    }
-  }
-  __syncthreads();
-  for (int64_t i = kk + 1 + threadIdx.x; i < rows; i += blockDim.x) {
-    const double tv = __dmul_rn(tau, v[i]);
-    for (int j = 0; j < cnt; ++j) {
-      double* q = Q + (int64_t)(c_lo + j) * ld + i;
-      *q = __dsub_rn(*q, __dmul_rn(tv, sh_tmp[j]));
-    }
-  }
-  __syncthreads();
-}
-
 // One-column table program on rows [r0, r1) of this block, written to Ac;
 // the column's statistics (NaN, infinite or overflowing square, non-trivial
 // tail, largest finite magnitude) merged into *cs.
@@ -242,8 +171,8 @@ __global__ void __launch_bounds__(256) table_eval_list_kernel(DevBatch b, DevDat
 
 // grid (blocks per candidate, candidates); rows of block b: [b*n/nb, (b+1)*n/nb)
 __global__ void __launch_bounds__(256) plain_eval_kernel(DevBatch b, DevData ds, const PlainCand* pc,
-                                                          const int32_t* list, int cand0, double* A, double* M,
-                                                          double* S, int tsqr, uint32_t* status, ColStat* cst) {
+                                                          const int32_t* list, int cand0, double* A, uint32_t* status,
+                                                          ColStat* cst) {
   extern __shared__ double smem[];
   const int c = list ? list[cand0 + blockIdx.y] : cand0 + blockIdx.y;
   const rrg_cand cd = b.cands[c];
@@ -263,60 +192,65 @@ __global__ void __launch_bounds__(256) plain_eval_kernel(DevBatch b, DevData ds,
   }
   for (int64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x)
     run_row64(code, cd.code_len, b.consts, ds, r, st, Ac, A, status);
-  if (!tsqr || cd.mode != RRG_TUNED) return;
-
-  // TSQR: [A | 1 | y] of this slice -> R (k x (k+1)) into S block blockIdx.x
-  const int k = pc[c].k;
-  double* Mc = M + pc[c].m_col * ds.n_pad;
-  for (int j = 0; j <= k; ++j)
-    for (int64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x)
-      Mc[(int64_t)j * ds.n_pad + r] = j < k - 1 ? Ac[(int64_t)j * ds.n_pad + r] : (j == k - 1 ? 1.0 : ds.y64[r]);
-  __syncthreads();
-  double* red = smem;  // reuse: (256/32) * (kMaxK+1) doubles
-  double* sh_tmp = smem + 8 * (kMaxK + 1);
-  double* Qs = Mc + r0;  // slice view, leading dimension n_pad
-  const int64_t rows = r1 - r0;
-  for (int kk = 0; kk < k; ++kk) {
-    const double tau = make_householder(Qs, ds.n_pad, rows, kk, red);
-    apply_householder(Qs, ds.n_pad, rows, kk, tau, kk + 1, k + 1, red, sh_tmp);
-  }
-  double* Sc = S + pc[c].s_off;
-  const int64_t ldS = (int64_t)nb * k;
-  for (int idx = threadIdx.x; idx < k * (k + 1); idx += blockDim.x) {
-    const int i = idx % k, j = idx / k;
-    Sc[(int64_t)j * ldS + (int64_t)blockIdx.x * k + i] = i <= j ? Qs[(int64_t)j * ds.n_pad + i] : 0.0;
-  }
 }
 
 namespace {
 
-// Element-wise block sums of part[0..cnt) (register arrays of KB entries).
-template <int KB>
-__device__ __forceinline__ void block_sum_vec_t(const double (&part)[KB], int cnt, double* red, double* out) {
-  const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
-  __syncthreads();
-#pragma unroll
-  for (int j = 0; j < KB; ++j)
-    if (j < cnt) {
-      const double v = warp_sum(part[j]);
-      if (l == 0) red[w * KB + j] = v;
-    }
-  __syncthreads();
-  for (int j = threadIdx.x; j < cnt; j += blockDim.x) {
-    double s = 0.0;
-    for (int i = 0; i < nw; ++i) s = __dadd_rn(s, red[i * KB + j]);
-    out[j] = s;
+// QSUM (csrc/common/rr_sum.h) of term(i, acc) over rows [start, rows) by the
+// block's 256 threads, thread t being lane t: per chunk of RR_CHUNK rows the
+// lanes' chains are folded as RR256, and the chunk totals are added in order
+// from 0.  Every thread gets the total.
+template <class F>
+__device__ __forceinline__ double block_qsum(int64_t start, int64_t rows, double* red, F&& term) {
+  double total = 0.0;
+  for (int64_t c0 = start / RR_CHUNK * RR_CHUNK; c0 < rows; c0 += RR_CHUNK) {
+    const int64_t hi = c0 + RR_CHUNK < rows ? c0 + RR_CHUNK : rows;
+    double p = 0.0;
+    for (int64_t i = c0 + threadIdx.x; i < hi; i += blockDim.x)
+      if (i >= start) p = term(i, p);
+    total = __dadd_rn(total, block_sum(p, red));
   }
-  __syncthreads();
+  return total;
 }
 
+// The same for cnt columns at once: term(i, part) adds row i's terms to
+// part[0 .. cnt); the totals land in tot[0 .. cnt) (shared).
+template <int KB, class F>
+__device__ __forceinline__ void block_qsum_vec(int64_t start, int64_t rows, int cnt, double* red, double* tmp,
+                                               double* tot, F&& term) {
+  for (int j = threadIdx.x; j < cnt; j += blockDim.x) tot[j] = 0.0;
+  __syncthreads();
+  for (int64_t c0 = start / RR_CHUNK * RR_CHUNK; c0 < rows; c0 += RR_CHUNK) {
+    const int64_t hi = c0 + RR_CHUNK < rows ? c0 + RR_CHUNK : rows;
+    double part[KB];
+#pragma unroll
+    for (int j = 0; j < KB; ++j) part[j] = 0.0;
+    for (int64_t i = c0 + threadIdx.x; i < hi; i += blockDim.x)
+      if (i >= start) term(i, part);
+    // element-wise block fold (warps, then the eight warp totals in order)
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int j = 0; j < KB; ++j)
+      if (j < cnt) {
+        const double v = warp_sum(part[j]);
+        if (l == 0) red[w * KB + j] = v;
+      }
+    __syncthreads();
+    for (int j = threadIdx.x; j < cnt; j += blockDim.x) {
+      double s = 0.0;
+      for (int i = 0; i < nw; ++i) s = __dadd_rn(s, red[i * KB + j]);
+      tot[j] = __dadd_rn(tot[j], s);
+    }
+    __syncthreads();
+  }
+  (void)tmp;
+}
 
 // Householder reflector of col[kk..rows) (Householder.h:67-96 semantics).
 // Returns tau; writes beta to col[kk] and the essential part below it.
 __device__ double make_householder_col(double* col, int64_t rows, int kk, double* red) {
-  double part = 0.0;
-  for (int64_t i = kk + 1 + threadIdx.x; i < rows; i += blockDim.x) part = __fma_rn(col[i], col[i], part);
-  const double tail_sq = (rows - kk == 1) ? 0.0 : block_sum(part, red);
+  const double tail_sq =
+      (rows - kk == 1) ? 0.0 : block_qsum(kk + 1, rows, red, [&](int64_t i, double p) { return __fma_rn(col[i], col[i], p); });
   const double c0 = col[kk];
   double tau, beta;
   __syncthreads();
@@ -356,19 +290,14 @@ __device__ void apply_householder_cols(double* const* colp, int64_t rows, int kk
   if (tau == 0.0) return;
   const double* v = colp[kk];
   double* cp[KB];
-  double part[KB];
 #pragma unroll
-  for (int j = 0; j < KB; ++j) {
-    cp[j] = j < cnt ? colp[c_lo + j] : nullptr;
-    part[j] = 0.0;
-  }
-  for (int64_t i = kk + 1 + threadIdx.x; i < rows; i += blockDim.x) {
+  for (int j = 0; j < KB; ++j) cp[j] = j < cnt ? colp[c_lo + j] : nullptr;
+  block_qsum_vec<KB>(kk + 1, rows, cnt, red, nullptr, sh_tmp, [&](int64_t i, double (&part)[KB]) {
     const double vi = v[i];
 #pragma unroll
     for (int j = 0; j < KB; ++j)
       if (j < cnt) part[j] = __fma_rn(vi, cp[j][i], part[j]);
-  }
-  block_sum_vec_t<KB>(part, cnt, red, sh_tmp);
+  });
   // tmp_j += Q[kk, j]; Q[kk, j] -= tau * tmp_j
   if (threadIdx.x == 0) {
     for (int j = 0; j < cnt; ++j) {
@@ -390,20 +319,19 @@ __device__ void apply_householder_cols(double* const* colp, int64_t rows, int kk
   __syncthreads();
 }
 
-// One block per tuned candidate: column-pivoted QR least squares.  KB bounds
-// the columns [A | 1 | y] (k + 1) so that per-column accumulators stay in
-// registers.  Pivoting swaps column pointers, not data.
+// One block per tuned candidate: column-pivoted QR least squares on
+// [A | 1 | y] with every sum in QSUM order (bit-identical to the chunked
+// passes of qr_chunk.cu).  KB bounds the columns (k + 1) so that per-column
+// accumulators stay in registers.  Pivoting swaps column pointers, not data.
 template <int KB>
 __global__ void __launch_bounds__(256) plain_qr_kernel_t(DevBatch b, DevData ds, const PlainCand* pc,
                                                           const int32_t* list, int cand0, const double* A, double* M,
-                                                          double* S, int tsqr, int nb, double* coefs, rrg_result* res,
-                                                          uint32_t* status, uint8_t* redo, const int32_t* colmap) {
+                                                          double* coefs, rrg_result* res, uint32_t* status,
+                                                          const int32_t* colmap) {
   extern __shared__ double smem[];
   const int c = list ? list[cand0 + blockIdx.x] : cand0 + blockIdx.x;
   const rrg_cand cd = b.cands[c];
   if (cd.mode != RRG_TUNED || (pc[c].pad & 1)) return;  // pad bit 0: outcome already written
-  // second pass of a tiled round: only the candidates the first pass flagged
-  if (!tsqr && redo && !redo[c]) return;
   const int k = pc[c].k;
   if (k + 1 > KB || k > kMaxK) {
     if (threadIdx.x == 0) atomicOr(status, ST_TOO_LARGE);
@@ -418,59 +346,31 @@ __global__ void __launch_bounds__(256) plain_qr_kernel_t(DevBatch b, DevData ds,
   int* misc = perm + kMaxK;                 // [0] pivot, [1] nonzero, [2..] recompute flags
   __shared__ double* colp[KB];              // current position -> column storage
 
-  int64_t ld, rows;
-  double* Q;
-  double part[KB];
-#pragma unroll
-  for (int j = 0; j < KB; ++j) part[j] = 0.0;
-  if (tsqr) {
-    Q = S + pc[c].s_off;
-    ld = (int64_t)nb * k;
-    rows = ld;
-    for (int j = threadIdx.x; j <= k; j += blockDim.x) colp[j] = Q + (int64_t)j * ld;
-    __syncthreads();
-    // initial column norms
-    for (int64_t i = threadIdx.x; i < rows; i += blockDim.x) {
-#pragma unroll
-      for (int j = 0; j < KB; ++j)
-        if (j < k) {
-          const double q = colp[j][i];
-          part[j] = __fma_rn(q, q, part[j]);
-        }
-    }
-  } else {
-    Q = M + pc[c].m_col * ds.n_pad;
-    ld = ds.n_pad;
-    rows = ds.n;
-    for (int j = threadIdx.x; j <= k; j += blockDim.x) colp[j] = Q + (int64_t)j * ld;
-    // [A | 1 | y] into the working columns; the initial norms on the way
-    // (each lane sums its rows in the same order as a separate pass would)
-#pragma unroll
-    for (int j = 0; j < KB; ++j) {
-      if (j > k) break;
-      double* dst = Q + (int64_t)j * ld;
-      if (j < k - 1) {
-        const double* src = factor_column(A, ds.n_pad, pc[c].a_col, j, colmap);
-        double acc = 0.0;
-        for (int64_t r = threadIdx.x; r < rows; r += blockDim.x) {
-          const double v = src[r];
-          dst[r] = v;
-          acc = __fma_rn(v, v, acc);
-        }
-        part[j] = acc;
-      } else if (j == k - 1) {
-        double acc = 0.0;
-        for (int64_t r = threadIdx.x; r < rows; r += blockDim.x) {
-          dst[r] = 1.0;
-          acc = __dadd_rn(acc, 1.0);
-        }
-        part[j] = acc;
-      } else {
-        for (int64_t r = threadIdx.x; r < rows; r += blockDim.x) dst[r] = ds.y64[r];
-      }
+  double* Q = M + pc[c].m_col * ds.n_pad;
+  const int64_t ld = ds.n_pad, rows = ds.n;
+  for (int j = threadIdx.x; j <= k; j += blockDim.x) colp[j] = Q + (int64_t)j * ld;
+  // [A | 1 | y] into the working columns
+  for (int j = 0; j <= k; ++j) {
+    double* dst = Q + (int64_t)j * ld;
+    if (j < k - 1) {
+      const double* src = factor_column(A, ds.n_pad, pc[c].a_col, j, colmap);
+      for (int64_t r = threadIdx.x; r < rows; r += blockDim.x) dst[r] = src[r];
+    } else if (j == k - 1) {
+      for (int64_t r = threadIdx.x; r < rows; r += blockDim.x) dst[r] = 1.0;
+    } else {
+      for (int64_t r = threadIdx.x; r < rows; r += blockDim.x) dst[r] = ds.y64[r];
     }
   }
-  block_sum_vec_t<KB>(part, k, red, sh_tmp);
+  __syncthreads();
+  // initial column norms
+  block_qsum_vec<KB>(0, rows, k, red, nullptr, sh_tmp, [&](int64_t i, double (&part)[KB]) {
+#pragma unroll
+    for (int j = 0; j < KB; ++j)
+      if (j < k) {
+        const double q = colp[j][i];
+        part[j] = __fma_rn(q, q, part[j]);
+      }
+  });
   const double rows_thr = (double)ds.n;
   const int size = (int)(rows < k ? rows : k);
   if (threadIdx.x == 0) {
@@ -532,12 +432,7 @@ __global__ void __launch_bounds__(256) plain_qr_kernel_t(DevBatch b, DevData ds,
     for (int j = kk + 1; j < k; ++j) {
       if (!rec[j]) continue;  // uniform
       const double* cj = colp[j];
-      double p1 = 0.0;
-      for (int64_t i = kk + 1 + threadIdx.x; i < rows; i += blockDim.x) {
-        const double q = cj[i];
-        p1 = __fma_rn(q, q, p1);
-      }
-      const double s = block_sum(p1, red);
+      const double s = block_qsum(kk + 1, rows, red, [&](int64_t i, double p) { return __fma_rn(cj[i], cj[i], p); });
       if (threadIdx.x == 0) {
         ndir[j] = __dsqrt_rn(s);
         nupd[j] = ndir[j];
@@ -558,19 +453,6 @@ __global__ void __launch_bounds__(256) plain_qr_kernel_t(DevBatch b, DevData ds,
     for (int j = 0; j < k; ++j) out[j] = 0.0;
     for (int i = 0; i < r; ++i) out[perm[i]] = cvec[i];
     res[c].rank = r;
-    if (tsqr && redo) {
-      // The tiled factorisation reproduces the direct one to rounding only.
-      // Where the rank rule or the pivot order is sensitive to rounding
-      // (a rank cut, or a trailing pivot far below the leading one), the
-      // candidate is re-solved by the direct column-pivoted QR on [A | 1 | y].
-      double rmax = 0.0, rmin = 1e308;
-      for (int i = 0; i < size; ++i) {
-        const double d = fabs(colp[i][i]);
-        rmax = d > rmax ? d : rmax;
-        rmin = d < rmin ? d : rmin;
-      }
-      redo[c] = (r < k || !(rmin > 1e-7 * rmax)) ? 1 : 0;
-    }
   }
 }
 
@@ -579,21 +461,21 @@ __global__ void __launch_bounds__(256) plain_qr_kernel_t(DevBatch b, DevData ds,
 int plain_qr_bucket(int cols) { return cols <= 4 ? 4 : (cols <= 8 ? 8 : (cols <= 16 ? 16 : kMaxK + 1)); }
 
 bool launch_plain_qr(int max_cols, int grid, cudaStream_t st, DevBatch b, DevData ds, const PlainCand* pc,
-                     const int32_t* list, int cand0, const double* A, double* M, double* S, int tsqr, int nb,
-                     double* coefs, rrg_result* res, uint32_t* status, uint8_t* redo, const int32_t* colmap) {
+                     const int32_t* list, int cand0, const double* A, double* M, double* coefs, rrg_result* res,
+                     uint32_t* status, const int32_t* colmap) {
   if (grid <= 0) return true;
   const size_t sm = plain_qr_smem();
   if (max_cols <= 4)
-    plain_qr_kernel_t<4><<<grid, 256, sm, st>>>(b, ds, pc, list, cand0, A, M, S, tsqr, nb, coefs, res, status, redo, colmap);
+    plain_qr_kernel_t<4><<<grid, 256, sm, st>>>(b, ds, pc, list, cand0, A, M, coefs, res, status, colmap);
   else if (max_cols <= 8)
-    plain_qr_kernel_t<8><<<grid, 256, sm, st>>>(b, ds, pc, list, cand0, A, M, S, tsqr, nb, coefs, res, status, redo, colmap);
+    plain_qr_kernel_t<8><<<grid, 256, sm, st>>>(b, ds, pc, list, cand0, A, M, coefs, res, status, colmap);
   else if (max_cols <= 16)
-    plain_qr_kernel_t<16><<<grid, 256, sm, st>>>(b, ds, pc, list, cand0, A, M, S, tsqr, nb, coefs, res, status, redo, colmap);
+    plain_qr_kernel_t<16><<<grid, 256, sm, st>>>(b, ds, pc, list, cand0, A, M, coefs, res, status, colmap);
   else
-    plain_qr_kernel_t<kMaxK + 1><<<grid, 256, sm, st>>>(b, ds, pc, list, cand0, A, M, S, tsqr, nb, coefs, res, status,
-                                                        redo, colmap);
+    plain_qr_kernel_t<kMaxK + 1><<<grid, 256, sm, st>>>(b, ds, pc, list, cand0, A, M, coefs, res, status, colmap);
   return launch_ok("launch_plain_qr");
 }
+
 
 
 // grid (ceil(n / RR_CHUNK), candidates): SSE of the rebuilt sum per chunk of

@@ -8,44 +8,20 @@ constexpr int kMaxCodeSmem = 4096;  // program words staged in shared memory per
 
 struct ColStat;
 // `list` (may be NULL) maps grid positions to candidates: candidate = list[cand0 + i].
-// cst (may be NULL; one-column programs, no TSQR): column statistics of every
+// cst (may be NULL; one-column programs): column statistics of every
 // written column, merged into cst[pc[c].a_col] (zeroed before the launch).
 __global__ void plain_eval_kernel(DevBatch b, DevData ds, const PlainCand* pc, const int32_t* list, int cand0,
-                                  double* A, double* M, double* S, int tsqr, uint32_t* status, ColStat* cst);
-// tsqr = 1: pivoted QR of the stacked slice triangles, and redo[c] = 1 when
-// the candidate must be re-solved directly; tsqr = 0 with redo != NULL: only
-// the flagged candidates, by the direct QR on [A | 1 | y].
+                                  double* A, uint32_t* status, ColStat* cst);
 // colmap (may be NULL): factor column j of candidate c is column
 // colmap[pc[c].a_col + j] of A (a shared factor table) instead of
 // column pc[c].a_col + j.
 // Column bucket (register footprint) of the QR kernel for k + 1 columns.
 int plain_qr_bucket(int cols);
-// One block per candidate of the launch; max_cols bounds k + 1 over them.
+// One block per candidate of the launch (the whole factorisation in one
+// launch; QSUM order, the bits of launch_qr_chunked); max_cols bounds k + 1.
 bool launch_plain_qr(int max_cols, int grid, cudaStream_t st, DevBatch b, DevData ds, const PlainCand* pc,
-                     const int32_t* list, int cand0, const double* A, double* M, double* S, int tsqr, int nb,
-                     double* coefs, rrg_result* res, uint32_t* status, uint8_t* redo, const int32_t* colmap);
-// The direct QR (tsqr = 0, no redo) of each listed candidate on a cluster of
-// eight CTAs of `warps` warps (qr_cluster.cu): bit-identical results for every
-// shape, a candidate's work spread over eight SMs.  warps = 0 takes the
-// bucket's default; a shape the kernel is not built for returns false.
-// count_bytes = false leaves the algorithmic-bytes counter alone (a timing trial).
-bool launch_plain_qr_cluster(int max_cols, int warps, int n_cand, cudaStream_t st, DevBatch b, DevData ds,
-                             const PlainCand* pc, const int32_t* list, int cand0, const double* A, double* M,
-                             double* coefs, rrg_result* res, uint32_t* status, const int32_t* colmap,
-                             bool count_bytes);
-// Warps per CTA the cluster QR is built for in a column bucket, the default
-// first; returns how many (0 for an unknown bucket).
-int qr_warp_variants(int bucket, int* out);
-// The list form of the cluster QR: n_clusters clusters take the candidates
-// list[0 .. *count) from the counter *next (zero before the launch), each
-// factorising in working slot (cluster index) of slot_cols >= bucket columns
-// of M.  Bit-identical to launch_plain_qr_cluster.
-bool launch_plain_qr_cluster_list(int bucket, int warps, int n_clusters, cudaStream_t st, DevBatch b, DevData ds,
-                                  const PlainCand* pc, const int32_t* list, const int32_t* count, int32_t* next,
-                                  const double* A, double* M, int slot_cols, double* coefs, rrg_result* res,
-                                  uint32_t* status, const int32_t* colmap, bool count_bytes);
-// Clusters of the list form that fit on the device at once (0 when unknown).
-int qr_cluster_list_clusters(int bucket, int warps);
+                     const int32_t* list, int cand0, const double* A, double* M, double* coefs, rrg_result* res,
+                     uint32_t* status, const int32_t* colmap);
 // dcount (may be NULL): grid positions at or beyond *dcount do nothing (a
 // list whose length the device decided; the grid covers its capacity).
 __global__ void plain_resid_kernel(DevBatch b, DevData ds, const PlainCand* pc, const int32_t* list, int cand0,

@@ -21,6 +21,7 @@
 #include "ftable.cuh"
 #include "mixed.cuh"
 #include "plain.cuh"
+#include "qr_chunk.cuh"
 #include "rescore.cuh"
 #include "runtime.cuh"
 #include "tune.cuh"
@@ -893,25 +894,23 @@ rrg_status rrg_context::mixed_subround(const rrg_dataset* ds, const int32_t* lis
       const int cols = cd.n_factors + 2;
       ++bucket_cap[cols <= 4 ? 0 : (cols <= 8 ? 1 : (cols <= 16 ? 2 : 3))];
     }
-    int qwarps[kQrBuckets] = {0, 0, 0, 0}, nclus[kQrBuckets] = {0, 0, 0, 0};
+    // working columns of the QR: each bucket factorises up to qbatch[q] of
+    // its candidates at a time (in order, as many batches as its capacity
+    // needs), the buckets sharing half the scratch budget in proportion to
+    // their capacities
+    const int64_t nch = (ds->n + RR_CHUNK - 1) / RR_CHUNK;
+    double slot_need = 0.0;
+    for (int q = 0; q < kQrBuckets; ++q) slot_need += (double)bucket_cap[q] * kBucketCols[q] * (double)col8;
+    const double share = slot_need > 0.0 ? std::min(1.0, (double)scratch_budget_bytes / 2 / slot_need) : 1.0;
+    int qbatch[kQrBuckets] = {0, 0, 0, 0};
+    size_t m_cols = 0, q_bytes = 0;
     for (int q = 0; q < kQrBuckets; ++q) {
       if (!bucket_cap[q]) continue;
-      bool trial = false;
-      qwarps[q] = tune_pick(TK_QR_LIST_WARPS, kBucketCols[q], ds->n, &trial);
-      int occ = qr_cluster_list_clusters(kBucketCols[q], qwarps[q]);
-      if (occ <= 0) occ = std::max(1, sm_count / 8);
-      nclus[q] = std::min(bucket_cap[q], occ);
+      qbatch[q] = std::max(1, std::min(bucket_cap[q], (int)((double)bucket_cap[q] * share)));
+      m_cols += (size_t)qbatch[q] * kBucketCols[q];
+      q_bytes += (size_t)round_up((int64_t)qr_chunk_scratch_bytes(qbatch[q], ds->n, kBucketCols[q]), 256);
     }
-    // working slots of the QR within half the scratch budget (the FP64
-    // table takes the other half): the widest buckets give up clusters first
-    auto slot_bytes = [&]() {
-      double t = 0.0;
-      for (int q = 0; q < kQrBuckets; ++q) t += (double)nclus[q] * kBucketCols[q] * (double)col8;
-      return t;
-    };
-    for (int q = kQrBuckets - 1; q >= 0 && slot_bytes() > (double)scratch_budget_bytes / 2; --q)
-      while (nclus[q] > 1 && slot_bytes() > (double)scratch_budget_bytes / 2) nclus[q] = (nclus[q] + 1) / 2;
-    const bool fits = slot_bytes() <= (double)scratch_budget_bytes / 2 &&
+    const bool fits = (double)m_cols * (double)col8 <= (double)scratch_budget_bytes / 2 &&
                       (double)ncol * (double)col8 <= (double)scratch_budget_bytes / 2;
     if (fits) {
       // host records of the lane: one-column pseudo-candidates of the table
@@ -969,15 +968,13 @@ rrg_status rrg_context::mixed_subround(const rrg_dataset* ds, const int32_t* lis
       if (pst != RRG_OK) return pst;
       const int nb_res = (int)((ds->n + RR_CHUNK - 1) / RR_CHUNK);
       const int nbx = (int)std::max<int64_t>(1, std::min<int64_t>(16, (ds->n + 32767) / 32768));
-      size_t m_cols = 0;
-      for (int q = 0; q < kQrBuckets; ++q) m_cols += (size_t)nclus[q] * kBucketCols[q];
       const size_t stat_words = 2 + kFbReasons + (size_t)n_levels;
       if (!d_rlist2.reserve(sizeof(int32_t) * (cnt + 1)) || !d_fbneed.reserve(std::max(1, ncol)) ||
           !d_fbcols.reserve(sizeof(int32_t) * (ncol + n_levels + 1)) ||
           !d_fbF64.reserve(col8 * std::max(1, ncol)) || !d_fbcst.reserve(sizeof(ColStat) * std::max(1, ncol)) ||
           !d_fbgram.reserve(sizeof(double) * (size_t)cnt * nbx * (kGramCols * (kGramCols + 1) / 2)) ||
-          !d_fbblist.reserve(sizeof(int32_t) * ((size_t)kQrBuckets * cnt + 2 * kQrBuckets)) ||
-          !d_fbM.reserve(col8 * std::max<size_t>(1, m_cols)) ||
+          !d_fbblist.reserve(sizeof(int32_t) * ((size_t)kQrBuckets * cnt + kQrBuckets)) ||
+          !d_fbM.reserve(col8 * std::max<size_t>(1, m_cols)) || !d_qrs.reserve(std::max<size_t>(256, q_bytes)) ||
           !h_fbstat.reserve(sizeof(int32_t) * stat_words)) {
         rrc::set_error("mixed round: re-scoring lane allocation failed");
         return RRG_E_OOM;
@@ -992,7 +989,6 @@ rrg_status rrg_context::mixed_subround(const rrg_dataset* ds, const int32_t* lis
       double* gpart = static_cast<double*>(d_fbgram.ptr);
       int32_t* blist = static_cast<int32_t*>(d_fbblist.ptr);
       int32_t* bcount = blist + (size_t)kQrBuckets * cnt;
-      int32_t* qnext = bcount + kQrBuckets;
       double* Mq = static_cast<double*>(d_fbM.ptr);
       const int32_t* d_ccol = pk.at<const int32_t>(d_ft, o_ccol);
       PlainCand* d_pcs = pf.at<PlainCand>(d_fbpack, o_pcs);
@@ -1037,7 +1033,7 @@ rrg_status rrg_context::mixed_subround(const rrg_dataset* ds, const int32_t* lis
       t0 = mark_begin();
       RRG_CUDA(cudaMemsetAsync(need, 0, std::max(1, ncol), stream));
       RRG_CUDA(cudaMemsetAsync(cst, 0, sizeof(ColStat) * std::max(1, ncol), stream));
-      RRG_CUDA(cudaMemsetAsync(bcount, 0, sizeof(int32_t) * 2 * kQrBuckets, stream));
+      RRG_CUDA(cudaMemsetAsync(bcount, 0, sizeof(int32_t) * kQrBuckets, stream));
       DevBatch fdev = dev;
       fdev.cands = pf.at<const rrg_cand>(d_fbpack, o_fc);
       fdev.code = pkt.at<const uint32_t>(d_ftp, o_tcode);
@@ -1098,69 +1094,43 @@ rrg_status rrg_context::mixed_subround(const rrg_dataset* ds, const int32_t* lis
       }
       mark_end(P_PLAIN_EVAL, t0);
       launches += n_levels + 6;
-      // launch-shape trials of the QR (the first round of a bucket and row
-      // class): the bucket counts are read back once so that a trial times
-      // real work; a repeat restarts from the table columns (same results)
-      {
-        bool qtrial[kQrBuckets] = {false, false, false, false}, any = false;
-        for (int q = 0; q < kQrBuckets; ++q) {
-          if (!nclus[q] || capturing) continue;
-          bool tr = false;
-          tune_pick(TK_QR_LIST_WARPS, kBucketCols[q], ds->n, &tr);
-          qtrial[q] = tr;
-          any = any || tr;
-        }
-        if (any) {
-          int32_t hb[kQrBuckets] = {0, 0, 0, 0};
-          RRG_CUDA(cudaMemcpyAsync(hb, bcount, sizeof hb, cudaMemcpyDeviceToHost, stream));
-          RRG_CUDA(cudaStreamSynchronize(stream));
-          size_t off = 0;
-          for (int q = 0; q < kQrBuckets; ++q) {
-            double* Mb = Mq + off * ds->n_pad;
-            off += (size_t)nclus[q] * kBucketCols[q];
-            if (!qtrial[q] || (int64_t)hb[q] * ds->n < kTuneMinWork) continue;
-            int vals[4];
-            float ms[4];
-            const int nv = tune_variants(TK_QR_LIST_WARPS, kBucketCols[q], vals);
-            for (int v = 0; v < nv; ++v) {
-              const int nc = std::min(nclus[q], std::max(1, qr_cluster_list_clusters(kBucketCols[q], vals[v])));
-              bool ok = true;
-              rrg_status ts = time_trial([&] {
-                ok = cudaMemsetAsync(qnext + q, 0, sizeof(int32_t), stream) == cudaSuccess &&
-                     launch_plain_qr_cluster_list(kBucketCols[q], vals[v], nc, stream, dev, dd, d_pcs,
-                                                  blist + (size_t)q * cnt, bcount + q, qnext + q, F64, Mb,
-                                                  kBucketCols[q], coefs, res, status, d_ccol, false);
-              }, ms[v]);
-              if (!ok) return RRG_E_CUDA;
-              if (ts != RRG_OK) return ts;
-              launches += 1;
-            }
-            tune_store(TK_QR_LIST_WARPS, kBucketCols[q], ds->n, vals, ms, nv);
-            bool tr = false;
-            qwarps[q] = tune_pick(TK_QR_LIST_WARPS, kBucketCols[q], ds->n, &tr);
-            nclus[q] = std::min(nclus[q], std::max(1, qr_cluster_list_clusters(kBucketCols[q], qwarps[q])));
-          }
-          RRG_CUDA(cudaMemsetAsync(qnext, 0, sizeof(int32_t) * kQrBuckets, stream));
-        }
-      }
-      // one list-form QR per column bucket, side by side on the side streams
+      // the QR of every bucket, side by side on the side streams: the chunked
+      // passes over the bucket's list, qbatch[q] candidates per batch
       t0 = mark_begin();
       RRG_CUDA(cudaEventRecord(fork_ev, stream));
       int used = 0;
-      size_t m_off = 0;
+      size_t m_off = 0, q_off = 0;
       for (int q = 0; q < kQrBuckets; ++q) {
-        if (!nclus[q]) continue;
+        if (!qbatch[q]) continue;
         cudaStream_t sq = side[used % kSide];
         if (used < kSide) RRG_CUDA(cudaStreamWaitEvent(sq, fork_ev, 0));
-        if (!launch_plain_qr_cluster_list(kBucketCols[q], qwarps[q], nclus[q], sq, dev, dd, d_pcs,
-                                          blist + (size_t)q * cnt, bcount + q, qnext + q, F64, Mq + m_off * ds->n_pad,
-                                          kBucketCols[q], coefs, res, status, d_ccol, true)) {
-          cuda_ok(cudaGetLastError(), "QR launch");
-          return RRG_E_CUDA;
+        for (int32_t t0b = 0; t0b < bucket_cap[q]; t0b += qbatch[q]) {
+          QrJob jb{};
+          jb.b = dev;
+          jb.ds = dd;
+          jb.pc = d_pcs;
+          jb.list = blist + (size_t)q * cnt;
+          jb.list_off = t0b;
+          jb.n_list = qbatch[q];
+          jb.dcount = bcount + q;
+          jb.A = F64;
+          jb.colmap = d_ccol;
+          jb.M = Mq + m_off * ds->n_pad;
+          jb.slot_cols = kBucketCols[q];
+          jb.coefs = coefs;
+          jb.res = res;
+          jb.status = status;
+          jb.count_bytes = 1;
+          jb.max_cols = kBucketCols[q];
+          qr_chunk_bind(jb, static_cast<char*>(d_qrs.ptr) + q_off);
+          if (!launch_qr_chunked(jb, qr_blocks(kBucketCols[q], (int64_t)qbatch[q] * nch), sq, &launches)) {
+            cuda_ok(cudaGetLastError(), "QR launch");
+            return RRG_E_CUDA;
+          }
         }
-        m_off += (size_t)nclus[q] * kBucketCols[q];
+        m_off += (size_t)qbatch[q] * kBucketCols[q];
+        q_off += (size_t)round_up((int64_t)qr_chunk_scratch_bytes(qbatch[q], ds->n, kBucketCols[q]), 256);
         ++used;
-        ++launches;
       }
       for (int i = 0; i < std::min(used, (int)kSide); ++i) {
         RRG_CUDA(cudaEventRecord(join_ev[i], side[i]));
@@ -1431,7 +1401,7 @@ rrg_status rrg_context::run_fp64_table(const rrg_dataset* ds, const std::vector<
         for (int32_t f0 = (int32_t)c0; f0 < c1; f0 += 65535) {
           const int32_t nfb = std::min<int32_t>(65535, c1 - f0);
           plain_eval_kernel<<<dim3(nb, nfb), 256, plain_eval_smem(), stream>>>(
-              fdev, dd, pk.at<const PlainCand>(d_ft64, o_fpc), nullptr, f0, F64, F64, nullptr, 0, status, cst);
+              fdev, dd, pk.at<const PlainCand>(d_ft64, o_fpc), nullptr, f0, F64, status, cst);
           ++launches;
         }
       };
@@ -1481,58 +1451,65 @@ rrg_status rrg_context::run_fp64_table(const rrg_dataset* ds, const std::vector<
     for (const auto& sb : subs) {
       const int32_t ns = sb.second - sb.first;
       if (ns <= 0) continue;
-      // register buckets of the sub-batch, each with the tuner's warps per CTA;
-      // a bucket the tuner has no choice for is timed in every shape first, on
-      // the round's stream alone (the factorisation restarts from the table
-      // columns, so a repeat gives the same bits)
+      // one factorisation per register bucket of the sub-batch, side by side
+      // on the side streams: one block per candidate while the rows fit one
+      // chunk, otherwise the chunked passes over the whole GPU (same bits)
       struct QrRun {
         int32_t b0, b1;
-        int bk, warps;
+        int bk;
+        size_t off;
       };
       std::vector<QrRun> runs;
+      const bool chunked = ds->n > RR_CHUNK;
+      size_t qbytes = 0;
       for (int32_t b0 = sb.first; b0 < sb.second;) {
         const int bk = bucket(list[pos + b0]);
         int32_t b1 = b0;
         while (b1 < sb.second && bucket(list[pos + b1]) == bk) ++b1;
-        bool trial = false;
-        int warps = tune_pick(TK_QR_WARPS, bk, ds->n, &trial);
-        if (trial && !capturing && (int64_t)(b1 - b0) * ds->n >= kTuneMinWork) {
-          int vals[4];
-          float ms[4];
-          const int nv = tune_variants(TK_QR_WARPS, bk, vals);
-          for (int v = 0; v < nv; ++v) {
-            bool ok = true;
-            rrg_status ts = time_trial([&] {
-              ok = launch_plain_qr_cluster(bk, vals[v], b1 - b0, stream, dev, dd, d_pcs, d_list, b0, F64, M, coefs,
-                                           res, status, d_cmap, false);
-              ++launches;
-            }, ms[v]);
-            if (!ok) {
-              cuda_ok(cudaGetLastError(), "QR launch");
-              return RRG_E_CUDA;
-            }
-            if (ts != RRG_OK) return ts;
-          }
-          tune_store(TK_QR_WARPS, bk, ds->n, vals, ms, nv);
-          warps = tune_pick(TK_QR_WARPS, bk, ds->n, &trial);
-        }
-        runs.push_back({b0, b1, bk, warps});
+        runs.push_back({b0, b1, bk, qbytes});
+        if (chunked) qbytes += (size_t)round_up((int64_t)qr_chunk_scratch_bytes(b1 - b0, ds->n, bk), 256);
         b0 = b1;
       }
+      if (chunked && !d_qrs.reserve(std::max<size_t>(qbytes, 256))) {
+        rrc::set_error("FP64 round: QR scratch allocation failed");
+        return RRG_E_OOM;
+      }
       t0 = mark_begin();
-      // one launch per register bucket, side by side on the side streams
       RRG_CUDA(cudaEventRecord(fork_ev, stream));
       int used = 0;
       for (const QrRun& r : runs) {
         cudaStream_t s = side[used % kSide];
         if (used < kSide) RRG_CUDA(cudaStreamWaitEvent(s, fork_ev, 0));
-        if (!launch_plain_qr_cluster(r.bk, r.warps, r.b1 - r.b0, s, dev, dd, d_pcs, d_list, r.b0, F64, M, coefs, res,
-                                     status, d_cmap, true)) {
+        bool ok;
+        if (!chunked) {
+          ok = launch_plain_qr(r.bk, r.b1 - r.b0, s, dev, dd, d_pcs, d_list, r.b0, F64, M, coefs, res, status, d_cmap);
+          ++launches;
+        } else {
+          QrJob jb{};
+          jb.b = dev;
+          jb.ds = dd;
+          jb.pc = d_pcs;
+          jb.list = d_list;
+          jb.list_off = r.b0;
+          jb.n_list = r.b1 - r.b0;
+          jb.dcount = nullptr;
+          jb.A = F64;
+          jb.colmap = d_cmap;
+          jb.M = M;
+          jb.slot_cols = 0;
+          jb.coefs = coefs;
+          jb.res = res;
+          jb.status = status;
+          jb.count_bytes = 1;
+          jb.max_cols = r.bk;
+          qr_chunk_bind(jb, static_cast<char*>(d_qrs.ptr) + r.off);
+          ok = launch_qr_chunked(jb, qr_blocks(r.bk, (int64_t)jb.n_list * jb.nch), s, &launches);
+        }
+        if (!ok) {
           cuda_ok(cudaGetLastError(), "QR launch");
           return RRG_E_CUDA;
         }
         ++used;
-        ++launches;
       }
       for (int i = 0; i < std::min(used, (int)kSide); ++i) {
         RRG_CUDA(cudaEventRecord(join_ev[i], side[i]));

@@ -23,6 +23,7 @@
 #include "ftable.cuh"
 #include "mixed.cuh"
 #include "plain.cuh"
+#include "qr_chunk.cuh"
 #include "runtime.cuh"
 
 using namespace rrd;
@@ -245,68 +246,13 @@ rrg_status rrg_context::stage_batch(const rrg_batch* b) {
   return RRG_OK;
 }
 
-// Plain FP64 round over `list` (or [lo, hi)), in sub-batches that fit the
-// scratch budget.
-rrg_status rrg_context::run_plain(const rrg_dataset* ds, int32_t lo, int32_t hi, bool predict_only,
-                                  const std::vector<int32_t>* list, uint32_t flags_or, bool tiled_any,
-                                  bool redo_sensitive) {
+// The values of candidate 0 (one untuned program) on every row, into d_A.
+rrg_status rrg_context::run_predict(const rrg_dataset* ds) {
   const DevData dd = ds->view();
-  const int64_t n_pad = ds->n_pad;
-  std::vector<int32_t> all;
-  if (!list) {
-    for (int32_t c = lo; c < hi; ++c) all.push_back(c);
-    list = &all;
-  }
-  const int32_t cnt = (int32_t)list->size();
-  if (cnt == 0) return RRG_OK;
-  struct Sub {
-    int32_t p, e, nb;
-    bool tsqr;
-  };
-  std::vector<Sub> subs;
   std::vector<PlainCand> pcs(host_cands.size());
-  int64_t max_cols = 1, max_s = 1, max_nb = 1;
-  for (int32_t p = 0; p < cnt;) {
-    int64_t cols = 0;
-    int32_t e = p;
-    while (e < cnt) {
-      const int32_t c = (*list)[e];
-      const rrg_cand& cd = host_cands[c];
-      const int64_t k = cd.mode == RRG_TUNED ? cd.n_factors + 1 : 1;
-      const int64_t need = (cols + 2 * k + 1) * n_pad * (int64_t)sizeof(double);
-      if (e > p && (size_t)need > scratch_budget_bytes) break;
-      pcs[c].a_col = cols;
-      pcs[c].m_col = cols + k;
-      pcs[c].k = (int32_t)k;
-      cols += 2 * k + 1;
-      ++e;
-    }
-    const int32_t ns = e - p;
-    int nb = (int)std::min<int64_t>(std::max<int64_t>(1, (4LL * sm_count + ns - 1) / ns), (ds->n + 1023) / 1024);
-    nb = std::max(nb, 1);
-    bool tsqr = !predict_only && ds->n >= 65536 && (ns < 2 * sm_count || tiled_any);
-    if (tsqr) nb = (int)std::max<int64_t>(1, std::min<int64_t>(std::max<int64_t>(nb, ds->n / 16384), ds->n / 2048));
-    tsqr = tsqr && nb > 1;
-    int64_t s_total = 0;
-    for (int32_t i = p; i < e; ++i) {
-      const int32_t c = (*list)[i];
-      pcs[c].s_off = s_total;
-      if (tsqr) s_total += (int64_t)nb * pcs[c].k * (pcs[c].k + 1);
-    }
-    max_cols = std::max(max_cols, cols);
-    max_s = std::max(max_s, s_total);
-    max_nb = std::max<int64_t>(max_nb, nb);
-    subs.push_back(Sub{p, e, nb, tsqr});
-    p = e;
-  }
-  const int nb_res = (int)((ds->n + RR_CHUNK - 1) / RR_CHUNK);
-  max_nb = std::max<int64_t>(max_nb, nb_res);
-  const size_t pc_bytes = sizeof(PlainCand) * host_cands.size();
-  const size_t list_bytes = sizeof(int32_t) * cnt;
-  if (!d_A.reserve((size_t)max_cols * n_pad * sizeof(double)) || !d_S.reserve((size_t)max_s * sizeof(double)) ||
-      !d_pc.reserve(pc_bytes) || !d_partial.reserve(sizeof(double) * (size_t)host_cands.size() * max_nb) ||
-      !h_pc.reserve(pc_bytes + list_bytes) || !d_list.reserve(list_bytes) ||
-      !d_redo.reserve(std::max<size_t>(1, host_cands.size()))) {
+  pcs[0] = PlainCand{0, 0, 0, 1, 0};
+  const size_t pc_bytes = sizeof(PlainCand) * pcs.size();
+  if (!d_A.reserve((size_t)ds->n_pad * sizeof(double)) || !d_pc.reserve(pc_bytes) || !h_pc.reserve(pc_bytes)) {
     rrc::set_error("device scratch allocation failed");
     return RRG_E_OOM;
   }
@@ -314,51 +260,14 @@ rrg_status rrg_context::run_plain(const rrg_dataset* ds, int32_t lo, int32_t hi,
   if (h_pc.used_in == round_seq) RRG_CUDA(cudaStreamSynchronize(stream));
   h_pc.used_in = round_seq;
   std::memcpy(h_pc.ptr, pcs.data(), pc_bytes);
-  std::memcpy(static_cast<char*>(h_pc.ptr) + pc_bytes, list->data(), list_bytes);
   RRG_CUDA(cudaMemcpyAsync(d_pc.ptr, h_pc.ptr, pc_bytes, cudaMemcpyHostToDevice, stream));
-  RRG_CUDA(cudaMemcpyAsync(d_list.ptr, static_cast<char*>(h_pc.ptr) + pc_bytes, list_bytes, cudaMemcpyHostToDevice,
-                           stream));
-  const PlainCand* pc = static_cast<const PlainCand*>(d_pc.ptr);
-  const int32_t* dl = static_cast<const int32_t*>(d_list.ptr);
-  double* A = static_cast<double*>(d_A.ptr);
-  double* S = static_cast<double*>(d_S.ptr);
-  double* coefs = static_cast<double*>(d_coefs.ptr);
-  rrg_result* res = static_cast<rrg_result*>(d_res.ptr);
-  uint32_t* status = static_cast<uint32_t*>(d_status.ptr);
-  double* partial = static_cast<double*>(d_partial.ptr);
-  for (const Sub& sb : subs) {
-    const int32_t ns = sb.e - sb.p;
-    cudaEvent_t t0 = mark_begin();
-    plain_eval_kernel<<<dim3(sb.nb, ns), 256, plain_eval_smem(), stream>>>(dev, dd, pc, dl, sb.p, A, A, S,
-                                                                            sb.tsqr ? 1 : 0, status, nullptr);
-    mark_end(P_PLAIN_EVAL, t0);
-    ++launches;
-    if (predict_only) continue;
-    t0 = mark_begin();
-    uint8_t* redo = static_cast<uint8_t*>(d_redo.ptr);
-    int kmax = 1;
-    for (int32_t i = sb.p; i < sb.e; ++i) kmax = std::max(kmax, pcs[(*list)[i]].k);
-    // launch_plain_qr reads (and so clears) the launch error itself: check
-    // its return value
-    if (!launch_plain_qr(kmax + 1, ns, stream, dev, dd, pc, dl, sb.p, A, A, S, sb.tsqr ? 1 : 0, sb.nb, coefs, res,
-                         status, (sb.tsqr && redo_sensitive) ? redo : nullptr, nullptr) ||
-        (sb.tsqr && redo_sensitive &&
-         !launch_plain_qr(kmax + 1, ns, stream, dev, dd, pc, dl, sb.p, A, A, S, 0, sb.nb, coefs, res, status, redo,
-                          nullptr))) {
-      rrc::set_error("plain round: QR launch failed");
-      return RRG_E_CUDA;
-    }
-    mark_end(P_PLAIN_QR, t0);
-    t0 = mark_begin();
-    plain_resid_kernel<<<dim3(nb_res, ns), 256, 0, stream>>>(dev, dd, pc, dl, sb.p, A, coefs, partial,
-                                                             nullptr);
-    mark_end(P_PLAIN_RESID, t0);
-    t0 = mark_begin();
-    finalize_kernel<<<(ns + 127) / 128, 128, 0, stream>>>(dev, dd, dl, sb.p, sb.e, partial, nb_res, coefs, res,
-                                                          flags_or, nullptr);
-    mark_end(P_FINAL, t0);
-    launches += 3;
-  }
+  const int nb = (int)std::max<int64_t>(1, std::min<int64_t>(4LL * sm_count, (ds->n + 1023) / 1024));
+  cudaEvent_t t0 = mark_begin();
+  plain_eval_kernel<<<dim3(nb, 1), 256, plain_eval_smem(), stream>>>(dev, dd, static_cast<const PlainCand*>(d_pc.ptr),
+                                                                      nullptr, 0, static_cast<double*>(d_A.ptr),
+                                                                      static_cast<uint32_t*>(d_status.ptr), nullptr);
+  mark_end(P_PLAIN_EVAL, t0);
+  ++launches;
   RRG_CUDA(cudaGetLastError());
   return RRG_OK;
 }
@@ -511,13 +420,7 @@ rrg_status rrg_context::enqueue_round(rrg_dataset* ds, const rrg_batch* b, int32
   // (SST = 0): R2 = 1 - SSE/SST is then decided by whether the SSE is exactly
   // zero (0/0 gives the NaN sentinel), which only the exact path settles.
   if (precision == RRG_PLAIN_FP64 || ds->n < mixed_min_rows || !(ds->sst > 0.0)) {
-    // few candidates on tall data: the tiled QR spreads each over the GPU;
-    // otherwise one block per candidate over the shared FP64 factor table
-    if (ds->n >= 65536 && (int64_t)reps.size() < 2 * sm_count) {
-      last_tiled = true;
-      st = run_plain(ds, 0, 0, false, &reps);
-    }
-    else st = run_fp64_table(ds, reps, 0u);
+    st = run_fp64_table(ds, reps, 0u);
   } else {
     st = run_mixed(ds, reps, precision == RRG_MIXED_CERTIFIED);
   }
@@ -600,10 +503,19 @@ rrg_status rrg_context::wait(int32_t timeout_ms) {
 }
 
 std::vector<DevBuf*> rrg_context::all_bufs() {
-  return {&d_batch, &d_A, &d_S, &d_pc, &d_partial, &d_list, &d_redo, &d_terms, &d_fallback, &d_sse1, &d_probe,
+  return {&d_batch, &d_A, &d_pc, &d_partial, &d_list, &d_qrs, &d_terms, &d_fallback, &d_sse1, &d_probe,
           &d_nanrow, &d_cert_e, &d_ft, &d_ftp, &d_ft64, &d_F, &d_P, &d_Pc, &d_psum, &d_fprobe, &d_fnan, &d_F64, &d_M,
           &d_colstat, &d_gram, &d_rlist2, &d_fbpack, &d_fbneed, &d_fbcols, &d_fbF64, &d_fbcst, &d_fbgram, &d_fbblist,
           &d_fbM, &d_fbctr, &d_res, &d_coefs, &d_status};
+}
+
+// Persistent grid of the chunked QR's passes for `items` candidate x chunk items.
+int rrg_context::qr_blocks(int max_cols, int64_t items) {
+  const int w = max_cols - 1;
+  const int g = w <= 4 ? 0 : (w <= 8 ? 1 : 2);
+  if (!qr_bps[g]) qr_bps[g] = qr_chunk_blocks_per_sm(max_cols);
+  const int64_t cap = (int64_t)sm_count * qr_bps[g];
+  return (int)std::max<int64_t>(1, std::min<int64_t>(cap, items));
 }
 
 int64_t rrg_context::device_bytes() {
@@ -915,7 +827,7 @@ rrg_status rrg_predict(rrg_dataset* ds, const rrg_batch* batch, double* values) 
   if (st != RRG_OK) return st;
   if (!ctx->d_status.reserve(64) || !ctx->h_status.reserve(64)) return RRG_E_OOM;
   RRG_CUDA(cudaMemsetAsync(ctx->d_status.ptr, 0, 64, ctx->stream));
-  st = ctx->run_plain(ds, 0, 1, true, nullptr, 0u);
+  st = ctx->run_predict(ds);
   if (st != RRG_OK) return st;
   RRG_CUDA(cudaMemcpyAsync(ctx->h_status.ptr, ctx->d_status.ptr, 64, cudaMemcpyDeviceToHost, ctx->stream));
   RRG_CUDA(cudaMemcpyAsync(values, ctx->d_A.ptr, sizeof(double) * ds->n, cudaMemcpyDeviceToHost, ctx->stream));

@@ -73,7 +73,12 @@ struct rrg_context {
   rrd::DevBatch dev{};
   std::vector<rrg_cand> host_cands;
   // plain scratch
-  DevBuf d_A, d_S, d_pc, d_partial, d_list, d_redo;
+  DevBuf d_A, d_pc, d_partial, d_list;
+  // chunked-QR state and chunk totals (qr_chunk.cu); blocks per SM of its
+  // passes by column group (0: not asked yet)
+  DevBuf d_qrs;
+  int qr_bps[3] = {0, 0, 0};
+  int qr_blocks(int max_cols, int64_t items);
   HostBuf h_pc, h_list;
   // mixed scratch
   DevBuf d_terms, d_fallback, d_sse1, d_probe, d_nanrow, d_cert_e;
@@ -111,7 +116,7 @@ struct rrg_context {
   // mixed-round statistics of the last round
   int64_t last_fallback = 0, last_plain_routed = 0, last_pass2 = 0, last_sentinel = 0;
   int64_t last_distinct = 0;  // candidates scored after merging identical factor lists
-  bool last_tiled = false;    // the round solved by the tiled QR (within 1e-10 of the direct one)
+  bool last_tiled = false;    // always false: every round's QR is the direct one
   int64_t last_reasons[16] = {0};
   // certified bound on the relative fitness error of a mixed result; larger
   // bounds are re-scored by the FP64 path
@@ -146,12 +151,8 @@ struct rrg_context {
   rrg_status trial_error();
 
   rrg_status stage_batch(const rrg_batch* b);
-  // plain FP64 over `list` (absolute candidate indices) or over [lo, hi) when list is empty
-  // tiled_any: use the tiled QR on tall data whatever the candidate count;
-  // redo_sensitive: re-solve rounding-sensitive tiled candidates directly
-  rrg_status run_plain(const rrg_dataset* ds, int32_t lo, int32_t hi, bool predict_only,
-                       const std::vector<int32_t>* list = nullptr, uint32_t flags_or = 0, bool tiled_any = false,
-                       bool redo_sensitive = true);
+  // the values of candidate 0 (an untuned program) on every row, into d_A
+  rrg_status run_predict(const rrg_dataset* ds);
   // mixed round over the shared FP32 factor table; FP64 re-scoring of the
   // candidates it cannot decide
   rrg_status run_mixed(const rrg_dataset* ds, const std::vector<int32_t>& cands, bool certify);

@@ -84,25 +84,16 @@ void save_locked(const Tuner& t) {
 
 const char* knob_name(int knob) {
   switch (knob) {
-    case TK_QR_WARPS: return "qr_warps";
     case TK_EVAL_WAVES: return "eval_waves";
     case TK_FAC_GROUP: return "fac_group";
     case TK_PAIR_UNIT: return "pair_unit";
-    case TK_FAC_STAGE: return "fac_stage";
-    default: return "qr_list_warps";
+    default: return "fac_stage";
   }
 }
 
 }  // namespace
 
 int tune_variants(int knob, int bucket, int* out) {
-  if (knob == TK_QR_WARPS) return qr_warp_variants(bucket, out);
-  if (knob == TK_QR_LIST_WARPS) {
-    // the same shapes, the widest first (few candidates: latency)
-    const int nv = qr_warp_variants(bucket, out);
-    std::sort(out, out + nv, [](int x, int y) { return x > y; });
-    return nv;
-  }
   if (knob == TK_EVAL_WAVES && bucket == 0) {
     out[0] = 4;
     out[1] = 2;

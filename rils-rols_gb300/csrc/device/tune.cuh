@@ -8,7 +8,6 @@
 namespace rrd {
 
 enum TuneKnob {
-  TK_QR_WARPS = 0,    // warps per CTA of the cluster QR, by column bucket
   TK_EVAL_WAVES = 1,  // FP64 evaluator: blocks per level launch = waves x SMs (bucket 0)
   TK_FAC_GROUP = 2,   // double-float evaluator: factors per block (bucket 0); each factor's
                       // values and sums are computed alone, whatever its block-mates
@@ -16,9 +15,7 @@ enum TuneKnob {
                       // formed alone, a long partner list only spreads over more blocks
   TK_FAC_STAGE = 4,   // double-float evaluator: 2 stages a chunk's X and y rows in shared memory by
                       // tensor copies, 1 reads them from global memory (bucket: feature count d)
-  TK_QR_LIST_WARPS = 5,  // warps per CTA of the cluster QR's list form (the FP64 re-scoring of a mixed
-                         // round: few candidates, so latency rather than throughput), by column bucket
-  TK_COUNT = 6
+  TK_COUNT = 5  // knob 0 is retired
 };
 
 // Values of a knob in a bucket, the default first; returns how many (<= 4).

@@ -19,8 +19,7 @@ RRG_UNTUNED, RRG_TUNED = 0, 1
 RRG_F_NONFINITE, RRG_F_RANK_DEFICIENT, RRG_F_QR_FALLBACK, RRG_F_VERIFIED_FP64, RRG_F_TOO_LARGE = 1, 2, 4, 8, 16
 RRG_MAX_TERMS = 64
 RRG_TUNE_OFF, RRG_TUNE_ON = 0, 1
-RRG_KNOB_QR_WARPS, RRG_KNOB_EVAL_WAVES, RRG_KNOB_FAC_GROUP, RRG_KNOB_PAIR_UNIT, RRG_KNOB_FAC_STAGE, RRG_KNOB_QR_LIST_WARPS = (
-    0, 1, 2, 3, 4, 5)
+RRG_KNOB_EVAL_WAVES, RRG_KNOB_FAC_GROUP, RRG_KNOB_PAIR_UNIT, RRG_KNOB_FAC_STAGE = 1, 2, 3, 4
 
 STATUS_NAMES = {0: "RRG_OK", 1: "RRG_E_INVALID", 2: "RRG_E_CUDA", 3: "RRG_E_NO_DEVICE", 4: "RRG_E_TIMEOUT",
                 5: "RRG_E_TOO_LARGE", 6: "RRG_E_OOM", 7: "RRG_E_DEVICE_FAULT"}

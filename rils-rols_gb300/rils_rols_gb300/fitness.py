@@ -249,12 +249,10 @@ def result_dtype() -> np.dtype:
 
 
 # ------------------------------------------------------ launch-shape tuner --
-QR_WARPS = _lib.RRG_KNOB_QR_WARPS
 EVAL_WAVES = _lib.RRG_KNOB_EVAL_WAVES
 FAC_GROUP = _lib.RRG_KNOB_FAC_GROUP
 PAIR_UNIT = _lib.RRG_KNOB_PAIR_UNIT
 FAC_STAGE = _lib.RRG_KNOB_FAC_STAGE
-QR_LIST_WARPS = _lib.RRG_KNOB_QR_LIST_WARPS
 
 
 def tune_mode(on: bool) -> None:

@@ -1,11 +1,9 @@
 """Device fitness path against the oracle and the reference's golden vectors.
 
-Plain FP64, one block per candidate (every round whose rows fit one block's
-pass, which is every round of the search on small data): bit-identical to the
-oracle, which is bit-identical to the reference.  Plain FP64 through the tiled
-QR (tall data, few candidates): every fitness within 1e-10 relative, same
-size, same NaN sentinel.  Mixed: penalised fitness within the tolerances
-below of the FP64 oracle.
+Plain FP64 (one block per candidate while the rows fit one chunk, the
+chunked passes beyond): bit-identical to the oracle, which is bit-identical
+to the reference built with the same reduction order.  Mixed: penalised
+fitness within the tolerances below of the FP64 oracle.
 """
 import numpy as np
 import pytest
@@ -105,13 +103,19 @@ def test_plain_bit_exact_with_golden(ctx, golden, name):
                 assert same_bits(dev["coefs"][i], ora["coefs"][i]), trees[i]
 
 
-def test_plain_tall_tsqr_matches_oracle(ctx):
-    # n >= 65536 with few candidates takes the tiled (TSQR) path
+def test_plain_tall_few_candidates_bit_exact(ctx):
+    # tall rows, few candidates: the chunked QR passes spread each candidate
+    # over the GPU in the oracle's summation order
     X, y, trees, _ = synth.batched_fitness(n=100_000, d=5, n_trees=24, seed=3, max_size=25)
     ds = ctx.dataset(X, y)
     ods = pyoracle.OracleDataset(X, y)
     b = encode(trees, tuned=True)
-    check_plain(ds.evaluate(b, PLAIN), ods.evaluate(b, threads=8), "tsqr")
+    dev, ora = ds.evaluate(b, PLAIN), ods.evaluate(b, threads=8)
+    check_plain(dev, ora, "tall")
+    for f in ("loss", "rmse", "rank"):
+        assert same_bits(dev[f], ora[f]), f
+    for i in range(len(trees)):
+        assert same_bits(dev["coefs"][i], ora["coefs"][i]), trees[i]
 
 
 def test_plain_batched_medium_bit_exact(ctx):

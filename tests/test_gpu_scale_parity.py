@@ -10,13 +10,11 @@ as the benchmark does, and a seeded sample of the candidates is compared:
 * the 1M-row regression search: its eight local-search rounds, one call per
   round, 96 candidates checked.
 
-Plain FP64 must be bit-identical to the oracle where the round solves by
-the direct QR; a round of fewer distinct candidates than twice the GPU's SMs
-on tall data (round 0 of the 1M-row search: 264 candidates) solves by the
-tiled QR instead (rrg_last_round_stats [17]), whose penalised fitness and
-RMSE are within 1e-10 relative with the same size, rank and sentinel.  The certified mixed form must be within 1e-6 relative in
-the penalised fitness with the same NaN sentinels, and the sample's best
-candidate the same.
+Plain FP64 must be bit-identical to the oracle in every round, whatever its
+size (round 0 of the 1M-row search has 264 candidates, the batched round
+8192; every QR runs in the same QSUM order).  The certified mixed form must
+be within 1e-6 relative in the penalised fitness with the same NaN
+sentinels, and the sample's best candidate the same.
 """
 import gzip
 import os
@@ -44,23 +42,14 @@ def pick(out, idx):
     return {k: np.asarray(v)[idx] for k, v in out.items() if k != "coefs"}
 
 
-REL_TILED = 1e-10
-
-
-def check(dev_plain, dev_cert, ora, tag, tiled=None):
-    # plain FP64: bit for bit, except candidates of tiled rounds (1e-10)
-    tiled = np.zeros(len(ora["loss"]), dtype=bool) if tiled is None else tiled
+def check(dev_plain, dev_cert, ora, tag):
+    # plain FP64: bit for bit
     for f in ("size", "rank"):
         assert np.array_equal(dev_plain[f], ora[f]), (tag, f)
     for f in ("loss", "rmse"):
         a, b = dev_plain[f], ora[f]
         exact = (a == b) | ((a != a) & (b != b))
-        assert np.all(exact | tiled), (tag, f, np.flatnonzero(~exact & ~tiled)[:5])
-    # tiled rounds: the penalised fitness and the RMSE within 1e-10 relative
-    fin = tiled & (ora["loss"] != 1000)
-    for a, b in ((fval(dev_plain), fval(ora)), (dev_plain["rmse"], ora["rmse"])):
-        err = np.abs(a[fin] - b[fin]) / np.maximum(np.abs(b[fin]), 1e-300)
-        assert np.all(err <= REL_TILED), (tag, float(err.max()) if len(err) else 0.0)
+        assert np.all(exact), (tag, f, np.flatnonzero(~exact)[:5])
     assert np.array_equal(dev_plain["loss"] == 1000, ora["loss"] == 1000), tag
     # certified: same sentinels, fitness within 1e-6
     sent = ora["loss"] == 1000
@@ -97,17 +86,15 @@ def test_regression_1m_rounds(ctx):
         r, t = line.split("\t")
         rounds.setdefault(int(r), []).append(t)
     ds = ctx.dataset(X, y)
-    plain, cert, trees, tiled = [], [], [], []
+    plain, cert, trees = [], [], []
     for r in sorted(rounds):
         b = encode(rounds[r], tuned=True)
         plain.append(ds.evaluate(b, PLAIN))
-        tiled.append(np.full(len(rounds[r]), ctx.last_round_stats()["tiled_qr"]))
         cert.append(ds.evaluate(b, CERTIFIED))
         trees += rounds[r]
     cat = lambda outs: {k: np.concatenate([o[k] for o in outs]) for k in ("loss", "rmse", "size", "rank")}  # noqa
     plain, cert = cat(plain), cat(cert)
-    tiled_round = np.concatenate(tiled)
     idx = np.sort(np.random.default_rng(22).choice(len(trees), 96, replace=False))
     ora = pyoracle.OracleDataset(X, y).evaluate(tree_encode.encode([trees[i] for i in idx]), threads=THREADS)
-    check(pick(plain, idx), pick(cert, idx), ora, "1M-row local-search rounds", tiled=tiled_round[idx])
+    check(pick(plain, idx), pick(cert, idx), ora, "1M-row local-search rounds")
     ds.close()
