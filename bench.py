@@ -30,6 +30,17 @@ kernel, the CPU oracle timed on the host cores, clocks.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
                   [--serve-jobs J] [--serve-only] [--quick]
+
+Measurement cases for profiling (one JSON line each, no bench contract):
+  --round-only R        round R of the headline workload, certified, once
+                        (with RRG_TUNE_CACHE set, no launch-shape trials):
+                        its phase times, algorithmic bytes and launches;
+  --case NAME --fac-stage S
+                        the double-float factor evaluator with X and y read
+                        from global memory (S = 1) or staged in shared memory
+                        by tensor copies (S = 2): local_search_d5 (the eight
+                        rounds), random_d10 / random_d20 (1500 random trees,
+                        n rows, d = 10 / 20); per step its time and the round's.
 """
 from __future__ import annotations
 
@@ -583,7 +594,7 @@ PHASE_KERNELS = {
     "factor_eval": "fac_eval_kernel (double-float factor table)",
     "pair_sums": "pair_sum_kernel",
     "fp64_eval": "plain_eval_kernel (FP64 table)",
-    "fp64_qr": "plain_qr_cluster_kernel (direct column-pivoted QR, FP64, 8-CTA clusters)",
+    "fp64_qr": "qr_passA_kernel + qr_sums_kernel (column-pivoted QR, FP64, chunked passes over the GPU)",
 }
 
 
@@ -709,6 +720,68 @@ def run_reference(args):
                       "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
 
 
+def round_only(args):
+    """One headline round, certified, on a fresh context: phase times (CUDA
+    events), the library's algorithmic bytes and the kernels launched."""
+    import torch
+    from rils_rols_gb300.fitness import CERTIFIED, Context, encode
+    X, y = regression_data(args.n)
+    rounds = load_rounds()
+    ctx = Context(0)
+    ds = ctx.dataset(X, y)
+    b = encode(rounds[args.round_only], tuned=True)
+    torch.cuda.synchronize()
+    ctx.set_timing(True)
+    ds.evaluate(b, CERTIFIED)
+    ctx.set_timing(False)
+    out = {"round": args.round_only, "candidates": len(rounds[args.round_only]), "n": args.n,
+           "phase_ms": {k: v[0] for k, v in ctx.last_round_timing().items() if v[0] > 0},
+           "phase_bytes": {k: v for k, v in ctx.last_round_bytes().items() if v > 0},
+           "launches": ctx.last_round_launches(), "stats": ctx.last_round_stats()}
+    ds.close()
+    ctx.close()
+    print(json.dumps(out))
+
+
+def eval_case(args):
+    """The double-float factor evaluator on a named case with the tensor-copy
+    staging knob pinned (1: X and y from global memory, 2: staged)."""
+    from rils_rols_gb300 import synth
+    from rils_rols_gb300.fitness import CERTIFIED, FAC_STAGE, Context, encode, tune_pin
+    if args.case == "local_search_d5":
+        X, y = regression_data(args.n)
+        batches = [encode(r, tuned=True) for r in load_rounds()]
+    else:
+        d = 10 if args.case == "random_d10" else 20
+        rng = np.random.default_rng(SEED)
+        X = rng.standard_normal((args.n, d))
+        _, y = synth.finite_target(rng, X, 15)
+        y = y + rng.normal(0, 0.01 * np.std(y), args.n)
+        batches = [encode([synth.random_tree(rng, int(rng.integers(3, 30)), d) for _ in range(1500)], tuned=True)]
+    d = X.shape[1]
+    if args.fac_stage:
+        tune_pin(FAC_STAGE, min(d, 64), args.fac_stage)
+    ctx = Context(0)
+    ctx.set_mixed_min_rows(0)
+    ds = ctx.dataset(X, y)
+    for b in batches:
+        ds.evaluate(b, CERTIFIED)
+    steps = []
+    for _ in range(max(1, args.steps)):
+        ctx.set_timing(True)
+        fe, tot = 0.0, 0.0
+        for b in batches:
+            t = time.perf_counter()
+            ds.evaluate(b, CERTIFIED)
+            tot += time.perf_counter() - t
+            fe += ctx.last_round_timing()["factor_eval"][0]
+        ctx.set_timing(False)
+        steps.append({"factor_eval_ms": fe, "rounds_ms": 1e3 * tot})
+    ds.close()
+    ctx.close()
+    print(json.dumps({"case": args.case, "n": args.n, "d": d, "fac_stage": args.fac_stage, "steps": steps}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -731,7 +804,18 @@ def main():
     ap.add_argument("--cls-fit-calls", type=int, default=20000,
                     help="max_fit_calls of the 200k-row classifier fits (0: no classifier leg)")
     ap.add_argument("--cls-only", action="store_true", help="only the classifier leg")
+    ap.add_argument("--round-only", type=int, default=-1, help="one headline round alone (profiling)")
+    ap.add_argument("--case", choices=["local_search_d5", "random_d10", "random_d20"],
+                    help="the factor evaluator on a named case (profiling)")
+    ap.add_argument("--fac-stage", type=int, default=0, choices=[0, 1, 2],
+                    help="with --case: 1 reads X and y from global memory, 2 stages them by tensor copies")
     args = ap.parse_args()
+    if args.round_only >= 0:
+        round_only(args)
+        return
+    if args.case:
+        eval_case(args)
+        return
     if args.serve_only:
         print(json.dumps(serving_leg(args)))
         return

@@ -40,7 +40,7 @@ constexpr int kResidThreads = 256;
 // chunk of the features its group reads, and of y, into shared memory with
 // tensor copies (cp.async.bulk.tensor, boxes of kTmaRows rows of one
 // feature) and evaluates from there; the same arithmetic on the same rows.
-constexpr int kFacStageMax = 16;  // features one staged group may read
+constexpr int kFacStageMax = 64;  // features one staged group may read (shared memory decides first)
 constexpr int kTmaRows = 256;     // rows per tensor-copy box
 
 // Self pairs of factor f sit at pair index 3f (f*f), 3f+1 (f*1), 3f+2 (f*y);

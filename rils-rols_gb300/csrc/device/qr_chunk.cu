@@ -649,7 +649,7 @@ __global__ void qr_solve_kernel(QrJob j) {
 
 template <int CG>
 bool launch_passes(const QrJob& job, int blocks, cudaStream_t st, int64_t* launches) {
-  const int steps = job.max_cols - 1;
+  const int steps = job.max_steps > 0 && job.max_steps < job.max_cols ? job.max_steps : job.max_cols - 1;
   // tickets (and every other field) start at zero
   if (cudaMemsetAsync(job.state, 0, sizeof(QrState) * (size_t)job.n_list, st) != cudaSuccess) {
     cudaGetLastError();

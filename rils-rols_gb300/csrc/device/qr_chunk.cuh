@@ -54,6 +54,7 @@ struct QrJob {
   uint32_t* status;
   int count_bytes;  // add the algorithmic bytes to the status block
   int max_cols;     // bound on k + 1 over the job's candidates (<= kQrMaxCols)
+  int max_steps;    // bound on the steps (k) over them; 0: max_cols - 1
   int nch;          // row chunks: ceil(n / RR_CHUNK)
   QrState* state;   // n_list entries
   double* part;     // n_list * (nch + 1) * max_cols chunk totals

@@ -887,21 +887,29 @@ rrg_status rrg_context::mixed_subround(const rrg_dataset* ds, const int32_t* lis
     const size_t col8 = sizeof(double) * (size_t)ds->n_pad;
     const size_t n_all = host_cands.size();
     static const int kBucketCols[kQrBuckets] = {4, 8, 16, RRG_MAX_TERMS + 1};
-    int bucket_cap[kQrBuckets] = {0, 0, 0, 0};
+    int bucket_cap[kQrBuckets] = {0, 0, 0, 0}, bucket_wide[kQrBuckets] = {0, 0, 0, 0};
     for (int32_t li = 0; li < cnt; ++li) {
       const rrg_cand& cd = host_cands[list[li]];
       if (cd.mode != RRG_TUNED) continue;
       const int cols = cd.n_factors + 2;
-      ++bucket_cap[cols <= 4 ? 0 : (cols <= 8 ? 1 : (cols <= 16 ? 2 : 3))];
+      const int q = cols <= 4 ? 0 : (cols <= 8 ? 1 : (cols <= 16 ? 2 : 3));
+      ++bucket_cap[q];
+      bucket_wide[q] = std::max(bucket_wide[q], cols);
     }
     // working columns of the QR: each bucket factorises up to qbatch[q] of
     // its candidates at a time (in order, as many batches as its capacity
     // needs), the buckets sharing half the scratch budget in proportion to
     // their capacities
     const int64_t nch = (ds->n + RR_CHUNK - 1) / RR_CHUNK;
-    double slot_need = 0.0;
-    for (int q = 0; q < kQrBuckets; ++q) slot_need += (double)bucket_cap[q] * kBucketCols[q] * (double)col8;
-    const double share = slot_need > 0.0 ? std::min(1.0, (double)scratch_budget_bytes / 2 / slot_need) : 1.0;
+    // (room for one candidate per bucket is set aside first, so that the
+    // rounded-down shares and that minimum stay within the half together)
+    double slot_need = 0.0, slot_min = 0.0;
+    for (int q = 0; q < kQrBuckets; ++q) {
+      slot_need += (double)bucket_cap[q] * kBucketCols[q] * (double)col8;
+      if (bucket_cap[q]) slot_min += (double)kBucketCols[q] * (double)col8;
+    }
+    const double room = std::max(0.0, (double)scratch_budget_bytes / 2 - slot_min);
+    const double share = slot_need > 0.0 ? std::min(1.0, room / slot_need) : 1.0;
     int qbatch[kQrBuckets] = {0, 0, 0, 0};
     size_t m_cols = 0, q_bytes = 0;
     for (int q = 0; q < kQrBuckets; ++q) {
@@ -1122,6 +1130,7 @@ rrg_status rrg_context::mixed_subround(const rrg_dataset* ds, const int32_t* lis
           jb.status = status;
           jb.count_bytes = 1;
           jb.max_cols = kBucketCols[q];
+          jb.max_steps = bucket_wide[q] - 1;
           qr_chunk_bind(jb, static_cast<char*>(d_qrs.ptr) + q_off);
           if (!launch_qr_chunked(jb, qr_blocks(kBucketCols[q], (int64_t)qbatch[q] * nch), sq, &launches)) {
             cuda_ok(cudaGetLastError(), "QR launch");
@@ -1456,7 +1465,7 @@ rrg_status rrg_context::run_fp64_table(const rrg_dataset* ds, const std::vector<
       // chunk, otherwise the chunked passes over the whole GPU (same bits)
       struct QrRun {
         int32_t b0, b1;
-        int bk;
+        int bk, wide;
         size_t off;
       };
       std::vector<QrRun> runs;
@@ -1465,8 +1474,13 @@ rrg_status rrg_context::run_fp64_table(const rrg_dataset* ds, const std::vector<
       for (int32_t b0 = sb.first; b0 < sb.second;) {
         const int bk = bucket(list[pos + b0]);
         int32_t b1 = b0;
-        while (b1 < sb.second && bucket(list[pos + b1]) == bk) ++b1;
-        runs.push_back({b0, b1, bk, qbytes});
+        int wide = 2;
+        while (b1 < sb.second && bucket(list[pos + b1]) == bk) {
+          const rrg_cand& cd = host_cands[list[pos + b1]];
+          if (cd.mode == RRG_TUNED) wide = std::max(wide, cd.n_factors + 2);
+          ++b1;
+        }
+        runs.push_back({b0, b1, bk, wide, qbytes});
         if (chunked) qbytes += (size_t)round_up((int64_t)qr_chunk_scratch_bytes(b1 - b0, ds->n, bk), 256);
         b0 = b1;
       }
@@ -1502,6 +1516,7 @@ rrg_status rrg_context::run_fp64_table(const rrg_dataset* ds, const std::vector<
           jb.status = status;
           jb.count_bytes = 1;
           jb.max_cols = r.bk;
+          jb.max_steps = r.wide - 1;
           qr_chunk_bind(jb, static_cast<char*>(d_qrs.ptr) + r.off);
           ok = launch_qr_chunked(jb, qr_blocks(r.bk, (int64_t)jb.n_list * jb.nch), s, &launches);
         }
