@@ -170,6 +170,19 @@ __device__ __forceinline__ void lane_rows(int64_t r0, int64_t lo, int64_t hi, F&
   }
 }
 
+// Rows of this thread's lane in sub-chunks of kSub rows (kSubU per lane):
+// body(s0, full) for each sub-chunk of the item in order; `full` when every
+// row of the sub-chunk is in [lo, hi).
+constexpr int kSub = 2048;
+constexpr int kSubU = kSub / 256;
+template <class F>
+__device__ __forceinline__ void sub_chunks(int64_t r0, int64_t lo, int64_t hi, F&& body) {
+  for (int64_t s0 = r0; s0 < r0 + kQC && s0 < hi; s0 += kSub) {
+    if (s0 + kSub <= lo) continue;
+    body(s0, s0 >= lo && s0 + kSub <= hi);
+  }
+}
+
 // Reads the item's state into V (thread 0).  kk < 0: the copy pass.
 __device__ void load_view(ItemView& V, const QrJob& j, int t, int ch, int kk, int pass_a) {
   QrState* S = j.state + t;
@@ -236,18 +249,21 @@ __device__ void load_view(ItemView& V, const QrJob& j, int t, int ch, int kk, in
 // ------------------------------------------------------- init and B(kk) ----
 // INIT: the copy pass (kk = -1).  Otherwise the rank-1 update of step kk and
 // the sums step kk + 1 needs.
-// Resident blocks the passes are compiled for (registers per thread <= 64K / (256 x blocks)).
-template <int CG>
+// Resident blocks the passes are compiled for (registers per thread <= 64K /
+// (256 x blocks)): the step passes stream columns with little register
+// state; the copy pass (run once) keeps a group's sources and sums.
+template <int CG, bool INIT = false>
 struct QrMinBlocks {
-  static constexpr int value = CG <= 8 ? 3 : 2;
+  static constexpr int value = CG <= 8 ? (INIT ? 3 : 4) : 2;
 };
 
 template <int CG, bool INIT>
-__global__ void __launch_bounds__(256, QrMinBlocks<CG>::value) qr_sums_kernel(QrJob j, int kk) {
+__global__ void __launch_bounds__(256, (QrMinBlocks<CG, INIT>::value)) qr_sums_kernel(QrJob j, int kk) {
   __shared__ ItemView V;
   __shared__ double red[8 * CG], outA[CG], outB[CG];
   __shared__ int s_flag;
   __shared__ double s_norm[kQrMaxCols], s_tail[kQrMaxCols];
+  __shared__ double sbuf[kSub];  // pass B: tau v_i of a sub-chunk (lane-owned entries)
   const int cnt = job_count(j);
   const int64_t items = (int64_t)cnt * j.nch;
   const int64_t rows = j.ds.n;
@@ -350,23 +366,41 @@ __global__ void __launch_bounds__(256, QrMinBlocks<CG>::value) qr_sums_kernel(Qr
       const int fq = V.fastq;
       double sf = 0.0;  // the summed column's chain, formed during the update
       if (V.upd) {
+        // tau v_i of a sub-chunk's rows staged in shared memory (each thread
+        // reads back only its own lane's entries), then each column streamed
+        // on its own: its loads are independent of the other columns' stores
         for (int g0 = 0; g0 < V.nwork; g0 += CG) {
           const int gc = V.nwork - g0 < CG ? V.nwork - g0 : CG;
-          const int fg = fq - g0;  // the summed column's place in this group (if in [0, gc))
-          lane_rows(r0, V.lo, V.hi, [&](int64_t i) {
-            // every load first, then the arithmetic and the stores
-            double a[CG];
-            const double tv = __dmul_rn(tau, vcol[i]);
-  #pragma unroll
-            for (int q = 0; q < CG; ++q)
-              if (q < gc) a[q] = Mb[(int64_t)V.work[g0 + q] * np + i];
-  #pragma unroll
-            for (int q = 0; q < CG; ++q)
-              if (q < gc) {
-                a[q] = __fma_rn(tv, V.ntmp[g0 + q], a[q]);
-                Mb[(int64_t)V.work[g0 + q] * np + i] = a[q];
-                if (q == fg) sf = __fma_rn(a[q], a[q], sf);
+          sub_chunks(r0, V.lo, V.hi, [&](int64_t s0, bool full) {
+#pragma unroll
+            for (int u = 0; u < kSubU; ++u) {
+              const int64_t i = s0 + threadIdx.x + 256 * u;
+              sbuf[threadIdx.x + 256 * u] = (full || (i >= V.lo && i < V.hi)) ? __dmul_rn(tau, vcol[i]) : 0.0;
+            }
+#pragma unroll
+            for (int q = 0; q < CG; ++q) {
+              if (q >= gc) break;
+              double* col = Mb + (int64_t)V.work[g0 + q] * np;
+              const double nt = V.ntmp[g0 + q];
+              const bool fsum = g0 + q == fq;
+              if (full) {
+#pragma unroll
+                for (int u = 0; u < kSubU; ++u) {
+                  const int64_t i = s0 + threadIdx.x + 256 * u;
+                  const double a = __fma_rn(sbuf[threadIdx.x + 256 * u], nt, col[i]);
+                  col[i] = a;
+                  if (fsum) sf = __fma_rn(a, a, sf);
+                }
+              } else {
+                for (int u = 0; u < kSubU; ++u) {
+                  const int64_t i = s0 + threadIdx.x + 256 * u;
+                  if (i < V.lo || i >= V.hi) continue;
+                  const double a = __fma_rn(sbuf[threadIdx.x + 256 * u], nt, col[i]);
+                  col[i] = a;
+                  if (fsum) sf = __fma_rn(a, a, sf);
+                }
               }
+            }
           });
         }
       }
@@ -482,6 +516,7 @@ __global__ void __launch_bounds__(256, QrMinBlocks<CG>::value) qr_passA_kernel(Q
   __shared__ ItemView V;
   __shared__ double red[8 * CG], outA[CG];
   __shared__ int s_flag;
+  __shared__ double sbuf[kSub];  // v_i of a sub-chunk (lane-owned entries)
   const int cnt = job_count(j);
   const int64_t items = (int64_t)cnt * j.nch;
   const int64_t rows = j.ds.n;
@@ -506,34 +541,43 @@ __global__ void __launch_bounds__(256, QrMinBlocks<CG>::value) qr_passA_kernel(Q
     }
     for (int g0 = 0; g0 < V.nwork; g0 += CG) {
       const int gc = V.nwork - g0 < CG ? V.nwork - g0 : CG;
-      const double* cp[CG];
       double pa[CG];
 #pragma unroll
-      for (int q = 0; q < CG; ++q) {
-        cp[q] = q < gc ? wcol(j, t, c, V.work[g0 + q]) : nullptr;
-        pa[q] = 0.0;
-      }
+      for (int q = 0; q < CG; ++q) pa[q] = 0.0;
       const bool first = g0 == 0;
-      auto load = [&](int64_t i, double (&a)[CG], double& p) {
-        p = pcol[i];
+      sub_chunks(r0, V.lo, V.hi, [&](int64_t s0, bool full) {
+        // the sub-chunk's v_i (divided once, by the first group) staged in
+        // shared memory; then each column's dot chain on its own
 #pragma unroll
-        for (int q = 0; q < CG; ++q)
-          if (q < gc) a[q] = cp[q][i];
-      };
-      auto finish = [&](int64_t i, const double (&a)[CG], double p) {
-        double v = p;
-        if (first) {
-          v = div_by(p, den, rden);
-          pcol[i] = v;
+        for (int u = 0; u < kSubU; ++u) {
+          const int64_t i = s0 + threadIdx.x + 256 * u;
+          double v = 0.0;
+          if (full || (i >= V.lo && i < V.hi)) {
+            v = pcol[i];
+            if (first) {
+              v = div_by(v, den, rden);
+              pcol[i] = v;
+            }
+          }
+          sbuf[threadIdx.x + 256 * u] = v;
         }
 #pragma unroll
-        for (int q = 0; q < CG; ++q)
-          if (q < gc) pa[q] = __fma_rn(v, a[q], pa[q]);
-      };
-      lane_rows(r0, V.lo, V.hi, [&](int64_t i) {
-        double a[CG], p;
-        load(i, a, p);
-        finish(i, a, p);
+        for (int q = 0; q < CG; ++q) {
+          if (q >= gc) break;
+          const double* col = wcol(j, t, c, V.work[g0 + q]);
+          double acc = pa[q];
+          if (full) {
+#pragma unroll
+            for (int u = 0; u < kSubU; ++u)
+              acc = __fma_rn(sbuf[threadIdx.x + 256 * u], col[s0 + threadIdx.x + 256 * u], acc);
+          } else {
+            for (int u = 0; u < kSubU; ++u) {
+              const int64_t i = s0 + threadIdx.x + 256 * u;
+              if (i >= V.lo && i < V.hi) acc = __fma_rn(sbuf[threadIdx.x + 256 * u], col[i], acc);
+            }
+          }
+          pa[q] = acc;
+        }
       });
       fold_lanes<CG>(pa, gc, red, outA);
       if (threadIdx.x < gc) *part_at(j, t, ch, g0 + threadIdx.x) = outA[threadIdx.x];
