@@ -245,7 +245,9 @@ def timed_rounds(ctx, ds, batches, prec, stream, flush):
     (rrg_round_submit + rrg_round_wait: host staging, every launch, results
     back in host memory), the whole step bracketed by CUDA events on the
     library's stream after an L2 flush; results are turned into Python
-    objects after the timed region."""
+    objects after the timed region.  A step is one search's rounds: the
+    column cache starts empty (cleared inside the timed region), so only the
+    step's later rounds read columns its earlier rounds evaluated."""
     import torch
 
     from rils_rols_gb300.fitness import decode_results, result_dtype
@@ -255,6 +257,7 @@ def timed_rounds(ctx, ds, batches, prec, stream, flush):
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
+    ctx.clear_column_cache()
     for b, (res, coefs) in zip(batches, bufs):
         ds.submit(b, prec, res, coefs)
         ds.wait()
@@ -289,6 +292,7 @@ def run_ours(args):
         """Per-phase device time, bytes, launches and statistics of one step,
         round by round (a separate, untimed pass with per-launch events)."""
         ctx.set_timing(True)
+        ctx.clear_column_cache()
         pm, pb, launches, stats = {}, {}, 0, []
         for b in bs:
             ds.evaluate(b, prec)
@@ -302,6 +306,7 @@ def run_ours(args):
         return pm, pb, launches, stats
 
     for _ in range(args.warmup):
+        ctx.clear_column_cache()
         for b in batches:
             ds.evaluate(b, CERTIFIED)
     barrier(world)
@@ -362,9 +367,21 @@ def run_ours(args):
     res["rows_nodes_per_s"] = nodes * float(args.n) * args.steps * world / t_max
     res["clocks"] = clk.summary()
     res["autotune"] = tune_report()
+    res["column_cache"] = {
+        "mode": "on (the library default), emptied at the start of every step: rounds 2-8 of a step read the "
+                "factor columns that its earlier rounds evaluated, as the rounds of one search do",
+        "double_float_columns_read": sum(st["cache_hits"] for st in stats),
+        "double_float_columns_evaluated": sum(st["cache_evals"] for st in stats),
+        "fp64_columns_read": sum(st["cache64_hits"] for st in stats),
+        "fp64_columns_evaluated": sum(st["cache64_evals"] for st in stats)}
     if args.quick:
         print(json.dumps(res))
         return
+    # the same steps with the cache off: every round evaluates all its factors
+    ctx.set_column_cache(False)
+    ntimes = [timed_rounds(ctx, ds, batches, CERTIFIED, stream, flush)[0] for _ in range(max(2, args.steps // 2))]
+    ctx.set_column_cache(True)
+    res["column_cache"]["off_evals_per_s"] = B * len(ntimes) / sum(ntimes)
     # the eight rounds concatenated into one batch (one call)
     allb = encode(trees, tuned=True)
     ctimes = [timed_rounds(ctx, ds, [allb], CERTIFIED, stream, flush)[0] for _ in range(max(2, args.steps // 2))]
@@ -378,8 +395,10 @@ def run_ours(args):
     mixed = concat_results(mixed_rounds)
     res["mixed_uncertified"] = {"evals_per_s": B * len(mtimes) / sum(mtimes),
                                 "note": "no FP64 re-scoring: fitness errors above 1e-6 occur, see accuracy_vs_fp64"}
-    # plain FP64: unbatched launches (one candidate per round) and the rounds
+    # plain FP64: unbatched launches (one candidate per round, no column
+    # cache: each candidate evaluated on its own) and the rounds
     singles = [encode([t], tuned=True) for t in trees[:args.unbatched_sample]]
+    ctx.set_column_cache(False)
     ds.evaluate(singles[0], PLAIN)
     torch.cuda.synchronize()
     t = time.perf_counter()
@@ -387,6 +406,7 @@ def run_ours(args):
         ds.evaluate(s1, PLAIN)
     torch.cuda.synchronize()
     unbatched = len(singles) / (time.perf_counter() - t)
+    ctx.set_column_cache(True)
     ptimes = []
     for _ in range(2):
         dt, plain_rounds = timed_rounds(ctx, ds, batches, PLAIN, stream, flush)
@@ -766,6 +786,7 @@ def eval_case(args):
         tune_pin(FAC_STAGE, min(d, 64), args.fac_stage)
     ctx = Context(0)
     ctx.set_mixed_min_rows(0)
+    ctx.set_column_cache(False)  # every step evaluates every factor: the evaluator is what is timed
     ds = ctx.dataset(X, y)
     for b in batches:
         ds.evaluate(b, CERTIFIED)

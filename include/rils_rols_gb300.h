@@ -239,7 +239,10 @@ int64_t rrg_last_round_launches(const rrg_context* ctx);
  *   candidates scored after merging those with identical factor lists.
  *   [17] 0 (formerly a tiled-QR flag: every round now solves by the direct
  *   column-pivoted QR, bit-identical to the oracle).  [18] 1 when the last
- *   round ran as a CUDA graph (rrg_context_set_graph).
+ *   round ran as a CUDA graph (rrg_context_set_graph).  [19] double-float
+ *   factor columns read from the column cache (rrg_context_set_column_cache)
+ *   [20] double-float table columns evaluated  [21] FP64 factor columns read
+ *   from the column cache  [22] FP64 table columns evaluated.
  * Returns the count written. */
 int32_t rrg_last_round_stats(const rrg_context* ctx, int64_t* out, int32_t n);
 
@@ -249,6 +252,21 @@ int32_t rrg_last_round_stats(const rrg_context* ctx, int64_t* out, int32_t n);
  * several contexts on one device (the serving loop) set them explicitly.
  * No counterpart in the reference (single-threaded, one fit per process). */
 rrg_status rrg_context_set_limits(rrg_context* ctx, int64_t scratch_bytes, int64_t table_bytes);
+
+/* Keep factor columns on the device across rounds (on by default).  A
+ * factor column is a function of the factor's program (constants by value)
+ * and of the dataset alone, and the consecutive rounds of a search share
+ * most factors, so a round reads the columns an earlier round on the same
+ * dataset evaluated instead of evaluating them again: the double-float
+ * columns of mixed rounds (with their sums and probe records) and the FP64
+ * columns of FP64 rounds, within the limits of rrg_context_set_limits, least
+ * recently used columns replaced first.  Results are the same bits either
+ * way.  Switching clears what is kept; so do destroying the dataset, a round
+ * on another dataset and a failed round.  RRG_E_INVALID while a round is in
+ * flight.  No counterpart in the reference. */
+rrg_status rrg_context_set_column_cache(rrg_context* ctx, int32_t on);
+/* Forget every kept column (the next round evaluates all its factors). */
+rrg_status rrg_context_clear_column_cache(rrg_context* ctx);
 
 /* How a mixed or certified round decides its second half.  On (the
  * default): on the device, from the solve's flags (the residual-pass list,

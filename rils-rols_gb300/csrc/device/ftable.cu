@@ -369,6 +369,7 @@ __global__ void __launch_bounds__(kFacThreads) fac_eval_kernel(const __grid_cons
   float4* st = stk + (size_t)warp * kMixedStackCap * 32 * 2 + lane;
   for (int i = 0; i < grp.y; ++i) {
     const int f = grp.x + i;
+    const int64_t fw = a.wcol ? a.wcol[f] : f;  // the column it writes
     const int2 mt = a.meta[f];
     const uint32_t* code = code_s + (mt.x - base);
     dfl ff = dfl_make(0.f, 0.f), fs = ff, fy = ff;
@@ -388,9 +389,9 @@ __global__ void __launch_bounds__(kFacThreads) fac_eval_kernel(const __grid_cons
         for (int u = 0; u < R; ++u)
           if (gr + u >= n) v[u] = dfl_make(0.f, 0.f);
       }
-      *reinterpret_cast<float4*>(a.F + (int64_t)f * n_pad + gr) = make_float4(v[0].hi, v[0].lo, v[1].hi, v[1].lo);
+      *reinterpret_cast<float4*>(a.F + fw * n_pad + gr) = make_float4(v[0].hi, v[0].lo, v[1].hi, v[1].lo);
       if constexpr (R == 4)
-        *reinterpret_cast<float4*>(a.F + (int64_t)f * n_pad + gr + 2) = make_float4(v[2].hi, v[2].lo, v[3].hi, v[3].lo);
+        *reinterpret_cast<float4*>(a.F + fw * n_pad + gr + 2) = make_float4(v[2].hi, v[2].lo, v[3].hi, v[3].lo);
       dfl y[4];
       if constexpr (R == 4) {
         const float4 yhv = *reinterpret_cast<const float4*>(yh + r);
@@ -438,7 +439,7 @@ __global__ void __launch_bounds__(kFacThreads) fac_eval_kernel(const __grid_cons
       const unsigned long long other = __shfl_xor_sync(0xffffffffu, first, o);
       first = other < first ? other : first;
     }
-    if (lane == 0 && first != ~0ull) atomicMin(a.fnan + f, first);
+    if (lane == 0 && first != ~0ull) atomicMin(a.fnan + fw, first);
     const dfl s0 = warp_dfl_sum(dfl_renorm(ff)), s1 = warp_dfl_sum(dfl_renorm(fs)), s2 = warp_dfl_sum(dfl_renorm(fy));
     if (lane == 0) {
       float* rw = red + warp * 6;
@@ -508,7 +509,7 @@ __global__ void __launch_bounds__(kPairThreads) pair_sum_kernel(PairArgs a) {
 
 // psum[p] = sum over chunks q (in order) of P[q][p], in FP64.
 __global__ void pair_reduce_kernel(const float2* P, int32_t n_pairs, int32_t n_chunks, int32_t p0, int32_t p1,
-                                   double* psum) {
+                                   double* psum, const int32_t* smap) {
   const int p = p0 + blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= p1) return;
   double s = 0.0;
@@ -516,7 +517,14 @@ __global__ void pair_reduce_kernel(const float2* P, int32_t n_pairs, int32_t n_c
     const float2 v = P[(size_t)q * n_pairs + p];
     s = __dadd_rn(s, __dadd_rn((double)v.x, (double)v.y));
   }
-  psum[p] = s;
+  psum[smap ? 3 * (int64_t)smap[p / 3] + p % 3 : (int64_t)p] = s;
+}
+
+__global__ void fill_slots_kernel(const int32_t* idx, int32_t n, unsigned long long* dst, int words,
+                                  unsigned long long v) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n)
+    for (int w = 0; w < words; ++w) dst[(int64_t)idx[i] * words + w] = v;
 }
 
 // The candidates of the residual pass have finite table values (the solve sends
@@ -683,10 +691,16 @@ bool launch_pair_sum(const PairArgs& a, int n_super, cudaStream_t st) {
   return launch_ok("launch_pair_sum");
 }
 bool launch_pair_reduce(const float2* P, int32_t n_pairs, int32_t n_chunks, int32_t p0, int32_t p1, double* psum,
-                        cudaStream_t st) {
+                        cudaStream_t st, const int32_t* smap) {
   if (p1 <= p0) return true;
-  pair_reduce_kernel<<<(p1 - p0 + 255) / 256, 256, 0, st>>>(P, n_pairs, n_chunks, p0, p1, psum);
+  pair_reduce_kernel<<<(p1 - p0 + 255) / 256, 256, 0, st>>>(P, n_pairs, n_chunks, p0, p1, psum, smap);
   return launch_ok("launch_pair_reduce");
+}
+bool launch_fill_slots(const int32_t* idx, int32_t n, unsigned long long* dst, int words, unsigned long long v,
+                       cudaStream_t st) {
+  if (n <= 0) return true;
+  fill_slots_kernel<<<(n + 255) / 256, 256, 0, st>>>(idx, n, dst, words, v);
+  return launch_ok("launch_fill_slots");
 }
 bool launch_ftab_resid(const ResidArgs& a, cudaStream_t st, int max_blocks) {
   if (a.n2 <= 0 || a.n_chunks <= 0) return true;

@@ -50,6 +50,7 @@ struct FacEvalArgs {
   const uint32_t* code;      // distinct factor programs, each ending in EMIT 0
   const int2* meta;          // [f] (code offset, length)
   const int2* groups;        // [g] (first factor, count); a group's programs are contiguous
+  const int32_t* wcol;       // [f] column of F (and of fnan) program f writes; NULL: column f
   const float* K;            // constant pool, double-float high parts
   const float* Klo;          // low parts
   int32_t chunk;             // rows per chunk, a multiple of kFacStep
@@ -57,7 +58,7 @@ struct FacEvalArgs {
                              // read columns of earlier levels from it
   float2* P;                 // [chunk][n_pairs] double-float partial sums
   int32_t n_pairs;
-  unsigned long long* fnan;  // [f] first row with a NaN value
+  unsigned long long* fnan;  // [column] first row with a NaN value
   uint32_t* status;
   // staging: 0 reads X and y from global memory (L2); 1 stages them.  The
   // features group g reads (of this launch's groups) are
@@ -101,7 +102,9 @@ struct ResidArgs {
 // light: the groups' programs are short and shallow (4 rows per thread);
 // otherwise 2 rows per thread
 bool launch_fac_eval(const FacEvalArgs& a, int n_groups, int n_chunks, bool light, cudaStream_t st);
-// The rows-per-thread class of a table program.
+// The rows-per-thread class of a program (4 rows per thread when light).  A
+// factor's class is taken from its own program, never from the table form
+// that reads shared columns: the class fixes the order of its self sums.
 inline bool fac_light(int code_len, int stack) { return stack <= 1 && code_len <= 16; }
 size_t fac_eval_smem();
 bool fac_allow_smem();
@@ -109,8 +112,14 @@ bool fac_allow_smem();
 int pair_row_blocks(int64_t n_pad);
 bool launch_pair_sum(const PairArgs& a, int n_row_blocks, cudaStream_t st);
 // psum[p] for p in [p0, p1): FP64 sum over the first n_chunks rows of P.
+// smap (may be NULL; self pairs): the sum of pair p goes to
+// psum[3 * smap[p / 3] + p % 3] instead (program p / 3's column).
 bool launch_pair_reduce(const float2* P, int32_t n_pairs, int32_t n_chunks, int32_t p0, int32_t p1, double* psum,
-                        cudaStream_t st);
+                        cudaStream_t st, const int32_t* smap = nullptr);
+// dst[idx[i] * words + w] = v for i < n, w < words (per-slot records of a
+// column arena)
+bool launch_fill_slots(const int32_t* idx, int32_t n, unsigned long long* dst, int words, unsigned long long v,
+                       cudaStream_t st);
 // max_blocks > 0: at most that many blocks walk the items (the grid shape
 // changes no result); otherwise one block per item.
 bool launch_ftab_resid(const ResidArgs& a, cudaStream_t st, int max_blocks = 0);

@@ -130,7 +130,7 @@ __global__ void __launch_bounds__(128) mixed_solve_kernel(SolveArgs a) {
   const int32_t* po = a.pair_of + (size_t)li * E;
   for (int e = lane; e < E; e += 32) {
     const int32_t p = po[e];
-    red[warp][e] = p >= 0 ? a.psum[p] : 0.0;
+    red[warp][e] = p >= 0 ? a.psum[p] : (p <= -2 ? a.pself[-2 - (int64_t)p] : 0.0);
   }
   __syncwarp();
   if (lane != 0) return;
@@ -471,7 +471,7 @@ __global__ void __launch_bounds__(128) mixed_solve_kernel(SolveArgs a) {
 // evenly over the dataset (every row when n <= kProbeRows).
 __global__ void __launch_bounds__(128) fac_probe_kernel(const uint32_t* code, const int2* meta, int32_t nf,
                                                         const double* K64, const float* K32, const float* K32lo,
-                                                        DevData ds, FacProbe* out) {
+                                                        DevData ds, FacProbe* out, const int32_t* omap) {
   const int lane = threadIdx.x & 31;
   const int f = blockIdx.x * 4 + (threadIdx.x >> 5);
   if (f >= nf) return;
@@ -514,7 +514,7 @@ __global__ void __launch_bounds__(128) fac_probe_kernel(const uint32_t* code, co
     r.dev = dev;
     r.rms = cnt > 0 ? (float)sqrt(ss / (double)cnt) : 0.f;
     r.flags = flags | (P == ds.n ? FP_ALL_ROWS : 0u);
-    out[f] = r;
+    out[omap ? omap[f] : f] = r;
   }
 }
 
@@ -545,7 +545,7 @@ __global__ void cand_probe_kernel(const rrg_cand* cands, const int32_t* list, in
     if (p.flags & FP_BAD32) r.bad32 |= 1u << i;
     if (p.flags & FP_FAIL) r.bad32 = 0xffffffffu;
     if (p.flags & FP_ALL_ROWS) r.all_rows = 1u;
-    const unsigned long long fr = fnan[fcol[f]];
+    const unsigned long long fr = fnan[fcol ? fcol[f] : f];
     first = fr < first ? fr : first;
   }
   out[c] = r;
@@ -586,9 +586,9 @@ __global__ void split_f32_kernel(const double* src, float* hi, float* lo, int64_
 
 // ----------------------------------------------------------- launchers ----
 bool launch_fac_probe(const uint32_t* code, const int2* meta, int32_t nf, const double* K64, const float* K32,
-                      const float* K32lo, const DevData& ds, FacProbe* out, cudaStream_t st) {
+                      const float* K32lo, const DevData& ds, FacProbe* out, cudaStream_t st, const int32_t* omap) {
   if (nf <= 0) return true;
-  fac_probe_kernel<<<(nf + 3) / 4, 128, 0, st>>>(code, meta, nf, K64, K32, K32lo, ds, out);
+  fac_probe_kernel<<<(nf + 3) / 4, 128, 0, st>>>(code, meta, nf, K64, K32, K32lo, ds, out, omap);
   return launch_ok("launch_fac_probe");
 }
 bool launch_cand_probe(const rrg_cand* cands, const int32_t* list, int32_t n_list, const int32_t* cand_fac,

@@ -62,7 +62,8 @@ struct SolveArgs {
   const int32_t* list;     // mixed candidates (absolute indices)
   int32_t n_list;
   const int32_t* pair_of;  // [list index][kMixedE] pair index of each Gram entry, -1 for none
-  const double* psum;      // [pair] FP64 sum over all rows
+  const double* psum;      // [pair] FP64 sum over all rows (pair index >= 0)
+  const double* pself;     // self sums by column: entry -2 - p of pair index p <= -2
   double* coefs;
   MixedTerm* terms;
   rrg_result* res;
@@ -81,9 +82,12 @@ struct SolveArgs {
 };
 
 // Host launchers (mixed.cu).
+// omap (may be NULL): the record of program f goes to out[omap[f]]
 bool launch_fac_probe(const uint32_t* code, const int2* meta, int32_t nf, const double* K64, const float* K32,
-                      const float* K32lo, const DevData& ds, FacProbe* out, cudaStream_t st);
-// cand_fac: [list index][kMixedMaxM] local factor ids; fcol: local factor -> table column
+                      const float* K32lo, const DevData& ds, FacProbe* out, cudaStream_t st,
+                      const int32_t* omap = nullptr);
+// cand_fac: [list index][kMixedMaxM] factor ids of fp; fcol (may be NULL:
+// the same ids): factor id -> column of fnan
 bool launch_cand_probe(const rrg_cand* cands, const int32_t* list, int32_t n_list, const int32_t* cand_fac,
                        const int32_t* fcol, const FacProbe* fp, const unsigned long long* fnan, ProbeOut* out,
                        int64_t* nanrow, cudaStream_t st);

@@ -41,6 +41,11 @@ bool cuda_ok(cudaError_t e, const char* what) {
     if (!cuda_ok((call), #call)) return RRG_E_CUDA; \
   } while (0)
 
+// pair indices of cross pairs while the pair map is built (then their rank)
+constexpr int32_t kCrossTag = 1 << 30;
+// most slots a column arena holds (the bookkeeping scans them)
+constexpr int64_t kCacheSlotsMax = 1 << 16;
+
 bool const_arg(int op) {
   if (op == RRG_OP_LDC || op == RRG_OP_PSC) return true;
   if (op >= RRG_OP_BIN) return (((op - RRG_OP_BIN) & 7) >> 1) == RRG_SRC_C;
@@ -350,6 +355,106 @@ bool build_table_programs(const std::vector<uint32_t>& lcode, const std::vector<
   return true;
 }
 
+// Slots of one sub-round's table columns in a column arena (colcache.h):
+// the factors found in the cache are read where they are; the others, and
+// the shared columns their programs read, are evaluated into slots taken for
+// them.  `ep` holds the evaluated programs in table order (levels ascending)
+// with their table reads renumbered to slots, `ewcol` the slot each writes.
+struct CachePlan {
+  TableProgs ep;
+  std::vector<int32_t> ewcol;
+  std::vector<int32_t> ecol;     // [evaluated program] its table column
+  std::vector<int32_t> fslot;    // [local factor] slot
+  std::vector<int32_t> mprog;    // local factors evaluated (not found)
+  std::vector<int32_t> scratch;  // slots of shared columns (this sub-round only)
+  int64_t hits = 0;
+};
+
+bool table_ref(uint32_t w) {
+  const int op = (int)(w & 0xffu);
+  return op == kOpLDT || op == kOpPST || (op >= RRG_OP_BIN && (((op - RRG_OP_BIN) & 7) >> 1) == kSrcT);
+}
+
+// Starts a sub-round of `cc`.  When the shared columns do not fit next to
+// the factors, tp is rebuilt without them; false when even then the
+// factors do not fit (the caller's sub-rounds are sized so that they do).
+bool plan_columns(ColumnCache& cc, const std::vector<uint32_t>& lcode, const std::vector<int2>& lmeta,
+                  const double* consts, TableProgs& tp, CachePlan& out) {
+  const int32_t nfl = (int32_t)lmeta.size();
+  cc.begin();
+  std::vector<std::string> keys(nfl);
+  std::vector<int32_t> fhit(nfl, -1);
+  out = CachePlan();
+  for (int32_t l = 0; l < nfl; ++l) {
+    keys[l] = factor_key(lcode.data() + lmeta[l].x, lmeta[l].y, consts);
+    fhit[l] = cc.find(keys[l]);
+    out.hits += fhit[l] >= 0 ? 1 : 0;
+  }
+  std::vector<int32_t> slot_of;
+  std::vector<uint8_t> need, is_fac;
+  int64_t n_new = 0;
+  auto plan = [&]() {
+    const int32_t nc = (int32_t)tp.meta.size();
+    slot_of.assign(nc, -1);
+    is_fac.assign(nc, 0);
+    need.assign(nc, 0);
+    for (int32_t l = 0; l < nfl; ++l) {
+      is_fac[tp.fcol[l]] = 1;
+      if (fhit[l] >= 0) slot_of[tp.fcol[l]] = fhit[l];
+      else need[tp.fcol[l]] = 1;
+    }
+    // a program reads columns of lower levels only (lower numbers)
+    for (int32_t c = nc - 1; c >= 0; --c) {
+      if (!need[c]) continue;
+      for (int pc = 0; pc < tp.meta[c].y; ++pc) {
+        const uint32_t w = tp.code[tp.meta[c].x + pc];
+        if (table_ref(w) && slot_of[w >> 8] < 0) need[w >> 8] = 1;
+      }
+    }
+    n_new = 0;
+    for (int32_t c = 0; c < nc; ++c) n_new += need[c] ? 1 : 0;
+    return n_new <= cc.available();
+  };
+  if (!plan()) {
+    if (!build_table_programs(lcode, lmeta, consts, tp, false) || !plan()) return false;
+  }
+  std::vector<int32_t> taken;
+  if (!cc.take(n_new, taken)) return false;
+  const int32_t nc = (int32_t)tp.meta.size();
+  size_t t = 0;
+  for (int32_t c = 0; c < nc; ++c)
+    if (need[c]) {
+      slot_of[c] = taken[t++];
+      if (!is_fac[c]) out.scratch.push_back(slot_of[c]);
+    }
+  out.fslot.resize(nfl);
+  for (int32_t l = 0; l < nfl; ++l) {
+    out.fslot[l] = slot_of[tp.fcol[l]];
+    if (fhit[l] < 0) {
+      cc.insert(keys[l], out.fslot[l]);
+      out.mprog.push_back(l);
+    }
+  }
+  TableProgs& ep = out.ep;
+  for (size_t L = 0, c0 = 0; L < tp.level_end.size(); c0 = tp.level_end[L++]) {
+    for (int32_t c = (int32_t)c0; c < tp.level_end[L]; ++c) {
+      if (!need[c]) continue;
+      const int off = (int)ep.code.size();
+      for (int pc = 0; pc < tp.meta[c].y; ++pc) {
+        uint32_t w = tp.code[tp.meta[c].x + pc];
+        if (table_ref(w)) w = (w & 0xffu) | ((uint32_t)slot_of[w >> 8] << 8);
+        ep.code.push_back(w);
+      }
+      ep.meta.push_back(make_int2(off, tp.meta[c].y));
+      ep.stack.push_back(tp.stack[c]);
+      out.ewcol.push_back(slot_of[c]);
+      out.ecol.push_back(c);
+    }
+    ep.level_end.push_back((int32_t)ep.meta.size());
+  }
+  return true;
+}
+
 }  // namespace
 
 void build_factor_table(const rrg_cand* cands, int32_t n_cand, const uint32_t* code, const double* consts,
@@ -457,7 +562,8 @@ rrg_status rrg_context::run_mixed(const rrg_dataset* ds, const std::vector<int32
   }
   std::vector<int32_t> fb_all;
   const size_t col_bytes = sizeof(float2) * (size_t)ds->n_pad;
-  const int64_t cap_f = std::max<int64_t>(16, (int64_t)(table_budget_bytes / col_bytes));
+  const int64_t cap_f =
+      std::min<int64_t>(kCacheSlotsMax, std::max<int64_t>(16, (int64_t)(table_budget_bytes / col_bytes)));
   std::vector<int32_t> lid(ft.meta.size(), -1), lf;
   size_t pos = 0;
   while (pos < mixed.size()) {
@@ -524,12 +630,59 @@ rrg_status rrg_context::mixed_subround(const rrg_dataset* ds, const int32_t* lis
   // shared columns on top of the factors must fit the table budget
   if ((double)tp.meta.size() * sizeof(float2) * (double)ds->n_pad > (double)table_budget_bytes)
     build_table_programs(lcode, lmeta, consts64, tp, false);
+  // Column cache: the factor columns an earlier round on this dataset left
+  // in the arena are read again; the others, and the shared columns their
+  // programs read, are evaluated into free or least recently used slots (the
+  // shared ones for this sub-round only).  Every kernel below addresses the
+  // arena by slot; the re-scoring lane keeps the table's own column numbers
+  // for its FP64 table.
+  const size_t col_bytes = sizeof(float2) * (size_t)ds->n_pad;
+  const int64_t climit =
+      std::min<int64_t>(kCacheSlotsMax, std::max<int64_t>(16, (int64_t)(table_budget_bytes / col_bytes)));
+  if (fcache.limit() != climit || fcache_npad != ds->n_pad) {
+    fcache.reset(climit);
+    fcache_npad = ds->n_pad;
+  }
+  fcache.bind(ds->uid);
+  if (!cache_on) fcache.clear();
+  CachePlan cp;
+  if (!plan_columns(fcache, lcode, lmeta, consts64, tp, cp)) {
+    rrc::set_error("mixed round: the column cache has no room for the sub-round");
+    return RRG_E_OOM;
+  }
+  // scratch slots go back to the free list when this sub-round is enqueued
+  struct GiveBack {
+    ColumnCache& cc;
+    std::vector<int32_t>& s;
+    ~GiveBack() { cc.give_back(s); }
+  } give_back{fcache, cp.scratch};
   const int32_t ncol = (int32_t)tp.meta.size();
   for (int32_t c = 0; c < ncol; ++c)
     if (tp.stack[c] > kMixedStackCap || tp.meta[c].y > kFacCodeSmem) {
       rrc::set_error("mixed round: a table program exceeds the evaluator's limits");
       return RRG_E_INVALID;
     }
+  const TableProgs& ep = cp.ep;
+  const std::vector<int32_t>& ewcol = cp.ewcol;
+  const std::vector<int32_t>& fslot = cp.fslot;
+  const std::vector<int32_t>& mprog = cp.mprog;
+  const int32_t ne = (int32_t)ep.meta.size();
+  last_cache_hits += cp.hits;
+  last_cache_evals += ne;
+  // rows per thread of each evaluated program.  It fixes the order of the
+  // factor's three self sums, so for a factor it is decided by the factor's
+  // own program (not by the shared columns its table program happens to
+  // read in this sub-round): a factor's sums are then the same bits in every
+  // round, kept or evaluated again.
+  std::vector<uint8_t> elight(ne);
+  {
+    std::vector<int32_t> fac_of(ncol, -1);
+    for (int32_t l = 0; l < nfl; ++l) fac_of[tp.fcol[l]] = l;
+    for (int32_t e = 0; e < ne; ++e) {
+      const int32_t l = fac_of[cp.ecol[e]];
+      elight[e] = l >= 0 ? fac_light(lmeta[l].y, ft.stack[lf[l]]) : fac_light(ep.meta[e].y, ep.stack[e]);
+    }
+  }
   // evaluator groups per level, of at most `gmax` factors: consecutive
   // columns of one rows-per-thread class whose programs fit the shared
   // buffer; per level the light groups first, then the others.  The group
@@ -545,16 +698,15 @@ rrg_status rrg_context::mixed_subround(const rrg_dataset* ds, const int32_t* lis
     size_t off = 0, off_foff = 0, off_feat = 0;
   };
   auto build_groups = [&](int gmax, GroupSet& gs) {
-    for (size_t L = 0, c0 = 0; L < tp.level_end.size(); ++L) {
-      const int32_t c1 = tp.level_end[L];
+    for (size_t L = 0, c0 = 0; L < ep.level_end.size(); ++L) {
+      const int32_t c1 = ep.level_end[L];
       std::vector<int2> heavy;
       int32_t n_light = 0;
       for (int32_t i = (int32_t)c0; i < c1;) {
-        const bool light = fac_light(tp.meta[i].y, tp.stack[i]);
+        const bool light = elight[i] != 0;
         int32_t j = i, words = 0;
-        while (j < c1 && j - i < gmax && words + tp.meta[j].y <= kFacCodeSmem &&
-               fac_light(tp.meta[j].y, tp.stack[j]) == light)
-          words += tp.meta[j++].y;
+        while (j < c1 && j - i < gmax && words + ep.meta[j].y <= kFacCodeSmem && (elight[j] != 0) == light)
+          words += ep.meta[j++].y;
         if (light) {
           gs.groups.push_back(make_int2(i, j - i));
           ++n_light;
@@ -573,8 +725,8 @@ rrg_status rrg_context::mixed_subround(const rrg_dataset* ds, const int32_t* lis
     for (const int2& g : gs.groups) {
       std::fill(used.begin(), used.end(), 0);
       for (int32_t c = g.x; c < g.x + g.y; ++c)
-        for (int pc = 0; pc < tp.meta[c].y; ++pc) {
-          const uint32_t w = tp.code[tp.meta[c].x + pc];
+        for (int pc = 0; pc < ep.meta[c].y; ++pc) {
+          const uint32_t w = ep.code[ep.meta[c].x + pc];
           const int op = (int)(w & 0xffu);
           if (op == RRG_OP_LDV || op == RRG_OP_PSV || (op >= RRG_OP_BIN && (((op - RRG_OP_BIN) & 7) >> 1) == RRG_SRC_V))
             used[w >> 8] = 1;
@@ -591,21 +743,24 @@ rrg_status rrg_context::mixed_subround(const rrg_dataset* ds, const int32_t* lis
   };
   bool gtrial = false;
   int gvals[4] = {tune_pick(TK_FAC_GROUP, 0, ds->n, &gtrial), 0, 0, 0};
-  gtrial = gtrial && !capturing && (int64_t)ncol * ds->n >= kTuneMinWork;
+  gtrial = gtrial && !capturing && (int64_t)ne * ds->n >= kTuneMinWork;
   const int ngv = gtrial ? tune_variants(TK_FAC_GROUP, 0, gvals) : 1;
   std::vector<GroupSet> gsets(ngv);
   for (int v = 0; v < ngv; ++v) build_groups(std::min(gvals[v], kFacGroupMax), gsets[v]);
   // row chunks of fac_chunk(d) rows (the self sums' partials are per chunk);
   // pair sums and the residual pass use kPairRows blocks
-  const int32_t n_self = 3 * ncol;
+  const int32_t n_self = 3 * ne;
   int chunk = fac_chunk(ds->d);
   if ((ds->n_pad + chunk - 1) / chunk > 65535) chunk = (int)round_up((ds->n_pad + 65534) / 65535, kFacStep);
   const int64_t n_chunks64 = (ds->n_pad + chunk - 1) / chunk;
   const int n_chunks = (int)n_chunks64;
   const int n_super = pair_row_blocks(ds->n_pad);
-  if (!d_F.reserve(sizeof(float2) * (size_t)ncol * ds->n_pad) ||
+  const size_t n_slots = (size_t)std::max<int64_t>(1, fcache.size());
+  if (!d_F.grow_keep(col_bytes * n_slots, d_F.cap) ||
       !d_P.reserve(sizeof(float2) * (size_t)n_chunks * std::max(1, n_self)) ||
-      !d_fnan.reserve(sizeof(unsigned long long) * ncol)) {
+      !d_cfnan.grow_keep(sizeof(unsigned long long) * n_slots, d_cfnan.cap) ||
+      !d_cself.grow_keep(sizeof(double) * 3 * n_slots, d_cself.cap) ||
+      !d_cprobe.grow_keep(sizeof(FacProbe) * n_slots, d_cprobe.cap)) {
     rrc::set_error("mixed round: factor table allocation failed");
     return RRG_E_OOM;
   }
@@ -613,7 +768,9 @@ rrg_status rrg_context::mixed_subround(const rrg_dataset* ds, const int32_t* lis
   // the pair map while it runs
   Packer pkt;
   const size_t o_tcode = pkt.add(tp.code.data(), sizeof(uint32_t) * tp.code.size());
-  const size_t o_tmeta = pkt.add(tp.meta.data(), sizeof(int2) * tp.meta.size());
+  const size_t o_ecode = pkt.add(ep.code.data(), sizeof(uint32_t) * std::max<size_t>(1, ep.code.size()));
+  const size_t o_emeta = pkt.add(ep.meta.data(), sizeof(int2) * std::max<size_t>(1, ep.meta.size()));
+  const size_t o_ewcol = pkt.add(ewcol.data(), sizeof(int32_t) * std::max<size_t>(1, ewcol.size()));
   for (GroupSet& gs : gsets) {
     gs.off = pkt.add(gs.groups.data(), sizeof(int2) * gs.groups.size());
     gs.off_foff = pkt.add(gs.feat_off.data(), sizeof(int32_t) * gs.feat_off.size());
@@ -622,16 +779,20 @@ rrg_status rrg_context::mixed_subround(const rrg_dataset* ds, const int32_t* lis
   rrg_status pst = pkt.send(h_ftp, d_ftp, stream, round_seq);
   if (pst != RRG_OK) return pst;
   float2* F = static_cast<float2*>(d_F.ptr);
-  float2* Pself = static_cast<float2*>(d_P.ptr);  // [chunk][3 ncol]
-  unsigned long long* fnan = static_cast<unsigned long long*>(d_fnan.ptr);
+  float2* Pself = static_cast<float2*>(d_P.ptr);  // [chunk][3 ne]
+  unsigned long long* fnan = static_cast<unsigned long long*>(d_cfnan.ptr);
+  double* cself = static_cast<double*>(d_cself.ptr);
+  FacProbe* cprobe = static_cast<FacProbe*>(d_cprobe.ptr);
   uint32_t* status = static_cast<uint32_t*>(d_status.ptr);
-  RRG_CUDA(cudaMemsetAsync(fnan, 0x7f, sizeof(unsigned long long) * ncol, stream));
+  const int32_t* d_ewcol = pkt.at<const int32_t>(d_ftp, o_ewcol);
+  if (!launch_fill_slots(d_ewcol, ne, fnan, 1, 0x7f7f7f7f7f7f7f7full, stream)) return RRG_E_CUDA;
 
   cudaEvent_t t0 = mark_begin();
   FacEvalArgs fa;
   fa.ds = dd;
-  fa.code = pkt.at<const uint32_t>(d_ftp, o_tcode);
-  fa.meta = pkt.at<const int2>(d_ftp, o_tmeta);
+  fa.code = pkt.at<const uint32_t>(d_ftp, o_ecode);
+  fa.meta = pkt.at<const int2>(d_ftp, o_emeta);
+  fa.wcol = d_ewcol;
   fa.K = dev.consts32;
   fa.Klo = dev.consts32lo;
   fa.chunk = chunk;
@@ -688,7 +849,7 @@ rrg_status rrg_context::mixed_subround(const rrg_dataset* ds, const int32_t* lis
     tune_store(TK_FAC_GROUP, 0, ds->n, gvals, ms, ngv);
   }
   const bool stage_ok = maps_ok && can_stage(gsets[gbest]);
-  if (strial && !capturing && stage_ok && (int64_t)ncol * ds->n >= kTuneMinWork) {
+  if (strial && !capturing && stage_ok && (int64_t)ne * ds->n >= kTuneMinWork) {
     // the first round of this feature count: reading X from global memory
     // and staging it, both timed on the real launches
     int vals[2] = {1, 2};
@@ -710,11 +871,11 @@ rrg_status rrg_context::mixed_subround(const rrg_dataset* ds, const int32_t* lis
   cmap.reserve((size_t)cnt * 4 + 16);
   std::vector<std::pair<int32_t, int32_t>> cross;
   std::vector<int32_t> pair_of((size_t)cnt * kMixedE, -1), cand_fac((size_t)cnt * kMixedMaxM, 0);
-  std::vector<int32_t> cand_col((size_t)cnt * kMixedMaxM, 0);
+  std::vector<int32_t> cand_col((size_t)cnt * kMixedMaxM, 0), cand_slot((size_t)cnt * kMixedMaxM, 0);
   auto cross_id = [&](int32_t x, int32_t y) {
     const int32_t gx = lf[x], gy = lf[y];
     const bool xa = ft.occ[gx] < ft.occ[gy] || (ft.occ[gx] == ft.occ[gy] && gx < gy);
-    const int32_t a = tp.fcol[xa ? x : y], b = tp.fcol[xa ? y : x];
+    const int32_t a = fslot[xa ? x : y], b = fslot[xa ? y : x];
     const uint64_t key = ((uint64_t)(uint32_t)a << 32) | (uint32_t)b;
     auto it = cmap.find(key);
     if (it != cmap.end()) return it->second;
@@ -730,17 +891,20 @@ rrg_status rrg_context::mixed_subround(const rrg_dataset* ds, const int32_t* lis
     int32_t l[kMixedMaxM];
     for (int s = 0; s < m; ++s) {
       l[s] = lid[ft.ids[ft.cand_off[c] + s]];
-      cand_fac[(size_t)li * kMixedMaxM + s] = l[s];
+      cand_fac[(size_t)li * kMixedMaxM + s] = fslot[l[s]];
       cand_col[(size_t)li * kMixedMaxM + s] = tp.fcol[l[s]];
+      cand_slot[(size_t)li * kMixedMaxM + s] = fslot[l[s]];
     }
+    // self sums by slot (entries -2 - p, p into the slots' self sums);
+    // cross pairs numbered from kCrossTag until their order is known
     int32_t* po = pair_of.data() + (size_t)li * kMixedE;
     int e = 0;
     for (int i = 0; i < kMixedMaxM; ++i)
       for (int j = i; j < kMixedMaxM; ++j, ++e)
-        if (i < m && j < m) po[e] = l[i] == l[j] ? 3 * tp.fcol[l[i]] : -2 - cross_id(l[i], l[j]);
+        if (i < m && j < m) po[e] = l[i] == l[j] ? -2 - 3 * fslot[l[i]] : kCrossTag + cross_id(l[i], l[j]);
     for (int i = 0; i < m; ++i) {
-      po[Gn + i] = 3 * tp.fcol[l[i]] + 1;
-      po[Gn + kMixedMaxM + i] = 3 * tp.fcol[l[i]] + 2;
+      po[Gn + i] = -2 - (3 * fslot[l[i]] + 1);
+      po[Gn + kMixedMaxM + i] = -2 - (3 * fslot[l[i]] + 2);
     }
   }
   // cross pairs sorted by (a, b); units = runs of equal a
@@ -753,7 +917,7 @@ rrg_status rrg_context::mixed_subround(const rrg_dataset* ds, const int32_t* lis
     partner[k] = cross[order[k]].second;
   }
   for (int32_t& p : pair_of)
-    if (p <= -2) p = n_self + rank[-2 - p];
+    if (p >= kCrossTag) p = rank[p - kCrossTag];
   // units of at most `maxp` partners (a launch shape only: each pair's sum
   // is formed alone; the tuner's TK_PAIR_UNIT)
   auto build_units = [&](int maxp, std::vector<int4>& units) {
@@ -771,17 +935,27 @@ rrg_status rrg_context::mixed_subround(const rrg_dataset* ds, const int32_t* lis
   const int npv = ptrial ? tune_variants(TK_PAIR_UNIT, 0, pvals) : 1;
   std::vector<std::vector<int4>> usets(npv);
   for (int v = 0; v < npv; ++v) build_units(pvals[v], usets[v]);
-  const int32_t n_pairs = n_self + n_cross;
   if (!d_Pc.reserve(sizeof(float2) * (size_t)n_super * std::max(1, n_cross)) ||
-      !d_psum.reserve(sizeof(double) * std::max(1, n_pairs)) || !d_fprobe.reserve(sizeof(FacProbe) * nfl)) {
+      !d_psum.reserve(sizeof(double) * std::max(1, n_cross))) {
     rrc::set_error("mixed round: factor table allocation failed");
     return RRG_E_OOM;
   }
+  // probe programs: the factors evaluated in this sub-round (their records
+  // go to their slots)
+  std::vector<uint32_t> pcode;
+  std::vector<int2> pmeta;
+  std::vector<int32_t> pslot;
+  for (int32_t l : mprog) {
+    pmeta.push_back(make_int2((int)pcode.size(), lmeta[l].y));
+    pcode.insert(pcode.end(), lcode.begin() + lmeta[l].x, lcode.begin() + lmeta[l].x + lmeta[l].y);
+    pslot.push_back(fslot[l]);
+  }
   Packer pk;
-  const size_t o_code = pk.add(lcode.data(), sizeof(uint32_t) * lcode.size());
-  const size_t o_meta = pk.add(lmeta.data(), sizeof(int2) * lmeta.size());
-  const size_t o_fcol = pk.add(tp.fcol.data(), sizeof(int32_t) * tp.fcol.size());
+  const size_t o_code = pk.add(pcode.data(), sizeof(uint32_t) * std::max<size_t>(1, pcode.size()));
+  const size_t o_meta = pk.add(pmeta.data(), sizeof(int2) * std::max<size_t>(1, pmeta.size()));
+  const size_t o_pslot = pk.add(pslot.data(), sizeof(int32_t) * std::max<size_t>(1, pslot.size()));
   const size_t o_ccol = pk.add(cand_col.data(), sizeof(int32_t) * cand_col.size());
+  const size_t o_cslot = pk.add(cand_slot.data(), sizeof(int32_t) * cand_slot.size());
   std::vector<size_t> o_units(npv);
   for (int v = 0; v < npv; ++v) o_units[v] = pk.add(usets[v].data(), sizeof(int4) * usets[v].size());
   const size_t o_partner = pk.add(partner.data(), sizeof(int32_t) * partner.size());
@@ -798,7 +972,7 @@ rrg_status rrg_context::mixed_subround(const rrg_dataset* ds, const int32_t* lis
   int32_t* d_list2 = pk.at<int32_t>(d_ft, o_list2);
   float2* Pcross = static_cast<float2*>(d_Pc.ptr);  // [row block][cross pairs]
   double* psum = static_cast<double*>(d_psum.ptr);
-  FacProbe* fprobe = static_cast<FacProbe*>(d_fprobe.ptr);
+  const int32_t* d_cslot = pk.at<const int32_t>(d_ft, o_cslot);
   const int fb_cap = std::max(1, (int)host_cands.size());
   const size_t back_bytes = sizeof(int32_t) * (fb_cap + 1 + kFbReasons) + (size_t)fb_cap;
   int32_t* fallback = static_cast<int32_t*>(d_fallback.ptr);
@@ -807,7 +981,7 @@ rrg_status rrg_context::mixed_subround(const rrg_dataset* ds, const int32_t* lis
   RRG_CUDA(cudaMemsetAsync(d_fallback.ptr, 0, back_bytes, stream));
   RRG_CUDA(cudaMemsetAsync(d_cert_e.ptr, 0xff, sizeof(double) * fb_cap, stream));  // NaN: no check
   mark_end(P_GRAM, t0);
-  phase_bytes[P_GRAM] += (double)ds->n * 8.0 * (double)(ds->d + 1 + ncol);
+  phase_bytes[P_GRAM] += (double)ds->n * 8.0 * (double)(ds->d + 1 + ne);
   t0 = mark_begin();
   PairArgs pa;
   pa.F = F;
@@ -836,12 +1010,13 @@ rrg_status rrg_context::mixed_subround(const rrg_dataset* ds, const int32_t* lis
     return RRG_E_CUDA;
   }
   mark_end(P_PAIRS, t0);
-  phase_bytes[P_PAIRS] += (double)ds->n * 8.0 * (double)ncol;
+  phase_bytes[P_PAIRS] += (double)ds->n * 8.0 * (double)nfl;
   t0 = mark_begin();
-  if (!launch_pair_reduce(Pself, n_self, n_chunks, 0, n_self, psum, stream) ||
-      !launch_pair_reduce(Pcross, n_cross, n_super, 0, n_cross, psum + n_self, stream) ||
-      !launch_fac_probe(d_code, d_meta, nfl, dev.consts, dev.consts32, dev.consts32lo, dd, fprobe, stream) ||
-      !launch_cand_probe(dev.cands, d_list, cnt, d_cfac, pk.at<const int32_t>(d_ft, o_fcol), fprobe, fnan,
+  if (!launch_pair_reduce(Pself, n_self, n_chunks, 0, n_self, cself, stream, d_ewcol) ||
+      !launch_pair_reduce(Pcross, n_cross, n_super, 0, n_cross, psum, stream) ||
+      !launch_fac_probe(d_code, d_meta, (int32_t)mprog.size(), dev.consts, dev.consts32, dev.consts32lo, dd, cprobe,
+                        stream, pk.at<const int32_t>(d_ft, o_pslot)) ||
+      !launch_cand_probe(dev.cands, d_list, cnt, d_cfac, nullptr, cprobe, fnan,
                          static_cast<ProbeOut*>(d_probe.ptr), static_cast<int64_t*>(d_nanrow.ptr), stream)) {
     cuda_ok(cudaGetLastError(), "mixed round launch");
     return RRG_E_CUDA;
@@ -853,6 +1028,7 @@ rrg_status rrg_context::mixed_subround(const rrg_dataset* ds, const int32_t* lis
   sa.n_list = cnt;
   sa.pair_of = pk.at<const int32_t>(d_ft, o_pair);
   sa.psum = psum;
+  sa.pself = cself;
   sa.coefs = static_cast<double*>(d_coefs.ptr);
   sa.terms = static_cast<MixedTerm*>(d_terms.ptr);
   sa.res = static_cast<rrg_result*>(d_res.ptr);
@@ -1019,7 +1195,7 @@ rrg_status rrg_context::mixed_subround(const rrg_dataset* ds, const int32_t* lis
       ra.list2 = list2;
       ra.n2 = cnt;
       ra.n2_dev = count2;
-      ra.cand_col = d_ccol;
+      ra.cand_col = d_cslot;
       ra.terms = static_cast<const MixedTerm*>(d_terms.ptr);
       ra.n_chunks = n_super;
       ra.sse = sse;
@@ -1198,7 +1374,7 @@ rrg_status rrg_context::mixed_subround(const rrg_dataset* ds, const int32_t* lis
     ra.list2 = d_list2;
     ra.n2 = (int32_t)list2.size();
     ra.n2_dev = nullptr;
-    ra.cand_col = pk.at<const int32_t>(d_ft, o_ccol);
+    ra.cand_col = d_cslot;
     ra.terms = static_cast<const MixedTerm*>(d_terms.ptr);
     ra.n_chunks = n_super;
     ra.sse = sse;
@@ -1255,8 +1431,11 @@ rrg_status rrg_context::run_fp64_table(const rrg_dataset* ds, const std::vector<
   const DevData dd = ds->view();
   const size_t col8 = sizeof(double) * (size_t)ds->n_pad;
   // factors per FP64 table (shared subtree columns come on top: keep room)
-  const int64_t fcap = std::max<int64_t>(2 * RRG_MAX_TERMS, (int64_t)(scratch_budget_bytes / 3 / col8));
+  const int64_t fcap =
+      std::min<int64_t>(kCacheSlotsMax, std::max<int64_t>(2 * RRG_MAX_TERMS, (int64_t)(scratch_budget_bytes / 3 / col8)));
   const int64_t mcap = std::max<int64_t>(2 * RRG_MAX_TERMS + 2, (int64_t)(scratch_budget_bytes / 2 / col8));
+  // FP64 column arena: the table's half of the scratch budget
+  const int64_t plimit = std::min<int64_t>(kCacheSlotsMax, std::max<int64_t>(fcap, (int64_t)(scratch_budget_bytes / 2 / col8)));
   const int nb_res = (int)((ds->n + RR_CHUNK - 1) / RR_CHUNK);
   const size_t n_all = host_cands.size();
   if (!d_partial.reserve(sizeof(double) * n_all * (size_t)nb_res)) {
@@ -1302,27 +1481,47 @@ rrg_status rrg_context::run_fp64_table(const rrg_dataset* ds, const std::vector<
       rrc::set_error("FP64 round: a factor program could not be parsed");
       return RRG_E_INVALID;
     }
-    if ((double)tp.meta.size() * (double)col8 > (double)scratch_budget_bytes / 2)
-      build_table_programs(lcode, lmeta, consts64, tp, false);
-    const int32_t ncol = (int32_t)tp.meta.size();
-    const std::vector<uint32_t>& fcode = tp.code;
-    std::vector<rrg_cand> fc(std::max(1, ncol));
-    std::vector<PlainCand> fpc(std::max(1, ncol));
-    for (int32_t i = 0; i < ncol; ++i) {
+    // Column cache (as in the mixed rounds): FP64 columns of earlier rounds
+    // on this dataset are read again, the others evaluated into slots of the
+    // FP64 arena; the QR, sentinel and residual kernels address it by slot.
+    if (pcache.limit() != plimit || pcache_npad != ds->n_pad) {
+      pcache.reset(plimit);
+      pcache_npad = ds->n_pad;
+    }
+    pcache.bind(ds->uid);
+    if (!cache_on) pcache.clear();
+    CachePlan cp;
+    if (!plan_columns(pcache, lcode, lmeta, consts64, tp, cp)) {
+      rrc::set_error("FP64 round: the column cache has no room for the table");
+      return RRG_E_OOM;
+    }
+    struct GiveBack {
+      ColumnCache& cc;
+      std::vector<int32_t>& s;
+      ~GiveBack() { cc.give_back(s); }
+    } give_back{pcache, cp.scratch};
+    const TableProgs& ep = cp.ep;
+    const int32_t ne = (int32_t)ep.meta.size();
+    last_cache64_hits += cp.hits;
+    last_cache64_evals += ne;
+    const std::vector<uint32_t>& fcode = ep.code;
+    std::vector<rrg_cand> fc(std::max(1, ne));
+    std::vector<PlainCand> fpc(std::max(1, ne));
+    for (int32_t i = 0; i < ne; ++i) {
       rrg_cand& p = fc[i];
-      p.code_offset = tp.meta[i].x;
-      p.code_len = tp.meta[i].y;
+      p.code_offset = ep.meta[i].x;
+      p.code_len = ep.meta[i].y;
       p.first_factor = 0;
       p.n_factors = 1;
       p.mode = RRG_UNTUNED;
       p.coef_offset = 0;
-      p.stack_need = tp.stack[i];
+      p.stack_need = ep.stack[i];
       p.reserved = 0;
-      if (tp.stack[i] > RRG_MAX_STACK) {
+      if (ep.stack[i] > RRG_MAX_STACK) {
         rrc::set_error("FP64 round: a table program exceeds the spill stack");
         return RRG_E_INVALID;
       }
-      fpc[i] = PlainCand{i, 0, 0, 1, 0};
+      fpc[i] = PlainCand{cp.ewcol[i], 0, 0, 1, 0};
     }
     // column map and QR working columns; QR sub-batches by the M budget
     std::vector<int32_t> colmap;
@@ -1349,11 +1548,12 @@ rrg_status rrg_context::run_fp64_table(const rrg_dataset* ds, const std::vector<
       p.pad = 0;
       mcol += need;
       mcols_max = std::max(mcols_max, mcol);
-      for (int s = 0; s < m; ++s) colmap.push_back(tp.fcol[lid[ft.ids[ft.cand_off[c] + s]]]);
+      for (int s = 0; s < m; ++s) colmap.push_back(cp.fslot[lid[ft.ids[ft.cand_off[c] + s]]]);
     }
     subs.push_back({sub0, ng});
     Packer pk;
-    const size_t o_fcode = pk.add(fcode.data(), sizeof(uint32_t) * fcode.size());
+    const size_t o_fcode = pk.add(fcode.data(), sizeof(uint32_t) * std::max<size_t>(1, fcode.size()));
+    const size_t o_ewcol = pk.add(cp.ewcol.data(), sizeof(int32_t) * std::max<size_t>(1, cp.ewcol.size()));
     const size_t o_fc = pk.add(fc.data(), sizeof(rrg_cand) * fc.size());
     const size_t o_fpc = pk.add(fpc.data(), sizeof(PlainCand) * fpc.size());
     const size_t o_cmap = pk.add(colmap.data(), sizeof(int32_t) * std::max<size_t>(1, colmap.size()));
@@ -1361,7 +1561,9 @@ rrg_status rrg_context::run_fp64_table(const rrg_dataset* ds, const std::vector<
     const size_t o_list = pk.add(list.data() + pos, sizeof(int32_t) * ng);
     rrg_status pst = pk.send(h_ft64, d_ft64, stream, round_seq);
     if (pst != RRG_OK) return pst;
-    if (!d_F64.reserve(col8 * std::max(1, ncol)) || !d_M.reserve(col8 * mcols_max)) {
+    const size_t n_slots = (size_t)std::max<int64_t>(1, pcache.size());
+    if (!d_F64.grow_keep(col8 * n_slots, d_F64.cap) || !d_M.reserve(col8 * mcols_max) ||
+        !d_ccst.grow_keep(sizeof(ColStat) * n_slots, d_ccst.cap)) {
       rrc::set_error("FP64 round: table allocation failed");
       return RRG_E_OOM;
     }
@@ -1379,30 +1581,29 @@ rrg_status rrg_context::run_fp64_table(const rrg_dataset* ds, const std::vector<
     DevBatch fdev = dev;
     fdev.cands = pk.at<const rrg_cand>(d_ft64, o_fc);
     fdev.code = pk.at<const uint32_t>(d_ft64, o_fcode);
-    fdev.n_cand = ncol;
+    fdev.n_cand = ne;
     fdev.n_code = (int32_t)fcode.size();
-    // column statistics of the table, gathered by the evaluator, then the
-    // candidates whose QR outcome is certainly the all-NaN sentinel (their
-    // QR and residual work is skipped)
-    if (!d_colstat.reserve(sizeof(ColStat) * (size_t)std::max(1, ncol))) {
-      rrc::set_error("FP64 round: scratch allocation failed");
-      return RRG_E_OOM;
-    }
-    ColStat* cst = static_cast<ColStat*>(d_colstat.ptr);
-    RRG_CUDA(cudaMemsetAsync(cst, 0, sizeof(ColStat) * (size_t)std::max(1, ncol), stream));
+    // column statistics of the table (by slot, kept with the columns),
+    // gathered by the evaluator, then the candidates whose QR outcome is
+    // certainly the all-NaN sentinel (their QR and residual work is skipped)
+    ColStat* cst = static_cast<ColStat*>(d_ccst.ptr);
+    static_assert(sizeof(ColStat) == 2 * sizeof(unsigned long long), "ColStat is two words");
+    if (!launch_fill_slots(pk.at<const int32_t>(d_ft64, o_ewcol), ne, reinterpret_cast<unsigned long long*>(cst), 2,
+                           0ull, stream))
+      return RRG_E_CUDA;
     cudaEvent_t t0 = mark_begin();
     // one launch (or several of at most 65535 columns) per level; blocks per
     // column from the tuner's SM waves (any value gives the same columns)
     bool wave_trial = false;
     int waves = tune_pick(TK_EVAL_WAVES, 0, ds->n, &wave_trial);
     size_t wave_level = 0;  // a trial times the widest level
-    for (size_t L = 0, c0 = 0, widest = 0; L < tp.level_end.size(); c0 = tp.level_end[L++])
-      if ((size_t)tp.level_end[L] - c0 > widest) {
-        widest = (size_t)tp.level_end[L] - c0;
+    for (size_t L = 0, c0 = 0, widest = 0; L < ep.level_end.size(); c0 = ep.level_end[L++])
+      if ((size_t)ep.level_end[L] - c0 > widest) {
+        widest = (size_t)ep.level_end[L] - c0;
         wave_level = L;
       }
-    for (size_t L = 0, c0 = 0; L < tp.level_end.size(); ++L) {
-      const int32_t c1 = tp.level_end[L];
+    for (size_t L = 0, c0 = 0; L < ep.level_end.size(); ++L) {
+      const int32_t c1 = ep.level_end[L];
       const int32_t nl = c1 - (int32_t)c0;
       auto eval_level = [&](int wv) {
         const int nb = (int)std::max<int64_t>(
@@ -1455,7 +1656,7 @@ rrg_status rrg_context::run_fp64_table(const rrg_dataset* ds, const std::vector<
       launches += 2;
     }
     mark_end(P_PLAIN_EVAL, t0);
-    phase_bytes[P_PLAIN_EVAL] += (double)ds->n * 8.0 * (double)(ds->d + ncol);
+    phase_bytes[P_PLAIN_EVAL] += (double)ds->n * 8.0 * (double)(ds->d + ne);
     launches += 2;
     for (const auto& sb : subs) {
       const int32_t ns = sb.second - sb.first;

@@ -71,6 +71,40 @@ bool DevBuf::reserve(size_t bytes) {
   cap = want;
   return true;
 }
+bool DevBuf::grow_keep(size_t bytes, size_t keep) {
+  if (bytes <= cap) return true;
+  if (frozen && *frozen) return false;
+  size_t want = round_up((int64_t)bytes, 1 << 20);
+  void* np = nullptr;
+  auto alloc = [&](size_t b) { return (st ? cudaMallocAsync(&np, b, st) : cudaMalloc(&np, b)) == cudaSuccess; };
+  if (!alloc(want)) {
+    cudaGetLastError();
+    if (!alloc(bytes)) {
+      cudaGetLastError();
+      return false;
+    }
+    want = bytes;
+  }
+  if (ptr) {
+    keep = std::min(keep, cap);
+    if (keep && cudaMemcpyAsync(np, ptr, keep, cudaMemcpyDeviceToDevice, st) != cudaSuccess) {
+      cudaGetLastError();
+      if (st) cudaFreeAsync(np, st);
+      else cudaFree(np);
+      return false;
+    }
+    if (st) {
+      cudaFreeAsync(ptr, st);
+    } else {
+      cudaDeviceSynchronize();
+      cudaFree(ptr);
+    }
+  }
+  ptr = np;
+  cap = want;
+  return true;
+}
+
 void DevBuf::release() {
   if (ptr) {
     if (st) cudaFreeAsync(ptr, st);
@@ -363,12 +397,17 @@ rrg_status rrg_context::submit(rrg_dataset* ds, const rrg_batch* b, int32_t prec
     } else {
       cudaGetLastError();
       ++graph_fallbacks;
+      // the captured work never ran: the columns it was to leave are not there
+      clear_caches();
       st = enqueue_round(ds, b, precision, n_coefs);
     }
   } else {
     st = enqueue_round(ds, b, precision, n_coefs);
   }
-  if (st != RRG_OK) return st;
+  if (st != RRG_OK) {
+    clear_caches();  // a round that failed part-way may have left slots unwritten
+    return st;
+  }
   RRG_CUDA(cudaEventRecord(done, stream));
   in_flight = true;
   out_results = results;
@@ -391,6 +430,7 @@ rrg_status rrg_context::enqueue_round(rrg_dataset* ds, const rrg_batch* b, int32
   fbstat_pending = false;
   launches = 0;
   last_plain_routed = last_fallback = last_pass2 = last_sentinel = 0;
+  last_cache_hits = last_cache_evals = last_cache64_hits = last_cache64_evals = 0;
   for (double& v : phase_bytes) v = 0.0;
   for (auto& r : last_reasons) r = 0;
   marks.clear();
@@ -439,6 +479,7 @@ rrg_status rrg_context::wait(int32_t timeout_ms) {
     if (e == cudaSuccess) break;
     if (e != cudaErrorNotReady) {
       in_flight = false;
+      clear_caches();
       cuda_ok(e, "round execution");
       return RRG_E_CUDA;
     }
@@ -452,6 +493,7 @@ rrg_status rrg_context::wait(int32_t timeout_ms) {
   in_flight = false;
   const uint32_t dev_status = *static_cast<uint32_t*>(h_status.ptr);
   if (dev_status != 0) {
+    clear_caches();  // columns of a round that reported an error are not kept
     char msg[128];
     std::snprintf(msg, sizeof msg, "device reported error status 0x%x", dev_status);
     rrc::set_error(msg);
@@ -504,9 +546,9 @@ rrg_status rrg_context::wait(int32_t timeout_ms) {
 
 std::vector<DevBuf*> rrg_context::all_bufs() {
   return {&d_batch, &d_A, &d_pc, &d_partial, &d_list, &d_qrs, &d_terms, &d_fallback, &d_sse1, &d_probe,
-          &d_nanrow, &d_cert_e, &d_ft, &d_ftp, &d_ft64, &d_F, &d_P, &d_Pc, &d_psum, &d_fprobe, &d_fnan, &d_F64, &d_M,
-          &d_colstat, &d_gram, &d_rlist2, &d_fbpack, &d_fbneed, &d_fbcols, &d_fbF64, &d_fbcst, &d_fbgram, &d_fbblist,
-          &d_fbM, &d_fbctr, &d_res, &d_coefs, &d_status};
+          &d_nanrow, &d_cert_e, &d_ft, &d_ftp, &d_ft64, &d_F, &d_P, &d_Pc, &d_psum, &d_F64, &d_M,
+          &d_gram, &d_rlist2, &d_fbpack, &d_fbneed, &d_fbcols, &d_fbF64, &d_fbcst, &d_fbgram, &d_fbblist,
+          &d_fbM, &d_fbctr, &d_cself, &d_cprobe, &d_cfnan, &d_ccst, &d_slots, &d_res, &d_coefs, &d_status};
 }
 
 // Persistent grid of the chunked QR's passes for `items` candidate x chunk items.
@@ -620,6 +662,7 @@ rrg_status make_dataset(rrg_context* ctx, const double* y, int64_t n, int32_t d,
   RRG_CUDA(cudaSetDevice(ctx->device));
   rrg_dataset* ds = new rrg_dataset();
   ds->ctx = ctx;
+  ds->uid = ++ctx->next_uid;
   ctx->datasets.push_back(ds);
   ds->n = n;
   ds->d = d;
@@ -698,7 +741,10 @@ rrg_status rrg_context_create(int32_t device, rrg_context** out) {
   size_t free_b = 0, total_b = 0;
   cudaMemGetInfo(&free_b, &total_b);
   ctx->scratch_budget_bytes = std::min<size_t>((size_t)64 << 30, free_b / 3);
-  ctx->table_budget_bytes = std::min<size_t>((size_t)32 << 30, free_b / 5);
+  // the double-float table is also the column cache of the rounds: a search
+  // at n = 1M keeps about 8K factor columns in 64 GiB (about 84% of a round's
+  // factors are then read instead of evaluated)
+  ctx->table_budget_bytes = std::min<size_t>((size_t)64 << 30, free_b / 4);
   bool side_ok = cudaEventCreateWithFlags(&ctx->fork_ev, cudaEventDisableTiming) == cudaSuccess;
   side_ok = side_ok && cudaEventCreate(&ctx->tune_ev[0]) == cudaSuccess && cudaEventCreate(&ctx->tune_ev[1]) == cudaSuccess;
   for (int i = 0; i < rrg_context::kSide && side_ok; ++i)
@@ -782,6 +828,9 @@ rrg_status rrg_dataset_destroy(rrg_dataset* ds) {
     // freed behind the context stream's queued work (every round of this
     // dataset ran on that stream or joined it)
     release_dataset_memory(ds, ctx->stream);
+    // its kept columns go with it
+    if (ctx->fcache.uid() == ds->uid) ctx->fcache.bind(0);
+    if (ctx->pcache.uid() == ds->uid) ctx->pcache.bind(0);
     auto it = std::find(ctx->datasets.begin(), ctx->datasets.end(), ds);
     if (it != ctx->datasets.end()) ctx->datasets.erase(it);
   }
@@ -852,13 +901,17 @@ int64_t rrg_last_round_launches(const rrg_context* ctx) { return ctx ? ctx->last
 
 int32_t rrg_last_round_stats(const rrg_context* ctx, int64_t* out, int32_t n) {
   if (!ctx || !out || n <= 0) return 0;
-  int64_t v[8 + kFbReasons] = {ctx->last_launches, ctx->last_plain_routed, ctx->last_fallback, ctx->last_pass2};
+  int64_t v[12 + kFbReasons] = {ctx->last_launches, ctx->last_plain_routed, ctx->last_fallback, ctx->last_pass2};
   for (int i = 0; i < kFbReasons; ++i) v[4 + i] = ctx->last_reasons[i];
   v[4 + kFbReasons] = ctx->last_sentinel;
   v[5 + kFbReasons] = ctx->last_distinct;
   v[6 + kFbReasons] = ctx->last_tiled ? 1 : 0;
   v[7 + kFbReasons] = ctx->last_graph ? 1 : 0;
-  const int32_t k = n < 8 + kFbReasons ? n : 8 + kFbReasons;
+  v[8 + kFbReasons] = ctx->last_cache_hits;
+  v[9 + kFbReasons] = ctx->last_cache_evals;
+  v[10 + kFbReasons] = ctx->last_cache64_hits;
+  v[11 + kFbReasons] = ctx->last_cache64_evals;
+  const int32_t k = n < 12 + kFbReasons ? n : 12 + kFbReasons;
   for (int32_t i = 0; i < k; ++i) out[i] = v[i];
   return k;
 }
@@ -880,6 +933,27 @@ rrg_status rrg_context_set_graph(rrg_context* ctx, int32_t on) {
     return RRG_E_INVALID;
   }
   ctx->graph_rounds = on != 0;
+  return RRG_OK;
+}
+
+rrg_status rrg_context_set_column_cache(rrg_context* ctx, int32_t on) {
+  if (!ctx) return RRG_E_INVALID;
+  if (ctx->in_flight) {
+    rrc::set_error("rrg_context_set_column_cache: a round is in flight");
+    return RRG_E_INVALID;
+  }
+  ctx->cache_on = on != 0;
+  ctx->clear_caches();
+  return RRG_OK;
+}
+
+rrg_status rrg_context_clear_column_cache(rrg_context* ctx) {
+  if (!ctx) return RRG_E_INVALID;
+  if (ctx->in_flight) {
+    rrc::set_error("rrg_context_clear_column_cache: a round is in flight");
+    return RRG_E_INVALID;
+  }
+  ctx->clear_caches();
   return RRG_OK;
 }
 

@@ -3,6 +3,7 @@
 #include <cstdint>
 #include <vector>
 
+#include "../host/colcache.h"
 #include "common.cuh"
 
 // Device allocation that only grows.  With an owner stream, allocation and
@@ -16,6 +17,8 @@ struct DevBuf {
   cudaStream_t st = nullptr;      // owner stream (nullptr: plain cudaMalloc / cudaFree)
   const bool* frozen = nullptr;   // while *frozen (a graph capture), growth is refused
   bool reserve(size_t bytes);
+  // grows to `bytes` keeping the first `keep` bytes (a stream-ordered copy)
+  bool grow_keep(size_t bytes, size_t keep);
   void release();
 };
 // Pinned host allocation that only grows.
@@ -29,6 +32,7 @@ struct HostBuf {
 
 struct rrg_dataset {
   rrg_context* ctx = nullptr;
+  uint64_t uid = 0;  // unique on its context: the column caches' entries belong to it
   int64_t n = 0, n_pad = 0;
   int32_t d = 0;
   double* X64 = nullptr;
@@ -102,7 +106,22 @@ struct rrg_context {
   // factor tables
   FactorTable ft;
   HostBuf h_ft, h_ftp, h_ft64;
-  DevBuf d_ft, d_ftp, d_ft64, d_F, d_P, d_Pc, d_psum, d_fprobe, d_fnan, d_F64, d_M, d_colstat, d_gram;
+  DevBuf d_ft, d_ftp, d_ft64, d_F, d_P, d_Pc, d_psum, d_F64, d_M, d_gram;
+  // factor columns kept across rounds of one dataset (colcache.h): the
+  // double-float columns of mixed rounds (arena d_F, with per slot the three
+  // self sums d_cself, the probe record d_cprobe and the first NaN row
+  // d_cfnan) and the FP64 columns of the FP64 table (arena d_F64, column
+  // statistics d_ccst)
+  bool cache_on = true;
+  ColumnCache fcache, pcache;
+  DevBuf d_cself, d_cprobe, d_cfnan, d_ccst, d_slots;
+  int64_t fcache_npad = 0, pcache_npad = 0;  // the row padding the arenas' slots are sized for
+  uint64_t next_uid = 0;
+  int64_t last_cache_hits = 0, last_cache_evals = 0, last_cache64_hits = 0, last_cache64_evals = 0;
+  void clear_caches() {
+    fcache.clear();
+    pcache.clear();
+  }
   // results
   DevBuf d_res, d_coefs, d_status;
   HostBuf h_res, h_coefs, h_status;

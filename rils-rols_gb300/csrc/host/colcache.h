@@ -1,0 +1,67 @@
+// Factor columns kept on the device across rounds: the host-side map from a
+// factor program to the slot of a column arena that holds its values.
+//
+// The candidates of a local-search round are perturbations of the current
+// model, and consecutive rounds perturb mostly the same model: the terms a
+// round leaves unchanged, and their perturbations, come back in the next
+// round.  A factor column is a function of its program (constants by value)
+// and of the dataset only, so the column a round evaluated can be read by a
+// later round on the same dataset instead of being evaluated again.  The
+// columns of the current sub-round are pinned; the others are reused least
+// recently used first.  Which slot a column sits in changes no value.
+#pragma once
+#include <cstdint>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+class ColumnCache {
+ public:
+  // Forget every entry and allow up to `limit` slots.
+  void reset(int64_t limit);
+  // Forget every entry (the slots stay allocated).
+  void clear();
+  // Entries belong to one dataset (by its unique id): another forgets them.
+  void bind(uint64_t ds_uid) {
+    if (ds_uid != uid_) clear();
+    uid_ = ds_uid;
+  }
+  uint64_t uid() const { return uid_; }
+  int64_t limit() const { return limit_; }
+  // slots handed out so far (the arena must hold that many columns)
+  int64_t size() const { return (int64_t)slot_.size(); }
+  // a new sub-round: nothing pinned
+  void begin() {
+    ++stamp_;
+    pinned_ = 0;
+  }
+  // the slot holding `key`, pinned for this sub-round, or -1
+  int32_t find(const std::string& key);
+  // slots that take() can still hand out in this sub-round
+  int64_t available() const { return limit_ - pinned_; }
+  // `count` slots for new columns, pinned: free ones first, then new ones up
+  // to the limit, then the least recently used entries (forgotten).  False,
+  // with nothing taken, when fewer are available.
+  bool take(int64_t count, std::vector<int32_t>& out);
+  // slot `s` (from take) now holds the column of `key`
+  void insert(const std::string& key, int32_t s);
+  // slots from take that hold no entry (scratch columns) back to the free list
+  void give_back(const std::vector<int32_t>& s);
+
+ private:
+  struct Slot {
+    std::string key;   // empty: no entry
+    int64_t last = -1;  // sub-round stamp of its last use
+  };
+  std::vector<Slot> slot_;
+  std::vector<int32_t> free_;
+  std::unordered_map<std::string, int32_t> map_;
+  int64_t limit_ = 0;
+  int64_t stamp_ = 0;
+  int64_t pinned_ = 0;  // slots used in this sub-round
+  uint64_t uid_ = 0;
+};
+
+// The cache key of a factor program (code words ending in EMIT): every word,
+// a constant operand replaced by its value's bits.
+std::string factor_key(const uint32_t* code, int len, const double* consts);

@@ -44,7 +44,10 @@ int64_t round_up64(int64_t v, int64_t m) { return (v + m - 1) / m * m; }
 
 // Device memory of one job: the resident dataset (X and y in FP64 and as
 // double-float pairs) plus the context's two scratch limits and a fixed
-// allowance for the per-round buffers (programs, pair sums, results).
+// allowance for the per-round buffers (programs, pair sums, results).  The
+// limits also bound the job's column caches (factor columns kept across its
+// rounds): 4096 double-float and 4096 FP64 columns where they fit the caps,
+// enough for most of a search's rounds to read instead of evaluate.
 struct Footprint {
   int64_t scratch, table, total;
 };
@@ -52,10 +55,11 @@ Footprint job_footprint(int64_t n, int64_t d) {
   const int64_t n_pad = round_up64(std::max<int64_t>(n, 1), 4096);
   const int64_t col64 = n_pad * 8;
   Footprint f;
-  // 256 FP64 columns of working space and 256 double-float factor columns,
-  // within [64 MiB, 16 GiB] / [64 MiB, 8 GiB]
-  f.scratch = std::min<int64_t>(std::max<int64_t>(256 * col64, 64ll << 20), 16ll << 30);
-  f.table = std::min<int64_t>(std::max<int64_t>(256 * col64, 64ll << 20), 8ll << 30);
+  // 8192 FP64 columns (half of them the FP64 column cache, half QR working
+  // columns) and 4096 double-float factor columns, within [64 MiB, 16 GiB] /
+  // [64 MiB, 8 GiB]
+  f.scratch = std::min<int64_t>(std::max<int64_t>(8192 * col64, 64ll << 20), 16ll << 30);
+  f.table = std::min<int64_t>(std::max<int64_t>(4096 * col64, 64ll << 20), 8ll << 30);
   const int64_t dataset = n_pad * (d + 1) * (8 + 4 + 4);
   f.total = dataset + f.scratch + f.table + (256ll << 20) + 64 * n_pad;
   return f;

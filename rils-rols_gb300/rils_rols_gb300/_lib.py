@@ -79,6 +79,7 @@ EXPORTS = [
     "rrg_context_set_timing", "rrg_last_round_timing", "rrg_last_round_bytes", "rrg_eval_plain_noalloc", "rrg_context_set_limits",
     "rrg_device_memory", "rrg_tune_set_mode", "rrg_tune_pin", "rrg_tune_reset", "rrg_tune_report",
     "rrg_context_set_mixed_min_rows", "rrg_context_set_async", "rrg_context_set_graph", "rrg_context_memory",
+    "rrg_context_set_column_cache", "rrg_context_clear_column_cache",
     "rrh_create", "rrh_destroy", "rrh_set_backend", "rrh_set_precision", "rrh_set_graph", "rrh_fit", "rrh_predict",
     "rrh_model_string", "rrh_model_prefix", "rrh_best_time", "rrh_total_time", "rrh_fit_calls", "rrh_counter",
     "rrh_last_error", "rrh_candidates", "rrh_rewrite", "rrh_encode", "rrh_rebuild",
@@ -120,6 +121,8 @@ def _declare(lib):
         "rrg_device_memory": (i32, [i32, P(C.c_int64), P(C.c_int64)]),
         "rrg_context_set_mixed_min_rows": (i32, [vp, i64]),
         "rrg_context_set_async": (i32, [vp, i32]),
+        "rrg_context_set_column_cache": (i32, [vp, i32]),
+        "rrg_context_clear_column_cache": (i32, [vp]),
         "rrg_context_set_graph": (i32, [vp, i32]),
         "rrg_context_memory": (i64, [vp]),
         "rrg_tune_set_mode": (i32, [i32]),

@@ -124,10 +124,11 @@ class Context:
                "one_pass", "cert", "other_nan")
 
     def last_round_stats(self) -> dict:
-        out = (C.c_int64 * 19)()
-        self.lib.rrg_last_round_stats(self.h, out, 19)
+        out = (C.c_int64 * 23)()
+        self.lib.rrg_last_round_stats(self.h, out, 23)
         d = {"launches": out[0], "plain_routed": out[1], "fp64_rescored": out[2], "residual_pass": out[3],
-             "qr_skipped_sentinel": out[15], "distinct": out[16], "tiled_qr": bool(out[17]), "graph": bool(out[18])}
+             "qr_skipped_sentinel": out[15], "distinct": out[16], "tiled_qr": bool(out[17]), "graph": bool(out[18]),
+             "cache_hits": out[19], "cache_evals": out[20], "cache64_hits": out[21], "cache64_evals": out[22]}
         d["rescore_reasons"] = {r: out[4 + i] for i, r in enumerate(self.REASONS) if out[4 + i]}
         return d
 
@@ -147,6 +148,20 @@ class Context:
         default) or read their flags back to the host twice (off); the same
         results either way."""
         check(self.lib.rrg_context_set_async(self.h, int(on)), "rrg_context_set_async")
+
+    def set_limits(self, scratch_bytes: int, table_bytes: int) -> None:
+        """Device-memory limits of the FP64 tables and QR working columns
+        (scratch) and of the double-float factor table (each >= 1 MiB)."""
+        check(self.lib.rrg_context_set_limits(self.h, int(scratch_bytes), int(table_bytes)), "rrg_context_set_limits")
+
+    def set_column_cache(self, on: bool = True) -> None:
+        """Keep factor columns on the device across rounds of one dataset (on,
+        the default); the same results either way."""
+        check(self.lib.rrg_context_set_column_cache(self.h, int(on)), "rrg_context_set_column_cache")
+
+    def clear_column_cache(self) -> None:
+        """Forget every kept column: the next round evaluates all its factors."""
+        check(self.lib.rrg_context_clear_column_cache(self.h), "rrg_context_clear_column_cache")
 
     def set_graph(self, on: bool = True) -> None:
         """Run every round as a CUDA graph (rounds that cannot be captured are

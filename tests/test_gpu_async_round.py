@@ -46,6 +46,7 @@ def compare(ctx, ds, trees, tag):
 def ctx():
     c = Context(0)
     c.set_mixed_min_rows(0)
+    c.set_column_cache(False)  # both forms evaluate the whole table every time
     yield c
     c.close()
 

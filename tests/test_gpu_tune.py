@@ -48,6 +48,7 @@ def same(a, b):
 def test_every_shape_gives_the_same_bits(data):
     X, y, trees = data
     ctx = Context(0)
+    ctx.set_column_cache(False)  # every round evaluates its columns: the shapes are timed and compared
     ds = ctx.dataset(X, y)
     batch = encode(trees, tuned=True)
     try:
@@ -75,6 +76,7 @@ def test_every_shape_gives_the_same_bits(data):
 def test_tuner_times_every_shape_once(data):
     X, y, trees = data
     ctx = Context(0)
+    ctx.set_column_cache(False)  # every round evaluates its columns: the shapes are timed and compared
     ds = ctx.dataset(X, y)
     batch = encode(trees, tuned=True)
     try:
@@ -105,6 +107,7 @@ def test_tuner_times_every_shape_once(data):
 def test_mixed_path_shapes_give_the_same_bits(data):
     X, y, trees = data
     ctx = Context(0)
+    ctx.set_column_cache(False)  # every round evaluates its columns: the shapes are timed and compared
     ds = ctx.dataset(X, y)
     batch = encode(trees, tuned=True)
     try:
