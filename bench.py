@@ -466,6 +466,11 @@ def run_ours(args):
                                "plain_fp64": accuracy(subset(rt["plain_fp64"]["out"], idx2), ora2),
                                "certified": accuracy(subset(rt["certified"]["out"], idx2), ora2)}}
     ds2.close()
+    # the serving and classifier legs make contexts of their own: this one's
+    # tables and column caches go first
+    ds.close()
+    ctx.close()
+    torch.cuda.synchronize()
     if args.serve_jobs > 0:
         res["serving"] = serving_leg(args, local)
     if args.cls_fit_calls > 0:

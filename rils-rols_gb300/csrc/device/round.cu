@@ -45,6 +45,10 @@ bool cuda_ok(cudaError_t e, const char* what) {
 constexpr int32_t kCrossTag = 1 << 30;
 // most slots a column arena holds (the bookkeeping scans them)
 constexpr int64_t kCacheSlotsMax = 1 << 16;
+// rows from which rounds keep their columns: below, evaluating a column
+// costs less than the bookkeeping of finding it (a 569-row classifier
+// search ran 0.46 ms per round slower with the cache)
+constexpr int64_t kCacheMinRows = 8192;
 
 bool const_arg(int op) {
   if (op == RRG_OP_LDC || op == RRG_OP_PSC) return true;
@@ -368,6 +372,8 @@ struct CachePlan {
   std::vector<int32_t> mprog;    // local factors evaluated (not found)
   std::vector<int32_t> scratch;  // slots of shared columns (this sub-round only)
   int64_t hits = 0;
+  int64_t arena = 0;             // slots the arena must hold
+  bool kept = false;             // the cache was used (slots scattered)
 };
 
 bool table_ref(uint32_t w) {
@@ -378,16 +384,33 @@ bool table_ref(uint32_t w) {
 // Starts a sub-round of `cc`.  When the shared columns do not fit next to
 // the factors, tp is rebuilt without them; false when even then the
 // factors do not fit (the caller's sub-rounds are sized so that they do).
-bool plan_columns(ColumnCache& cc, const std::vector<uint32_t>& lcode, const std::vector<int2>& lmeta,
+// keep = false bypasses the cache (small datasets, where evaluating a
+// column costs less than looking it up): every column is evaluated into
+// slot = its table column, and whatever the cache held is forgotten.
+bool plan_columns(ColumnCache& cc, bool keep, const std::vector<uint32_t>& lcode, const std::vector<int2>& lmeta,
                   const double* consts, TableProgs& tp, CachePlan& out) {
   const int32_t nfl = (int32_t)lmeta.size();
-  cc.begin();
-  std::vector<std::string> keys(nfl);
-  std::vector<int32_t> fhit(nfl, -1);
   out = CachePlan();
+  if (!keep) {
+    if (cc.size() > 0) cc.reset(cc.limit());
+    const int32_t nc = (int32_t)tp.meta.size();
+    out.ep = tp;
+    out.ewcol.resize(nc);
+    out.ecol.resize(nc);
+    for (int32_t c = 0; c < nc; ++c) out.ewcol[c] = out.ecol[c] = c;
+    out.fslot = tp.fcol;
+    for (int32_t l = 0; l < nfl; ++l) out.mprog.push_back(l);
+    out.arena = nc;
+    return true;
+  }
+  out.kept = true;
+  cc.begin();
+  std::vector<uint64_t> hash(nfl);
+  std::vector<int32_t> fhit(nfl, -1);
+  auto prog = [&](int32_t l) { return FactorProg{lcode.data() + lmeta[l].x, lmeta[l].y, consts}; };
   for (int32_t l = 0; l < nfl; ++l) {
-    keys[l] = factor_key(lcode.data() + lmeta[l].x, lmeta[l].y, consts);
-    fhit[l] = cc.find(keys[l]);
+    hash[l] = prog(l).hash();
+    fhit[l] = cc.find(prog(l), hash[l]);
     out.hits += fhit[l] >= 0 ? 1 : 0;
   }
   std::vector<int32_t> slot_of;
@@ -431,7 +454,7 @@ bool plan_columns(ColumnCache& cc, const std::vector<uint32_t>& lcode, const std
   for (int32_t l = 0; l < nfl; ++l) {
     out.fslot[l] = slot_of[tp.fcol[l]];
     if (fhit[l] < 0) {
-      cc.insert(keys[l], out.fslot[l]);
+      cc.insert(prog(l), hash[l], out.fslot[l]);
       out.mprog.push_back(l);
     }
   }
@@ -452,6 +475,7 @@ bool plan_columns(ColumnCache& cc, const std::vector<uint32_t>& lcode, const std
     }
     ep.level_end.push_back((int32_t)ep.meta.size());
   }
+  out.arena = cc.size();
   return true;
 }
 
@@ -644,9 +668,8 @@ rrg_status rrg_context::mixed_subround(const rrg_dataset* ds, const int32_t* lis
     fcache_npad = ds->n_pad;
   }
   fcache.bind(ds->uid);
-  if (!cache_on) fcache.clear();
   CachePlan cp;
-  if (!plan_columns(fcache, lcode, lmeta, consts64, tp, cp)) {
+  if (!plan_columns(fcache, cache_on && ds->n >= kCacheMinRows, lcode, lmeta, consts64, tp, cp)) {
     rrc::set_error("mixed round: the column cache has no room for the sub-round");
     return RRG_E_OOM;
   }
@@ -755,7 +778,7 @@ rrg_status rrg_context::mixed_subround(const rrg_dataset* ds, const int32_t* lis
   const int64_t n_chunks64 = (ds->n_pad + chunk - 1) / chunk;
   const int n_chunks = (int)n_chunks64;
   const int n_super = pair_row_blocks(ds->n_pad);
-  const size_t n_slots = (size_t)std::max<int64_t>(1, fcache.size());
+  const size_t n_slots = (size_t)std::max<int64_t>(1, cp.arena);
   if (!d_F.grow_keep(col_bytes * n_slots, d_F.cap) ||
       !d_P.reserve(sizeof(float2) * (size_t)n_chunks * std::max(1, n_self)) ||
       !d_cfnan.grow_keep(sizeof(unsigned long long) * n_slots, d_cfnan.cap) ||
@@ -785,7 +808,10 @@ rrg_status rrg_context::mixed_subround(const rrg_dataset* ds, const int32_t* lis
   FacProbe* cprobe = static_cast<FacProbe*>(d_cprobe.ptr);
   uint32_t* status = static_cast<uint32_t*>(d_status.ptr);
   const int32_t* d_ewcol = pkt.at<const int32_t>(d_ftp, o_ewcol);
-  if (!launch_fill_slots(d_ewcol, ne, fnan, 1, 0x7f7f7f7f7f7f7f7full, stream)) return RRG_E_CUDA;
+  if (!cp.kept)
+    RRG_CUDA(cudaMemsetAsync(fnan, 0x7f, sizeof(unsigned long long) * std::max(1, ne), stream));
+  else if (!launch_fill_slots(d_ewcol, ne, fnan, 1, 0x7f7f7f7f7f7f7f7full, stream))
+    return RRG_E_CUDA;
 
   cudaEvent_t t0 = mark_begin();
   FacEvalArgs fa;
@@ -1489,9 +1515,8 @@ rrg_status rrg_context::run_fp64_table(const rrg_dataset* ds, const std::vector<
       pcache_npad = ds->n_pad;
     }
     pcache.bind(ds->uid);
-    if (!cache_on) pcache.clear();
     CachePlan cp;
-    if (!plan_columns(pcache, lcode, lmeta, consts64, tp, cp)) {
+    if (!plan_columns(pcache, cache_on && ds->n >= kCacheMinRows, lcode, lmeta, consts64, tp, cp)) {
       rrc::set_error("FP64 round: the column cache has no room for the table");
       return RRG_E_OOM;
     }
@@ -1561,7 +1586,7 @@ rrg_status rrg_context::run_fp64_table(const rrg_dataset* ds, const std::vector<
     const size_t o_list = pk.add(list.data() + pos, sizeof(int32_t) * ng);
     rrg_status pst = pk.send(h_ft64, d_ft64, stream, round_seq);
     if (pst != RRG_OK) return pst;
-    const size_t n_slots = (size_t)std::max<int64_t>(1, pcache.size());
+    const size_t n_slots = (size_t)std::max<int64_t>(1, cp.arena);
     if (!d_F64.grow_keep(col8 * n_slots, d_F64.cap) || !d_M.reserve(col8 * mcols_max) ||
         !d_ccst.grow_keep(sizeof(ColStat) * n_slots, d_ccst.cap)) {
       rrc::set_error("FP64 round: table allocation failed");
@@ -1588,8 +1613,10 @@ rrg_status rrg_context::run_fp64_table(const rrg_dataset* ds, const std::vector<
     // certainly the all-NaN sentinel (their QR and residual work is skipped)
     ColStat* cst = static_cast<ColStat*>(d_ccst.ptr);
     static_assert(sizeof(ColStat) == 2 * sizeof(unsigned long long), "ColStat is two words");
-    if (!launch_fill_slots(pk.at<const int32_t>(d_ft64, o_ewcol), ne, reinterpret_cast<unsigned long long*>(cst), 2,
-                           0ull, stream))
+    if (!cp.kept)
+      RRG_CUDA(cudaMemsetAsync(cst, 0, sizeof(ColStat) * (size_t)std::max(1, ne), stream));
+    else if (!launch_fill_slots(pk.at<const int32_t>(d_ft64, o_ewcol), ne, reinterpret_cast<unsigned long long*>(cst),
+                                2, 0ull, stream))
       return RRG_E_CUDA;
     cudaEvent_t t0 = mark_begin();
     // one launch (or several of at most 65535 columns) per level; blocks per

@@ -6,32 +6,107 @@
 
 #include "../../../include/rils_rols_gb300.h"
 
+namespace {
+
+bool const_operand(int op) {
+  return op == RRG_OP_LDC || op == RRG_OP_PSC || (op >= RRG_OP_BIN && (((op - RRG_OP_BIN) & 7) >> 1) == RRG_SRC_C);
+}
+
+uint64_t const_bits(const double* consts, uint32_t w) {
+  uint64_t b;
+  std::memcpy(&b, consts + (w >> 8), sizeof b);
+  return b;
+}
+
+// the key words of one code word: itself, or (bit 63 | opcode, value bits)
+// for a constant operand (code words have bit 63 clear)
+template <class F>
+void key_words(uint32_t w, const double* consts, F&& out) {
+  const int op = (int)(w & 0xffu);
+  if (const_operand(op)) {
+    out((1ull << 63) | (uint64_t)op);
+    out(const_bits(consts, w));
+  } else {
+    out((uint64_t)w);
+  }
+}
+
+}  // namespace
+
+uint64_t FactorProg::hash() const {
+  uint64_t h = 0xcbf29ce484222325ull;
+  for (int i = 0; i < len; ++i)
+    key_words(code[i], consts, [&](uint64_t v) {
+      h ^= v;
+      h *= 0x100000001b3ull;
+      h ^= h >> 31;
+    });
+  return h;
+}
+
 void ColumnCache::reset(int64_t limit) {
   slot_.clear();
   free_.clear();
-  map_.clear();
+  head_.clear();
   limit_ = limit;
   pinned_ = 0;
 }
 
 void ColumnCache::clear() {
   pinned_ = 0;
-  map_.clear();
+  head_.clear();
   free_.clear();
   for (int32_t s = (int32_t)slot_.size() - 1; s >= 0; --s) {
-    slot_[s].key.clear();
-    slot_[s].last = -1;
+    Slot& sl = slot_[s];
+    sl.held = false;
+    sl.next = -1;
+    sl.last = -1;
     free_.push_back(s);
   }
 }
 
-int32_t ColumnCache::find(const std::string& key) {
-  auto it = map_.find(key);
-  if (it == map_.end()) return -1;
-  Slot& sl = slot_[it->second];
-  if (sl.last != stamp_) ++pinned_;
-  sl.last = stamp_;
-  return it->second;
+bool ColumnCache::matches(const Slot& s, const FactorProg& p) const {
+  size_t k = 0;
+  bool ok = true;
+  for (int i = 0; i < p.len && ok; ++i)
+    key_words(p.code[i], p.consts, [&](uint64_t v) {
+      ok = ok && k < s.key.size() && s.key[k] == v;
+      ++k;
+    });
+  return ok && k == s.key.size();
+}
+
+int32_t ColumnCache::find(const FactorProg& p, uint64_t h) {
+  auto it = head_.find(h);
+  if (it == head_.end()) return -1;
+  for (int32_t s = it->second; s >= 0; s = slot_[s].next) {
+    Slot& sl = slot_[s];
+    if (!matches(sl, p)) continue;
+    if (sl.last != stamp_) ++pinned_;
+    sl.last = stamp_;
+    return s;
+  }
+  return -1;
+}
+
+void ColumnCache::forget(int32_t s) {
+  Slot& sl = slot_[s];
+  if (!sl.held) return;
+  auto it = head_.find(sl.hash);
+  if (it != head_.end()) {
+    if (it->second == s) {
+      if (sl.next >= 0) it->second = sl.next;
+      else head_.erase(it);
+    } else {
+      for (int32_t q = it->second; q >= 0; q = slot_[q].next)
+        if (slot_[q].next == s) {
+          slot_[q].next = sl.next;
+          break;
+        }
+    }
+  }
+  sl.held = false;
+  sl.next = -1;
 }
 
 bool ColumnCache::take(int64_t count, std::vector<int32_t>& out) {
@@ -57,13 +132,11 @@ bool ColumnCache::take(int64_t count, std::vector<int32_t>& out) {
     // least recently used entries not pinned by this sub-round (ties by slot)
     std::vector<std::pair<int64_t, int32_t>> old;
     for (int32_t s = 0; s < (int32_t)slot_.size(); ++s)
-      if (!slot_[s].key.empty() && slot_[s].last < stamp_) old.push_back({slot_[s].last, s});
+      if (slot_[s].held && slot_[s].last < stamp_) old.push_back({slot_[s].last, s});
     const size_t need = (size_t)(count - (int64_t)out.size());
     std::partial_sort(old.begin(), old.begin() + need, old.end());
     for (size_t i = 0; i < need; ++i) {
-      Slot& sl = slot_[old[i].second];
-      map_.erase(sl.key);
-      sl.key.clear();
+      forget(old[i].second);
       out.push_back(old[i].second);
     }
   }
@@ -72,35 +145,21 @@ bool ColumnCache::take(int64_t count, std::vector<int32_t>& out) {
   return true;
 }
 
-void ColumnCache::insert(const std::string& key, int32_t s) {
-  slot_[s].key = key;
-  slot_[s].last = stamp_;
-  map_[key] = s;
+void ColumnCache::insert(const FactorProg& p, uint64_t h, int32_t s) {
+  Slot& sl = slot_[s];
+  sl.key.clear();
+  for (int i = 0; i < p.len; ++i) key_words(p.code[i], p.consts, [&](uint64_t v) { sl.key.push_back(v); });
+  sl.hash = h;
+  sl.held = true;
+  sl.last = stamp_;
+  auto it = head_.find(h);
+  sl.next = it == head_.end() ? -1 : it->second;
+  head_[h] = s;
 }
 
 void ColumnCache::give_back(const std::vector<int32_t>& s) {
   for (int32_t v : s) {
-    slot_[v].key.clear();
+    forget(v);
     free_.push_back(v);
   }
-}
-
-std::string factor_key(const uint32_t* code, int len, const double* consts) {
-  std::string k;
-  k.reserve((size_t)len * 5);
-  for (int i = 0; i < len; ++i) {
-    const uint32_t w = code[i];
-    const int op = (int)(w & 0xffu);
-    const bool c = op == RRG_OP_LDC || op == RRG_OP_PSC ||
-                   (op >= RRG_OP_BIN && (((op - RRG_OP_BIN) & 7) >> 1) == RRG_SRC_C);
-    if (c) {
-      uint64_t bits;
-      std::memcpy(&bits, consts + (w >> 8), sizeof bits);
-      k.push_back((char)op);
-      k.append(reinterpret_cast<const char*>(&bits), sizeof bits);
-    } else {
-      k.append(reinterpret_cast<const char*>(&w), sizeof w);
-    }
-  }
-  return k;
 }

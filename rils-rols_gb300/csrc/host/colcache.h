@@ -9,11 +9,22 @@
 // later round on the same dataset instead of being evaluated again.  The
 // columns of the current sub-round are pinned; the others are reused least
 // recently used first.  Which slot a column sits in changes no value.
+//
+// Entries are found by a 64-bit hash of the program and confirmed word by
+// word against the program kept with the slot, so a lookup allocates nothing.
 #pragma once
 #include <cstdint>
-#include <string>
 #include <unordered_map>
 #include <vector>
+
+// A factor program as the cache sees it: code words ending in EMIT, whose
+// constant operands are compared by value.
+struct FactorProg {
+  const uint32_t* code;
+  int len;
+  const double* consts;
+  uint64_t hash() const;
+};
 
 class ColumnCache {
  public:
@@ -35,33 +46,34 @@ class ColumnCache {
     ++stamp_;
     pinned_ = 0;
   }
-  // the slot holding `key`, pinned for this sub-round, or -1
-  int32_t find(const std::string& key);
+  // the slot holding the column of `p` (hash h), pinned for this sub-round, or -1
+  int32_t find(const FactorProg& p, uint64_t h);
   // slots that take() can still hand out in this sub-round
   int64_t available() const { return limit_ - pinned_; }
   // `count` slots for new columns, pinned: free ones first, then new ones up
   // to the limit, then the least recently used entries (forgotten).  False,
   // with nothing taken, when fewer are available.
   bool take(int64_t count, std::vector<int32_t>& out);
-  // slot `s` (from take) now holds the column of `key`
-  void insert(const std::string& key, int32_t s);
+  // slot `s` (from take) now holds the column of `p` (hash h)
+  void insert(const FactorProg& p, uint64_t h, int32_t s);
   // slots from take that hold no entry (scratch columns) back to the free list
   void give_back(const std::vector<int32_t>& s);
 
  private:
   struct Slot {
-    std::string key;   // empty: no entry
-    int64_t last = -1;  // sub-round stamp of its last use
+    std::vector<uint64_t> key;  // the program: words, a constant as its opcode and value bits
+    uint64_t hash = 0;
+    int32_t next = -1;   // next slot with the same hash
+    bool held = false;   // holds an entry
+    int64_t last = -1;   // sub-round stamp of its last use
   };
+  bool matches(const Slot& s, const FactorProg& p) const;
+  void forget(int32_t s);
   std::vector<Slot> slot_;
   std::vector<int32_t> free_;
-  std::unordered_map<std::string, int32_t> map_;
+  std::unordered_map<uint64_t, int32_t> head_;  // hash -> first slot with it
   int64_t limit_ = 0;
   int64_t stamp_ = 0;
   int64_t pinned_ = 0;  // slots used in this sub-round
   uint64_t uid_ = 0;
 };
-
-// The cache key of a factor program (code words ending in EMIT): every word,
-// a constant operand replaced by its value's bits.
-std::string factor_key(const uint32_t* code, int len, const double* consts);
