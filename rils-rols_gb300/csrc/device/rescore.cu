@@ -1,5 +1,8 @@
 // Device-side lists of a mixed round's second half (declared in rescore.cuh).
+#include <algorithm>
+
 #include "mixed.cuh"
+#include "plain.cuh"
 #include "rescore.cuh"
 
 namespace rrd {
@@ -48,7 +51,7 @@ __global__ void __launch_bounds__(kScanThreads) pass2_compact_kernel(const int32
 
 __global__ void rescore_mark_kernel(const rrg_cand* cands, const int32_t* fb, int32_t cap, const int32_t* li_of,
                                     const int32_t* cand_col, const int32_t* dep_off, const int32_t* deps,
-                                    uint8_t* need) {
+                                    const int32_t* kept, uint8_t* need) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int cnt = min(fb[0], cap);
   if (i >= cnt) return;
@@ -59,8 +62,8 @@ __global__ void rescore_mark_kernel(const rrg_cand* cands, const int32_t* fb, in
   const int m = cd.mode == RRG_TUNED ? cd.n_factors : 1;
   for (int s = 0; s < m && s < kMixedMaxM; ++s) {
     const int col = cand_col[(size_t)li * kMixedMaxM + s];
-    need[col] = 1;
-    for (int j = dep_off[col]; j < dep_off[col + 1]; ++j) need[deps[j]] = 1;
+    need[col] = kept && kept[col] >= 0 ? kNeedCopy : kNeedEval;
+    for (int j = dep_off[col]; j < dep_off[col + 1]; ++j) need[deps[j]] = kept && kept[deps[j]] >= 0 ? kNeedCopy : kNeedEval;
   }
 }
 
@@ -74,7 +77,7 @@ __global__ void __launch_bounds__(kScanThreads) rescore_levels_kernel(const uint
     int base = 0;
     for (int32_t c0 = lo; c0 < hi; c0 += kScanThreads) {
       const int32_t col = c0 + (int32_t)threadIdx.x;
-      const int flag = col < hi && need[col] ? 1 : 0;
+      const int flag = col < hi && need[col] == kNeedEval ? 1 : 0;
       const int pos = block_prefix(flag, warp_tot, &total);
       if (flag) cols[lo + base + pos] = col;
       base += total;
@@ -96,7 +99,52 @@ __global__ void rescore_buckets_kernel(const rrg_cand* cands, const int32_t* fb,
   blist[(size_t)q * cap + slot] = c;
 }
 
+// Columns marked kNeedCopy: the column and its statistics from the cache
+// arena (slot kept[col]) into the table (column col).  grid (x: row blocks of
+// the column, y: columns in steps of gridDim.y).
+__global__ void lane_copy_kernel(const uint8_t* need, const int32_t* kept, int32_t ncol, const double* arena,
+                                 const ColStat* arena_cs, double* table, ColStat* table_cs, int64_t n_pad) {
+  for (int32_t col = blockIdx.y; col < ncol; col += gridDim.y) {
+    if (need[col] != kNeedCopy) continue;
+    const double* src = arena + (int64_t)kept[col] * n_pad;
+    double* dst = table + (int64_t)col * n_pad;
+    for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n_pad; r += (int64_t)gridDim.x * blockDim.x)
+      dst[r] = src[r];
+    if (blockIdx.x == 0 && threadIdx.x == 0) table_cs[col] = arena_cs[kept[col]];
+  }
+}
+
+// Columns of a completed round's table into cache slots: pair i copies
+// table column pairs[2i] to arena slot pairs[2i + 1], with its statistics.
+__global__ void cache_store_kernel(const int32_t* pairs, int32_t n_pairs, const double* table, const ColStat* table_cs,
+                                   double* arena, ColStat* arena_cs, int64_t n_pad) {
+  for (int32_t i = blockIdx.y; i < n_pairs; i += gridDim.y) {
+    const int32_t col = pairs[2 * i], slot = pairs[2 * i + 1];
+    const double* src = table + (int64_t)col * n_pad;
+    double* dst = arena + (int64_t)slot * n_pad;
+    for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n_pad; r += (int64_t)gridDim.x * blockDim.x)
+      dst[r] = src[r];
+    if (blockIdx.x == 0 && threadIdx.x == 0) arena_cs[slot] = table_cs[col];
+  }
+}
+
 }  // namespace
+
+bool launch_lane_copy(const uint8_t* need, const int32_t* kept, int32_t ncol, const double* arena,
+                      const ColStat* arena_cs, double* table, ColStat* table_cs, int64_t n_pad, cudaStream_t st) {
+  if (ncol <= 0) return true;
+  const dim3 grid((unsigned)std::min<int64_t>(16, (n_pad + 4095) / 4096), (unsigned)std::min(ncol, 4096));
+  lane_copy_kernel<<<grid, 256, 0, st>>>(need, kept, ncol, arena, arena_cs, table, table_cs, n_pad);
+  return launch_ok("launch_lane_copy");
+}
+
+bool launch_cache_store(const int32_t* pairs, int32_t n_pairs, const double* table, const ColStat* table_cs,
+                        double* arena, ColStat* arena_cs, int64_t n_pad, cudaStream_t st) {
+  if (n_pairs <= 0) return true;
+  const dim3 grid((unsigned)std::min<int64_t>(64, (n_pad + 4095) / 4096), (unsigned)std::min(n_pairs, 4096));
+  cache_store_kernel<<<grid, 256, 0, st>>>(pairs, n_pairs, table, table_cs, arena, arena_cs, n_pad);
+  return launch_ok("launch_cache_store");
+}
 
 bool launch_pass2_compact(const int32_t* list, int32_t cnt, const uint8_t* pass2, int32_t* list2, int32_t* count2,
                           cudaStream_t st) {
@@ -105,10 +153,10 @@ bool launch_pass2_compact(const int32_t* list, int32_t cnt, const uint8_t* pass2
 }
 
 bool launch_rescore_mark(const rrg_cand* cands, const int32_t* fb, int32_t cap, const int32_t* li_of,
-                         const int32_t* cand_col, const int32_t* dep_off, const int32_t* deps, uint8_t* need,
-                         cudaStream_t st) {
+                         const int32_t* cand_col, const int32_t* dep_off, const int32_t* deps, const int32_t* kept,
+                         uint8_t* need, cudaStream_t st) {
   if (cap <= 0) return true;
-  rescore_mark_kernel<<<(cap + 127) / 128, 128, 0, st>>>(cands, fb, cap, li_of, cand_col, dep_off, deps, need);
+  rescore_mark_kernel<<<(cap + 127) / 128, 128, 0, st>>>(cands, fb, cap, li_of, cand_col, dep_off, deps, kept, need);
   return launch_ok("launch_rescore_mark");
 }
 

@@ -45,6 +45,13 @@ bool cuda_ok(cudaError_t e, const char* what) {
 constexpr int32_t kCrossTag = 1 << 30;
 // most slots a column arena holds (the bookkeeping scans them)
 constexpr int64_t kCacheSlotsMax = 1 << 16;
+// FP64 column arena: slots of the scratch budget's half for the FP64 table
+int64_t fp64_cache_slots(size_t scratch_bytes, int64_t n_pad) {
+  const double col8 = 8.0 * (double)n_pad;
+  const int64_t fcap =
+      std::min<int64_t>(kCacheSlotsMax, std::max<int64_t>(2 * RRG_MAX_TERMS, (int64_t)(scratch_bytes / 3 / col8)));
+  return std::min<int64_t>(kCacheSlotsMax, std::max<int64_t>(fcap, (int64_t)(scratch_bytes / 2 / col8)));
+}
 // rows from which rounds keep their columns: below, evaluating a column
 // costs less than the bookkeeping of finding it (a 569-row classifier
 // search ran 0.46 ms per round slower with the cache)
@@ -1123,9 +1130,35 @@ rrg_status rrg_context::mixed_subround(const rrg_dataset* ds, const int32_t* lis
     const bool fits = (double)m_cols * (double)col8 <= (double)scratch_budget_bytes / 2 &&
                       (double)ncol * (double)col8 <= (double)scratch_budget_bytes / 2;
     if (fits) {
+      // FP64 column cache: a factor column it holds is copied into the
+      // lane's table when a re-scored candidate reads it (kept[col] = its
+      // slot); the factor columns the lane evaluates are stored into it when
+      // the next round starts (which ones, the device decides: the lane's
+      // marks are read back with the round's results)
+      std::vector<int32_t> kept(std::max(1, ncol), -1);
+      const bool keep64 = cache_on && ds->n >= kCacheMinRows;
+      int64_t n_kept = 0;
+      if (keep64) {
+        const int64_t pl = fp64_cache_slots(scratch_budget_bytes, ds->n_pad);
+        if (pcache.limit() != pl || pcache_npad != ds->n_pad) {
+          pcache.reset(pl);
+          pcache_npad = ds->n_pad;
+        }
+        pcache.bind(ds->uid);
+        pcache.begin();
+        for (int32_t l = 0; l < nfl; ++l) {
+          const FactorProg fp{lcode.data() + lmeta[l].x, lmeta[l].y, consts64};
+          const int32_t sl = pcache.find(fp, fp.hash());
+          if (sl >= 0) {
+            kept[tp.fcol[l]] = sl;
+            ++n_kept;
+          }
+        }
+      }
       // host records of the lane: one-column pseudo-candidates of the table
-      // programs, the shared-column closure of every column, placements of
-      // the round's candidates (factor columns through cand_col)
+      // programs, the shared-column closure of every column (a kept column's
+      // own closure is not needed), placements of the round's candidates
+      // (factor columns through cand_col)
       std::vector<rrg_cand> fc(std::max(1, ncol));
       std::vector<PlainCand> fpc(std::max(1, ncol));
       std::vector<int32_t> dep_off(ncol + 1, 0), deps;
@@ -1150,7 +1183,7 @@ rrg_status rrg_context::mixed_subround(const rrg_dataset* ds, const int32_t* lis
           if (!tref) continue;
           const int32_t a = (int32_t)(w >> 8);
           cl.push_back(a);
-          cl.insert(cl.end(), closure[a].begin(), closure[a].end());  // a is of a lower level
+          if (kept[a] < 0) cl.insert(cl.end(), closure[a].begin(), closure[a].end());  // a is of a lower level
         }
         std::sort(cl.begin(), cl.end());
         cl.erase(std::unique(cl.begin(), cl.end()), cl.end());
@@ -1174,6 +1207,7 @@ rrg_status rrg_context::mixed_subround(const rrg_dataset* ds, const int32_t* lis
       const size_t o_liof = pf.add(li_of.data(), sizeof(int32_t) * li_of.size());
       const size_t o_pcs = pf.add(pcs.data(), sizeof(PlainCand) * pcs.size());
       const size_t o_lend = pf.add(tp.level_end.data(), sizeof(int32_t) * tp.level_end.size());
+      const size_t o_kept = pf.add(kept.data(), sizeof(int32_t) * kept.size());
       pst = pf.send(h_fbpack, d_fbpack, stream, round_seq);
       if (pst != RRG_OK) return pst;
       const int nb_res = (int)((ds->n + RR_CHUNK - 1) / RR_CHUNK);
@@ -1250,14 +1284,18 @@ rrg_status rrg_context::mixed_subround(const rrg_dataset* ds, const int32_t* lis
       fdev.n_cand = ncol;
       fdev.n_code = (int32_t)tp.code.size();
       clear_results_kernel<<<(cnt + 255) / 256, 256, 0, stream>>>(fb_list, cnt, res, fb_count);
+      const int32_t* d_kept = pf.at<const int32_t>(d_fbpack, o_kept);
       if (!launch_rescore_mark(dev.cands, fallback, cnt, pf.at<const int32_t>(d_fbpack, o_liof), d_ccol,
-                               pf.at<const int32_t>(d_fbpack, o_doff), pf.at<const int32_t>(d_fbpack, o_deps), need,
-                               stream) ||
+                               pf.at<const int32_t>(d_fbpack, o_doff), pf.at<const int32_t>(d_fbpack, o_deps),
+                               n_kept ? d_kept : nullptr, need, stream) ||
           !launch_rescore_levels(need, pf.at<const int32_t>(d_fbpack, o_lend), n_levels, lvl_cols, lvl_count,
-                                 stream)) {
+                                 stream) ||
+          (n_kept && !launch_lane_copy(need, d_kept, ncol, static_cast<const double*>(d_F64.ptr),
+                                       static_cast<const ColStat*>(d_ccst.ptr), F64, cst, ds->n_pad, stream))) {
         cuda_ok(cudaGetLastError(), "re-scoring list launch");
         return RRG_E_CUDA;
       }
+      last_cache64_hits += n_kept;
       bool wave_trial = false;
       int waves = tune_pick(TK_EVAL_WAVES, 0, ds->n, &wave_trial);
       const int max_nbc = (int)std::max<int64_t>(1, (ds->n + 1023) / 1024);
@@ -1366,6 +1404,30 @@ rrg_status rrg_context::mixed_subround(const rrg_dataset* ds, const int32_t* lis
       if (n_levels)
         RRG_CUDA(cudaMemcpyAsync(hs + 2 + kFbReasons, lvl_count, sizeof(int32_t) * n_levels, cudaMemcpyDeviceToHost,
                                  stream));
+      if (keep64) {
+        // the lane's marks, and the factor programs whose columns it may
+        // evaluate, for the store into the cache when the next round starts
+        if (!h_fbneed.reserve((size_t)std::max(1, ncol))) {
+          rrc::set_error("mixed round: staging allocation failed");
+          return RRG_E_OOM;
+        }
+        RRG_CUDA(cudaMemcpyAsync(h_fbneed.ptr, need, (size_t)std::max(1, ncol), cudaMemcpyDeviceToHost, stream));
+        LaneStore& ls = lane_store;
+        ls.valid = true;
+        ls.uid = ds->uid;
+        ls.n_pad = ds->n_pad;
+        ls.code.clear();
+        ls.meta.clear();
+        ls.col.clear();
+        const double* pool = consts64;
+        ls.consts.assign(pool, pool + std::max(0, dev.n_consts));
+        for (int32_t l = 0; l < nfl; ++l) {
+          if (kept[tp.fcol[l]] >= 0) continue;
+          ls.meta.push_back(make_int2((int)ls.code.size(), lmeta[l].y));
+          ls.code.insert(ls.code.end(), lcode.begin() + lmeta[l].x, lcode.begin() + lmeta[l].x + lmeta[l].y);
+          ls.col.push_back(tp.fcol[l]);
+        }
+      }
       fbstat_pending = true;
       fbstat_levels = n_levels;
       fbstat_rows = (double)ds->n;
@@ -1461,7 +1523,7 @@ rrg_status rrg_context::run_fp64_table(const rrg_dataset* ds, const std::vector<
       std::min<int64_t>(kCacheSlotsMax, std::max<int64_t>(2 * RRG_MAX_TERMS, (int64_t)(scratch_budget_bytes / 3 / col8)));
   const int64_t mcap = std::max<int64_t>(2 * RRG_MAX_TERMS + 2, (int64_t)(scratch_budget_bytes / 2 / col8));
   // FP64 column arena: the table's half of the scratch budget
-  const int64_t plimit = std::min<int64_t>(kCacheSlotsMax, std::max<int64_t>(fcap, (int64_t)(scratch_budget_bytes / 2 / col8)));
+  const int64_t plimit = fp64_cache_slots(scratch_budget_bytes, ds->n_pad);
   const int nb_res = (int)((ds->n + RR_CHUNK - 1) / RR_CHUNK);
   const size_t n_all = host_cands.size();
   if (!d_partial.reserve(sizeof(double) * n_all * (size_t)nb_res)) {
@@ -1776,3 +1838,51 @@ rrg_status rrg_context::run_fp64_table(const rrg_dataset* ds, const std::vector<
   return RRG_OK;
 }
 
+// The factor columns the previous round's re-scoring lane evaluated, from its
+// FP64 table into FP64 cache slots (the table is rewritten only by the next
+// lane, later on the same stream).  Called when a round starts; a store for
+// another dataset, or after the cache was cleared, is dropped.
+rrg_status rrg_context::store_lane_columns() {
+  if (!lane_store.valid) return RRG_OK;
+  LaneStore& ls = lane_store;
+  ls.valid = false;
+  if (!cache_on || pcache.uid() != ls.uid || pcache_npad != ls.n_pad || ls.col.empty()) return RRG_OK;
+  const uint8_t* need = static_cast<const uint8_t*>(h_fbneed.ptr);
+  pcache.begin();
+  std::vector<int32_t> fsel;
+  std::vector<uint64_t> hsel;
+  for (size_t f = 0; f < ls.col.size(); ++f) {
+    if (need[ls.col[f]] != kNeedEval) continue;
+    const FactorProg fp{ls.code.data() + ls.meta[f].x, ls.meta[f].y, ls.consts.data()};
+    const uint64_t h = fp.hash();
+    if (pcache.find(fp, h) >= 0) continue;  // stored meanwhile
+    fsel.push_back((int32_t)f);
+    hsel.push_back(h);
+  }
+  const int64_t k = std::min<int64_t>((int64_t)fsel.size(), pcache.available());
+  if (k <= 0) return RRG_OK;
+  std::vector<int32_t> slots;
+  if (!pcache.take(k, slots)) return RRG_OK;
+  std::vector<int32_t> pairs(2 * (size_t)k);
+  for (int64_t i = 0; i < k; ++i) {
+    const int32_t f = fsel[i];
+    pcache.insert(FactorProg{ls.code.data() + ls.meta[f].x, ls.meta[f].y, ls.consts.data()}, hsel[i], slots[i]);
+    pairs[2 * i] = ls.col[f];
+    pairs[2 * i + 1] = slots[i];
+  }
+  const size_t col8 = sizeof(double) * (size_t)ls.n_pad;
+  const size_t n_slots = (size_t)pcache.size();
+  if (!d_F64.grow_keep(col8 * n_slots, d_F64.cap) || !d_ccst.grow_keep(sizeof(ColStat) * n_slots, d_ccst.cap) ||
+      !h_store.reserve(sizeof(int32_t) * pairs.size()) || !d_store.reserve(sizeof(int32_t) * pairs.size())) {
+    rrc::set_error("column cache: allocation failed");
+    return RRG_E_OOM;
+  }
+  std::memcpy(h_store.ptr, pairs.data(), sizeof(int32_t) * pairs.size());
+  RRG_CUDA(cudaMemcpyAsync(d_store.ptr, h_store.ptr, sizeof(int32_t) * pairs.size(), cudaMemcpyHostToDevice, stream));
+  if (!launch_cache_store(static_cast<const int32_t*>(d_store.ptr), (int32_t)k, static_cast<const double*>(d_fbF64.ptr),
+                          static_cast<const ColStat*>(d_fbcst.ptr), static_cast<double*>(d_F64.ptr),
+                          static_cast<ColStat*>(d_ccst.ptr), ls.n_pad, stream))
+    return RRG_E_CUDA;
+  ++launches;
+  return RRG_OK;
+}

@@ -368,6 +368,13 @@ rrg_status rrg_context::submit(rrg_dataset* ds, const rrg_batch* b, int32_t prec
     // a reused staging buffer, table sub-rounds) is enqueued directly.
     cudaGraph_t g = nullptr;
     rrg_status cst = RRG_E_CUDA;
+    // the previous lane's columns go into the FP64 cache before the capture
+    // (storing them may grow the cache's arena, which a capture refuses)
+    const rrg_status sst = store_lane_columns();
+    if (sst != RRG_OK) {
+      clear_caches();
+      return sst;
+    }
     if (cudaStreamBeginCapture(stream, cudaStreamCaptureModeRelaxed) == cudaSuccess) {
       capturing = true;
       cst = enqueue_round(ds, b, precision, n_coefs);
@@ -435,6 +442,10 @@ rrg_status rrg_context::enqueue_round(rrg_dataset* ds, const rrg_batch* b, int32
   for (auto& r : last_reasons) r = 0;
   marks.clear();
   event_next = 0;
+  // columns the previous round's re-scoring lane evaluated go into the FP64
+  // column cache before anything of this round is queued
+  st = store_lane_columns();
+  if (st != RRG_OK) return st;
   st = stage_batch(b);
   if (st != RRG_OK) return st;
   const size_t res_bytes = sizeof(rrg_result) * std::max(1, b->n_cand);
@@ -548,7 +559,7 @@ std::vector<DevBuf*> rrg_context::all_bufs() {
   return {&d_batch, &d_A, &d_pc, &d_partial, &d_list, &d_qrs, &d_terms, &d_fallback, &d_sse1, &d_probe,
           &d_nanrow, &d_cert_e, &d_ft, &d_ftp, &d_ft64, &d_F, &d_P, &d_Pc, &d_psum, &d_F64, &d_M,
           &d_gram, &d_rlist2, &d_fbpack, &d_fbneed, &d_fbcols, &d_fbF64, &d_fbcst, &d_fbgram, &d_fbblist,
-          &d_fbM, &d_fbctr, &d_cself, &d_cprobe, &d_cfnan, &d_ccst, &d_slots, &d_res, &d_coefs, &d_status};
+          &d_fbM, &d_fbctr, &d_cself, &d_cprobe, &d_cfnan, &d_ccst, &d_slots, &d_store, &d_res, &d_coefs, &d_status};
 }
 
 // Persistent grid of the chunked QR's passes for `items` candidate x chunk items.
@@ -600,6 +611,8 @@ rrg_context::~rrg_context() {
   h_list.release();
   h_fbpack.release();
   h_fbstat.release();
+  h_fbneed.release();
+  h_store.release();
   h_ft.release();
   h_ftp.release();
   h_ft64.release();

@@ -118,9 +118,25 @@ struct rrg_context {
   int64_t fcache_npad = 0, pcache_npad = 0;  // the row padding the arenas' slots are sized for
   uint64_t next_uid = 0;
   int64_t last_cache_hits = 0, last_cache_evals = 0, last_cache64_hits = 0, last_cache64_evals = 0;
+  // the factor programs of the last re-scoring lane whose columns it may
+  // have evaluated (its marks come back in h_fbneed with the round), stored
+  // into the FP64 cache when the next round starts
+  struct LaneStore {
+    bool valid = false;
+    uint64_t uid = 0;
+    int64_t n_pad = 0;
+    std::vector<uint32_t> code;
+    std::vector<int2> meta;
+    std::vector<double> consts;
+    std::vector<int32_t> col;  // the lane table column of each program
+  } lane_store;
+  HostBuf h_fbneed, h_store;
+  DevBuf d_store;
+  rrg_status store_lane_columns();
   void clear_caches() {
     fcache.clear();
     pcache.clear();
+    lane_store.valid = false;
   }
   // results
   DevBuf d_res, d_coefs, d_status;

@@ -1,6 +1,7 @@
 """Factor columns kept across rounds (rrg_context_set_column_cache): the
-rounds of a search trajectory read the columns earlier rounds evaluated, and
-every result is the same bits as with the cache off, for each precision,
+rounds of a search trajectory read the columns earlier rounds evaluated (the
+double-float table, the FP64 table and the FP64 re-scoring lane of mixed
+rounds), and every result is the same bits as with the cache off, for each precision,
 under eviction pressure (a table limit of a few columns), across a switch of
 datasets, as CUDA graphs, and against the oracle."""
 import numpy as np
@@ -68,6 +69,12 @@ def test_cached_rounds_are_bit_identical(data, prec):
     assert s_on[0][key] == 0
     assert sum(s[key] for s in s_on[1:]) > 0  # later rounds read kept columns
     assert all(s[key] == 0 for s in s_off)
+    if prec != PLAIN:
+        # the FP64 re-scoring lane: columns it evaluated in one round are
+        # stored when the next starts, and later lanes copy them in
+        assert sum(s["fp64_rescored"] for s in s_on) > 0
+        assert sum(s["cache64_hits"] for s in s_on[2:]) > 0
+        assert all(s["cache64_hits"] == 0 for s in s_off)
     on.close()
     off.close()
 
