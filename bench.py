@@ -46,6 +46,7 @@ Measurement cases for profiling (one JSON line each, no bench contract):
 from __future__ import annotations
 
 import argparse
+import gc
 import gzip
 import json
 import os
@@ -252,6 +253,8 @@ def timed_rounds(ctx, ds, batches, prec, stream, flush):
 
     from rils_rols_gb300.fitness import decode_results, result_dtype
     bufs = [(np.zeros(len(b), dtype=result_dtype()), np.zeros(max(1, b.n_coefs), dtype=np.float64)) for b in batches]
+    gc.collect()
+    gc.disable()  # no collector pause of the harness inside the timed region
     with torch.cuda.stream(stream):
         flush.zero_()
         e0 = torch.cuda.Event(enable_timing=True)
@@ -264,6 +267,7 @@ def timed_rounds(ctx, ds, batches, prec, stream, flush):
     with torch.cuda.stream(stream):
         e1.record(stream)
     e1.synchronize()
+    gc.enable()
     return e0.elapsed_time(e1) / 1e3, [decode_results(r, c, b) for b, (r, c) in zip(batches, bufs)]
 
 
@@ -328,6 +332,7 @@ def run_ours(args):
     e2e_times = []
     for step in range(args.warmup + args.steps):
         torch.cuda.synchronize()
+        gc.collect()
         t = time.perf_counter()
         d2 = ctx.dataset(Xp, yp)
         for r in rounds:
@@ -373,7 +378,9 @@ def run_ours(args):
         "double_float_columns_read": sum(st["cache_hits"] for st in stats),
         "double_float_columns_evaluated": sum(st["cache_evals"] for st in stats),
         "fp64_columns_read": sum(st["cache64_hits"] for st in stats),
-        "fp64_columns_evaluated": sum(st["cache64_evals"] for st in stats)}
+        "fp64_columns_evaluated": sum(st["cache64_evals"] for st in stats),
+        "pair_sums_read": sum(st["pair_hits"] for st in stats),
+        "pair_sums_formed": sum(st["pair_evals"] for st in stats)}
     if args.quick:
         print(json.dumps(res))
         return

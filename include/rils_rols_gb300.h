@@ -242,7 +242,8 @@ int64_t rrg_last_round_launches(const rrg_context* ctx);
  *   round ran as a CUDA graph (rrg_context_set_graph).  [19] double-float
  *   factor columns read from the column cache (rrg_context_set_column_cache)
  *   [20] double-float table columns evaluated  [21] FP64 factor columns read
- *   from the column cache  [22] FP64 table columns evaluated.
+ *   from the column cache  [22] FP64 table columns evaluated  [23] cross-pair
+ *   sums read from the column cache  [24] cross-pair sums formed.
  * Returns the count written. */
 int32_t rrg_last_round_stats(const rrg_context* ctx, int64_t* out, int32_t n);
 
@@ -258,8 +259,9 @@ rrg_status rrg_context_set_limits(rrg_context* ctx, int64_t scratch_bytes, int64
  * and of the dataset alone, and the consecutive rounds of a search share
  * most factors, so a round reads the columns an earlier round on the same
  * dataset evaluated instead of evaluating them again: the double-float
- * columns of mixed rounds (with their sums and probe records) and the FP64
- * columns of FP64 rounds, within the limits of rrg_context_set_limits, least
+ * columns of mixed rounds (with their sums, probe records and cross-pair
+ * sums) and the FP64 columns of FP64 rounds and of the mixed rounds' FP64
+ * re-scoring, within the limits of rrg_context_set_limits, least
  * recently used columns replaced first.  Results are the same bits either
  * way.  Switching clears what is kept; so do destroying the dataset, a round
  * on another dataset and a failed round.  RRG_E_INVALID while a round is in

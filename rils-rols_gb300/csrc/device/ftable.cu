@@ -457,6 +457,13 @@ __global__ void __launch_bounds__(kFacThreads) fac_eval_kernel(const __grid_cons
   }
 }
 
+// low part of the double-float product (ah, al) x (bh, bl), symmetric in the
+// two operands: fma(ah, bh, -ah*bh) + (ah*bl + al*bh)
+__device__ __forceinline__ float pair_lo(float ah, float al, float bh, float bl) {
+  const float p = DF_MUL(ah, bh);
+  return DF_ADD(DF_FMA(ah, bh, -p), DF_ADD(DF_MUL(ah, bl), DF_MUL(al, bh)));
+}
+
 __global__ void __launch_bounds__(kPairThreads) pair_sum_kernel(PairArgs a) {
   __shared__ float red[kPairBatch][kPairThreads / 32][2];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -484,11 +491,12 @@ __global__ void __launch_bounds__(kPairThreads) pair_sum_kernel(PairArgs a) {
           const float4 bv = *reinterpret_cast<const float4*>(fb + r);
           // without the non-finite guards: a non-finite factor value turns the
           // sum NaN instead of +-inf, and the solve sends every candidate with a
-          // non-finite cross sum (NaN or inf alike) to the FP64 path
-          const float p0v = DF_MUL(av[s].x, bv.x);
-          acc2(acc, p0v, DF_FMA(av[s].y, bv.x, DF_FMA(av[s].x, bv.y, DF_FMA(av[s].x, bv.x, -p0v))));
-          const float p1v = DF_MUL(av[s].z, bv.z);
-          acc2(acc, p1v, DF_FMA(av[s].w, bv.z, DF_FMA(av[s].z, bv.w, DF_FMA(av[s].z, bv.z, -p1v))));
+          // non-finite cross sum (NaN or inf alike) to the FP64 path.  The
+          // product is symmetric in its operands (the exact error of hi x hi,
+          // then the rounded sum of the two rounded cross products), so a
+          // pair's sum is the same bits whichever factor a unit holds
+          acc2(acc, DF_MUL(av[s].x, bv.x), pair_lo(av[s].x, av[s].y, bv.x, bv.y));
+          acc2(acc, DF_MUL(av[s].z, bv.z), pair_lo(av[s].z, av[s].w, bv.z, bv.w));
         }
       }
       const dfl v = warp_dfl_sum(dfl_renorm(acc));
@@ -509,7 +517,7 @@ __global__ void __launch_bounds__(kPairThreads) pair_sum_kernel(PairArgs a) {
 
 // psum[p] = sum over chunks q (in order) of P[q][p], in FP64.
 __global__ void pair_reduce_kernel(const float2* P, int32_t n_pairs, int32_t n_chunks, int32_t p0, int32_t p1,
-                                   double* psum, const int32_t* smap) {
+                                   double* psum, const int32_t* smap, const int32_t* omap) {
   const int p = p0 + blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= p1) return;
   double s = 0.0;
@@ -517,7 +525,7 @@ __global__ void pair_reduce_kernel(const float2* P, int32_t n_pairs, int32_t n_c
     const float2 v = P[(size_t)q * n_pairs + p];
     s = __dadd_rn(s, __dadd_rn((double)v.x, (double)v.y));
   }
-  psum[smap ? 3 * (int64_t)smap[p / 3] + p % 3 : (int64_t)p] = s;
+  psum[omap ? (int64_t)omap[p] : (smap ? 3 * (int64_t)smap[p / 3] + p % 3 : (int64_t)p)] = s;
 }
 
 __global__ void fill_slots_kernel(const int32_t* idx, int32_t n, unsigned long long* dst, int words,
@@ -691,9 +699,9 @@ bool launch_pair_sum(const PairArgs& a, int n_super, cudaStream_t st) {
   return launch_ok("launch_pair_sum");
 }
 bool launch_pair_reduce(const float2* P, int32_t n_pairs, int32_t n_chunks, int32_t p0, int32_t p1, double* psum,
-                        cudaStream_t st, const int32_t* smap) {
+                        cudaStream_t st, const int32_t* smap, const int32_t* omap) {
   if (p1 <= p0) return true;
-  pair_reduce_kernel<<<(p1 - p0 + 255) / 256, 256, 0, st>>>(P, n_pairs, n_chunks, p0, p1, psum, smap);
+  pair_reduce_kernel<<<(p1 - p0 + 255) / 256, 256, 0, st>>>(P, n_pairs, n_chunks, p0, p1, psum, smap, omap);
   return launch_ok("launch_pair_reduce");
 }
 bool launch_fill_slots(const int32_t* idx, int32_t n, unsigned long long* dst, int words, unsigned long long v,

@@ -114,8 +114,9 @@ bool launch_pair_sum(const PairArgs& a, int n_row_blocks, cudaStream_t st);
 // psum[p] for p in [p0, p1): FP64 sum over the first n_chunks rows of P.
 // smap (may be NULL; self pairs): the sum of pair p goes to
 // psum[3 * smap[p / 3] + p % 3] instead (program p / 3's column).
+// omap (may be NULL): the sum of pair p goes to psum[omap[p]].
 bool launch_pair_reduce(const float2* P, int32_t n_pairs, int32_t n_chunks, int32_t p0, int32_t p1, double* psum,
-                        cudaStream_t st, const int32_t* smap = nullptr);
+                        cudaStream_t st, const int32_t* smap = nullptr, const int32_t* omap = nullptr);
 // dst[idx[i] * words + w] = v for i < n, w < words (per-slot records of a
 // column arena)
 bool launch_fill_slots(const int32_t* idx, int32_t n, unsigned long long* dst, int words, unsigned long long v,

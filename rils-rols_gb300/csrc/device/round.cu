@@ -45,6 +45,10 @@ bool cuda_ok(cudaError_t e, const char* what) {
 constexpr int32_t kCrossTag = 1 << 30;
 // most slots a column arena holds (the bookkeeping scans them)
 constexpr int64_t kCacheSlotsMax = 1 << 16;
+// pair cache: slots of the pair array (8 bytes each); registry size at which
+// the factor ids start afresh
+constexpr int64_t kPairSlots = 1 << 22;
+constexpr size_t kRegistryMax = (size_t)1 << 19;
 // mixed rounds with fewer candidates decide their second half on the host
 constexpr int64_t kAsyncMinCands = 64;
 // FP64 column arena: slots of the scratch budget's half for the FP64 table
@@ -903,24 +907,45 @@ rrg_status rrg_context::mixed_subround(const rrg_dataset* ds, const int32_t* lis
   } else if (!gtrial && !eval_all(gsets[0], stage_pick && stage_ok)) {
     return RRG_E_CUDA;
   }
-  // pair map over table columns: self pairs 3t..3t+2, cross pairs oriented
-  // so that `a` is the rarer factor (its partners are then the widely shared
-  // ones, hot in L2)
+  // Pair map: self pairs by slot (entries -2 - p into the slots' self
+  // sums); cross pairs oriented so that `a` is the rarer factor (its
+  // partners are then the widely shared ones, hot in L2) and kept across
+  // rounds like the columns (the pair cache, keyed by the two factors'
+  // registry ids; a pair's sum is the same bits in either orientation):
+  // only the pairs not found are summed, into their slots of the pair array.
+  auto prog_of = [&](int32_t l) { return FactorProg{lcode.data() + lmeta[l].x, lmeta[l].y, consts64}; };
+  const bool keepp = cp.kept;
+  std::vector<uint32_t> fid;
+  if (keepp) {
+    if (freg.size() > kRegistryMax) {
+      freg.clear();
+      pairc.clear();
+    }
+    if (pairc.limit() != kPairSlots) pairc.reset(kPairSlots);
+    pairc.bind(ds->uid);
+    pairc.begin();
+    fid.resize(nfl);
+    for (int32_t l = 0; l < nfl; ++l) {
+      const FactorProg fp = prog_of(l);
+      fid[l] = freg.id(fp, fp.hash());
+    }
+  } else if (pairc.size() > 0) {
+    pairc.reset(pairc.limit());  // the pair array is rewritten from slot 0 below
+  }
   std::unordered_map<uint64_t, int32_t> cmap;
   cmap.reserve((size_t)cnt * 4 + 16);
-  std::vector<std::pair<int32_t, int32_t>> cross;
+  std::vector<std::pair<int32_t, int32_t>> cross;  // (a, b) local factors, oriented
   std::vector<int32_t> pair_of((size_t)cnt * kMixedE, -1), cand_fac((size_t)cnt * kMixedMaxM, 0);
   std::vector<int32_t> cand_col((size_t)cnt * kMixedMaxM, 0), cand_slot((size_t)cnt * kMixedMaxM, 0);
   auto cross_id = [&](int32_t x, int32_t y) {
     const int32_t gx = lf[x], gy = lf[y];
-    const bool xa = ft.occ[gx] < ft.occ[gy] || (ft.occ[gx] == ft.occ[gy] && gx < gy);
-    const int32_t a = fslot[xa ? x : y], b = fslot[xa ? y : x];
-    const uint64_t key = ((uint64_t)(uint32_t)a << 32) | (uint32_t)b;
+    if (!(ft.occ[gx] < ft.occ[gy] || (ft.occ[gx] == ft.occ[gy] && gx < gy))) std::swap(x, y);
+    const uint64_t key = ((uint64_t)(uint32_t)x << 32) | (uint32_t)y;
     auto it = cmap.find(key);
     if (it != cmap.end()) return it->second;
     const int32_t id = (int32_t)cross.size();
     cmap.emplace(key, id);
-    cross.push_back({a, b});
+    cross.push_back({x, y});
     return id;
   };
   constexpr int Gn = GramSize<kMixedMaxM>::G;
@@ -946,36 +971,64 @@ rrg_status rrg_context::mixed_subround(const rrg_dataset* ds, const int32_t* lis
       po[Gn + kMixedMaxM + i] = -2 - (3 * fslot[l[i]] + 2);
     }
   }
-  // cross pairs sorted by (a, b); units = runs of equal a
+  // slots of the cross pairs; the pairs to sum (not found)
   const int32_t n_cross = (int32_t)cross.size();
-  std::vector<int32_t> order(n_cross), rank(n_cross), partner(n_cross);
-  std::iota(order.begin(), order.end(), 0);
-  std::sort(order.begin(), order.end(), [&](int32_t x, int32_t y) { return cross[x] < cross[y]; });
-  for (int32_t k = 0; k < n_cross; ++k) {
-    rank[order[k]] = k;
-    partner[k] = cross[order[k]].second;
+  std::vector<int32_t> cslot(n_cross), miss;
+  if (keepp) {
+    std::vector<uint64_t> pkey(n_cross);
+    for (int32_t k = 0; k < n_cross; ++k) {
+      const uint32_t ia = fid[cross[k].first], ib = fid[cross[k].second];
+      pkey[k] = ((uint64_t)std::min(ia, ib) << 32) | std::max(ia, ib);
+      cslot[k] = pairc.find(pkey[k]);
+      if (cslot[k] < 0) miss.push_back(k);
+    }
+    std::vector<int32_t> got;
+    if (!pairc.take((int64_t)miss.size(), got)) {
+      rrc::set_error("mixed round: the pair cache has no room for the sub-round");
+      return RRG_E_OOM;
+    }
+    for (size_t i = 0; i < miss.size(); ++i) {
+      cslot[miss[i]] = got[i];
+      pairc.insert(pkey[miss[i]], got[i]);
+    }
+  } else {
+    for (int32_t k = 0; k < n_cross; ++k) cslot[k] = k;
+    miss.resize(n_cross);
+    std::iota(miss.begin(), miss.end(), 0);
   }
+  const int32_t n_miss = (int32_t)miss.size();
+  last_pair_hits += n_cross - n_miss;
+  last_pair_evals += n_miss;
   for (int32_t& p : pair_of)
-    if (p >= kCrossTag) p = rank[p - kCrossTag];
+    if (p >= kCrossTag) p = cslot[p - kCrossTag];
+  // the pairs to sum by (a's slot, b's slot); units = runs of equal a
+  std::vector<int32_t> order(miss), partner(n_miss), omap(n_miss);
+  auto slot_pair = [&](int32_t k) { return std::make_pair(fslot[cross[k].first], fslot[cross[k].second]); };
+  std::sort(order.begin(), order.end(), [&](int32_t x, int32_t y) { return slot_pair(x) < slot_pair(y); });
+  for (int32_t i = 0; i < n_miss; ++i) {
+    partner[i] = fslot[cross[order[i]].second];
+    omap[i] = cslot[order[i]];
+  }
   // units of at most `maxp` partners (a launch shape only: each pair's sum
   // is formed alone; the tuner's TK_PAIR_UNIT)
   auto build_units = [&](int maxp, std::vector<int4>& units) {
-    for (int32_t k = 0; k < n_cross;) {
-      const int32_t a = cross[order[k]].first;
+    for (int32_t k = 0; k < n_miss;) {
+      const int32_t a = fslot[cross[order[k]].first];
       int32_t e = k;
-      while (e < n_cross && cross[order[e]].first == a) ++e;
+      while (e < n_miss && fslot[cross[order[e]].first] == a) ++e;
       for (int32_t s0 = k; s0 < e; s0 += maxp) units.push_back(make_int4(a, s0, std::min(e, s0 + maxp), 0));
       k = e;
     }
   };
   bool ptrial = false;
   int pvals[4] = {tune_pick(TK_PAIR_UNIT, 0, ds->n, &ptrial), 0, 0, 0};
-  ptrial = ptrial && !capturing && (int64_t)n_cross * ds->n >= kTuneMinWork;
+  ptrial = ptrial && !capturing && (int64_t)n_miss * ds->n >= kTuneMinWork;
   const int npv = ptrial ? tune_variants(TK_PAIR_UNIT, 0, pvals) : 1;
   std::vector<std::vector<int4>> usets(npv);
   for (int v = 0; v < npv; ++v) build_units(pvals[v], usets[v]);
-  if (!d_Pc.reserve(sizeof(float2) * (size_t)n_super * std::max(1, n_cross)) ||
-      !d_psum.reserve(sizeof(double) * std::max(1, n_cross))) {
+  const size_t n_pslots = (size_t)std::max<int64_t>(1, keepp ? pairc.size() : n_cross);
+  if (!d_Pc.reserve(sizeof(float2) * (size_t)n_super * std::max(1, n_miss)) ||
+      !d_psum.grow_keep(sizeof(double) * n_pslots, d_psum.cap)) {
     rrc::set_error("mixed round: factor table allocation failed");
     return RRG_E_OOM;
   }
@@ -997,7 +1050,8 @@ rrg_status rrg_context::mixed_subround(const rrg_dataset* ds, const int32_t* lis
   const size_t o_cslot = pk.add(cand_slot.data(), sizeof(int32_t) * cand_slot.size());
   std::vector<size_t> o_units(npv);
   for (int v = 0; v < npv; ++v) o_units[v] = pk.add(usets[v].data(), sizeof(int4) * usets[v].size());
-  const size_t o_partner = pk.add(partner.data(), sizeof(int32_t) * partner.size());
+  const size_t o_partner = pk.add(partner.data(), sizeof(int32_t) * std::max<size_t>(1, partner.size()));
+  const size_t o_omap = pk.add(omap.data(), sizeof(int32_t) * std::max<size_t>(1, omap.size()));
   const size_t o_pair = pk.add(pair_of.data(), sizeof(int32_t) * pair_of.size());
   const size_t o_list = pk.add(list, sizeof(int32_t) * cnt);
   const size_t o_cfac = pk.add(cand_fac.data(), sizeof(int32_t) * cand_fac.size());
@@ -1027,7 +1081,7 @@ rrg_status rrg_context::mixed_subround(const rrg_dataset* ds, const int32_t* lis
   pa.n_pad = ds->n_pad;
   pa.partner = pk.at<const int32_t>(d_ft, o_partner);
   pa.P = Pcross;
-  pa.n_pairs = n_cross;
+  pa.n_pairs = n_miss;
   pa.cross0 = 0;
   auto pair_all = [&](int v) {
     pa.units = pk.at<const int4>(d_ft, o_units[v]);
@@ -1052,7 +1106,8 @@ rrg_status rrg_context::mixed_subround(const rrg_dataset* ds, const int32_t* lis
   phase_bytes[P_PAIRS] += (double)ds->n * 8.0 * (double)nfl;
   t0 = mark_begin();
   if (!launch_pair_reduce(Pself, n_self, n_chunks, 0, n_self, cself, stream, d_ewcol) ||
-      !launch_pair_reduce(Pcross, n_cross, n_super, 0, n_cross, psum, stream) ||
+      !launch_pair_reduce(Pcross, n_miss, n_super, 0, n_miss, psum, stream, nullptr,
+                          pk.at<const int32_t>(d_ft, o_omap)) ||
       !launch_fac_probe(d_code, d_meta, (int32_t)mprog.size(), dev.consts, dev.consts32, dev.consts32lo, dd, cprobe,
                         stream, pk.at<const int32_t>(d_ft, o_pslot)) ||
       !launch_cand_probe(dev.cands, d_list, cnt, d_cfac, nullptr, cprobe, fnan,

@@ -438,6 +438,7 @@ rrg_status rrg_context::enqueue_round(rrg_dataset* ds, const rrg_batch* b, int32
   launches = 0;
   last_plain_routed = last_fallback = last_pass2 = last_sentinel = 0;
   last_cache_hits = last_cache_evals = last_cache64_hits = last_cache64_evals = 0;
+  last_pair_hits = last_pair_evals = 0;
   for (double& v : phase_bytes) v = 0.0;
   for (auto& r : last_reasons) r = 0;
   marks.clear();
@@ -844,6 +845,7 @@ rrg_status rrg_dataset_destroy(rrg_dataset* ds) {
     // its kept columns go with it
     if (ctx->fcache.uid() == ds->uid) ctx->fcache.bind(0);
     if (ctx->pcache.uid() == ds->uid) ctx->pcache.bind(0);
+    if (ctx->pairc.uid() == ds->uid) ctx->pairc.bind(0);
     auto it = std::find(ctx->datasets.begin(), ctx->datasets.end(), ds);
     if (it != ctx->datasets.end()) ctx->datasets.erase(it);
   }
@@ -914,7 +916,7 @@ int64_t rrg_last_round_launches(const rrg_context* ctx) { return ctx ? ctx->last
 
 int32_t rrg_last_round_stats(const rrg_context* ctx, int64_t* out, int32_t n) {
   if (!ctx || !out || n <= 0) return 0;
-  int64_t v[12 + kFbReasons] = {ctx->last_launches, ctx->last_plain_routed, ctx->last_fallback, ctx->last_pass2};
+  int64_t v[14 + kFbReasons] = {ctx->last_launches, ctx->last_plain_routed, ctx->last_fallback, ctx->last_pass2};
   for (int i = 0; i < kFbReasons; ++i) v[4 + i] = ctx->last_reasons[i];
   v[4 + kFbReasons] = ctx->last_sentinel;
   v[5 + kFbReasons] = ctx->last_distinct;
@@ -924,7 +926,9 @@ int32_t rrg_last_round_stats(const rrg_context* ctx, int64_t* out, int32_t n) {
   v[9 + kFbReasons] = ctx->last_cache_evals;
   v[10 + kFbReasons] = ctx->last_cache64_hits;
   v[11 + kFbReasons] = ctx->last_cache64_evals;
-  const int32_t k = n < 12 + kFbReasons ? n : 12 + kFbReasons;
+  v[12 + kFbReasons] = ctx->last_pair_hits;
+  v[13 + kFbReasons] = ctx->last_pair_evals;
+  const int32_t k = n < 14 + kFbReasons ? n : 14 + kFbReasons;
   for (int32_t i = 0; i < k; ++i) out[i] = v[i];
   return k;
 }

@@ -114,10 +114,13 @@ struct rrg_context {
   // statistics d_ccst)
   bool cache_on = true;
   ColumnCache fcache, pcache;
+  FactorRegistry freg;  // factor ids of the pair cache
+  PairCache pairc;      // cross-pair sums kept across rounds (slots of d_psum)
   DevBuf d_cself, d_cprobe, d_cfnan, d_ccst, d_slots;
   int64_t fcache_npad = 0, pcache_npad = 0;  // the row padding the arenas' slots are sized for
   uint64_t next_uid = 0;
   int64_t last_cache_hits = 0, last_cache_evals = 0, last_cache64_hits = 0, last_cache64_evals = 0;
+  int64_t last_pair_hits = 0, last_pair_evals = 0;
   // the factor programs of the last re-scoring lane whose columns it may
   // have evaluated (its marks come back in h_fbneed with the round), stored
   // into the FP64 cache when the next round starts
@@ -136,6 +139,7 @@ struct rrg_context {
   void clear_caches() {
     fcache.clear();
     pcache.clear();
+    pairc.clear();
     lane_store.valid = false;
   }
   // results

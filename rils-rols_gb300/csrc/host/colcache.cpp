@@ -163,3 +163,89 @@ void ColumnCache::give_back(const std::vector<int32_t>& s) {
     free_.push_back(v);
   }
 }
+
+uint32_t FactorRegistry::id(const FactorProg& p, uint64_t h) {
+  auto it = head_.find(h);
+  int32_t first = it == head_.end() ? -1 : it->second;
+  for (int32_t q = first; q >= 0; q = e_[q].next) {
+    const std::vector<uint64_t>& k = e_[q].key;
+    size_t j = 0;
+    bool ok = true;
+    for (int i = 0; i < p.len && ok; ++i)
+      key_words(p.code[i], p.consts, [&](uint64_t v) {
+        ok = ok && j < k.size() && k[j] == v;
+        ++j;
+      });
+    if (ok && j == k.size()) return (uint32_t)q;
+  }
+  Entry en;
+  for (int i = 0; i < p.len; ++i) key_words(p.code[i], p.consts, [&](uint64_t v) { en.key.push_back(v); });
+  en.next = first;
+  e_.push_back(std::move(en));
+  head_[h] = (int32_t)e_.size() - 1;
+  return (uint32_t)e_.size() - 1;
+}
+
+void PairCache::clear() {
+  pinned_ = 0;
+  map_.clear();
+  free_.clear();
+  for (int32_t s = (int32_t)slot_.size() - 1; s >= 0; --s) {
+    slot_[s].held = false;
+    slot_[s].last = -1;
+    free_.push_back(s);
+  }
+}
+
+int32_t PairCache::find(uint64_t key) {
+  auto it = map_.find(key);
+  if (it == map_.end()) return -1;
+  Slot& sl = slot_[it->second];
+  if (sl.last != stamp_) ++pinned_;
+  sl.last = stamp_;
+  return it->second;
+}
+
+bool PairCache::take(int64_t count, std::vector<int32_t>& out) {
+  out.clear();
+  if (count <= 0) return true;
+  if (available() < count) return false;
+  while ((int64_t)out.size() < count && !free_.empty()) {
+    out.push_back(free_.back());
+    free_.pop_back();
+  }
+  if ((int64_t)out.size() < count && (int64_t)slot_.size() < limit_) {
+    const int64_t want = count - (int64_t)out.size();
+    const int64_t grow = std::min(limit_ - (int64_t)slot_.size(), std::max(want, (int64_t)slot_.size()));
+    const int32_t s0 = (int32_t)slot_.size();
+    slot_.resize(slot_.size() + (size_t)grow);
+    for (int32_t s = s0; s < (int32_t)slot_.size(); ++s) {
+      if ((int64_t)out.size() < count) out.push_back(s);
+      else free_.push_back(s);
+    }
+  }
+  if ((int64_t)out.size() < count) {
+    std::vector<std::pair<int64_t, int32_t>> old;
+    for (int32_t s = 0; s < (int32_t)slot_.size(); ++s)
+      if (slot_[s].held && slot_[s].last < stamp_) old.push_back({slot_[s].last, s});
+    const size_t need = (size_t)(count - (int64_t)out.size());
+    std::partial_sort(old.begin(), old.begin() + need, old.end());
+    for (size_t i = 0; i < need; ++i) {
+      Slot& sl = slot_[old[i].second];
+      map_.erase(sl.key);
+      sl.held = false;
+      out.push_back(old[i].second);
+    }
+  }
+  for (int32_t s : out) slot_[s].last = stamp_;
+  pinned_ += count;
+  return true;
+}
+
+void PairCache::insert(uint64_t key, int32_t s) {
+  Slot& sl = slot_[s];
+  sl.key = key;
+  sl.held = true;
+  sl.last = stamp_;
+  map_[key] = s;
+}

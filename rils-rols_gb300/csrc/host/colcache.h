@@ -26,6 +26,68 @@ struct FactorProg {
   uint64_t hash() const;
 };
 
+// Persistent ids of the factor programs seen on one dataset (found by hash,
+// confirmed word by word): the keys of the pair cache.
+class FactorRegistry {
+ public:
+  void clear() {
+    e_.clear();
+    head_.clear();
+  }
+  size_t size() const { return e_.size(); }
+  uint32_t id(const FactorProg& p, uint64_t h);
+
+ private:
+  struct Entry {
+    std::vector<uint64_t> key;
+    int32_t next = -1;
+  };
+  std::vector<Entry> e_;
+  std::unordered_map<uint64_t, int32_t> head_;
+};
+
+// Pair sums kept across rounds: a map from a pair of factor ids to a slot
+// of a device array, least recently used slots replaced (the bookkeeping
+// of ColumnCache with exact 64-bit keys).
+class PairCache {
+ public:
+  void reset(int64_t limit) {
+    slot_.clear();
+    free_.clear();
+    map_.clear();
+    limit_ = limit;
+    pinned_ = 0;
+  }
+  void clear();
+  void bind(uint64_t ds_uid) {
+    if (ds_uid != uid_) clear();
+    uid_ = ds_uid;
+  }
+  uint64_t uid() const { return uid_; }
+  int64_t limit() const { return limit_; }
+  int64_t size() const { return (int64_t)slot_.size(); }
+  void begin() {
+    ++stamp_;
+    pinned_ = 0;
+  }
+  int32_t find(uint64_t key);
+  int64_t available() const { return limit_ - pinned_; }
+  bool take(int64_t count, std::vector<int32_t>& out);
+  void insert(uint64_t key, int32_t s);
+
+ private:
+  struct Slot {
+    uint64_t key = 0;
+    bool held = false;
+    int64_t last = -1;
+  };
+  std::vector<Slot> slot_;
+  std::vector<int32_t> free_;
+  std::unordered_map<uint64_t, int32_t> map_;
+  int64_t limit_ = 0, stamp_ = 0, pinned_ = 0;
+  uint64_t uid_ = 0;
+};
+
 class ColumnCache {
  public:
   // Forget every entry and allow up to `limit` slots.

@@ -124,11 +124,12 @@ class Context:
                "one_pass", "cert", "other_nan")
 
     def last_round_stats(self) -> dict:
-        out = (C.c_int64 * 23)()
-        self.lib.rrg_last_round_stats(self.h, out, 23)
+        out = (C.c_int64 * 25)()
+        self.lib.rrg_last_round_stats(self.h, out, 25)
         d = {"launches": out[0], "plain_routed": out[1], "fp64_rescored": out[2], "residual_pass": out[3],
              "qr_skipped_sentinel": out[15], "distinct": out[16], "tiled_qr": bool(out[17]), "graph": bool(out[18]),
-             "cache_hits": out[19], "cache_evals": out[20], "cache64_hits": out[21], "cache64_evals": out[22]}
+             "cache_hits": out[19], "cache_evals": out[20], "cache64_hits": out[21], "cache64_evals": out[22],
+             "pair_hits": out[23], "pair_evals": out[24]}
         d["rescore_reasons"] = {r: out[4 + i] for i, r in enumerate(self.REASONS) if out[4 + i]}
         return d
 

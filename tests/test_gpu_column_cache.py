@@ -70,6 +70,8 @@ def test_cached_rounds_are_bit_identical(data, prec):
     assert sum(s[key] for s in s_on[1:]) > 0  # later rounds read kept columns
     assert all(s[key] == 0 for s in s_off)
     if prec != PLAIN:
+        # cross-pair sums of earlier rounds read again
+        assert sum(s["pair_hits"] for s in s_on[1:]) > 0 and all(s["pair_hits"] == 0 for s in s_off)
         # the FP64 re-scoring lane: columns it evaluated in one round are
         # stored when the next starts, and later lanes copy them in
         assert sum(s["fp64_rescored"] for s in s_on) > 0
