@@ -2,7 +2,8 @@
 with a small C++ harness: lookups confirm the program word by word (equal
 hashes do not alias), constants compare by value, the sub-round's columns
 are pinned, the least recently used entries go first, scratch slots come
-back, a new dataset forgets every entry (CPU only)."""
+back, a new dataset forgets every entry; the factor registry and the pair
+cache behind the kept pair sums likewise (CPU only)."""
 import shutil
 import subprocess
 from pathlib import Path
@@ -87,6 +88,35 @@ int main() {
   cc.begin();
   CHECK(cc.find(fp(0), fp(0).hash()) < 0 && cc.find(fp(3), 99) < 0);
   CHECK(cc.available() == 4);
+
+  // factor registry: one id per program content, colliding hashes kept apart
+  FactorRegistry reg;
+  const uint32_t i0 = reg.id(fp(0), fp(0).hash());
+  CHECK(reg.id(fp(1), fp(1).hash()) == i0);  // same factor, other pool index
+  const uint32_t i2 = reg.id(fp(2), 5), i3 = reg.id(fp(3), 5);
+  CHECK(i2 != i3 && i2 != i0 && reg.id(fp(2), 5) == i2 && reg.id(fp(3), 5) == i3 && reg.size() == 3);
+
+  // pair cache: exact keys, pinning, least recently used replaced, rebinding
+  PairCache pc;
+  pc.reset(3);
+  pc.bind(1);
+  pc.begin();
+  CHECK(pc.find(11) < 0 && pc.take(2, out));
+  pc.insert(11, out[0]);
+  pc.insert(12, out[1]);
+  const int32_t k11 = out[0], k12 = out[1];
+  pc.begin();
+  CHECK(pc.find(12) == k12 && pc.take(1, out));
+  pc.insert(13, out[0]);
+  pc.begin();
+  CHECK(pc.find(13) >= 0 && pc.find(12) == k12);
+  CHECK(pc.available() == 1 && pc.take(1, out) && out[0] == k11);  // 11 was used longest ago
+  pc.insert(14, out[0]);
+  CHECK(pc.find(11) < 0 && pc.find(14) == k11);
+  CHECK(pc.available() == 0 && !pc.take(1, out));
+  pc.bind(2);
+  pc.begin();
+  CHECK(pc.find(12) < 0 && pc.find(14) < 0 && pc.available() == 3);
   std::printf("ok\n");
   return 0;
 }
