@@ -1,7 +1,9 @@
 """Rounds run as CUDA graphs (rrg_context_set_graph) against the same rounds
 launched directly: the same bits in every result field and coefficient, for
-small FP64 rounds (the classifier's shape) and for certified mixed rounds
-whose second half the device decides; the statistics report that the round
+small FP64 rounds (the classifier's shape), for certified mixed rounds
+whose second half the device decides, and for a certified round of fewer
+than 64 candidates (host-decided when launched directly, device-decided when
+captured); the statistics report that the round
 really ran as a graph, and a second round on the same context (the previous
 graph updated or rebuilt) gives the same results again."""
 import numpy as np
@@ -56,3 +58,10 @@ def test_graph_small_fp64_rounds():
 def test_graph_certified_mixed_round():
     X, y, trees, _ = synth.batched_fitness(n=60_000, d=6, n_trees=1500, seed=31)
     run(X, y, trees, CERTIFIED, "certified mixed", min_rows=0)
+
+
+def test_graph_small_certified_round():
+    # fewer than 64 candidates: launched directly the round reads its flags
+    # back (host-decided second half); captured it decides them on the device
+    X, y, trees, _ = synth.batched_fitness(n=60_000, d=6, n_trees=48, seed=37)
+    run(X, y, trees, CERTIFIED, "small certified", min_rows=0)
