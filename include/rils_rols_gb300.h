@@ -278,9 +278,9 @@ rrg_status rrg_context_clear_column_cache(rrg_context* ctx);
  * the flags back twice in mid-round and builds the FP64 path's programs for
  * the re-scored candidates only.  Results are the same bits either way; a
  * round whose double-float table needs sub-rounds always takes the second
- * form, and so does a round of fewer than 64 mixed candidates outside a
- * graph capture (its read-back costs less than the device-decided lane's
- * launches).  RRG_E_INVALID while a round is in flight.  No counterpart in the
+ * form, and so does a round of fewer than 64 mixed candidates when rounds
+ * do not run as graphs (its read-back costs less than the device-decided
+ * lane's launches).  RRG_E_INVALID while a round is in flight.  No counterpart in the
  * reference. */
 rrg_status rrg_context_set_async(rrg_context* ctx, int32_t on);
 

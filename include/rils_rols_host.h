@@ -50,6 +50,10 @@ int32_t rrh_set_precision(rrh_model* m, int32_t precision);
  * off by default.  The same search and results either way.  No counterpart
  * in the reference. */
 int32_t rrh_set_graph(rrh_model* m, int32_t on);
+/* Keep factor columns across the device backend's rounds
+ * (rrg_context_set_column_cache); on by default.  The same search and
+ * results either way.  No counterpart in the reference. */
+int32_t rrh_set_column_cache(rrh_model* m, int32_t on);
 
 /* fit(X, y, data_cnt, feat_cnt), X row-major n x d (rils_rols_cpp.cpp:717-728).
  * Returns RRG_OK or an rrg_status; never exits the process. */

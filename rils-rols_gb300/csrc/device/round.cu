@@ -623,11 +623,12 @@ rrg_status rrg_context::run_mixed(const rrg_dataset* ds, const std::vector<int32
     }
     // one sub-round (the table budget holds the whole round): its second
     // half is decided on the device, with no read-back.  A round of few
-    // candidates reads its flags back instead (outside a graph capture): on
-    // a recorded 1M-row search the 2416 one-candidate rounds took 0.26 s so
+    // candidates reads its flags back instead (unless rounds run as graphs,
+    // whose captures need the device-decided form and its buffers): on a
+    // recorded 1M-row search the 2416 one-candidate rounds took 0.26 s so
     // against 0.45 s with the device-decided lane's launches
     const bool async = async_rounds && pos == 0 && end == mixed.size() &&
-                       (capturing || (int64_t)(end - pos) >= kAsyncMinCands);
+                       (graph_rounds || capturing || (int64_t)(end - pos) >= kAsyncMinCands);
     bool async_done = false;
     const rrg_status st = mixed_subround(ds, mixed.data() + pos, (int32_t)(end - pos), lf, lid, certify, fb_all,
                                          async, &async_done);

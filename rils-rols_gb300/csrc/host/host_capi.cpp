@@ -15,6 +15,7 @@ struct rrh_model {
   rrh::Search search;
   rrg_context* ctx = nullptr;  // owned; created on first use of the device backend
   bool graph = false;          // device rounds as CUDA graphs (rrh_set_graph)
+  bool column_cache = true;    // factor columns kept across rounds (rrh_set_column_cache)
   rrh_model(bool c, int mfc, int ms, double cp, int mc, double ss, bool v, int rs) : search(c, mfc, ms, cp, mc, ss, v, rs) {}
   ~rrh_model() {
     if (ctx) rrg_context_destroy(ctx);
@@ -29,6 +30,7 @@ void* dev_dataset_create(void* self, const double* X, const double* y, int64_t n
   if (!m->ctx) {
     if (rrg_context_create(0, &m->ctx) != RRG_OK) return nullptr;
     if (m->graph) rrg_context_set_graph(m->ctx, 1);
+    if (!m->column_cache) rrg_context_set_column_cache(m->ctx, 0);
   }
   rrg_dataset* ds = nullptr;
   if (rrg_dataset_create(m->ctx, X, y, n, d, &ds) != RRG_OK) return nullptr;
@@ -97,6 +99,12 @@ int32_t rrh_set_graph(rrh_model* m, int32_t on) {
   if (!m) return RRG_E_INVALID;
   m->graph = on != 0;
   return m->ctx ? rrg_context_set_graph(m->ctx, on) : RRG_OK;
+}
+
+int32_t rrh_set_column_cache(rrh_model* m, int32_t on) {
+  if (!m) return RRG_E_INVALID;
+  m->column_cache = on != 0;
+  return m->ctx ? rrg_context_set_column_cache(m->ctx, on) : RRG_OK;
 }
 
 int32_t rrh_set_precision(rrh_model* m, int32_t p) {

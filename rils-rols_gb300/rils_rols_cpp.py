@@ -43,6 +43,11 @@ class rils_rols:  # noqa: N801 - name of the reference class
         """Run the device rounds as CUDA graphs (the same search and results)."""
         _lib.check(self._lib.rrh_set_graph(self._h, int(bool(on))), "rrh_set_graph")
 
+    def set_column_cache(self, on: bool = True) -> None:
+        """Keep factor columns across the device rounds (on by default; the same
+        search and results)."""
+        _lib.check(self._lib.rrh_set_column_cache(self._h, int(bool(on))), "rrh_set_column_cache")
+
     def counters(self) -> dict:
         names = ["ls_calls", "main_it", "device_rounds", "candidates_scored", "skipped_perts", "total_perts",
                  "backend_ns"]

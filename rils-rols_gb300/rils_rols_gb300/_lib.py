@@ -80,7 +80,8 @@ EXPORTS = [
     "rrg_device_memory", "rrg_tune_set_mode", "rrg_tune_pin", "rrg_tune_reset", "rrg_tune_report",
     "rrg_context_set_mixed_min_rows", "rrg_context_set_async", "rrg_context_set_graph", "rrg_context_memory",
     "rrg_context_set_column_cache", "rrg_context_clear_column_cache",
-    "rrh_create", "rrh_destroy", "rrh_set_backend", "rrh_set_precision", "rrh_set_graph", "rrh_fit", "rrh_predict",
+    "rrh_create", "rrh_destroy", "rrh_set_backend", "rrh_set_precision", "rrh_set_graph", "rrh_set_column_cache",
+    "rrh_fit", "rrh_predict",
     "rrh_model_string", "rrh_model_prefix", "rrh_best_time", "rrh_total_time", "rrh_fit_calls", "rrh_counter",
     "rrh_last_error", "rrh_candidates", "rrh_rewrite", "rrh_encode", "rrh_rebuild",
     "rrs_create", "rrs_destroy", "rrs_set_backend", "rrs_submit", "rrs_wait", "rrs_result", "rrs_stats_get",
@@ -134,6 +135,7 @@ def _declare(lib):
         "rrh_set_backend": (i32, [vp, P(Backend)]),
         "rrh_set_precision": (i32, [vp, i32]),
         "rrh_set_graph": (i32, [vp, i32]),
+        "rrh_set_column_cache": (i32, [vp, i32]),
         "rrh_fit": (i32, [vp, dp, dp, i32, i32]),
         "rrh_predict": (i32, [vp, dp, i32, i32, dp]),
         "rrh_model_string": (i32, [vp, cp, i32]),

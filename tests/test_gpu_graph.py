@@ -2,8 +2,8 @@
 launched directly: the same bits in every result field and coefficient, for
 small FP64 rounds (the classifier's shape), for certified mixed rounds
 whose second half the device decides, and for a certified round of fewer
-than 64 candidates (host-decided when launched directly, device-decided when
-captured); the statistics report that the round
+than 64 candidates (host-decided without graphs, device-decided as a
+graph); the statistics report that the round
 really ran as a graph, and a second round on the same context (the previous
 graph updated or rebuilt) gives the same results again."""
 import numpy as np
@@ -61,7 +61,24 @@ def test_graph_certified_mixed_round():
 
 
 def test_graph_small_certified_round():
-    # fewer than 64 candidates: launched directly the round reads its flags
-    # back (host-decided second half); captured it decides them on the device
+    # fewer than 64 candidates: without graphs the round reads its flags back
+    # (host-decided second half); as a graph it decides them on the device
     X, y, trees, _ = synth.batched_fitness(n=60_000, d=6, n_trees=48, seed=37)
-    run(X, y, trees, CERTIFIED, "small certified", min_rows=0)
+    b = encode(trees, tuned=True)
+    direct = Context(0)
+    graph = Context(0)
+    try:
+        for c in (direct, graph):
+            c.set_mixed_min_rows(0)
+            c.set_column_cache(False)
+        want = direct.dataset(X, y).evaluate(b, CERTIFIED)
+        graph.set_graph(True)
+        ds = graph.dataset(X, y)
+        same(ds.evaluate(b, CERTIFIED), want, "first graph round (may allocate, then run directly)")
+        for i in range(3):
+            got = ds.evaluate(b, CERTIFIED)
+            assert graph.last_round_stats()["graph"], i
+            same(got, want, ("small certified", i))
+    finally:
+        direct.close()
+        graph.close()
