@@ -262,12 +262,15 @@ rrg_status rrg_context_set_limits(rrg_context* ctx, int64_t scratch_bytes, int64
  * columns of mixed rounds (with their sums, probe records and cross-pair
  * sums) and the FP64 columns of FP64 rounds and of the mixed rounds' FP64
  * re-scoring, within the limits of rrg_context_set_limits, least
- * recently used columns replaced first.  Results are the same bits either
- * way.  Switching clears what is kept; so do destroying the dataset, a round
- * on another dataset and a failed round.  RRG_E_INVALID while a round is in
- * flight.  No counterpart in the reference. */
+ * recently used columns replaced first.  Datasets of fewer than 8192 rows
+ * do not use it (there evaluating a column costs less than finding it).
+ * Results are the same bits either way.  Switching clears what is kept; so
+ * do destroying the dataset, a round on another dataset and a failed round.
+ * RRG_E_INVALID while a round is in flight.  No counterpart in the
+ * reference. */
 rrg_status rrg_context_set_column_cache(rrg_context* ctx, int32_t on);
-/* Forget every kept column (the next round evaluates all its factors). */
+/* Forget every kept column (the next round evaluates all its factors);
+ * RRG_E_INVALID while a round is in flight. */
 rrg_status rrg_context_clear_column_cache(rrg_context* ctx);
 
 /* How a mixed or certified round decides its second half.  On (the
