@@ -380,7 +380,8 @@ def run_ours(args):
         "fp64_columns_read": sum(st["cache64_hits"] for st in stats),
         "fp64_columns_evaluated": sum(st["cache64_evals"] for st in stats),
         "pair_sums_read": sum(st["pair_hits"] for st in stats),
-        "pair_sums_formed": sum(st["pair_evals"] for st in stats)}
+        "pair_sums_formed": sum(st["pair_evals"] for st in stats),
+        "context_device_bytes": ctx.memory()}
     if args.quick:
         print(json.dumps(res))
         return

@@ -155,6 +155,11 @@ class Context:
         (scratch) and of the double-float factor table (each >= 1 MiB)."""
         check(self.lib.rrg_context_set_limits(self.h, int(scratch_bytes), int(table_bytes)), "rrg_context_set_limits")
 
+    def memory(self) -> int:
+        """Device bytes the context's buffers hold (tables, column caches,
+        scratch; datasets not included)."""
+        return int(self.lib.rrg_context_memory(self.h))
+
     def set_column_cache(self, on: bool = True) -> None:
         """Keep factor columns on the device across rounds of one dataset (on,
         the default); the same results either way."""
