@@ -486,15 +486,16 @@ def run_ours(args):
     print(json.dumps(res))
 
 
-def regression_fit_leg(X, y, calls):
+def regression_fit_leg(X, y, calls, precision="mixed"):
     """A regression fit on the 1M-row data through the drop-in module
-    (rils_rols_cpp.rils_rols, certified mixed precision), max_fit_calls =
-    `calls`: the search submits its own rounds, so evals/s here is what a fit
-    sees (host search included in the wall time)."""
+    (rils_rols_cpp.rils_rols, certified mixed precision unless `precision`
+    is "plain"), max_fit_calls = `calls`: the search submits its own rounds,
+    so evals/s here is what a fit sees (host search included in the wall
+    time)."""
     import rils_rols_cpp
     n, d = X.shape
     m = rils_rols_cpp.rils_rols(False, calls, 1 << 30, 0.001, 50, 1.0, False, SEED % 100000)
-    m.set_precision("mixed")
+    m.set_precision(precision)
     t = time.perf_counter()
     m.fit(X.reshape(-1), y, n, d)
     wall = time.perf_counter() - t
@@ -838,6 +839,8 @@ def main():
     ap.add_argument("--serve-fit-calls", type=int, default=100000)
     ap.add_argument("--serve-active", type=int, default=16)
     ap.add_argument("--serve-only", action="store_true", help="only the serving leg")
+    ap.add_argument("--fit-only", action="store_true",
+                    help="only the 1M-row regression fit, certified mixed and plain FP64 (the drop-in default)")
     ap.add_argument("--cls-fit-calls", type=int, default=20000,
                     help="max_fit_calls of the 200k-row classifier fits (0: no classifier leg)")
     ap.add_argument("--cls-only", action="store_true", help="only the classifier leg")
@@ -855,6 +858,10 @@ def main():
         return
     if args.serve_only:
         print(json.dumps(serving_leg(args)))
+        return
+    if args.fit_only:
+        X, y = regression_data(args.n)
+        print(json.dumps({p: regression_fit_leg(X, y, args.fit_calls_1m, p) for p in ("mixed", "plain")}))
         return
     if args.cls_only:
         print(json.dumps(classifier_leg(args)))
